@@ -1,0 +1,230 @@
+/*
+ * tracer_gpu.h -- C ABI of the GB300 (sm_103a) per-timestep hot path of
+ * seantrim/tracer_code: variable-viscosity streamfunction multigrid solve,
+ * Runge-Kutta tracer advection with grid-to-tracer Taylor interpolation, and
+ * the tracer-ratio composition step.
+ *
+ * The reference is one Fortran program whose state lives in the modules
+ * `basics` (basics.f90:1-35) and `arrays` (arrays.f90:1-19).  Its hot path is
+ * called from main.f90:174-205 through four argument-less subroutines:
+ *
+ *     multigrid            iterative_solver.f90:79-173
+ *     compute_velocities   momentum.f90:532-551
+ *     stats                basics.f90:236-324
+ *     energy_time          energy.f90:117-453
+ *
+ * This header replaces those four calls with handle-based entry points.  The
+ * module state becomes an opaque handle (tc_handle) whose fields live in HBM;
+ * host arrays cross the boundary only in tc_upload_state/tc_download_state.
+ * A Fortran host binds these functions through ISO_C_BINDING (the binding
+ * module is shown in INTEGRATION.md) and maps a non-zero status to `stop`,
+ * which is what the reference does at each of its error sites.
+ *
+ * Array conventions (identical to the reference's allocations, basics.f90:37-110):
+ *   - FP64, Fortran column-major (i, the horizontal index, fastest);
+ *   - T, SF        : (-span:nx+span, -span:nz+span), span = order/2+1;
+ *   - Cnew         : (1:ntype, -span:nx+span, -span:nz+span), type fastest;
+ *   - u, w         : (-span_interp:nx+span_interp, -span_interp:nz+span_interp);
+ *   - rtr, str     : (1:ntr) FP64; Ttype : (1:ntr) int32 (0 = ambient);
+ *   - ntr = (nx+1)*(nz+1)*tpc  (basics.f90:146).
+ *
+ * Every function returns a tc_status (0 = success).  Handles are independent
+ * (an ensemble runs one handle per case); a handle is not re-entrant and is
+ * used from one host thread at a time.  All device work of a handle is issued
+ * on one CUDA stream (tc_set_stream).
+ */
+#ifndef TRACER_GPU_H
+#define TRACER_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TC_MAX_TYPES 4
+#define TC_ABI_VERSION 2
+
+/* Status codes.  Each reference `stop` site has its own code. */
+typedef enum tc_status {
+    TC_OK = 0,
+    TC_ERR_ARG = 1,              /* bad argument / null pointer / size mismatch          */
+    TC_ERR_UNSUPPORTED = 2,      /* input combination outside the implemented path        */
+    TC_ERR_MG_CYCLES = 3,        /* "Too Many Multigrid Cycles Needed" iterative_solver.f90:164-167 */
+    TC_ERR_MG_RESIDUAL = 4,      /* "Abnormally High Residual Detected" iterative_solver.f90:275-278 */
+    TC_ERR_TRACER_OUTSIDE = 5,   /* "Tracer advected outside of domain" composition.f90:709-712 */
+    TC_ERR_RK2_STABILITY = 6,    /* "Advective Eigenvalues Exceed Diffusive" energy.f90:626-629 */
+    TC_ERR_LOOP_CAP = 7,         /* a data-dependent smoothing loop hit its iteration cap   */
+    TC_ERR_CUDA = 8,             /* a CUDA runtime error; see tc_last_error()               */
+    TC_ERR_ALLOC = 9,            /* device or host allocation failed                        */
+    TC_ERR_STATE = 10,           /* call order violated (e.g. step before upload)           */
+    TC_ERR_SINGULAR = 11         /* zero pivot in the coarsest-grid banded LU (DGBTRF INFO>0) */
+} tc_status;
+
+/*
+ * Inputs of main.f90:8-116 that the hot path reads.  Field names follow the
+ * reference.  Fixed by this implementation (not parameters): Database=2,
+ * iterate=1, local_time=0, tracer=0, equalize=0 (see tc_create).
+ */
+typedef struct tc_params {
+    /* grid options (main.f90:9-21) */
+    int32_t nx, nz;             /* cells; multigrid_setup may change them (optimize_grid) */
+    double  aspect;
+    int32_t order;              /* space order (even); the GPU path implements order=2   */
+    int32_t gridX, gridZ;       /* 0 = uniform (GPU path: uniform only)                  */
+    double  spaceX, spaceZ, thickness;
+    int32_t nbound;
+    /* velocity solver options (main.f90:23-34) */
+    int32_t non_Newtonian;      /* GPU path: 0                                           */
+    int32_t iterate_order;      /* 1 = Richardson/Chebyshev smoother                     */
+    double  tolerance;          /* relative L1 residual for multigrid convergence       */
+    int32_t Nmulti;             /* smoother sweeps per level visit                        */
+    int32_t mingrid;
+    int32_t grids;              /* max multigrid levels, 2..6                            */
+    double  eig_ratio;
+    int32_t vis_iter;
+    int32_t max_cycles;
+    /* time stepping (main.f90:36-50) */
+    int32_t torder;             /* 2 or 4 (RK4 for the field T method, main.f90:37)     */
+    double  courant, courantT, courantC, courant_stream;
+    int32_t RK_update;
+    double  dt_manual;
+    /* tracers (main.f90:52-59) */
+    int32_t comp;               /* 1 = compositional tracers                              */
+    int32_t ntype;              /* enriched tracer types (1..TC_MAX_TYPES)                */
+    int32_t tpc;                /* tracers per cell corner                                */
+    double  dist_factor;
+    /* initial and boundary conditions (main.f90:61-74) */
+    int32_t Tbot, Vbc;
+    double  dlayer, dent;
+    /* buoyancy, heating, conductivity (main.f90:76-96) */
+    double  RaT;
+    double  RaC[TC_MAX_TYPES];
+    double  H;
+    double  conduct_factor[TC_MAX_TYPES];
+    double  Htype[TC_MAX_TYPES];
+    /* viscosity (main.f90:98-115) */
+    double  eig_ratio_min;
+    int32_t ivis;               /* 0 isoviscous, 1 T,z, 2 T,z,C, 3 T + plastic (oracle)  */
+    double  visP, visT, delta_visT, yield, yield_gradient, yield_depth;
+    double  visC[TC_MAX_TYPES];
+    double  delta_visC[TC_MAX_TYPES];
+    /* Multigrid coarse-level start (no reference input).  0 = the reference's
+     * behaviour (iterative_solver.f90:120-160): a smoothed coarse level keeps
+     * its previous correction as the starting guess when a new restricted
+     * residual arrives.  1 = that correction restarts from zero (textbook
+     * correction scheme).  With more than two levels the reference behaviour
+     * stalls or diverges on high-contrast starts (e.g. 1024x256, visT=1e4). */
+    int32_t mg_zero_coarse;
+    int32_t reserved_[3];
+} tc_params;
+
+/* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
+ * (basics.f90:316-322).  Arrays are indexed by type-1. */
+typedef struct tc_stats_row {
+    double  time, Tavg, vrms, Nu, Nu_bot, RaT_avg, mobility, strain_max, q1, q2, q3, q4;
+    int32_t empty_cells, tracer_min, tracer_max, tstep;
+    double  Cavg[TC_MAX_TYPES];
+    double  ent[TC_MAX_TYPES];
+    int32_t n_eta, n_temp;
+    int32_t n_comp[TC_MAX_TYPES];
+    double  eig_fine;
+} tc_stats_row;
+
+/* Derived sizes a caller needs to size its arrays. */
+typedef struct tc_info {
+    int32_t nx, nz;             /* after optimize_grid                                    */
+    int32_t span, span_interp, grids, nsteps;
+    int64_t ntr;
+    int32_t ngrid_coarse, kl, ku;
+    int32_t nx_grid[8], nz_grid[8];
+    double  dr, ds;
+} tc_info;
+
+typedef struct tc_handle tc_handle;
+
+/* Fills *p with the shipped main.f90 defaults, switched to the path this
+ * library implements (comp=1, ntype=1, tracer=0, equalize=0, non_Newtonian=0,
+ * ivis=2, torder=4).  Replaces the hard-coded input block main.f90:8-116. */
+void tc_default_params(tc_params* p);
+
+/* Setup: main.f90:118-136 (compute_smoothing_parameters, multigrid_setup,
+ * compute_basics, storage, FD_coefficients, build_grid with restart=0 grid
+ * coordinates, derivative_eigenvalues, stability_RK4_smoother,
+ * stability_vis_smoother).  Allocates all device state for one case. */
+tc_status tc_create(const tc_params* p, tc_handle** out);
+tc_status tc_destroy(tc_handle* h);
+tc_status tc_get_info(const tc_handle* h, tc_info* info);
+
+/* All later device work of the handle is issued on `stream` (a cudaStream_t;
+ * NULL = the legacy default stream). */
+tc_status tc_set_stream(tc_handle* h, void* stream);
+
+/* Restart-style state injection: the restart branch of build_grid
+ * (grid.f90:55-96: enforceBCs(T), enforceBCs_stream(1,SF), enforceBCs_comp,
+ * tracers_to_corners with smoothing off) followed by main.f90:137-143
+ * (smoother_time_T(T), smoother_time, load_conductivity_array) and the
+ * zeroed coarse-level corrections of main.f90:162.  Cnew may be NULL
+ * (zero start).  Ttype may be NULL when comp=0. */
+tc_status tc_upload_state(tc_handle* h, const double* T, const double* Cnew,
+                          const double* SF, const double* rtr, const double* str,
+                          const int32_t* Ttype, int64_t ntr);
+
+/* Copies the state back in the same layouts (any pointer may be NULL). */
+tc_status tc_download_state(tc_handle* h, double* T, double* Cnew, double* SF,
+                            double* rtr, double* str, int32_t* Ttype);
+
+/* Module clock: basics::tstep and basics::time, owned by the host loop. */
+tc_status tc_set_clock(tc_handle* h, int32_t tstep, double time);
+
+/* multigrid (iterative_solver.f90:79-173): solves for SF; *cycles_out
+ * (may be NULL) receives the number of multigrid cycles q. */
+tc_status tc_multigrid(tc_handle* h, int32_t* cycles_out);
+
+/* compute_velocities (momentum.f90:532-551) with velocityBCs. */
+tc_status tc_compute_velocities(tc_handle* h);
+
+/* stats (basics.f90:236-324): one stats.dat row. */
+tc_status tc_stats(tc_handle* h, tc_stats_row* row);
+
+/* energy_time (energy.f90:117-453): one RK step of T, tracers and C,
+ * including the multigrid re-solves between stages (RK_update=1).
+ * *dt_out (may be NULL) receives dt. */
+tc_status tc_energy_time(tc_handle* h, double* dt_out);
+
+/* One pass of the main.f90:174-205 loop body: multigrid, compute_velocities,
+ * stats, energy_time, time += dt, tstep += 1.  row and cycles may be NULL. */
+tc_status tc_step(tc_handle* h, tc_stats_row* row, int32_t* cycles, double* dt_out);
+
+/* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */
+tc_status tc_download_velocities(tc_handle* h, double* u, double* w);
+
+/* tracers_to_corners (composition.f90:669-790) on the given positions,
+ * smoothing on: Cnew, count_type, nempty, Cvis, Cbuoy, conduct are updated.
+ * rtr/str are HOST arrays of ntr doubles. */
+tc_status tc_tracers_to_corners(tc_handle* h, const double* rtr, const double* str);
+
+/* Copies count_type (0:ntype, -span:nx+span, -span:nz+span) as int32. */
+tc_status tc_download_counts(tc_handle* h, int32_t* count_type);
+
+/* Diagnostic copy of an internal field (no counterpart in the reference; used
+ * by the parity tests).  `name` is a reference array name: T, SF, Tvis, Tbuoy,
+ * u, w, conduct, conduct_r, conduct_s, Cnew, Cvis, Cbuoy (type >= 1),
+ * vis_grid, vis_x, vis_z, vis_xx, vis_zz, vis_xz, dt_stream, ratio, RHS,
+ * error, residual, dt_vis (level >= 1), DERr_u, DERr_w, dts_array.  out
+ * receives the level's ghost-padded box (-span:nx_l+span, -span:nz_l+span)
+ * in Fortran order; entries outside the reference array's own bounds are
+ * unspecified. */
+tc_status tc_debug_field(tc_handle* h, const char* name, int32_t level, int32_t type, double* out);
+
+/* sizeof(tc_params), sizeof(tc_stats_row), sizeof(tc_info) as compiled, so a
+ * binding can check its struct layouts. */
+void tc_abi_sizes(int32_t sizes[3]);
+
+/* Text of the last CUDA error seen by the handle ("" if none). */
+const char* tc_last_error(const tc_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRACER_GPU_H */

@@ -1,0 +1,475 @@
+// k_field.cu -- fine-grid field kernels: boundary conditions, the T and C
+// filters, conductivity, velocities, energy-equation RK stages, time-step
+// bound and the stats.dat integrals.
+//
+// Reference: energy.f90 (load_conductivity_array :31-58, energy_space :60-80,
+// energy_time :117-453, enforceBCs :455-475, stability_RK4 :600-646, eigA /
+// eigD :686-706), smoother.f90 / multigrid_cycle.f90 (smoothness, smoother_space,
+// smoother_time, smoother_time_T), momentum.f90 (compute_strain_rate_invariant
+// :32-62, compute_velocities :532-551), composition.f90 (enforceBCs_comp
+// :792-803, velocityBCs :806-836, compute_derivatives :900-919) and basics.f90
+// (stats :236-324, integrate2D / integrate1Dx / integrate1Dz :341-403).
+// Uniform grid metrics: xr=zs=1, xrr=zss=0.  Every kernel keeps the
+// reference's operation order (no FMA contraction), so with identical inputs
+// its output equals the CPU restatement bit for bit.
+#include "tc_device.cuh"
+
+// enforceBCs (energy.f90:455-475): every ghost / boundary-row value as a
+// function of interior values only.
+__global__ void k_enforce_T(Lay L, Range2 r, double* __restrict__ T, int Tbot) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int nx = L.a, nz = L.b;
+    if (i >= 0 && i <= nx && k >= 1 && k <= nz - 1) return;
+    int mi = (i < 0) ? -i : ((i > nx) ? 2 * nx - i : i);
+    double v;
+    if (k > nz) v = -T[IX(L, mi, 2 * nz - k)];
+    else if (k == nz) v = 0.0;
+    else if (k < 0) {
+        double src = T[IX(L, mi, -k)];
+        v = (Tbot == 0) ? (-(src - 1.0) + 1.0) : src;
+    } else if (k == 0) v = (Tbot == 0) ? 1.0 : T[IX(L, mi, 0)];
+    else v = T[IX(L, mi, k)];
+    T[IX(L, i, k)] = v;
+}
+void launch_enforce_T(cudaStream_t s, const Lay& L, double* T, int Tbot) {
+    Range2 r{-SP, L.a + SP, -SP, L.b + SP};
+    k_enforce_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, T, Tbot);
+}
+
+// enforceBCs_comp (composition.f90:792-803).  Its four statements share one
+// loop over i, so rows -1 and nz+1 take the PREVIOUS values of the outer side
+// ghosts at columns -2 and nx+2 (they are refreshed only in the i=2 pass).
+// Cprev holds those previous values (it may alias C: the thread that owns a
+// side ghost reads its old value before overwriting it).
+__global__ void k_enforce_comp(Lay L, Range2 r, double* C, const double* Cprev) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int nx = L.a, nz = L.b;
+    if (i >= 0 && i <= nx && k >= 0 && k <= nz) return;
+    const bool outer = (i == -2 || i == nx + 2);
+    if (outer && (k == -1 || k == nz + 1)) return;  // written by the owner of (i, 1) / (i, nz-1)
+    int mi = (i < 0) ? -i : ((i > nx) ? 2 * nx - i : i);
+    if (k >= 0 && k <= nz) {
+        double v = C[IX(L, mi, k)];
+        if (outer && (k == 1 || k == nz - 1)) {
+            double old = Cprev[IX(L, i, k)];
+            C[IX(L, i, (k == 1) ? -1 : nz + 1)] = old;
+            if (k == 1 && nz - 1 == 1) C[IX(L, i, nz + 1)] = old;
+        }
+        C[IX(L, i, k)] = v;
+        return;
+    }
+    int mk = (k < 0) ? -k : 2 * nz - k;
+    C[IX(L, i, k)] = C[IX(L, mi, mk)];
+}
+void launch_enforce_comp(cudaStream_t s, const Lay& L, double* C, const double* Cprev_ghosts) {
+    Range2 r{-SP, L.a + SP, -SP, L.b + SP};
+    k_enforce_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, C, Cprev_ghosts ? Cprev_ghosts : C);
+}
+
+// smoothness (multigrid_cycle.f90:175-195): largest jump to the five
+// neighbours (i,k-1),(i+1,k-1),(i+1,k),(i,k+1),(i+1,k+1).
+__global__ void k_smoothness(Lay L, Range2 r, const double* __restrict__ T, RedScratch rs, double* out) {
+    RANGE_IK(r);
+    double a = -INFINITY;
+    if (inr) {
+        const size_t ld = (size_t)L.ld;
+        size_t x = IX(L, i, k);
+        double c = T[x];
+        double a1 = fabs(T[x - ld] - c), a2 = fabs(T[x + 1 - ld] - c), a3 = fabs(T[x + 1] - c);
+        double a4 = fabs(T[x + ld] - c), a5 = fabs(T[x + 1 + ld] - c);
+        a = fmax(fmax(fmax(fmax(a1, a2), a3), a4), a5);
+        if (a < 0.0) a = 0.0;
+    }
+    reduce_to(RED_MAX, a, rs.part, rs.count, out);
+}
+void launch_smoothness(cudaStream_t s, const Lay& L, const double* f, RedScratch rs, DevScalars* ds) {
+    Range2 r{0, L.a - 1, 1, L.b - 1};
+    k_smoothness<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, f, rs, &ds->diff);
+}
+
+__device__ __forceinline__ double lap5(const double* __restrict__ T, size_t x, size_t ld, double dr2, double ds2) {
+    double c = T[x];
+    double Trr = (T[x - 1] + -2.0 * c + T[x + 1]) / dr2;
+    double Tss = (T[x - ld] + -2.0 * c + T[x + ld]) / ds2;
+    return Trr + Tss;
+}
+
+// one Richardson step of smoother_time_T (smoother.f90:343-377)
+__global__ void k_smooth_T(Lay L, Phys P, Range2 r, const double* __restrict__ Tin, double* __restrict__ Tout,
+                           const double* __restrict__ dts) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    double temp = lap5(Tin, x, (size_t)L.ld, P.dr2, P.ds2);
+    double d = dts[x] * P.courantT;
+    Tout[x] = Tin[x] + d * temp;
+}
+void launch_smooth_T_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Tin, double* Tout,
+                          const double* dts) {
+    Range2 r{0, L.a, 0, L.b};
+    k_smooth_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tin, Tout, dts);
+}
+
+// one step of smoother_time (smoother.f90:287-341) for one type
+__global__ void k_smooth_C(Lay L, Phys P, Range2 r, const double* __restrict__ Cin, double* __restrict__ Cout,
+                           const double* __restrict__ dts, double c) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    double temp = lap5(Cin, x, (size_t)L.ld, P.dr2, P.ds2);
+    double d = dts[x] * P.courantC;
+    double v = Cin[x] + c * d * temp;
+    if (v < 0.0) v = 0.0;
+    if (v > 1.0) v = 1.0;
+    Cout[x] = v;
+}
+void launch_smooth_C_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Cin, double* Cout,
+                          const double* dts, double c) {
+    Range2 r{0, L.a, 0, L.b};
+    k_smooth_C<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Cin, Cout, dts, c);
+}
+
+// load_conductivity_array (energy.f90:31-58)
+__global__ void k_conduct(Lay L, Phys P, Range2 r, CPtrs Cv, double* __restrict__ cd) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int nx = L.a, nz = L.b;
+    int mi = (i < 0) ? -i : ((i > nx) ? 2 * nx - i : i);
+    int mk = (k < 0) ? -k : ((k > nz) ? 2 * nz - k : k);
+    double c = 1.0;
+    if (P.comp != 0)
+        for (int j = 0; j < P.ntype; j++) c = exp(-Cv.p[j][IX(L, mi, mk)] * P.lncf[j]);
+    cd[IX(L, i, k)] = c;
+}
+__global__ void k_conduct_grad(Lay L, Phys P, Range2 r, const double* __restrict__ cd, double* __restrict__ cr,
+                               double* __restrict__ cs) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t ld = (size_t)L.ld;
+    size_t x = IX(L, i, k);
+    cr[x] = (-0.5 * cd[x - 1] + 0.5 * cd[x + 1]) / P.dr;
+    cs[x] = (-0.5 * cd[x - ld] + 0.5 * cd[x + ld]) / P.ds;
+}
+void launch_conductivity(cudaStream_t s, const Lay& L, const Phys& P, const double* const* Cvis, double* conduct,
+                         double* conduct_r, double* conduct_s) {
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
+    Range2 r{-SP, L.a + SP, -SP, L.b + SP};
+    k_conduct<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, C, conduct);
+    Range2 r2{-1, L.a + 1, -1, L.b + 1};
+    k_conduct_grad<<<grid_for(r2), dim3(BX, BY), 0, s>>>(L, P, r2, conduct, conduct_r, conduct_s);
+}
+
+// compute_velocities + velocityBCs (momentum.f90:532-551, composition.f90:806-836),
+// span_interp = 1.  Each cell's final value is written from SF directly.
+__device__ __forceinline__ double uf_(const Lay& L, const Phys& P, const double* SF, int i, int k) {
+    const size_t ld = (size_t)L.ld;
+    size_t x = IX(L, i, k);
+    return (-0.5 * SF[x - ld] + 0.5 * SF[x + ld]) / P.ds;
+}
+__device__ __forceinline__ double wf_(const Lay& L, const Phys& P, const double* SF, int i, int k) {
+    size_t x = IX(L, i, k);
+    return -((-0.5 * SF[x - 1] + 0.5 * SF[x + 1]) / P.dr);
+}
+__global__ void k_velocities(Lay L, Phys P, Range2 r, const double* __restrict__ SF, double* __restrict__ u,
+                             double* __restrict__ w) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int nx = L.a, nz = L.b;
+    const double vs = (P.Vbc == 1) ? -1.0 : 1.0;
+    // ---- u ----
+    double uv;
+    if (i == 0 || i == nx) uv = 0.0;
+    else if (P.Vbc == 1 && (k == 0 || k == nz)) uv = 0.0;
+    else {
+        // value of u(ii,kk) after the first two statements of velocityBCs
+        auto u_step1 = [&](int ii, int kk) -> double {
+            if (kk < 0) return vs * uf_(L, P, SF, ii, -kk);
+            if (kk > nz) return vs * uf_(L, P, SF, ii, 2 * nz - kk);
+            return uf_(L, P, SF, ii, kk);
+        };
+        if (i < 0) uv = -u_step1(-i, k);
+        else if (i > nx) uv = -u_step1(2 * nx - i, k);
+        else uv = u_step1(i, k);
+    }
+    // ---- w ----
+    double wv;
+    if (k == 0 || k == nz) wv = 0.0;
+    else {
+        int mi = (i < 0) ? -i : ((i > nx) ? 2 * nx - i : i);
+        if (k < 0) wv = -wf_(L, P, SF, mi, -k);
+        else if (k > nz) wv = -wf_(L, P, SF, mi, 2 * nz - k);
+        else wv = wf_(L, P, SF, mi, k);
+    }
+    size_t x = IX(L, i, k);
+    u[x] = uv;
+    w[x] = wv;
+}
+void launch_velocities(cudaStream_t s, const Lay& L, const Phys& P, const double* SF, double* u, double* w) {
+    Range2 r{-1, L.a + 1, -1, L.b + 1};
+    k_velocities<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, SF, u, w);
+}
+
+// compute_derivatives (composition.f90:900-919), order=2
+__global__ void k_derivatives(Lay L, Phys P, Range2 r, const double* __restrict__ f, double* __restrict__ der) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    der[x] = (-0.5 * f[x - 1] + 0.5 * f[x + 1]) / P.dr;
+}
+void launch_derivatives(cudaStream_t s, const Lay& L, const Phys& P, const double* f, double* der) {
+    Range2 r{0, L.a, -1, L.b + 1};
+    k_derivatives<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, f, der);
+}
+
+// stability_RK4 (energy.f90:600-646), tracer=0 branch of eigA
+__global__ void k_stab(Lay L, Phys P, Range2 r, const double* __restrict__ cd, const double* __restrict__ cr,
+                       const double* __restrict__ cs, const double* __restrict__ u, const double* __restrict__ w,
+                       RedScratch rs, double* outA, int which) {
+    RANGE_IK(r);
+    double v = -INFINITY;
+    if (inr) {
+        size_t x = IX(L, i, k);
+        if (which == 0) {
+            double ax = -(cd[x] * 0.0) - u[x] + cr[x];
+            double az = -(cd[x] * 0.0) - w[x] + cs[x];
+            v = fabs(ax) * P.Tr_max + fabs(az) * P.Ts_max;
+        } else {
+            v = cd[x] * (fabs(P.Trr_max) + fabs(P.Tss_max));
+        }
+    }
+    reduce_to(RED_MAX, v, rs.part, rs.count, outA);
+}
+__global__ void k_dt(Phys P, DevScalars* ds, double courant, double dt_manual) {
+    double dt;
+    if (P.RaT != 0.0) {
+        double eA = ds->eA_max, eD = ds->eD_max, dtA, dtD;
+        if (eA < 0.0) eA = 0.0;
+        if (eD < 0.0) eD = 0.0;
+        if (P.torder == 2) {
+            if (eA >= eD) ds->flag_rk2 = 1;
+            dtA = 1.0 / eA;
+            dtD = 2.0 / eD;
+        } else {
+            dtA = 2.8 / eA;
+            dtD = 2.8 / eD;
+        }
+        if (eA == 0.0) dt = dtD;
+        else dt = 1.0 / (1.0 / dtA + 1.0 / dtD);
+    } else {
+        dt = dt_manual;
+    }
+    ds->dt = courant * dt;
+}
+void launch_stability(cudaStream_t s, const Lay& L, const Phys& P, const double* conduct, const double* conduct_r,
+                      const double* conduct_s, const double* u, const double* w, double courant, double dt_manual,
+                      RedScratch rs, DevScalars* ds) {
+    Range2 r{0, L.a, 0, L.b};
+    if (P.RaT != 0.0) {
+        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eA_max, 0);
+        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eD_max, 1);
+    }
+    k_dt<<<1, 1, 0, s>>>(P, ds, courant, dt_manual);
+}
+
+// energy_space (energy.f90:60-80) and the four RK stage updates of energy_time
+__global__ void k_energy(Lay L, Phys P, Range2 r, int stage, const double* __restrict__ Tin,
+                         const double* __restrict__ T0, double* __restrict__ T, double* __restrict__ Tout,
+                         const double* __restrict__ cd, const double* __restrict__ cr, const double* __restrict__ cs,
+                         const double* __restrict__ u, const double* __restrict__ w, CPtrs Cv, const DevScalars* ds) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t ld = (size_t)L.ld;
+    size_t x = IX(L, i, k);
+    double Tr = (-0.5 * Tin[x - 1] + 0.5 * Tin[x + 1]) / P.dr;
+    double Ts = (-0.5 * Tin[x - ld] + 0.5 * Tin[x + ld]) / P.ds;
+    double c = Tin[x];
+    double Trr = (Tin[x - 1] + -2.0 * c + Tin[x + 1]) / P.dr2;
+    double Tss = (Tin[x - ld] + -2.0 * c + Tin[x + ld]) / P.ds2;
+    double kx = cr[x], kz = cs[x];
+    double heat;
+    if (P.comp == 0) heat = P.H;
+    else {
+        double sC = 0.0;
+        for (int j = 0; j < P.ntype; j++) sC = sC + Cv.p[j][x];
+        heat = P.H * (1.0 - sC);
+        for (int j = 0; j < P.ntype; j++) heat = P.Htype[j] * Cv.p[j][x] + heat;
+    }
+    double temp = cd[x] * (Trr + Tss) + (kx * Tr + kz * Ts) - u[x] * Tr - w[x] * Ts + heat;
+    const double dt = ds->dt;
+    if (stage == 1) {
+        T[x] = temp;
+        Tout[x] = T0[x] + 0.5 * dt * temp;
+    } else if (stage == 2) {
+        T[x] = T[x] + 2.0 * temp;
+        Tout[x] = T0[x] + 0.5 * dt * temp;
+    } else if (stage == 3) {
+        T[x] = T[x] + 2.0 * temp;
+        Tout[x] = T0[x] + dt * temp;
+    } else {
+        T[x] = T0[x] + (dt / 6.0) * (T[x] + temp);
+    }
+}
+void launch_energy_stage(cudaStream_t s, const Lay& L, const Phys& P, int stage, const double* Tin,
+                         const double* T0, double* T, double* Tout, const double* conduct, const double* conduct_r,
+                         const double* conduct_s, const double* u, const double* w, const double* const* Cvis,
+                         const DevScalars* ds) {
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
+    Range2 r{0, L.a, 0, L.b};
+    k_energy<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, stage, Tin, T0, T, Tout, conduct, conduct_r, conduct_s, u,
+                                                   w, C, ds);
+}
+
+// compute_strain_rate_invariant (momentum.f90:32-62), interior nodes
+__global__ void k_strain(Lay L, Phys P, Range2 r, const double* __restrict__ u, const double* __restrict__ w,
+                         double* __restrict__ st) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t ld = (size_t)L.ld;
+    size_t x = IX(L, i, k);
+    double ur = (-0.5 * u[x - 1] + 0.5 * u[x + 1]) / P.dr;
+    double us = (-0.5 * u[x - ld] + 0.5 * u[x + ld]) / P.ds;
+    double wr = (-0.5 * w[x - 1] + 0.5 * w[x + 1]) / P.dr;
+    double ws = (-0.5 * w[x - ld] + 0.5 * w[x + ld]) / P.ds;
+    double q = 0.5 * (2.0 * (ur * ur + ws * ws) + (us + wr) * (us + wr));
+    st[x] = sqrt(q);
+}
+void launch_strain(cudaStream_t s, const Lay& L, const Phys& P, const double* u, const double* w, double* strain) {
+    Range2 r{0, L.a, 0, L.b};
+    k_strain<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, u, w, strain);
+}
+
+// ---------------------------------------------------------------------------
+// stats: integrate1Dx of each row in the reference's serial order (one
+// thread per row), then integrate1Dz serially; the host applies the final
+// divisions and square roots exactly as basics.f90:236-324.
+// integ layout: [0..3] C by type, [4..7] C from kent by type, [8] u^2+w^2,
+// [9] T, [10] RaT/conduct/vis, [11] top-row u^2+w^2, [12] Nu numerator,
+// [13] Nu denominator, [14] Nu_bot numerator, [15..18] q1..q4
+// ---------------------------------------------------------------------------
+#define NROWINT 7
+__global__ void k_stats_rows(Lay L, Phys P, const double* __restrict__ T, const double* __restrict__ u,
+                             const double* __restrict__ w, const double* __restrict__ cd,
+                             const double* __restrict__ vis, CPtrs Cn, double* __restrict__ rows) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nx = L.a, nz = L.b;
+    if (k > nz) return;
+    const int nrow = NROWINT;
+    // integrands: 0..ntype-1 C, then 4: u^2+w^2, 5: T, 6: RaT/conduct/vis
+    double acc[NROWINT];
+    for (int q = 0; q < nrow; q++) acc[q] = 0.0;
+    auto f = [&](int q, int i) -> double {
+        size_t x = IX(L, i, k);
+        if (q < 4) return (q < P.ntype) ? Cn.p[q][x] : 0.0;
+        if (q == 4) return u[x] * u[x] + w[x] * w[x];
+        if (q == 5) return T[x];
+        return P.RaT / cd[x] / vis[x];
+    };
+    for (int q = 0; q < nrow; q++) {
+        if (q < 4 && q >= P.ntype) continue;
+        if (q >= 5 && P.RaT == 0.0) continue;
+        double fint = 0.0;
+        double fprev = f(q, 0);
+        for (int i = 0; i <= nx - 1; i++) {
+            double fn = f(q, i + 1);
+            fint = fint + 0.5 * (fprev * 1.0 + fn * 1.0) * P.dr;
+            fprev = fn;
+        }
+        acc[q] = fint;
+    }
+    for (int q = 0; q < nrow; q++) rows[(size_t)q * (nz + 1) + k] = acc[q];
+}
+__global__ void k_stats_final(Lay L, Phys P, int kent, const double* __restrict__ rows,
+                              const double* __restrict__ T, const double* __restrict__ u,
+                              const double* __restrict__ w, const double* __restrict__ cd,
+                              const double* __restrict__ st, DevScalars* ds) {
+    const int nx = L.a, nz = L.b;
+    const int t = threadIdx.x;
+    const size_t ld = (size_t)L.ld;
+    // threads 0..6: z-integrals of the row integrals; 7..10: from kent for C types
+    if (t < NROWINT + 4) {
+        int q = (t < NROWINT) ? t : (t - NROWINT);
+        int k0 = (t < NROWINT) ? 0 : kent;
+        bool active = true;
+        if (q < 4 && q >= P.ntype) active = false;
+        if (t >= NROWINT && q >= 4) active = false;
+        if (active) {
+            const double* f = rows + (size_t)q * (nz + 1);
+            double fint = 0.0;
+            for (int k = k0; k <= nz - 1; k++) fint = fint + 0.5 * (f[k] * 1.0 + f[k + 1] * 1.0) * P.ds;
+            int slot = (t < NROWINT) ? ((q < 4) ? q : (q - 4 + 8)) : (4 + q);
+            ds->integ[slot] = fint;
+        }
+    } else if (t == 16) {
+        // top-row mobility integrand and the Nusselt integrands
+        double a = 0.0, b = 0.0, c = 0.0, m = 0.0;
+        auto top = [&](int i) { size_t x = IX(L, i, nz); return u[x] * u[x] + w[x] * w[x]; };
+        auto Tzs = [&](int i) { size_t x = IX(L, i, nz); return (-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0; };
+        auto Tzb = [&](int i) { size_t x = IX(L, i, 0); return (-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0; };
+        for (int i = 0; i <= nx - 1; i++) {
+            m = m + 0.5 * (top(i) * 1.0 + top(i + 1) * 1.0) * P.dr;
+            if (P.RaT != 0.0) {
+                double ai = -cd[IX(L, i, nz)] * Tzs(i), ai1 = -cd[IX(L, i + 1, nz)] * Tzs(i + 1);
+                a = a + 0.5 * (ai * 1.0 + ai1 * 1.0) * P.dr;
+                double bi = T[IX(L, i, 0)], bi1 = T[IX(L, i + 1, 0)];
+                b = b + 0.5 * (bi * 1.0 + bi1 * 1.0) * P.dr;
+                double ci = -cd[IX(L, i, 0)] * Tzb(i), ci1 = -cd[IX(L, i + 1, 0)] * Tzb(i + 1);
+                c = c + 0.5 * (ci * 1.0 + ci1 * 1.0) * P.dr;
+            }
+        }
+        ds->integ[11] = m;
+        ds->integ[12] = a;
+        ds->integ[13] = b;
+        ds->integ[14] = c;
+        if (P.RaT != 0.0) {
+            auto dz = [&](int i, int kk) { size_t x = IX(L, i, kk); return -0.5 * T[x - ld] + 0.5 * T[x + ld]; };
+            ds->integ[15] = -(cd[IX(L, 0, nz)] * dz(0, nz)) / P.ds / 1.0;
+            ds->integ[16] = -(cd[IX(L, nx, nz)] * dz(nx, nz)) / P.ds / 1.0;
+            ds->integ[17] = -(cd[IX(L, nx, 0)] * dz(nx, 0)) / P.ds / 1.0;
+            ds->integ[18] = -(cd[IX(L, 0, 0)] * dz(0, 0)) / P.ds / 1.0;
+        }
+        double smax = -INFINITY;
+        for (int i = 0; i <= nx; i++) smax = fmax(smax, st[IX(L, i, nz)]);
+        ds->strain_max = smax;
+    }
+}
+__global__ void k_nempty_stats(Lay L, Range2 r, const int* __restrict__ ne, DevScalars* ds) {
+    RANGE_IK(r);
+    __shared__ int smin, smax, szero;
+    int tid = threadIdx.x + threadIdx.y * blockDim.x;
+    if (tid == 0) { smin = 0x7fffffff; smax = -0x7fffffff; szero = 0; }
+    __syncthreads();
+    if (inr) {
+        int v = ne[IX(L, i, k)];
+        atomicMin(&smin, v);
+        atomicMax(&smax, v);
+        if (v == 0) atomicAdd(&szero, 1);
+    }
+    __syncthreads();
+    if (tid == 0) {
+        atomicMin(&ds->nempty_min, smin);
+        atomicMax(&ds->nempty_max, smax);
+        atomicAdd(&ds->empty_cells, szero);
+    }
+}
+__global__ void k_nempty_init(DevScalars* ds) {
+    ds->nempty_min = 0x7fffffff;
+    ds->nempty_max = -0x7fffffff;
+    ds->empty_cells = 0;
+}
+void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const double* T, const double* u,
+                  const double* w, const double* conduct, const double* vis, const double* strain,
+                  const double* const* Cnew, const int* nempty, double* rows, DevScalars* ds) {
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
+    k_stats_rows<<<(L.b + 1 + 63) / 64, 64, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows);
+    k_stats_final<<<1, 32, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds);
+    if (P.comp == 1) {
+        Range2 r{0, L.a, 0, L.b};
+        k_nempty_init<<<1, 1, 0, s>>>(ds);
+        k_nempty_stats<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, nempty, ds);
+    }
+}

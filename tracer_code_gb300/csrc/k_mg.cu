@@ -1,0 +1,629 @@
+// k_mg.cu -- multigrid kernels: per-level viscosity, eigenvalue ratios,
+// folded 13-point operator, Richardson/Chebyshev sweeps, residual,
+// restriction, prolongation and the coarsest-grid banded LU.
+//
+// Reference: iterative_solver.f90 (multigrid :79-173, prolong :175-233,
+// compute_residual :258-279, viscosity_gradients :290-329, compute_viscosity
+// :331-377, viscosityBCs(_initialize) :379-453, stream_space :456-561,
+// compute_RHS :563-594, restrict(_coefficients) :596-664, test_eigenvalues
+// :666-698, iterate_local_time_steps :700-748, eigI/eigR :750-857,
+// iterate_stream :860-963, enforceBCs_stream :965-989,
+// Compute_Matrix_coarse :1026-1179, Compute_coarse_vector :1181-1193,
+// Stream_grid_coarse :1195-1204) and smoother.f90 (vis_space, smoother_vis).
+// The kernels specialise the metric terms to the uniform grid (xr=zs=1,
+// xrr=...=0), which leaves every retained product and sum of the reference
+// unchanged.
+#include "tc_device.cuh"
+
+#include <stdio.h>
+
+// ---------------------------------------------------------------------------
+// visf on the full ghost-padded level-1 box (momentum.f90:1-30; ivis 0,1,2,-1)
+// ---------------------------------------------------------------------------
+__global__ void k_visf1(Lay L, Phys P, Range2 r, double* __restrict__ vis, const double* __restrict__ Tvis, CPtrs C,
+                        const double* __restrict__ zg) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    double v;
+    if (P.ivis == 1) {
+        v = exp(-Tvis[x] * P.lnvisT + (1.0 - zg[k]) * P.lnvisP);
+    } else if (P.ivis == 2 && P.comp == 1) {
+        double d = 0.0;
+        for (int j = 0; j < P.ntype; j++) d = d + C.p[j][x] * P.lnvisC[j];
+        if (P.RaT != 0.0) v = exp(-Tvis[x] * P.lnvisT - d + (1.0 - zg[k]) * P.lnvisP);
+        else v = exp(-d + (1.0 - zg[k]) * P.lnvisP);
+    } else if (P.ivis == -1) {
+        v = exp((1.0 - zg[k]) * P.lnvisP);
+    } else {
+        v = 1.0;
+    }
+    vis[x] = v;
+}
+void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis, const double* Tvis,
+                        const double* const* Cvis, const double* zg) {
+    Range2 r{-SP, L.a + SP, -SP, L.b + SP};
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
+    k_visf1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, vis, Tvis, C, zg);
+}
+
+// ---------------------------------------------------------------------------
+// viscosity_gradients (+ test_eigenvalues ratio and its minimum)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void eig_pair(const LevConst& c, double v, double vx, double vz, double vxx, double vzz,
+                                         double vxz, double& eR, double& eI) {
+    double t1 = (vxx - vzz) * c.eK1;
+    double t2 = v * c.eK2;
+    double t3 = 2.0 * v * c.eTrrss;
+    double t4 = 4.0 * vxz * c.eTrs;
+    eR = -(t1 + t2 + t3 + t4);
+    double t5 = 2.0 * vx * c.eK5;
+    double t6 = 2.0 * vz * c.eK6;
+    eI = fabs(t5) + fabs(t6);
+}
+
+__global__ void k_vis_grad(Lay L, LevConst c, Range2 r, const double* __restrict__ V, double* __restrict__ vx,
+                           double* __restrict__ vz, double* __restrict__ vxx, double* __restrict__ vzz,
+                           double* __restrict__ vxz, double* __restrict__ ratio, int do_eig, int ivis,
+                           RedScratch rs, double* out_min) {
+    RANGE_IK(r);
+    double rat = INFINITY;
+    if (inr) {
+        size_t x = IX(L, i, k);
+        if (ivis == 0) {
+            vx[x] = 0.0; vz[x] = 0.0; vxx[x] = 0.0; vzz[x] = 0.0; vxz[x] = 0.0;
+        } else {
+            const size_t ld = (size_t)L.ld;
+            double v0 = V[x], vm = V[x - 1], vp = V[x + 1], vzm = V[x - ld], vzp = V[x + ld];
+            double vis_r = (-0.5 * vm + 0.5 * vp) / c.dr;
+            double vis_rr = (vm + -2.0 * v0 + vp) / c.dr2;
+            double vis_s = (-0.5 * vzm + 0.5 * vzp) / c.ds;
+            double vis_ss = (vzm + -2.0 * v0 + vzp) / c.ds2;
+            double vis_rs = (0.25 * V[x - 1 - ld] + -0.25 * V[x + 1 - ld] + -0.25 * V[x - 1 + ld] + 0.25 * V[x + 1 + ld]) / c.drds;
+            vx[x] = vis_r; vz[x] = vis_s; vxx[x] = vis_rr; vzz[x] = vis_ss; vxz[x] = vis_rs;
+            if (do_eig) {
+                double eR, eI;
+                eig_pair(c, v0, vis_r, vis_s, vis_rr, vis_ss, vis_rs, eR, eI);
+                rat = fabs(eR / eI);
+                ratio[x] = rat;
+            }
+        }
+    }
+    if (do_eig && ivis != 0) reduce_to(RED_MIN, rat, rs.part, rs.count, out_min);
+}
+void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_eig, int ivis, RedScratch rs,
+                     DevScalars* ds) {
+    Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
+    k_vis_grad<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
+                                                     lv.ratio, do_eig, ivis, rs, &ds->ratio_min);
+}
+
+// ---------------------------------------------------------------------------
+// one Chebyshev step of smoother_vis with viscosityBCs fused
+// ---------------------------------------------------------------------------
+__global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restrict__ Vin, double* __restrict__ Vout,
+                             const double* __restrict__ dtv, double c, int RaTnz, double visT2) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t ld = (size_t)L.ld;
+    size_t x = IX(L, i, k);
+    double v0 = Vin[x];
+    double Trr = (Vin[x - 1] + -2.0 * v0 + Vin[x + 1]) / cc.dr2;
+    double Tss = (Vin[x - ld] + -2.0 * v0 + Vin[x + ld]) / cc.ds2;
+    double temp = Trr + Tss;
+    double dts = dtv[x] * 0.99;
+    double v = v0 + c * dts * temp;
+    Vout[x] = v;
+    const int a = L.a, b = L.b;
+    // side ghosts (rows 0..b): V(-i,k)=V(i,k), V(a+i,k)=V(a-i,k)
+    int gi[3] = {i, 0, 0};
+    int ng = 1;
+    if (i >= 1 && i <= SP) gi[ng++] = -i;
+    if (i >= a - SP && i <= a - 1) gi[ng++] = 2 * a - i;
+    for (int t = 1; t < ng; t++) Vout[IX(L, gi[t], k)] = v;
+    // top/bottom ghosts of this column and of its side-ghost columns
+    if (k >= 1 && k <= SP) {
+        double g = RaTnz ? (1.0 / v / visT2) : v;
+        for (int t = 0; t < ng; t++) Vout[IX(L, gi[t], -k)] = g;
+    }
+    if (k >= b - SP && k <= b - 1) {
+        double g = RaTnz ? (1.0 / v) : v;
+        for (int t = 0; t < ng; t++) Vout[IX(L, gi[t], 2 * b - k)] = g;
+    }
+}
+void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
+                       int kmax, int RaT_nonzero, double visT2) {
+    Range2 r{0, lv.L.a, kmin, kmax};
+    k_vis_smooth<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vin, vout, lv.dt_vis, c, RaT_nonzero, visT2);
+}
+
+// ---------------------------------------------------------------------------
+// restrict_coefficients + boundary injection of viscosityBCs_initialize
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double restrict9(const double* __restrict__ in, const Lay& F, int ii, int kk) {
+    // corner term repeats (ii-1,kk+1) and omits (ii+1,kk-1), as iterative_solver.f90:607
+    double corners = (in[IX(F, ii - 1, kk - 1)] + in[IX(F, ii - 1, kk + 1)] + in[IX(F, ii + 1, kk + 1)] +
+                      in[IX(F, ii - 1, kk + 1)]) / 16.0;
+    double sides = (in[IX(F, ii - 1, kk)] + in[IX(F, ii, kk - 1)] + in[IX(F, ii + 1, kk)] + in[IX(F, ii, kk + 1)]) / 8.0;
+    double centre = in[IX(F, ii, kk)] / 4.0;
+    return corners + sides + centre;
+}
+__global__ void k_restrict_vis(Lay C, Lay F, Range2 r, const double* __restrict__ vf, double* __restrict__ vc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int a = C.a, b = C.b;
+    double v;
+    if (i >= 1 && i <= a - 1 && k >= 1 && k <= b - 1) v = restrict9(vf, F, 2 * i, 2 * k);
+    else if (k >= 1 && k <= b - 1) v = (i == 0) ? vf[IX(F, 0, 2 * k)] : vf[IX(F, F.a, 2 * k)];
+    else v = (k == 0) ? vf[IX(F, 2 * i, 0)] : vf[IX(F, 2 * i, F.b)];
+    vc[IX(C, i, k)] = v;
+}
+void launch_restrict_vis(cudaStream_t s, const Level& coarse, const Level& fine, const double* vfine, double* vcoarse) {
+    Range2 r{0, coarse.L.a, 0, coarse.L.b};
+    k_restrict_vis<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, vfine, vcoarse);
+}
+
+// ghosts of viscosityBCs_initialize computed from their mirror sources
+__global__ void k_vis_bcs_init(Lay L, Range2 r, double* __restrict__ V, int RaTnz, double visT2) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int a = L.a, b = L.b;
+    if (i >= 0 && i <= a && k >= 0 && k <= b) return;
+    int mi = (i < 0) ? -i : ((i > a) ? 2 * a - i : i);
+    if (k >= 0 && k <= b) {
+        V[IX(L, i, k)] = V[IX(L, mi, k)];
+        return;
+    }
+    int mk = (k < 0) ? -k : 2 * b - k;
+    double src = V[IX(L, mi, mk)];
+    double g;
+    if (RaTnz) g = (k < 0) ? (1.0 / src / visT2) : (1.0 / src);
+    else g = src;
+    V[IX(L, i, k)] = g;
+}
+void launch_vis_bcs_init(cudaStream_t s, const Level& coarse, double* v, int RaT_nonzero, double visT2) {
+    Range2 r{-SP, coarse.L.a + SP, -SP, coarse.L.b + SP};
+    k_vis_bcs_init<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, r, v, RaT_nonzero, visT2);
+}
+
+// ---------------------------------------------------------------------------
+// iterate_local_time_steps + folding of stream_space into 13 coefficients
+// ---------------------------------------------------------------------------
+__global__ void k_level_coefs(Lay L, LevConst c, Range2 r, const double* __restrict__ V, const double* __restrict__ vx,
+                              const double* __restrict__ vz, const double* __restrict__ vxx,
+                              const double* __restrict__ vzz, const double* __restrict__ vxz,
+                              const double* __restrict__ ratio, double* __restrict__ dts, double* __restrict__ coef,
+                              double* __restrict__ cA, double* __restrict__ cB, double courant_stream, int cheb) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    double v = V[x], ax = vx[x], az = vz[x], axx = vxx[x], azz = vzz[x], axz = vxz[x];
+    double eR, eI;
+    eig_pair(c, v, ax, az, axx, azz, axz, eR, eI);
+    dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
+    double g0 = axx - azz, g1 = v, g2 = 2.0 * v, g3 = 4.0 * axz, g4 = 2.0 * ax, g5 = 2.0 * az;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) {
+        double A = g0 * c.fold[d][0];
+        A = fma(g1, c.fold[d][1], A);
+        A = fma(g2, c.fold[d][2], A);
+        A = fma(g3, c.fold[d][3], A);
+        A = fma(g4, c.fold[d][4], A);
+        A = fma(g5, c.fold[d][5], A);
+        coef[(size_t)d * L.plane + x] = A;
+    }
+    if (cheb) {
+        double rr = ratio[x];
+        double lb = (rr > 1.0e99) ? -2.0 : (-2.0 * (rr * rr) / (1.0 + rr * rr));
+        const double la = -1.0;
+        cA[x] = -lb - la;
+        cB[x] = lb - la;
+    }
+}
+void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int ivis, double courant_stream,
+                        int cheb_level) {
+    (void)ivis;
+    Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
+    k_level_coefs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
+                                                        lv.ratio, lv.dt_stream, lv.coef, lv.cA, lv.cB,
+                                                        courant_stream, cheb_level);
+}
+
+// ---------------------------------------------------------------------------
+// folded operator: RHS - L S at an interior point
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double folded_residual(const Lay& L, const double* __restrict__ S,
+                                                  const double* __restrict__ coef, double rhs, size_t x) {
+    const size_t ld = (size_t)L.ld, pl = L.plane;
+    const double* cf = coef + x;
+    double acc = rhs;
+    acc = fma(-__ldg(cf + 0 * pl), __ldg(S + x), acc);
+    acc = fma(-__ldg(cf + 1 * pl), __ldg(S + x - 1), acc);
+    acc = fma(-__ldg(cf + 2 * pl), __ldg(S + x + 1), acc);
+    acc = fma(-__ldg(cf + 3 * pl), __ldg(S + x - 2), acc);
+    acc = fma(-__ldg(cf + 4 * pl), __ldg(S + x + 2), acc);
+    acc = fma(-__ldg(cf + 5 * pl), __ldg(S + x - ld), acc);
+    acc = fma(-__ldg(cf + 6 * pl), __ldg(S + x + ld), acc);
+    acc = fma(-__ldg(cf + 7 * pl), __ldg(S + x - 2 * ld), acc);
+    acc = fma(-__ldg(cf + 8 * pl), __ldg(S + x + 2 * ld), acc);
+    acc = fma(-__ldg(cf + 9 * pl), __ldg(S + x - 1 - ld), acc);
+    acc = fma(-__ldg(cf + 10 * pl), __ldg(S + x + 1 - ld), acc);
+    acc = fma(-__ldg(cf + 11 * pl), __ldg(S + x - 1 + ld), acc);
+    acc = fma(-__ldg(cf + 12 * pl), __ldg(S + x + 1 + ld), acc);
+    return acc;
+}
+
+// writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
+// derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
+__device__ __forceinline__ void store_stream(const Lay& L, double* __restrict__ S, int i, int k, double v, int Vbc) {
+    const int a = L.a, b = L.b;
+    int gi[3] = {i, 0, 0};
+    double si[3] = {1.0, -1.0, -1.0};
+    int ng = 1;
+    if (i <= SP) gi[ng++] = -i;
+    if (i >= a - SP) gi[ng++] = 2 * a - i;
+    int gk[3] = {k, 0, 0};
+    const double zsgn = (Vbc == 1) ? 1.0 : -1.0;
+    double sk[3] = {1.0, zsgn, zsgn};
+    int nk = 1;
+    if (k <= SP) gk[nk++] = -k;
+    if (k >= b - SP) gk[nk++] = 2 * b - k;
+    for (int u = 0; u < nk; u++)
+        for (int t = 0; t < ng; t++) S[IX(L, gi[t], gk[u])] = (si[t] * sk[u]) * v;
+}
+
+__global__ void k_sweep(Lay L, Range2 r, const double* __restrict__ Sin, double* __restrict__ Sout,
+                        const double* __restrict__ coef, const double* __restrict__ rhs,
+                        const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
+                        double c_uniform, int per_point, double temp, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(L, i, k);
+    double res = folded_residual(L, Sin, coef, __ldg(rhs + x), x);
+    double c = per_point ? 2.0 / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
+    double v = fma(c * __ldg(dts + x), res, __ldg(Sin + x));
+    store_stream(L, Sout, i, k, v, Vbc);
+}
+void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
+                  int per_point, double temp, int Vbc) {
+    Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
+    k_sweep<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
+                                                  c_uniform, per_point, temp, Vbc);
+}
+
+__global__ void k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
+                           const double* __restrict__ rhs, double* __restrict__ res, RedScratch rs, double* out,
+                           double div1, double div2) {
+    RANGE_IK(r);
+    double a = 0.0;
+    if (inr) {
+        size_t x = IX(L, i, k);
+        double v = folded_residual(L, S, coef, __ldg(rhs + x), x);
+        res[x] = v;
+        a = fabs(v);
+    }
+    reduce_to(RED_SUM, a, rs.part, rs.count, out, div1, div2);
+}
+void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out) {
+    Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
+    k_residual<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef, lv.rhs, lv.res, rs, res_out,
+                                                     (double)(lv.L.a - 1), (double)(lv.L.b - 1));
+}
+
+__global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    rc[IX(C, i, k)] = restrict9(rf, F, 2 * i, 2 * k);
+}
+void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c) {
+    Range2 r{1, coarse.L.a - 1, 1, coarse.L.b - 1};
+    k_restrict_res<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c);
+}
+
+// prolong (bilinear, additive) with the fine level's stream BCs fused
+__global__ void k_prolong(Lay C, Lay F, Range2 r, const double* __restrict__ ec, double* __restrict__ ef, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    size_t x = IX(F, i, k);
+    double add;
+    bool ie = (i % 2) == 0, ke = (k % 2) == 0;
+    if (ie && ke) add = ec[IX(C, i / 2, k / 2)];
+    else if (ie) add = (ec[IX(C, i / 2, (k - 1) / 2)] + ec[IX(C, i / 2, (k + 1) / 2)]) / 2.0;
+    else if (ke) add = (ec[IX(C, (i - 1) / 2, k / 2)] + ec[IX(C, (i + 1) / 2, k / 2)]) / 2.0;
+    else
+        add = (ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
+               ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / 4.0;
+    store_stream(F, ef, i, k, ef[x] + add, Vbc);
+}
+void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc) {
+    Range2 r{1, fine.L.a - 1, 1, fine.L.b - 1};
+    k_prolong<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc);
+}
+
+// enforceBCs_stream: walls zero, ghosts mirrored from the interior
+__global__ void k_stream_bcs(Lay L, Range2 r, double* __restrict__ S, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const int a = L.a, b = L.b;
+    if (i > 0 && i < a && k > 0 && k < b) return;
+    int mi = i, mk = k;
+    double sg = 1.0;
+    if (i < 0) { mi = -i; sg = -sg; }
+    else if (i > a) { mi = 2 * a - i; sg = -sg; }
+    if (k < 0) { mk = -k; if (Vbc == 0) sg = -sg; }
+    else if (k > b) { mk = 2 * b - k; if (Vbc == 0) sg = -sg; }
+    double v = 0.0;
+    if (mi > 0 && mi < a && mk > 0 && mk < b) v = sg * S[IX(L, mi, mk)];
+    S[IX(L, i, k)] = v;
+}
+void launch_stream_bcs(cudaStream_t s, const Level& lv, double* S, int Vbc) {
+    Range2 r{-SP, lv.L.a + SP, -SP, lv.L.b + SP};
+    k_stream_bcs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, Vbc);
+}
+
+// ---------------------------------------------------------------------------
+// coarsest grid: band assembly (Database=2 ordering), DGBEQU row scaling,
+// dgbtf2 LU with partial pivoting, dgbtrs solve, scatter + BCs
+// ---------------------------------------------------------------------------
+__global__ void k_coarse_build(Lay L, const double* __restrict__ coef, double* __restrict__ AB, double* __restrict__ rowb,
+                               int n, int kl, int ku, int Vbc) {
+    int pp = 1 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    if (pp > n) return;
+    const int nxc = L.a, nzc = L.b, N = nzc + 1, ldab = 2 * kl + ku + 1, kv1 = kl + ku + 1;
+    int kp = pp - N * ((pp - 1) / N) - 1, ip = (pp - 1) / N;
+#define ABr(rw, cl) AB[(size_t)((rw) - 1) + (size_t)((cl) - 1) * ldab]
+    // loop order of Compute_Matrix_coarse: j=-2..2, kq ascending
+    const int od[13][3] = {{-2, 0, 3}, {-1, -1, 9}, {-1, 0, 1}, {-1, 1, 11}, {0, -2, 7}, {0, -1, 5}, {0, 0, 0},
+                           {0, 1, 6},  {0, 2, 8},   {1, -1, 10}, {1, 0, 2},  {1, 1, 12}, {2, 0, 4}};
+    if (ip > 0 && ip < nxc && kp > 0 && kp < nzc) {
+        size_t x = IX(L, ip, kp);
+        for (int t = 0; t < 13; t++) {
+            int iq = ip + od[t][0], kq = kp + od[t][1];
+            if (iq >= 0 && iq <= nxc && kq >= 0 && kq <= nzc) {
+                int q = N * iq + kq + 1;
+                int rw = kv1 + pp - q;
+                if (rw >= 1 && rw <= ldab) ABr(rw, q) = coef[(size_t)od[t][2] * L.plane + x];
+            }
+        }
+        for (int t = 0; t < 13; t++) {
+            int iq = ip + od[t][0], kq = kp + od[t][1];
+            if (iq < 0 || iq > nxc || kq < 0 || kq > nzc) {
+                int iiq, kkq;
+                double xval, zval;
+                if (iq < 0) { iiq = -iq; xval = -1.0; }
+                else if (iq > nxc) { iiq = 2 * nxc - iq; xval = -1.0; }
+                else { iiq = iq; xval = 1.0; }
+                if (kq < 0) { kkq = -kq; zval = (Vbc == 0) ? -1.0 : 1.0; }
+                else if (kq > nzc) { kkq = 2 * nzc - kq; zval = (Vbc == 0) ? -1.0 : 1.0; }
+                else { kkq = kq; zval = 1.0; }
+                int q = N * iiq + kkq + 1;
+                int rw = kv1 + pp - q;
+                if (rw >= 1 && rw <= ldab) ABr(rw, q) = ABr(rw, q) + coef[(size_t)od[t][2] * L.plane + x] * (xval * zval);
+            }
+        }
+    } else {
+        ABr(kv1, pp) = 1.0;
+    }
+    // DGBEQU row factor of row pp, then scaling of the row
+    double m = 0.0;
+    int q0 = max(1, pp - kl), q1 = min(n, pp + ku);
+    for (int q = q0; q <= q1; q++) m = fmax(m, fabs(ABr(kv1 + pp - q, q)));
+    const double smlnum = 2.2250738585072014e-308, bignum = 1.0 / smlnum;
+    double R = 1.0 / fmin(fmax(m, smlnum), bignum);
+    rowb[pp - 1] = R;
+    for (int q = q0; q <= q1; q++) ABr(kv1 + pp - q, q) = R * ABr(kv1 + pp - q, q);
+#undef ABr
+}
+void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* rowb, int kl, int ku, int Vbc) {
+    int n = (lv.L.a + 1) * (lv.L.b + 1);
+    cudaMemsetAsync(band, 0, sizeof(double) * (size_t)(2 * kl + ku + 1) * n, s);
+    k_coarse_build<<<(n + 127) / 128, 128, 0, s>>>(lv.L, lv.coef, band, rowb, n, kl, ku, Vbc);
+}
+
+// dgbtf2 on one CTA.  The band lives in shared memory when it fits.
+__global__ void k_coarse_lu(double* __restrict__ ABg, int* __restrict__ ipiv, int n, int kl, int ku, int in_smem,
+                            int* info_out) {
+    extern __shared__ double sm[];
+    const int ldab = 2 * kl + ku + 1, KV = ku + kl;
+    const size_t tot = (size_t)ldab * n;
+    double* AB = in_smem ? sm : ABg;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (in_smem)
+        for (size_t t = tid; t < tot; t += nth) sm[t] = ABg[t];
+    __shared__ int sJP, sJU, sInfo;
+    __shared__ double sPiv;
+    if (tid == 0) { sJU = 1; sInfo = 0; }
+    __syncthreads();
+#define A_(rw, cl) AB[(size_t)((rw) - 1) + (size_t)((cl) - 1) * ldab]
+    for (int j = ku + 2; j <= min(KV, n); j++)
+        for (int i = KV - j + 2 + tid; i <= kl; i += nth) A_(i, j) = 0.0;
+    __syncthreads();
+    for (int j = 1; j <= n; j++) {
+        if (j + KV <= n)
+            for (int i = 1 + tid; i <= kl; i += nth) A_(i, j + KV) = 0.0;
+        const int KM = min(kl, n - j);
+        __syncthreads();
+        if (tid < 32) {
+            // idamax: first index of the largest |value| among rows KV+1..KV+1+KM
+            double best = -1.0;
+            int bi = 1 << 30;
+            for (int t = 1 + tid; t <= KM + 1; t += 32) {
+                double v = fabs(A_(KV + t, j));
+                if (v > best) { best = v; bi = t; }
+            }
+            for (int off = 16; off > 0; off >>= 1) {
+                double ob = __shfl_down_sync(0xffffffffu, best, off);
+                int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (tid == 0) {
+                sJP = bi;
+                ipiv[j - 1] = bi + j - 1;
+                sPiv = A_(KV + bi, j);
+                if (sPiv != 0.0) sJU = max(sJU, min(j + ku + bi - 1, n));
+                else if (sInfo == 0) sInfo = j;
+            }
+        }
+        __syncthreads();
+        const int JP = sJP, JU = sJU;
+        if (sPiv != 0.0) {
+            if (JP != 1) {
+                for (int c = tid; c <= JU - j; c += nth) {
+                    double t0 = A_(KV + JP - c, j + c);
+                    A_(KV + JP - c, j + c) = A_(KV + 1 - c, j + c);
+                    A_(KV + 1 - c, j + c) = t0;
+                }
+                __syncthreads();
+            }
+            if (KM > 0) {
+                const double rcp = 1.0 / A_(KV + 1, j);
+                for (int t = 1 + tid; t <= KM; t += nth) A_(KV + 1 + t, j) = rcp * A_(KV + 1 + t, j);
+                __syncthreads();
+                const int ncol = JU - j;
+                for (int e = tid; e < ncol * KM; e += nth) {
+                    int c = 1 + e / KM, t = 1 + e % KM;
+                    double temp = -A_(KV + 1 - c, j + c);
+                    if (temp != 0.0) A_(KV + 1 + t - c, j + c) = A_(KV + 1 + t - c, j + c) + A_(KV + 1 + t, j) * temp;
+                }
+            }
+        }
+        __syncthreads();
+    }
+#undef A_
+    if (in_smem)
+        for (size_t t = tid; t < tot; t += nth) ABg[t] = sm[t];
+    if (tid == 0) *info_out = sInfo;
+}
+void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, int ku, DevScalars* ds) {
+    size_t bytes = sizeof(double) * (size_t)(2 * kl + ku + 1) * n;
+    int in_smem = bytes <= 200 * 1024 ? 1 : 0;
+    size_t sm = in_smem ? bytes : 0;
+    if (in_smem) cudaFuncSetAttribute(k_coarse_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info);
+}
+
+// Compute_coarse_vector + DGBTRS + Stream_grid_coarse + enforceBCs_stream
+__global__ void k_coarse_solve(Lay L, const double* __restrict__ ABg, const int* __restrict__ ipiv,
+                               const double* __restrict__ rowb, const double* __restrict__ rhs, int n, int kl, int ku,
+                               int in_smem, double* __restrict__ Bg, double* __restrict__ err, int Vbc) {
+    extern __shared__ double sm[];
+    const int ldab = 2 * kl + ku + 1, KD = ku + kl + 1, K = kl + ku;
+    const size_t tot = (size_t)ldab * n;
+    const double* AB = in_smem ? sm : ABg;
+    double* B = in_smem ? (sm + tot) : Bg;
+    const int tid = threadIdx.x, nth = blockDim.x;
+    if (in_smem)
+        for (size_t t = tid; t < tot; t += nth) sm[t] = ABg[t];
+    const int nxc = L.a, nzc = L.b, N = nzc + 1;
+    for (int pp = 1 + tid; pp <= n; pp += nth) {
+        int kp = pp - N * ((pp - 1) / N) - 1, ip = (pp - 1) / N;
+        double v = 0.0;
+        if (ip >= 1 && ip <= nxc - 1 && kp >= 1 && kp <= nzc - 1) v = rhs[IX(L, ip, kp)] * rowb[pp - 1];
+        B[pp - 1] = v;
+    }
+    __syncthreads();
+#define A_(rw, cl) AB[(size_t)((rw) - 1) + (size_t)((cl) - 1) * ldab]
+    if (tid < 32) {
+        // L solve with row interchanges
+        if (kl > 0)
+            for (int j = 1; j <= n - 1; j++) {
+                int LM = min(kl, n - j);
+                int Lr = ipiv[j - 1];
+                if (Lr != j) {
+                    if (tid == 0) { double t0 = B[Lr - 1]; B[Lr - 1] = B[j - 1]; B[j - 1] = t0; }
+                    __syncwarp();
+                }
+                double temp = -B[j - 1];
+                if (temp != 0.0)
+                    for (int t = 1 + tid; t <= LM; t += 32) B[j + t - 1] = B[j + t - 1] + A_(KD + t, j) * temp;
+                __syncwarp();
+            }
+        // dtbsv: upper, no transpose, non-unit
+        for (int j = n; j >= 1; j--) {
+            double bj = B[j - 1];
+            if (bj != 0.0) {
+                int Lc = K + 1 - j;
+                double temp = bj / A_(K + 1, j);
+                __syncwarp();
+                if (tid == 0) B[j - 1] = temp;
+                for (int i = j - 1 - tid; i >= max(1, j - K); i -= 32) B[i - 1] = B[i - 1] - temp * A_(Lc + i, j);
+            }
+            __syncwarp();
+        }
+    }
+#undef A_
+    __syncthreads();
+    // scatter (all nodes, walls included) then ghosts
+    for (int pp = 1 + tid; pp <= n; pp += nth) {
+        int kp = pp - N * ((pp - 1) / N) - 1, ip = (pp - 1) / N;
+        double v = B[pp - 1];
+        if (ip == 0 || ip == nxc || kp == 0 || kp == nzc) v = 0.0;
+        err[IX(L, ip, kp)] = v;
+    }
+    __syncthreads();
+    const int wi = nxc + 1 + 2 * SP, wk = nzc + 1 + 2 * SP;
+    for (int t = tid; t < wi * wk; t += nth) {
+        int i = -SP + t % wi, k = -SP + t / wi;
+        if (i >= 0 && i <= nxc && k >= 0 && k <= nzc) continue;
+        int mi = i, mk = k;
+        double sg = 1.0;
+        if (i < 0) { mi = -i; sg = -sg; }
+        else if (i > nxc) { mi = 2 * nxc - i; sg = -sg; }
+        if (k < 0) { mk = -k; if (Vbc == 0) sg = -sg; }
+        else if (k > nzc) { mk = 2 * nzc - k; if (Vbc == 0) sg = -sg; }
+        double v = 0.0;
+        if (mi > 0 && mi < nxc && mk > 0 && mk < nzc) v = sg * err[IX(L, mi, mk)];
+        err[IX(L, i, k)] = v;
+    }
+}
+void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                         int n, int kl, int ku, double* bvec, double* err, int Vbc) {
+    size_t bytes = sizeof(double) * ((size_t)(2 * kl + ku + 1) * n + n);
+    int in_smem = bytes <= 200 * 1024 ? 1 : 0;
+    size_t sm = in_smem ? bytes : 0;
+    if (in_smem) cudaFuncSetAttribute(k_coarse_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_coarse_solve<<<1, 512, sm, s>>>(lv.L, band, ipiv, rowb, lv.rhs, n, kl, ku, in_smem, bvec, err, Vbc);
+}
+
+__global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    size_t st = (size_t)gridDim.x * blockDim.x;
+    for (; t < n; t += st) dst[t] = src[t];
+}
+void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n) {
+    int nb = (int)((n + 255) / 256);
+    if (nb > 1216) nb = 1216;
+    k_copy<<<nb, 256, 0, s>>>(dst, src, n);
+}
+
+// compute_RHS(1) and compute_reference_residual(1)
+__global__ void k_rhs1(Lay L, Phys P, Range2 r, const double* __restrict__ Tb, CPtrs Cb, double* __restrict__ rhs,
+                       RedScratch rs, double* out, double div1, double div2) {
+    RANGE_IK(r);
+    double a = 0.0;
+    if (inr) {
+        size_t x = IX(L, i, k);
+        double R = 0.0;
+        if (P.RaT != 0.0) {
+            double Tr = (-0.5 * Tb[x - 1] + 0.5 * Tb[x + 1]) / P.dr;
+            R = P.RaT * Tr;
+        }
+        if (P.comp == 1)
+            for (int j = 0; j < P.ntype; j++) {
+                double Cr = (-0.5 * Cb.p[j][x - 1] + 0.5 * Cb.p[j][x + 1]) / P.dr;
+                R = R - P.RaC[j] * Cr;
+            }
+        rhs[x] = R;
+        a = fabs(R);
+    }
+    reduce_to(RED_SUM, a, rs.part, rs.count, out, div1, div2);
+}
+void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
+                 double* rhs, RedScratch rs, DevScalars* ds) {
+    Range2 r{1, L.a - 1, 1, L.b - 1};
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cbuoy[j];
+    k_rhs1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tbuoy, C, rhs, rs, &ds->res_ref, (double)(L.a - 2),
+                                                 (double)(L.b - 2));
+}

@@ -1,0 +1,1008 @@
+// tc_api.cu -- the C ABI of include/tracer_gpu.h and the host-side drivers
+// that sequence the kernels exactly as the reference sequences its loops.
+//
+// Control flow replaces these reference subroutines (one C++ function each,
+// same names): multigrid, iterate_stream, compute_viscosity, smoother_vis,
+// smoother_time, smoother_time_T, tracers_to_corners, energy_time, stats
+// (iterative_solver.f90, smoother.f90, composition.f90, energy.f90,
+// basics.f90).  All arithmetic runs in the kernels; the host only keeps the
+// reference's module scalars (Nvis_store, nn_store, n_eta, eig_fine, n_temp,
+// n_comp, kent, mass, time, tstep) and reads back the device scalars that the
+// reference's data-dependent loops branch on.
+#include "tc_device.cuh"
+#include "tc_setup.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace {
+
+const double kPi = 3.1415926535897932;
+
+struct Handle {
+    tc_params p{};
+    int nx = 0, nz = 0, grids = 0, nsteps = 0, ntype = 0;
+    int64_t ntr = 0;
+    int ngrid_coarse = 0, kl = 0, ku = 0;
+    std::vector<int> multi;  // multi(0:nsteps+1)
+    double grid_dr = 0, grid_ds = 0;
+    double delta_T = 2.0, delta_C[TC_MAX_TYPES];
+    tcs::EigBase eb{};
+    Phys P{};
+    Level lev[TC_MAXLEV + 1];
+    Lay L1{};
+    // fine fields (level-1 layout)
+    double *T = nullptr, *T0 = nullptr, *T1 = nullptr, *T2 = nullptr, *SF = nullptr;
+    double *Tvis = nullptr, *Tvis2 = nullptr, *Tbuoy = nullptr;
+    double *u = nullptr, *w = nullptr, *du = nullptr, *dw = nullptr;
+    double *conduct = nullptr, *conduct_r = nullptr, *conduct_s = nullptr, *dts = nullptr, *strain = nullptr;
+    double* Cnew[TC_MAX_TYPES] = {};
+    double* C0[TC_MAX_TYPES] = {};
+    double* Cvis[TC_MAX_TYPES] = {};
+    double* Cvis2[TC_MAX_TYPES] = {};
+    double* Cbuoy[TC_MAX_TYPES] = {};
+    int *counts = nullptr, *nempty = nullptr;
+    double* zg = nullptr;  // device, index k+SP+1
+    double *rtr = nullptr, *str = nullptr, *rtr0 = nullptr, *str0 = nullptr, *rtr1 = nullptr, *str1 = nullptr,
+           *rtr2 = nullptr, *str2 = nullptr;
+    int* ttype = nullptr;
+    double *band = nullptr, *rowb = nullptr, *bvec = nullptr;
+    int* ipiv = nullptr;
+    double* rows = nullptr;
+    RedScratch rs{};
+    DevScalars* ds = nullptr;
+    DevScalars* hs = nullptr;  // pinned mirror
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::vector<void*> allocs;
+    // module state
+    int tstep = 0;
+    double time = 0.0, dt = 0.0;
+    int kent = 0;
+    double mass[TC_MAX_TYPES] = {};
+    int n_eta = 0, n_temp = 0, n_comp[TC_MAX_TYPES] = {};
+    double eig_fine = 0.0;
+    int Nvis_store = 0, nn_store = 1;
+    int ratio_level = 0;
+    bool uploaded = false, lu_valid = false;
+    int last_cycles = 0;
+    long loop_cap = 100000;
+    std::string err;
+};
+
+#define CK(call)                                                      \
+    do {                                                              \
+        cudaError_t e_ = (call);                                      \
+        if (e_ != cudaSuccess) {                                      \
+            h->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
+            return TC_ERR_CUDA;                                       \
+        }                                                             \
+    } while (0)
+#define TRY(x)                    \
+    do {                          \
+        tc_status s_ = (x);       \
+        if (s_ != TC_OK) return s_; \
+    } while (0)
+
+tc_status dalloc(Handle* h, void** p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        h->err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+        return TC_ERR_ALLOC;
+    }
+    h->allocs.push_back(*p);
+    e = cudaMemset(*p, 0, bytes);
+    if (e != cudaSuccess) {
+        h->err = std::string("cudaMemset: ") + cudaGetErrorString(e);
+        return TC_ERR_CUDA;
+    }
+    return TC_OK;
+}
+template <class T>
+tc_status dalloc_t(Handle* h, T** p, size_t n) {
+    void* q = nullptr;
+    tc_status s = dalloc(h, &q, n * sizeof(T));
+    *p = (T*)q;
+    return s;
+}
+
+Lay make_lay(int a, int b) {
+    Lay L;
+    L.a = a; L.b = b;
+    int ni = a + 1 + 2 * SP;
+    L.ld = (ni + 31) / 32 * 32;
+    L.nk = b + 1 + 2 * SP;
+    L.plane = (size_t)L.ld * L.nk;
+    return L;
+}
+
+// Synchronise and fetch the device scalars; reports sticky kernel faults.
+tc_status sync_scalars(Handle* h) {
+    CK(cudaMemcpyAsync(h->hs, h->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    return TC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// boundary-condition and copy helpers
+// ---------------------------------------------------------------------------
+void copy_plane(Handle* h, double* dst, const double* src) {
+    cudaMemcpyAsync(dst, src, sizeof(double) * h->L1.plane, cudaMemcpyDeviceToDevice, h->st);
+}
+
+// load_conductivity_array (energy.f90:31-58)
+void load_conductivity_array(Handle* h) {
+    launch_conductivity(h->st, h->L1, h->P, h->Cvis, h->conduct, h->conduct_r, h->conduct_s);
+}
+
+// smoother_time_T (smoother.f90:343-377)
+tc_status smoother_time_T(Handle* h, const double* Tin) {
+    copy_plane(h, h->Tvis, Tin);
+    copy_plane(h, h->Tbuoy, Tin);
+    if (h->p.RaT == 0.0) return TC_OK;
+    int n = 0;
+    for (;;) {
+        launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
+        TRY(sync_scalars(h));
+        if (h->hs->diff < h->delta_T) { h->n_temp = n; break; }
+        if (n >= h->loop_cap) return TC_ERR_LOOP_CAP;
+        launch_smooth_T_step(h->st, h->L1, h->P, h->Tvis, h->Tvis2, h->dts);
+        launch_enforce_T(h->st, h->L1, h->Tvis2, h->p.Tbot);
+        std::swap(h->Tvis, h->Tvis2);
+        n++;
+    }
+    return TC_OK;
+}
+
+// smoother_time (smoother.f90:287-341)
+tc_status smoother_time(Handle* h) {
+    int Niter = 10;
+    const double lb = -5.0, la = -1.0;
+    for (int t = 0; t < h->ntype; t++) {
+        copy_plane(h, h->Cvis[t], h->Cnew[t]);
+        copy_plane(h, h->Cbuoy[t], h->Cnew[t]);
+    }
+    for (int t = 0; t < h->ntype; t++) {
+        int nn = 0;
+        bool trigger = false;
+        long guard = 0;
+        for (;;) {
+            for (int n = 1; n <= Niter; n++) {
+                launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
+                TRY(sync_scalars(h));
+                if (h->hs->diff < h->delta_C[t]) { trigger = true; break; }
+                double c;
+                if (nn == 0) {
+                    int ntemp = Niter - n + 1;
+                    c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
+                } else c = 1.0;
+                launch_smooth_C_step(h->st, h->L1, h->P, h->Cvis[t], h->Cvis2[t], h->dts, c);
+                launch_enforce_comp(h->st, h->L1, h->Cvis2[t], h->Cvis[t]);
+                std::swap(h->Cvis[t], h->Cvis2[t]);
+            }
+            if (trigger) break;
+            Niter = 1;
+            nn++;
+            if (++guard > h->loop_cap) return TC_ERR_LOOP_CAP;
+        }
+        h->n_comp[t] = nn;
+    }
+    return TC_OK;
+}
+
+// tracers_to_corners (composition.f90:669-790), comp=1, tracer=0
+tc_status tracers_to_corners(Handle* h, const double* rr, const double* ss, bool smooth) {
+    launch_histogram(h->st, h->L1, h->P, h->ntr, rr, ss, h->ttype, h->counts, h->ds);
+    launch_counts_to_comp(h->st, h->L1, h->P, h->counts, h->nempty, h->Cnew);
+    for (int t = 0; t < h->ntype; t++) launch_enforce_comp(h->st, h->L1, h->Cnew[t], h->Cnew[t]);
+    if (smooth) TRY(smoother_time(h));
+    load_conductivity_array(h);
+    return TC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// multigrid pieces
+// ---------------------------------------------------------------------------
+double* cur_vis(Handle* h, int l) { return h->lev[l].vis[h->lev[l].vcur]; }
+double* cur_err(Handle* h, int l) { return h->lev[l].err[h->lev[l].ecur]; }
+
+// viscosity_gradients + test_eigenvalues
+void grad_eig(Handle* h, int level, bool eig) {
+    Level& lv = h->lev[level];
+    launch_vis_grad(h->st, lv, cur_vis(h, level), eig ? 1 : 0, h->p.ivis, h->rs, h->ds);
+    if (eig) h->ratio_level = (h->p.ivis != 0) ? level : 0;
+}
+
+// smoother_vis (smoother.f90:166-263)
+tc_status smoother_vis(Handle* h, int level, int interpolate) {
+    Level& lv = h->lev[level];
+    int option, Niter;
+    double lb, la;
+    if (level == 1 && interpolate == 0) { option = 1; Niter = 6; lb = -5.0; la = -2.0; }
+    else { option = 0; Niter = h->p.vis_iter; lb = -2.0; la = -1.0; }
+    if (interpolate == 0 || level == 1) { h->Nvis_store = 0; h->nn_store = 1; }
+    const int a = lv.L.a, b = lv.L.b;
+    int kmin, kmax;
+    if (h->p.RaT == 0.0) { kmin = 0; kmax = b; } else { kmin = 1; kmax = b - 1; }
+    const int RaTnz = (h->p.RaT != 0.0) ? 1 : 0;
+    const double visT2 = h->p.visT * h->p.visT;
+    (void)a;
+    // the buffer that smoothing writes must already hold the rows it leaves unchanged
+    CK(cudaMemcpyAsync(lv.vis[1 - lv.vcur], lv.vis[lv.vcur], sizeof(double) * lv.L.plane, cudaMemcpyDeviceToDevice,
+                       h->st));
+    int n = 0;
+    bool trigger = false;
+    long guard = 0;
+    for (;;) {
+        const int nn_begin = h->nn_store;
+        for (int nn = nn_begin; nn <= Niter; nn++) {
+            grad_eig(h, level, true);
+            const bool ivis0 = (h->p.ivis == 0);
+            if (option == 1) {
+                bool need = (h->Nvis_store >= 1) && !ivis0 && !(n > 20);
+                double rmin = 0.0;
+                if (need || (h->Nvis_store >= 1 || ivis0 || n > 20)) {
+                    TRY(sync_scalars(h));
+                    rmin = h->hs->ratio_min;
+                }
+                if ((h->Nvis_store >= 1 && rmin > h->p.eig_ratio_min) || ivis0 || n > 20) {
+                    h->eig_fine = ivis0 ? 1.0e99 : rmin;
+                    h->n_eta = n;
+                    trigger = true;
+                    break;
+                }
+            } else if (interpolate == 0) {
+                double rmin = 0.0;
+                if (!ivis0) {
+                    TRY(sync_scalars(h));
+                    rmin = h->hs->ratio_min;
+                }
+                if (rmin > h->p.eig_ratio || ivis0) { trigger = true; h->nn_store = nn; break; }
+            } else {
+                if (h->Nvis_store >= 1 || ivis0) { trigger = true; break; }
+            }
+            const int ntemp = Niter - nn + 1;
+            const double c = 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
+            launch_vis_smooth(h->st, lv, lv.vis[lv.vcur], lv.vis[1 - lv.vcur], c, kmin, kmax, RaTnz, visT2);
+            lv.vcur = 1 - lv.vcur;
+            if (++guard > h->loop_cap) return TC_ERR_LOOP_CAP;
+        }
+        if (trigger) break;
+        h->Nvis_store = h->Nvis_store + 1;
+        h->nn_store = 1;
+        if (option == 1) { h->nn_store = 1; Niter = 6; lb = -2.0; la = -1.0; }
+        n = n + 1;
+        if (++guard > h->loop_cap) return TC_ERR_LOOP_CAP;
+    }
+    return TC_OK;
+}
+
+// compute_viscosity (iterative_solver.f90:331-377)
+tc_status compute_viscosity(Handle* h, int level) {
+    if (level == 1) {
+        launch_visf_level1(h->st, h->L1, h->P, cur_vis(h, 1), h->Tvis, h->Cvis, h->zg);
+        TRY(smoother_vis(h, 1, 0));
+        return TC_OK;
+    }
+    const int l1 = level - 1;
+    Level& f = h->lev[l1];
+    Level& c = h->lev[level];
+    const size_t by = sizeof(double) * f.L.plane;
+    double* src[6] = {cur_vis(h, l1), f.vx, f.vz, f.vxx, f.vzz, f.vxz};
+    for (int q = 0; q < 6; q++) CK(cudaMemcpyAsync(f.bak[q], src[q], by, cudaMemcpyDeviceToDevice, h->st));
+    TRY(smoother_vis(h, l1, 1));
+    launch_restrict_vis(h->st, c, f, cur_vis(h, l1), cur_vis(h, level));
+    launch_vis_bcs_init(h->st, c, cur_vis(h, level), h->p.RaT != 0.0 ? 1 : 0, h->p.visT * h->p.visT);
+    if (level < h->grids) TRY(smoother_vis(h, level, 0));
+    else grad_eig(h, level, false);
+    double* dst[6] = {cur_vis(h, l1), f.vx, f.vz, f.vxx, f.vzz, f.vxz};
+    for (int q = 0; q < 6; q++) CK(cudaMemcpyAsync(dst[q], f.bak[q], by, cudaMemcpyDeviceToDevice, h->st));
+    return TC_OK;
+}
+
+// iterate_stream (iterative_solver.f90:860-963), iterate_order=1
+void iterate_stream(Handle* h, int level, int dir) {
+    Level& lv = h->lev[level];
+    const int Niter = h->p.Nmulti;
+    const bool cheb_pp = (level == h->ratio_level);
+    for (int n = 1; n <= Niter; n++) {
+        const double ntemp = (double)(Niter - n + 1);
+        const double la = -1.0;
+        const double temp = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
+        double c = 1.0;
+        int per_point = 0;
+        if (dir != 1) {
+            if (cheb_pp) per_point = 1;
+            else {
+                const double lb = -2.0;
+                c = 2.0 / (-lb - la + (lb - la) * temp);
+            }
+        }
+        launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], c, per_point, temp, h->p.Vbc);
+        lv.ecur = 1 - lv.ecur;
+    }
+    launch_residual(h->st, lv, lv.err[lv.ecur], h->rs, &h->ds->res_mag[level]);
+}
+
+// multigrid (iterative_solver.f90:79-173), Newtonian branch
+tc_status multigrid(Handle* h) {
+    if (!h->uploaded) return TC_ERR_STATE;
+    const int G = h->grids;
+    copy_plane(h, cur_err(h, 1), h->SF);
+    launch_rhs1(h->st, h->L1, h->P, h->Tbuoy, h->Cbuoy, h->lev[1].rhs, h->rs, h->ds);
+    for (int l = 1; l <= G; l++) TRY(compute_viscosity(h, l));
+    for (int l = 1; l <= G; l++)
+        launch_level_coefs(h->st, h->lev[l], cur_vis(h, l), h->p.ivis, h->p.courant_stream, l == h->ratio_level ? 1 : 0);
+    if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) {
+        launch_coarse_build(h->st, h->lev[G], h->band, h->rowb, h->kl, h->ku, h->p.Vbc);
+        launch_coarse_lu(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ds);
+        h->lu_valid = true;
+    }
+    TRY(sync_scalars(h));
+    if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
+    const double res_ref1 = h->hs->res_ref;
+    int q = 1;
+    for (;;) {
+        bool conv = false;
+        for (int pp = 1; pp <= h->nsteps; pp++) {
+            const int level = h->multi[pp];
+            const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
+            if (h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse)
+                CK(cudaMemsetAsync(cur_err(h, level), 0, sizeof(double) * h->lev[level].L.plane, h->st));
+            if (h->multi[pp - 1] < h->multi[pp] && level > 1)
+                launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs);
+            if (level < G) {
+                iterate_stream(h, level, dir);
+            } else {
+                Level& lv = h->lev[G];
+                launch_coarse_solve(h->st, lv, h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku, h->bvec,
+                                    cur_err(h, G), h->p.Vbc);
+            }
+            if (level == 1) {
+                TRY(sync_scalars(h));
+                const double rm = h->hs->res_mag[1];
+                if (rm > 1.0e10 * res_ref1) return TC_ERR_MG_RESIDUAL;
+                if (rm / res_ref1 <= h->p.tolerance) { conv = true; break; }
+            }
+            if (h->multi[pp + 1] < h->multi[pp])
+                launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
+                               h->p.Vbc);
+        }
+        if (conv) break;
+        q = q + 1;
+        if (q > h->p.max_cycles) { h->last_cycles = q; return TC_ERR_MG_CYCLES; }
+    }
+    copy_plane(h, h->SF, cur_err(h, 1));
+    h->last_cycles = q;
+    return TC_OK;
+}
+
+void compute_velocities(Handle* h) { launch_velocities(h->st, h->L1, h->P, h->SF, h->u, h->w); }
+
+tc_status check_flags(Handle* h) {
+    TRY(sync_scalars(h));
+    if (h->hs->flag_outside) return TC_ERR_TRACER_OUTSIDE;
+    if (h->hs->flag_rk2) return TC_ERR_RK2_STABILITY;
+    return TC_OK;
+}
+
+tc_status update_velocities(Handle* h) {
+    TRY(multigrid(h));
+    compute_velocities(h);
+    return TC_OK;
+}
+
+// energy_time (energy.f90:117-453): field T, compositional tracers, local_time=0
+tc_status energy_time(Handle* h) {
+    if (!h->uploaded) return TC_ERR_STATE;
+    const bool trc = (h->p.comp == 1);
+    const int torder = h->p.torder;
+    const bool rat = (h->p.RaT != 0.0);
+    launch_stability(h->st, h->L1, h->P, h->conduct, h->conduct_r, h->conduct_s, h->u, h->w, h->p.courant,
+                     h->p.dt_manual, h->rs, h->ds);
+    TRY(check_flags(h));
+    for (int t = 0; t < h->ntype; t++) copy_plane(h, h->C0[t], h->Cnew[t]);
+    copy_plane(h, h->T0, h->T);
+    if (trc) { std::swap(h->rtr0, h->rtr); std::swap(h->str0, h->str); }
+    auto derivs = [&]() {
+        launch_derivatives(h->st, h->L1, h->P, h->u, h->du);
+        launch_derivatives(h->st, h->L1, h->P, h->w, h->dw);
+    };
+    auto restore_C = [&]() { for (int t = 0; t < h->ntype; t++) copy_plane(h, h->Cnew[t], h->C0[t]); };
+    auto stage_T = [&](int stage, const double* Tin, double* Tout) {
+        launch_energy_stage(h->st, h->L1, h->P, stage, Tin, h->T0, h->T, Tout, h->conduct, h->conduct_r, h->conduct_s,
+                            h->u, h->w, h->Cvis, h->ds);
+        launch_enforce_T(h->st, h->L1, stage == 4 ? h->T : Tout, h->p.Tbot);
+    };
+    // ---- stage 1 ----
+    if (rat) stage_T(1, h->T0, h->T1);
+    if (trc) {
+        derivs();
+        launch_tracer_stage(h->st, h->L1, h->P, torder, 1, h->ntr, h->rtr0, h->str0, h->rtr0, h->str0, h->rtr, h->str,
+                            h->rtr1, h->str1, h->u, h->w, h->du, h->dw, h->ds);
+    }
+    // ---- stage 2 ----
+    if (h->p.RK_update == 1) {
+        if (trc) TRY(tracers_to_corners(h, h->rtr1, h->str1, true));
+        TRY(smoother_time_T(h, h->T1));
+        TRY(update_velocities(h));
+        if (trc) derivs();
+    }
+    if (rat) stage_T(2, h->T1, h->T2);
+    if (trc)
+        launch_tracer_stage(h->st, h->L1, h->P, torder, 2, h->ntr, h->rtr1, h->str1, h->rtr0, h->str0, h->rtr, h->str,
+                            h->rtr2, h->str2, h->u, h->w, h->du, h->dw, h->ds);
+    if (torder >= 3) {
+        // ---- stage 3 ----
+        if (h->p.RK_update == 1) {
+            if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr2, h->str2, true)); }
+            TRY(smoother_time_T(h, h->T2));
+            TRY(update_velocities(h));
+            if (trc) derivs();
+        }
+        if (rat) stage_T(3, h->T2, h->T1);
+        if (trc)
+            launch_tracer_stage(h->st, h->L1, h->P, torder, 3, h->ntr, h->rtr2, h->str2, h->rtr0, h->str0, h->rtr,
+                                h->str, h->rtr1, h->str1, h->u, h->w, h->du, h->dw, h->ds);
+        // ---- stage 4 ----
+        if (h->p.RK_update == 1) {
+            if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr1, h->str1, true)); }
+            TRY(smoother_time_T(h, h->T1));
+            TRY(update_velocities(h));
+            if (trc) derivs();
+        }
+        if (rat) stage_T(4, h->T1, h->T1);
+        if (trc)
+            launch_tracer_stage(h->st, h->L1, h->P, torder, 4, h->ntr, h->rtr1, h->str1, h->rtr0, h->str0, h->rtr,
+                                h->str, nullptr, nullptr, h->u, h->w, h->du, h->dw, h->ds);
+    }
+    // ---- wrap up ----
+    if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr, h->str, true)); }
+    TRY(smoother_time_T(h, h->T));
+    TRY(check_flags(h));
+    h->dt = h->hs->dt;
+    return TC_OK;
+}
+
+// stats (basics.f90:236-324)
+tc_status stats(Handle* h, tc_stats_row* row) {
+    std::memset(row, 0, sizeof(*row));
+    const double asp = h->p.aspect;
+    launch_strain(h->st, h->L1, h->P, h->u, h->w, h->strain);
+    launch_stats(h->st, h->L1, h->P, h->kent, h->T, h->u, h->w, h->conduct, cur_vis(h, 1), h->strain, h->Cnew,
+                 h->nempty, h->rows, h->ds);
+    TRY(sync_scalars(h));
+    const DevScalars& s = *h->hs;
+    if (h->p.comp == 1) {
+        for (int t = 0; t < h->ntype; t++) row->Cavg[t] = s.integ[t] / asp;
+        if (h->tstep == 0)
+            for (int t = 0; t < h->ntype; t++) h->mass[t] = row->Cavg[t];
+        for (int t = 0; t < h->ntype; t++) row->ent[t] = s.integ[4 + t] / asp / h->mass[t];
+        row->empty_cells = s.empty_cells;
+        row->tracer_min = s.nempty_min;
+        row->tracer_max = s.nempty_max;
+    }
+    row->vrms = std::pow(s.integ[8] / asp, 0.5);
+    row->mobility = std::pow(s.integ[11] / asp, 0.5) / row->vrms;
+    row->strain_max = s.strain_max;
+    if (h->p.RaT != 0.0) {
+        row->Tavg = s.integ[9] / asp;
+        row->RaT_avg = s.integ[10] / asp;
+        row->Nu = s.integ[12] / s.integ[13];
+        row->Nu_bot = s.integ[14] / asp;
+        row->q1 = s.integ[15]; row->q2 = s.integ[16]; row->q3 = s.integ[17]; row->q4 = s.integ[18];
+    }
+    row->time = h->time;
+    row->tstep = h->tstep;
+    row->n_eta = h->n_eta;
+    row->n_temp = h->n_temp;
+    row->eig_fine = h->eig_fine;
+    for (int t = 0; t < TC_MAX_TYPES; t++) row->n_comp[t] = h->n_comp[t];
+    return TC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// creation
+// ---------------------------------------------------------------------------
+tc_status create(Handle* h, const tc_params* in) {
+    h->p = *in;
+    tc_params& p = h->p;
+    if (p.order != 2) { h->err = "the GPU path implements order=2"; return TC_ERR_UNSUPPORTED; }
+    if (p.gridX != 0 || p.gridZ != 0) { h->err = "the GPU path implements uniform grids"; return TC_ERR_UNSUPPORTED; }
+    if (p.non_Newtonian != 0 || p.ivis == 3) { h->err = "the GPU path implements Newtonian viscosity"; return TC_ERR_UNSUPPORTED; }
+    if (p.iterate_order != 1) { h->err = "iterate_order must be 1"; return TC_ERR_UNSUPPORTED; }
+    if (p.RaT == 0.0) { h->err = "the GPU path implements thermal or thermochemical convection (RaT != 0)"; return TC_ERR_UNSUPPORTED; }
+    if (p.torder != 2 && p.torder != 4) return TC_ERR_UNSUPPORTED;
+    if (p.grids < 2 || p.grids > 6) return TC_ERR_ARG;
+    if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
+    if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
+    h->nx = p.nx; h->nz = p.nz; h->grids = p.grids;
+    {
+        const long nb = (long)((p.nx + 2 + BX - 1) / BX) * (long)((p.nz + 2 + BY - 1) / BY);
+        if (nb > TC_MAX_RED_BLOCKS) { h->err = "grid too large for the reduction scratch"; return TC_ERR_UNSUPPORTED; }
+    }
+    h->ntype = (p.comp == 1) ? p.ntype : 0;
+    // compute_smoothing_parameters (multigrid_cycle.f90:131-173)
+    if (p.ivis == 0 || p.RaT == 0.0) h->delta_T = 2.0;
+    else h->delta_T = (p.visT != 1.0) ? std::log(p.delta_visT) / std::log(p.visT) : 2.0;
+    for (int t = 0; t < TC_MAX_TYPES; t++) h->delta_C[t] = 2.0;
+    if (p.comp == 1) {
+        for (int t = 0; t < p.ntype; t++)
+            if (p.conduct_factor[t] != 1.0)
+                h->delta_C[t] = std::fabs(std::log(p.delta_visC[t]) / std::log(1.0 / p.conduct_factor[t]));
+        if (p.ivis == 2)
+            for (int t = 0; t < p.ntype; t++)
+                if (p.visC[t] != 1.0) h->delta_C[t] = std::fabs(std::log(p.delta_visC[t]) / std::log(p.visC[t]));
+    }
+    // multigrid_setup
+    tcs::optimize_grid(h->nx, h->nz, h->grids, p.mingrid);
+    std::vector<int> tab = tcs::cycle_table(h->grids);
+    if (tab.empty()) return TC_ERR_ARG;
+    h->nsteps = (int)tab.size();
+    h->multi.assign(h->nsteps + 2, 0);
+    for (int i = 0; i < h->nsteps; i++) h->multi[i + 1] = tab[i];
+    h->multi[0] = h->multi[h->nsteps];
+    h->multi[h->nsteps + 1] = h->multi[1];
+    const int nx = h->nx, nz = h->nz, G = h->grids;
+    for (int l = 1; l <= G; l++)
+        if ((nx >> (l - 1)) < 4 || (nz >> (l - 1)) < 4) { h->err = "grid too coarse for the level count"; return TC_ERR_ARG; }
+    // compute_basics
+    tcs::LevSpacing s1;
+    tcs::level_spacing(p.aspect, nx, nz, s1);
+    h->grid_dr = s1.dr; h->grid_ds = s1.ds;
+    h->ntr = (p.comp == 1) ? (int64_t)(nx + 1) * (nz + 1) * p.tpc : 0;
+    const int nxc = nx >> (G - 1), nzc = nz >> (G - 1);
+    h->ngrid_coarse = (nxc + 1) * (nzc + 1);
+    tcs::coarse_bandwidth(nxc, nzc, 2, 1, h->kl, h->ku);
+    // FD coefficients and eigenvalue bases
+    tcs::FD fd;
+    tcs::fd_coefficients(2, fd);
+    tcs::derivative_eigenvalues(fd, 1, h->eb);
+    // entrainment_setup (composition.f90:582-591), uniform zgrid
+    h->kent = 0;
+    for (int k = 0; k <= nz; k++)
+        if (s1.ds * (double)k <= p.dent) h->kent = k;
+    // ---- physics scalars ----
+    Phys& P = h->P;
+    P.nx = nx; P.nz = nz; P.ntype = h->ntype; P.comp = p.comp; P.ivis = p.ivis; P.Tbot = p.Tbot; P.Vbc = p.Vbc;
+    P.torder = p.torder; P.aspect = p.aspect; P.dr = s1.dr; P.ds = s1.ds; P.dr2 = s1.dr2; P.ds2 = s1.ds2;
+    P.dro2 = 0.5 * s1.dr; P.dso2 = 0.5 * s1.ds; P.RaT = p.RaT;
+    P.lnvisT = std::log(p.visT); P.lnvisP = std::log(p.visP); P.visT2 = p.visT * p.visT; P.H = p.H;
+    for (int t = 0; t < TC_MAX_TYPES; t++) {
+        P.RaC[t] = p.RaC[t]; P.lnvisC[t] = (p.visC[t] > 0.0) ? std::log(p.visC[t]) : 0.0; P.Htype[t] = p.Htype[t];
+        P.lncf[t] = (p.conduct_factor[t] > 0.0) ? std::log(1.0 / p.conduct_factor[t]) : 0.0;
+    }
+    P.courantT = p.courantT; P.courantC = p.courantC;
+    P.Tr_max = h->eb.Tr / s1.dr; P.Ts_max = h->eb.Tr / s1.ds;
+    P.Trr_max = -h->eb.Trr / s1.dr2; P.Tss_max = -h->eb.Trr / s1.ds2;
+    // ---- stream ----
+    cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return TC_ERR_CUDA; }
+    h->own_stream = true;
+    // ---- allocations ----
+    h->L1 = make_lay(nx, nz);
+    const size_t pl = h->L1.plane;
+    double** fine[] = {&h->T, &h->T0, &h->T1, &h->T2, &h->SF, &h->Tvis, &h->Tvis2, &h->Tbuoy, &h->u, &h->w,
+                       &h->du, &h->dw, &h->conduct, &h->conduct_r, &h->conduct_s, &h->dts, &h->strain};
+    for (double** q : fine) TRY(dalloc_t(h, q, pl));
+    for (int t = 0; t < h->ntype; t++) {
+        TRY(dalloc_t(h, &h->Cnew[t], pl)); TRY(dalloc_t(h, &h->C0[t], pl)); TRY(dalloc_t(h, &h->Cvis[t], pl));
+        TRY(dalloc_t(h, &h->Cvis2[t], pl)); TRY(dalloc_t(h, &h->Cbuoy[t], pl));
+    }
+    TRY(dalloc_t(h, &h->counts, pl * (size_t)(h->ntype + 1)));
+    TRY(dalloc_t(h, &h->nempty, pl));
+    TRY(dalloc_t(h, &h->zg, (size_t)nz + 1 + 2 * (SP + 1)));
+    if (h->ntr > 0) {
+        double** tr[] = {&h->rtr, &h->str, &h->rtr0, &h->str0, &h->rtr1, &h->str1, &h->rtr2, &h->str2};
+        for (double** q : tr) TRY(dalloc_t(h, q, (size_t)h->ntr));
+        TRY(dalloc_t(h, &h->ttype, (size_t)h->ntr));
+    }
+    const int ldab = 2 * h->kl + h->ku + 1;
+    TRY(dalloc_t(h, &h->band, (size_t)ldab * h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->rowb, (size_t)h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->bvec, (size_t)h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));
+    TRY(dalloc_t(h, &h->rs.part, (size_t)4 * TC_MAX_RED_BLOCKS));
+    TRY(dalloc_t(h, &h->rs.count, (size_t)8));
+    TRY(dalloc_t(h, &h->ds, (size_t)1));
+    e = cudaMallocHost((void**)&h->hs, sizeof(DevScalars));
+    if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return TC_ERR_ALLOC; }
+    std::memset(h->hs, 0, sizeof(DevScalars));
+    // ---- levels ----
+    const int odi[TC_NCOEF] = TC_OFFSETS_DI, odk[TC_NCOEF] = TC_OFFSETS_DK;
+    auto Dv = [&](const double* D, int j) { return (j < -3 || j > 3) ? 0.0 : D[j + 3]; };
+    for (int l = 1; l <= G; l++) {
+        Level& lv = h->lev[l];
+        lv.L = make_lay(nx >> (l - 1), nz >> (l - 1));
+        const size_t lp = lv.L.plane;
+        for (int q = 0; q < 2; q++) { TRY(dalloc_t(h, &lv.err[q], lp)); TRY(dalloc_t(h, &lv.vis[q], lp)); }
+        lv.ecur = 0; lv.vcur = 0;
+        double** lf[] = {&lv.vx, &lv.vz, &lv.vxx, &lv.vzz, &lv.vxz, &lv.dt_vis, &lv.dt_stream, &lv.ratio, &lv.rhs,
+                         &lv.res, &lv.cA, &lv.cB};
+        for (double** q : lf) TRY(dalloc_t(h, q, lp));
+        for (int q = 0; q < 6; q++) TRY(dalloc_t(h, &lv.bak[q], lp));
+        TRY(dalloc_t(h, &lv.coef, lp * TC_NCOEF));
+        tcs::LevSpacing s;
+        tcs::level_spacing(p.aspect, lv.L.a, lv.L.b, s);
+        LevConst& c = lv.c;
+        c.dr = s.dr; c.ds = s.ds; c.dr2 = s.dr2; c.ds2 = s.ds2; c.dr3 = s.dr3; c.ds3 = s.ds3; c.dr4 = s.dr4;
+        c.ds4 = s.ds4; c.drds = s.drds; c.drds2 = s.drds2; c.dr2ds = s.dr2ds; c.dr2ds2 = s.dr2ds2;
+        // scaled bounds (test_eigenvalues / iterate_local_time_steps preamble)
+        const double Ts = h->eb.Tr / s.ds, Tss = -h->eb.Trr / s.ds2, Tsss = h->eb.Trrr / s.ds3,
+                     Tssss = h->eb.Trrrr / s.ds4, Trr = -h->eb.Trr / s.dr2, Trrr = h->eb.Trrr / s.dr3,
+                     Trrrr = h->eb.Trrrr / s.dr4, Trs = -h->eb.Trs / s.drds, Trrss = h->eb.Trrss / s.dr2ds2,
+                     Trss = h->eb.Trrs / s.drds2, Trrs = h->eb.Trrs / s.dr2ds;
+        (void)Ts;
+        c.eK1 = Trr - Tss; c.eK2 = Trrrr + Tssss; c.eTrrss = Trrss; c.eTrs = Trs;
+        c.eK5 = Trrr + Trss; c.eK6 = Tsss + Trrs;
+        for (int d = 0; d < TC_NCOEF; d++) {
+            const int di = odi[d], dk = odk[d];
+            double Srr = 0, Sss = 0, Srrr = 0, Ssss = 0, Srrrr = 0, Sssss = 0;
+            if (dk == 0) { Srr = Dv(fd.D2, di) / s.dr2; Srrr = Dv(fd.D3, di) / s.dr3; Srrrr = Dv(fd.D4, di) / s.dr4; }
+            if (di == 0) { Sss = Dv(fd.D2, dk) / s.ds2; Ssss = Dv(fd.D3, dk) / s.ds3; Sssss = Dv(fd.D4, dk) / s.ds4; }
+            const bool in1 = (di >= -1 && di <= 1 && dk >= -1 && dk <= 1);
+            const double Srs = in1 ? (Dv(fd.D1, dk) * Dv(fd.D1, di)) / s.drds : 0.0;
+            const double Srss = in1 ? (Dv(fd.D2, dk) * Dv(fd.D1, di)) / s.drds2 : 0.0;
+            const double Srrs = in1 ? (Dv(fd.D1, dk) * Dv(fd.D2, di)) / s.dr2ds : 0.0;
+            const double Srrss = in1 ? (Dv(fd.D2, dk) * Dv(fd.D2, di)) / s.dr2ds2 : 0.0;
+            c.fold[d][0] = Srr - Sss;
+            c.fold[d][1] = Srrrr + Sssss;
+            c.fold[d][2] = Srrss;
+            c.fold[d][3] = Srs;
+            c.fold[d][4] = Srrr + Srss;
+            c.fold[d][5] = Ssss + Srrs;
+        }
+        // stability_vis_smoother (uniform: eI = 0)
+        {
+            const double Trr_l = -h->eb.Trr / s.dr2, Tss_l = -h->eb.Trr / s.ds2;
+            const double eR = std::fabs(Trr_l / 1.0) + std::fabs(Tss_l / 1.0);
+            const double eI = std::fabs(0.0 / 1.0) * (h->eb.Tr / s.dr) + std::fabs(0.0 / 1.0) * (h->eb.Tr / s.ds);
+            const double dtv = 2.0 * eR / (eR * eR + eI * eI);
+            std::vector<double> hv(lp, 0.0);
+            for (int i = 0; i <= lv.L.a; i++)
+                for (int k = 1; k <= lv.L.b - 1; k++) hv[IX(lv.L, i, k)] = dtv;
+            CK(cudaMemcpy(lv.dt_vis, hv.data(), lp * sizeof(double), cudaMemcpyHostToDevice));
+        }
+    }
+    // stability_RK4_smoother: dts_array
+    {
+        const double Tr_max = h->eb.Tr / s1.dr, Ts_max = h->eb.Tr / s1.ds;
+        const double Trr_max = -h->eb.Trr / s1.dr2, Tss_max = -h->eb.Trr / s1.ds2;
+        const double eR = std::fabs(Trr_max / 1.0) + std::fabs(Tss_max / 1.0);
+        const double eI = std::fabs(0.0 / 1.0) * Tr_max + std::fabs(0.0 / 1.0) * Ts_max;
+        const double v = 2.0 * eR / (eR * eR + eI * eI);
+        std::vector<double> hv(pl, 0.0);
+        for (int i = 0; i <= nx; i++)
+            for (int k = 0; k <= nz; k++) hv[IX(h->L1, i, k)] = v;
+        CK(cudaMemcpy(h->dts, hv.data(), pl * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    // zg (grid.f90:46-109, restart=0 coordinates, uniform)
+    {
+        std::vector<double> z((size_t)nz + 1 + 2 * (SP + 1));
+        auto Z = [&](int k) -> double& { return z[(size_t)(k + SP + 1)]; };
+        for (int k = 0; k <= nz; k++) Z(k) = s1.ds * (double)k;
+        for (int k = 1; k <= SP + 1; k++) { Z(-k) = -Z(k); Z(nz + k) = 1.0 - Z(nz - k) + 1.0; }
+        Z(0) = 0.0; Z(nz) = 1.0;
+        CK(cudaMemcpy(h->zg, z.data(), z.size() * sizeof(double), cudaMemcpyHostToDevice));
+        h->zg += SP + 1;  // kernels index zg[k], k >= -3
+    }
+    CK(cudaDeviceSynchronize());
+    return TC_OK;
+}
+
+// Fortran-layout (nx+5)x(nz+5) host array <-> padded device plane
+tc_status put_field(Handle* h, double* dev, const double* host) {
+    const size_t ni = (size_t)h->nx + 1 + 2 * SP, nk = (size_t)h->nz + 1 + 2 * SP;
+    CK(cudaMemcpy2DAsync(dev, h->L1.ld * sizeof(double), host, ni * sizeof(double), ni * sizeof(double), nk,
+                         cudaMemcpyHostToDevice, h->st));
+    return TC_OK;
+}
+tc_status get_field(Handle* h, double* host, const double* dev) {
+    const size_t ni = (size_t)h->nx + 1 + 2 * SP, nk = (size_t)h->nz + 1 + 2 * SP;
+    CK(cudaMemcpy2DAsync(host, ni * sizeof(double), dev, h->L1.ld * sizeof(double), ni * sizeof(double), nk,
+                         cudaMemcpyDeviceToHost, h->st));
+    return TC_OK;
+}
+
+tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF, const double* r, const double* s,
+                 const int32_t* tt, int64_t n) {
+    if (!T || !SF) return TC_ERR_ARG;
+    if (h->p.comp == 1 && (n != h->ntr || !r || !s || !tt)) return TC_ERR_ARG;
+    TRY(put_field(h, h->T, T));
+    TRY(put_field(h, h->SF, SF));
+    const size_t ni = (size_t)h->nx + 1 + 2 * SP, nk = (size_t)h->nz + 1 + 2 * SP;
+    std::vector<double> tmp;
+    for (int t = 0; t < h->ntype; t++) {
+        if (Cn) {
+            tmp.resize(ni * nk);
+            for (size_t x = 0; x < ni * nk; x++) tmp[x] = Cn[x * h->ntype + t];
+            TRY(put_field(h, h->Cnew[t], tmp.data()));
+            CK(cudaStreamSynchronize(h->st));
+        } else {
+            CK(cudaMemsetAsync(h->Cnew[t], 0, sizeof(double) * h->L1.plane, h->st));
+        }
+    }
+    if (h->p.comp == 1) {
+        CK(cudaMemcpyAsync(h->rtr, r, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->str, s, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->ttype, tt, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    }
+    CK(cudaMemsetAsync(h->ds, 0, sizeof(DevScalars), h->st));
+    launch_enforce_T(h->st, h->L1, h->T, h->p.Tbot);
+    launch_stream_bcs(h->st, h->lev[1], h->SF, h->p.Vbc);
+    for (int t = 0; t < h->ntype; t++) launch_enforce_comp(h->st, h->L1, h->Cnew[t], h->Cnew[t]);
+    for (int l = 2; l <= h->grids; l++)
+        for (int q = 0; q < 2; q++) CK(cudaMemsetAsync(h->lev[l].err[q], 0, sizeof(double) * h->lev[l].L.plane, h->st));
+    h->uploaded = true;
+    if (h->p.comp == 1) TRY(tracers_to_corners(h, h->rtr, h->str, false));
+    TRY(smoother_time_T(h, h->T));
+    if (h->p.comp != 0) TRY(smoother_time(h));
+    load_conductivity_array(h);
+    TRY(check_flags(h));
+    return TC_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+struct tc_handle {
+    Handle h;
+};
+
+extern "C" {
+
+void tc_default_params(tc_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->nx = 200; p->nz = 200; p->aspect = 1.0; p->order = 2;
+    p->gridX = 0; p->gridZ = 0; p->spaceX = 1.0; p->spaceZ = 1.0; p->thickness = 0.1; p->nbound = 8;
+    p->non_Newtonian = 0; p->iterate_order = 1; p->tolerance = 1.0e-3; p->Nmulti = 70; p->mingrid = 4;
+    p->grids = 2; p->eig_ratio = 4.0; p->vis_iter = 12; p->max_cycles = 1000;
+    p->torder = 4; p->courant = 0.99; p->courantT = 0.99; p->courantC = 0.99; p->courant_stream = 0.99;
+    p->RK_update = 1; p->dt_manual = 0.5;
+    p->comp = 1; p->ntype = 1; p->tpc = 30; p->dist_factor = 1.0e-4;
+    p->Tbot = 0; p->Vbc = 0; p->dlayer = 0.1; p->dent = 0.1;
+    p->RaT = 1.0e3 / 3.0; p->H = 0.0;
+    for (int t = 0; t < TC_MAX_TYPES; t++) {
+        p->RaC[t] = 0.0; p->conduct_factor[t] = 1.0; p->Htype[t] = 0.0; p->visC[t] = 1.0; p->delta_visC[t] = 2.0;
+    }
+    p->eig_ratio_min = 4.0; p->ivis = 2; p->visP = 1.0; p->visT = 3.0e4; p->delta_visT = 100.0;
+    p->yield = 15.0; p->yield_gradient = 0.0; p->yield_depth = 0.1;
+}
+
+void tc_abi_sizes(int32_t sizes[3]) {
+    sizes[0] = (int32_t)sizeof(tc_params);
+    sizes[1] = (int32_t)sizeof(tc_stats_row);
+    sizes[2] = (int32_t)sizeof(tc_info);
+}
+
+tc_status tc_create(const tc_params* p, tc_handle** out) {
+    if (!p || !out) return TC_ERR_ARG;
+    *out = nullptr;
+    tc_handle* H = new (std::nothrow) tc_handle();
+    if (!H) return TC_ERR_ALLOC;
+    tc_status s = create(&H->h, p);
+    if (s != TC_OK) {
+        static thread_local std::string last;
+        last = H->h.err;
+        tc_destroy(H);
+        return s;
+    }
+    *out = H;
+    return TC_OK;
+}
+
+tc_status tc_destroy(tc_handle* H) {
+    if (!H) return TC_OK;
+    Handle* h = &H->h;
+    if (h->st) cudaStreamSynchronize(h->st);
+    for (void* q : h->allocs) cudaFree(q);
+    if (h->hs) cudaFreeHost(h->hs);
+    if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+    delete H;
+    return TC_OK;
+}
+
+tc_status tc_get_info(const tc_handle* H, tc_info* info) {
+    if (!H || !info) return TC_ERR_ARG;
+    const Handle* h = &H->h;
+    std::memset(info, 0, sizeof(*info));
+    info->nx = h->nx; info->nz = h->nz; info->span = SP; info->span_interp = 1; info->grids = h->grids;
+    info->nsteps = h->nsteps; info->ntr = h->ntr; info->ngrid_coarse = h->ngrid_coarse; info->kl = h->kl;
+    info->ku = h->ku;
+    for (int l = 1; l <= h->grids && l <= 8; l++) { info->nx_grid[l - 1] = h->lev[l].L.a; info->nz_grid[l - 1] = h->lev[l].L.b; }
+    info->dr = h->grid_dr; info->ds = h->grid_ds;
+    return TC_OK;
+}
+
+tc_status tc_set_stream(tc_handle* H, void* stream) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (h->st) cudaStreamSynchronize(h->st);
+    if (h->own_stream && h->st) cudaStreamDestroy(h->st);
+    h->own_stream = false;
+    h->st = (cudaStream_t)stream;
+    return TC_OK;
+}
+
+tc_status tc_upload_state(tc_handle* H, const double* T, const double* Cnew, const double* SF, const double* rtr,
+                          const double* str, const int32_t* Ttype, int64_t ntr) {
+    if (!H) return TC_ERR_ARG;
+    return upload(&H->h, T, Cnew, SF, rtr, str, Ttype, ntr);
+}
+
+tc_status tc_download_state(tc_handle* H, double* T, double* Cnew, double* SF, double* rtr, double* str,
+                            int32_t* Ttype) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (T) TRY(get_field(h, T, h->T));
+    if (SF) TRY(get_field(h, SF, h->SF));
+    if (Cnew && h->ntype > 0) {
+        const size_t ni = (size_t)h->nx + 1 + 2 * SP, nk = (size_t)h->nz + 1 + 2 * SP;
+        std::vector<double> tmp(ni * nk);
+        for (int t = 0; t < h->ntype; t++) {
+            TRY(get_field(h, tmp.data(), h->Cnew[t]));
+            CK(cudaStreamSynchronize(h->st));
+            for (size_t x = 0; x < ni * nk; x++) Cnew[x * h->ntype + t] = tmp[x];
+        }
+    }
+    if (h->p.comp == 1) {
+        if (rtr) CK(cudaMemcpyAsync(rtr, h->rtr, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
+        if (str) CK(cudaMemcpyAsync(str, h->str, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
+        if (Ttype) CK(cudaMemcpyAsync(Ttype, h->ttype, sizeof(int32_t) * h->ntr, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
+}
+
+tc_status tc_set_clock(tc_handle* H, int32_t tstep, double time) {
+    if (!H) return TC_ERR_ARG;
+    H->h.tstep = tstep;
+    H->h.time = time;
+    return TC_OK;
+}
+
+tc_status tc_multigrid(tc_handle* H, int32_t* cycles_out) {
+    if (!H) return TC_ERR_ARG;
+    tc_status s = multigrid(&H->h);
+    if (cycles_out) *cycles_out = H->h.last_cycles;
+    return s;
+}
+
+tc_status tc_compute_velocities(tc_handle* H) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    compute_velocities(h);
+    CK(cudaGetLastError());
+    return TC_OK;
+}
+
+tc_status tc_stats(tc_handle* H, tc_stats_row* row) {
+    if (!H || !row) return TC_ERR_ARG;
+    return stats(&H->h, row);
+}
+
+tc_status tc_energy_time(tc_handle* H, double* dt_out) {
+    if (!H) return TC_ERR_ARG;
+    tc_status s = energy_time(&H->h);
+    if (dt_out) *dt_out = H->h.dt;
+    return s;
+}
+
+tc_status tc_step(tc_handle* H, tc_stats_row* row, int32_t* cycles, double* dt_out) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    tc_status s = multigrid(h);
+    if (cycles) *cycles = h->last_cycles;
+    if (s != TC_OK) return s;
+    compute_velocities(h);
+    tc_stats_row tmp;
+    TRY(stats(h, row ? row : &tmp));
+    TRY(energy_time(h));
+    if (dt_out) *dt_out = h->dt;
+    h->time = h->time + h->dt;
+    h->tstep += 1;
+    return TC_OK;
+}
+
+tc_status tc_download_velocities(tc_handle* H, double* u, double* w) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    // (-1:nx+1, -1:nz+1) sub-box of the padded plane
+    const size_t ni = (size_t)h->nx + 3, nk = (size_t)h->nz + 3;
+    const size_t off = IX(h->L1, -1, -1);
+    if (u) CK(cudaMemcpy2DAsync(u, ni * sizeof(double), h->u + off, h->L1.ld * sizeof(double), ni * sizeof(double), nk,
+                                cudaMemcpyDeviceToHost, h->st));
+    if (w) CK(cudaMemcpy2DAsync(w, ni * sizeof(double), h->w + off, h->L1.ld * sizeof(double), ni * sizeof(double), nk,
+                                cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
+}
+
+tc_status tc_tracers_to_corners(tc_handle* H, const double* rtr, const double* str) {
+    if (!H || !rtr || !str) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (h->p.comp != 1) return TC_ERR_UNSUPPORTED;
+    CK(cudaMemcpyAsync(h->rtr2, rtr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->str2, str, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    TRY(tracers_to_corners(h, h->rtr2, h->str2, true));
+    return check_flags(h);
+}
+
+tc_status tc_download_counts(tc_handle* H, int32_t* count_type) {
+    if (!H || !count_type) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    const int nt = h->ntype + 1;
+    std::vector<int> hv(h->L1.plane * (size_t)nt);
+    CK(cudaMemcpyAsync(hv.data(), h->counts, hv.size() * sizeof(int), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    const int ni = h->nx + 1 + 2 * SP, nk = h->nz + 1 + 2 * SP;
+    for (int kk = 0; kk < nk; kk++)
+        for (int ii = 0; ii < ni; ii++)
+            for (int t = 0; t < nt; t++)
+                count_type[((size_t)kk * ni + ii) * nt + t] = hv[(size_t)t * h->L1.plane + (size_t)ii + (size_t)kk * h->L1.ld];
+    return TC_OK;
+}
+
+tc_status tc_debug_field(tc_handle* H, const char* name, int32_t level, int32_t type, double* out) {
+    if (!H || !name || !out) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    std::string n(name);
+    const double* src = nullptr;
+    Lay L = h->L1;
+    auto ty = [&](double* const* a) -> const double* { return (type >= 1 && type <= h->ntype) ? a[type - 1] : nullptr; };
+    if (level >= 1 && level <= h->grids) {
+        Level& lv = h->lev[level];
+        if (n == "vis_grid") src = lv.vis[lv.vcur];
+        else if (n == "vis_x") src = lv.vx;
+        else if (n == "vis_z") src = lv.vz;
+        else if (n == "vis_xx") src = lv.vxx;
+        else if (n == "vis_zz") src = lv.vzz;
+        else if (n == "vis_xz") src = lv.vxz;
+        else if (n == "dt_stream") src = lv.dt_stream;
+        else if (n == "ratio") src = lv.ratio;
+        else if (n == "RHS") src = lv.rhs;
+        else if (n == "error") src = lv.err[lv.ecur];
+        else if (n == "residual") src = lv.res;
+        else if (n == "dt_vis") src = lv.dt_vis;
+        if (src) L = lv.L;
+    }
+    if (!src) {
+        if (n == "T") src = h->T;
+        else if (n == "SF") src = h->SF;
+        else if (n == "Tvis") src = h->Tvis;
+        else if (n == "Tbuoy") src = h->Tbuoy;
+        else if (n == "u") src = h->u;
+        else if (n == "w") src = h->w;
+        else if (n == "conduct") src = h->conduct;
+        else if (n == "conduct_r") src = h->conduct_r;
+        else if (n == "conduct_s") src = h->conduct_s;
+        else if (n == "DERr_u") src = h->du;
+        else if (n == "DERr_w") src = h->dw;
+        else if (n == "dts_array") src = h->dts;
+        else if (n == "Cnew") src = ty(h->Cnew);
+        else if (n == "Cvis") src = ty(h->Cvis);
+        else if (n == "Cbuoy") src = ty(h->Cbuoy);
+    }
+    if (!src) return TC_ERR_ARG;
+    const size_t ni = (size_t)L.a + 1 + 2 * SP, nk = (size_t)L.b + 1 + 2 * SP;
+    CK(cudaMemcpy2DAsync(out, ni * sizeof(double), src, L.ld * sizeof(double), ni * sizeof(double), nk,
+                         cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
+}
+
+const char* tc_last_error(const tc_handle* H) {
+    if (!H) return "";
+    return H->h.err.c_str();
+}
+
+}  // extern "C"

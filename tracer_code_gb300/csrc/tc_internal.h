@@ -1,0 +1,162 @@
+// tc_internal.h -- device state layout and kernel launchers of the GB300 path.
+//
+// Layout in HBM.  Every field of multigrid level l (1 = finest) is a 2-D FP64
+// array over the ghost-padded index box (-SP:nx_l+SP, -SP:nz_l+SP), SP=2
+// (span of the order-2 stencils), stored column-major with i fastest and the
+// row length padded to a multiple of 32 doubles (256 B) so every k-row starts
+// on an L2-sector boundary:  addr(i,k) = (i+SP) + (k+SP)*ld.  Arrays that the
+// reference declares with a smaller box (interior-only coefficients, u/w with
+// span_interp=1, DERr with i in 0:nx) use the same mapping, so one index
+// function serves every kernel.  Tracer arrays are flat FP64/int32 vectors in
+// reference id order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "tracer_gpu.h"
+
+#define SP 2
+#define TC_MAXLEV 6
+#define TC_NCOEF 13
+#define TC_MAX_RED_BLOCKS 8192
+
+// 13-point stencil offsets used by the folded operator, in this order.
+#define TC_OFFSETS_DI {0, -1, 1, -2, 2, 0, 0, 0, 0, -1, 1, -1, 1}
+#define TC_OFFSETS_DK {0, 0, 0, 0, 0, -1, 1, -2, 2, -1, -1, 1, 1}
+
+struct Lay {
+    int a, b;     // nx_l, nz_l
+    int ld, nk;   // padded row length, number of rows (b+1+2SP)
+    size_t plane; // ld*nk
+};
+
+#ifdef __CUDACC__
+__host__ __device__ __forceinline__
+#else
+inline
+#endif
+size_t IX(const Lay& L, int i, int k) { return (size_t)(i + SP) + (size_t)(k + SP) * (size_t)L.ld; }
+
+// Per-level constants (grid spacings and scaled eigenvalue bounds).
+struct LevConst {
+    double dr, ds, dr2, ds2, dr3, ds3, dr4, ds4, drds, drds2, dr2ds, dr2ds2;
+    // eigR constants: K1 = Trr-Tss, K2 = Trrrr+Tssss, Trrss, Trs ; eigI: K5 = Trrr+Trss, K6 = Tsss+Trrs
+    double eK1, eK2, eTrrss, eTrs, eK5, eK6;
+    // folded-operator basis: for each offset d, (Srr-Sss, Srrrr+Sssss, Srrss, Srs, Srrr+Srss, Ssss+Srrs)
+    double fold[TC_NCOEF][6];
+    double dtvis_scale;  // unused placeholder
+};
+
+// Scalars that kernels produce and the host reads back.
+struct DevScalars {
+    double ratio_min;
+    double diff;
+    double res_mag[TC_MAXLEV + 1];
+    double res_ref;
+    double dt;
+    double eA_max, eD_max;
+    double integ[32];
+    double strain_max;
+    int    nempty_min, nempty_max, empty_cells;
+    int    flag_outside;     // tracer outside the domain
+    int    flag_rk2;         // RK2 precondition failed
+    int    lu_info;          // first zero pivot of the coarse LU (0 = none)
+    int    pad[2];
+};
+
+// Reduction scratch: per-block partials plus a completion counter.
+struct RedScratch {
+    double* part;         // [4][TC_MAX_RED_BLOCKS]
+    unsigned int* count;  // [8]
+};
+
+struct Level {
+    Lay L;
+    double* err[2];
+    int ecur;
+    double* vis[2];
+    int vcur;
+    double *vx, *vz, *vxx, *vzz, *vxz;
+    double* bak[6];  // saved vis, vx, vz, vxx, vzz, vxz (compute_viscosity)
+    double *dt_vis, *dt_stream, *ratio, *rhs, *res;
+    double* coef;    // TC_NCOEF planes
+    double *cA, *cB; // Chebyshev denominators for the level with finite eigenvalue ratios
+    LevConst c;
+};
+
+// Host-side scalars of the physics configuration, passed by value to kernels.
+struct Phys {
+    int nx, nz, ntype, comp, ivis, Tbot, Vbc, torder;
+    double aspect, dr, ds, dr2, ds2, dro2, dso2;
+    double RaT, RaC[TC_MAX_TYPES], lnvisT, lnvisP, lnvisC[TC_MAX_TYPES], visT2, H, Htype[TC_MAX_TYPES];
+    double lncf[TC_MAX_TYPES];   // log(1/conduct_factor)
+    double courantT, courantC;
+    double Tr_max, Ts_max, Trr_max, Tss_max;  // stability_RK4 scaled bounds (finest grid)
+};
+
+// ---------------------------------------------------------------------------
+// launchers (k_mg.cu)
+// ---------------------------------------------------------------------------
+void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis, const double* Tvis,
+                        const double* const* Cvis, const double* zg);
+void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_eig, int ivis, RedScratch rs,
+                     DevScalars* ds);
+void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
+                       int kmax, int RaT_nonzero, double visT2);
+void launch_restrict_vis(cudaStream_t s, const Level& coarse, const Level& fine, const double* vfine, double* vcoarse);
+void launch_vis_bcs_init(cudaStream_t s, const Level& coarse, double* v, int RaT_nonzero, double visT2);
+void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int ivis, double courant_stream,
+                        int cheb_level);
+void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
+                  int per_point, double temp, int Vbc);
+void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out);
+void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c);
+void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc);
+void launch_stream_bcs(cudaStream_t s, const Level& lv, double* S, int Vbc);
+void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* rowb, int kl, int ku, int Vbc);
+void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, int ku, DevScalars* ds);
+void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                         int n, int kl, int ku, double* bvec, double* err, int Vbc);
+void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n);
+void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
+                 double* rhs, RedScratch rs, DevScalars* ds);
+
+// ---------------------------------------------------------------------------
+// launchers (k_field.cu)
+// ---------------------------------------------------------------------------
+void launch_enforce_T(cudaStream_t s, const Lay& L, double* T, int Tbot);
+void launch_enforce_comp(cudaStream_t s, const Lay& L, double* C, const double* Cprev_ghosts);
+void launch_smoothness(cudaStream_t s, const Lay& L, const double* f, RedScratch rs, DevScalars* ds);
+void launch_smooth_T_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Tin, double* Tout,
+                          const double* dts);
+void launch_smooth_C_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Cin, double* Cout,
+                          const double* dts, double c);
+void launch_conductivity(cudaStream_t s, const Lay& L, const Phys& P, const double* const* Cvis, double* conduct,
+                         double* conduct_r, double* conduct_s);
+void launch_velocities(cudaStream_t s, const Lay& L, const Phys& P, const double* SF, double* u, double* w);
+void launch_derivatives(cudaStream_t s, const Lay& L, const Phys& P, const double* f, double* der);
+void launch_stability(cudaStream_t s, const Lay& L, const Phys& P, const double* conduct, const double* conduct_r,
+                      const double* conduct_s, const double* u, const double* w, double courant, double dt_manual,
+                      RedScratch rs, DevScalars* ds);
+void launch_energy_stage(cudaStream_t s, const Lay& L, const Phys& P, int stage, const double* Tin,
+                         const double* T0, double* T, double* Tout, const double* conduct, const double* conduct_r,
+                         const double* conduct_s, const double* u, const double* w, const double* const* Cvis,
+                         const DevScalars* ds);
+void launch_strain(cudaStream_t s, const Lay& L, const Phys& P, const double* u, const double* w, double* strain);
+void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const double* T, const double* u,
+                  const double* w, const double* conduct, const double* vis, const double* strain,
+                  const double* const* Cnew, const int* nempty, double* rows, DevScalars* ds);
+
+// ---------------------------------------------------------------------------
+// launchers (k_tracer.cu)
+// ---------------------------------------------------------------------------
+void launch_tracer_stage(cudaStream_t s, const Lay& L, const Phys& P, int torder, int stage, int64_t ntr,
+                         const double* rin, const double* sin, const double* r0, const double* s0, double* racc,
+                         double* sacc, double* rout, double* sout, const double* u, const double* w,
+                         const double* du, const double* dw, const DevScalars* ds);
+void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* r, const double* sv,
+                      const int* ttype, int* counts, DevScalars* ds);
+void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* counts, int* nempty,
+                           double* const* Cnew);
