@@ -1,0 +1,341 @@
+"""Benchmark: timesteps/s of the per-timestep hot path at 1024x256 cells with
+25 tracers per cell (6,585,625 tracers), multigrid to 1e-8 relative residual.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One step = one pass of the reference main loop body (main.f90:181-204):
+multigrid, compute_velocities, stats, energy_time (RK4: three more multigrid
+solves, four tracer RK stages, four tracer-ratio composition passes).
+
+ours: W untimed steps, then K steps timed with CUDA events on the library's
+stream (barrier + synchronize on both sides, max over ranks).  N>1 runs N
+independent replicas (one case per GPU; the path does not shard).  Inputs
+are larger than L2 (the tracer state alone is 6.6M x 8 FP64 arrays).
+Prints one JSON line (rank 0) with the contract keys plus roofline,
+cpu_baseline, e2e, clocks and gpu_launches.
+
+reference: the CPU restatement of the reference (oracle/, OpenMP on all host
+cores) on the same workload; each step is a bounded sample (two multigrid
+calls capped at 1 and 2 W-cycles, one RK step without re-solves, one
+tracer-ratio pass) from which the full timestep time is assembled with the
+workload's cycle count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "timesteps/s 1024x256 grid, 6.5M tracers: learned+mixed vs plain MG @ 1e-8 resid"
+UNIT = "timesteps/s"
+# Average W-cycles per timestep (4 solves) of this workload, measured on the
+# GPU arm over its first steps (same algorithm, same tolerance); used only to
+# assemble the CPU reference arm's timestep from its bounded sample when it
+# runs without the GPU arm in the same process.
+CYCLES_PER_STEP_DEFAULT = 228.0
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the level-1
+# smoother kernel (profiles/k_sweep_1024x256.md); None until captured.
+SWEEP_DRAM_BYTES = None
+
+
+def workload_params():
+    from tracer_code_gb300 import config_1024x256
+    p = config_1024x256()
+    p.mg_zero_coarse = 1
+    return p
+
+
+def workload_desc(p) -> dict:
+    ntr = (p.nx + 1) * (p.nz + 1) * p.tpc
+    return {
+        "workload": f"{p.nx}x{p.nz} cells, aspect {p.aspect:g}, {p.tpc} tracers/cell ({ntr:,} tracers), "
+                    f"Ra={p.RaT:g}, B={p.RaC[0] / p.RaT:g}, dense layer z<{p.dlayer:g}, "
+                    f"eta=exp(-ln({p.visT:g})T)*10 in enriched, RK4, FP64 multigrid {p.grids} levels to {p.tolerance:g}",
+        "grid": f"{p.nx}x{p.nz}",
+        "tracers": ntr,
+        "solver": "plain FP64 multigrid (W-cycle, Chebyshev-Richardson smoother, banded LU coarse solve), "
+                  "coarse corrections restart from zero (mg_zero_coarse=1)",
+        "l2": "inputs larger than L2 (tracer state 6.6M x 8 FP64 arrays = 421 MB)",
+        "parallelism": "replicas (one independent case per GPU)",
+    }
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{index}.csv") if os.path.isdir(
+            os.path.join(ROOT, "gpurun_out")) else f"/tmp/tc_clocks_{os.getpid()}_{index}.csv"
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self) -> dict:
+        try:
+            rows = [l.strip().split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            rows = []
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_sample(p, threads: int, cycles_per_step: float, seed: int = 1) -> dict:
+    """Bounded sample of the CPU restatement on the full workload; returns the
+    assembled timestep time and its parts."""
+    from oracle.pyoracle import Oracle
+    from tracer_code_gb300 import TracerError, state
+    st = state.initial_state(p, seed=seed)
+    q = p.copy()
+    times = {}
+    for cap in (1, 2):
+        q.max_cycles = cap
+        o2 = Oracle(q, threads=threads)
+        o2.upload(st)
+        t0 = time.perf_counter()
+        try:
+            o2.multigrid()
+        except TracerError as e:
+            if e.status != 3:
+                raise
+        times[cap] = time.perf_counter() - t0
+        if cap == 2:
+            o2.compute_velocities()
+            qq = q.copy()
+            qq.RK_update = 0
+            o3 = Oracle(qq, threads=threads)
+            o3.upload(st)
+            o3.set("SF", o2.download()["SF"])
+            o3.compute_velocities()
+            t0 = time.perf_counter()
+            o3.energy_time()
+            times["rk_step_no_resolve"] = time.perf_counter() - t0
+            r = o3.download()
+            t0 = time.perf_counter()
+            o3.tracers_to_corners(r["rtr"], r["str"])
+            times["tracers_to_corners"] = time.perf_counter() - t0
+            o3.close()
+        o2.close()
+    per_cycle = max(times[2] - times[1], 1e-9)
+    fixed = max(times[1] - per_cycle, 0.0)
+    step = 4 * fixed + cycles_per_step * per_cycle + times["rk_step_no_resolve"] + 3 * times["tracers_to_corners"]
+    return {"step_s": step, "per_cycle_s": per_cycle, "per_solve_fixed_s": fixed,
+            "rk_step_no_resolve_s": times["rk_step_no_resolve"], "tracers_to_corners_s": times["tracers_to_corners"],
+            "sample_s": sum(v for v in times.values())}
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    p = workload_params()
+    threads = os.cpu_count() or 1
+    samples = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_sample(p, threads, CYCLES_PER_STEP_DEFAULT)
+        if i >= args.warmup:
+            samples.append(r)
+    step_s = statistics.mean(r["step_s"] for r in samples)
+    value = 1.0 / step_s
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_desc(p),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"per step: CPU restatement multigrid capped at 1 and 2 W-cycles, one RK4 step "
+                                   f"without re-solves, one tracer-ratio pass; timestep assembled as "
+                                   f"4*fixed + {CYCLES_PER_STEP_DEFAULT:g} cycles + RK + 3 ratio passes",
+                         "parts": samples[-1]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int, local_rank: int):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from tracer_code_gb300 import Simulation, state
+
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream()
+    p = workload_params()
+    sim = Simulation(p, stream=stream.cuda_stream)
+    st = state.initial_state(p, seed=1 + rank)
+    sim.upload(st)
+    cycles = []
+    for _ in range(args.warmup):
+        _, q, _ = sim.step()
+        cycles.append(q)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    n0 = Simulation.kernel_launches()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    solves = []
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            _, q, _ = sim.step()
+            solves.append(q)
+        e1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = Simulation.kernel_launches() - n0
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * args.steps / (ms_max * 1e-3)
+    cycles_per_step = statistics.mean(solves)
+    # dominant kernel: level-1 smoother sweep, timed live on the same stream
+    sweep_ms = sim.time_sweep(1, 70)
+    ni, nk = p.nx - 1, p.nz - 1
+    alg_bytes = 88.0 * ni * nk
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    peak, src = peaks()
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SWEEP_DRAM_BYTES, "kernel": "k_sweep (level 1, 1023x255 points)",
+            "kernel_ms": sweep_ms, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured"
+            else "fallback 6.8 TB/s",
+            "note": "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s"}
+    # end to end: the same steps through tc_step_host with pinned host state
+    host = {}
+    dl = sim.download()
+    for key in ("T", "SF", "Cnew", "rtr", "str", "Ttype"):
+        a = dl[key]
+        pt = torch.empty(a.shape, dtype=torch.float64 if a.dtype == np.float64 else torch.int32).pin_memory()
+        host[key] = pt.numpy()
+        host[key][...] = a
+    h2d = sum(host[k].nbytes for k in ("T", "SF", "Cnew", "rtr", "str", "Ttype"))
+    d2h = sum(host[k].nbytes for k in ("T", "SF", "Cnew", "rtr", "str"))
+    k_e2e = max(1, min(args.steps, 3))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(k_e2e):
+        sim.step_host(host)
+    torch.cuda.synchronize()
+    te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(te, op=dist.ReduceOp.MAX)
+    e2e_value = world * k_e2e / float(te.item())
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded conductive T + uniform tracers)",
+            "config": dict(workload_desc(p), cycles_per_step=solves, warmup_cycles_per_step=cycles,
+                           tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc)),
+            "roofline": roof,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "steps": k_e2e, "api": "tc_step_host (C ABI, pinned host arrays)"},
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        if not args.no_cpu_baseline:
+            cps = float(cycles_per_step)
+            r = cpu_sample(p, os.cpu_count() or 1, cps)
+            line["cpu_baseline"] = {"value": 1.0 / r["step_s"], "unit": UNIT, "cores": os.cpu_count() or 1,
+                                    "kind": "port",
+                                    "sample": f"CPU restatement, full workload: multigrid capped at 1 and 2 W-cycles, "
+                                              f"one RK4 step without re-solves, one tracer-ratio pass "
+                                              f"({r['sample_s']:.1f} s); timestep = 4*fixed + {cps:g} cycles + RK "
+                                              f"+ 3 ratio passes",
+                                    "parts": r}
+        print(json.dumps(line), flush=True)
+    sim.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-solve", action="store_true",
+                    help="profiling case: upload the workload, run one multigrid solve, exit")
+    args = ap.parse_args()
+    if args.profile_solve:
+        from tracer_code_gb300 import Simulation, state
+        p = workload_params()
+        sim = Simulation(p)
+        sim.upload(state.initial_state(p, seed=1))
+        n0 = Simulation.kernel_launches()
+        q = sim.multigrid()
+        print(json.dumps({"profile_solve": True, "cycles": q, "launches_before_solve": n0,
+                          "launches_in_solve": Simulation.kernel_launches() - n0}), flush=True)
+        sim.close()
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -193,8 +193,28 @@ tc_status tc_stats(tc_handle* h, tc_stats_row* row);
 tc_status tc_energy_time(tc_handle* h, double* dt_out);
 
 /* One pass of the main.f90:174-205 loop body: multigrid, compute_velocities,
- * stats, energy_time, time += dt, tstep += 1.  row and cycles may be NULL. */
+ * stats, energy_time, time += dt, tstep += 1.  *cycles receives the W-cycles
+ * of all multigrid solves of the step (the main solve and the RK re-solves).
+ * row, cycles and dt_out may be NULL. */
 tc_status tc_step(tc_handle* h, tc_stats_row* row, int32_t* cycles, double* dt_out);
+
+/* One main-loop step with the state in HOST arrays (the drop-in for a host
+ * that keeps the reference's module arrays): copies T, Cnew, SF, rtr, str,
+ * Ttype in, runs tc_step, copies T, Cnew, SF, rtr, str back.  The arrays
+ * must hold the state the previous call (or tc_download_state) returned;
+ * after changing them, call tc_upload_state instead.  Any of row, cycles,
+ * dt_out may be NULL.  No counterpart in the reference beyond tc_step. */
+tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double* rtr, double* str,
+                       const int32_t* Ttype, int64_t ntr, tc_stats_row* row, int32_t* cycles, double* dt_out);
+
+/* Diagnostics (no counterpart in the reference).  tc_time_sweep times
+ * `nsweeps` back-to-back launches of the multigrid smoother kernel of `level`
+ * with CUDA events on the handle's stream (state left unchanged) and writes
+ * the mean milliseconds per launch.  tc_kernel_launches returns how many
+ * kernels this library has launched in the process so far (graph replays
+ * count every kernel node). */
+tc_status tc_time_sweep(tc_handle* h, int32_t level, int32_t nsweeps, double* ms_per_sweep);
+int64_t tc_kernel_launches(void);
 
 /* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */
 tc_status tc_download_velocities(tc_handle* h, double* u, double* w);

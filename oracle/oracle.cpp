@@ -1390,6 +1390,7 @@ struct Oracle {
         }
     }
     int last_cycles = 0;
+    int cycles_acc = 0;
     // multigrid (iterative_solver.f90:79-173)
     int multigrid() {
         int st;
@@ -1454,6 +1455,7 @@ struct Oracle {
         }
         SF = error[1];
         last_cycles = q;
+        cycles_acc += q;
         return TC_OK;
     }
 
@@ -1984,6 +1986,7 @@ int tco_energy_time(void* h, double* dt) {
 }
 int tco_step(void* h, tc_stats_row* row, int32_t* cycles, double* dt_out) {
     Oracle* o = (Oracle*)h;
+    o->cycles_acc = 0;
     int st = o->multigrid();
     if (cycles) *cycles = o->last_cycles;
     if (st) return st;
@@ -1991,6 +1994,7 @@ int tco_step(void* h, tc_stats_row* row, int32_t* cycles, double* dt_out) {
     tc_stats_row tmp;
     o->stats(row ? row : &tmp);
     st = o->energy_time();
+    if (cycles) *cycles = o->cycles_acc;
     if (st) return st;
     if (dt_out) *dt_out = o->dt;
     o->time = o->time + o->dt;

@@ -31,7 +31,7 @@ EXPORTS = [
     "tc_default_params", "tc_abi_sizes", "tc_create", "tc_destroy", "tc_get_info", "tc_set_stream",
     "tc_upload_state", "tc_download_state", "tc_set_clock", "tc_multigrid", "tc_compute_velocities", "tc_stats",
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
-    "tc_last_error", "tc_debug_field",
+    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_kernel_launches",
 ]
 
 
@@ -74,6 +74,11 @@ def load_library(build_if_missing: bool = False):
         L.tc_tracers_to_corners.argtypes = [vp, vp, vp]
         L.tc_download_counts.argtypes = [vp, vp]
         L.tc_debug_field.argtypes = [vp, C.c_char_p, C.c_int32, C.c_int32, vp]
+        L.tc_step_host.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, C.POINTER(StatsRow),
+                                   C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+        L.tc_time_sweep.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
+        L.tc_kernel_launches.argtypes = []
+        L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]
         L.tc_last_error.restype = C.c_char_p
         for name in EXPORTS:
@@ -206,6 +211,25 @@ class Simulation:
         row = StatsRow(); q = C.c_int32(0); dt = C.c_double(0)
         self._chk(self.L.tc_step(self.h, C.byref(row), C.byref(q), C.byref(dt)), "step")
         return row.as_dict(), q.value, dt.value
+
+    def step_host(self, st: dict):
+        """tc_step_host on host arrays (pinned for end-to-end timing); st is
+        updated in place and must hold the state the previous call returned."""
+        row = StatsRow(); q = C.c_int32(0); dt = C.c_double(0)
+        n = 0 if st.get("rtr") is None else st["rtr"].size
+        self._chk(self.L.tc_step_host(self.h, _ptr(st["T"]), _ptr(st.get("Cnew")), _ptr(st["SF"]),
+                                      _ptr(st.get("rtr")), _ptr(st.get("str")), _ptr(st.get("Ttype")), n,
+                                      C.byref(row), C.byref(q), C.byref(dt)), "step_host")
+        return row.as_dict(), q.value, dt.value
+
+    def time_sweep(self, level: int = 1, nsweeps: int = 70) -> float:
+        ms = C.c_double(0)
+        self._chk(self.L.tc_time_sweep(self.h, level, nsweeps, C.byref(ms)), "time_sweep")
+        return ms.value
+
+    @staticmethod
+    def kernel_launches() -> int:
+        return int(load_library().tc_kernel_launches())
 
     def velocities(self):
         shp = (self.nz + 3, self.nx + 3)

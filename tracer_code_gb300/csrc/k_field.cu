@@ -34,7 +34,7 @@ __global__ void k_enforce_T(Lay L, Range2 r, double* __restrict__ T, int Tbot) {
 }
 void launch_enforce_T(cudaStream_t s, const Lay& L, double* T, int Tbot) {
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
-    k_enforce_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, T, Tbot);
+    k_enforce_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, T, Tbot); tc_note_launch();
 }
 
 // enforceBCs_comp (composition.f90:792-803).  Its four statements share one
@@ -65,7 +65,7 @@ __global__ void k_enforce_comp(Lay L, Range2 r, double* C, const double* Cprev) 
 }
 void launch_enforce_comp(cudaStream_t s, const Lay& L, double* C, const double* Cprev_ghosts) {
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
-    k_enforce_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, C, Cprev_ghosts ? Cprev_ghosts : C);
+    k_enforce_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, C, Cprev_ghosts ? Cprev_ghosts : C); tc_note_launch();
 }
 
 // smoothness (multigrid_cycle.f90:175-195): largest jump to the five
@@ -86,7 +86,7 @@ __global__ void k_smoothness(Lay L, Range2 r, const double* __restrict__ T, RedS
 }
 void launch_smoothness(cudaStream_t s, const Lay& L, const double* f, RedScratch rs, DevScalars* ds) {
     Range2 r{0, L.a - 1, 1, L.b - 1};
-    k_smoothness<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, f, rs, &ds->diff);
+    k_smoothness<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, f, rs, &ds->diff); tc_note_launch();
 }
 
 __device__ __forceinline__ double lap5(const double* __restrict__ T, size_t x, size_t ld, double dr2, double ds2) {
@@ -109,7 +109,7 @@ __global__ void k_smooth_T(Lay L, Phys P, Range2 r, const double* __restrict__ T
 void launch_smooth_T_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Tin, double* Tout,
                           const double* dts) {
     Range2 r{0, L.a, 0, L.b};
-    k_smooth_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tin, Tout, dts);
+    k_smooth_T<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tin, Tout, dts); tc_note_launch();
 }
 
 // one step of smoother_time (smoother.f90:287-341) for one type
@@ -128,7 +128,7 @@ __global__ void k_smooth_C(Lay L, Phys P, Range2 r, const double* __restrict__ C
 void launch_smooth_C_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Cin, double* Cout,
                           const double* dts, double c) {
     Range2 r{0, L.a, 0, L.b};
-    k_smooth_C<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Cin, Cout, dts, c);
+    k_smooth_C<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Cin, Cout, dts, c); tc_note_launch();
 }
 
 // load_conductivity_array (energy.f90:31-58)
@@ -157,9 +157,9 @@ void launch_conductivity(cudaStream_t s, const Lay& L, const Phys& P, const doub
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
-    k_conduct<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, C, conduct);
+    k_conduct<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, C, conduct); tc_note_launch();
     Range2 r2{-1, L.a + 1, -1, L.b + 1};
-    k_conduct_grad<<<grid_for(r2), dim3(BX, BY), 0, s>>>(L, P, r2, conduct, conduct_r, conduct_s);
+    k_conduct_grad<<<grid_for(r2), dim3(BX, BY), 0, s>>>(L, P, r2, conduct, conduct_r, conduct_s); tc_note_launch();
 }
 
 // compute_velocities + velocityBCs (momentum.f90:532-551, composition.f90:806-836),
@@ -209,7 +209,7 @@ __global__ void k_velocities(Lay L, Phys P, Range2 r, const double* __restrict__
 }
 void launch_velocities(cudaStream_t s, const Lay& L, const Phys& P, const double* SF, double* u, double* w) {
     Range2 r{-1, L.a + 1, -1, L.b + 1};
-    k_velocities<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, SF, u, w);
+    k_velocities<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, SF, u, w); tc_note_launch();
 }
 
 // compute_derivatives (composition.f90:900-919), order=2
@@ -221,7 +221,7 @@ __global__ void k_derivatives(Lay L, Phys P, Range2 r, const double* __restrict_
 }
 void launch_derivatives(cudaStream_t s, const Lay& L, const Phys& P, const double* f, double* der) {
     Range2 r{0, L.a, -1, L.b + 1};
-    k_derivatives<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, f, der);
+    k_derivatives<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, f, der); tc_note_launch();
 }
 
 // stability_RK4 (energy.f90:600-646), tracer=0 branch of eigA
@@ -268,10 +268,10 @@ void launch_stability(cudaStream_t s, const Lay& L, const Phys& P, const double*
                       RedScratch rs, DevScalars* ds) {
     Range2 r{0, L.a, 0, L.b};
     if (P.RaT != 0.0) {
-        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eA_max, 0);
-        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eD_max, 1);
+        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eA_max, 0); tc_note_launch();
+        k_stab<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, conduct, conduct_r, conduct_s, u, w, rs, &ds->eD_max, 1); tc_note_launch();
     }
-    k_dt<<<1, 1, 0, s>>>(P, ds, courant, dt_manual);
+    k_dt<<<1, 1, 0, s>>>(P, ds, courant, dt_manual); tc_note_launch();
 }
 
 // energy_space (energy.f90:60-80) and the four RK stage updates of energy_time
@@ -320,7 +320,7 @@ void launch_energy_stage(cudaStream_t s, const Lay& L, const Phys& P, int stage,
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
     Range2 r{0, L.a, 0, L.b};
     k_energy<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, stage, Tin, T0, T, Tout, conduct, conduct_r, conduct_s, u,
-                                                   w, C, ds);
+                                                   w, C, ds); tc_note_launch();
 }
 
 // compute_strain_rate_invariant (momentum.f90:32-62), interior nodes
@@ -339,7 +339,7 @@ __global__ void k_strain(Lay L, Phys P, Range2 r, const double* __restrict__ u, 
 }
 void launch_strain(cudaStream_t s, const Lay& L, const Phys& P, const double* u, const double* w, double* strain) {
     Range2 r{0, L.a, 0, L.b};
-    k_strain<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, u, w, strain);
+    k_strain<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, u, w, strain); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -465,11 +465,11 @@ void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const d
                   const double* const* Cnew, const int* nempty, double* rows, DevScalars* ds) {
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
-    k_stats_rows<<<(L.b + 1 + 63) / 64, 64, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows);
-    k_stats_final<<<1, 32, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds);
+    k_stats_rows<<<(L.b + 1 + 63) / 64, 64, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows); tc_note_launch();
+    k_stats_final<<<1, 32, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds); tc_note_launch();
     if (P.comp == 1) {
         Range2 r{0, L.a, 0, L.b};
-        k_nempty_init<<<1, 1, 0, s>>>(ds);
-        k_nempty_stats<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, nempty, ds);
+        k_nempty_init<<<1, 1, 0, s>>>(ds); tc_note_launch();
+        k_nempty_stats<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, nempty, ds); tc_note_launch();
     }
 }

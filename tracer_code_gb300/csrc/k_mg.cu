@@ -45,7 +45,7 @@ void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
-    k_visf1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, vis, Tvis, C, zg);
+    k_visf1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, vis, Tvis, C, zg); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -96,7 +96,7 @@ void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_
                      DevScalars* ds) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_vis_grad<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
-                                                     lv.ratio, do_eig, ivis, rs, &ds->ratio_min);
+                                                     lv.ratio, do_eig, ivis, rs, &ds->ratio_min); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -135,7 +135,7 @@ __global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restr
 void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
                        int kmax, int RaT_nonzero, double visT2) {
     Range2 r{0, lv.L.a, kmin, kmax};
-    k_vis_smooth<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vin, vout, lv.dt_vis, c, RaT_nonzero, visT2);
+    k_vis_smooth<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vin, vout, lv.dt_vis, c, RaT_nonzero, visT2); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -161,7 +161,7 @@ __global__ void k_restrict_vis(Lay C, Lay F, Range2 r, const double* __restrict_
 }
 void launch_restrict_vis(cudaStream_t s, const Level& coarse, const Level& fine, const double* vfine, double* vcoarse) {
     Range2 r{0, coarse.L.a, 0, coarse.L.b};
-    k_restrict_vis<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, vfine, vcoarse);
+    k_restrict_vis<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, vfine, vcoarse); tc_note_launch();
 }
 
 // ghosts of viscosityBCs_initialize computed from their mirror sources
@@ -184,7 +184,7 @@ __global__ void k_vis_bcs_init(Lay L, Range2 r, double* __restrict__ V, int RaTn
 }
 void launch_vis_bcs_init(cudaStream_t s, const Level& coarse, double* v, int RaT_nonzero, double visT2) {
     Range2 r{-SP, coarse.L.a + SP, -SP, coarse.L.b + SP};
-    k_vis_bcs_init<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, r, v, RaT_nonzero, visT2);
+    k_vis_bcs_init<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, r, v, RaT_nonzero, visT2); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -227,7 +227,7 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_level_coefs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
                                                         lv.ratio, lv.dt_stream, lv.coef, lv.cA, lv.cB,
-                                                        courant_stream, cheb_level);
+                                                        courant_stream, cheb_level); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -289,7 +289,7 @@ void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* So
                   int per_point, double temp, int Vbc) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_sweep<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
-                                                  c_uniform, per_point, temp, Vbc);
+                                                  c_uniform, per_point, temp, Vbc); tc_note_launch();
 }
 
 __global__ void k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
@@ -308,7 +308,7 @@ __global__ void k_residual(Lay L, Range2 r, const double* __restrict__ S, const 
 void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_residual<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef, lv.rhs, lv.res, rs, res_out,
-                                                     (double)(lv.L.a - 1), (double)(lv.L.b - 1));
+                                                     (double)(lv.L.a - 1), (double)(lv.L.b - 1)); tc_note_launch();
 }
 
 __global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc) {
@@ -318,7 +318,7 @@ __global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict_
 }
 void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c) {
     Range2 r{1, coarse.L.a - 1, 1, coarse.L.b - 1};
-    k_restrict_res<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c);
+    k_restrict_res<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
 }
 
 // prolong (bilinear, additive) with the fine level's stream BCs fused
@@ -338,7 +338,7 @@ __global__ void k_prolong(Lay C, Lay F, Range2 r, const double* __restrict__ ec,
 }
 void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc) {
     Range2 r{1, fine.L.a - 1, 1, fine.L.b - 1};
-    k_prolong<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc);
+    k_prolong<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
 }
 
 // enforceBCs_stream: walls zero, ghosts mirrored from the interior
@@ -359,7 +359,7 @@ __global__ void k_stream_bcs(Lay L, Range2 r, double* __restrict__ S, int Vbc) {
 }
 void launch_stream_bcs(cudaStream_t s, const Level& lv, double* S, int Vbc) {
     Range2 r{-SP, lv.L.a + SP, -SP, lv.L.b + SP};
-    k_stream_bcs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, Vbc);
+    k_stream_bcs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, Vbc); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -418,7 +418,7 @@ __global__ void k_coarse_build(Lay L, const double* __restrict__ coef, double* _
 void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* rowb, int kl, int ku, int Vbc) {
     int n = (lv.L.a + 1) * (lv.L.b + 1);
     cudaMemsetAsync(band, 0, sizeof(double) * (size_t)(2 * kl + ku + 1) * n, s);
-    k_coarse_build<<<(n + 127) / 128, 128, 0, s>>>(lv.L, lv.coef, band, rowb, n, kl, ku, Vbc);
+    k_coarse_build<<<(n + 127) / 128, 128, 0, s>>>(lv.L, lv.coef, band, rowb, n, kl, ku, Vbc); tc_note_launch();
 }
 
 // dgbtf2 on one CTA.  The band lives in shared memory when it fits.
@@ -500,7 +500,7 @@ void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, in
     int in_smem = bytes <= 200 * 1024 ? 1 : 0;
     size_t sm = in_smem ? bytes : 0;
     if (in_smem) cudaFuncSetAttribute(k_coarse_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info);
+    k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info); tc_note_launch();
 }
 
 // Compute_coarse_vector + DGBTRS + Stream_grid_coarse + enforceBCs_stream
@@ -583,7 +583,7 @@ void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, co
     int in_smem = bytes <= 200 * 1024 ? 1 : 0;
     size_t sm = in_smem ? bytes : 0;
     if (in_smem) cudaFuncSetAttribute(k_coarse_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_coarse_solve<<<1, 512, sm, s>>>(lv.L, band, ipiv, rowb, lv.rhs, n, kl, ku, in_smem, bvec, err, Vbc);
+    k_coarse_solve<<<1, 512, sm, s>>>(lv.L, band, ipiv, rowb, lv.rhs, n, kl, ku, in_smem, bvec, err, Vbc); tc_note_launch();
 }
 
 __global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
@@ -594,7 +594,7 @@ __global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src,
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n) {
     int nb = (int)((n + 255) / 256);
     if (nb > 1216) nb = 1216;
-    k_copy<<<nb, 256, 0, s>>>(dst, src, n);
+    k_copy<<<nb, 256, 0, s>>>(dst, src, n); tc_note_launch();
 }
 
 // compute_RHS(1) and compute_reference_residual(1)
@@ -625,5 +625,5 @@ void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuo
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cbuoy[j];
     k_rhs1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tbuoy, C, rhs, rs, &ds->res_ref, (double)(L.a - 2),
-                                                 (double)(L.b - 2));
+                                                 (double)(L.b - 2)); tc_note_launch();
 }

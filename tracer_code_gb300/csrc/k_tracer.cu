@@ -100,7 +100,7 @@ void launch_tracer_stage(cudaStream_t s, const Lay& L, const Phys& P, int torder
     if (ntr <= 0) return;
     unsigned nb = (unsigned)((ntr + 255) / 256);
     k_tracer_stage<<<nb, 256, 0, s>>>(L, P, torder, stage, ntr, rin, sin, r0, s0, racc, sacc, rout, sout, u, w, du,
-                                      dw, ds);
+                                      dw, ds); tc_note_launch();
 }
 
 // histogram of tracers_to_corners (composition.f90:695-726): nint() rounds
@@ -132,7 +132,7 @@ void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, 
     cudaMemsetAsync(counts, 0, sizeof(int) * L.plane * (size_t)(P.ntype + 1), s);
     if (ntr <= 0) return;
     unsigned nb = (unsigned)((ntr + 255) / 256);
-    k_histogram<<<nb, 256, 0, s>>>(L, P, ntr, r, sv, ttype, counts, &ds->flag_outside);
+    k_histogram<<<nb, 256, 0, s>>>(L, P, ntr, r, sv, ttype, counts, &ds->flag_outside); tc_note_launch();
 }
 
 // ghost mirror of count_type, nempty and the tracer ratio (composition.f90:745-776)
@@ -170,5 +170,5 @@ void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* cou
     CPtrsW C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
-    k_counts_to_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, counts, nempty, C);
+    k_counts_to_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, counts, nempty, C); tc_note_launch();
 }

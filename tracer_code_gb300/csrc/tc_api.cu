@@ -19,10 +19,16 @@
 #include <string>
 #include <vector>
 
+#include <atomic>
+
+static std::atomic<long long> g_launches{0};
+void tc_note_launch(long long n) { g_launches.fetch_add(n); }
+
 namespace {
 
 const double kPi = 3.1415926535897932;
 
+struct CycleGraphs;
 struct Handle {
     tc_params p{};
     int nx = 0, nz = 0, grids = 0, nsteps = 0, ntype = 0;
@@ -72,6 +78,9 @@ struct Handle {
     int last_cycles = 0;
     long loop_cap = 100000;
     std::string err;
+    CycleGraphs* graphs = nullptr;
+    bool no_graphs = false;
+    int cycles_acc = 0;  // W-cycles of all solves since tc_step began
 };
 
 #define CK(call)                                                      \
@@ -326,8 +335,60 @@ void iterate_stream(Handle* h, int level, int dir) {
         launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], c, per_point, temp, h->p.Vbc);
         lv.ecur = 1 - lv.ecur;
     }
+    if (Niter % 2 == 1) {
+        // keep the level's current buffer fixed across visits (graph replay relies on it)
+        launch_copy_plane(h->st, lv.err[1 - lv.ecur], lv.err[lv.ecur], lv.L.plane);
+        lv.ecur = 1 - lv.ecur;
+    }
     launch_residual(h->st, lv, lv.err[lv.ecur], h->rs, &h->ds->res_mag[level]);
 }
+
+// Work of one multigrid cycle after the level-1 visit (p = 2..nsteps);
+// no host synchronisation inside, so it can be captured in a CUDA graph.
+void enqueue_cycle_rest(Handle* h) {
+    const int G = h->grids;
+    for (int pp = 2; pp <= h->nsteps; pp++) {
+        const int level = h->multi[pp];
+        const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
+        if (h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse)
+            cudaMemsetAsync(cur_err(h, level), 0, sizeof(double) * h->lev[level].L.plane, h->st);
+        if (h->multi[pp - 1] < h->multi[pp] && level > 1)
+            launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs);
+        if (level < G) {
+            iterate_stream(h, level, dir);
+        } else {
+            launch_coarse_solve(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku, h->bvec,
+                                cur_err(h, G), h->p.Vbc);
+        }
+        if (h->multi[pp + 1] < h->multi[pp])
+            launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
+                           h->p.Vbc);
+    }
+}
+
+// Graph of a replayable sequence; rebuilt when the inputs it bakes in change.
+struct CycleGraphs {
+    cudaGraphExec_t l1 = nullptr, rest = nullptr;
+    long long n_l1 = 0, n_rest = 0;  // kernel nodes per graph
+    int ratio_level = -1, zero = -1, dir1 = -1;
+    cudaStream_t st = nullptr;
+};
+
+tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int arg, long long* nkernels) {
+    cudaGraph_t g = nullptr;
+    const long long before = g_launches.load();
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    fn(h, arg);
+    CK(cudaStreamEndCapture(h->st, &g));
+    *nkernels = g_launches.load() - before;
+    g_launches.fetch_sub(*nkernels);  // capturing enqueues nothing
+    cudaError_t e = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) { h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return TC_ERR_CUDA; }
+    return TC_OK;
+}
+void enqueue_l1(Handle* h, int dir) { iterate_stream(h, 1, dir); }
+void enqueue_rest(Handle* h, int) { enqueue_cycle_rest(h); }
 
 // multigrid (iterative_solver.f90:79-173), Newtonian branch
 tc_status multigrid(Handle* h) {
@@ -346,39 +407,39 @@ tc_status multigrid(Handle* h) {
     TRY(sync_scalars(h));
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     const double res_ref1 = h->hs->res_ref;
+    // p=1 is the only level-1 visit of every cycle table; the convergence test
+    // follows it, then p=2..nsteps run unconditionally.
+    const int dir1 = (h->multi[2] > h->multi[1]) ? 0 : 1;
+    CycleGraphs& cg = *h->graphs;
+    const bool use_graphs = (h->st != nullptr) && !h->no_graphs;
+    if (use_graphs && (cg.l1 == nullptr || cg.ratio_level != h->ratio_level || cg.zero != h->p.mg_zero_coarse ||
+                       cg.dir1 != dir1 || cg.st != h->st)) {
+        if (cg.l1) cudaGraphExecDestroy(cg.l1);
+        if (cg.rest) cudaGraphExecDestroy(cg.rest);
+        cg.l1 = cg.rest = nullptr;
+        TRY(capture(h, &cg.l1, enqueue_l1, dir1, &cg.n_l1));
+        TRY(capture(h, &cg.rest, enqueue_rest, 0, &cg.n_rest));
+        cg.ratio_level = h->ratio_level;
+        cg.zero = h->p.mg_zero_coarse;
+        cg.dir1 = dir1;
+        cg.st = h->st;
+    }
     int q = 1;
     for (;;) {
-        bool conv = false;
-        for (int pp = 1; pp <= h->nsteps; pp++) {
-            const int level = h->multi[pp];
-            const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
-            if (h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse)
-                CK(cudaMemsetAsync(cur_err(h, level), 0, sizeof(double) * h->lev[level].L.plane, h->st));
-            if (h->multi[pp - 1] < h->multi[pp] && level > 1)
-                launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs);
-            if (level < G) {
-                iterate_stream(h, level, dir);
-            } else {
-                Level& lv = h->lev[G];
-                launch_coarse_solve(h->st, lv, h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku, h->bvec,
-                                    cur_err(h, G), h->p.Vbc);
-            }
-            if (level == 1) {
-                TRY(sync_scalars(h));
-                const double rm = h->hs->res_mag[1];
-                if (rm > 1.0e10 * res_ref1) return TC_ERR_MG_RESIDUAL;
-                if (rm / res_ref1 <= h->p.tolerance) { conv = true; break; }
-            }
-            if (h->multi[pp + 1] < h->multi[pp])
-                launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
-                               h->p.Vbc);
-        }
-        if (conv) break;
+        if (use_graphs) { CK(cudaGraphLaunch(cg.l1, h->st)); tc_note_launch(cg.n_l1); }
+        else iterate_stream(h, 1, dir1);
+        TRY(sync_scalars(h));
+        const double rm = h->hs->res_mag[1];
+        if (rm > 1.0e10 * res_ref1) return TC_ERR_MG_RESIDUAL;
+        if (rm / res_ref1 <= h->p.tolerance) break;
+        if (use_graphs) { CK(cudaGraphLaunch(cg.rest, h->st)); tc_note_launch(cg.n_rest); }
+        else enqueue_cycle_rest(h);
         q = q + 1;
         if (q > h->p.max_cycles) { h->last_cycles = q; return TC_ERR_MG_CYCLES; }
     }
     copy_plane(h, h->SF, cur_err(h, 1));
     h->last_cycles = q;
+    h->cycles_acc += q;
     return TC_OK;
 }
 
@@ -584,6 +645,8 @@ tc_status create(Handle* h, const tc_params* in) {
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return TC_ERR_CUDA; }
     h->own_stream = true;
+    h->graphs = new CycleGraphs();
+    h->no_graphs = (std::getenv("TC_NO_GRAPHS") != nullptr);
     // ---- allocations ----
     h->L1 = make_lay(nx, nz);
     const size_t pl = h->L1.plane;
@@ -806,6 +869,11 @@ tc_status tc_destroy(tc_handle* H) {
     if (h->st) cudaStreamSynchronize(h->st);
     for (void* q : h->allocs) cudaFree(q);
     if (h->hs) cudaFreeHost(h->hs);
+    if (h->graphs) {
+        if (h->graphs->l1) cudaGraphExecDestroy(h->graphs->l1);
+        if (h->graphs->rest) cudaGraphExecDestroy(h->graphs->rest);
+        delete h->graphs;
+    }
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     delete H;
     return TC_OK;
@@ -900,18 +968,74 @@ tc_status tc_energy_time(tc_handle* H, double* dt_out) {
 tc_status tc_step(tc_handle* H, tc_stats_row* row, int32_t* cycles, double* dt_out) {
     if (!H) return TC_ERR_ARG;
     Handle* h = &H->h;
+    h->cycles_acc = 0;
     tc_status s = multigrid(h);
     if (cycles) *cycles = h->last_cycles;
     if (s != TC_OK) return s;
     compute_velocities(h);
     tc_stats_row tmp;
     TRY(stats(h, row ? row : &tmp));
-    TRY(energy_time(h));
+    s = energy_time(h);
+    if (cycles) *cycles = h->cycles_acc;
+    if (s != TC_OK) return s;
     if (dt_out) *dt_out = h->dt;
     h->time = h->time + h->dt;
     h->tstep += 1;
     return TC_OK;
 }
+
+tc_status tc_step_host(tc_handle* H, double* T, double* Cnew, double* SF, double* rtr, double* str,
+                       const int32_t* Ttype, int64_t ntr, tc_stats_row* row, int32_t* cycles, double* dt_out) {
+    if (!H || !T || !SF) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    if (h->p.comp == 1 && (ntr != h->ntr || !rtr || !str || !Ttype || !Cnew)) return TC_ERR_ARG;
+    TRY(put_field(h, h->T, T));
+    TRY(put_field(h, h->SF, SF));
+    if (h->ntype == 1) TRY(put_field(h, h->Cnew[0], Cnew));
+    if (h->p.comp == 1) {
+        CK(cudaMemcpyAsync(h->rtr, rtr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->str, str, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        CK(cudaMemcpyAsync(h->ttype, Ttype, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    }
+    tc_status s = tc_step(H, row, cycles, dt_out);
+    if (s != TC_OK) return s;
+    TRY(get_field(h, T, h->T));
+    TRY(get_field(h, SF, h->SF));
+    if (h->ntype == 1) TRY(get_field(h, Cnew, h->Cnew[0]));
+    if (h->p.comp == 1) {
+        CK(cudaMemcpyAsync(rtr, h->rtr, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
+        CK(cudaMemcpyAsync(str, h->str, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
+    }
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
+}
+
+tc_status tc_time_sweep(tc_handle* H, int32_t level, int32_t nsweeps, double* ms_per_sweep) {
+    if (!H || !ms_per_sweep || nsweeps < 1) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (level < 1 || level >= h->grids) return TC_ERR_ARG;
+    Level& lv = h->lev[level];
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    // sweeps read lv.err[cur] and write the other buffer; the state is untouched
+    double* in = lv.err[lv.ecur];
+    double* out = lv.err[1 - lv.ecur];
+    launch_sweep(h->st, lv, in, out, 1.0, 0, 0.0, h->p.Vbc);
+    CK(cudaEventRecord(e0, h->st));
+    for (int n = 0; n < nsweeps; n++) launch_sweep(h->st, lv, in, out, 1.0, 0, 0.0, h->p.Vbc);
+    CK(cudaEventRecord(e1, h->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_sweep = (double)ms / nsweeps;
+    return TC_OK;
+}
+
+int64_t tc_kernel_launches(void) { return (int64_t)g_launches.load(); }
 
 tc_status tc_download_velocities(tc_handle* H, double* u, double* w) {
     if (!H) return TC_ERR_ARG;

@@ -91,6 +91,9 @@ __device__ __forceinline__ void reduce_to(int op, double v, double* part, unsign
     }
 }
 
+// Host-side count of kernels this library enqueues (tc_kernel_launches).
+void tc_note_launch(long long n = 1);
+
 struct CPtrs {
     const double* p[TC_MAX_TYPES];
 };
