@@ -58,7 +58,8 @@ typedef enum tc_status {
     TC_ERR_CUDA = 8,             /* a CUDA runtime error; see tc_last_error()               */
     TC_ERR_ALLOC = 9,            /* device or host allocation failed                        */
     TC_ERR_STATE = 10,           /* call order violated (e.g. step before upload)           */
-    TC_ERR_SINGULAR = 11         /* zero pivot in the coarsest-grid banded LU (DGBTRF INFO>0) */
+    TC_ERR_SINGULAR = 11,        /* zero pivot in the coarsest-grid banded LU (DGBTRF INFO>0) */
+    TC_ERR_TOO_LARGE = 12        /* input larger than the fixed buffer of an allocation-free call */
 } tc_status;
 
 /*
@@ -240,6 +241,31 @@ tc_status tc_debug_field(tc_handle* h, const char* name, int32_t level, int32_t 
 /* sizeof(tc_params), sizeof(tc_stats_row), sizeof(tc_info) as compiled, so a
  * binding can check its struct layouts. */
 void tc_abi_sizes(int32_t sizes[3]);
+
+/* Allocation-free stats.dat row (no counterpart in the reference: it exists
+ * for hosts that cannot let a library allocate device memory, e.g. an
+ * OpenACC / CUDA Fortran port of the reference that owns every device array
+ * in its own pool, or an application under a fixed device-memory budget;
+ * such a host cannot create a tc_handle, which allocates).  Computes the
+ * same row as tc_stats (basics.f90:236-324) from device arrays the caller
+ * owns, in the reference's layouts: T, conduct, vis (vis_grid of level 1)
+ * and nempty on (-2:nx+2, -2:nz+2); u, w on (-1:nx+1, -1:nz+1); Cnew on
+ * (1:ntype, -2:nx+2, -2:nz+2).  Uniform grid, order 2.  kent and mass
+ * (host array, may be NULL: ent = 0) are the entrainment inputs of stats;
+ * time, tstep and the smoother counters of the row are left 0.  Work is
+ * issued on `stream` (a cudaStream_t, NULL = legacy default) and the call
+ * returns after it finished.
+ * It calls no cudaMalloc/cudaFree: its scratch is one fixed device array of
+ * 229,712 bytes that every GPU loading this library holds until exit, which
+ * limits nz to TC_NOALLOC_MAX_NZ (larger nz returns TC_ERR_TOO_LARGE).  The
+ * first call on a device looks up that array's device address (with the
+ * device current) and should come before any stream capture on it.  All
+ * calls share the array: calls whose work overlaps on the GPU race. */
+#define TC_NOALLOC_MAX_NZ 4096
+tc_status tc_stats_noalloc(const double* T, const double* u, const double* w, const double* conduct,
+                           const double* vis, const double* Cnew, const int32_t* nempty, int32_t nx, int32_t nz,
+                           int32_t ntype, double aspect, double RaT, int32_t kent, const double* mass,
+                           tc_stats_row* row, void* stream);
 
 /* Text of the last CUDA error seen by the handle ("" if none). */
 const char* tc_last_error(const tc_handle* h);

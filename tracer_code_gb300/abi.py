@@ -23,6 +23,7 @@ STATUS = {
     9: "TC_ERR_ALLOC",
     10: "TC_ERR_STATE",
     11: "TC_ERR_SINGULAR",
+    12: "TC_ERR_TOO_LARGE",
 }
 
 # Reference `stop` messages that each status replaces.
