@@ -150,6 +150,28 @@ def test_full_steps_parity(gpu_lib):
     assert np.abs(a["str"] - b["str"]).max() <= 1e-10
 
 
+@pytest.mark.parametrize("zero", [0, 1])
+def test_fused_cluster_visits_match_per_sweep_launches(gpu_lib, zero, monkeypatch):
+    """Small levels smoothed by one thread-block-cluster launch per visit give
+    the same multigrid state bit for bit as one launch per sweep."""
+    p = case_1024_like()
+    p.mg_zero_coarse = zero
+    st = fresh_state(p)
+    out = []
+    for env in (None, "1"):
+        if env:
+            monkeypatch.setenv("TC_NO_FUSED_VISITS", env)
+        g = Simulation(p)
+        g.upload(st)
+        q = g.multigrid()
+        out.append((q, g.download()["SF"], [g.get("error", l) for l in range(2, g.info.grids)]))
+        g.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    for a, b in zip(out[0][2], out[1][2]):
+        assert np.array_equal(a, b)
+
+
 def test_fault_tracer_outside_domain(gpu_lib):
     p = case_128_like()
     st = fresh_state(p)

@@ -503,87 +503,93 @@ void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, in
     k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info); tc_note_launch();
 }
 
-// Compute_coarse_vector + DGBTRS + Stream_grid_coarse + enforceBCs_stream
-__global__ void k_coarse_solve(Lay L, const double* __restrict__ ABg, const int* __restrict__ ipiv,
-                               const double* __restrict__ rowb, const double* __restrict__ rhs, int n, int kl, int ku,
-                               int in_smem, double* __restrict__ Bg, double* __restrict__ err, int Vbc) {
+// Explicit inverse of the factored coarse matrix: column j of A^-1 is the
+// DGBTRS solve (row interchanges + L solve, then dtbsv) of the unit vector
+// e_j.  One warp per column; the band is staged in shared memory when it
+// fits.  Stored row-major (Ainv[p*n + q]) for the coalesced products below.
+__global__ void k_coarse_inverse(const double* __restrict__ ABg, const int* __restrict__ ipiv_g, int n, int kl,
+                                 int ku, int in_smem, double* __restrict__ Ainv, double* __restrict__ Bscratch) {
     extern __shared__ double sm[];
     const int ldab = 2 * kl + ku + 1, KD = ku + kl + 1, K = kl + ku;
     const size_t tot = (size_t)ldab * n;
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nth >> 5;
     const double* AB = in_smem ? sm : ABg;
-    double* B = in_smem ? (sm + tot) : Bg;
-    const int tid = threadIdx.x, nth = blockDim.x;
-    if (in_smem)
+    int* ipv = (int*)(sm + (in_smem ? tot : 0));
+    double* Bw = in_smem ? (double*)(ipv + ((n + 1) & ~1)) + (size_t)warp * n : Bscratch + ((size_t)blockIdx.x * nw + warp) * n;
+    if (in_smem) {
         for (size_t t = tid; t < tot; t += nth) sm[t] = ABg[t];
-    const int nxc = L.a, nzc = L.b, N = nzc + 1;
-    for (int pp = 1 + tid; pp <= n; pp += nth) {
-        int kp = pp - N * ((pp - 1) / N) - 1, ip = (pp - 1) / N;
-        double v = 0.0;
-        if (ip >= 1 && ip <= nxc - 1 && kp >= 1 && kp <= nzc - 1) v = rhs[IX(L, ip, kp)] * rowb[pp - 1];
-        B[pp - 1] = v;
+        for (int t = tid; t < n; t += nth) ipv[t] = ipiv_g[t];
     }
     __syncthreads();
+    const int* piv = in_smem ? ipv : ipiv_g;
+    const int j = blockIdx.x * nw + warp + 1;  // column of A^-1 (1-based)
+    if (j > n) return;
 #define A_(rw, cl) AB[(size_t)((rw) - 1) + (size_t)((cl) - 1) * ldab]
-    if (tid < 32) {
-        // L solve with row interchanges
-        if (kl > 0)
-            for (int j = 1; j <= n - 1; j++) {
-                int LM = min(kl, n - j);
-                int Lr = ipiv[j - 1];
-                if (Lr != j) {
-                    if (tid == 0) { double t0 = B[Lr - 1]; B[Lr - 1] = B[j - 1]; B[j - 1] = t0; }
-                    __syncwarp();
-                }
-                double temp = -B[j - 1];
-                if (temp != 0.0)
-                    for (int t = 1 + tid; t <= LM; t += 32) B[j + t - 1] = B[j + t - 1] + A_(KD + t, j) * temp;
-                __syncwarp();
-            }
-        // dtbsv: upper, no transpose, non-unit
-        for (int j = n; j >= 1; j--) {
-            double bj = B[j - 1];
-            if (bj != 0.0) {
-                int Lc = K + 1 - j;
-                double temp = bj / A_(K + 1, j);
-                __syncwarp();
-                if (tid == 0) B[j - 1] = temp;
-                for (int i = j - 1 - tid; i >= max(1, j - K); i -= 32) B[i - 1] = B[i - 1] - temp * A_(Lc + i, j);
-            }
+    for (int t = lane; t < n; t += 32) Bw[t] = (t == j - 1) ? 1.0 : 0.0;
+    __syncwarp();
+    for (int jj = 1; jj <= n - 1; jj++) {
+        const int LM = min(kl, n - jj);
+        const int Lr = piv[jj - 1];
+        if (Lr != jj) {
+            if (lane == 0) { double t0 = Bw[Lr - 1]; Bw[Lr - 1] = Bw[jj - 1]; Bw[jj - 1] = t0; }
             __syncwarp();
         }
+        const double temp = -Bw[jj - 1];
+        if (temp != 0.0)
+            for (int t = 1 + lane; t <= LM; t += 32) Bw[jj + t - 1] = Bw[jj + t - 1] + A_(KD + t, jj) * temp;
+        __syncwarp();
+    }
+    for (int jj = n; jj >= 1; jj--) {
+        const double bj = Bw[jj - 1];
+        if (bj != 0.0) {
+            const int Lc = K + 1 - jj;
+            const double temp = bj / A_(K + 1, jj);
+            __syncwarp();
+            if (lane == 0) Bw[jj - 1] = temp;
+            for (int i = jj - 1 - lane; i >= max(1, jj - K); i -= 32) Bw[i - 1] = Bw[i - 1] - temp * A_(Lc + i, jj);
+        }
+        __syncwarp();
     }
 #undef A_
-    __syncthreads();
-    // scatter (all nodes, walls included) then ghosts
-    for (int pp = 1 + tid; pp <= n; pp += nth) {
-        int kp = pp - N * ((pp - 1) / N) - 1, ip = (pp - 1) / N;
-        double v = B[pp - 1];
-        if (ip == 0 || ip == nxc || kp == 0 || kp == nzc) v = 0.0;
-        err[IX(L, ip, kp)] = v;
-    }
-    __syncthreads();
-    const int wi = nxc + 1 + 2 * SP, wk = nzc + 1 + 2 * SP;
-    for (int t = tid; t < wi * wk; t += nth) {
-        int i = -SP + t % wi, k = -SP + t / wi;
-        if (i >= 0 && i <= nxc && k >= 0 && k <= nzc) continue;
-        int mi = i, mk = k;
-        double sg = 1.0;
-        if (i < 0) { mi = -i; sg = -sg; }
-        else if (i > nxc) { mi = 2 * nxc - i; sg = -sg; }
-        if (k < 0) { mk = -k; if (Vbc == 0) sg = -sg; }
-        else if (k > nzc) { mk = 2 * nzc - k; if (Vbc == 0) sg = -sg; }
-        double v = 0.0;
-        if (mi > 0 && mi < nxc && mk > 0 && mk < nzc) v = sg * err[IX(L, mi, mk)];
-        err[IX(L, i, k)] = v;
-    }
+    for (int p = lane; p < n; p += 32) Ainv[(size_t)p * n + (j - 1)] = Bw[p];
 }
-void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
-                         int n, int kl, int ku, double* bvec, double* err, int Vbc) {
-    size_t bytes = sizeof(double) * ((size_t)(2 * kl + ku + 1) * n + n);
-    int in_smem = bytes <= 200 * 1024 ? 1 : 0;
-    size_t sm = in_smem ? bytes : 0;
-    if (in_smem) cudaFuncSetAttribute(k_coarse_solve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    k_coarse_solve<<<1, 512, sm, s>>>(lv.L, band, ipiv, rowb, lv.rhs, n, kl, ku, in_smem, bvec, err, Vbc); tc_note_launch();
+void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, int n, int kl, int ku, double* Ainv,
+                           double* bscratch) {
+    const int nw = 8;
+    const size_t band_bytes = sizeof(double) * (size_t)(2 * kl + ku + 1) * n;
+    const size_t smem = band_bytes + sizeof(int) * (size_t)((n + 1) & ~1) + sizeof(double) * (size_t)nw * n;
+    const int in_smem = smem <= 200 * 1024 ? 1 : 0;
+    const size_t sm = in_smem ? smem : 0;
+    if (in_smem) cudaFuncSetAttribute(k_coarse_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    k_coarse_inverse<<<(n + nw - 1) / nw, 32 * nw, sm, s>>>(band, ipiv, n, kl, ku, in_smem, Ainv, bscratch); tc_note_launch();
+}
+
+// Coarsest-level solve as x = A^-1 (RowB .* RHS) (Compute_coarse_vector,
+// DGBTRS, Stream_grid_coarse): one warp per interior unknown, the boundary
+// unknowns are zero (walls); ghosts are written with the stream BCs.
+__global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
+                               const double* __restrict__ rhs, int n, double* __restrict__ err, int Vbc) {
+    const int lane = threadIdx.x & 31;
+    const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // 0-based row
+    if (pw >= n) return;
+    const int nzc = L.b, nxc = L.a, N = nzc + 1;
+    const int kp = pw % N, ip = pw / N;
+    if (ip < 1 || ip > nxc - 1 || kp < 1 || kp > nzc - 1) return;
+    const double* row = Ainv + (size_t)pw * n;
+    double acc = 0.0;
+    for (int q = lane; q < n; q += 32) {
+        const int kq = q % N, iq = q / N;
+        if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
+            acc = fma(__ldg(row + q), __ldg(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) store_stream(L, err, ip, kp, acc, Vbc);
+}
+void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
+                         int Vbc) {
+    const int threads = 256;
+    const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
+    k_coarse_apply<<<nb, threads, 0, s>>>(lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
 }
 
 __global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n) {

@@ -56,7 +56,7 @@ struct Handle {
     double *rtr = nullptr, *str = nullptr, *rtr0 = nullptr, *str0 = nullptr, *rtr1 = nullptr, *str1 = nullptr,
            *rtr2 = nullptr, *str2 = nullptr;
     int* ttype = nullptr;
-    double *band = nullptr, *rowb = nullptr, *bvec = nullptr;
+    double *band = nullptr, *rowb = nullptr, *bvec = nullptr, *ainv = nullptr;
     int* ipiv = nullptr;
     double* rows = nullptr;
     RedScratch rs{};
@@ -81,6 +81,7 @@ struct Handle {
     CycleGraphs* graphs = nullptr;
     bool no_graphs = false;
     int cycles_acc = 0;  // W-cycles of all solves since tc_step began
+    bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
 };
 
 #define CK(call)                                                      \
@@ -319,6 +320,19 @@ void iterate_stream(Handle* h, int level, int dir) {
     Level& lv = h->lev[level];
     const int Niter = h->p.Nmulti;
     const bool cheb_pp = (level == h->ratio_level);
+    if (h->fuse_visits && level > 1 && Niter <= 128) {
+        // the whole visit in one cluster launch (same arithmetic, same result)
+        double cv[128], tv[128];
+        for (int n = 1; n <= Niter; n++) {
+            const double ntemp = (double)(Niter - n + 1);
+            const double la = -1.0, lb = -2.0;
+            tv[n - 1] = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
+            cv[n - 1] = (dir == 1) ? 1.0 : 2.0 / (-lb - la + (lb - la) * tv[n - 1]);
+        }
+        if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, tv, Niter, (dir != 1 && cheb_pp) ? 1 : 0,
+                                 h->p.Vbc) == 0)
+            return;
+    }
     for (int n = 1; n <= Niter; n++) {
         const double ntemp = (double)(Niter - n + 1);
         const double la = -1.0;
@@ -357,8 +371,7 @@ void enqueue_cycle_rest(Handle* h) {
         if (level < G) {
             iterate_stream(h, level, dir);
         } else {
-            launch_coarse_solve(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku, h->bvec,
-                                cur_err(h, G), h->p.Vbc);
+            launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_err(h, G), h->p.Vbc);
         }
         if (h->multi[pp + 1] < h->multi[pp])
             launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
@@ -402,6 +415,7 @@ tc_status multigrid(Handle* h) {
     if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) {
         launch_coarse_build(h->st, h->lev[G], h->band, h->rowb, h->kl, h->ku, h->p.Vbc);
         launch_coarse_lu(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ds);
+        launch_coarse_inverse(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ainv, h->bvec);
         h->lu_valid = true;
     }
     TRY(sync_scalars(h));
@@ -647,6 +661,7 @@ tc_status create(Handle* h, const tc_params* in) {
     h->own_stream = true;
     h->graphs = new CycleGraphs();
     h->no_graphs = (std::getenv("TC_NO_GRAPHS") != nullptr);
+    h->fuse_visits = (std::getenv("TC_NO_FUSED_VISITS") == nullptr) && visit_cluster_setup() > 0;
     // ---- allocations ----
     h->L1 = make_lay(nx, nz);
     const size_t pl = h->L1.plane;
@@ -668,7 +683,8 @@ tc_status create(Handle* h, const tc_params* in) {
     const int ldab = 2 * h->kl + h->ku + 1;
     TRY(dalloc_t(h, &h->band, (size_t)ldab * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->rowb, (size_t)h->ngrid_coarse));
-    TRY(dalloc_t(h, &h->bvec, (size_t)h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->ainv, (size_t)h->ngrid_coarse * h->ngrid_coarse));
+    TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
     TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));
     TRY(dalloc_t(h, &h->rs.part, (size_t)4 * TC_MAX_RED_BLOCKS));

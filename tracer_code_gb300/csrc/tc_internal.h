@@ -117,9 +117,16 @@ void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, cons
 void launch_stream_bcs(cudaStream_t s, const Level& lv, double* S, int Vbc);
 void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* rowb, int kl, int ku, int Vbc);
 void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, int ku, DevScalars* ds);
-void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
-                         int n, int kl, int ku, double* bvec, double* err, int Vbc);
+void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, int n, int kl, int ku, double* Ainv,
+                           double* bscratch);
+void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
+                         int Vbc);
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n);
+
+// (k_visit.cu) one whole smoother visit of a small level as one cluster launch
+int visit_cluster_setup();
+int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
+                         int nsweeps, int per_point, int Vbc);
 void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
                  double* rhs, RedScratch rs, DevScalars* ds);
 
