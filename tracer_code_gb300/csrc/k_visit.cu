@@ -7,12 +7,17 @@
 // whatever the size), and a W-cycle at 6 levels makes 24 visits x 70 sweeps
 // to the two smallest smoothed levels.  Here each CTA of a cluster (up to
 // 16) keeps a band of rows of the level in shared memory (two ping-pong
-// buffers with two halo rows on each side), computes its rows, stores the
-// rows its neighbours need as halo directly into their shared memory
-// (distributed shared memory), and the cluster meets at one hardware
-// barrier per sweep.  The arithmetic per point is the same as k_sweep /
-// k_residual (same folded operator, same order), so the level ends in the
-// same state bit for bit.
+// buffers with two halo rows on each side), every thread owns one point and
+// holds that point's 13 operator coefficients, RHS and pseudo-time step in
+// registers for the whole visit, stores the values its neighbours need as
+// halo directly into their shared memory (distributed shared memory, the
+// addresses resolved once before the first sweep), and the cluster meets at
+// one hardware barrier per sweep.  The per-point Chebyshev factor of the
+// level with finite eigenvalue ratios comes from a table built once per
+// multigrid call (k_cheb_table), so no FP64 division sits in the sweep.
+// The arithmetic per point is the same as k_sweep / k_residual (same folded
+// operator, same order, the same correctly rounded division for the table),
+// so the level ends in the same state bit for bit.
 #include "tc_device.cuh"
 
 #include <cooperative_groups.h>
@@ -20,11 +25,18 @@
 namespace cg = cooperative_groups;
 
 #define VISIT_MAX_SWEEPS 128
+#define VISIT_THREADS 256
+#define VISIT_MAX_CLUSTER 16
+#define VISIT_SMEM_MAX (96 * 1024)
 
 struct VisitParams {
     Lay L;
     int nsweeps, per_point, Vbc, nrows_max;
     double c[VISIT_MAX_SWEEPS];
+};
+
+struct ChebTemps {
+    int nsweeps;
     double temp[VISIT_MAX_SWEEPS];
 };
 
@@ -35,32 +47,25 @@ __device__ __forceinline__ void band_of(int rank, int C, int b, int& k0, int& k1
     k1 = k0 + base + (rank < rem ? 1 : 0) - 1;
 }
 
-__device__ __forceinline__ double stencil_res(const double* __restrict__ S, int W, size_t x,
-                                              const double* __restrict__ cf, size_t pl, double rhs) {
-    // identical term order to folded_residual (k_mg.cu); S has row stride W
-    double acc = rhs;
-    acc = fma(-__ldg(cf + 0 * pl), S[x], acc);
-    acc = fma(-__ldg(cf + 1 * pl), S[x - 1], acc);
-    acc = fma(-__ldg(cf + 2 * pl), S[x + 1], acc);
-    acc = fma(-__ldg(cf + 3 * pl), S[x - 2], acc);
-    acc = fma(-__ldg(cf + 4 * pl), S[x + 2], acc);
-    acc = fma(-__ldg(cf + 5 * pl), S[x - W], acc);
-    acc = fma(-__ldg(cf + 6 * pl), S[x + W], acc);
-    acc = fma(-__ldg(cf + 7 * pl), S[x - 2 * W], acc);
-    acc = fma(-__ldg(cf + 8 * pl), S[x + 2 * W], acc);
-    acc = fma(-__ldg(cf + 9 * pl), S[x - 1 - W], acc);
-    acc = fma(-__ldg(cf + 10 * pl), S[x + 1 - W], acc);
-    acc = fma(-__ldg(cf + 11 * pl), S[x - 1 + W], acc);
-    acc = fma(-__ldg(cf + 12 * pl), S[x + 1 + W], acc);
-    return acc;
+// c(n, point) = 2 / (cA + cB*temp(n)) for the per-point Chebyshev level,
+// the expression k_sweep evaluates, stored as tab[n*(a-1)(b-1) + (i-1) + (k-1)(a-1)].
+__global__ void k_cheb_table(Lay L, ChebTemps T, const double* __restrict__ cA, const double* __restrict__ cB,
+                             double* __restrict__ tab) {
+    const int a = L.a, b = L.b, npts = (a - 1) * (b - 1);
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < npts; p += gridDim.x * blockDim.x) {
+        const int i = 1 + p % (a - 1), k = 1 + p / (a - 1);
+        const size_t x = IX(L, i, k);
+        const double A = __ldg(cA + x), B = __ldg(cB + x);
+        for (int n = 0; n < T.nsweeps; n++) tab[(size_t)n * npts + p] = 2.0 / (A + B * T.temp[n]);
+    }
 }
 
-__global__ void __launch_bounds__(256) k_visit_cluster(VisitParams P, double* __restrict__ Sg,
-                                                       const double* __restrict__ coef,
-                                                       const double* __restrict__ rhs,
-                                                       const double* __restrict__ dts,
-                                                       const double* __restrict__ cA,
-                                                       const double* __restrict__ cB, double* __restrict__ res) {
+__global__ void __launch_bounds__(VISIT_THREADS) k_visit_cluster(VisitParams P, double* __restrict__ Sg,
+                                                                 const double* __restrict__ coef,
+                                                                 const double* __restrict__ rhs,
+                                                                 const double* __restrict__ dts,
+                                                                 const double* __restrict__ ctab,
+                                                                 double* __restrict__ res) {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     const Lay& L = P.L;
@@ -82,37 +87,75 @@ __global__ void __launch_bounds__(256) k_visit_cluster(VisitParams P, double* __
         buf0[(size_t)r * W + c] = v;
         buf1[(size_t)r * W + c] = v;
     }
+    // this thread's point (the launcher guarantees one point per thread at most)
+    const bool act = tid < cnt * (a - 1);
+    const int i = act ? 1 + tid % (a - 1) : 1, k = act ? k0 + tid / (a - 1) : k0;
+    const int r = k - k0 + 2;
+    const int xs = r * W + i + SP;
+    const size_t xg = IX(L, i, k);
+    const int npl = (a - 1) * (b - 1), gp = (i - 1) + (k - 1) * (a - 1);
+    double cf[TC_NCOEF];
+    double rh = 0.0, dt = 0.0;
+    if (act) {
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) cf[d] = -__ldg(coef + xg + (size_t)d * L.plane);
+        rh = __ldg(rhs + xg);
+        dt = __ldg(dts + xg);
+    } else {
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) cf[d] = 0.0;
+    }
+    // local mirror targets: side ghost column (enforceBCs_stream antisymmetric
+    // walls) and the ghost row -1 / b+1 held as halo by the first / last CTA
+    const int side = (i <= SP) ? r * W + (-i + SP) : (i >= a - SP) ? r * W + (2 * a - i + SP) : -1;
+    const int grow = (k == 1) ? (r - 2) * W + i + SP : (k == b - 1) ? (r + 2) * W + i + SP : -1;
+    // halo rows of the neighbouring CTAs (at most two on each side)
+    // (slot j serves the CTA at offset d = -2, -1, +1, +2; null = not a halo row there)
+    double* rem0[4];
+    double* rem1[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const int d = (j < 2) ? j - 2 : j - 1, o = me + d;
+        rem0[j] = nullptr;
+        rem1[j] = nullptr;
+        if (o < 0 || o >= C || !act) continue;
+        int ok0, ok1;
+        band_of(o, C, b, ok0, ok1);
+        if ((k >= ok0 - 2 && k <= ok0 - 1) || (k >= ok1 + 1 && k <= ok1 + 2)) {
+            const int off = (k - ok0 + 2) * W + i + SP;
+            rem0[j] = cl.map_shared_rank(buf0, o) + off;
+            rem1[j] = cl.map_shared_rank(buf1, o) + off;
+        }
+    }
     cl.sync();
-    const int npts = cnt * (a - 1);
     for (int n = 0; n < P.nsweeps; n++) {
         const double* cur = (n & 1) ? buf1 : buf0;
         double* nxt = (n & 1) ? buf0 : buf1;
-        const double cu = P.c[n], tn = P.temp[n];
-        for (int pidx = tid; pidx < npts; pidx += nth) {
-            const int k = k0 + pidx / (a - 1), i = 1 + pidx % (a - 1);
-            const int r = k - k0 + 2;
-            const size_t xs = (size_t)r * W + (size_t)(i + SP);
-            const size_t xg = IX(L, i, k);
-            const double rs = stencil_res(cur, W, xs, coef + xg, L.plane, __ldg(rhs + xg));
-            const double c = P.per_point ? 2.0 / (__ldg(cA + xg) + __ldg(cB + xg) * tn) : cu;
-            const double v = fma(c * __ldg(dts + xg), rs, cur[xs]);
+        if (act) {
+            const double c = P.per_point ? __ldg(ctab + (size_t)n * npl + gp) : P.c[n];
+            // identical term order to folded_residual (k_mg.cu)
+            double acc = rh;
+            acc = fma(cf[0], cur[xs], acc);
+            acc = fma(cf[1], cur[xs - 1], acc);
+            acc = fma(cf[2], cur[xs + 1], acc);
+            acc = fma(cf[3], cur[xs - 2], acc);
+            acc = fma(cf[4], cur[xs + 2], acc);
+            acc = fma(cf[5], cur[xs - W], acc);
+            acc = fma(cf[6], cur[xs + W], acc);
+            acc = fma(cf[7], cur[xs - 2 * W], acc);
+            acc = fma(cf[8], cur[xs + 2 * W], acc);
+            acc = fma(cf[9], cur[xs - 1 - W], acc);
+            acc = fma(cf[10], cur[xs + 1 - W], acc);
+            acc = fma(cf[11], cur[xs - 1 + W], acc);
+            acc = fma(cf[12], cur[xs + 1 + W], acc);
+            const double v = fma(c * dt, acc, cur[xs]);
             nxt[xs] = v;
-            // side ghosts of this row (enforceBCs_stream: antisymmetric walls)
-            if (i <= SP) nxt[(size_t)r * W + (size_t)(-i + SP)] = -v;
-            if (i >= a - SP) nxt[(size_t)r * W + (size_t)(2 * a - i + SP)] = -v;
-            // ghost rows -1 / b+1 are halo rows of the first / last CTA
-            if (k == 1) nxt[(size_t)(r - 2) * W + (size_t)(i + SP)] = zsgn * v;  // row -1 (this CTA owns row 1)
-            if (k == b - 1) nxt[(size_t)(r + 2) * W + (size_t)(i + SP)] = zsgn * v;  // row b+1
-            // halo rows of the neighbouring CTAs
-            for (int d = -2; d <= 2; d++) {
-                const int o = me + d;
-                if (d == 0 || o < 0 || o >= C) continue;
-                int ok0, ok1;
-                band_of(o, C, b, ok0, ok1);
-                if ((k >= ok0 - 2 && k <= ok0 - 1) || (k >= ok1 + 1 && k <= ok1 + 2)) {
-                    double* rb = cl.map_shared_rank(nxt, o);
-                    rb[(size_t)(k - ok0 + 2) * W + (size_t)(i + SP)] = v;
-                }
+            if (side >= 0) nxt[side] = -v;
+            if (grow >= 0) nxt[grow] = zsgn * v;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                double* q = (n & 1) ? rem0[j] : rem1[j];
+                if (q) *q = v;
             }
         }
         cl.sync();
@@ -120,29 +163,40 @@ __global__ void __launch_bounds__(256) k_visit_cluster(VisitParams P, double* __
     // final state: owned rows (with side ghosts) to global, then ghost rows
     const double* fin = (P.nsweeps & 1) ? buf1 : buf0;
     for (int t = tid; t < cnt * W; t += nth) {
-        const int r = 2 + t / W, c = t % W;
-        Sg[IX(L, c - SP, k0 - 2 + r)] = fin[(size_t)r * W + c];
+        const int rr = 2 + t / W, c = t % W;
+        Sg[IX(L, c - SP, k0 - 2 + rr)] = fin[(size_t)rr * W + c];
     }
     // residual on owned points (halos are current after the last barrier)
-    for (int pidx = tid; pidx < npts; pidx += nth) {
-        const int k = k0 + pidx / (a - 1), i = 1 + pidx % (a - 1);
-        const size_t xs = (size_t)(k - k0 + 2) * W + (size_t)(i + SP);
-        const size_t xg = IX(L, i, k);
-        res[xg] = stencil_res(fin, W, xs, coef + xg, L.plane, __ldg(rhs + xg));
+    if (act) {
+        double acc = rh;
+        acc = fma(cf[0], fin[xs], acc);
+        acc = fma(cf[1], fin[xs - 1], acc);
+        acc = fma(cf[2], fin[xs + 1], acc);
+        acc = fma(cf[3], fin[xs - 2], acc);
+        acc = fma(cf[4], fin[xs + 2], acc);
+        acc = fma(cf[5], fin[xs - W], acc);
+        acc = fma(cf[6], fin[xs + W], acc);
+        acc = fma(cf[7], fin[xs - 2 * W], acc);
+        acc = fma(cf[8], fin[xs + 2 * W], acc);
+        acc = fma(cf[9], fin[xs - 1 - W], acc);
+        acc = fma(cf[10], fin[xs + 1 - W], acc);
+        acc = fma(cf[11], fin[xs - 1 + W], acc);
+        acc = fma(cf[12], fin[xs + 1 + W], acc);
+        res[xg] = acc;
     }
     __threadfence();
     cl.sync();  // global rows written; no CTA leaves while others may touch its shared memory
     // top/bottom ghost rows from the (now global) interior rows
     if (me == 0 || me == C - 1) {
         for (int t = tid; t < 2 * W; t += nth) {
-            const int g = 1 + t / W, c = t % W, i = c - SP;
+            const int g = 1 + t / W, c = t % W, ii = c - SP;
             if (me == 0) {
-                const double v = Sg[IX(L, i, g)];
-                Sg[IX(L, i, -g)] = zsgn * v;
+                const double v = Sg[IX(L, ii, g)];
+                Sg[IX(L, ii, -g)] = zsgn * v;
             }
             if (me == C - 1) {
-                const double v = Sg[IX(L, i, b - g)];
-                Sg[IX(L, i, b + g)] = zsgn * v;
+                const double v = Sg[IX(L, ii, b - g)];
+                Sg[IX(L, ii, b + g)] = zsgn * v;
             }
         }
     }
@@ -153,15 +207,16 @@ __global__ void __launch_bounds__(256) k_visit_cluster(VisitParams P, double* __
 // resident (0 = the fused visit is unavailable, callers use per-sweep launches).
 int visit_cluster_setup() {
     if (cudaFuncSetAttribute(k_visit_cluster, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return 0;
-    if (cudaFuncSetAttribute(k_visit_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) != cudaSuccess)
+    if (cudaFuncSetAttribute(k_visit_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, VISIT_SMEM_MAX) !=
+        cudaSuccess)
         return 0;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(16, 1, 1);
-    cfg.blockDim = dim3(256, 1, 1);
-    cfg.dynamicSmemBytes = 96 * 1024;
+    cfg.gridDim = dim3(VISIT_MAX_CLUSTER, 1, 1);
+    cfg.blockDim = dim3(VISIT_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = VISIT_SMEM_MAX;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 16;
+    attr[0].val.clusterDim.x = VISIT_MAX_CLUSTER;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
@@ -174,27 +229,53 @@ int visit_cluster_setup() {
     return n;
 }
 
+// Cluster size and shared memory for a level, or 0 if the level is not fused
+// (more than one point per thread, too many sweeps or too little shared memory).
+static int visit_shape(const Lay& L, int nsweeps, int* rows_max, size_t* smem) {
+    const int a = L.a, b = L.b;
+    if (nsweeps > VISIT_MAX_SWEEPS || b - 1 < 2 || a - 1 < 1) return 0;
+    const int C = (b - 1 < VISIT_MAX_CLUSTER) ? (b - 1) : VISIT_MAX_CLUSTER;
+    const int nr = b - 1, rm = nr / C + (nr % C ? 1 : 0);
+    if (rm * (a - 1) > VISIT_THREADS) return 0;
+    const size_t sm = sizeof(double) * 2 * (size_t)(rm + 4) * (size_t)(a + 1 + 2 * SP);
+    if (sm > VISIT_SMEM_MAX) return 0;
+    *rows_max = rm;
+    *smem = sm;
+    return C;
+}
+
+int visit_cluster_fits(const Lay& L, int nsweeps) {
+    int rm;
+    size_t sm;
+    return visit_shape(L, nsweeps, &rm, &sm) > 0;
+}
+
+void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab) {
+    ChebTemps T;
+    T.nsweeps = nsweeps;
+    for (int n = 0; n < nsweeps; n++) T.temp[n] = tvals[n];
+    const int npts = (lv.L.a - 1) * (lv.L.b - 1);
+    k_cheb_table<<<(npts + 255) / 256, 256, 0, s>>>(lv.L, T, lv.cA, lv.cB, tab); tc_note_launch();
+}
+
 // Returns 0 if the level was handled here (caller skips the per-sweep path).
-int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
+int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* ctab,
                          int nsweeps, int per_point, int Vbc) {
-    const int a = lv.L.a, b = lv.L.b;
-    if (nsweeps > VISIT_MAX_SWEEPS || (a - 1) * (b - 1) > 4096 || b - 1 < 2) return 1;
-    const int C = (b - 1 < 16) ? (b - 1) : 16;
-    const int nr = b - 1, rows_max = nr / C + (nr % C ? 1 : 0);
-    if (rows_max < 1) return 1;
-    const int W = a + 1 + 2 * SP;
-    const size_t smem = sizeof(double) * 2 * (size_t)(rows_max + 4) * W;
-    if (smem > 96 * 1024) return 1;
+    int rows_max;
+    size_t smem;
+    const int C = visit_shape(lv.L, nsweeps, &rows_max, &smem);
+    if (C == 0) return 1;
+    if (per_point && ctab == nullptr) return 1;
     VisitParams P;
     P.L = lv.L;
     P.nsweeps = nsweeps;
     P.per_point = per_point;
     P.Vbc = Vbc;
     P.nrows_max = rows_max;
-    for (int n = 0; n < nsweeps; n++) { P.c[n] = cvals[n]; P.temp[n] = tvals[n]; }
+    for (int n = 0; n < nsweeps; n++) P.c[n] = cvals[n];
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)C, 1, 1);
-    cfg.blockDim = dim3(256, 1, 1);
+    cfg.blockDim = dim3(VISIT_THREADS, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -205,8 +286,7 @@ int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const doubl
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     cudaError_t e = cudaLaunchKernelEx(&cfg, k_visit_cluster, P, S, (const double*)lv.coef, (const double*)lv.rhs,
-                                       (const double*)lv.dt_stream, (const double*)lv.cA, (const double*)lv.cB,
-                                       lv.res);
+                                       (const double*)lv.dt_stream, ctab, lv.res);
     if (e != cudaSuccess) return 2;
     tc_note_launch();
     return 0;

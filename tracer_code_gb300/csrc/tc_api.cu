@@ -82,6 +82,8 @@ struct Handle {
     bool no_graphs = false;
     int cycles_acc = 0;  // W-cycles of all solves since tc_step began
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
+    double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
+    int ctab_level = 0;        // level the table was built for (0 = none)
 };
 
 #define CK(call)                                                      \
@@ -315,6 +317,17 @@ tc_status compute_viscosity(Handle* h, int level) {
     return TC_OK;
 }
 
+// Chebyshev node temp(n) and uniform factor c(n) of sweep n=1..Niter
+// (iterative_solver.f90:873-885), stored at index n-1.
+void cheb_temps(int Niter, int dir, double* tv, double* cv) {
+    for (int n = 1; n <= Niter; n++) {
+        const double ntemp = (double)(Niter - n + 1);
+        const double la = -1.0, lb = -2.0;
+        tv[n - 1] = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
+        cv[n - 1] = (dir == 1) ? 1.0 : 2.0 / (-lb - la + (lb - la) * tv[n - 1]);
+    }
+}
+
 // iterate_stream (iterative_solver.f90:860-963), iterate_order=1
 void iterate_stream(Handle* h, int level, int dir) {
     Level& lv = h->lev[level];
@@ -323,14 +336,10 @@ void iterate_stream(Handle* h, int level, int dir) {
     if (h->fuse_visits && level > 1 && Niter <= 128) {
         // the whole visit in one cluster launch (same arithmetic, same result)
         double cv[128], tv[128];
-        for (int n = 1; n <= Niter; n++) {
-            const double ntemp = (double)(Niter - n + 1);
-            const double la = -1.0, lb = -2.0;
-            tv[n - 1] = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
-            cv[n - 1] = (dir == 1) ? 1.0 : 2.0 / (-lb - la + (lb - la) * tv[n - 1]);
-        }
-        if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, tv, Niter, (dir != 1 && cheb_pp) ? 1 : 0,
-                                 h->p.Vbc) == 0)
+        cheb_temps(Niter, dir, tv, cv);
+        const int pp = (dir != 1 && cheb_pp) ? 1 : 0;
+        if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, (h->ctab_level == level) ? h->ctab : nullptr, Niter,
+                                 pp, h->p.Vbc) == 0)
             return;
     }
     for (int n = 1; n <= Niter; n++) {
@@ -412,6 +421,14 @@ tc_status multigrid(Handle* h) {
     for (int l = 1; l <= G; l++) TRY(compute_viscosity(h, l));
     for (int l = 1; l <= G; l++)
         launch_level_coefs(h->st, h->lev[l], cur_vis(h, l), h->p.ivis, h->p.courant_stream, l == h->ratio_level ? 1 : 0);
+    h->ctab_level = 0;
+    if (h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
+        visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti)) {
+        double cv[128], tv[128];
+        cheb_temps(h->p.Nmulti, 0, tv, cv);
+        launch_cheb_table(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab);
+        h->ctab_level = h->ratio_level;
+    }
     if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) {
         launch_coarse_build(h->st, h->lev[G], h->band, h->rowb, h->kl, h->ku, h->p.Vbc);
         launch_coarse_lu(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ds);
@@ -686,6 +703,7 @@ tc_status create(Handle* h, const tc_params* in) {
     TRY(dalloc_t(h, &h->ainv, (size_t)h->ngrid_coarse * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
+    if (h->fuse_visits) TRY(dalloc_t(h, &h->ctab, (size_t)128 * 4096));
     TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));
     TRY(dalloc_t(h, &h->rs.part, (size_t)4 * TC_MAX_RED_BLOCKS));
     TRY(dalloc_t(h, &h->rs.count, (size_t)8));

@@ -125,7 +125,9 @@ void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n)
 
 // (k_visit.cu) one whole smoother visit of a small level as one cluster launch
 int visit_cluster_setup();
-int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
+int visit_cluster_fits(const Lay& L, int nsweeps);
+void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab);
+int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* ctab,
                          int nsweeps, int per_point, int Vbc);
 void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
                  double* rhs, RedScratch rs, DevScalars* ds);
