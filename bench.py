@@ -43,25 +43,35 @@ CYCLES_PER_STEP_DEFAULT = 228.0
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the level-1
 # smoother kernel (profiles/k_sweep_1024x256.md); None until captured.
 SWEEP_DRAM_BYTES = None
+SWEEP32_DRAM_BYTES = None
 
 
-def workload_params():
+def workload_params(solver: str = "plain"):
     from tracer_code_gb300 import config_1024x256
     p = config_1024x256()
     p.mg_zero_coarse = 1
+    p.solver_precision = 1 if solver == "mixed" else 0
     return p
 
 
-def workload_desc(p) -> dict:
+SOLVER_DESC = {
+    "plain": "plain FP64 multigrid (W-cycle, Chebyshev-Richardson smoother, banded LU coarse solve), "
+             "coarse corrections restart from zero (mg_zero_coarse=1)",
+    "mixed": "mixed-precision multigrid: the same W-cycle with FP32 smoother, residuals and transfers on levels "
+             "1..grids-1 inside FP64 defect correction (FP64 level-1 residual, streamfunction and updates, FP64 "
+             "coarse solve), same 1e-8 test; no learned guess yet",
+}
+
+
+def workload_desc(p, solver: str) -> dict:
     ntr = (p.nx + 1) * (p.nz + 1) * p.tpc
     return {
         "workload": f"{p.nx}x{p.nz} cells, aspect {p.aspect:g}, {p.tpc} tracers/cell ({ntr:,} tracers), "
                     f"Ra={p.RaT:g}, B={p.RaC[0] / p.RaT:g}, dense layer z<{p.dlayer:g}, "
-                    f"eta=exp(-ln({p.visT:g})T)*10 in enriched, RK4, FP64 multigrid {p.grids} levels to {p.tolerance:g}",
+                    f"eta=exp(-ln({p.visT:g})T)*10 in enriched, RK4, multigrid {p.grids} levels to {p.tolerance:g}",
         "grid": f"{p.nx}x{p.nz}",
         "tracers": ntr,
-        "solver": "plain FP64 multigrid (W-cycle, Chebyshev-Richardson smoother, banded LU coarse solve), "
-                  "coarse corrections restart from zero (mg_zero_coarse=1)",
+        "solver": SOLVER_DESC[solver],
         "l2": "inputs larger than L2 (tracer state 6.6M x 8 FP64 arrays = 421 MB)",
         "parallelism": "replicas (one independent case per GPU)",
     }
@@ -186,7 +196,7 @@ def run_reference(args, rank: int, world: int):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_desc(p),
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_desc(p, "plain"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"per step: CPU restatement multigrid capped at 1 and 2 W-cycles, one RK4 step "
                                    f"without re-solves, one tracer-ratio pass; timestep assembled as "
@@ -197,6 +207,43 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def timed_steps(sim, stream, steps: int, warmup: int, barrier):
+    """W untimed steps, then K steps between CUDA events on the library's
+    stream; returns (ms, cycles of the timed steps, cycles of the warm-up,
+    kernel launches in the timed region)."""
+    import torch
+    from tracer_code_gb300 import Simulation
+    warm = [sim.step()[1] for _ in range(warmup)]
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    n0 = Simulation.kernel_launches()
+    e0.record(stream)
+    cyc = [sim.step()[1] for _ in range(steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    return e0.elapsed_time(e1), cyc, warm, Simulation.kernel_launches() - n0
+
+
+def sweep_roofline(sim, p, fp32: bool) -> dict:
+    """Level-1 smoother sweep timed live on the library's stream."""
+    sweep_ms = sim.time_sweep(1, 70)
+    ni, nk = p.nx - 1, p.nz - 1
+    alg_bytes = (44.0 if fp32 else 88.0) * ni * nk
+    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
+    peak, src = peaks()
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": SWEEP32_DRAM_BYTES if fp32 else SWEEP_DRAM_BYTES,
+            "kernel": ("k_sweep32" if fp32 else "k_sweep") + f" (level 1, {ni}x{nk} points)",
+            "alg_bytes_per_launch": alg_bytes, "kernel_ms": sweep_ms,
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured" else "fallback 6.8 TB/s",
+            "note": ("FP32: 44 B/pt (13 coefficients + RHS + dt + psi in/out at half width, per the FP64 88 B/pt "
+                     "count); level-1 FP32 working set 17.8 MB is L2-resident between sweeps" if fp32 else
+                     "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s")}
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -205,52 +252,27 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
     torch.cuda.set_device(local_rank)
     stream = torch.cuda.Stream()
-    p = workload_params()
-    sim = Simulation(p, stream=stream.cuda_stream)
-    st = state.initial_state(p, seed=1 + rank)
-    sim.upload(st)
-    cycles = []
-    for _ in range(args.warmup):
-        _, q, _ = sim.step()
-        cycles.append(q)
 
     def barrier():
         if world > 1:
             dist.barrier()
 
-    n0 = Simulation.kernel_launches()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    solves = []
-    barrier()
-    torch.cuda.synchronize()
+    def max_over_ranks(x: float) -> float:
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # headline arm: mixed-precision solver
+    p = workload_params("mixed")
+    st = state.initial_state(p, seed=1 + rank)
+    sim = Simulation(p, stream=stream.cuda_stream)
+    sim.upload(st)
     with ClockSampler(local_rank) as clk:
-        e0.record(stream)
-        for _ in range(args.steps):
-            _, q, _ = sim.step()
-            solves.append(q)
-        e1.record(stream)
-        torch.cuda.synchronize()
-    barrier()
-    launches = Simulation.kernel_launches() - n0
-    ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+        ms, solves, cycles, launches = timed_steps(sim, stream, args.steps, args.warmup, barrier)
+    ms_max = max_over_ranks(ms)
     value = world * args.steps / (ms_max * 1e-3)
-    cycles_per_step = statistics.mean(solves)
-    # dominant kernel: level-1 smoother sweep, timed live on the same stream
-    sweep_ms = sim.time_sweep(1, 70)
-    ni, nk = p.nx - 1, p.nz - 1
-    alg_bytes = 88.0 * ni * nk
-    achieved = alg_bytes / (sweep_ms * 1e-3) / 1e9
-    peak, src = peaks()
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": SWEEP_DRAM_BYTES, "kernel": "k_sweep (level 1, 1023x255 points)",
-            "kernel_ms": sweep_ms, "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured"
-            else "fallback 6.8 TB/s",
-            "note": "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s"}
+    roof = sweep_roofline(sim, p, fp32=True)
     # end to end: the same steps through tc_step_host with pinned host state
     host = {}
     dl = sim.download()
@@ -268,17 +290,27 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     for _ in range(k_e2e):
         sim.step_host(host)
     torch.cuda.synchronize()
-    te = torch.tensor([time.perf_counter() - t0], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(te, op=dist.ReduceOp.MAX)
-    e2e_value = world * k_e2e / float(te.item())
+    e2e_value = world * k_e2e / max_over_ranks(time.perf_counter() - t0)
+    sim.close()
+    # comparison arm: plain FP64 multigrid on the same initial state
+    pp = workload_params("plain")
+    sim0 = Simulation(pp, stream=stream.cuda_stream)
+    sim0.upload(st)
+    ms0, solves0, cycles0, _ = timed_steps(sim0, stream, args.steps, args.warmup, barrier)
+    plain_value = world * args.steps / (max_over_ranks(ms0) * 1e-3)
+    roof0 = sweep_roofline(sim0, pp, fp32=False)
+    sim0.close()
     if rank == 0:
+        cfg = dict(workload_desc(p, "mixed"), cycles_per_step=solves, warmup_cycles_per_step=cycles,
+                   tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
+                   plain_fp64={"timesteps_per_s": plain_value, "ms_per_step": ms0 / args.steps,
+                               "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0},
+                   speedup_vs_plain_fp64=value / plain_value)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded conductive T + uniform tracers)",
-            "config": dict(workload_desc(p), cycles_per_step=solves, warmup_cycles_per_step=cycles,
-                           tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc)),
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded conductive T + uniform tracers)",
+            "config": cfg,
             "roofline": roof,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "steps": k_e2e, "api": "tc_step_host (C ABI, pinned host arrays)"},
@@ -286,17 +318,16 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             "gpu_launches": int(launches),
         }
         if not args.no_cpu_baseline:
-            cps = float(cycles_per_step)
-            r = cpu_sample(p, os.cpu_count() or 1, cps)
+            cps = float(statistics.mean(solves0))
+            r = cpu_sample(pp, os.cpu_count() or 1, cps)
             line["cpu_baseline"] = {"value": 1.0 / r["step_s"], "unit": UNIT, "cores": os.cpu_count() or 1,
                                     "kind": "port",
-                                    "sample": f"CPU restatement, full workload: multigrid capped at 1 and 2 W-cycles, "
-                                              f"one RK4 step without re-solves, one tracer-ratio pass "
+                                    "sample": f"CPU restatement (FP64), full workload: multigrid capped at 1 and 2 "
+                                              f"W-cycles, one RK4 step without re-solves, one tracer-ratio pass "
                                               f"({r['sample_s']:.1f} s); timestep = 4*fixed + {cps:g} cycles + RK "
                                               f"+ 3 ratio passes",
                                     "parts": r}
         print(json.dumps(line), flush=True)
-    sim.close()
 
 
 def main():
@@ -308,10 +339,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling case: upload the workload, run one multigrid solve, exit")
+    ap.add_argument("--solver", default="plain", choices=["plain", "mixed"],
+                    help="solver of --profile-solve")
     args = ap.parse_args()
     if args.profile_solve:
         from tracer_code_gb300 import Simulation, state
-        p = workload_params()
+        p = workload_params(args.solver)
         sim = Simulation(p)
         sim.upload(state.initial_state(p, seed=1))
         n0 = Simulation.kernel_launches()

@@ -117,7 +117,16 @@ typedef struct tc_params {
      * correction scheme).  With more than two levels the reference behaviour
      * stalls or diverges on high-contrast starts (e.g. 1024x256, visT=1e4). */
     int32_t mg_zero_coarse;
-    int32_t reserved_[3];
+    /* No reference counterpart.  0 = every multigrid operation in FP64 with
+     * the reference's arithmetic.  1 = mixed precision: the smoother, the
+     * residuals of levels 2..grids-1 and the restrictions/prolongations
+     * between them run in FP32, inside an FP64 defect-correction loop that
+     * keeps the level-1 residual (and with it the convergence test), the
+     * streamfunction and its updates in FP64; the coarsest direct solve
+     * stays FP64.  The tolerance test is the reference's, so the solution
+     * meets the same relative residual; cycle counts may differ. */
+    int32_t solver_precision;
+    int32_t reserved_[2];
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
@@ -210,11 +219,18 @@ tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double
 
 /* Diagnostics (no counterpart in the reference).  tc_time_sweep times
  * `nsweeps` back-to-back launches of the multigrid smoother kernel of `level`
- * with CUDA events on the handle's stream (state left unchanged) and writes
+ * (the FP32 one under solver_precision = 1) with CUDA events on the handle's
+ * stream (state left unchanged) and writes
  * the mean milliseconds per launch.  tc_kernel_launches returns how many
  * kernels this library has launched in the process so far (graph replays
  * count every kernel node). */
 tc_status tc_time_sweep(tc_handle* h, int32_t level, int32_t nsweeps, double* ms_per_sweep);
+/* Times `reps` back-to-back smoother visits (Nmulti sweeps and the residual,
+ * in the handle's solver precision; level 1 of the mixed solve includes its
+ * FP64 residual, FP32 RHS and FP64 update) of `level` on the handle's stream
+ * and writes the mean milliseconds per visit.  The level's correction arrays
+ * are left changed; the next tc_multigrid starts from SF as always. */
+tc_status tc_time_visit(tc_handle* h, int32_t level, int32_t reps, double* ms_per_visit);
 int64_t tc_kernel_launches(void);
 
 /* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */

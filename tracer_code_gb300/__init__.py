@@ -31,7 +31,7 @@ EXPORTS = [
     "tc_default_params", "tc_abi_sizes", "tc_create", "tc_destroy", "tc_get_info", "tc_set_stream",
     "tc_upload_state", "tc_download_state", "tc_set_clock", "tc_multigrid", "tc_compute_velocities", "tc_stats",
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
-    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_kernel_launches",
+    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches",
 ]
 
 
@@ -77,6 +77,7 @@ def load_library(build_if_missing: bool = False):
         L.tc_step_host.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64, C.POINTER(StatsRow),
                                    C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.tc_time_sweep.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
+        L.tc_time_visit.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]
@@ -225,6 +226,11 @@ class Simulation:
     def time_sweep(self, level: int = 1, nsweeps: int = 70) -> float:
         ms = C.c_double(0)
         self._chk(self.L.tc_time_sweep(self.h, level, nsweeps, C.byref(ms)), "time_sweep")
+        return ms.value
+
+    def time_visit(self, level: int, reps: int = 20) -> float:
+        ms = C.c_double(0)
+        self._chk(self.L.tc_time_visit(self.h, level, reps, C.byref(ms)), "time_visit")
         return ms.value
 
     @staticmethod

@@ -141,14 +141,6 @@ void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, doubl
 // ---------------------------------------------------------------------------
 // restrict_coefficients + boundary injection of viscosityBCs_initialize
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double restrict9(const double* __restrict__ in, const Lay& F, int ii, int kk) {
-    // corner term repeats (ii-1,kk+1) and omits (ii+1,kk-1), as iterative_solver.f90:607
-    double corners = (in[IX(F, ii - 1, kk - 1)] + in[IX(F, ii - 1, kk + 1)] + in[IX(F, ii + 1, kk + 1)] +
-                      in[IX(F, ii - 1, kk + 1)]) / 16.0;
-    double sides = (in[IX(F, ii - 1, kk)] + in[IX(F, ii, kk - 1)] + in[IX(F, ii + 1, kk)] + in[IX(F, ii, kk + 1)]) / 8.0;
-    double centre = in[IX(F, ii, kk)] / 4.0;
-    return corners + sides + centre;
-}
 __global__ void k_restrict_vis(Lay C, Lay F, Range2 r, const double* __restrict__ vf, double* __restrict__ vc) {
     RANGE_IK(r);
     if (!inr) return;
@@ -233,45 +225,7 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
 // ---------------------------------------------------------------------------
 // folded operator: RHS - L S at an interior point
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ double folded_residual(const Lay& L, const double* __restrict__ S,
-                                                  const double* __restrict__ coef, double rhs, size_t x) {
-    const size_t ld = (size_t)L.ld, pl = L.plane;
-    const double* cf = coef + x;
-    double acc = rhs;
-    acc = fma(-__ldg(cf + 0 * pl), __ldg(S + x), acc);
-    acc = fma(-__ldg(cf + 1 * pl), __ldg(S + x - 1), acc);
-    acc = fma(-__ldg(cf + 2 * pl), __ldg(S + x + 1), acc);
-    acc = fma(-__ldg(cf + 3 * pl), __ldg(S + x - 2), acc);
-    acc = fma(-__ldg(cf + 4 * pl), __ldg(S + x + 2), acc);
-    acc = fma(-__ldg(cf + 5 * pl), __ldg(S + x - ld), acc);
-    acc = fma(-__ldg(cf + 6 * pl), __ldg(S + x + ld), acc);
-    acc = fma(-__ldg(cf + 7 * pl), __ldg(S + x - 2 * ld), acc);
-    acc = fma(-__ldg(cf + 8 * pl), __ldg(S + x + 2 * ld), acc);
-    acc = fma(-__ldg(cf + 9 * pl), __ldg(S + x - 1 - ld), acc);
-    acc = fma(-__ldg(cf + 10 * pl), __ldg(S + x + 1 - ld), acc);
-    acc = fma(-__ldg(cf + 11 * pl), __ldg(S + x - 1 + ld), acc);
-    acc = fma(-__ldg(cf + 12 * pl), __ldg(S + x + 1 + ld), acc);
-    return acc;
-}
 
-// writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
-// derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
-__device__ __forceinline__ void store_stream(const Lay& L, double* __restrict__ S, int i, int k, double v, int Vbc) {
-    const int a = L.a, b = L.b;
-    int gi[3] = {i, 0, 0};
-    double si[3] = {1.0, -1.0, -1.0};
-    int ng = 1;
-    if (i <= SP) gi[ng++] = -i;
-    if (i >= a - SP) gi[ng++] = 2 * a - i;
-    int gk[3] = {k, 0, 0};
-    const double zsgn = (Vbc == 1) ? 1.0 : -1.0;
-    double sk[3] = {1.0, zsgn, zsgn};
-    int nk = 1;
-    if (k <= SP) gk[nk++] = -k;
-    if (k >= b - SP) gk[nk++] = 2 * b - k;
-    for (int u = 0; u < nk; u++)
-        for (int t = 0; t < ng; t++) S[IX(L, gi[t], gk[u])] = (si[t] * sk[u]) * v;
-}
 
 __global__ void k_sweep(Lay L, Range2 r, const double* __restrict__ Sin, double* __restrict__ Sout,
                         const double* __restrict__ coef, const double* __restrict__ rhs,

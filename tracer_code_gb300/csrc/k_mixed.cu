@@ -1,0 +1,182 @@
+// k_mixed.cu -- FP32 multigrid of the mixed-precision solve and the bridges
+// between it and the FP64 streamfunction.
+//
+// The mixed solve runs the reference's W-cycle (multigrid,
+// iterative_solver.f90:79-173) as defect correction.  Level 1 keeps the
+// streamfunction psi, its RHS, the 13 folded coefficient planes and the
+// residual in FP64.  Each level-1 visit smooths the correction equation
+// L e = r in FP32 from e = 0 with r = RHS - L psi rounded to FP32
+// (k_residual_to32), then adds e to psi in FP64 (k_update64) and the FP64
+// residual of the new psi takes the reference's convergence test.  Levels
+// 2..grids-1 hold FP32 corrections exactly as the reference holds FP64 ones
+// (same sweeps, restriction, prolongation), the coarsest direct solve
+// applies the FP64 inverse to the FP32 RHS, and the last prolongation adds
+// the FP32 correction of level 2 to psi in FP64 (k_prolong_into64).  Since
+// the smoother is linear, an exact-arithmetic run of this sequence produces
+// the same iterates as the reference's; rounding enters only through the
+// corrections, which the FP64 residual of every cycle measures.
+//
+// Sizes and traffic: a level-l FP32 sweep moves 13 coefficient + RHS + dt +
+// psi-in + psi-out floats = 68 B per point (half the FP64 sweep's 136 B);
+// at 1024x256 the level-1 FP32 working set (17.8 MB) stays in L2.
+#include "tc_device.cuh"
+
+namespace {
+
+__global__ void k_to_f32(const double* __restrict__ in, float* __restrict__ out, size_t n) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t st = (size_t)gridDim.x * blockDim.x;
+    for (; t < n; t += st) out[t] = (float)in[t];
+}
+void to_f32(cudaStream_t s, const double* in, float* out, size_t n) {
+    int nb = (int)((n + 255) / 256);
+    if (nb > 2432) nb = 2432;
+    k_to_f32<<<nb, 256, 0, s>>>(in, out, n); tc_note_launch();
+}
+
+__global__ void k_sweep32(Lay L, Range2 r, const float* __restrict__ Sin, float* __restrict__ Sout,
+                          const float* __restrict__ coef, const float* __restrict__ rhs,
+                          const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
+                          float c_uniform, int per_point, float temp, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    const float res = folded_residual<float>(L, Sin, coef, __ldg(rhs + x), x);
+    const float c = per_point ? 2.0f / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
+    const float v = fmaf(c * __ldg(dts + x), res, __ldg(Sin + x));
+    store_stream<float>(L, Sout, i, k, v, Vbc);
+}
+
+__global__ void k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
+                             const float* __restrict__ rhs, float* __restrict__ res) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    res[x] = folded_residual<float>(L, S, coef, __ldg(rhs + x), x);
+}
+
+template <typename Tin>
+__global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ rf, float* __restrict__ rc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    rc[IX(C, i, k)] = (float)restrict9<Tin>(rf, F, 2 * i, 2 * k);
+}
+
+// bilinear prolongation value of the coarse correction at fine (i,k)
+template <typename T>
+__device__ __forceinline__ T prolong_value(const Lay& C, const float* __restrict__ ec, int i, int k) {
+    const bool ie = (i % 2) == 0, ke = (k % 2) == 0;
+    if (ie && ke) return (T)ec[IX(C, i / 2, k / 2)];
+    if (ie) return ((T)ec[IX(C, i / 2, (k - 1) / 2)] + (T)ec[IX(C, i / 2, (k + 1) / 2)]) / T(2);
+    if (ke) return ((T)ec[IX(C, (i - 1) / 2, k / 2)] + (T)ec[IX(C, (i + 1) / 2, k / 2)]) / T(2);
+    return ((T)ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + (T)ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
+            (T)ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + (T)ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / T(4);
+}
+
+template <typename T>
+__global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* __restrict__ ec, T* __restrict__ ef, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(F, i, k);
+    store_stream<T>(F, ef, i, k, ef[x] + prolong_value<T>(C, ec, i, k), Vbc);
+}
+
+// FP64 residual of psi, rounded to FP32 as the RHS of the level-1 correction
+__global__ void k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
+                                const double* __restrict__ rhs, float* __restrict__ rhs32) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    rhs32[x] = (float)folded_residual<double>(L, S, coef, __ldg(rhs + x), x);
+}
+
+// psi += e in FP64, ghosts from the new interior value
+__global__ void k_update64(Lay L, Range2 r, double* __restrict__ S, const float* __restrict__ e, int Vbc) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    store_stream<double>(L, S, i, k, S[x] + (double)e[x], Vbc);
+}
+
+// coarsest level: x = A^-1 (RowB .* rhs) in FP64 from the FP32 RHS, stored as FP32
+__global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
+                                 const float* __restrict__ rhs, int n, float* __restrict__ err, int Vbc) {
+    const int lane = threadIdx.x & 31;
+    const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (pw >= n) return;
+    const int nzc = L.b, nxc = L.a, N = nzc + 1;
+    const int kp = pw % N, ip = pw / N;
+    if (ip < 1 || ip > nxc - 1 || kp < 1 || kp > nzc - 1) return;
+    const double* row = Ainv + (size_t)pw * n;
+    double acc = 0.0;
+    for (int q = lane; q < n; q += 32) {
+        const int kq = q % N, iq = q / N;
+        if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
+            acc = fma(__ldg(row + q), (double)__ldg(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+    }
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) store_stream<float>(L, err, ip, kp, (float)acc, Vbc);
+}
+
+Range2 interior(const Lay& L) { return Range2{1, L.a - 1, 1, L.b - 1}; }
+
+}  // namespace
+
+void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb) {
+    to_f32(s, lv.coef, lv.coef32, (size_t)TC_NCOEF * lv.L.plane);
+    to_f32(s, lv.dt_stream, lv.dts32, lv.L.plane);
+    if (cheb) {
+        to_f32(s, lv.cA, lv.cA32, lv.L.plane);
+        to_f32(s, lv.cB, lv.cB32, lv.L.plane);
+    }
+}
+
+void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
+                    float temp, int Vbc) {
+    const Range2 r = interior(lv.L);
+    k_sweep32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, Sin, Sout, lv.coef32, lv.rhs32, lv.dts32, lv.cA32,
+                                                    lv.cB32, c_uniform, per_point, temp, Vbc); tc_note_launch();
+}
+
+void launch_residual32(cudaStream_t s, const Level& lv, const float* S) {
+    const Range2 r = interior(lv.L);
+    k_residual32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef32, lv.rhs32, lv.res32); tc_note_launch();
+}
+
+void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c) {
+    const Range2 r = interior(coarse.L);
+    k_restrict_to32<float><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+}
+
+void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c) {
+    const Range2 r = interior(coarse.L);
+    k_restrict_to32<double><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+}
+
+void launch_prolong32(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, float* ef, int Vbc) {
+    const Range2 r = interior(fine.L);
+    k_prolong_add<float><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
+}
+
+void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, double* S,
+                           int Vbc) {
+    const Range2 r = interior(fine.L);
+    k_prolong_add<double><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, S, Vbc); tc_note_launch();
+}
+
+void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32) {
+    const Range2 r = interior(lv.L);
+    k_residual_to32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef, lv.rhs, rhs32); tc_note_launch();
+}
+
+void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc) {
+    const Range2 r = interior(lv.L);
+    k_update64<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, e, Vbc); tc_note_launch();
+}
+
+void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
+                           int Vbc) {
+    const int threads = 256;
+    const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
+    k_coarse_apply32<<<nb, threads, 0, s>>>(lv.L, Ainv, rowb, lv.rhs32, n, err, Vbc); tc_note_launch();
+}

@@ -84,6 +84,9 @@ struct Handle {
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
     double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
     int ctab_level = 0;        // level the table was built for (0 = none)
+    float* ctab32 = nullptr;   // the same for the FP32 smoother of the mixed solve
+    int ctab32_level = 0;
+    cudaError_t enq_err = cudaSuccess;  // first error of an enqueue-only helper (checked by its caller)
 };
 
 #define CK(call)                                                      \
@@ -93,6 +96,11 @@ struct Handle {
             h->err = std::string(#call) + ": " + cudaGetErrorString(e_); \
             return TC_ERR_CUDA;                                       \
         }                                                             \
+    } while (0)
+#define CKV(call)                                                    \
+    do {                                                             \
+        cudaError_t e_ = (call);                                     \
+        if (e_ != cudaSuccess && h->enq_err == cudaSuccess) h->enq_err = e_; \
     } while (0)
 #define TRY(x)                    \
     do {                          \
@@ -388,6 +396,76 @@ void enqueue_cycle_rest(Handle* h) {
     }
 }
 
+// ---- mixed precision (solver_precision = 1) --------------------------------
+float* cur_e32(Handle* h, int l) { return h->lev[l].e32[h->lev[l].e32cur]; }
+
+// iterate_stream on the FP32 correction of `level` (same sweeps and factors
+// as iterate_stream); level 1 skips the FP32 residual (its residual is FP64).
+void iterate_stream32(Handle* h, int level, int dir) {
+    Level& lv = h->lev[level];
+    const int Niter = h->p.Nmulti;
+    const bool cheb_pp = (level == h->ratio_level);
+    const int pp = (dir != 1 && cheb_pp) ? 1 : 0;
+    if (h->fuse_visits && level > 1 && Niter <= 128) {
+        double cv[128], tv[128];
+        cheb_temps(Niter, dir, tv, cv);
+        if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, (h->ctab32_level == level) ? h->ctab32 : nullptr,
+                                   Niter, pp, h->p.Vbc) == 0)
+            return;
+    }
+    for (int n = 1; n <= Niter; n++) {
+        const double ntemp = (double)(Niter - n + 1);
+        const double la = -1.0, lb = -2.0;
+        const double temp = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
+        double c = 1.0;
+        if (dir != 1 && !cheb_pp) c = 2.0 / (-lb - la + (lb - la) * temp);
+        launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], (float)c, pp, (float)temp, h->p.Vbc);
+        lv.e32cur = 1 - lv.e32cur;
+    }
+    if (Niter % 2 == 1) {
+        CKV(cudaMemcpyAsync(lv.e32[1 - lv.e32cur], lv.e32[lv.e32cur], sizeof(float) * lv.L.plane,
+                            cudaMemcpyDeviceToDevice, h->st));
+        lv.e32cur = 1 - lv.e32cur;
+    }
+    if (level > 1) launch_residual32(h->st, lv, cur_e32(h, level));
+}
+
+// level-1 visit of the mixed solve: r = RHS - L psi (FP64) -> FP32 RHS,
+// correction from zero, psi += e (FP64), FP64 residual and its L1 mean
+void enqueue_l1_mixed(Handle* h, int dir) {
+    Level& l1 = h->lev[1];
+    launch_residual_to32(h->st, l1, cur_err(h, 1), l1.rhs32);
+    CKV(cudaMemsetAsync(cur_e32(h, 1), 0, sizeof(float) * l1.L.plane, h->st));
+    iterate_stream32(h, 1, dir);
+    launch_update64(h->st, l1, cur_err(h, 1), cur_e32(h, 1), h->p.Vbc);
+    launch_residual(h->st, l1, cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+}
+
+// p = 2..nsteps of the mixed solve (enqueue_cycle_rest on FP32 corrections)
+void enqueue_rest_mixed(Handle* h, int) {
+    const int G = h->grids;
+    for (int pp = 2; pp <= h->nsteps; pp++) {
+        const int level = h->multi[pp];
+        const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
+        const bool down = h->multi[pp - 1] < h->multi[pp];
+        if (down && level > 1 && level < G && h->p.mg_zero_coarse)
+            CKV(cudaMemsetAsync(cur_e32(h, level), 0, sizeof(float) * h->lev[level].L.plane, h->st));
+        if (down && level == 2)
+            launch_restrict64to32(h->st, h->lev[2], h->lev[1], h->lev[1].res, h->lev[2].rhs32);
+        else if (down && level > 2)
+            launch_restrict32(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res32, h->lev[level].rhs32);
+        if (level < G) iterate_stream32(h, level, dir);
+        else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_e32(h, G), h->p.Vbc);
+        if (h->multi[pp + 1] < h->multi[pp]) {
+            if (level == 2)
+                launch_prolong_into64(h->st, h->lev[2], h->lev[1], cur_e32(h, 2), cur_err(h, 1), h->p.Vbc);
+            else
+                launch_prolong32(h->st, h->lev[level], h->lev[level - 1], cur_e32(h, level), cur_e32(h, level - 1),
+                                 h->p.Vbc);
+        }
+    }
+}
+
 // Graph of a replayable sequence; rebuilt when the inputs it bakes in change.
 struct CycleGraphs {
     cudaGraphExec_t l1 = nullptr, rest = nullptr;
@@ -402,6 +480,10 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     fn(h, arg);
     CK(cudaStreamEndCapture(h->st, &g));
+    if (h->enq_err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        CK(h->enq_err);
+    }
     *nkernels = g_launches.load() - before;
     g_launches.fetch_sub(*nkernels);  // capturing enqueues nothing
     cudaError_t e = cudaGraphInstantiate(out, g, 0);
@@ -421,9 +503,21 @@ tc_status multigrid(Handle* h) {
     for (int l = 1; l <= G; l++) TRY(compute_viscosity(h, l));
     for (int l = 1; l <= G; l++)
         launch_level_coefs(h->st, h->lev[l], cur_vis(h, l), h->p.ivis, h->p.courant_stream, l == h->ratio_level ? 1 : 0);
+    const bool mixed = (h->p.solver_precision == 1);
+    if (mixed) {
+        for (int l = 1; l < G; l++) launch_level_to_f32(h->st, h->lev[l], l == h->ratio_level ? 1 : 0);
+        h->ctab32_level = 0;
+        if (h->ctab32 && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
+            visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti, 1)) {
+            double cv[128], tv[128];
+            cheb_temps(h->p.Nmulti, 0, tv, cv);
+            launch_cheb_table32(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab32);
+            h->ctab32_level = h->ratio_level;
+        }
+    }
     h->ctab_level = 0;
-    if (h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
-        visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti)) {
+    if (!mixed && h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
+        visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti, 0)) {
         double cv[128], tv[128];
         cheb_temps(h->p.Nmulti, 0, tv, cv);
         launch_cheb_table(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab);
@@ -443,13 +537,16 @@ tc_status multigrid(Handle* h) {
     const int dir1 = (h->multi[2] > h->multi[1]) ? 0 : 1;
     CycleGraphs& cg = *h->graphs;
     const bool use_graphs = (h->st != nullptr) && !h->no_graphs;
+    void (*f_l1)(Handle*, int) = mixed ? enqueue_l1_mixed : enqueue_l1;
+    void (*f_rest)(Handle*, int) = mixed ? enqueue_rest_mixed : enqueue_rest;
+    h->enq_err = cudaSuccess;
     if (use_graphs && (cg.l1 == nullptr || cg.ratio_level != h->ratio_level || cg.zero != h->p.mg_zero_coarse ||
                        cg.dir1 != dir1 || cg.st != h->st)) {
         if (cg.l1) cudaGraphExecDestroy(cg.l1);
         if (cg.rest) cudaGraphExecDestroy(cg.rest);
         cg.l1 = cg.rest = nullptr;
-        TRY(capture(h, &cg.l1, enqueue_l1, dir1, &cg.n_l1));
-        TRY(capture(h, &cg.rest, enqueue_rest, 0, &cg.n_rest));
+        TRY(capture(h, &cg.l1, f_l1, dir1, &cg.n_l1));
+        TRY(capture(h, &cg.rest, f_rest, 0, &cg.n_rest));
         cg.ratio_level = h->ratio_level;
         cg.zero = h->p.mg_zero_coarse;
         cg.dir1 = dir1;
@@ -458,13 +555,15 @@ tc_status multigrid(Handle* h) {
     int q = 1;
     for (;;) {
         if (use_graphs) { CK(cudaGraphLaunch(cg.l1, h->st)); tc_note_launch(cg.n_l1); }
-        else iterate_stream(h, 1, dir1);
+        else f_l1(h, dir1);
+        CK(h->enq_err);
         TRY(sync_scalars(h));
         const double rm = h->hs->res_mag[1];
         if (rm > 1.0e10 * res_ref1) return TC_ERR_MG_RESIDUAL;
         if (rm / res_ref1 <= h->p.tolerance) break;
         if (use_graphs) { CK(cudaGraphLaunch(cg.rest, h->st)); tc_note_launch(cg.n_rest); }
-        else enqueue_cycle_rest(h);
+        else f_rest(h, 0);
+        CK(h->enq_err);
         q = q + 1;
         if (q > h->p.max_cycles) { h->last_cycles = q; return TC_ERR_MG_CYCLES; }
     }
@@ -613,6 +712,7 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.grids < 2 || p.grids > 6) return TC_ERR_ARG;
     if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
+    if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;
     h->nx = p.nx; h->nz = p.nz; h->grids = p.grids;
     {
         const long nb = (long)((p.nx + 2 + BX - 1) / BX) * (long)((p.nz + 2 + BY - 1) / BY);
@@ -704,6 +804,7 @@ tc_status create(Handle* h, const tc_params* in) {
     TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
     if (h->fuse_visits) TRY(dalloc_t(h, &h->ctab, (size_t)128 * 4096));
+    if (h->fuse_visits && p.solver_precision == 1) TRY(dalloc_t(h, &h->ctab32, (size_t)128 * 16384));
     TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));
     TRY(dalloc_t(h, &h->rs.part, (size_t)4 * TC_MAX_RED_BLOCKS));
     TRY(dalloc_t(h, &h->rs.count, (size_t)8));
@@ -725,6 +826,14 @@ tc_status create(Handle* h, const tc_params* in) {
         for (double** q : lf) TRY(dalloc_t(h, q, lp));
         for (int q = 0; q < 6; q++) TRY(dalloc_t(h, &lv.bak[q], lp));
         TRY(dalloc_t(h, &lv.coef, lp * TC_NCOEF));
+        lv.coef32 = lv.dts32 = lv.cA32 = lv.cB32 = lv.rhs32 = lv.res32 = nullptr;
+        lv.e32[0] = lv.e32[1] = nullptr;
+        lv.e32cur = 0;
+        if (p.solver_precision == 1) {
+            TRY(dalloc_t(h, &lv.coef32, lp * TC_NCOEF));
+            float** f32[] = {&lv.dts32, &lv.cA32, &lv.cB32, &lv.rhs32, &lv.res32, &lv.e32[0], &lv.e32[1]};
+            for (float** q : f32) TRY(dalloc_t(h, q, lp));
+        }
         tcs::LevSpacing s;
         tcs::level_spacing(p.aspect, lv.L.a, lv.L.b, s);
         LevConst& c = lv.c;
@@ -1053,12 +1162,16 @@ tc_status tc_time_sweep(tc_handle* H, int32_t level, int32_t nsweeps, double* ms
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    // sweeps read lv.err[cur] and write the other buffer; the state is untouched
-    double* in = lv.err[lv.ecur];
-    double* out = lv.err[1 - lv.ecur];
-    launch_sweep(h->st, lv, in, out, 1.0, 0, 0.0, h->p.Vbc);
+    // sweeps read the current buffer and write the other one; the state is
+    // untouched.  The mixed solve times its FP32 smoother kernel.
+    const bool mixed = (h->p.solver_precision == 1);
+    auto sweep = [&]() {
+        if (mixed) launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], 1.0f, 0, 0.0f, h->p.Vbc);
+        else launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], 1.0, 0, 0.0, h->p.Vbc);
+    };
+    sweep();
     CK(cudaEventRecord(e0, h->st));
-    for (int n = 0; n < nsweeps; n++) launch_sweep(h->st, lv, in, out, 1.0, 0, 0.0, h->p.Vbc);
+    for (int n = 0; n < nsweeps; n++) sweep();
     CK(cudaEventRecord(e1, h->st));
     CK(cudaEventSynchronize(e1));
     float ms = 0.f;
@@ -1066,6 +1179,35 @@ tc_status tc_time_sweep(tc_handle* H, int32_t level, int32_t nsweeps, double* ms
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_sweep = (double)ms / nsweeps;
+    return TC_OK;
+}
+
+tc_status tc_time_visit(tc_handle* H, int32_t level, int32_t reps, double* ms_per_visit) {
+    if (!H || !ms_per_visit || reps < 1) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    if (level < 1 || level >= h->grids) return TC_ERR_ARG;
+    const bool mixed = (h->p.solver_precision == 1);
+    auto visit = [&]() {
+        if (level == 1 && mixed) enqueue_l1_mixed(h, 0);
+        else if (mixed) iterate_stream32(h, level, 0);
+        else iterate_stream(h, level, 0);
+    };
+    h->enq_err = cudaSuccess;
+    visit();
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, h->st));
+    for (int n = 0; n < reps; n++) visit();
+    CK(cudaEventRecord(e1, h->st));
+    CK(cudaEventSynchronize(e1));
+    CK(h->enq_err);
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_visit = (double)ms / reps;
     return TC_OK;
 }
 

@@ -100,3 +100,63 @@ struct CPtrs {
 struct CPtrsW {
     double* p[TC_MAX_TYPES];
 };
+
+// ---------------------------------------------------------------------------
+// Stencil helpers shared by the FP64 kernels (reference arithmetic) and their
+// FP32 instances in the mixed-precision solve.
+// ---------------------------------------------------------------------------
+
+// full-weighting restriction at fine point (ii,kk); the corner term repeats
+// (ii-1,kk+1) and omits (ii+1,kk-1), as iterative_solver.f90:607
+template <typename T>
+__device__ __forceinline__ T restrict9(const T* __restrict__ in, const Lay& F, int ii, int kk) {
+    T corners = (in[IX(F, ii - 1, kk - 1)] + in[IX(F, ii - 1, kk + 1)] + in[IX(F, ii + 1, kk + 1)] +
+                 in[IX(F, ii - 1, kk + 1)]) / T(16);
+    T sides = (in[IX(F, ii - 1, kk)] + in[IX(F, ii, kk - 1)] + in[IX(F, ii + 1, kk)] + in[IX(F, ii, kk + 1)]) / T(8);
+    T centre = in[IX(F, ii, kk)] / T(4);
+    return corners + sides + centre;
+}
+
+// rhs - L S at x with the 13 folded coefficient planes (stream_space with
+// the Database=2 order-2 stencil, iterative_solver.f90:456-561)
+template <typename T>
+__device__ __forceinline__ T folded_residual(const Lay& L, const T* __restrict__ S, const T* __restrict__ coef, T rhs,
+                                             size_t x) {
+    const size_t ld = (size_t)L.ld, pl = L.plane;
+    const T* cf = coef + x;
+    T acc = rhs;
+    acc = fma(-__ldg(cf + 0 * pl), __ldg(S + x), acc);
+    acc = fma(-__ldg(cf + 1 * pl), __ldg(S + x - 1), acc);
+    acc = fma(-__ldg(cf + 2 * pl), __ldg(S + x + 1), acc);
+    acc = fma(-__ldg(cf + 3 * pl), __ldg(S + x - 2), acc);
+    acc = fma(-__ldg(cf + 4 * pl), __ldg(S + x + 2), acc);
+    acc = fma(-__ldg(cf + 5 * pl), __ldg(S + x - ld), acc);
+    acc = fma(-__ldg(cf + 6 * pl), __ldg(S + x + ld), acc);
+    acc = fma(-__ldg(cf + 7 * pl), __ldg(S + x - 2 * ld), acc);
+    acc = fma(-__ldg(cf + 8 * pl), __ldg(S + x + 2 * ld), acc);
+    acc = fma(-__ldg(cf + 9 * pl), __ldg(S + x - 1 - ld), acc);
+    acc = fma(-__ldg(cf + 10 * pl), __ldg(S + x + 1 - ld), acc);
+    acc = fma(-__ldg(cf + 11 * pl), __ldg(S + x - 1 + ld), acc);
+    acc = fma(-__ldg(cf + 12 * pl), __ldg(S + x + 1 + ld), acc);
+    return acc;
+}
+
+// writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
+// derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
+template <typename T>
+__device__ __forceinline__ void store_stream(const Lay& L, T* __restrict__ S, int i, int k, T v, int Vbc) {
+    const int a = L.a, b = L.b;
+    int gi[3] = {i, 0, 0};
+    T si[3] = {T(1), T(-1), T(-1)};
+    int ng = 1;
+    if (i <= SP) gi[ng++] = -i;
+    if (i >= a - SP) gi[ng++] = 2 * a - i;
+    int gk[3] = {k, 0, 0};
+    const T zsgn = (Vbc == 1) ? T(1) : T(-1);
+    T sk[3] = {T(1), zsgn, zsgn};
+    int nk = 1;
+    if (k <= SP) gk[nk++] = -k;
+    if (k >= b - SP) gk[nk++] = 2 * b - k;
+    for (int u = 0; u < nk; u++)
+        for (int t = 0; t < ng; t++) S[IX(L, gi[t], gk[u])] = (si[t] * sk[u]) * v;
+}

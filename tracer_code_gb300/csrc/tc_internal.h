@@ -84,6 +84,12 @@ struct Level {
     double* coef;    // TC_NCOEF planes
     double *cA, *cB; // Chebyshev denominators for the level with finite eigenvalue ratios
     LevConst c;
+    // FP32 copies for the mixed-precision solve (null unless solver_precision = 1):
+    // coefficients, pseudo-time step and Chebyshev denominators rounded from
+    // the FP64 ones; RHS, correction (two buffers) and residual in FP32
+    float *coef32, *dts32, *cA32, *cB32, *rhs32, *res32;
+    float* e32[2];
+    int e32cur;
 };
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
@@ -125,10 +131,28 @@ void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n)
 
 // (k_visit.cu) one whole smoother visit of a small level as one cluster launch
 int visit_cluster_setup();
-int visit_cluster_fits(const Lay& L, int nsweeps);
+int visit_cluster_fits(const Lay& L, int nsweeps, int fp32);
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab);
+void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab);
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* ctab,
                          int nsweeps, int per_point, int Vbc);
+int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const float* ctab,
+                           int nsweeps, int per_point, int Vbc);
+
+// (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
+void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
+void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
+                    float temp, int Vbc);
+void launch_residual32(cudaStream_t s, const Level& lv, const float* S);
+void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c);
+void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c);
+void launch_prolong32(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, float* ef, int Vbc);
+void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, double* S,
+                           int Vbc);
+void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32);
+void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc);
+void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
+                           int Vbc);
 void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
                  double* rhs, RedScratch rs, DevScalars* ds);
 
