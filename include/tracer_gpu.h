@@ -59,7 +59,9 @@ typedef enum tc_status {
     TC_ERR_ALLOC = 9,            /* device or host allocation failed                        */
     TC_ERR_STATE = 10,           /* call order violated (e.g. step before upload)           */
     TC_ERR_SINGULAR = 11,        /* zero pivot in the coarsest-grid banded LU (DGBTRF INFO>0) */
-    TC_ERR_TOO_LARGE = 12        /* input larger than the fixed buffer of an allocation-free call */
+    TC_ERR_TOO_LARGE = 12,       /* input larger than the fixed buffer of an allocation-free call */
+    TC_ERR_DEVICE_TIMEOUT = 13   /* a bounded wait inside a kernel gave up (the kernel returned; the
+                                    handle's results are invalid, the CUDA context stays usable) */
 } tc_status;
 
 /*

@@ -150,12 +150,16 @@ def test_full_steps_parity(gpu_lib):
     assert np.abs(a["str"] - b["str"]).max() <= 1e-10
 
 
-@pytest.mark.parametrize("zero", [0, 1])
-def test_fused_cluster_visits_match_per_sweep_launches(gpu_lib, zero, monkeypatch):
+@pytest.mark.parametrize("zero,prec,nx,nz,grids", [(0, 0, 128, 32, 4), (1, 0, 128, 32, 4), (1, 0, 256, 64, 5),
+                                                    (0, 1, 128, 32, 4), (1, 1, 256, 64, 5)])
+def test_fused_cluster_visits_match_per_sweep_launches(gpu_lib, zero, prec, nx, nz, grids, monkeypatch):
     """Small levels smoothed by one thread-block-cluster launch per visit give
-    the same multigrid state bit for bit as one launch per sweep."""
-    p = case_1024_like()
+    the same multigrid state bit for bit as one launch per sweep, in FP64 and
+    in the FP32 smoother of the mixed solve (one-CTA, multi-CTA and
+    two-rows-away halo exchanges all occur across these shapes)."""
+    p = case_1024_like(nx=nx, nz=nz, grids=grids, tpc=2)
     p.mg_zero_coarse = zero
+    p.solver_precision = prec
     st = fresh_state(p)
     out = []
     for env in (None, "1"):

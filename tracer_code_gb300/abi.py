@@ -24,6 +24,7 @@ STATUS = {
     10: "TC_ERR_STATE",
     11: "TC_ERR_SINGULAR",
     12: "TC_ERR_TOO_LARGE",
+    13: "TC_ERR_DEVICE_TIMEOUT",
 }
 
 # Reference `stop` messages that each status replaces.

@@ -3,21 +3,34 @@
 // sweeps with enforceBCs_stream after each, then compute_residual) in ONE
 // launch of a thread-block cluster.
 //
-// Why: below 16K points a sweep is latency bound (about 6.5 us per launch
-// whatever the size), and a W-cycle at 6 levels makes 24 visits x 70 sweeps
-// to the two smallest smoothed levels.  Here each CTA of a cluster (up to
-// 16) keeps a band of rows of the level in shared memory (two ping-pong
-// buffers with two halo rows on each side), every thread owns one point and
-// holds that point's 13 operator coefficients, RHS and pseudo-time step in
-// registers for the whole visit, stores the values its neighbours need as
-// halo directly into their shared memory (distributed shared memory, the
-// addresses resolved once before the first sweep), and the cluster meets at
-// one hardware barrier per sweep.  The per-point Chebyshev factor of the
-// level with finite eigenvalue ratios comes from a table built once per
-// multigrid call (k_cheb_table), so no FP64 division sits in the sweep.
-// The arithmetic per point is the same as k_sweep / k_residual (same folded
-// operator, same order, the same correctly rounded division for the table),
-// so the level ends in the same state bit for bit.
+// Why: below ~16K points a sweep is latency bound (several microseconds per
+// launch whatever the size), and a W-cycle at 6 levels makes 30 visits of
+// 70 sweeps to levels 3..5 alone.
+//
+// Layout.  The level's interior rows 1..b-1 are cut into bands of `rpc` rows,
+// one band per CTA of a cluster (up to 16 CTAs).  Each CTA keeps its band
+// plus two halo rows on each side in shared memory (ping-pong buffers; three
+// when the cluster has more than one CTA, see below).  Each thread owns a
+// vertical strip of P points of one column (rows r..r+P-1): it keeps their
+// 13 folded operator coefficients, RHS and pseudo-time step in registers
+// for the whole visit and loads the 5P+8 stencil values the strip needs
+// once per sweep (instead of 13P), so a sweep costs few shared-memory loads.
+//
+// Exchange.  After computing a sweep, a thread stores the values of its
+// points that are halo rows of a neighbouring CTA straight into that CTA's
+// next buffer with st.async, which signals the receiver's mbarrier with the
+// byte count; a CTA waits only for the bytes its own halo needs (no
+// cluster-wide barrier per sweep).  A neighbour can run at most one sweep
+// ahead (it needs this CTA's halo to start the next), so with three
+// buffers it never writes a buffer this CTA is still reading.  Every wait
+// is bounded: past the limit the kernel sets DevScalars.visit_timeout,
+// leaves the sweep loop on all threads and returns normally.
+//
+// Arithmetic per point is that of k_sweep / k_residual (same folded
+// operator taps in the same order, the Chebyshev factor from a table of the
+// same correctly rounded division; FP32 divides in the sweep exactly as
+// k_sweep32 does), so the level ends in the same state bit for bit as with
+// one launch per sweep; the FP32 instance is the smoother of the mixed solve.
 #include "tc_device.cuh"
 
 #include <cooperative_groups.h>
@@ -25,15 +38,16 @@
 namespace cg = cooperative_groups;
 
 #define VISIT_MAX_SWEEPS 128
-#define VISIT_THREADS 256
 #define VISIT_MAX_CLUSTER 16
 #define VISIT_SMEM_MAX (96 * 1024)
+#define VISIT_WAIT_LIMIT (1 << 20)
 
 template <typename T>
 struct VisitParams {
     Lay L;
-    int nsweeps, per_point, Vbc, nrows_max;
-    T c[VISIT_MAX_SWEEPS];
+    int nsweeps, per_point, Vbc, rpc;
+    T c[VISIT_MAX_SWEEPS];     // uniform Chebyshev/Richardson factor of sweep n
+    T temp[VISIT_MAX_SWEEPS];  // Chebyshev node of sweep n (per-point factor, FP32)
 };
 
 template <typename T>
@@ -41,13 +55,6 @@ struct ChebTemps {
     int nsweeps;
     T temp[VISIT_MAX_SWEEPS];
 };
-
-// rows k0..k1 of CTA `rank` out of C (interior rows 1..b-1 split evenly)
-__device__ __forceinline__ void band_of(int rank, int C, int b, int& k0, int& k1) {
-    const int nr = b - 1, base = nr / C, rem = nr % C;
-    k0 = 1 + rank * base + min(rank, rem);
-    k1 = k0 + base + (rank < rem ? 1 : 0) - 1;
-}
 
 // c(n, point) = 2 / (cA + cB*temp(n)) for the per-point Chebyshev level,
 // the expression k_sweep evaluates, stored as tab[n*(a-1)(b-1) + (i-1) + (k-1)(a-1)].
@@ -63,168 +70,356 @@ __global__ void k_cheb_table(Lay L, ChebTemps<T> Q, const T* __restrict__ cA, co
     }
 }
 
-// One visit; T = double reproduces the reference arithmetic, T = float is the
-// smoother of the mixed-precision solve.  NT threads per CTA, one point each.
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT) k_visit_cluster(VisitParams<T> P, T* __restrict__ Sg, const T* __restrict__ coef,
-                                                      const T* __restrict__ rhs, const T* __restrict__ dts,
-                                                      const T* __restrict__ ctab, T* __restrict__ res) {
+// ---- cluster shared-memory primitives ---------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, int rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void st_async(uint32_t raddr, float v, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];" ::"r"(raddr),
+                 "r"(__float_as_uint(v)), "r"(rbar)
+                 : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t raddr, double v, uint32_t rbar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];" ::"r"(raddr),
+                 "l"(__double_as_longlong(v)), "r"(rbar)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint32_t a, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(uint32_t a, int bytes) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(a), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t a, int parity) {
+    uint32_t ok;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2; "
+        "selp.u32 %0, 1, 0, p; }"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// One visit.  NT threads per CTA; thread t owns column i = 1 + t % (a-1),
+// strip j = t / (a-1) of its CTA's band (rows k0 + jP .. k0 + jP + P-1).
+// W is the shared-memory row stride (>= a+5, a compile-time class so the
+// stencil offsets fold into the load instructions).
+template <typename T, int P, int NT, int W>
+__global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __restrict__ Sg,
+                                                         const T* __restrict__ coef, const T* __restrict__ rhs,
+                                                         const T* __restrict__ dts, const T* __restrict__ ctab,
+                                                         const T* __restrict__ cA, const T* __restrict__ cB,
+                                                         T* __restrict__ res, int* __restrict__ timeout_flag) {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
-    const Lay& L = P.L;
-    const int a = L.a, b = L.b, W = a + 1 + 2 * SP;  // shared row: columns -SP..a+SP
-    int k0, k1;
-    band_of(me, C, b, k0, k1);
-    const int cnt = k1 - k0 + 1, R = P.nrows_max + 4;  // rows k0-2..k1+2 (buffer sized for the largest band)
+    const Lay& L = Q.L;
+    const int a = L.a, b = L.b;  // shared row: columns -SP..a+SP (W >= a + 1 + 2SP)
+    const int rpc = Q.rpc;
+    const int k0 = 1 + me * rpc, k1 = min(b - 1, k0 + rpc - 1);
+    // rows k0-2 .. k0+rpcp+1 with the band rounded up to whole strips, so the
+    // loads of a strip that runs past the band's last row stay inside the buffer
+    const int R = ((rpc + P - 1) / P) * P + 4;
+    const int nbuf = (C > 1) ? 3 : 2;
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    T* buf0 = reinterpret_cast<T*>(sm_raw);
-    T* buf1 = buf0 + (size_t)R * W;
-    const int tid = threadIdx.x, nth = blockDim.x;
-    const T zsgn = (P.Vbc == 1) ? T(1) : T(-1);
-    // load rows k0-2..k1+2 (ghosts and walls included) into both buffers
-    for (int t = tid; t < (cnt + 4) * W; t += nth) {
-        const int r = t / W, c = t % W;
-        const int k = k0 - 2 + r, i = c - SP;
-        T v = T(0);
-        if (k >= -SP && k <= b + SP) v = Sg[IX(L, i, k)];
-        buf0[(size_t)r * W + c] = v;
-        buf1[(size_t)r * W + c] = v;
-    }
-    // this thread's point (the launcher guarantees one point per thread at most)
-    const bool act = tid < cnt * (a - 1);
-    const int i = act ? 1 + tid % (a - 1) : 1, k = act ? k0 + tid / (a - 1) : k0;
-    const int r = k - k0 + 2;
-    const int xs = r * W + i + SP;
-    const size_t xg = IX(L, i, k);
-    const int npl = (a - 1) * (b - 1), gp = (i - 1) + (k - 1) * (a - 1);
-    T cf[TC_NCOEF];
-    T rh = T(0), dt = T(0);
-    if (act) {
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm_raw);  // 3 mbarriers (first 32 B)
+    T* buf = reinterpret_cast<T*>(sm_raw + 32);
+    const size_t bsz = (size_t)R * W;
+    const int tid = threadIdx.x;
+    const T zsgn = (Q.Vbc == 1) ? T(1) : T(-1);
+    // rows k0-2..k1+2 (ghosts, walls and halos) into every buffer; four
+    // independent global loads in flight per thread
+    {
+        const int wa = a + 1 + 2 * SP, n_el = (k1 - k0 + 5) * wa;
+        for (int t0 = tid; t0 < n_el; t0 += 4 * NT) {
+            T v[4];
 #pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++) cf[d] = -__ldg(coef + xg + (size_t)d * L.plane);
-        rh = __ldg(rhs + xg);
-        dt = __ldg(dts + xg);
-    } else {
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * NT;
+                const int r = t / wa, c = t % wa, k = k0 - 2 + r;
+                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? Sg[IX(L, c - SP, k)] : T(0);
+            }
 #pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++) cf[d] = T(0);
-    }
-    // local mirror targets: side ghost column (enforceBCs_stream antisymmetric
-    // walls) and the ghost row -1 / b+1 held as halo by the first / last CTA
-    const int side = (i <= SP) ? r * W + (-i + SP) : (i >= a - SP) ? r * W + (2 * a - i + SP) : -1;
-    const int grow = (k == 1) ? (r - 2) * W + i + SP : (k == b - 1) ? (r + 2) * W + i + SP : -1;
-    // halo rows of the neighbouring CTAs (at most two on each side)
-    // (slot j serves the CTA at offset d = -2, -1, +1, +2; null = not a halo row there)
-    T* rem0[4];
-    T* rem1[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const int d = (j < 2) ? j - 2 : j - 1, o = me + d;
-        rem0[j] = nullptr;
-        rem1[j] = nullptr;
-        if (o < 0 || o >= C || !act) continue;
-        int ok0, ok1;
-        band_of(o, C, b, ok0, ok1);
-        if ((k >= ok0 - 2 && k <= ok0 - 1) || (k >= ok1 + 1 && k <= ok1 + 2)) {
-            const int off = (k - ok0 + 2) * W + i + SP;
-            rem0[j] = cl.map_shared_rank(buf0, o) + off;
-            rem1[j] = cl.map_shared_rank(buf1, o) + off;
-        }
-    }
-    cl.sync();
-    for (int n = 0; n < P.nsweeps; n++) {
-        const T* cur = (n & 1) ? buf1 : buf0;
-        T* nxt = (n & 1) ? buf0 : buf1;
-        if (act) {
-            const T c = P.per_point ? __ldg(ctab + (size_t)n * npl + gp) : P.c[n];
-            // identical term order to folded_residual
-            T acc = rh;
-            acc = fma(cf[0], cur[xs], acc);
-            acc = fma(cf[1], cur[xs - 1], acc);
-            acc = fma(cf[2], cur[xs + 1], acc);
-            acc = fma(cf[3], cur[xs - 2], acc);
-            acc = fma(cf[4], cur[xs + 2], acc);
-            acc = fma(cf[5], cur[xs - W], acc);
-            acc = fma(cf[6], cur[xs + W], acc);
-            acc = fma(cf[7], cur[xs - 2 * W], acc);
-            acc = fma(cf[8], cur[xs + 2 * W], acc);
-            acc = fma(cf[9], cur[xs - 1 - W], acc);
-            acc = fma(cf[10], cur[xs + 1 - W], acc);
-            acc = fma(cf[11], cur[xs - 1 + W], acc);
-            acc = fma(cf[12], cur[xs + 1 + W], acc);
-            const T v = fma(c * dt, acc, cur[xs]);
-            nxt[xs] = v;
-            if (side >= 0) nxt[side] = -v;
-            if (grow >= 0) nxt[grow] = zsgn * v;
-#pragma unroll
-            for (int j = 0; j < 4; j++) {
-                T* q = (n & 1) ? rem0[j] : rem1[j];
-                if (q) *q = v;
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * NT;
+                if (t >= n_el) break;
+                const int r = t / wa, c = t % wa;
+                for (int q = 0; q < nbuf; q++) buf[q * bsz + (size_t)r * W + c] = v[u];
             }
         }
-        if (C == 1) __syncthreads();
-        else cl.sync();
     }
-    // final state: owned rows (with side ghosts) to global, then ghost rows
-    const T* fin = (P.nsweeps & 1) ? buf1 : buf0;
-    for (int t = tid; t < cnt * W; t += nth) {
-        const int rr = 2 + t / W, c = t % W;
-        Sg[IX(L, c - SP, k0 - 2 + rr)] = fin[(size_t)rr * W + c];
+    if (tid == 0 && C > 1) {
+        for (int q = 0; q < 3; q++) mbar_init(smem_addr(&bar[q]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // residual on owned points (halos are current after the last barrier)
-    if (act && res != nullptr) {
-        T acc = rh;
-        acc = fma(cf[0], fin[xs], acc);
-        acc = fma(cf[1], fin[xs - 1], acc);
-        acc = fma(cf[2], fin[xs + 1], acc);
-        acc = fma(cf[3], fin[xs - 2], acc);
-        acc = fma(cf[4], fin[xs + 2], acc);
-        acc = fma(cf[5], fin[xs - W], acc);
-        acc = fma(cf[6], fin[xs + W], acc);
-        acc = fma(cf[7], fin[xs - 2 * W], acc);
-        acc = fma(cf[8], fin[xs + 2 * W], acc);
-        acc = fma(cf[9], fin[xs - 1 - W], acc);
-        acc = fma(cf[10], fin[xs + 1 - W], acc);
-        acc = fma(cf[11], fin[xs - 1 + W], acc);
-        acc = fma(cf[12], fin[xs + 1 + W], acc);
-        res[xg] = acc;
+    // this thread's strip
+    const int cols = a - 1;
+    const int i = 1 + tid % cols, strip = tid / cols;
+    const int kr = k0 + strip * P;  // first row of the strip
+    const int r0 = kr - k0 + 2;     // its buffer row
+    const int cc = i + SP;          // buffer column
+    const int npl = cols * (b - 1);
+    bool act[P];
+    T cf[P][TC_NCOEF], rh[P], dt[P];
+    // FP32 evaluates the per-point Chebyshev factor 2/(cA + cB*temp) in the
+    // sweep (as k_sweep32 does); FP64 reads it from the table (a division in
+    // the sweep would dominate its FP64 pipe), prefetched two sweeps ahead
+    constexpr bool kDivide = (sizeof(T) == sizeof(float));
+    T ca[P], cbv[P];
+    // per-thread flags: the column has a mirrored side ghost; the strip holds
+    // row 1 or b-1 (ghost row -1 / b+1); the strip holds halo rows of another
+    // CTA (bit 4+j of point p: CTA me-2, me-1, me+1, me+2 for j = 0..3)
+    const bool has_side = (i <= SP || i >= a - SP);
+    const int side = (i <= SP) ? SP - i : 2 * a - i + SP;
+    bool has_grow = false;
+    int remote = 0;  // bit (4p + j)
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+        const int k = kr + p;
+        act[p] = (strip * P + p < rpc) && (tid < (NT / cols) * cols) && (k <= k1);
+        const size_t xg = IX(L, i, act[p] ? k : k0);
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) cf[p][d] = act[p] ? -__ldg(coef + xg + (size_t)d * L.plane) : T(0);
+        rh[p] = act[p] ? __ldg(rhs + xg) : T(0);
+        dt[p] = act[p] ? __ldg(dts + xg) : T(0);
+        ca[p] = (kDivide && Q.per_point && act[p]) ? __ldg(cA + xg) : T(1);
+        cbv[p] = (kDivide && Q.per_point && act[p]) ? __ldg(cB + xg) : T(0);
+        if (!act[p]) continue;
+        if (k == 1 || k == b - 1) has_grow = true;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const int o = me + ((j < 2) ? j - 2 : j - 1);
+            if (o < 0 || o >= C) continue;
+            const int ok0 = 1 + o * rpc, ok1 = min(b - 1, ok0 + rpc - 1);
+            if ((k >= ok0 - 2 && k <= ok0 - 1) || (k >= ok1 + 1 && k <= ok1 + 2)) remote |= 1 << (4 * p + j);
+        }
+    }
+    // bytes this CTA receives per sweep: its halo rows that other CTAs own
+    int expect = 0;
+    for (int k = k0 - 2; k <= k1 + 2; k++)
+        if ((k < k0 || k > k1) && k >= 1 && k <= b - 1) expect += cols * (int)sizeof(T);
+    cl.sync();  // buffers loaded and mbarriers initialised cluster-wide
+    int phase = 0;  // bit q: parity of mbarrier q's current phase
+    int cur_b = 0;
+    bool timed_out = false;
+    const size_t tab_base = (size_t)(i - 1) + (size_t)(kr - 1) * cols;
+    // table prefetch ring (FP64 per-point level): factors of sweeps n, n+1
+    T pre0[P], pre1[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+        const bool ld = !kDivide && Q.per_point && act[p];
+        pre0[p] = (ld && Q.nsweeps > 0) ? __ldg(ctab + tab_base + (size_t)p * cols) : T(0);
+        pre1[p] = (ld && Q.nsweeps > 1) ? __ldg(ctab + (size_t)npl + tab_base + (size_t)p * cols) : T(0);
+    }
+    for (int n = 0; n < Q.nsweeps; n++) {
+        const int nxt_b = (cur_b + 1 == nbuf) ? 0 : cur_b + 1;
+        const T* cur = buf + (size_t)cur_b * bsz;
+        T* nxt = buf + (size_t)nxt_b * bsz;
+        if (act[0]) {
+            T cp[P];
+            if (Q.per_point && kDivide) {
+                const T tn = Q.temp[n];
+#pragma unroll
+                for (int p = 0; p < P; p++) cp[p] = T(2) / (ca[p] + cbv[p] * tn);
+            } else if (Q.per_point) {
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    cp[p] = pre0[p];
+                    pre0[p] = pre1[p];
+                    pre1[p] = (act[p] && n + 2 < Q.nsweeps)
+                                  ? __ldg(ctab + (size_t)(n + 2) * npl + tab_base + (size_t)p * cols)
+                                  : T(0);
+                }
+            } else {
+                const T c = Q.c[n];
+#pragma unroll
+                for (int p = 0; p < P; p++) cp[p] = c;
+            }
+            // strip values: centre column rows r0-2..r0+P+1, columns i+-1 rows
+            // r0-1..r0+P, columns i+-2 rows r0..r0+P-1 (rows past the band are
+            // inside the padded buffer; their results are not stored)
+            const T* cb = cur + (size_t)r0 * W + cc;
+            T v0[P + 4], vm1[P + 2], vp1[P + 2], vm2[P], vp2[P];
+#pragma unroll
+            for (int q = 0; q < P + 4; q++) v0[q] = cb[(q - 2) * W];
+#pragma unroll
+            for (int q = 0; q < P + 2; q++) {
+                vm1[q] = cb[(q - 1) * W - 1];
+                vp1[q] = cb[(q - 1) * W + 1];
+            }
+#pragma unroll
+            for (int q = 0; q < P; q++) {
+                vm2[q] = cb[q * W - 2];
+                vp2[q] = cb[q * W + 2];
+            }
+            // folded_residual tap order per point: (0,0) (-1,0) (1,0) (-2,0)
+            // (2,0) (0,-1) (0,1) (0,-2) (0,2) (-1,-1) (1,-1) (-1,1) (1,1); the
+            // P chains are independent and interleave
+            T acc[P];
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][0], v0[p + 2], rh[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][1], vm1[p + 1], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][2], vp1[p + 1], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][3], vm2[p], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][4], vp2[p], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][5], v0[p + 1], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][6], v0[p + 3], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][7], v0[p], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][8], v0[p + 4], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][9], vm1[p], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][10], vp1[p], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][11], vm1[p + 2], acc[p]);
+#pragma unroll
+            for (int p = 0; p < P; p++) acc[p] = fma(cf[p][12], vp1[p + 2], acc[p]);
+            T v[P];
+#pragma unroll
+            for (int p = 0; p < P; p++) v[p] = fma(cp[p] * dt[p], acc[p], v0[p + 2]);
+            T* nb = nxt + (size_t)r0 * W + cc;
+#pragma unroll
+            for (int p = 0; p < P; p++)
+                if (act[p]) nb[p * W] = v[p];
+            if (has_side) {
+                T* ns = nxt + (size_t)r0 * W + side;
+#pragma unroll
+                for (int p = 0; p < P; p++)
+                    if (act[p]) ns[p * W] = -v[p];
+            }
+            if (has_grow) {
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+                    if (!act[p]) continue;
+                    if (kr + p == 1) nb[(p - 2) * W] = zsgn * v[p];
+                    if (kr + p == b - 1) nb[(p + 2) * W] = zsgn * v[p];
+                }
+            }
+            if (remote) {
+                const uint32_t nbar = smem_addr(&bar[nxt_b]);
+#pragma unroll
+                for (int p = 0; p < P; p++) {
+#pragma unroll
+                    for (int j = 0; j < 4; j++) {
+                        if (!(remote & (1 << (4 * p + j)))) continue;
+                        const int o = me + ((j < 2) ? j - 2 : j - 1);
+                        const int ok0 = 1 + o * rpc;
+                        const uint32_t dst = smem_addr(nxt + (size_t)(kr + p - ok0 + 2) * W + cc);
+                        st_async(cluster_addr(dst, o), v[p], cluster_addr(nbar, o));
+                    }
+                }
+            }
+        }
+        if (C > 1) {
+            if (tid == 0) mbar_arrive_expect(smem_addr(&bar[nxt_b]), expect);
+            __syncthreads();
+            int it = 0, to = 0;
+            while (!mbar_try_wait(smem_addr(&bar[nxt_b]), (phase >> nxt_b) & 1)) {
+                if (++it > VISIT_WAIT_LIMIT) { to = 1; break; }
+            }
+            phase ^= 1 << nxt_b;
+            if (__syncthreads_or(to)) { timed_out = true; break; }
+        } else {
+            __syncthreads();
+        }
+        cur_b = nxt_b;
+    }
+    if (timed_out) {
+        if (tid == 0) atomicExch(timeout_flag, 1);
+    } else {
+        // final state: owned rows (with side ghosts) to global, then the residual
+        const T* fin = buf + (size_t)cur_b * bsz;
+        const int wa = a + 1 + 2 * SP;
+        for (int t = tid; t < (k1 - k0 + 1) * wa; t += NT) {
+            const int rr = 2 + t / wa, c = t % wa;
+            Sg[IX(L, c - SP, k0 - 2 + rr)] = fin[(size_t)rr * W + c];
+        }
+        if (res != nullptr) {
+#pragma unroll
+            for (int p = 0; p < P; p++) {
+                if (!act[p]) continue;
+                const int r = r0 + p;
+                const size_t xs = (size_t)r * W + cc;
+                T acc = rh[p];
+                acc = fma(cf[p][0], fin[xs], acc);
+                acc = fma(cf[p][1], fin[xs - 1], acc);
+                acc = fma(cf[p][2], fin[xs + 1], acc);
+                acc = fma(cf[p][3], fin[xs - 2], acc);
+                acc = fma(cf[p][4], fin[xs + 2], acc);
+                acc = fma(cf[p][5], fin[xs - W], acc);
+                acc = fma(cf[p][6], fin[xs + W], acc);
+                acc = fma(cf[p][7], fin[xs - 2 * W], acc);
+                acc = fma(cf[p][8], fin[xs + 2 * W], acc);
+                acc = fma(cf[p][9], fin[xs - 1 - W], acc);
+                acc = fma(cf[p][10], fin[xs + 1 - W], acc);
+                acc = fma(cf[p][11], fin[xs - 1 + W], acc);
+                acc = fma(cf[p][12], fin[xs + 1 + W], acc);
+                res[IX(L, i, kr + p)] = acc;
+            }
+        }
     }
     __threadfence();
-    cl.sync();  // global rows written; no CTA leaves while others may touch its shared memory
+    cl.sync();  // global rows written; no CTA leaves while another may still address its shared memory
+    if (timed_out) return;
     // top/bottom ghost rows from the (now global) interior rows
     if (me == 0 || me == C - 1) {
-        for (int t = tid; t < 2 * W; t += nth) {
-            const int g = 1 + t / W, c = t % W, ii = c - SP;
-            if (me == 0) {
-                const T v = Sg[IX(L, ii, g)];
-                Sg[IX(L, ii, -g)] = zsgn * v;
-            }
-            if (me == C - 1) {
-                const T v = Sg[IX(L, ii, b - g)];
-                Sg[IX(L, ii, b + g)] = zsgn * v;
-            }
+        const int wa = a + 1 + 2 * SP;
+        for (int t = tid; t < 2 * wa; t += NT) {
+            const int g = 1 + t / wa, c = t % wa, ii = c - SP;
+            if (me == 0) Sg[IX(L, ii, -g)] = zsgn * Sg[IX(L, ii, g)];
+            if (me == C - 1) Sg[IX(L, ii, b + g)] = zsgn * Sg[IX(L, ii, b - g)];
         }
     }
 }
 
-template <typename T, int NT>
-static bool visit_attrs() {
-    if (cudaFuncSetAttribute(k_visit_cluster<T, NT>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
-        return false;
-    return cudaFuncSetAttribute(k_visit_cluster<T, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                VISIT_SMEM_MAX) == cudaSuccess;
+// ---- host side ----------------------------------------------------------------
+// shared-memory row-stride classes (a + 5 for a = 32..512, rounded to 8)
+#define VISIT_FOR_EACH_W(X) X(40) X(72) X(136) X(264) X(520)
+static int w_class(int a) {
+    const int need = a + 1 + 2 * SP;
+    const int cls[5] = {40, 72, 136, 264, 520};
+    for (int c : cls)
+        if (need <= c) return c;
+    return 0;
 }
 
-// Kernel attributes for clusters of up to 16 CTAs and 96 KB of shared memory;
-// returns how many 16-CTA clusters with that much shared memory can be
-// resident (0 = the fused visit is unavailable, callers use per-sweep launches).
+template <typename T, int P, int NT, int W>
+static bool visit_attrs1() {
+    auto k = k_visit_cluster<T, P, NT, W>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) return false;
+    return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, VISIT_SMEM_MAX) == cudaSuccess;
+}
+template <typename T, int P, int NT>
+static bool visit_attrs() {
+    bool ok = true;
+#define X(w) ok = ok && visit_attrs1<T, P, NT, w>();
+    VISIT_FOR_EACH_W(X)
+#undef X
+    return ok;
+}
+
+// Sets the kernel attributes; returns how many 16-CTA clusters of the
+// largest configuration can be resident (0 = fused visits unavailable).
 int visit_cluster_setup() {
-    if (!visit_attrs<double, 256>() || !visit_attrs<float, 256>() || !visit_attrs<float, 1024>()) {
+    if (!visit_attrs<double, 1, 256>() || !visit_attrs<float, 4, 256>() || !visit_attrs<float, 2, 512>()) {
         cudaGetLastError();
         return 0;
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(VISIT_MAX_CLUSTER, 1, 1);
-    cfg.blockDim = dim3(1024, 1, 1);
+    cfg.blockDim = dim3(512, 1, 1);
     cfg.dynamicSmemBytes = VISIT_SMEM_MAX;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -234,43 +429,55 @@ int visit_cluster_setup() {
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     int n = 0;
-    if (cudaOccupancyMaxActiveClusters(&n, k_visit_cluster<float, 1024>, &cfg) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveClusters(&n, k_visit_cluster<float, 2, 512, 520>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         return 0;
     }
     return n;
 }
 
-// Cluster size, threads per CTA and shared memory for a level, or 0 if the
-// level is not fused (more points than threads, too many sweeps or too
-// little shared memory).  FP64 uses 256 threads per CTA (13 coefficients in
-// registers need more than the 64 a 1024-thread CTA allows); FP32 takes 256
-// when that covers the level and 1024 otherwise.
-static int visit_shape(const Lay& L, int nsweeps, size_t esize, int* nt, int* rows_max, size_t* smem) {
-    const int a = L.a, b = L.b;
-    if (nsweeps > VISIT_MAX_SWEEPS || b - 1 < 2 || a - 1 < 1) return 0;
-    // as many CTAs as rows up to 16: fewer, fuller CTAs measured slower (the
-    // sweep is bound by shared-memory loads per CTA, not by the barrier)
-    const int C = (b - 1 < VISIT_MAX_CLUSTER) ? (b - 1) : VISIT_MAX_CLUSTER;
-    const int nr = b - 1, rm = nr / C + (nr % C ? 1 : 0);
-    int threads = 256;
-    if (rm * (a - 1) > threads) {
-        if (esize == sizeof(double)) return 0;
-        threads = 1024;
-        if (rm * (a - 1) > threads) return 0;
+struct VisitShape {
+    int C, rpc, nt, p, w;
+    size_t smem;
+};
+
+// FP32: strips of 4 points, as few CTAs as the columns allow (one CTA for a
+// level whose rows fit; the sweep is bound by per-CTA shared-memory loads and
+// the exchange, so fuller CTAs win).  FP64: strips of 1 point spread over up
+// to 16 CTAs (the FP64 pipe of each SM is the bound, so more SMs win).
+static bool visit_shape(const Lay& L, int nsweeps, bool fp32, VisitShape* s) {
+    const int cols = L.a - 1, rows = L.b - 1;
+    if (nsweeps > VISIT_MAX_SWEEPS || rows < 2 || cols < 1) return false;
+    s->w = w_class(L.a);
+    if (s->w == 0) return false;
+    if (fp32) {
+        // 512 threads in strips of 2 (four warps per scheduler hide the
+        // shared-memory and FMA latencies better than strips of 4 on 256)
+        s->p = 2;
+        s->nt = 512;
+        if (cols > s->nt) return false;
+        s->rpc = (s->nt / cols) * s->p;
+        s->C = (rows + s->rpc - 1) / s->rpc;
+    } else {
+        s->p = 1;
+        s->nt = 256;
+        int C = rows < VISIT_MAX_CLUSTER ? rows : VISIT_MAX_CLUSTER;
+        s->rpc = (rows + C - 1) / C;
+        s->C = (rows + s->rpc - 1) / s->rpc;
+        if (s->rpc * cols > s->nt) return false;
     }
-    const size_t sm = esize * 2 * (size_t)(rm + 4) * (size_t)(a + 1 + 2 * SP);
-    if (sm > VISIT_SMEM_MAX) return 0;
-    *nt = threads;
-    *rows_max = rm;
-    *smem = sm;
-    return C;
+    if (s->C > VISIT_MAX_CLUSTER) return false;
+    if (s->C == 1) s->rpc = rows;
+    const size_t esz = fp32 ? sizeof(float) : sizeof(double);
+    const int nbuf = (s->C > 1) ? 3 : 2;
+    const int rpcp = ((s->rpc + s->p - 1) / s->p) * s->p;
+    s->smem = 32 + esz * nbuf * (size_t)(rpcp + 4) * (size_t)s->w;
+    return s->smem <= VISIT_SMEM_MAX;
 }
 
 int visit_cluster_fits(const Lay& L, int nsweeps, int fp32) {
-    int nt, rm;
-    size_t sm;
-    return visit_shape(L, nsweeps, fp32 ? sizeof(float) : sizeof(double), &nt, &rm, &sm) > 0;
+    VisitShape s;
+    return visit_shape(L, nsweeps, fp32 != 0, &s) ? 1 : 0;
 }
 
 template <typename T>
@@ -285,51 +492,71 @@ static void cheb_table_t(cudaStream_t s, const Lay& L, const double* tvals, int 
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab) {
     cheb_table_t<double>(s, lv.L, tvals, nsweeps, lv.cA, lv.cB, tab);
 }
-void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab) {
-    cheb_table_t<float>(s, lv.L, tvals, nsweeps, lv.cA32, lv.cB32, tab);
-}
 
-template <typename T>
-static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* rhs, const T* dts, const T* ctab,
-                   T* res, const double* cvals, int nsweeps, int per_point, int Vbc) {
-    int nt, rows_max;
-    size_t smem;
-    const int C = visit_shape(L, nsweeps, sizeof(T), &nt, &rows_max, &smem);
-    if (C == 0) return 1;
-    if (per_point && ctab == nullptr) return 1;
-    VisitParams<T> P;
-    P.L = L;
-    P.nsweeps = nsweeps;
-    P.per_point = per_point;
-    P.Vbc = Vbc;
-    P.nrows_max = rows_max;
-    for (int n = 0; n < nsweeps; n++) P.c[n] = (T)cvals[n];
+template <typename T, int P, int NT>
+static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const VisitParams<T>& Q, T* S, const T* coef,
+                                const T* rhs, const T* dts, const T* ctab, const T* cA, const T* cB, T* res,
+                                int* flag) {
+    void (*kern)(VisitParams<T>, T*, const T*, const T*, const T*, const T*, const T*, const T*, T*, int*) = nullptr;
+    switch (sh.w) {
+#define X(w) \
+    case w: kern = k_visit_cluster<T, P, NT, w>; break;
+        VISIT_FOR_EACH_W(X)
+#undef X
+        default: return cudaErrorInvalidValue;
+    }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)C, 1, 1);
-    cfg.blockDim = dim3((unsigned)nt, 1, 1);
-    cfg.dynamicSmemBytes = smem;
+    cfg.gridDim = dim3((unsigned)sh.C, 1, 1);
+    cfg.blockDim = dim3((unsigned)NT, 1, 1);
+    cfg.dynamicSmemBytes = sh.smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.x = (unsigned)sh.C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
+}
+
+template <typename T>
+static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* rhs, const T* dts, const T* ctab,
+                   const T* cA, const T* cB, T* res, const double* cvals, const double* tvals, int nsweeps,
+                   int per_point, int Vbc, int* flag) {
+    VisitShape sh;
+    if (!visit_shape(L, nsweeps, sizeof(T) == sizeof(float), &sh)) return 1;
+    if (per_point && sizeof(T) == sizeof(double) && ctab == nullptr) return 1;
+    VisitParams<T> Q;
+    Q.L = L;
+    Q.nsweeps = nsweeps;
+    Q.per_point = per_point;
+    Q.Vbc = Vbc;
+    Q.rpc = sh.rpc;
+    for (int n = 0; n < nsweeps; n++) {
+        Q.c[n] = (T)cvals[n];
+        Q.temp[n] = (T)tvals[n];
+    }
     cudaError_t e;
-    if (nt == 256) e = cudaLaunchKernelEx(&cfg, k_visit_cluster<T, 256>, P, S, coef, rhs, dts, ctab, res);
-    else e = cudaLaunchKernelEx(&cfg, k_visit_cluster<T, 1024>, P, S, coef, rhs, dts, ctab, res);
+    if constexpr (sizeof(T) == sizeof(double)) {
+        e = visit_launch<T, 1, 256>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
+    } else {
+        if (sh.p == 4) e = visit_launch<T, 4, 256>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
+        else e = visit_launch<T, 2, 512>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
+    }
     if (e != cudaSuccess) return 2;
     tc_note_launch();
     return 0;
 }
 
 // Returns 0 if the level was handled here (caller skips the per-sweep path).
-int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* ctab,
-                         int nsweeps, int per_point, int Vbc) {
-    return visit_t<double>(s, lv.L, S, lv.coef, lv.rhs, lv.dt_stream, ctab, lv.res, cvals, nsweeps, per_point, Vbc);
+int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
+                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag) {
+    return visit_t<double>(s, lv.L, S, lv.coef, lv.rhs, lv.dt_stream, ctab, lv.cA, lv.cB, lv.res, cvals, tvals,
+                           nsweeps, per_point, Vbc, timeout_flag);
 }
-int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const float* ctab,
-                           int nsweeps, int per_point, int Vbc) {
-    return visit_t<float>(s, lv.L, S, lv.coef32, lv.rhs32, lv.dts32, ctab, lv.res32, cvals, nsweeps, per_point, Vbc);
+int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
+                           int nsweeps, int per_point, int Vbc, int* timeout_flag) {
+    return visit_t<float>(s, lv.L, S, lv.coef32, lv.rhs32, lv.dts32, nullptr, lv.cA32, lv.cB32, lv.res32, cvals,
+                          tvals, nsweeps, per_point, Vbc, timeout_flag);
 }

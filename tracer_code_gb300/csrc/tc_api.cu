@@ -84,8 +84,6 @@ struct Handle {
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
     double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
     int ctab_level = 0;        // level the table was built for (0 = none)
-    float* ctab32 = nullptr;   // the same for the FP32 smoother of the mixed solve
-    int ctab32_level = 0;
     cudaError_t enq_err = cudaSuccess;  // first error of an enqueue-only helper (checked by its caller)
 };
 
@@ -346,8 +344,8 @@ void iterate_stream(Handle* h, int level, int dir) {
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
         const int pp = (dir != 1 && cheb_pp) ? 1 : 0;
-        if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, (h->ctab_level == level) ? h->ctab : nullptr, Niter,
-                                 pp, h->p.Vbc) == 0)
+        if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, tv, (h->ctab_level == level) ? h->ctab : nullptr,
+                                 Niter, pp, h->p.Vbc, &h->ds->visit_timeout) == 0)
             return;
     }
     for (int n = 1; n <= Niter; n++) {
@@ -409,8 +407,8 @@ void iterate_stream32(Handle* h, int level, int dir) {
     if (h->fuse_visits && level > 1 && Niter <= 128) {
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
-        if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, (h->ctab32_level == level) ? h->ctab32 : nullptr,
-                                   Niter, pp, h->p.Vbc) == 0)
+        if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, tv, Niter, pp, h->p.Vbc,
+                                   &h->ds->visit_timeout) == 0)
             return;
     }
     for (int n = 1; n <= Niter; n++) {
@@ -506,14 +504,6 @@ tc_status multigrid(Handle* h) {
     const bool mixed = (h->p.solver_precision == 1);
     if (mixed) {
         for (int l = 1; l < G; l++) launch_level_to_f32(h->st, h->lev[l], l == h->ratio_level ? 1 : 0);
-        h->ctab32_level = 0;
-        if (h->ctab32 && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
-            visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti, 1)) {
-            double cv[128], tv[128];
-            cheb_temps(h->p.Nmulti, 0, tv, cv);
-            launch_cheb_table32(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab32);
-            h->ctab32_level = h->ratio_level;
-        }
     }
     h->ctab_level = 0;
     if (!mixed && h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
@@ -529,6 +519,7 @@ tc_status multigrid(Handle* h) {
         launch_coarse_inverse(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ainv, h->bvec);
         h->lu_valid = true;
     }
+    CK(cudaMemsetAsync(&h->ds->visit_timeout, 0, sizeof(int), h->st));
     TRY(sync_scalars(h));
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     const double res_ref1 = h->hs->res_ref;
@@ -558,6 +549,10 @@ tc_status multigrid(Handle* h) {
         else f_l1(h, dir1);
         CK(h->enq_err);
         TRY(sync_scalars(h));
+        if (h->hs->visit_timeout) {
+            h->err = "fused smoother visit: neighbour wait exceeded its bound";
+            return TC_ERR_DEVICE_TIMEOUT;
+        }
         const double rm = h->hs->res_mag[1];
         if (rm > 1.0e10 * res_ref1) return TC_ERR_MG_RESIDUAL;
         if (rm / res_ref1 <= h->p.tolerance) break;
@@ -804,7 +799,6 @@ tc_status create(Handle* h, const tc_params* in) {
     TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
     if (h->fuse_visits) TRY(dalloc_t(h, &h->ctab, (size_t)128 * 4096));
-    if (h->fuse_visits && p.solver_precision == 1) TRY(dalloc_t(h, &h->ctab32, (size_t)128 * 16384));
     TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));
     TRY(dalloc_t(h, &h->rs.part, (size_t)4 * TC_MAX_RED_BLOCKS));
     TRY(dalloc_t(h, &h->rs.count, (size_t)8));

@@ -63,7 +63,8 @@ struct DevScalars {
     int    flag_outside;     // tracer outside the domain
     int    flag_rk2;         // RK2 precondition failed
     int    lu_info;          // first zero pivot of the coarse LU (0 = none)
-    int    pad[2];
+    int    visit_timeout;    // a fused visit's bounded neighbour wait gave up
+    int    pad;
 };
 
 // Reduction scratch: per-block partials plus a completion counter.
@@ -133,11 +134,10 @@ void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n)
 int visit_cluster_setup();
 int visit_cluster_fits(const Lay& L, int nsweeps, int fp32);
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab);
-void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab);
-int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* ctab,
-                         int nsweeps, int per_point, int Vbc);
-int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const float* ctab,
-                           int nsweeps, int per_point, int Vbc);
+int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
+                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag);
+int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
+                           int nsweeps, int per_point, int Vbc, int* timeout_flag);
 
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
