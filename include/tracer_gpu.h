@@ -128,7 +128,11 @@ typedef struct tc_params {
      * stays FP64.  The tolerance test is the reference's, so the solution
      * meets the same relative residual; cycle counts may differ. */
     int32_t solver_precision;
-    int32_t reserved_[2];
+    /* No reference counterpart.  1 = start each multigrid solve from the
+     * attached network's guess (tracer_nn.h) when its level-1 residual is
+     * below that of the previous streamfunction; 0 = always from the latter. */
+    int32_t learned_guess;
+    int32_t reserved_[1];
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat

@@ -1,6 +1,7 @@
 """The C-ABI library loads on a machine without a GPU and exports every
-function include/tracer_gpu.h declares; ctypes structs match the C layout.
-No compute call is made here."""
+function include/*.h declares (tracer_gpu.h: the solver, tracer_nn.h: the
+learned guess); ctypes structs match the C layout.  No compute call is made
+here."""
 import ctypes as C
 import os
 import re
@@ -21,9 +22,14 @@ def lib():
 
 
 def header_functions():
-    txt = open(os.path.join(ROOT, "include", "tracer_gpu.h")).read()
-    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
-    return sorted(set(re.findall(r"\b(tc_[a-z_0-9]+)\s*\(", txt)))
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        txt = re.sub(r"/\*.*?\*/", "", open(os.path.join(inc, f)).read(), flags=re.S)
+        names |= set(re.findall(r"\b((?:tc|tcnn)_[a-z_0-9]+)\s*\(", txt))
+    return sorted(names)
 
 
 def test_header_declares_the_drop_in_entry_points():

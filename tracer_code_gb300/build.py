@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtracer_gpu.so")
 
-SOURCES = ["k_mg.cu", "k_visit.cu", "k_mixed.cu", "k_field.cu", "k_tracer.cu", "k_noalloc.cu", "tc_api.cu", "tc_setup.cpp"]
+SOURCES = ["k_mg.cu", "k_visit.cu", "k_mixed.cu", "k_conv.cu", "k_nn.cu", "tc_nn_api.cu", "k_field.cu", "k_tracer.cu", "k_noalloc.cu", "tc_api.cu", "tc_setup.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -44,7 +44,8 @@ def common_flags() -> list[str]:
 
 def _deps(src: str) -> list[str]:
     hdrs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    return [os.path.join(CSRC, src), os.path.join(INCLUDE, "tracer_gpu.h")] + hdrs
+    pub = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    return [os.path.join(CSRC, src)] + pub + hdrs
 
 
 def _compile(src: str, force: bool) -> str:

@@ -1,0 +1,206 @@
+// k_conv.cu -- 3x3 convolution (stride 1, zero padding 1) of NHWC BF16
+// tensors as an implicit GEMM on the 5th-generation tensor cores.
+//
+// GEMM view: M = 128 output pixels of one tile (BX x BY pixels of one
+// image), N = output channels (32..256, TMEM columns), K = 9 taps x input
+// channels.  One K stage is one tap and KC input channels: the activation
+// operand is KC/8 TMA boxes {8 channels, BX, BY} taken at the tap's pixel
+// offset (out-of-image rows and columns are zero-filled by the TMA unit,
+// which is the convolution's zero padding), the weight operand is one bulk
+// copy of a pre-packed [KC/8][N][8] slab.  A four-stage ring of shared
+// buffers overlaps the copies with the MMAs: thread 0 issues the copies,
+// thread 32 the tcgen05.mma instructions (KC/16 per stage) and commits each
+// stage's release and, at the end, the accumulator's completion; then the
+// four warps read their 32 TMEM lanes (pixels), add the bias, apply ReLU and
+// store BF16 at a channel offset of the output tensor (so a layer can write
+// into one half of a concatenation buffer).  Every wait is bounded; past the
+// bound the kernel records a failure flag and skips its remaining work.
+#include "nn_conv.cuh"
+#include "tc_nn.h"
+
+#include <cstdio>
+#include <cudaTypedefs.h>
+
+namespace nn {
+
+constexpr int kStages = 4;
+
+struct ConvArgs {
+    int nb, H, W;              // batch, image height and width
+    int bx, by;                // tile: bx * by = 128 pixels
+    int cin, cin_off;          // input channels (multiple of 16) and their first channel in the input tensor
+    int kc;                    // channels per K stage (16, 32 or 64)
+    int cout_store, cout_off, cout_tot;  // channels stored, their offset and the output tensor's channel count
+    int relu;
+    const __nv_bfloat16* wpack;  // [9][cin/kc][kc/8][N][8]
+    const float* bias;           // [N] or null
+    __nv_bfloat16* out;
+    int* fail;
+};
+
+template <int N>
+__global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done;
+    __shared__ uint32_t tmem_base;
+    __shared__ int bad;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int a_bytes = a.kc * 256;        // 128 rows x kc channels x 2 B
+    const int b_bytes = N * a.kc * 2;
+    const int st_bytes = a_bytes + b_bytes;
+    const int nchunk = a.cin / a.kc, nsteps = 9 * nchunk;
+    // tile coordinates
+    const int tiles_x = a.W / a.bx, tiles_y = a.H / a.by;
+    int t = blockIdx.x;
+    const int tx = t % tiles_x;
+    t /= tiles_x;
+    const int ty = t % tiles_y;
+    const int n = t / tiles_y;
+    const int x0 = tx * a.bx, y0 = ty * a.by;
+    if (tid == 0) {
+        bad = 0;
+        for (int s = 0; s < kStages; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tmem_base)),
+                     "r"(N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_base;
+
+    if (tid == 0) {
+        // producer: stage s of step i holds tap i / nchunk, channel chunk i % nchunk
+        for (int i = 0; i < nsteps; i++) {
+            const int s = i % kStages;
+            if (i >= kStages && !mbar_wait(&empty[s], ((i / kStages) - 1) & 1)) { bad = 1; break; }
+            const int tap = i / nchunk, ch = i % nchunk;
+            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+            unsigned char* As = smem + (size_t)s * st_bytes;
+            unsigned char* Bs = As + a_bytes;
+            mbar_expect_tx(&full[s], (uint32_t)st_bytes);
+            for (int j = 0; j < a.kc / 8; j++)
+                tma_load4(As + j * 2048, &xmap, a.cin_off + ch * a.kc + j * 8, x0 + dx, y0 + dy, n, &full[s]);
+            bulk_load(Bs, a.wpack + (size_t)i * N * a.kc, (uint32_t)b_bytes, &full[s]);
+        }
+    } else if (tid == 32) {
+        // MMA issuer
+        constexpr uint32_t idesc = idesc_bf16(128, N);
+        for (int i = 0; i < nsteps; i++) {
+            const int s = i % kStages;
+            if (!mbar_wait(&full[s], (i / kStages) & 1)) { bad = 1; break; }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t As = saddr(smem + (size_t)s * st_bytes), Bs = As + a_bytes;
+            for (int kk = 0; kk < a.kc / 16; kk++) {
+                const uint64_t ad = smem_desc(As + kk * 2 * 2048, 2048, 128);
+                const uint64_t bd = smem_desc(Bs + kk * 2 * N * 16, N * 16, 128);
+                umma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+            }
+            umma_commit(&empty[s]);
+        }
+        umma_commit(&done);
+    }
+    __syncthreads();  // roles finished; `bad` visible to every thread
+    // epilogue: warp w holds pixels 32w..32w+31 of the tile (warp-uniform
+    // decision, the TMEM loads are warp-collective)
+    const bool ok = __all_sync(0xffffffffu, mbar_wait(&done, 0) ? 1 : 0) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int m = warp * 32 + lane;
+    const int px = x0 + m % a.bx, py = y0 + m / a.bx;
+    if (ok && !bad) {
+        __nv_bfloat16* op = a.out + (((size_t)n * a.H + py) * a.W + px) * a.cout_tot + a.cout_off;
+        for (int c0 = 0; c0 < a.cout_store; c0 += 8) {
+            float v[8];
+            tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            __align__(16) __nv_bfloat16 o[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                float y = v[j] + (a.bias ? __ldg(a.bias + c0 + j) : 0.f);
+                if (a.relu) y = fmaxf(y, 0.f);
+                o[j] = __float2bfloat16(y);
+            }
+            *reinterpret_cast<uint4*>(op + c0) = *reinterpret_cast<const uint4*>(o);
+        }
+    }
+    if ((!ok || bad) && lane == 0) atomicExch(a.fail, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N));
+}
+
+// ---- host ---------------------------------------------------------------------
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+template <int N>
+static bool conv_attr() {
+    static bool done = false;
+    if (!done) {
+        const int smax = kStages * (64 * 256 + N * 64 * 2);
+        if (cudaFuncSetAttribute(k_conv3x3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess)
+            return false;
+        done = true;
+    }
+    return true;
+}
+
+}  // namespace nn
+
+using namespace nn;
+
+// x: [nb][H][W][cin_tot] BF16; computes channels [0, N) of the GEMM and stores
+// the first cout_store of them at out[..][cout_off + c] of an output tensor
+// with cout_tot channels.
+int conv3x3_launch(cudaStream_t s, const __nv_bfloat16* x, int nb, int H, int W, int cin_tot, int cin_off, int cin,
+                   const __nv_bfloat16* wpack, const float* bias, int N, int relu, __nv_bfloat16* out, int cout_tot,
+                   int cout_off, int cout_store, int* fail) {
+    if (cin % 16 || cin_off % 8 || cout_off % 8 || cout_store % 8 || cout_store > N) return 1;
+    if (!(N == 32 || N == 64 || N == 128 || N == 256)) return 1;
+    const int bx = W < 128 ? W : 128;
+    if (128 % bx) return 1;
+    const int by = 128 / bx;
+    if (W % bx || H % by) return 1;
+    auto enc = encode_fn();
+    if (!enc) return 2;
+    CUtensorMap map;
+    cuuint64_t dims[4] = {(cuuint64_t)cin_tot, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)nb};
+    cuuint64_t strides[3] = {(cuuint64_t)cin_tot * 2, (cuuint64_t)W * cin_tot * 2, (cuuint64_t)H * W * cin_tot * 2};
+    cuuint32_t box[4] = {8, (cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    if (enc(&map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void*)x, dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return 3;
+    ConvArgs a;
+    a.nb = nb; a.H = H; a.W = W; a.bx = bx; a.by = by;
+    a.cin = cin; a.cin_off = cin_off; a.kc = conv_kc(cin);
+    a.cout_store = cout_store; a.cout_off = cout_off; a.cout_tot = cout_tot;
+    a.relu = relu; a.wpack = wpack; a.bias = bias; a.out = out; a.fail = fail;
+    const int smem = kStages * (a.kc * 256 + N * a.kc * 2);
+    const unsigned grid = (unsigned)(nb * (H / by) * (W / bx));
+    switch (N) {
+        case 32: if (!conv_attr<32>()) return 4; k_conv3x3<32><<<grid, 128, smem, s>>>(map, a); break;
+        case 64: if (!conv_attr<64>()) return 4; k_conv3x3<64><<<grid, 128, smem, s>>>(map, a); break;
+        case 128: if (!conv_attr<128>()) return 4; k_conv3x3<128><<<grid, 128, smem, s>>>(map, a); break;
+        default: if (!conv_attr<256>()) return 4; k_conv3x3<256><<<grid, 128, smem, s>>>(map, a); break;
+    }
+    tc_note_launch();
+    return cudaGetLastError() == cudaSuccess ? 0 : 5;
+}

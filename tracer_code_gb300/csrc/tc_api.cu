@@ -11,6 +11,7 @@
 // reference's data-dependent loops branch on.
 #include "tc_device.cuh"
 #include "tc_setup.h"
+#include "tracer_nn.h"
 
 #include <cmath>
 #include <cstdio>
@@ -23,6 +24,17 @@
 
 static std::atomic<long long> g_launches{0};
 void tc_note_launch(long long n) { g_launches.fetch_add(n); }
+
+// learned initial guess (k_nn.cu, tc_nn_api.cu)
+struct tc_net_impl;
+tc_net_impl* tcnn_impl(tc_net* n);
+int* net_fail(tc_net_impl* n);
+void net_dims(const tc_net_impl* n, int* H, int* W);
+void nn_fields_to_raw(cudaStream_t s, const Lay& L, const double* vis, const double* rhs, const double* SF,
+                      float* raw);
+void nn_field_to_img(cudaStream_t s, const Lay& L, const double* S, float* img);
+int nn_guess(tc_net_impl* n, cudaStream_t s, const Lay& L, const double* vis, const double* rhs, const double* SF,
+             float* raw, double* G, int Vbc);
 
 namespace {
 
@@ -85,6 +97,14 @@ struct Handle {
     double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
     int ctab_level = 0;        // level the table was built for (0 = none)
     cudaError_t enq_err = cudaSuccess;  // first error of an enqueue-only helper (checked by its caller)
+    // learned initial guess
+    tc_net_impl* net = nullptr;
+    double* guess = nullptr;  // candidate start (level-1 layout)
+    float* nn_raw = nullptr;  // network input scratch [3][nz][nx]
+    long long guess_used = 0, guess_offered = 0;
+    // training-sample recorder (caller-owned device buffers)
+    float *rec_raw = nullptr, *rec_sf = nullptr;
+    int rec_cap = 0, rec_count = 0;
 };
 
 #define CK(call)                                                      \
@@ -520,8 +540,37 @@ tc_status multigrid(Handle* h) {
         h->lu_valid = true;
     }
     CK(cudaMemsetAsync(&h->ds->visit_timeout, 0, sizeof(int), h->st));
+    const size_t img = (size_t)h->nx * h->nz;
+    const bool rec = h->rec_raw && h->rec_count < h->rec_cap;
+    if (rec)
+        nn_fields_to_raw(h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1),
+                         h->rec_raw + (size_t)h->rec_count * 3 * img);
+    const bool try_guess = h->p.learned_guess == 1 && h->net != nullptr;
+    if (try_guess) {
+        // candidate start from the network; keep it only if its level-1 residual is smaller
+        if (nn_guess(h->net, h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
+                     h->p.Vbc) != 0) {
+            h->err = "learned guess: network forward failed";
+            return TC_ERR_CUDA;
+        }
+        launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+        launch_residual(h->st, h->lev[1], h->guess, h->rs, &h->ds->res_mag[0]);
+    }
     TRY(sync_scalars(h));
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
+    if (try_guess) {
+        int f = 0;
+        CK(cudaMemcpy(&f, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToHost));
+        if (f) {
+            h->err = "learned guess: a convolution's bounded wait gave up";
+            return TC_ERR_DEVICE_TIMEOUT;
+        }
+        h->guess_offered++;
+        if (h->hs->res_mag[0] < h->hs->res_mag[1]) {
+            copy_plane(h, cur_err(h, 1), h->guess);
+            h->guess_used++;
+        }
+    }
     const double res_ref1 = h->hs->res_ref;
     // p=1 is the only level-1 visit of every cycle table; the convergence test
     // follows it, then p=2..nsteps run unconditionally.
@@ -565,6 +614,10 @@ tc_status multigrid(Handle* h) {
     copy_plane(h, h->SF, cur_err(h, 1));
     h->last_cycles = q;
     h->cycles_acc += q;
+    if (rec) {
+        nn_field_to_img(h->st, h->lev[1].L, h->SF, h->rec_sf + (size_t)h->rec_count * img);
+        h->rec_count++;
+    }
     return TC_OK;
 }
 
@@ -997,6 +1050,40 @@ tc_status tc_create(const tc_params* p, tc_handle** out) {
         return s;
     }
     *out = H;
+    return TC_OK;
+}
+
+tc_status tc_attach_net(tc_handle* H, tc_net* net) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    tc_net_impl* n = tcnn_impl(net);
+    if (n) {
+        int nh = 0, nw = 0;
+        net_dims(n, &nh, &nw);
+        if (nh != h->nz || nw != h->nx) return TC_ERR_ARG;
+        if (!h->guess) TRY(dalloc_t(h, &h->guess, h->L1.plane));
+        if (!h->nn_raw) TRY(dalloc_t(h, &h->nn_raw, (size_t)3 * h->nx * h->nz));
+    }
+    h->net = n;
+    return TC_OK;
+}
+
+tc_status tc_record_solves(tc_handle* H, float* raw, float* sf_new, int32_t capacity) {
+    if (!H || capacity < 0 || (capacity > 0 && (!raw || !sf_new))) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    h->rec_raw = capacity > 0 ? raw : nullptr;
+    h->rec_sf = capacity > 0 ? sf_new : nullptr;
+    h->rec_cap = capacity;
+    h->rec_count = 0;
+    return TC_OK;
+}
+
+int32_t tc_record_count(const tc_handle* H) { return H ? H->h.rec_count : 0; }
+
+tc_status tc_guess_stats(const tc_handle* H, int64_t* used, int64_t* offered) {
+    if (!H) return TC_ERR_ARG;
+    if (used) *used = H->h.guess_used;
+    if (offered) *offered = H->h.guess_offered;
     return TC_OK;
 }
 
