@@ -130,9 +130,13 @@ typedef struct tc_params {
     int32_t solver_precision;
     /* No reference counterpart.  1 = start each multigrid solve from the
      * attached network's guess (tracer_nn.h) when its level-1 residual is
-     * below that of the previous streamfunction; 0 = always from the latter. */
+     * below that of the previous streamfunction; 2 = always from the guess;
+     * 0 = always from the previous streamfunction. */
     int32_t learned_guess;
-    int32_t reserved_[1];
+    /* Passes of a separable (1,2,1)/4 filter applied to the network's
+     * correction before it is added (removes grid-scale noise that the
+     * BF16 output carries; 0 = none). */
+    int32_t learned_smooth;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat

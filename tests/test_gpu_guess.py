@@ -1,0 +1,114 @@
+"""The learned initial guess inside the solver.
+
+  - the recorder stores, per solve, the fields the solve started from and
+    the converged streamfunction (FP32 images of the level-1 fields);
+  - with any network attached (here an untrained one) every solve still
+    meets the reference's tolerance: the solver starts from the network's
+    guess only when its level-1 residual is smaller, and Nu/Vrms/mass after
+    several steps agree with the run without the network to 1e-6 relative;
+  - the committed trained network (tracer_code_gb300/weights) lowers the
+    W-cycle count of the mixed solver on a case whose physics it was not
+    trained on (the gain is printed).
+"""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+from tracer_code_gb300 import Simulation, state
+from tracer_code_gb300.abi import config_1024x256
+
+pytestmark = pytest.mark.gpu
+
+WEIGHTS = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tracer_code_gb300", "weights",
+                       "guess_512x128.npy")
+
+
+def case(nx=256, nz=64, grids=4, prec=1, Ra=1e6, visT=1e3):
+    p = config_1024x256()
+    p.nx, p.nz, p.tpc, p.grids = nx, nz, 4, grids
+    p.RaT = Ra
+    p.RaC[0] = 0.6 * Ra
+    p.visT = visT
+    p.mg_zero_coarse = 1
+    p.solver_precision = prec
+    return p
+
+
+def test_recorder_stores_solve_inputs_and_results(gpu_lib):
+    from tracer_code_gb300 import learned
+    p = case()
+    sim = Simulation(p)
+    sim.upload(state.initial_state(p, seed=4))
+    sim.step()
+    raw = torch.zeros((4, 3, p.nz, p.nx), dtype=torch.float32, device="cuda")
+    sf = torch.zeros((4, p.nz, p.nx), dtype=torch.float32, device="cuda")
+    learned.record_solves(sim, raw.data_ptr(), sf.data_ptr(), 4)
+    sf_before = sim.download()["SF"]
+    sim.multigrid()
+    sf_after = sim.download()["SF"]
+    assert learned.record_count(sim) == 1
+    SP = 2
+    prev = sf_before[SP:SP + p.nz, SP:SP + p.nx]  # nodes k = 0..nz-1, i = 0..nx-1
+    new = sf_after[SP:SP + p.nz, SP:SP + p.nx]
+    assert np.array_equal(raw[0, 2].cpu().numpy(), prev.astype(np.float32))
+    assert np.array_equal(sf[0].cpu().numpy(), new.astype(np.float32))
+    vis = sim.get("vis_grid", 1)[SP:SP + p.nz, SP:SP + p.nx]
+    assert np.allclose(raw[0, 0].cpu().numpy(), np.log10(vis), rtol=1e-6, atol=1e-6)
+    sim.step()  # four more solves, capacity 4 in total
+    assert learned.record_count(sim) == 4
+    sim.close()
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_untrained_guess_keeps_the_solution(gpu_lib, prec):
+    from tracer_code_gb300 import learned
+    p = case(prec=prec)
+    st = state.initial_state(p, seed=2)
+    rows = []
+    for use in (0, 1):
+        q = p.copy()
+        q.learned_guess = use
+        sim = Simulation(q)
+        net = learned.Net(1, p.nz, p.nx, seed=5)
+        learned.attach(sim, net)
+        sim.upload(st)
+        rows.append([sim.step()[0] for _ in range(3)])
+        if use:
+            used, offered = learned.guess_stats(sim)
+            assert offered == 12
+        sim.close()
+        net.close()
+    for a, b in zip(rows[0], rows[1]):
+        for key in ["Nu", "vrms"]:
+            assert abs(a[key] - b[key]) <= 1e-6 * abs(a[key]), key
+        assert abs(a["Cavg"][0] - b["Cavg"][0]) <= 1e-6 * abs(a["Cavg"][0])
+
+
+@pytest.mark.skipif(not os.path.exists(WEIGHTS), reason="no trained weights")
+def test_trained_guess_lowers_cycle_count(gpu_lib):
+    from tracer_code_gb300 import learned
+    # physics inside the training ranges, seed and parameters not used in training
+    p = case(nx=512, nz=128, grids=5, prec=1, Ra=3.3e6, visT=2.2e3)
+    st = state.initial_state(p, seed=777)
+    cycles = {}
+    for use in (0, 1):
+        q = p.copy()
+        q.learned_guess = use
+        sim = Simulation(q)
+        net = learned.Net(1, p.nz, p.nx)
+        net.load(WEIGHTS)
+        learned.attach(sim, net)
+        sim.upload(st)
+        for _ in range(4):  # start-up transient, not counted
+            sim.step()
+        cycles[use] = sum(sim.step()[1] for _ in range(6))
+        if use:
+            cycles["used"], cycles["offered"] = learned.guess_stats(sim)
+        sim.close()
+        net.close()
+    print(f"W-cycles over 6 steps: plain start {cycles[0]}, learned start {cycles[1]} "
+          f"(guess used in {cycles['used']} of {cycles['offered']} solves)")
+    assert cycles[1] <= cycles[0]

@@ -70,7 +70,7 @@ class Params(C.Structure):
         ("eig_ratio_min", C.c_double), ("ivis", C.c_int32), ("visP", C.c_double), ("visT", C.c_double),
         ("delta_visT", C.c_double), ("yield_", C.c_double), ("yield_gradient", C.c_double),
         ("yield_depth", C.c_double), ("visC", _D4), ("delta_visC", _D4),
-        ("mg_zero_coarse", C.c_int32), ("solver_precision", C.c_int32), ("learned_guess", C.c_int32), ("reserved_", C.c_int32 * 1),
+        ("mg_zero_coarse", C.c_int32), ("solver_precision", C.c_int32), ("learned_guess", C.c_int32), ("learned_smooth", C.c_int32),
     ]
 
     def copy(self) -> "Params":

@@ -698,16 +698,41 @@ void nn_fields_to_raw(cudaStream_t s, const Lay& L, const double* vis, const dou
 void nn_field_to_img(cudaStream_t s, const Lay& L, const double* S, float* img) {
     k_field_to_img<<<nblk((size_t)L.a * L.b), 256, 0, s>>>(L, S, img); tc_note_launch();
 }
+namespace {
+// one pass of the separable (1,2,1)/4 x (1,2,1)/4 filter on the interior
+// nodes of an H x W image (boundary nodes i = 0, k = 0 and the absent
+// i = W, k = H count as zero)
+__global__ void k_binomial(const float* __restrict__ in, int H, int W, float* __restrict__ out) {
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < (size_t)H * W;
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(t % W), y = (int)(t / W);
+        if (x < 1 || y < 1) { out[t] = 0.f; continue; }
+        auto v = [&](int yy, int xx) { return (xx < 1 || yy < 1 || xx >= W || yy >= H) ? 0.f : in[(size_t)yy * W + xx]; };
+        float s = 0.f;
+        const float w[3] = {0.25f, 0.5f, 0.25f};
+        for (int a = -1; a <= 1; a++)
+            for (int b = -1; b <= 1; b++) s += w[a + 1] * w[b + 1] * v(y + a, x + b);
+        out[t] = s;
+    }
+}
+}  // namespace
+
 // network guess from the level-1 fields into G (a zeroed plane: walls stay 0)
 int nn_guess(tc_net_impl* n, cudaStream_t s, const Lay& L, const double* vis, const double* rhs, const double* SF,
-             float* raw, double* G, int Vbc) {
+             float* raw, double* G, int Vbc, int smooth) {
     if (n->H != L.b || n->W != L.a) return 1;
     cudaStream_t keep = n->st;
     n->st = s;
     nn_fields_to_raw(s, L, vis, rhs, SF, raw);
     net_prepare(n, raw, 1);
     const int r = net_forward(n, 1);
-    k_guess<<<nblk((size_t)L.a * L.b), 256, 0, s>>>(L, SF, n->out, n->stats, G, Vbc); tc_note_launch();
+    float* o = n->out;
+    for (int f = 0; f < smooth; f++) {
+        float* dst = (o == n->out) ? n->dout : n->out;
+        k_binomial<<<nblk((size_t)L.a * L.b), 256, 0, s>>>(o, L.b, L.a, dst); tc_note_launch();
+        o = dst;
+    }
+    k_guess<<<nblk((size_t)L.a * L.b), 256, 0, s>>>(L, SF, o, n->stats, G, Vbc); tc_note_launch();
     n->st = keep;
     return r;
 }

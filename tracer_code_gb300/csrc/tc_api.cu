@@ -34,7 +34,7 @@ void nn_fields_to_raw(cudaStream_t s, const Lay& L, const double* vis, const dou
                       float* raw);
 void nn_field_to_img(cudaStream_t s, const Lay& L, const double* S, float* img);
 int nn_guess(tc_net_impl* n, cudaStream_t s, const Lay& L, const double* vis, const double* rhs, const double* SF,
-             float* raw, double* G, int Vbc);
+             float* raw, double* G, int Vbc, int smooth);
 
 namespace {
 
@@ -545,11 +545,12 @@ tc_status multigrid(Handle* h) {
     if (rec)
         nn_fields_to_raw(h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1),
                          h->rec_raw + (size_t)h->rec_count * 3 * img);
-    const bool try_guess = h->p.learned_guess == 1 && h->net != nullptr;
+    const bool try_guess = (h->p.learned_guess == 1 || h->p.learned_guess == 2) && h->net != nullptr;
     if (try_guess) {
-        // candidate start from the network; keep it only if its level-1 residual is smaller
+        // candidate start from the network; with learned_guess = 1 it is kept
+        // only if its level-1 residual is smaller
         if (nn_guess(h->net, h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
-                     h->p.Vbc) != 0) {
+                     h->p.Vbc, h->p.learned_smooth) != 0) {
             h->err = "learned guess: network forward failed";
             return TC_ERR_CUDA;
         }
@@ -566,7 +567,7 @@ tc_status multigrid(Handle* h) {
             return TC_ERR_DEVICE_TIMEOUT;
         }
         h->guess_offered++;
-        if (h->hs->res_mag[0] < h->hs->res_mag[1]) {
+        if (h->p.learned_guess == 2 || h->hs->res_mag[0] < h->hs->res_mag[1]) {
             copy_plane(h, cur_err(h, 1), h->guess);
             h->guess_used++;
         }
@@ -761,6 +762,7 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
     if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;
+    if (p.learned_guess < 0 || p.learned_guess > 2 || p.learned_smooth < 0 || p.learned_smooth > 64) return TC_ERR_ARG;
     h->nx = p.nx; h->nz = p.nz; h->grids = p.grids;
     {
         const long nb = (long)((p.nx + 2 + BX - 1) / BX) * (long)((p.nz + 2 + BY - 1) / BY);
