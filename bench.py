@@ -59,8 +59,12 @@ SOLVER_DESC = {
              "coarse corrections restart from zero (mg_zero_coarse=1)",
     "mixed": "mixed-precision multigrid: the same W-cycle with FP32 smoother, residuals and transfers on levels "
              "1..grids-1 inside FP64 defect correction (FP64 level-1 residual, streamfunction and updates, FP64 "
-             "coarse solve), same 1e-8 test; no learned guess yet",
+             "coarse solve), same 1e-8 test",
+    "learned": "learned + mixed: the mixed-precision multigrid, each solve offered the encoder-decoder's initial "
+               "guess (BF16 tcgen05 network trained at 512x128) and started from it when its level-1 residual is "
+               "below the previous streamfunction's; same 1e-8 test",
 }
+GUESS_WEIGHTS = os.path.join(ROOT, "tracer_code_gb300", "weights", "guess_512x128.npy")
 
 
 def workload_desc(p, solver: str) -> dict:
@@ -263,13 +267,19 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # headline arm: mixed-precision solver
+    from tracer_code_gb300 import learned
+    # headline arm: mixed-precision solver with the learned initial guess
     p = workload_params("mixed")
+    p.learned_guess = 1
     st = state.initial_state(p, seed=1 + rank)
     sim = Simulation(p, stream=stream.cuda_stream)
+    net = learned.Net(1, p.nz, p.nx, stream=stream.cuda_stream)
+    net.load(GUESS_WEIGHTS)
+    learned.attach(sim, net)
     sim.upload(st)
     with ClockSampler(local_rank) as clk:
         ms, solves, cycles, launches = timed_steps(sim, stream, args.steps, args.warmup, barrier)
+    guess_used, guess_offered = learned.guess_stats(sim)
     ms_max = max_over_ranks(ms)
     value = world * args.steps / (ms_max * 1e-3)
     roof = sweep_roofline(sim, p, fp32=True)
@@ -292,6 +302,14 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     torch.cuda.synchronize()
     e2e_value = world * k_e2e / max_over_ranks(time.perf_counter() - t0)
     sim.close()
+    net.close()
+    # the same mixed solver without the network
+    pm = workload_params("mixed")
+    simm = Simulation(pm, stream=stream.cuda_stream)
+    simm.upload(st)
+    msm, solvesm, _, _ = timed_steps(simm, stream, args.steps, args.warmup, barrier)
+    mixed_value = world * args.steps / (max_over_ranks(msm) * 1e-3)
+    simm.close()
     # comparison arm: plain FP64 multigrid on the same initial state
     pp = workload_params("plain")
     sim0 = Simulation(pp, stream=stream.cuda_stream)
@@ -301,8 +319,12 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     roof0 = sweep_roofline(sim0, pp, fp32=False)
     sim0.close()
     if rank == 0:
-        cfg = dict(workload_desc(p, "mixed"), cycles_per_step=solves, warmup_cycles_per_step=cycles,
+        cfg = dict(workload_desc(p, "learned"), cycles_per_step=solves, warmup_cycles_per_step=cycles,
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
+                   learned_guess={"weights": os.path.relpath(GUESS_WEIGHTS, ROOT), "solves_offered": guess_offered,
+                                  "solves_started_from_guess": guess_used},
+                   mixed_without_guess={"timesteps_per_s": mixed_value, "ms_per_step": msm / args.steps,
+                                        "cycles_per_step": solvesm},
                    plain_fp64={"timesteps_per_s": plain_value, "ms_per_step": ms0 / args.steps,
                                "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0},
                    speedup_vs_plain_fp64=value / plain_value)
@@ -341,7 +363,26 @@ def main():
                     help="profiling case: upload the workload, run one multigrid solve, exit")
     ap.add_argument("--solver", default="plain", choices=["plain", "mixed"],
                     help="solver of --profile-solve")
+    ap.add_argument("--profile-net", action="store_true",
+                    help="profiling case: one guess-network forward and backward on one 1024x256 image, exit")
     args = ap.parse_args()
+    if args.profile_net:
+        import numpy as np
+        import torch
+        from tracer_code_gb300 import learned
+        p = workload_params("mixed")
+        net = learned.Net(1, p.nz, p.nx)
+        net.load(GUESS_WEIGHTS)
+        rng = np.random.default_rng(1)
+        raw = torch.from_numpy(rng.normal(size=(1, 3, p.nz, p.nx)).astype(np.float32)).cuda()
+        sf = torch.from_numpy(rng.normal(size=(1, p.nz, p.nx)).astype(np.float32)).cuda()
+        out = torch.empty((1, p.nz, p.nx), dtype=torch.float32, device="cuda")
+        net.forward(raw.data_ptr(), 1, out.data_ptr())
+        loss = net.loss_backward(raw.data_ptr(), sf.data_ptr(), 1)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_net": True, "loss": loss}), flush=True)
+        net.close()
+        return
     if args.profile_solve:
         from tracer_code_gb300 import Simulation, state
         p = workload_params(args.solver)

@@ -229,8 +229,9 @@ tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double
 
 /* Diagnostics (no counterpart in the reference).  tc_time_sweep times
  * `nsweeps` back-to-back launches of the multigrid smoother kernel of `level`
- * (the FP32 one under solver_precision = 1) with CUDA events on the handle's
- * stream (state left unchanged) and writes
+ * (the FP32 one under solver_precision = 1), replayed as one CUDA graph as
+ * the solver runs them, with CUDA events on the handle's stream (state left
+ * unchanged) and writes
  * the mean milliseconds per launch.  tc_kernel_launches returns how many
  * kernels this library has launched in the process so far (graph replays
  * count every kernel node). */

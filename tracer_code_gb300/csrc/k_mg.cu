@@ -227,7 +227,7 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
 // ---------------------------------------------------------------------------
 
 
-__global__ void k_sweep(Lay L, Range2 r, const double* __restrict__ Sin, double* __restrict__ Sout,
+__global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double* __restrict__ Sin, double* __restrict__ Sout,
                         const double* __restrict__ coef, const double* __restrict__ rhs,
                         const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
                         double c_uniform, int per_point, double temp, int Vbc) {
@@ -246,7 +246,7 @@ void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* So
                                                   c_uniform, per_point, temp, Vbc); tc_note_launch();
 }
 
-__global__ void k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
+__global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
                            const double* __restrict__ rhs, double* __restrict__ res, RedScratch rs, double* out,
                            double div1, double div2) {
     RANGE_IK(r);

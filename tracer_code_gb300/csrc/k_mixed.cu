@@ -34,8 +34,8 @@ void to_f32(cudaStream_t s, const double* in, float* out, size_t n) {
     k_to_f32<<<nb, 256, 0, s>>>(in, out, n); tc_note_launch();
 }
 
-__global__ void k_sweep32(Lay L, Range2 r, const float* __restrict__ Sin, float* __restrict__ Sout,
-                          const float* __restrict__ coef, const float* __restrict__ rhs,
+__global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float* __restrict__ Sin,
+                                                   float* __restrict__ Sout, const float* __restrict__ coef, const float* __restrict__ rhs,
                           const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
                           float c_uniform, int per_point, float temp, int Vbc) {
     RANGE_IK(r);
@@ -47,7 +47,7 @@ __global__ void k_sweep32(Lay L, Range2 r, const float* __restrict__ Sin, float*
     store_stream<float>(L, Sout, i, k, v, Vbc);
 }
 
-__global__ void k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
+__global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
                              const float* __restrict__ rhs, float* __restrict__ res) {
     RANGE_IK(r);
     if (!inr) return;
@@ -82,7 +82,7 @@ __global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* __restrict__ 
 }
 
 // FP64 residual of psi, rounded to FP32 as the RHS of the level-1 correction
-__global__ void k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
+__global__ void __launch_bounds__(256, 1) k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
                                 const double* __restrict__ rhs, float* __restrict__ rhs32) {
     RANGE_IK(r);
     if (!inr) return;

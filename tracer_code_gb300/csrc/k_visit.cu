@@ -413,7 +413,7 @@ static bool visit_attrs() {
 // Sets the kernel attributes; returns how many 16-CTA clusters of the
 // largest configuration can be resident (0 = fused visits unavailable).
 int visit_cluster_setup() {
-    if (!visit_attrs<double, 1, 256>() || !visit_attrs<float, 4, 256>() || !visit_attrs<float, 2, 512>()) {
+    if (!visit_attrs<double, 1, 256>() || !visit_attrs<float, 1, 256>() || !visit_attrs<float, 2, 512>()) {
         cudaGetLastError();
         return 0;
     }
@@ -450,7 +450,10 @@ static bool visit_shape(const Lay& L, int nsweeps, bool fp32, VisitShape* s) {
     if (nsweeps > VISIT_MAX_SWEEPS || rows < 2 || cols < 1) return false;
     s->w = w_class(L.a);
     if (s->w == 0) return false;
-    if (fp32) {
+    const int spread_C = rows < VISIT_MAX_CLUSTER ? rows : VISIT_MAX_CLUSTER;
+    const int spread_rpc = (rows + spread_C - 1) / spread_C;
+    if (fp32 && spread_rpc * cols > 256) {
+        // too many points to spread one per thread over 16 CTAs of 256:
         // 512 threads in strips of 2 (four warps per scheduler hide the
         // shared-memory and FMA latencies better than strips of 4 on 256)
         s->p = 2;
@@ -459,10 +462,11 @@ static bool visit_shape(const Lay& L, int nsweeps, bool fp32, VisitShape* s) {
         s->rpc = (s->nt / cols) * s->p;
         s->C = (rows + s->rpc - 1) / s->rpc;
     } else {
+        // one point per thread over up to 16 CTAs: more SMs issue the sweep
+        // (measured faster than fewer, fuller CTAs for levels of <= 4K points)
         s->p = 1;
         s->nt = 256;
-        int C = rows < VISIT_MAX_CLUSTER ? rows : VISIT_MAX_CLUSTER;
-        s->rpc = (rows + C - 1) / C;
+        s->rpc = spread_rpc;
         s->C = (rows + s->rpc - 1) / s->rpc;
         if (s->rpc * cols > s->nt) return false;
     }
@@ -541,7 +545,7 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
     if constexpr (sizeof(T) == sizeof(double)) {
         e = visit_launch<T, 1, 256>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
     } else {
-        if (sh.p == 4) e = visit_launch<T, 4, 256>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
+        if (sh.p == 1) e = visit_launch<T, 1, 256>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
         else e = visit_launch<T, 2, 512>(sh, s, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
     }
     if (e != cudaSuccess) return 2;

@@ -1252,11 +1252,25 @@ tc_status tc_time_sweep(tc_handle* H, int32_t level, int32_t nsweeps, double* ms
         if (mixed) launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], 1.0f, 0, 0.0f, h->p.Vbc);
         else launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], 1.0, 0, 0.0, h->p.Vbc);
     };
-    sweep();
-    CK(cudaEventRecord(e0, h->st));
+    // the sweeps are captured in a CUDA graph and replayed, as the solver
+    // runs them (per-launch host overhead would otherwise dominate)
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    const long long before = g_launches.load();
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     for (int n = 0; n < nsweeps; n++) sweep();
+    CK(cudaStreamEndCapture(h->st, &g));
+    g_launches.fetch_sub(g_launches.load() - before);
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    CK(cudaGraphLaunch(ge, h->st));
+    CK(cudaEventRecord(e0, h->st));
+    CK(cudaGraphLaunch(ge, h->st));
     CK(cudaEventRecord(e1, h->st));
     CK(cudaEventSynchronize(e1));
+    cudaGraphExecDestroy(ge);
+    tc_note_launch(2LL * nsweeps);
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, e0, e1));
     cudaEventDestroy(e0);

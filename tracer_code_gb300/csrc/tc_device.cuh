@@ -119,25 +119,26 @@ __device__ __forceinline__ T restrict9(const T* __restrict__ in, const Lay& F, i
 
 // rhs - L S at x with the 13 folded coefficient planes (stream_space with
 // the Database=2 order-2 stencil, iterative_solver.f90:456-561)
+// All 26 loads are issued before the first multiply-add (independent loads
+// in flight together instead of one L2 round trip per term); the sum keeps
+// the tap order below, so the result does not depend on the load schedule.
 template <typename T>
 __device__ __forceinline__ T folded_residual(const Lay& L, const T* __restrict__ S, const T* __restrict__ coef, T rhs,
                                              size_t x) {
-    const size_t ld = (size_t)L.ld, pl = L.plane;
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const size_t pl = L.plane;
     const T* cf = coef + x;
+    const T* s = S + x;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    T c[TC_NCOEF], v[TC_NCOEF];
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) {
+        c[d] = __ldg(cf + d * pl);
+        v[d] = __ldg(s + off[d]);
+    }
     T acc = rhs;
-    acc = fma(-__ldg(cf + 0 * pl), __ldg(S + x), acc);
-    acc = fma(-__ldg(cf + 1 * pl), __ldg(S + x - 1), acc);
-    acc = fma(-__ldg(cf + 2 * pl), __ldg(S + x + 1), acc);
-    acc = fma(-__ldg(cf + 3 * pl), __ldg(S + x - 2), acc);
-    acc = fma(-__ldg(cf + 4 * pl), __ldg(S + x + 2), acc);
-    acc = fma(-__ldg(cf + 5 * pl), __ldg(S + x - ld), acc);
-    acc = fma(-__ldg(cf + 6 * pl), __ldg(S + x + ld), acc);
-    acc = fma(-__ldg(cf + 7 * pl), __ldg(S + x - 2 * ld), acc);
-    acc = fma(-__ldg(cf + 8 * pl), __ldg(S + x + 2 * ld), acc);
-    acc = fma(-__ldg(cf + 9 * pl), __ldg(S + x - 1 - ld), acc);
-    acc = fma(-__ldg(cf + 10 * pl), __ldg(S + x + 1 - ld), acc);
-    acc = fma(-__ldg(cf + 11 * pl), __ldg(S + x - 1 + ld), acc);
-    acc = fma(-__ldg(cf + 12 * pl), __ldg(S + x + 1 + ld), acc);
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) acc = fma(-c[d], v[d], acc);
     return acc;
 }
 
