@@ -41,9 +41,11 @@ UNIT = "timesteps/s"
 # runs without the GPU arm in the same process.
 CYCLES_PER_STEP_DEFAULT = 228.0
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the level-1
-# smoother kernel (profiles/k_sweep_1024x256.md); None until captured.
-SWEEP_DRAM_BYTES = None
-SWEEP32_DRAM_BYTES = None
+# smoother kernels from one ncu capture each (cold cache; the FP64 kernel in
+# profiles/multigrid_solve_1024x256.md, the FP32 one in
+# profiles/k_sweep32_1024x256.md).
+SWEEP_DRAM_BYTES = 34.0e6
+SWEEP32_DRAM_BYTES = 17.26e6
 
 
 def workload_params(solver: str = "plain"):
