@@ -354,6 +354,53 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         print(json.dumps(line), flush=True)
 
 
+def run_ensemble(args):
+    """Batched ensemble: args.ensemble cases (tracer_code_gb300.ensemble.case_params), mixed solver,
+    learned guess and autotuned launch shapes per case, stepped together by tc_ensemble_step."""
+    import torch
+    from tracer_code_gb300.ensemble import Ensemble, case_params
+    t0 = time.time()
+    params = [case_params(i) for i in range(args.ensemble)]
+    ens = Ensemble(params, weights=GUESS_WEIGHTS, autotune=True)
+    setup_s = time.time() - t0
+    # cases whose run stops (tracers leaving the domain, a diverging solve:
+    # the reference's `stop` sites) stop during the warm-up and are left out
+    for _ in range(args.warmup):
+        ens.step(strict=False)
+    torch.cuda.synchronize()
+    active = list(ens.active)
+    t1 = time.perf_counter()
+    cyc = []
+    for _ in range(args.steps):
+        _, c, _ = ens.step(strict=False)
+        cyc.append([c[i] for i in active])
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t1
+    if ens.active != active:
+        raise RuntimeError(f"cases stopped inside the timed steps: {sorted(set(active) - set(ens.active))}")
+    ntr = sum(ens.ntr[i] for i in active)
+    sizes = {}
+    for p in params:
+        k = f"{p.nx}x{p.nz}"
+        sizes[k] = sizes.get(k, 0) + 1
+    line = {
+        "metric": "tracer*RK-stages/s, batched ensemble", "value": ntr * 4 * args.steps / el,
+        "unit": "tracer*RK-stages/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64", "data": "synthetic (seeded per case)",
+        "config": {"workload": f"{args.ensemble} independent cases, grids {sizes}, 10-25 tracers/cell, "
+                               f"Ra 1e5-1e7, B 0.2-1.0, viscosity contrast 1e2-1e5",
+                   "tracers_total": ntr, "cases_timed": len(active),
+                   "cases_stopped_in_warmup": {str(k): v for k, v in sorted(ens.stopped.items())},
+                   "per_case_timesteps_per_s": args.steps / el,
+                   "cycles_per_step_per_case": cyc, "setup_s": setup_s,
+                   "execution": "one handle and stream per case, tc_step issued by a host thread pool "
+                                "(tc_ensemble_step); per-case CUDA graphs; launch shapes from tc_autotune"},
+    }
+    ens.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,7 +414,13 @@ def main():
                     help="solver of --profile-solve")
     ap.add_argument("--profile-net", action="store_true",
                     help="profiling case: one guess-network forward and backward on one 1024x256 image, exit")
+    ap.add_argument("--ensemble", type=int, default=0, metavar="N",
+                    help="instead of the headline: N independent cases (256x64/512x128/1024x256 in turn, "
+                         "randomised physics) stepped together; prints aggregate tracer*RK-stages/s")
     args = ap.parse_args()
+    if args.ensemble:
+        run_ensemble(args)
+        return
     if args.profile_net:
         import numpy as np
         import torch

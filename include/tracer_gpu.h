@@ -227,6 +227,27 @@ tc_status tc_step(tc_handle* h, tc_stats_row* row, int32_t* cycles, double* dt_o
 tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double* rtr, double* str,
                        const int32_t* Ttype, int64_t ntr, tc_stats_row* row, int32_t* cycles, double* dt_out);
 
+/* Autotuner (no reference counterpart).  For each smoothed level it times,
+ * on this handle's GPU and in its solver precision, the per-sweep smoother
+ * kernel under eight block shapes of at most 256 threads and a fused
+ * cluster visit against one
+ * launch per sweep (CUDA-graph replays), and keeps the fastest of each.
+ * Results are unchanged by the choice (the arithmetic per point does not
+ * depend on the launch shape).  If `choices` is not NULL it receives
+ * (block x, block y, fused) for levels 1..grids-1.  Needs uploaded state;
+ * the levels' corrections are restored afterwards. */
+tc_status tc_autotune(tc_handle* h, int32_t* choices);
+
+/* Ensemble of independent cases (no reference counterpart: the reference
+ * runs one case per process).  One tc_step on each of the n handles, the
+ * handles' work issued concurrently by up to nthreads host threads, each
+ * handle on its own stream, so the GPU runs the cases' kernels side by side.
+ * rows[i], cycles[i], dts[i], status[i] receive case i's results (any may be
+ * NULL); returns the first non-OK status or TC_OK.  The handles must be
+ * distinct, and no other thread may use them during the call. */
+tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc_stats_row* rows, int32_t* cycles,
+                           double* dts, tc_status* status);
+
 /* Diagnostics (no counterpart in the reference).  tc_time_sweep times
  * `nsweeps` back-to-back launches of the multigrid smoother kernel of `level`
  * (the FP32 one under solver_precision = 1), replayed as one CUDA graph as

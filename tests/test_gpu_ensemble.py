@@ -1,0 +1,68 @@
+"""Autotuner and ensemble.
+
+  - tc_autotune changes launch shapes only: a multigrid solve after tuning
+    gives the same streamfunction bit for bit and the same cycle count, in
+    FP64 and in the mixed solver;
+  - tc_ensemble_step runs cases of different grid sizes concurrently; every
+    case ends in the state, statistics and cycle counts it reaches when it is
+    stepped alone.
+"""
+import numpy as np
+import pytest
+
+from tracer_code_gb300 import Simulation, state
+from tracer_code_gb300.abi import config_1024x256
+
+pytestmark = pytest.mark.gpu
+
+
+def small(nx, nz, grids, prec, Ra=1e6, visT=1e3, tpc=4):
+    p = config_1024x256()
+    p.nx, p.nz, p.grids, p.tpc = nx, nz, grids, tpc
+    p.RaT = Ra
+    p.RaC[0] = 0.6 * Ra
+    p.visT = visT
+    p.mg_zero_coarse = 1
+    p.solver_precision = prec
+    return p
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_autotune_keeps_results(gpu_lib, prec):
+    p = small(256, 64, 4, prec)
+    st = state.initial_state(p, seed=3)
+    out = []
+    for tune in (False, True):
+        sim = Simulation(p)
+        sim.upload(st)
+        if tune:
+            choice = sim.autotune()
+            assert len(choice) == p.grids - 1
+            assert all(bx * by >= 32 for bx, by, _ in choice)
+        q = sim.multigrid()
+        out.append((q, sim.download()["SF"]))
+        sim.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+
+
+def test_ensemble_matches_cases_stepped_alone(gpu_lib):
+    from tracer_code_gb300.ensemble import Ensemble
+    params = [small(256, 64, 4, 1, Ra=3e5), small(512, 128, 5, 1, Ra=2e6, visT=300.0),
+              small(256, 64, 4, 0, Ra=1e6, visT=5e3), small(512, 128, 5, 1, Ra=8e5, tpc=6)]
+    ens = Ensemble(params, seeds=[11, 12, 13, 14], autotune=True)
+    res = [ens.step() for _ in range(2)]
+    states = [s.download() for s in ens.sims]
+    ens.close()
+    for i, p in enumerate(params):
+        sim = Simulation(p)
+        sim.upload(state.initial_state(p, seed=11 + i))
+        for n in range(2):
+            row, q, dt = sim.step()
+            assert q == res[n][1][i]
+            assert dt == res[n][2][i]
+            assert row["Nu"] == res[n][0][i]["Nu"]
+        d = sim.download()
+        assert np.array_equal(d["SF"], states[i]["SF"])
+        assert np.array_equal(d["rtr"], states[i]["rtr"])
+        sim.close()

@@ -31,7 +31,7 @@ EXPORTS = [
     "tc_default_params", "tc_abi_sizes", "tc_create", "tc_destroy", "tc_get_info", "tc_set_stream",
     "tc_upload_state", "tc_download_state", "tc_set_clock", "tc_multigrid", "tc_compute_velocities", "tc_stats",
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
-    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches",
+    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
 ]
 
 
@@ -78,6 +78,8 @@ def load_library(build_if_missing: bool = False):
                                    C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         L.tc_time_sweep.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
         L.tc_time_visit.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
+        L.tc_autotune.argtypes = [vp, vp]
+        L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]
@@ -227,6 +229,13 @@ class Simulation:
         ms = C.c_double(0)
         self._chk(self.L.tc_time_sweep(self.h, level, nsweeps, C.byref(ms)), "time_sweep")
         return ms.value
+
+    def autotune(self) -> list:
+        """Runs tc_autotune; returns [(block_x, block_y, fused)] for levels 1..grids-1."""
+        g = self.info.grids
+        out = (C.c_int32 * (3 * max(g - 1, 1)))()
+        self._chk(self.L.tc_autotune(self.h, out), "autotune")
+        return [(out[3 * i], out[3 * i + 1], out[3 * i + 2]) for i in range(g - 1)]
 
     def time_visit(self, level: int, reps: int = 20) -> float:
         ms = C.c_double(0)

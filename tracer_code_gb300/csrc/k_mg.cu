@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
                         const double* __restrict__ coef, const double* __restrict__ rhs,
                         const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
                         double c_uniform, int per_point, double temp, int Vbc) {
-    RANGE_IK(r);
+    RANGE_IK_DYN(r);
     if (!inr) return;
     size_t x = IX(L, i, k);
     double res = folded_residual(L, Sin, coef, __ldg(rhs + x), x);
@@ -242,7 +242,8 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
 void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
                   int per_point, double temp, int Vbc) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
-    k_sweep<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
+    k_sweep<<<grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s>>>(
+        lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
                                                   c_uniform, per_point, temp, Vbc); tc_note_launch();
 }
 

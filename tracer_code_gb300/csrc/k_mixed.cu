@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
                                                    float* __restrict__ Sout, const float* __restrict__ coef, const float* __restrict__ rhs,
                           const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
                           float c_uniform, int per_point, float temp, int Vbc) {
-    RANGE_IK(r);
+    RANGE_IK_DYN(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
     const float res = folded_residual<float>(L, Sin, coef, __ldg(rhs + x), x);
@@ -134,8 +134,9 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb) {
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc) {
     const Range2 r = interior(lv.L);
-    k_sweep32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, Sin, Sout, lv.coef32, lv.rhs32, lv.dts32, lv.cA32,
-                                                    lv.cB32, c_uniform, per_point, temp, Vbc); tc_note_launch();
+    k_sweep32<<<grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s>>>(
+        lv.L, r, Sin, Sout, lv.coef32, lv.rhs32, lv.dts32, lv.cA32, lv.cB32, c_uniform, per_point, temp, Vbc);
+    tc_note_launch();
 }
 
 void launch_residual32(cudaStream_t s, const Level& lv, const float* S) {

@@ -21,9 +21,16 @@
 #include <vector>
 
 #include <atomic>
+#include <thread>
 
 static std::atomic<long long> g_launches{0};
-void tc_note_launch(long long n) { g_launches.fetch_add(n); }
+// per host thread, so that graph capture counts only its own thread's
+// launches while other handles run on other threads (tc_ensemble_step)
+static thread_local long long t_launches = 0;
+void tc_note_launch(long long n) {
+    g_launches.fetch_add(n);
+    t_launches += n;
+}
 
 // learned initial guess (k_nn.cu, tc_nn_api.cu)
 struct tc_net_impl;
@@ -97,6 +104,7 @@ struct Handle {
     double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
     int ctab_level = 0;        // level the table was built for (0 = none)
     cudaError_t enq_err = cudaSuccess;  // first error of an enqueue-only helper (checked by its caller)
+    int device = 0;                     // CUDA device the handle's memory lives on
     // learned initial guess
     tc_net_impl* net = nullptr;
     double* guess = nullptr;  // candidate start (level-1 layout)
@@ -359,7 +367,7 @@ void iterate_stream(Handle* h, int level, int dir) {
     Level& lv = h->lev[level];
     const int Niter = h->p.Nmulti;
     const bool cheb_pp = (level == h->ratio_level);
-    if (h->fuse_visits && level > 1 && Niter <= 128) {
+    if (h->fuse_visits && lv.fuse && level > 1 && Niter <= 128) {
         // the whole visit in one cluster launch (same arithmetic, same result)
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
@@ -424,7 +432,7 @@ void iterate_stream32(Handle* h, int level, int dir) {
     const int Niter = h->p.Nmulti;
     const bool cheb_pp = (level == h->ratio_level);
     const int pp = (dir != 1 && cheb_pp) ? 1 : 0;
-    if (h->fuse_visits && level > 1 && Niter <= 128) {
+    if (h->fuse_visits && lv.fuse && level > 1 && Niter <= 128) {
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
         if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, tv, Niter, pp, h->p.Vbc,
@@ -494,7 +502,7 @@ struct CycleGraphs {
 
 tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int arg, long long* nkernels) {
     cudaGraph_t g = nullptr;
-    const long long before = g_launches.load();
+    const long long before = t_launches;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     fn(h, arg);
     CK(cudaStreamEndCapture(h->st, &g));
@@ -502,8 +510,9 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
         cudaGraphDestroy(g);
         CK(h->enq_err);
     }
-    *nkernels = g_launches.load() - before;
+    *nkernels = t_launches - before;
     g_launches.fetch_sub(*nkernels);  // capturing enqueues nothing
+    t_launches -= *nkernels;
     cudaError_t e = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     if (e != cudaSuccess) { h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return TC_ERR_CUDA; }
@@ -823,6 +832,7 @@ tc_status create(Handle* h, const tc_params* in) {
     P.Tr_max = h->eb.Tr / s1.dr; P.Ts_max = h->eb.Tr / s1.ds;
     P.Trr_max = -h->eb.Trr / s1.dr2; P.Tss_max = -h->eb.Trr / s1.ds2;
     // ---- stream ----
+    cudaGetDevice(&h->device);
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return TC_ERR_CUDA; }
     h->own_stream = true;
@@ -875,6 +885,9 @@ tc_status create(Handle* h, const tc_params* in) {
         for (double** q : lf) TRY(dalloc_t(h, q, lp));
         for (int q = 0; q < 6; q++) TRY(dalloc_t(h, &lv.bak[q], lp));
         TRY(dalloc_t(h, &lv.coef, lp * TC_NCOEF));
+        lv.sweep_bx = BX;
+        lv.sweep_by = BY;
+        lv.fuse = 1;
         lv.coef32 = lv.dts32 = lv.cA32 = lv.cB32 = lv.rhs32 = lv.res32 = nullptr;
         lv.e32[0] = lv.e32[1] = nullptr;
         lv.e32cur = 0;
@@ -1011,6 +1024,44 @@ tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF,
 struct tc_handle {
     Handle h;
 };
+
+namespace {
+// time one replay of the launches `fn` enqueues, captured as a CUDA graph (ms)
+template <class F>
+tc_status graph_time(Handle* h, F&& fn, double* ms_out) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ge = nullptr;
+    const long long before = t_launches;
+    h->enq_err = cudaSuccess;
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    fn();
+    CK(cudaStreamEndCapture(h->st, &g));
+    g_launches.fetch_sub(t_launches - before);
+    t_launches = before;
+    if (h->enq_err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        CK(h->enq_err);
+    }
+    cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    CK(ie);
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaGraphLaunch(ge, h->st));
+    CK(cudaEventRecord(e0, h->st));
+    CK(cudaGraphLaunch(ge, h->st));
+    CK(cudaEventRecord(e1, h->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaGraphExecDestroy(ge);
+    *ms_out = ms;
+    return TC_OK;
+}
+}  // namespace
 
 extern "C" {
 
@@ -1210,6 +1261,108 @@ tc_status tc_step(tc_handle* H, tc_stats_row* row, int32_t* cycles, double* dt_o
     return TC_OK;
 }
 
+
+tc_status tc_autotune(tc_handle* H, int32_t* choices) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    const bool mixed = (h->p.solver_precision == 1);
+    const int G = h->grids;
+    // candidate block shapes (at most 256 threads: the kernels' launch bounds)
+    const int shapes[][2] = {{32, 8}, {64, 4}, {128, 2}, {256, 1}, {32, 4}, {16, 16}, {64, 2}, {16, 8}};
+    for (int l = 1; l < G; l++) {
+        Level& lv = h->lev[l];
+        // the timed sweeps and visits change the level's corrections: keep a copy
+        const size_t bytes = lv.L.plane * (mixed ? sizeof(float) : sizeof(double));
+        void* save[2] = {nullptr, nullptr};
+        for (int q = 0; q < 2; q++) {
+            CK(cudaMalloc(&save[q], bytes));
+            CK(cudaMemcpyAsync(save[q], mixed ? (void*)lv.e32[q] : (void*)lv.err[q], bytes, cudaMemcpyDeviceToDevice,
+                               h->st));
+        }
+        // block shape of the per-sweep smoother kernel
+        double best = 1e30;
+        int bb = 0;
+        for (int c = 0; c < (int)(sizeof(shapes) / sizeof(shapes[0])); c++) {
+            lv.sweep_bx = shapes[c][0];
+            lv.sweep_by = shapes[c][1];
+            double ms = 0;
+            TRY(graph_time(h, [&]() {
+                for (int n = 0; n < 20; n++) {
+                    if (mixed) launch_sweep32(h->st, lv, lv.e32[0], lv.e32[1], 1.0f, 0, 0.f, h->p.Vbc);
+                    else launch_sweep(h->st, lv, lv.err[0], lv.err[1], 1.0, 0, 0.0, h->p.Vbc);
+                }
+            }, &ms));
+            if (ms < best) { best = ms; bb = c; }
+        }
+        lv.sweep_bx = shapes[bb][0];
+        lv.sweep_by = shapes[bb][1];
+        // one cluster launch per visit or one launch per sweep
+        lv.fuse = 1;
+        if (l > 1 && h->fuse_visits && visit_cluster_fits(lv.L, h->p.Nmulti, mixed ? 1 : 0)) {
+            double t_fused = 0, t_plain = 0;
+            for (int f = 1; f >= 0; f--) {
+                lv.fuse = f;
+                double ms = 0;
+                TRY(graph_time(h, [&]() {
+                    for (int v = 0; v < 2; v++) {
+                        if (mixed) iterate_stream32(h, l, 1);
+                        else iterate_stream(h, l, 1);
+                    }
+                }, &ms));
+                (f ? t_fused : t_plain) = ms;
+            }
+            lv.fuse = (t_fused <= t_plain) ? 1 : 0;
+        }
+        for (int q = 0; q < 2; q++) {
+            CK(cudaMemcpyAsync(mixed ? (void*)lv.e32[q] : (void*)lv.err[q], save[q], bytes, cudaMemcpyDeviceToDevice,
+                               h->st));
+        }
+        CK(cudaStreamSynchronize(h->st));
+        for (int q = 0; q < 2; q++) cudaFree(save[q]);
+        if (choices) {
+            choices[3 * (l - 1) + 0] = lv.sweep_bx;
+            choices[3 * (l - 1) + 1] = lv.sweep_by;
+            choices[3 * (l - 1) + 2] = lv.fuse;
+        }
+    }
+    // the cycle graphs bake in launch shapes: capture again at the next solve
+    CycleGraphs& cg = *h->graphs;
+    if (cg.l1) cudaGraphExecDestroy(cg.l1);
+    if (cg.rest) cudaGraphExecDestroy(cg.rest);
+    cg.l1 = cg.rest = nullptr;
+    return TC_OK;
+}
+
+tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc_stats_row* rows, int32_t* cycles,
+                           double* dts, tc_status* status) {
+    if (!hs || n < 1 || nthreads < 1) return TC_ERR_ARG;
+    for (int i = 0; i < n; i++)
+        if (!hs[i]) return TC_ERR_ARG;
+    std::atomic<int> next{0};
+    std::vector<tc_status> st((size_t)n, TC_OK);
+    auto work = [&]() {
+        for (;;) {
+            const int i = next.fetch_add(1);
+            if (i >= n) break;
+            cudaSetDevice(hs[i]->h.device);
+            st[(size_t)i] = tc_step(hs[i], rows ? &rows[i] : nullptr, cycles ? &cycles[i] : nullptr,
+                                    dts ? &dts[i] : nullptr);
+        }
+    };
+    const int T = nthreads < n ? nthreads : n;
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    tc_status first = TC_OK;
+    for (int i = 0; i < n; i++) {
+        if (status) status[i] = st[(size_t)i];
+        if (first == TC_OK && st[(size_t)i] != TC_OK) first = st[(size_t)i];
+    }
+    return first;
+}
+
 tc_status tc_step_host(tc_handle* H, double* T, double* Cnew, double* SF, double* rtr, double* str,
                        const int32_t* Ttype, int64_t ntr, tc_stats_row* row, int32_t* cycles, double* dt_out) {
     if (!H || !T || !SF) return TC_ERR_ARG;
@@ -1256,11 +1409,12 @@ tc_status tc_time_sweep(tc_handle* H, int32_t level, int32_t nsweeps, double* ms
     // runs them (per-launch host overhead would otherwise dominate)
     cudaGraph_t g = nullptr;
     cudaGraphExec_t ge = nullptr;
-    const long long before = g_launches.load();
+    const long long before = t_launches;
     CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
     for (int n = 0; n < nsweeps; n++) sweep();
     CK(cudaStreamEndCapture(h->st, &g));
-    g_launches.fetch_sub(g_launches.load() - before);
+    g_launches.fetch_sub(t_launches - before);
+    t_launches = before;
     cudaError_t ie = cudaGraphInstantiate(&ge, g, 0);
     cudaGraphDestroy(g);
     CK(ie);

@@ -34,6 +34,17 @@ inline int nblocks_of(const Range2& r) {
     const int i = (r).i0 + (int)(blockIdx.x * BX + threadIdx.x); \
     const int k = (r).k0 + (int)(blockIdx.y * BY + threadIdx.y); \
     const bool inr = (i <= (r).i1) && (k <= (r).k1);
+// the same for kernels launched with a tuned block shape (blockDim.x x blockDim.y)
+#define RANGE_IK_DYN(r)                                \
+    const int i = (r).i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x); \
+    const int k = (r).k0 + (int)(blockIdx.y * blockDim.y + threadIdx.y); \
+    const bool inr = (i <= (r).i1) && (k <= (r).k1);
+inline dim3 grid_for_shape(const Range2& r, int bx, int by) {
+    int ni = r.i1 - r.i0 + 1, nk = r.k1 - r.k0 + 1;
+    if (ni < 1) ni = 1;
+    if (nk < 1) nk = 1;
+    return dim3((unsigned)((ni + bx - 1) / bx), (unsigned)((nk + by - 1) / by), 1);
+}
 
 enum { RED_SUM = 0, RED_MIN = 1, RED_MAX = 2 };
 

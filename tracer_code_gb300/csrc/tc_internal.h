@@ -91,6 +91,10 @@ struct Level {
     float *coef32, *dts32, *cA32, *cB32, *rhs32, *res32;
     float* e32[2];
     int e32cur;
+    // launch configuration of this level's smoother, set by tc_autotune
+    // (defaults: 32x8 blocks; fused visits wherever they fit)
+    int sweep_bx, sweep_by;
+    int fuse;  // 1 = one cluster launch per visit when the level fits, 0 = one launch per sweep
 };
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
