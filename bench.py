@@ -16,7 +16,7 @@ cpu_baseline, e2e, clocks and gpu_launches.
 
 reference: the CPU restatement of the reference (oracle/, OpenMP on all host
 cores) on the same workload; each step is a bounded sample (two multigrid
-calls capped at 1 and 2 W-cycles, one RK step without re-solves, one
+calls capped at 2 and 24 W-cycles, one RK step without re-solves, one
 tracer-ratio pass) from which the full timestep time is assembled with the
 workload's cycle count.
 """
@@ -40,6 +40,9 @@ UNIT = "timesteps/s"
 # assemble the CPU reference arm's timestep from its bounded sample when it
 # runs without the GPU arm in the same process.
 CYCLES_PER_STEP_DEFAULT = 228.0
+# W-cycle caps of the two CPU multigrid calls of one bounded sample (their
+# difference gives the time per cycle, about 10 s of CPU work per sample)
+CPU_SAMPLE_CYCLES = (2, 24)
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the level-1
 # smoother kernels from one ncu capture each (cold cache; the FP64 kernel in
 # profiles/multigrid_solve_1024x256.md, the FP32 one in
@@ -151,7 +154,8 @@ def cpu_sample(p, threads: int, cycles_per_step: float, seed: int = 1) -> dict:
     st = state.initial_state(p, seed=seed)
     q = p.copy()
     times = {}
-    for cap in (1, 2):
+    lo, hi = CPU_SAMPLE_CYCLES
+    for cap in (lo, hi):
         q.max_cycles = cap
         o2 = Oracle(q, threads=threads)
         o2.upload(st)
@@ -162,7 +166,7 @@ def cpu_sample(p, threads: int, cycles_per_step: float, seed: int = 1) -> dict:
             if e.status != 3:
                 raise
         times[cap] = time.perf_counter() - t0
-        if cap == 2:
+        if cap == hi:
             o2.compute_velocities()
             qq = q.copy()
             qq.RK_update = 0
@@ -179,8 +183,8 @@ def cpu_sample(p, threads: int, cycles_per_step: float, seed: int = 1) -> dict:
             times["tracers_to_corners"] = time.perf_counter() - t0
             o3.close()
         o2.close()
-    per_cycle = max(times[2] - times[1], 1e-9)
-    fixed = max(times[1] - per_cycle, 0.0)
+    per_cycle = max((times[hi] - times[lo]) / (hi - lo), 1e-9)
+    fixed = max(times[lo] - lo * per_cycle, 0.0)
     step = 4 * fixed + cycles_per_step * per_cycle + times["rk_step_no_resolve"] + 3 * times["tracers_to_corners"]
     return {"step_s": step, "per_cycle_s": per_cycle, "per_solve_fixed_s": fixed,
             "rk_step_no_resolve_s": times["rk_step_no_resolve"], "tracers_to_corners_s": times["tracers_to_corners"],
@@ -204,7 +208,7 @@ def run_reference(args, rank: int, world: int):
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_desc(p, "plain"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"per step: CPU restatement multigrid capped at 1 and 2 W-cycles, one RK4 step "
+                         "sample": f"per step: CPU restatement multigrid capped at {CPU_SAMPLE_CYCLES[0]} and {CPU_SAMPLE_CYCLES[1]} W-cycles, one RK4 step "
                                    f"without re-solves, one tracer-ratio pass; timestep assembled as "
                                    f"4*fixed + {CYCLES_PER_STEP_DEFAULT:g} cycles + RK + 3 ratio passes",
                          "parts": samples[-1]},
@@ -346,7 +350,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
             r = cpu_sample(pp, os.cpu_count() or 1, cps)
             line["cpu_baseline"] = {"value": 1.0 / r["step_s"], "unit": UNIT, "cores": os.cpu_count() or 1,
                                     "kind": "port",
-                                    "sample": f"CPU restatement (FP64), full workload: multigrid capped at 1 and 2 "
+                                    "sample": f"CPU restatement (FP64), full workload: multigrid capped at {CPU_SAMPLE_CYCLES[0]} and {CPU_SAMPLE_CYCLES[1]} "
                                               f"W-cycles, one RK4 step without re-solves, one tracer-ratio pass "
                                               f"({r['sample_s']:.1f} s); timestep = 4*fixed + {cps:g} cycles + RK "
                                               f"+ 3 ratio passes",
