@@ -130,7 +130,9 @@ typedef struct tc_params {
     int32_t solver_precision;
     /* No reference counterpart.  1 = start each multigrid solve from the
      * attached network's guess (tracer_nn.h) when its level-1 residual is
-     * below that of the previous streamfunction; 2 = always from the guess;
+     * below that of the previous streamfunction; after 8 rejections in a row
+     * the guess is offered on every 32nd solve only, until it is taken again
+     * (the plain start is used alone meanwhile); 2 = always from the guess;
      * 0 = always from the previous streamfunction. */
     int32_t learned_guess;
     /* Passes of a separable (1,2,1)/4 filter applied to the network's

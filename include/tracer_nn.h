@@ -68,7 +68,8 @@ tc_status tcnn_conv3x3(const uint16_t* x, int32_t nb, int32_t H, int32_t W, int3
  * than `capacity` are stored: raw[n][3][nz][nx] (channels as above, taken
  * when the solve starts) and sf_new[n][nz][nx] (the converged streamfunction).
  * tc_record_count returns how many are stored; tc_guess_stats how many
- * solves used the network's guess and how many were offered one. */
+ * solves used the network's guess and how many were offered one (solves
+ * skipped by the back-off of learned_guess = 1 are not offered one). */
 tc_status tc_attach_net(tc_handle* h, tc_net* net);
 tc_status tc_record_solves(tc_handle* h, float* raw, float* sf_new, int32_t capacity);
 int32_t tc_record_count(const tc_handle* h);

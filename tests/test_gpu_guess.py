@@ -4,8 +4,9 @@
     the converged streamfunction (FP32 images of the level-1 fields);
   - with any network attached (here an untrained one) every solve still
     meets the reference's tolerance: the solver starts from the network's
-    guess only when its level-1 residual is smaller, and Nu/Vrms/mass after
-    several steps agree with the run without the network to 1e-6 relative;
+    guess only when its level-1 residual is smaller (and stops offering it
+    after repeated rejections), and Nu/Vrms/mass after several steps agree
+    with the run without the network to 1e-6 relative;
   - the committed trained network (tracer_code_gb300/weights) lowers the
     W-cycle count of the mixed solver on a case whose physics it was not
     trained on (the gain is printed).
@@ -78,7 +79,9 @@ def test_untrained_guess_keeps_the_solution(gpu_lib, prec):
         rows.append([sim.step()[0] for _ in range(3)])
         if use:
             used, offered = learned.guess_stats(sim)
-            assert offered == 12
+            # 12 solves; after 8 rejections in a row the guess is offered on
+            # every 32nd solve only
+            assert 8 <= offered <= 12 and used <= offered
         sim.close()
         net.close()
     for a, b in zip(rows[0], rows[1]):

@@ -110,6 +110,11 @@ struct Handle {
     double* guess = nullptr;  // candidate start (level-1 layout)
     float* nn_raw = nullptr;  // network input scratch [3][nz][nx]
     long long guess_used = 0, guess_offered = 0;
+    // learned_guess = 1 stops offering the guess after kGuessPatience
+    // rejections in a row and then offers it on every kGuessProbe-th solve
+    // only (the plain start is then used alone, as it was chosen anyway)
+    int guess_reject_streak = 0;
+    long long guess_solves = 0;
     // training-sample recorder (caller-owned device buffers)
     float *rec_raw = nullptr, *rec_sf = nullptr;
     int rec_cap = 0, rec_count = 0;
@@ -554,7 +559,12 @@ tc_status multigrid(Handle* h) {
     if (rec)
         nn_fields_to_raw(h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1),
                          h->rec_raw + (size_t)h->rec_count * 3 * img);
-    const bool try_guess = (h->p.learned_guess == 1 || h->p.learned_guess == 2) && h->net != nullptr;
+    const int kGuessPatience = 8, kGuessProbe = 32;
+    bool try_guess = (h->p.learned_guess == 1 || h->p.learned_guess == 2) && h->net != nullptr;
+    if (try_guess && h->p.learned_guess == 1 && h->guess_reject_streak >= kGuessPatience &&
+        (h->guess_solves % kGuessProbe) != 0)
+        try_guess = false;
+    if (h->p.learned_guess != 0 && h->net != nullptr) h->guess_solves++;
     if (try_guess) {
         // candidate start from the network; with learned_guess = 1 it is kept
         // only if its level-1 residual is smaller
@@ -579,6 +589,9 @@ tc_status multigrid(Handle* h) {
         if (h->p.learned_guess == 2 || h->hs->res_mag[0] < h->hs->res_mag[1]) {
             copy_plane(h, cur_err(h, 1), h->guess);
             h->guess_used++;
+            h->guess_reject_streak = 0;
+        } else {
+            h->guess_reject_streak++;
         }
     }
     const double res_ref1 = h->hs->res_ref;
