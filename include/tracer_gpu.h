@@ -231,13 +231,15 @@ tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double
 
 /* Autotuner (no reference counterpart).  For each smoothed level it times,
  * on this handle's GPU and in its solver precision, the per-sweep smoother
- * kernel under eight block shapes of at most 256 threads and a fused
- * cluster visit against one
- * launch per sweep (CUDA-graph replays), and keeps the fastest of each.
- * Results are unchanged by the choice (the arithmetic per point does not
- * depend on the launch shape).  If `choices` is not NULL it receives
- * (block x, block y, fused) for levels 1..grids-1.  Needs uploaded state;
- * the levels' corrections are restored afterwards. */
+ * kernel under eight block shapes of at most 256 threads, and one launch per
+ * sweep against fused cluster visits of every shape that fits (1 or 2
+ * points per thread strip, 1 to 16 CTAs), with CUDA-graph replays, and keeps
+ * the fastest of each.  Results are unchanged by the choice (the arithmetic
+ * per point does not depend on the launch shape).  If `choices` is not NULL
+ * it receives (block x, block y, visit) for levels 1..grids-1, visit = 0 for
+ * one launch per sweep, 1 for the default fused shape, else 100 x points
+ * per strip + CTAs.  Needs uploaded state; the levels' corrections are
+ * restored afterwards. */
 tc_status tc_autotune(tc_handle* h, int32_t* choices);
 
 /* Ensemble of independent cases (no reference counterpart: the reference

@@ -445,14 +445,26 @@ struct VisitShape {
 // level whose rows fit; the sweep is bound by per-CTA shared-memory loads and
 // the exchange, so fuller CTAs win).  FP64: strips of 1 point spread over up
 // to 16 CTAs (the FP64 pipe of each SM is the bound, so more SMs win).
-static bool visit_shape(const Lay& L, int nsweeps, bool fp32, VisitShape* s) {
+//
+// cfg != 0 asks for a specific shape instead (tc_autotune): cfg = 100*P + C
+// with P = 1 (256 threads) or 2 (512 threads, FP32 only) points per strip and
+// C CTAs wanted; false if it does not fit.
+static bool visit_shape(const Lay& L, int nsweeps, bool fp32, int cfg, VisitShape* s) {
     const int cols = L.a - 1, rows = L.b - 1;
     if (nsweeps > VISIT_MAX_SWEEPS || rows < 2 || cols < 1) return false;
     s->w = w_class(L.a);
     if (s->w == 0) return false;
     const int spread_C = rows < VISIT_MAX_CLUSTER ? rows : VISIT_MAX_CLUSTER;
     const int spread_rpc = (rows + spread_C - 1) / spread_C;
-    if (fp32 && spread_rpc * cols > 256) {
+    if (cfg != 0) {
+        const int p = cfg / 100, want = cfg % 100;
+        if (!(p == 1 || (p == 2 && fp32)) || want < 1 || want > VISIT_MAX_CLUSTER) return false;
+        s->p = p;
+        s->nt = (p == 1) ? 256 : 512;
+        s->rpc = (rows + want - 1) / want;
+        s->C = (rows + s->rpc - 1) / s->rpc;
+        if ((s->nt / cols) * p < s->rpc) return false;
+    } else if (fp32 && spread_rpc * cols > 256) {
         // too many points to spread one per thread over 16 CTAs of 256:
         // 512 threads in strips of 2 (four warps per scheduler hide the
         // shared-memory and FMA latencies better than strips of 4 on 256)
@@ -479,9 +491,9 @@ static bool visit_shape(const Lay& L, int nsweeps, bool fp32, VisitShape* s) {
     return s->smem <= VISIT_SMEM_MAX;
 }
 
-int visit_cluster_fits(const Lay& L, int nsweeps, int fp32) {
+int visit_cluster_fits(const Lay& L, int nsweeps, int fp32, int cfg) {
     VisitShape s;
-    return visit_shape(L, nsweeps, fp32 != 0, &s) ? 1 : 0;
+    return visit_shape(L, nsweeps, fp32 != 0, cfg, &s) ? 1 : 0;
 }
 
 template <typename T>
@@ -527,9 +539,9 @@ static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const Visi
 template <typename T>
 static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* rhs, const T* dts, const T* ctab,
                    const T* cA, const T* cB, T* res, const double* cvals, const double* tvals, int nsweeps,
-                   int per_point, int Vbc, int* flag) {
+                   int per_point, int Vbc, int* flag, int cfg) {
     VisitShape sh;
-    if (!visit_shape(L, nsweeps, sizeof(T) == sizeof(float), &sh)) return 1;
+    if (!visit_shape(L, nsweeps, sizeof(T) == sizeof(float), cfg, &sh)) return 1;
     if (per_point && sizeof(T) == sizeof(double) && ctab == nullptr) return 1;
     VisitParams<T> Q;
     Q.L = L;
@@ -557,10 +569,10 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
                          const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag) {
     return visit_t<double>(s, lv.L, S, lv.coef, lv.rhs, lv.dt_stream, ctab, lv.cA, lv.cB, lv.res, cvals, tvals,
-                           nsweeps, per_point, Vbc, timeout_flag);
+                           nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg);
 }
 int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
                            int nsweeps, int per_point, int Vbc, int* timeout_flag) {
     return visit_t<float>(s, lv.L, S, lv.coef32, lv.rhs32, lv.dts32, nullptr, lv.cA32, lv.cB32, lv.res32, cvals,
-                          tvals, nsweeps, per_point, Vbc, timeout_flag);
+                          tvals, nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg);
 }

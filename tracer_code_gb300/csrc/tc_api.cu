@@ -901,6 +901,7 @@ tc_status create(Handle* h, const tc_params* in) {
         lv.sweep_bx = BX;
         lv.sweep_by = BY;
         lv.fuse = 1;
+        lv.visit_cfg = 0;
         lv.coef32 = lv.dts32 = lv.cA32 = lv.cB32 = lv.rhs32 = lv.res32 = nullptr;
         lv.e32[0] = lv.e32[1] = nullptr;
         lv.e32cur = 0;
@@ -1310,22 +1311,36 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         }
         lv.sweep_bx = shapes[bb][0];
         lv.sweep_by = shapes[bb][1];
-        // one cluster launch per visit or one launch per sweep
+        // one launch per sweep, or one cluster launch per visit in one of
+        // several shapes (points per strip x CTAs)
         lv.fuse = 1;
+        lv.visit_cfg = 0;
         if (l > 1 && h->fuse_visits && visit_cluster_fits(lv.L, h->p.Nmulti, mixed ? 1 : 0)) {
-            double t_fused = 0, t_plain = 0;
-            for (int f = 1; f >= 0; f--) {
-                lv.fuse = f;
-                double ms = 0;
-                TRY(graph_time(h, [&]() {
+            auto time_visits = [&](double* ms) {
+                return graph_time(h, [&]() {
                     for (int v = 0; v < 2; v++) {
                         if (mixed) iterate_stream32(h, l, 1);
                         else iterate_stream(h, l, 1);
                     }
-                }, &ms));
-                (f ? t_fused : t_plain) = ms;
+                }, ms);
+            };
+            double best_v = 1e30;
+            int best_cfg = -1;  // -1 = one launch per sweep
+            lv.fuse = 0;
+            TRY(time_visits(&best_v));
+            lv.fuse = 1;
+            std::vector<int> cfgs = {0};
+            for (int p : {1, 2})
+                for (int c : {1, 2, 4, 8, 16}) cfgs.push_back(100 * p + c);
+            for (int cfg : cfgs) {
+                if (!visit_cluster_fits(lv.L, h->p.Nmulti, mixed ? 1 : 0, cfg)) continue;
+                lv.visit_cfg = cfg;
+                double ms = 0;
+                TRY(time_visits(&ms));
+                if (ms < best_v) { best_v = ms; best_cfg = cfg; }
             }
-            lv.fuse = (t_fused <= t_plain) ? 1 : 0;
+            lv.fuse = (best_cfg >= 0) ? 1 : 0;
+            lv.visit_cfg = (best_cfg > 0) ? best_cfg : 0;
         }
         for (int q = 0; q < 2; q++) {
             CK(cudaMemcpyAsync(mixed ? (void*)lv.e32[q] : (void*)lv.err[q], save[q], bytes, cudaMemcpyDeviceToDevice,
@@ -1336,7 +1351,7 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         if (choices) {
             choices[3 * (l - 1) + 0] = lv.sweep_bx;
             choices[3 * (l - 1) + 1] = lv.sweep_by;
-            choices[3 * (l - 1) + 2] = lv.fuse;
+            choices[3 * (l - 1) + 2] = lv.fuse ? (lv.visit_cfg ? lv.visit_cfg : 1) : 0;
         }
     }
     // the cycle graphs bake in launch shapes: capture again at the next solve

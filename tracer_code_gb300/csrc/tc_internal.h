@@ -94,7 +94,8 @@ struct Level {
     // launch configuration of this level's smoother, set by tc_autotune
     // (defaults: 32x8 blocks; fused visits wherever they fit)
     int sweep_bx, sweep_by;
-    int fuse;  // 1 = one cluster launch per visit when the level fits, 0 = one launch per sweep
+    int fuse;       // 1 = one cluster launch per visit when the level fits, 0 = one launch per sweep
+    int visit_cfg;  // shape of the fused visit: 0 = default, else 100*points per strip + CTAs
 };
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
@@ -136,7 +137,7 @@ void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n)
 
 // (k_visit.cu) one whole smoother visit of a small level as one cluster launch
 int visit_cluster_setup();
-int visit_cluster_fits(const Lay& L, int nsweeps, int fp32);
+int visit_cluster_fits(const Lay& L, int nsweeps, int fp32, int cfg = 0);
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab);
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
                          const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag);
