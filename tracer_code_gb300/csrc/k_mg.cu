@@ -231,6 +231,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
                         const double* __restrict__ coef, const double* __restrict__ rhs,
                         const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
                         double c_uniform, int per_point, double temp, int Vbc) {
+    pdl_entry();
     RANGE_IK_DYN(r);
     if (!inr) return;
     size_t x = IX(L, i, k);
@@ -238,18 +239,19 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
     double c = per_point ? 2.0 / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
     double v = fma(c * __ldg(dts + x), res, __ldg(Sin + x));
     store_stream(L, Sout, i, k, v, Vbc);
+    pdl_done();
 }
 void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
                   int per_point, double temp, int Vbc) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
-    k_sweep<<<grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s>>>(
-        lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
+    launch_pdl(k_sweep, grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
                                                   c_uniform, per_point, temp, Vbc); tc_note_launch();
 }
 
 __global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
                            const double* __restrict__ rhs, double* __restrict__ res, RedScratch rs, double* out,
                            double div1, double div2) {
+    pdl_entry();
     RANGE_IK(r);
     double a = 0.0;
     if (inr) {
@@ -259,25 +261,29 @@ __global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const doub
         a = fabs(v);
     }
     reduce_to(RED_SUM, a, rs.part, rs.count, out, div1, div2);
+    pdl_done();
 }
 void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
-    k_residual<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef, lv.rhs, lv.res, rs, res_out,
+    launch_pdl(k_residual, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef, lv.rhs, lv.res, rs, res_out,
                                                      (double)(lv.L.a - 1), (double)(lv.L.b - 1)); tc_note_launch();
 }
 
 __global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     rc[IX(C, i, k)] = restrict9(rf, F, 2 * i, 2 * k);
+    pdl_done();
 }
 void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c) {
     Range2 r{1, coarse.L.a - 1, 1, coarse.L.b - 1};
-    k_restrict_res<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_res, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
 }
 
 // prolong (bilinear, additive) with the fine level's stream BCs fused
 __global__ void k_prolong(Lay C, Lay F, Range2 r, const double* __restrict__ ec, double* __restrict__ ef, int Vbc) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     size_t x = IX(F, i, k);
@@ -290,10 +296,11 @@ __global__ void k_prolong(Lay C, Lay F, Range2 r, const double* __restrict__ ec,
         add = (ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
                ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / 4.0;
     store_stream(F, ef, i, k, ef[x] + add, Vbc);
+    pdl_done();
 }
 void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc) {
     Range2 r{1, fine.L.a - 1, 1, fine.L.b - 1};
-    k_prolong<<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
+    launch_pdl(k_prolong, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
 }
 
 // enforceBCs_stream: walls zero, ghosts mirrored from the interior
@@ -524,6 +531,7 @@ void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, 
 // unknowns are zero (walls); ghosts are written with the stream BCs.
 __global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
                                const double* __restrict__ rhs, int n, double* __restrict__ err, int Vbc) {
+    pdl_entry();
     const int lane = threadIdx.x & 31;
     const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // 0-based row
     if (pw >= n) return;
@@ -539,23 +547,26 @@ __global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const dou
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
     if (lane == 0) store_stream(L, err, ip, kp, acc, Vbc);
+    pdl_done();
 }
 void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
                          int Vbc) {
     const int threads = 256;
     const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
-    k_coarse_apply<<<nb, threads, 0, s>>>(lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
+    launch_pdl(k_coarse_apply, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
 }
 
 __global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+    pdl_entry();
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t st = (size_t)gridDim.x * blockDim.x;
     for (; t < n; t += st) dst[t] = src[t];
+    pdl_done();
 }
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n) {
     int nb = (int)((n + 255) / 256);
     if (nb > 1216) nb = 1216;
-    k_copy<<<nb, 256, 0, s>>>(dst, src, n); tc_note_launch();
+    launch_pdl(k_copy, nb, 256, 0, s, dst, src, n); tc_note_launch();
 }
 
 // compute_RHS(1) and compute_reference_residual(1)

@@ -38,6 +38,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
                                                    float* __restrict__ Sout, const float* __restrict__ coef, const float* __restrict__ rhs,
                           const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
                           float c_uniform, int per_point, float temp, int Vbc) {
+    pdl_entry();
     RANGE_IK_DYN(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
@@ -45,21 +46,26 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
     const float c = per_point ? 2.0f / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
     const float v = fmaf(c * __ldg(dts + x), res, __ldg(Sin + x));
     store_stream<float>(L, Sout, i, k, v, Vbc);
+    pdl_done();
 }
 
 __global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
                              const float* __restrict__ rhs, float* __restrict__ res) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
     res[x] = folded_residual<float>(L, S, coef, __ldg(rhs + x), x);
+    pdl_done();
 }
 
 template <typename Tin>
 __global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ rf, float* __restrict__ rc) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     rc[IX(C, i, k)] = (float)restrict9<Tin>(rf, F, 2 * i, 2 * k);
+    pdl_done();
 }
 
 // bilinear prolongation value of the coarse correction at fine (i,k)
@@ -75,32 +81,39 @@ __device__ __forceinline__ T prolong_value(const Lay& C, const float* __restrict
 
 template <typename T>
 __global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* __restrict__ ec, T* __restrict__ ef, int Vbc) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(F, i, k);
     store_stream<T>(F, ef, i, k, ef[x] + prolong_value<T>(C, ec, i, k), Vbc);
+    pdl_done();
 }
 
 // FP64 residual of psi, rounded to FP32 as the RHS of the level-1 correction
 __global__ void __launch_bounds__(256, 1) k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
                                 const double* __restrict__ rhs, float* __restrict__ rhs32) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
     rhs32[x] = (float)folded_residual<double>(L, S, coef, __ldg(rhs + x), x);
+    pdl_done();
 }
 
 // psi += e in FP64, ghosts from the new interior value
 __global__ void k_update64(Lay L, Range2 r, double* __restrict__ S, const float* __restrict__ e, int Vbc) {
+    pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
     store_stream<double>(L, S, i, k, S[x] + (double)e[x], Vbc);
+    pdl_done();
 }
 
 // coarsest level: x = A^-1 (RowB .* rhs) in FP64 from the FP32 RHS, stored as FP32
 __global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
                                  const float* __restrict__ rhs, int n, float* __restrict__ err, int Vbc) {
+    pdl_entry();
     const int lane = threadIdx.x & 31;
     const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (pw >= n) return;
@@ -116,6 +129,7 @@ __global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const d
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
     if (lane == 0) store_stream<float>(L, err, ip, kp, (float)acc, Vbc);
+    pdl_done();
 }
 
 Range2 interior(const Lay& L) { return Range2{1, L.a - 1, 1, L.b - 1}; }
@@ -134,50 +148,49 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb) {
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc) {
     const Range2 r = interior(lv.L);
-    k_sweep32<<<grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s>>>(
-        lv.L, r, Sin, Sout, lv.coef32, lv.rhs32, lv.dts32, lv.cA32, lv.cB32, c_uniform, per_point, temp, Vbc);
+    launch_pdl(k_sweep32, grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef32, lv.rhs32, lv.dts32, lv.cA32, lv.cB32, c_uniform, per_point, temp, Vbc);
     tc_note_launch();
 }
 
 void launch_residual32(cudaStream_t s, const Level& lv, const float* S) {
     const Range2 r = interior(lv.L);
-    k_residual32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef32, lv.rhs32, lv.res32); tc_note_launch();
+    launch_pdl(k_residual32, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef32, lv.rhs32, lv.res32); tc_note_launch();
 }
 
 void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c) {
     const Range2 r = interior(coarse.L);
-    k_restrict_to32<float><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_to32<float>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
 }
 
 void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c) {
     const Range2 r = interior(coarse.L);
-    k_restrict_to32<double><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_to32<double>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
 }
 
 void launch_prolong32(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, float* ef, int Vbc) {
     const Range2 r = interior(fine.L);
-    k_prolong_add<float><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
+    launch_pdl(k_prolong_add<float>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, ec, ef, Vbc); tc_note_launch();
 }
 
 void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, double* S,
                            int Vbc) {
     const Range2 r = interior(fine.L);
-    k_prolong_add<double><<<grid_for(r), dim3(BX, BY), 0, s>>>(coarse.L, fine.L, r, ec, S, Vbc); tc_note_launch();
+    launch_pdl(k_prolong_add<double>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, ec, S, Vbc); tc_note_launch();
 }
 
 void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32) {
     const Range2 r = interior(lv.L);
-    k_residual_to32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, lv.coef, lv.rhs, rhs32); tc_note_launch();
+    launch_pdl(k_residual_to32, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef, lv.rhs, rhs32); tc_note_launch();
 }
 
 void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc) {
     const Range2 r = interior(lv.L);
-    k_update64<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, S, e, Vbc); tc_note_launch();
+    launch_pdl(k_update64, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, e, Vbc); tc_note_launch();
 }
 
 void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
                            int Vbc) {
     const int threads = 256;
     const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
-    k_coarse_apply32<<<nb, threads, 0, s>>>(lv.L, Ainv, rowb, lv.rhs32, n, err, Vbc); tc_note_launch();
+    launch_pdl(k_coarse_apply32, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs32, n, err, Vbc); tc_note_launch();
 }

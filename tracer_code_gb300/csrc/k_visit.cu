@@ -115,6 +115,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
                                                          const T* __restrict__ dts, const T* __restrict__ ctab,
                                                          const T* __restrict__ cA, const T* __restrict__ cB,
                                                          T* __restrict__ res, int* __restrict__ timeout_flag) {
+    pdl_entry();
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     const Lay& L = Q.L;
@@ -372,6 +373,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
     }
     __threadfence();
     cl.sync();  // global rows written; no CTA leaves while another may still address its shared memory
+    pdl_done();
     if (timed_out) return;
     // top/bottom ghost rows from the (now global) interior rows
     if (me == 0 || me == C - 1) {
@@ -526,13 +528,15 @@ static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const Visi
     cfg.blockDim = dim3((unsigned)NT, 1, 1);
     cfg.dynamicSmemBytes = sh.smem;
     cfg.stream = s;
-    cudaLaunchAttribute attr[1];
+    cudaLaunchAttribute attr[2];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = (unsigned)sh.C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
+    attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[1].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = 2;
     return cudaLaunchKernelEx(&cfg, kern, Q, S, coef, rhs, dts, ctab, cA, cB, res, flag);
 }
 

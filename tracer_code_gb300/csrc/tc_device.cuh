@@ -172,3 +172,31 @@ __device__ __forceinline__ void store_stream(const Lay& L, T* __restrict__ S, in
     for (int u = 0; u < nk; u++)
         for (int t = 0; t < ng; t++) S[IX(L, gi[t], gk[u])] = (si[t] * sk[u]) * v;
 }
+
+// ---------------------------------------------------------------------------
+// Programmatic dependent launch.  Kernels of the multigrid cycle start with
+// pdl_entry(), which waits until the previous kernel of the stream has
+// completed and its writes are visible (griddepcontrol.wait), and end with
+// pdl_done(), which lets the next kernel be scheduled while this one drains
+// (griddepcontrol.launch_dependents; a thread that returns early counts as
+// done).  launch_pdl() launches with the attribute that allows the early
+// scheduling; without it both calls cost nothing.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pdl_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_done() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
+}
