@@ -269,16 +269,27 @@ void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratc
                                                      (double)(lv.L.a - 1), (double)(lv.L.b - 1)); tc_note_launch();
 }
 
-__global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc) {
+__global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc,
+                               double* __restrict__ zero, size_t zn) {
     pdl_entry();
+    if (zero != nullptr) {
+        // clear the level's correction plane in the same launch (grid-stride)
+        const size_t nt = (size_t)gridDim.x * gridDim.y * blockDim.x * blockDim.y;
+        const size_t t0 = ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x * blockDim.y +
+                          (size_t)threadIdx.y * blockDim.x + threadIdx.x;
+        for (size_t t = t0; t < zn; t += nt) zero[t] = 0.0;
+    }
     RANGE_IK(r);
     if (!inr) return;
     rc[IX(C, i, k)] = restrict9(rf, F, 2 * i, 2 * k);
     pdl_done();
 }
-void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c) {
+void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c,
+                         double* zero) {
     Range2 r{1, coarse.L.a - 1, 1, coarse.L.b - 1};
-    launch_pdl(k_restrict_res, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_res, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c, zero,
+               zero ? coarse.L.plane : (size_t)0);
+    tc_note_launch();
 }
 
 // prolong (bilinear, additive) with the fine level's stream BCs fused

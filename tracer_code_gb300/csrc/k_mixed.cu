@@ -59,9 +59,22 @@ __global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const fl
     pdl_done();
 }
 
+// zero[0..zn) = 0 over the whole launch (grid-stride), so a correction plane
+// can be cleared in the same kernel that writes its level's RHS
+template <typename T>
+__device__ __forceinline__ void zero_plane(T* __restrict__ z, size_t zn) {
+    if (z == nullptr) return;
+    const size_t nt = (size_t)gridDim.x * gridDim.y * blockDim.x * blockDim.y;
+    const size_t t0 = ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x * blockDim.y +
+                      (size_t)threadIdx.y * blockDim.x + threadIdx.x;
+    for (size_t t = t0; t < zn; t += nt) z[t] = T(0);
+}
+
 template <typename Tin>
-__global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ rf, float* __restrict__ rc) {
+__global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ rf, float* __restrict__ rc,
+                                float* __restrict__ zero, size_t zn) {
     pdl_entry();
+    zero_plane(zero, zn);
     RANGE_IK(r);
     if (!inr) return;
     rc[IX(C, i, k)] = (float)restrict9<Tin>(rf, F, 2 * i, 2 * k);
@@ -91,8 +104,10 @@ __global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* __restrict__ 
 
 // FP64 residual of psi, rounded to FP32 as the RHS of the level-1 correction
 __global__ void __launch_bounds__(256, 1) k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
-                                const double* __restrict__ rhs, float* __restrict__ rhs32) {
+                                const double* __restrict__ rhs, float* __restrict__ rhs32,
+                                float* __restrict__ zero, size_t zn) {
     pdl_entry();
+    zero_plane(zero, zn);
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
@@ -157,14 +172,20 @@ void launch_residual32(cudaStream_t s, const Level& lv, const float* S) {
     launch_pdl(k_residual32, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef32, lv.rhs32, lv.res32); tc_note_launch();
 }
 
-void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c) {
+void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c,
+                       float* zero) {
     const Range2 r = interior(coarse.L);
-    launch_pdl(k_restrict_to32<float>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_to32<float>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c, zero,
+               zero ? coarse.L.plane : (size_t)0);
+    tc_note_launch();
 }
 
-void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c) {
+void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c,
+                           float* zero) {
     const Range2 r = interior(coarse.L);
-    launch_pdl(k_restrict_to32<double>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c); tc_note_launch();
+    launch_pdl(k_restrict_to32<double>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, rf, rhs_c, zero,
+               zero ? coarse.L.plane : (size_t)0);
+    tc_note_launch();
 }
 
 void launch_prolong32(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, float* ef, int Vbc) {
@@ -178,9 +199,11 @@ void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fin
     launch_pdl(k_prolong_add<double>, grid_for(r), dim3(BX, BY), 0, s, coarse.L, fine.L, r, ec, S, Vbc); tc_note_launch();
 }
 
-void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32) {
+void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32, float* zero) {
     const Range2 r = interior(lv.L);
-    launch_pdl(k_residual_to32, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef, lv.rhs, rhs32); tc_note_launch();
+    launch_pdl(k_residual_to32, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, lv.coef, lv.rhs, rhs32, zero,
+               zero ? lv.L.plane : (size_t)0);
+    tc_note_launch();
 }
 
 void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc) {

@@ -412,10 +412,10 @@ void enqueue_cycle_rest(Handle* h) {
     for (int pp = 2; pp <= h->nsteps; pp++) {
         const int level = h->multi[pp];
         const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
-        if (h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse)
-            cudaMemsetAsync(cur_err(h, level), 0, sizeof(double) * h->lev[level].L.plane, h->st);
+        const bool zero = h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse;
         if (h->multi[pp - 1] < h->multi[pp] && level > 1)
-            launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs);
+            launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs,
+                                zero ? cur_err(h, level) : nullptr);
         if (level < G) {
             iterate_stream(h, level, dir);
         } else {
@@ -465,8 +465,7 @@ void iterate_stream32(Handle* h, int level, int dir) {
 // correction from zero, psi += e (FP64), FP64 residual and its L1 mean
 void enqueue_l1_mixed(Handle* h, int dir) {
     Level& l1 = h->lev[1];
-    launch_residual_to32(h->st, l1, cur_err(h, 1), l1.rhs32);
-    CKV(cudaMemsetAsync(cur_e32(h, 1), 0, sizeof(float) * l1.L.plane, h->st));
+    launch_residual_to32(h->st, l1, cur_err(h, 1), l1.rhs32, cur_e32(h, 1));
     iterate_stream32(h, 1, dir);
     launch_update64(h->st, l1, cur_err(h, 1), cur_e32(h, 1), h->p.Vbc);
     launch_residual(h->st, l1, cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
@@ -479,12 +478,12 @@ void enqueue_rest_mixed(Handle* h, int) {
         const int level = h->multi[pp];
         const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
         const bool down = h->multi[pp - 1] < h->multi[pp];
-        if (down && level > 1 && level < G && h->p.mg_zero_coarse)
-            CKV(cudaMemsetAsync(cur_e32(h, level), 0, sizeof(float) * h->lev[level].L.plane, h->st));
+        float* zero = (down && level > 1 && level < G && h->p.mg_zero_coarse) ? cur_e32(h, level) : nullptr;
         if (down && level == 2)
-            launch_restrict64to32(h->st, h->lev[2], h->lev[1], h->lev[1].res, h->lev[2].rhs32);
+            launch_restrict64to32(h->st, h->lev[2], h->lev[1], h->lev[1].res, h->lev[2].rhs32, zero);
         else if (down && level > 2)
-            launch_restrict32(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res32, h->lev[level].rhs32);
+            launch_restrict32(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res32, h->lev[level].rhs32,
+                              zero);
         if (level < G) iterate_stream32(h, level, dir);
         else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_e32(h, G), h->p.Vbc);
         if (h->multi[pp + 1] < h->multi[pp]) {

@@ -124,7 +124,9 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
 void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
                   int per_point, double temp, int Vbc);
 void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out);
-void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c);
+// zero != null: also clears that plane (the coarse level's correction) in the same launch
+void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, double* rhs_c,
+                         double* zero = nullptr);
 void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc);
 void launch_stream_bcs(cudaStream_t s, const Level& lv, double* S, int Vbc);
 void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* rowb, int kl, int ku, int Vbc);
@@ -149,12 +151,14 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc);
 void launch_residual32(cudaStream_t s, const Level& lv, const float* S);
-void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c);
-void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c);
+void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c,
+                       float* zero = nullptr);
+void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c,
+                           float* zero = nullptr);
 void launch_prolong32(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, float* ef, int Vbc);
 void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fine, const float* ec, double* S,
                            int Vbc);
-void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32);
+void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32, float* zero = nullptr);
 void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc);
 void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
                            int Vbc);
