@@ -231,13 +231,23 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
                         const double* __restrict__ coef, const double* __restrict__ rhs,
                         const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
                         double c_uniform, int per_point, double temp, int Vbc) {
-    pdl_entry();
     RANGE_IK_DYN(r);
+    const size_t x = inr ? IX(L, i, k) : 0;
+    // coefficients, dt and Chebyshev denominators do not change within a solve
+    double cf[TC_NCOEF], dt = 0.0, ca = 1.0, cb = 0.0;
+    if (inr) {
+        fold_coefs(L, coef, x, cf);
+        dt = __ldg(dts + x);
+        if (per_point) {
+            ca = __ldg(cA + x);
+            cb = __ldg(cB + x);
+        }
+    }
+    pdl_entry();
     if (!inr) return;
-    size_t x = IX(L, i, k);
-    double res = folded_residual(L, Sin, coef, __ldg(rhs + x), x);
-    double c = per_point ? 2.0 / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
-    double v = fma(c * __ldg(dts + x), res, __ldg(Sin + x));
+    double res = fold_apply(L, Sin, x, cf, __ldg(rhs + x));
+    double c = per_point ? 2.0 / (ca + cb * temp) : c_uniform;
+    double v = fma(c * dt, res, __ldg(Sin + x));
     store_stream(L, Sout, i, k, v, Vbc);
     pdl_done();
 }
@@ -251,12 +261,14 @@ void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* So
 __global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
                            const double* __restrict__ rhs, double* __restrict__ res, RedScratch rs, double* out,
                            double div1, double div2) {
-    pdl_entry();
     RANGE_IK(r);
     double a = 0.0;
+    double cf[TC_NCOEF];
+    if (inr) fold_coefs(L, coef, IX(L, i, k), cf);
+    pdl_entry();
     if (inr) {
         size_t x = IX(L, i, k);
-        double v = folded_residual(L, S, coef, __ldg(rhs + x), x);
+        double v = fold_apply(L, S, x, cf, __ldg(rhs + x));
         res[x] = v;
         a = fabs(v);
     }

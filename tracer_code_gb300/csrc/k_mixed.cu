@@ -38,24 +38,36 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
                                                    float* __restrict__ Sout, const float* __restrict__ coef, const float* __restrict__ rhs,
                           const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
                           float c_uniform, int per_point, float temp, int Vbc) {
-    pdl_entry();
     RANGE_IK_DYN(r);
+    const size_t x = inr ? IX(L, i, k) : 0;
+    // coefficients, dt and Chebyshev denominators do not change within a solve
+    float cf[TC_NCOEF], dt = 0.f, ca = 1.f, cb = 0.f;
+    if (inr) {
+        fold_coefs<float>(L, coef, x, cf);
+        dt = __ldg(dts + x);
+        if (per_point) {
+            ca = __ldg(cA + x);
+            cb = __ldg(cB + x);
+        }
+    }
+    pdl_entry();
     if (!inr) return;
-    const size_t x = IX(L, i, k);
-    const float res = folded_residual<float>(L, Sin, coef, __ldg(rhs + x), x);
-    const float c = per_point ? 2.0f / (__ldg(cA + x) + __ldg(cB + x) * temp) : c_uniform;
-    const float v = fmaf(c * __ldg(dts + x), res, __ldg(Sin + x));
+    const float res = fold_apply<float>(L, Sin, x, cf, __ldg(rhs + x));
+    const float c = per_point ? 2.0f / (ca + cb * temp) : c_uniform;
+    const float v = fmaf(c * dt, res, __ldg(Sin + x));
     store_stream<float>(L, Sout, i, k, v, Vbc);
     pdl_done();
 }
 
 __global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
                              const float* __restrict__ rhs, float* __restrict__ res) {
-    pdl_entry();
     RANGE_IK(r);
+    const size_t x = inr ? IX(L, i, k) : 0;
+    float cf[TC_NCOEF];
+    if (inr) fold_coefs<float>(L, coef, x, cf);
+    pdl_entry();
     if (!inr) return;
-    const size_t x = IX(L, i, k);
-    res[x] = folded_residual<float>(L, S, coef, __ldg(rhs + x), x);
+    res[x] = fold_apply<float>(L, S, x, cf, __ldg(rhs + x));
     pdl_done();
 }
 

@@ -115,7 +115,6 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
                                                          const T* __restrict__ dts, const T* __restrict__ ctab,
                                                          const T* __restrict__ cA, const T* __restrict__ cB,
                                                          T* __restrict__ res, int* __restrict__ timeout_flag) {
-    pdl_entry();
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     const Lay& L = Q.L;
@@ -132,31 +131,6 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
     const size_t bsz = (size_t)R * W;
     const int tid = threadIdx.x;
     const T zsgn = (Q.Vbc == 1) ? T(1) : T(-1);
-    // rows k0-2..k1+2 (ghosts, walls and halos) into every buffer; four
-    // independent global loads in flight per thread
-    {
-        const int wa = a + 1 + 2 * SP, n_el = (k1 - k0 + 5) * wa;
-        for (int t0 = tid; t0 < n_el; t0 += 4 * NT) {
-            T v[4];
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int t = t0 + u * NT;
-                const int r = t / wa, c = t % wa, k = k0 - 2 + r;
-                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? Sg[IX(L, c - SP, k)] : T(0);
-            }
-#pragma unroll
-            for (int u = 0; u < 4; u++) {
-                const int t = t0 + u * NT;
-                if (t >= n_el) break;
-                const int r = t / wa, c = t % wa;
-                for (int q = 0; q < nbuf; q++) buf[q * bsz + (size_t)r * W + c] = v[u];
-            }
-        }
-    }
-    if (tid == 0 && C > 1) {
-        for (int q = 0; q < 3; q++) mbar_init(smem_addr(&bar[q]), 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
     // this thread's strip
     const int cols = a - 1;
     const int i = 1 + tid % cols, strip = tid / cols;
@@ -185,7 +159,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
         const size_t xg = IX(L, i, act[p] ? k : k0);
 #pragma unroll
         for (int d = 0; d < TC_NCOEF; d++) cf[p][d] = act[p] ? -__ldg(coef + xg + (size_t)d * L.plane) : T(0);
-        rh[p] = act[p] ? __ldg(rhs + xg) : T(0);
+        rh[p] = T(0);
         dt[p] = act[p] ? __ldg(dts + xg) : T(0);
         ca[p] = (kDivide && Q.per_point && act[p]) ? __ldg(cA + xg) : T(1);
         cbv[p] = (kDivide && Q.per_point && act[p]) ? __ldg(cB + xg) : T(0);
@@ -198,6 +172,37 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
             const int ok0 = 1 + o * rpc, ok1 = min(b - 1, ok0 + rpc - 1);
             if ((k >= ok0 - 2 && k <= ok0 - 1) || (k >= ok1 + 1 && k <= ok1 + 2)) remote |= 1 << (4 * p + j);
         }
+    }
+    // everything above is fixed within a solve; the RHS and the level's state
+    // come from earlier kernels of the stream
+    pdl_entry();
+#pragma unroll
+    for (int p = 0; p < P; p++)
+        if (act[p]) rh[p] = __ldg(rhs + IX(L, i, kr + p));
+    // rows k0-2..k1+2 (ghosts, walls and halos) into every buffer; four
+    // independent global loads in flight per thread
+    {
+        const int wa = a + 1 + 2 * SP, n_el = (k1 - k0 + 5) * wa;
+        for (int t0 = tid; t0 < n_el; t0 += 4 * NT) {
+            T v[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * NT;
+                const int r = t / wa, c = t % wa, k = k0 - 2 + r;
+                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? Sg[IX(L, c - SP, k)] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int t = t0 + u * NT;
+                if (t >= n_el) break;
+                const int r = t / wa, c = t % wa;
+                for (int q = 0; q < nbuf; q++) buf[q * bsz + (size_t)r * W + c] = v[u];
+            }
+        }
+    }
+    if (tid == 0 && C > 1) {
+        for (int q = 0; q < 3; q++) mbar_init(smem_addr(&bar[q]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // bytes this CTA receives per sweep: its halo rows that other CTAs own
     int expect = 0;

@@ -153,6 +153,30 @@ __device__ __forceinline__ T folded_residual(const Lay& L, const T* __restrict__
     return acc;
 }
 
+// folded_residual in two phases, so that a kernel can load the coefficient
+// planes (written once per multigrid call) before it waits for the previous
+// kernel of the stream, and the stencil values and RHS after: same terms,
+// same order, same result
+template <typename T>
+__device__ __forceinline__ void fold_coefs(const Lay& L, const T* __restrict__ coef, size_t x, T* c) {
+    const size_t pl = L.plane;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) c[d] = __ldg(coef + x + d * pl);
+}
+template <typename T>
+__device__ __forceinline__ T fold_apply(const Lay& L, const T* __restrict__ S, size_t x, const T* c, T rhs) {
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const T* s = S + x;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    T v[TC_NCOEF];
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) v[d] = __ldg(s + off[d]);
+    T acc = rhs;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) acc = fma(-c[d], v[d], acc);
+    return acc;
+}
+
 // writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
 // derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
 template <typename T>
