@@ -241,6 +241,13 @@ tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double
  * per strip + CTAs.  Needs uploaded state; the levels' corrections are
  * restored afterwards. */
 tc_status tc_autotune(tc_handle* h, int32_t* choices);
+/* Applies launch shapes in tc_autotune's `choices` format (3 ints per level
+ * 1..grids-1: sweep block x, block y, visit = 0 one launch per sweep / 1
+ * default fused visit / 100*P + C), e.g. shapes tuned once on another handle
+ * of the same grid and precision.  TC_ERR_ARG (nothing changed) if a block
+ * has more than 256 threads or a visit shape does not fit its level.  Shapes
+ * do not change the arithmetic. */
+tc_status tc_set_launch_shapes(tc_handle* h, const int32_t* choices);
 
 /* Ensemble of independent cases (no reference counterpart: the reference
  * runs one case per process).  One tc_step on each of the n handles, the

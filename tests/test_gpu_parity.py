@@ -195,3 +195,68 @@ def test_fault_cycle_cap(gpu_lib):
     with pytest.raises(TracerError) as e:
         g.multigrid()
     assert e.value.status == 3
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_every_visit_shape_matches_per_sweep_launches(gpu_lib, prec):
+    """Every fused-visit shape that fits (1 or 2 points per strip, 1-16 CTAs),
+    applied through tc_set_launch_shapes, ends the solve in the state one
+    launch per sweep reaches, bit for bit."""
+    p = case_1024_like(nx=256, nz=64, grids=5, tpc=2)
+    p.mg_zero_coarse = 1
+    p.solver_precision = prec
+    st = fresh_state(p)
+
+    def solve(shapes):
+        g = Simulation(p)
+        g.upload(st)
+        if shapes is not None:
+            g.set_launch_shapes(shapes)
+        q = g.multigrid()
+        out = (q, g.download()["SF"], [g.get("error", l) for l in range(2, g.info.grids)])
+        g.close()
+        return out
+
+    g = Simulation(p)
+    nlev = g.info.grids - 1
+    base = [(32, 8, 0)] * nlev
+    ref = solve(base)
+    tried = 0
+    cfgs = [100 * P + C for P in ((1, 2) if prec == 1 else (1,)) for C in (1, 2, 4, 8, 16)]
+    for cfg in cfgs:
+        # the shape on every level it fits, per-sweep launches elsewhere
+        shapes = list(base)
+        for l in range(2, nlev + 1):
+            trial = list(shapes)
+            trial[l - 1] = (32, 8, cfg)
+            try:
+                g.set_launch_shapes(trial)
+            except TracerError:
+                continue
+            shapes = trial
+        if shapes == base:
+            continue
+        tried += 1
+        out = solve(shapes)
+        assert out[0] == ref[0], cfg
+        assert np.array_equal(out[1], ref[1]), cfg
+        for a, b in zip(out[2], ref[2]):
+            assert np.array_equal(a, b), cfg
+    g.close()
+    assert tried >= (6 if prec == 1 else 4)
+
+
+def test_set_launch_shapes_rejects_bad_shapes(gpu_lib):
+    """tc_set_launch_shapes refuses a block of more than 256 threads and a
+    visit shape that does not fit its level (TC_ERR_ARG), changing nothing."""
+    p = case_1024_like(nx=256, nz=64, grids=5, tpc=2)
+    g = Simulation(p)
+    nlev = g.info.grids - 1
+    for bad in ([(32, 16, 1)] + [(32, 8, 1)] * (nlev - 1),
+                [(32, 8, 1)] * (nlev - 1) + [(32, 8, 299)],
+                [(32, 8, 201)] + [(32, 8, 1)] * (nlev - 1)):
+        with pytest.raises(TracerError) as e:
+            g.set_launch_shapes(bad)
+        assert e.value.status == 1
+    g.set_launch_shapes([(64, 4, 1)] * nlev)
+    g.close()

@@ -1361,6 +1361,32 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
     return TC_OK;
 }
 
+tc_status tc_set_launch_shapes(tc_handle* H, const int32_t* choices) {
+    if (!H || !choices) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    const bool mixed = (h->p.solver_precision == 1);
+    const int G = h->grids;
+    for (int l = 1; l < G; l++) {
+        const int bx = choices[3 * (l - 1)], by = choices[3 * (l - 1) + 1], v = choices[3 * (l - 1) + 2];
+        if (bx < 1 || by < 1 || bx * by > 256 || (bx * by) % 32 != 0 || v < 0) return TC_ERR_ARG;
+        if (v > 1 && (l == 1 || !h->fuse_visits || !visit_cluster_fits(h->lev[l].L, h->p.Nmulti, mixed ? 1 : 0, v)))
+            return TC_ERR_ARG;
+    }
+    for (int l = 1; l < G; l++) {
+        Level& lv = h->lev[l];
+        lv.sweep_bx = choices[3 * (l - 1)];
+        lv.sweep_by = choices[3 * (l - 1) + 1];
+        const int v = choices[3 * (l - 1) + 2];
+        lv.fuse = (v != 0) ? 1 : 0;
+        lv.visit_cfg = (v > 1) ? v : 0;
+    }
+    CycleGraphs& cg = *h->graphs;
+    if (cg.l1) cudaGraphExecDestroy(cg.l1);
+    if (cg.rest) cudaGraphExecDestroy(cg.rest);
+    cg.l1 = cg.rest = nullptr;
+    return TC_OK;
+}
+
 tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc_stats_row* rows, int32_t* cycles,
                            double* dts, tc_status* status) {
     if (!hs || n < 1 || nthreads < 1) return TC_ERR_ARG;

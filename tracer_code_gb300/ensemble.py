@@ -57,7 +57,19 @@ class Ensemble:
                 self.nets.append(net)
             sim.upload(state.initial_state(q, seed=(seeds[i] if seeds else 1 + i)))
             self.sims.append(sim)
-        self.tuning = [s.autotune() for s in self.sims] if autotune else None
+        self.tuning = None
+        if autotune:
+            # launch shapes depend on the level sizes and the precision only:
+            # tune the first case of each kind, apply its shapes to the rest
+            tuned = {}
+            self.tuning = []
+            for s, p in zip(self.sims, params):
+                key = (p.nx, p.nz, s.info.grids, p.solver_precision, p.Nmulti)
+                if key in tuned:
+                    s.set_launch_shapes(tuned[key])
+                else:
+                    tuned[key] = s.autotune()
+                self.tuning.append(tuned[key])
         self.n = len(self.sims)
         self.ntr = [s.ntr for s in self.sims]
         # cases still running; a case stops (as the reference's run stops) at
