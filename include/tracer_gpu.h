@@ -231,22 +231,24 @@ tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double
 
 /* Autotuner (no reference counterpart).  For each smoothed level it times,
  * on this handle's GPU and in its solver precision, the per-sweep smoother
- * kernel under eight block shapes of at most 256 threads, and one launch per
- * sweep against fused cluster visits of every shape that fits (1 or 2
- * points per thread strip, 1 to 16 CTAs), with CUDA-graph replays, and keeps
- * the fastest of each.  Results are unchanged by the choice (the arithmetic
- * per point does not depend on the launch shape).  If `choices` is not NULL
- * it receives (block x, block y, visit) for levels 1..grids-1, visit = 0 for
- * one launch per sweep, 1 for the default fused shape, else 100 x points
- * per strip + CTAs.  Needs uploaded state; the levels' corrections are
- * restored afterwards. */
+ * kernel under eight block shapes of at most 256 threads, then visits of 1
+ * to 6 sweeps per launch of the tiled smoother (FP64: 1 or 2) and fused
+ * cluster visits of every shape that fits (1 or 2 points per thread strip,
+ * 1 to 16 CTAs), with CUDA-graph replays, and keeps the fastest of each.
+ * Results are unchanged by the choice (the arithmetic per point does not
+ * depend on the launch shape).  If `choices` is not NULL it receives (block
+ * x, block y, visit) for levels 1..grids-1, visit = 0 for one launch per
+ * sweep, 1000 + n for n sweeps per launch, 1 for the default fused shape,
+ * else 100 x points per strip + CTAs.  Needs uploaded state; the levels'
+ * corrections are restored afterwards. */
 tc_status tc_autotune(tc_handle* h, int32_t* choices);
 /* Applies launch shapes in tc_autotune's `choices` format (3 ints per level
  * 1..grids-1: sweep block x, block y, visit = 0 one launch per sweep / 1
- * default fused visit / 100*P + C), e.g. shapes tuned once on another handle
- * of the same grid and precision.  TC_ERR_ARG (nothing changed) if a block
- * has more than 256 threads or a visit shape does not fit its level.  Shapes
- * do not change the arithmetic. */
+ * default fused visit / 100*P + C / 1000 + n for n sweeps per launch of the
+ * tiled smoother, n = 2, or 3 in the mixed solver), e.g. shapes tuned once on
+ * another handle of the same grid and precision.  TC_ERR_ARG (nothing
+ * changed) if a block has more than 256 threads or a visit shape does not fit
+ * its level.  Shapes do not change the arithmetic. */
 tc_status tc_set_launch_shapes(tc_handle* h, const int32_t* choices);
 
 /* Ensemble of independent cases (no reference counterpart: the reference

@@ -227,8 +227,8 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
 // ---------------------------------------------------------------------------
 
 
-__global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double* __restrict__ Sin, double* __restrict__ Sout,
-                        const double* __restrict__ coef, const double* __restrict__ rhs,
+__global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double* Sin, double* Sout,
+                        const double* __restrict__ coef, const double* rhs,
                         const double* __restrict__ dts, const double* __restrict__ cA, const double* __restrict__ cB,
                         double c_uniform, int per_point, double temp, int Vbc) {
     RANGE_IK_DYN(r);
@@ -245,9 +245,9 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
     }
     pdl_entry();
     if (!inr) return;
-    double res = fold_apply(L, Sin, x, cf, __ldg(rhs + x));
+    double res = fold_apply(L, Sin, x, cf, ld_state(rhs + x));
     double c = per_point ? 2.0 / (ca + cb * temp) : c_uniform;
-    double v = fma(c * dt, res, __ldg(Sin + x));
+    double v = fma(c * dt, res, ld_state(Sin + x));
     store_stream(L, Sout, i, k, v, Vbc);
     pdl_done();
 }
@@ -258,8 +258,8 @@ void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* So
                                                   c_uniform, per_point, temp, Vbc); tc_note_launch();
 }
 
-__global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
-                           const double* __restrict__ rhs, double* __restrict__ res, RedScratch rs, double* out,
+__global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* S, const double* __restrict__ coef,
+                           const double* rhs, double* res, RedScratch rs, double* out,
                            double div1, double div2) {
     RANGE_IK(r);
     double a = 0.0;
@@ -268,7 +268,7 @@ __global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const doub
     pdl_entry();
     if (inr) {
         size_t x = IX(L, i, k);
-        double v = fold_apply(L, S, x, cf, __ldg(rhs + x));
+        double v = fold_apply(L, S, x, cf, ld_state(rhs + x));
         res[x] = v;
         a = fabs(v);
     }
@@ -281,8 +281,8 @@ void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratc
                                                      (double)(lv.L.a - 1), (double)(lv.L.b - 1)); tc_note_launch();
 }
 
-__global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* __restrict__ rf, double* __restrict__ rc,
-                               double* __restrict__ zero, size_t zn) {
+__global__ void k_restrict_res(Lay C, Lay F, Range2 r, const double* rf, double* rc,
+                               double* zero, size_t zn) {
     pdl_entry();
     if (zero != nullptr) {
         // clear the level's correction plane in the same launch (grid-stride)
@@ -305,20 +305,20 @@ void launch_restrict_res(cudaStream_t s, const Level& coarse, const Level& fine,
 }
 
 // prolong (bilinear, additive) with the fine level's stream BCs fused
-__global__ void k_prolong(Lay C, Lay F, Range2 r, const double* __restrict__ ec, double* __restrict__ ef, int Vbc) {
+__global__ void k_prolong(Lay C, Lay F, Range2 r, const double* ec, double* ef, int Vbc) {
     pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     size_t x = IX(F, i, k);
     double add;
     bool ie = (i % 2) == 0, ke = (k % 2) == 0;
-    if (ie && ke) add = ec[IX(C, i / 2, k / 2)];
-    else if (ie) add = (ec[IX(C, i / 2, (k - 1) / 2)] + ec[IX(C, i / 2, (k + 1) / 2)]) / 2.0;
-    else if (ke) add = (ec[IX(C, (i - 1) / 2, k / 2)] + ec[IX(C, (i + 1) / 2, k / 2)]) / 2.0;
+    if (ie && ke) add = ld_state(ec + IX(C, i / 2, k / 2));
+    else if (ie) add = (ld_state(ec + IX(C, i / 2, (k - 1) / 2)) + ld_state(ec + IX(C, i / 2, (k + 1) / 2))) / 2.0;
+    else if (ke) add = (ld_state(ec + IX(C, (i - 1) / 2, k / 2)) + ld_state(ec + IX(C, (i + 1) / 2, k / 2))) / 2.0;
     else
-        add = (ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
-               ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / 4.0;
-    store_stream(F, ef, i, k, ef[x] + add, Vbc);
+        add = (ld_state(ec + IX(C, (i - 1) / 2, (k - 1) / 2)) + ld_state(ec + IX(C, (i + 1) / 2, (k - 1) / 2)) +
+               ld_state(ec + IX(C, (i + 1) / 2, (k + 1) / 2)) + ld_state(ec + IX(C, (i - 1) / 2, (k + 1) / 2))) / 4.0;
+    store_stream(F, ef, i, k, ld_state(ef + x) + add, Vbc);
     pdl_done();
 }
 void launch_prolong(cudaStream_t s, const Level& coarse, const Level& fine, const double* ec, double* ef, int Vbc) {
@@ -553,7 +553,7 @@ void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, 
 // DGBTRS, Stream_grid_coarse): one warp per interior unknown, the boundary
 // unknowns are zero (walls); ghosts are written with the stream BCs.
 __global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
-                               const double* __restrict__ rhs, int n, double* __restrict__ err, int Vbc) {
+                               const double* rhs, int n, double* err, int Vbc) {
     pdl_entry();
     const int lane = threadIdx.x & 31;
     const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // 0-based row
@@ -566,7 +566,7 @@ __global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const dou
     for (int q = lane; q < n; q += 32) {
         const int kq = q % N, iq = q / N;
         if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
-            acc = fma(__ldg(row + q), __ldg(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+            acc = fma(__ldg(row + q), ld_state(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
     if (lane == 0) store_stream(L, err, ip, kp, acc, Vbc);
@@ -579,11 +579,11 @@ void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, co
     launch_pdl(k_coarse_apply, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
 }
 
-__global__ void k_copy(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+__global__ void k_copy(double* dst, const double* src, size_t n) {
     pdl_entry();
     size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     size_t st = (size_t)gridDim.x * blockDim.x;
-    for (; t < n; t += st) dst[t] = src[t];
+    for (; t < n; t += st) dst[t] = ld_state(src + t);
     pdl_done();
 }
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n) {

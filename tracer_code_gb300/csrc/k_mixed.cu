@@ -34,8 +34,8 @@ void to_f32(cudaStream_t s, const double* in, float* out, size_t n) {
     k_to_f32<<<nb, 256, 0, s>>>(in, out, n); tc_note_launch();
 }
 
-__global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float* __restrict__ Sin,
-                                                   float* __restrict__ Sout, const float* __restrict__ coef, const float* __restrict__ rhs,
+__global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float* Sin,
+                                                   float* Sout, const float* __restrict__ coef, const float* rhs,
                           const float* __restrict__ dts, const float* __restrict__ cA, const float* __restrict__ cB,
                           float c_uniform, int per_point, float temp, int Vbc) {
     RANGE_IK_DYN(r);
@@ -52,22 +52,22 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
     }
     pdl_entry();
     if (!inr) return;
-    const float res = fold_apply<float>(L, Sin, x, cf, __ldg(rhs + x));
+    const float res = fold_apply<float>(L, Sin, x, cf, ld_state(rhs + x));
     const float c = per_point ? 2.0f / (ca + cb * temp) : c_uniform;
-    const float v = fmaf(c * dt, res, __ldg(Sin + x));
+    const float v = fmaf(c * dt, res, ld_state(Sin + x));
     store_stream<float>(L, Sout, i, k, v, Vbc);
     pdl_done();
 }
 
-__global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* __restrict__ S, const float* __restrict__ coef,
-                             const float* __restrict__ rhs, float* __restrict__ res) {
+__global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* S, const float* __restrict__ coef,
+                             const float* rhs, float* res) {
     RANGE_IK(r);
     const size_t x = inr ? IX(L, i, k) : 0;
     float cf[TC_NCOEF];
     if (inr) fold_coefs<float>(L, coef, x, cf);
     pdl_entry();
     if (!inr) return;
-    res[x] = fold_apply<float>(L, S, x, cf, __ldg(rhs + x));
+    res[x] = fold_apply<float>(L, S, x, cf, ld_state(rhs + x));
     pdl_done();
 }
 
@@ -83,8 +83,8 @@ __device__ __forceinline__ void zero_plane(T* __restrict__ z, size_t zn) {
 }
 
 template <typename Tin>
-__global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ rf, float* __restrict__ rc,
-                                float* __restrict__ zero, size_t zn) {
+__global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* rf, float* rc,
+                                float* zero, size_t zn) {
     pdl_entry();
     zero_plane(zero, zn);
     RANGE_IK(r);
@@ -97,49 +97,49 @@ __global__ void k_restrict_to32(Lay C, Lay F, Range2 r, const Tin* __restrict__ 
 template <typename T>
 __device__ __forceinline__ T prolong_value(const Lay& C, const float* __restrict__ ec, int i, int k) {
     const bool ie = (i % 2) == 0, ke = (k % 2) == 0;
-    if (ie && ke) return (T)ec[IX(C, i / 2, k / 2)];
-    if (ie) return ((T)ec[IX(C, i / 2, (k - 1) / 2)] + (T)ec[IX(C, i / 2, (k + 1) / 2)]) / T(2);
-    if (ke) return ((T)ec[IX(C, (i - 1) / 2, k / 2)] + (T)ec[IX(C, (i + 1) / 2, k / 2)]) / T(2);
-    return ((T)ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + (T)ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
-            (T)ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + (T)ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / T(4);
+    if (ie && ke) return (T)ld_state(ec + IX(C, i / 2, k / 2));
+    if (ie) return ((T)ld_state(ec + IX(C, i / 2, (k - 1) / 2)) + (T)ld_state(ec + IX(C, i / 2, (k + 1) / 2))) / T(2);
+    if (ke) return ((T)ld_state(ec + IX(C, (i - 1) / 2, k / 2)) + (T)ld_state(ec + IX(C, (i + 1) / 2, k / 2))) / T(2);
+    return ((T)ld_state(ec + IX(C, (i - 1) / 2, (k - 1) / 2)) + (T)ld_state(ec + IX(C, (i + 1) / 2, (k - 1) / 2)) +
+            (T)ld_state(ec + IX(C, (i + 1) / 2, (k + 1) / 2)) + (T)ld_state(ec + IX(C, (i - 1) / 2, (k + 1) / 2))) / T(4);
 }
 
 template <typename T>
-__global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* __restrict__ ec, T* __restrict__ ef, int Vbc) {
+__global__ void k_prolong_add(Lay C, Lay F, Range2 r, const float* ec, T* ef, int Vbc) {
     pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(F, i, k);
-    store_stream<T>(F, ef, i, k, ef[x] + prolong_value<T>(C, ec, i, k), Vbc);
+    store_stream<T>(F, ef, i, k, ld_state(ef + x) + prolong_value<T>(C, ec, i, k), Vbc);
     pdl_done();
 }
 
 // FP64 residual of psi, rounded to FP32 as the RHS of the level-1 correction
-__global__ void __launch_bounds__(256, 1) k_residual_to32(Lay L, Range2 r, const double* __restrict__ S, const double* __restrict__ coef,
-                                const double* __restrict__ rhs, float* __restrict__ rhs32,
-                                float* __restrict__ zero, size_t zn) {
+__global__ void __launch_bounds__(256, 1) k_residual_to32(Lay L, Range2 r, const double* S, const double* __restrict__ coef,
+                                const double* rhs, float* rhs32,
+                                float* zero, size_t zn) {
     pdl_entry();
     zero_plane(zero, zn);
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
-    rhs32[x] = (float)folded_residual<double>(L, S, coef, __ldg(rhs + x), x);
+    rhs32[x] = (float)folded_residual<double>(L, S, coef, ld_state(rhs + x), x);
     pdl_done();
 }
 
 // psi += e in FP64, ghosts from the new interior value
-__global__ void k_update64(Lay L, Range2 r, double* __restrict__ S, const float* __restrict__ e, int Vbc) {
+__global__ void k_update64(Lay L, Range2 r, double* S, const float* e, int Vbc) {
     pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
-    store_stream<double>(L, S, i, k, S[x] + (double)e[x], Vbc);
+    store_stream<double>(L, S, i, k, ld_state(S + x) + (double)ld_state(e + x), Vbc);
     pdl_done();
 }
 
 // coarsest level: x = A^-1 (RowB .* rhs) in FP64 from the FP32 RHS, stored as FP32
 __global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
-                                 const float* __restrict__ rhs, int n, float* __restrict__ err, int Vbc) {
+                                 const float* rhs, int n, float* err, int Vbc) {
     pdl_entry();
     const int lane = threadIdx.x & 31;
     const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -152,7 +152,7 @@ __global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const d
     for (int q = lane; q < n; q += 32) {
         const int kq = q % N, iq = q / N;
         if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
-            acc = fma(__ldg(row + q), (double)__ldg(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+            acc = fma(__ldg(row + q), (double)ld_state(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
     if (lane == 0) store_stream<float>(L, err, ip, kp, (float)acc, Vbc);

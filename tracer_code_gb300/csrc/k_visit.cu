@@ -110,11 +110,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t a, int parity) {
 // W is the shared-memory row stride (>= a+5, a compile-time class so the
 // stencil offsets fold into the load instructions).
 template <typename T, int P, int NT, int W>
-__global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __restrict__ Sg,
-                                                         const T* __restrict__ coef, const T* __restrict__ rhs,
+__global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg,
+                                                         const T* __restrict__ coef, const T* rhs,
                                                          const T* __restrict__ dts, const T* __restrict__ ctab,
                                                          const T* __restrict__ cA, const T* __restrict__ cB,
-                                                         T* __restrict__ res, int* __restrict__ timeout_flag) {
+                                                         T* res, int* timeout_flag) {
     cg::cluster_group cl = cg::this_cluster();
     const int C = (int)cl.num_blocks(), me = (int)cl.block_rank();
     const Lay& L = Q.L;
@@ -178,7 +178,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
     pdl_entry();
 #pragma unroll
     for (int p = 0; p < P; p++)
-        if (act[p]) rh[p] = __ldg(rhs + IX(L, i, kr + p));
+        if (act[p]) rh[p] = ld_state(rhs + IX(L, i, kr + p));
     // rows k0-2..k1+2 (ghosts, walls and halos) into every buffer; four
     // independent global loads in flight per thread
     {
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
             for (int u = 0; u < 4; u++) {
                 const int t = t0 + u * NT;
                 const int r = t / wa, c = t % wa, k = k0 - 2 + r;
-                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? Sg[IX(L, c - SP, k)] : T(0);
+                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? ld_state(Sg + IX(L, c - SP, k)) : T(0);
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -385,8 +385,8 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* __
         const int wa = a + 1 + 2 * SP;
         for (int t = tid; t < 2 * wa; t += NT) {
             const int g = 1 + t / wa, c = t % wa, ii = c - SP;
-            if (me == 0) Sg[IX(L, ii, -g)] = zsgn * Sg[IX(L, ii, g)];
-            if (me == C - 1) Sg[IX(L, ii, b + g)] = zsgn * Sg[IX(L, ii, b - g)];
+            if (me == 0) Sg[IX(L, ii, -g)] = zsgn * ld_state(Sg + IX(L, ii, g));
+            if (me == C - 1) Sg[IX(L, ii, b + g)] = zsgn * ld_state(Sg + IX(L, ii, b - g));
         }
     }
 }

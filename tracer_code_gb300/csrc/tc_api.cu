@@ -367,6 +367,16 @@ void cheb_temps(int Niter, int dir, double* tv, double* cv) {
     }
 }
 
+// factor c and Chebyshev node temp of sweep n (1-based) of a visit of Niter
+// sweeps: iterate_stream's expressions (c = 1 for a Richardson visit, dir=1;
+// c unused on the per-point Chebyshev level)
+static void sweep_factors(int Niter, int n, int dir, bool cheb_pp, double* c, double* temp) {
+    const double ntemp = (double)(Niter - n + 1);
+    const double la = -1.0, lb = -2.0;
+    *temp = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
+    *c = (dir != 1 && !cheb_pp) ? 2.0 / (-lb - la + (lb - la) * *temp) : 1.0;
+}
+
 // iterate_stream (iterative_solver.f90:860-963), iterate_order=1
 void iterate_stream(Handle* h, int level, int dir) {
     Level& lv = h->lev[level];
@@ -381,23 +391,23 @@ void iterate_stream(Handle* h, int level, int dir) {
                                  Niter, pp, h->p.Vbc, &h->ds->visit_timeout) == 0)
             return;
     }
-    for (int n = 1; n <= Niter; n++) {
-        const double ntemp = (double)(Niter - n + 1);
-        const double la = -1.0;
-        const double temp = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
-        double c = 1.0;
-        int per_point = 0;
-        if (dir != 1) {
-            if (cheb_pp) per_point = 1;
-            else {
-                const double lb = -2.0;
-                c = 2.0 / (-lb - la + (lb - la) * temp);
-            }
+    const int per_point = (dir != 1 && cheb_pp) ? 1 : 0;
+    int flips = 0;
+    for (int n = 1; n <= Niter;) {
+        double cs[2], ts[2];
+        for (int j = 0; j < 2 && n + j <= Niter; j++) sweep_factors(Niter, n + j, dir, cheb_pp, &cs[j], &ts[j]);
+        const int ns = (lv.blk == 2 && n + 1 <= Niter) ? 2 : (lv.blk >= 1 ? 1 : 0);
+        if (ns > 0 &&
+            launch_sweep_blk64(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], ns, cs, ts, per_point, h->p.Vbc)) {
+            n += ns;
+        } else {
+            launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], cs[0], per_point, ts[0], h->p.Vbc);
+            n += 1;
         }
-        launch_sweep(h->st, lv, lv.err[lv.ecur], lv.err[1 - lv.ecur], c, per_point, temp, h->p.Vbc);
         lv.ecur = 1 - lv.ecur;
+        flips++;
     }
-    if (Niter % 2 == 1) {
+    if (flips % 2 == 1) {
         // keep the level's current buffer fixed across visits (graph replay relies on it)
         launch_copy_plane(h->st, lv.err[1 - lv.ecur], lv.err[lv.ecur], lv.L.plane);
         lv.ecur = 1 - lv.ecur;
@@ -444,16 +454,29 @@ void iterate_stream32(Handle* h, int level, int dir) {
                                    &h->ds->visit_timeout) == 0)
             return;
     }
-    for (int n = 1; n <= Niter; n++) {
-        const double ntemp = (double)(Niter - n + 1);
-        const double la = -1.0, lb = -2.0;
-        const double temp = std::cos((2.0 * ntemp - 1.0) * kPi / (double)(2 * Niter));
-        double c = 1.0;
-        if (dir != 1 && !cheb_pp) c = 2.0 / (-lb - la + (lb - la) * temp);
-        launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], (float)c, pp, (float)temp, h->p.Vbc);
+    int flips = 0;
+    for (int n = 1; n <= Niter;) {
+        // lv.blk sweeps per launch of the tiled smoother while that many
+        // remain, then single sweeps of it (lv.blk = 0: k_sweep32)
+        const int ns = (lv.blk >= 1 && n + lv.blk - 1 <= Niter) ? lv.blk : (lv.blk >= 1 ? 1 : 0);
+        float cs[6], ts[6];
+        for (int j = 0; j < (ns > 0 ? ns : 1); j++) {
+            double c, temp;
+            sweep_factors(Niter, n + j, dir, cheb_pp, &c, &temp);
+            cs[j] = (float)c;
+            ts[j] = (float)temp;
+        }
+        if (ns > 0 &&
+            launch_sweep_blk32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], ns, cs, ts, pp, h->p.Vbc)) {
+            n += ns;
+        } else {
+            launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], cs[0], pp, ts[0], h->p.Vbc);
+            n += 1;
+        }
         lv.e32cur = 1 - lv.e32cur;
+        flips++;
     }
-    if (Niter % 2 == 1) {
+    if (flips % 2 == 1) {
         CKV(cudaMemcpyAsync(lv.e32[1 - lv.e32cur], lv.e32[lv.e32cur], sizeof(float) * lv.L.plane,
                             cudaMemcpyDeviceToDevice, h->st));
         lv.e32cur = 1 - lv.e32cur;
@@ -886,6 +909,8 @@ tc_status create(Handle* h, const tc_params* in) {
     // ---- levels ----
     const int odi[TC_NCOEF] = TC_OFFSETS_DI, odk[TC_NCOEF] = TC_OFFSETS_DK;
     auto Dv = [&](const double* D, int j) { return (j < -3 || j > 3) ? 0.0 : D[j + 3]; };
+    int n_sms = 0;
+    CK(cudaDeviceGetAttribute(&n_sms, cudaDevAttrMultiProcessorCount, h->device));
     for (int l = 1; l <= G; l++) {
         Level& lv = h->lev[l];
         lv.L = make_lay(nx >> (l - 1), nz >> (l - 1));
@@ -901,6 +926,15 @@ tc_status create(Handle* h, const tc_params* in) {
         lv.sweep_by = BY;
         lv.fuse = 1;
         lv.visit_cfg = 0;
+        lv.blk = 0;
+        // mixed solve, a level below the first that no cluster visit covers:
+        // six sweeps per launch of the tiled smoother when its tiles fit one
+        // wave (measured faster than one launch per sweep at 512x128; slower
+        // at 1024x256, and in FP64, where the redundant halo work costs FP64
+        // issue slots)
+        if (p.solver_precision == 1 && l > 1 && !(h->fuse_visits && visit_cluster_fits(lv.L, p.Nmulti, 1)) &&
+            sweep_blk_tiles(lv.L) <= n_sms)
+            lv.blk = 6;
         lv.coef32 = lv.dts32 = lv.cA32 = lv.cB32 = lv.rhs32 = lv.res32 = nullptr;
         lv.e32[0] = lv.e32[1] = nullptr;
         lv.e32cur = 0;
@@ -1310,23 +1344,30 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         }
         lv.sweep_bx = shapes[bb][0];
         lv.sweep_by = shapes[bb][1];
-        // one launch per sweep, or one cluster launch per visit in one of
-        // several shapes (points per strip x CTAs)
-        lv.fuse = 1;
+        // unfused visits: 1..6 sweeps per launch (tiled smoother for 2..6;
+        // FP64 at most 2); then one cluster launch per visit in each shape
+        // that fits (points per strip x CTAs)
+        auto time_visits = [&](double* ms) {
+            return graph_time(h, [&]() {
+                for (int v = 0; v < 2; v++) {
+                    if (mixed) iterate_stream32(h, l, 1);
+                    else iterate_stream(h, l, 1);
+                }
+            }, ms);
+        };
+        lv.fuse = 0;
         lv.visit_cfg = 0;
+        double best_v = 1e30;
+        int best_blk = 0;
+        for (int blk = 0; blk <= (mixed ? 6 : 2); blk++) {
+            lv.blk = blk;
+            double ms = 0;
+            TRY(time_visits(&ms));
+            if (ms < best_v) { best_v = ms; best_blk = blk; }
+        }
+        lv.blk = best_blk;
+        int best_cfg = -1;  // -1 = unfused
         if (l > 1 && h->fuse_visits && visit_cluster_fits(lv.L, h->p.Nmulti, mixed ? 1 : 0)) {
-            auto time_visits = [&](double* ms) {
-                return graph_time(h, [&]() {
-                    for (int v = 0; v < 2; v++) {
-                        if (mixed) iterate_stream32(h, l, 1);
-                        else iterate_stream(h, l, 1);
-                    }
-                }, ms);
-            };
-            double best_v = 1e30;
-            int best_cfg = -1;  // -1 = one launch per sweep
-            lv.fuse = 0;
-            TRY(time_visits(&best_v));
             lv.fuse = 1;
             std::vector<int> cfgs = {0};
             for (int p : {1, 2})
@@ -1338,9 +1379,9 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
                 TRY(time_visits(&ms));
                 if (ms < best_v) { best_v = ms; best_cfg = cfg; }
             }
-            lv.fuse = (best_cfg >= 0) ? 1 : 0;
-            lv.visit_cfg = (best_cfg > 0) ? best_cfg : 0;
         }
+        lv.fuse = (best_cfg >= 0) ? 1 : 0;
+        lv.visit_cfg = (best_cfg > 0) ? best_cfg : 0;
         for (int q = 0; q < 2; q++) {
             CK(cudaMemcpyAsync(mixed ? (void*)lv.e32[q] : (void*)lv.err[q], save[q], bytes, cudaMemcpyDeviceToDevice,
                                h->st));
@@ -1350,7 +1391,7 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         if (choices) {
             choices[3 * (l - 1) + 0] = lv.sweep_bx;
             choices[3 * (l - 1) + 1] = lv.sweep_by;
-            choices[3 * (l - 1) + 2] = lv.fuse ? (lv.visit_cfg ? lv.visit_cfg : 1) : 0;
+            choices[3 * (l - 1) + 2] = lv.fuse ? (lv.visit_cfg ? lv.visit_cfg : 1) : (lv.blk > 0 ? 1000 + lv.blk : 0);
         }
     }
     // the cycle graphs bake in launch shapes: capture again at the next solve
@@ -1369,16 +1410,21 @@ tc_status tc_set_launch_shapes(tc_handle* H, const int32_t* choices) {
     for (int l = 1; l < G; l++) {
         const int bx = choices[3 * (l - 1)], by = choices[3 * (l - 1) + 1], v = choices[3 * (l - 1) + 2];
         if (bx < 1 || by < 1 || bx * by > 256 || (bx * by) % 32 != 0 || v < 0) return TC_ERR_ARG;
-        if (v > 1 && (l == 1 || !h->fuse_visits || !visit_cluster_fits(h->lev[l].L, h->p.Nmulti, mixed ? 1 : 0, v)))
+        if (v > 1000) {
+            if (!(v == 1001 || v == 1002 || (v >= 1003 && v <= 1006 && mixed))) return TC_ERR_ARG;
+        } else if (v > 1 &&
+                   (l == 1 || !h->fuse_visits || !visit_cluster_fits(h->lev[l].L, h->p.Nmulti, mixed ? 1 : 0, v))) {
             return TC_ERR_ARG;
+        }
     }
     for (int l = 1; l < G; l++) {
         Level& lv = h->lev[l];
         lv.sweep_bx = choices[3 * (l - 1)];
         lv.sweep_by = choices[3 * (l - 1) + 1];
         const int v = choices[3 * (l - 1) + 2];
-        lv.fuse = (v != 0) ? 1 : 0;
-        lv.visit_cfg = (v > 1) ? v : 0;
+        lv.fuse = (v != 0 && v < 1000) ? 1 : 0;
+        lv.visit_cfg = (v > 1 && v < 1000) ? v : 0;
+        lv.blk = (v > 1000) ? v - 1000 : 0;
     }
     CycleGraphs& cg = *h->graphs;
     if (cg.l1) cudaGraphExecDestroy(cg.l1);

@@ -119,12 +119,22 @@ struct CPtrsW {
 
 // full-weighting restriction at fine point (ii,kk); the corner term repeats
 // (ii-1,kk+1) and omits (ii+1,kk-1), as iterative_solver.f90:607
+// Loads of data that an earlier kernel of the stream wrote (streamfunction
+// corrections, RHS, residuals) go to L2 only (ld.global.cg).  With
+// programmatic dependent launch a kernel's CTAs can run on SMs whose L1 still
+// holds lines of the same buffer from two launches back (ping-pong buffers),
+// and a plain or non-coherent load could return such a stale line; the
+// solve-constant coefficients keep __ldg.
 template <typename T>
-__device__ __forceinline__ T restrict9(const T* __restrict__ in, const Lay& F, int ii, int kk) {
-    T corners = (in[IX(F, ii - 1, kk - 1)] + in[IX(F, ii - 1, kk + 1)] + in[IX(F, ii + 1, kk + 1)] +
-                 in[IX(F, ii - 1, kk + 1)]) / T(16);
-    T sides = (in[IX(F, ii - 1, kk)] + in[IX(F, ii, kk - 1)] + in[IX(F, ii + 1, kk)] + in[IX(F, ii, kk + 1)]) / T(8);
-    T centre = in[IX(F, ii, kk)] / T(4);
+__device__ __forceinline__ T ld_state(const T* p) { return __ldcg(p); }
+
+template <typename T>
+__device__ __forceinline__ T restrict9(const T* in, const Lay& F, int ii, int kk) {
+    T corners = (ld_state(in + IX(F, ii - 1, kk - 1)) + ld_state(in + IX(F, ii - 1, kk + 1)) +
+                 ld_state(in + IX(F, ii + 1, kk + 1)) + ld_state(in + IX(F, ii - 1, kk + 1))) / T(16);
+    T sides = (ld_state(in + IX(F, ii - 1, kk)) + ld_state(in + IX(F, ii, kk - 1)) + ld_state(in + IX(F, ii + 1, kk)) +
+               ld_state(in + IX(F, ii, kk + 1))) / T(8);
+    T centre = ld_state(in + IX(F, ii, kk)) / T(4);
     return corners + sides + centre;
 }
 
@@ -134,7 +144,7 @@ __device__ __forceinline__ T restrict9(const T* __restrict__ in, const Lay& F, i
 // in flight together instead of one L2 round trip per term); the sum keeps
 // the tap order below, so the result does not depend on the load schedule.
 template <typename T>
-__device__ __forceinline__ T folded_residual(const Lay& L, const T* __restrict__ S, const T* __restrict__ coef, T rhs,
+__device__ __forceinline__ T folded_residual(const Lay& L, const T* S, const T* __restrict__ coef, T rhs,
                                              size_t x) {
     const ptrdiff_t ld = (ptrdiff_t)L.ld;
     const size_t pl = L.plane;
@@ -145,7 +155,7 @@ __device__ __forceinline__ T folded_residual(const Lay& L, const T* __restrict__
 #pragma unroll
     for (int d = 0; d < TC_NCOEF; d++) {
         c[d] = __ldg(cf + d * pl);
-        v[d] = __ldg(s + off[d]);
+        v[d] = ld_state(s + off[d]);
     }
     T acc = rhs;
 #pragma unroll
@@ -164,13 +174,13 @@ __device__ __forceinline__ void fold_coefs(const Lay& L, const T* __restrict__ c
     for (int d = 0; d < TC_NCOEF; d++) c[d] = __ldg(coef + x + d * pl);
 }
 template <typename T>
-__device__ __forceinline__ T fold_apply(const Lay& L, const T* __restrict__ S, size_t x, const T* c, T rhs) {
+__device__ __forceinline__ T fold_apply(const Lay& L, const T* S, size_t x, const T* c, T rhs) {
     const ptrdiff_t ld = (ptrdiff_t)L.ld;
     const T* s = S + x;
     const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
     T v[TC_NCOEF];
 #pragma unroll
-    for (int d = 0; d < TC_NCOEF; d++) v[d] = __ldg(s + off[d]);
+    for (int d = 0; d < TC_NCOEF; d++) v[d] = ld_state(s + off[d]);
     T acc = rhs;
 #pragma unroll
     for (int d = 0; d < TC_NCOEF; d++) acc = fma(-c[d], v[d], acc);
@@ -180,7 +190,7 @@ __device__ __forceinline__ T fold_apply(const Lay& L, const T* __restrict__ S, s
 // writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
 // derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
 template <typename T>
-__device__ __forceinline__ void store_stream(const Lay& L, T* __restrict__ S, int i, int k, T v, int Vbc) {
+__device__ __forceinline__ void store_stream(const Lay& L, T* S, int i, int k, T v, int Vbc) {
     const int a = L.a, b = L.b;
     int gi[3] = {i, 0, 0};
     T si[3] = {T(1), T(-1), T(-1)};
@@ -206,6 +216,12 @@ __device__ __forceinline__ void store_stream(const Lay& L, T* __restrict__ S, in
 // done).  launch_pdl() launches with the attribute that allows the early
 // scheduling; without it both calls cost nothing.
 // ---------------------------------------------------------------------------
+//
+// A kernel that uses them must not declare __restrict__ on a pointer whose
+// memory an earlier kernel writes and which it reads or writes after
+// pdl_entry(): the compiler may move accesses through such a pointer across
+// the wait (it assumes nothing else touches that memory).  Solve-constant
+// data (operator coefficients, dt, Chebyshev tables) may keep it.
 __device__ __forceinline__ void pdl_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_done() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 

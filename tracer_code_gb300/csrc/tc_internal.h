@@ -96,6 +96,7 @@ struct Level {
     int sweep_bx, sweep_by;
     int fuse;       // 1 = one cluster launch per visit when the level fits, 0 = one launch per sweep
     int visit_cfg;  // shape of the fused visit: 0 = default, else 100*points per strip + CTAs
+    int blk;        // when not fused: 0 = one k_sweep / k_sweep32 launch per sweep, n = n sweeps per k_sweep_blk launch
 };
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
@@ -151,6 +152,12 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc);
 void launch_residual32(cudaStream_t s, const Level& lv, const float* S);
+// ns sweeps in one launch (k_sweepblk.cu); false if ns is not available
+bool launch_sweep_blk32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, int ns, const float* c,
+                        const float* temp, int per_point, int Vbc);
+bool launch_sweep_blk64(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, int ns, const double* c,
+                        const double* temp, int per_point, int Vbc);
+int sweep_blk_tiles(const Lay& L);  // CTAs of one launch of the tiled smoother
 void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c,
                        float* zero = nullptr);
 void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c,
