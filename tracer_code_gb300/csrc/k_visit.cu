@@ -48,7 +48,45 @@ struct VisitParams {
     int nsweeps, per_point, Vbc, rpc;
     T c[VISIT_MAX_SWEEPS];     // uniform Chebyshev/Richardson factor of sweep n
     T temp[VISIT_MAX_SWEEPS];  // Chebyshev node of sweep n (per-point factor, FP32)
+    // optional transfers fused into the visit (nullptr: none)
+    const T* ec;  // prolong: the coarser level's correction, added to the level's state first
+    Lay Lc;
+    T* rc;        // restrict: the final residual's full weighting into the coarser RHS
+    Lay Lr;
+    T* zc;        // with the restriction: the coarser correction set to zero (zn values)
+    size_t zn;
 };
+
+// bilinear prolongation of the coarse correction at fine point (i,k): the
+// value prolong (iterative_solver.f90:175-233) adds, in k_prolong's order
+template <typename T>
+__device__ __forceinline__ T prolong_at(const Lay& C, const T* ec, int i, int k) {
+    const bool ie = (i % 2) == 0, ke = (k % 2) == 0;
+    if (ie && ke) return ld_state(ec + IX(C, i / 2, k / 2));
+    if (ie) return (ld_state(ec + IX(C, i / 2, (k - 1) / 2)) + ld_state(ec + IX(C, i / 2, (k + 1) / 2))) / T(2);
+    if (ke) return (ld_state(ec + IX(C, (i - 1) / 2, k / 2)) + ld_state(ec + IX(C, (i + 1) / 2, k / 2))) / T(2);
+    return (ld_state(ec + IX(C, (i - 1) / 2, (k - 1) / 2)) + ld_state(ec + IX(C, (i + 1) / 2, (k - 1) / 2)) +
+            ld_state(ec + IX(C, (i + 1) / 2, (k + 1) / 2)) + ld_state(ec + IX(C, (i - 1) / 2, (k + 1) / 2))) /
+           T(4);
+}
+
+// the level's state at (ii,kk) after the fused prolongation: interior points
+// get psi + prolong, ghosts the mirrored interior value times the boundary
+// signs (store_stream's rule), walls stay
+template <typename T>
+__device__ __forceinline__ T state_after_prolong(const Lay& L, const Lay& C, const T* S, const T* ec, int ii, int kk,
+                                                 T zsgn) {
+    const int a = L.a, b = L.b;
+    int mi = ii, mk = kk;
+    T si = T(1), sk = T(1);
+    if (ii < 0) { mi = -ii; si = T(-1); }
+    else if (ii > a) { mi = 2 * a - ii; si = T(-1); }
+    if (kk < 0) { mk = -kk; sk = zsgn; }
+    else if (kk > b) { mk = 2 * b - kk; sk = zsgn; }
+    if (mi < 1 || mi > a - 1 || mk < 1 || mk > b - 1) return ld_state(S + IX(L, ii, kk));
+    const T v = ld_state(S + IX(L, mi, mk)) + prolong_at(C, ec, mi, mk);
+    return (si * sk) * v;
+}
 
 template <typename T>
 struct ChebTemps {
@@ -126,7 +164,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
     const int R = ((rpc + P - 1) / P) * P + 4;
     const int nbuf = (C > 1) ? 3 : 2;
     extern __shared__ __align__(16) unsigned char sm_raw[];
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm_raw);  // 3 mbarriers (first 32 B)
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm_raw);  // 4 mbarriers (first 32 B)
     T* buf = reinterpret_cast<T*>(sm_raw + 32);
     const size_t bsz = (size_t)R * W;
     const int tid = threadIdx.x;
@@ -189,7 +227,10 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
             for (int u = 0; u < 4; u++) {
                 const int t = t0 + u * NT;
                 const int r = t / wa, c = t % wa, k = k0 - 2 + r;
-                v[u] = (t < n_el && k >= -SP && k <= b + SP) ? ld_state(Sg + IX(L, c - SP, k)) : T(0);
+                v[u] = (t < n_el && k >= -SP && k <= b + SP)
+                           ? (Q.ec ? state_after_prolong(L, Q.Lc, Sg, Q.ec, c - SP, k, zsgn)
+                                   : ld_state(Sg + IX(L, c - SP, k)))
+                           : T(0);
             }
 #pragma unroll
             for (int u = 0; u < 4; u++) {
@@ -201,7 +242,8 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
         }
     }
     if (tid == 0 && C > 1) {
-        for (int q = 0; q < 3; q++) mbar_init(smem_addr(&bar[q]), 1);
+        // 0-2: the sweep buffers; 3: the residual rows of the fused restriction
+        for (int q = 0; q < 4; q++) mbar_init(smem_addr(&bar[q]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // bytes this CTA receives per sweep: its halo rows that other CTAs own
@@ -352,7 +394,11 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
             const int rr = 2 + t / wa, c = t % wa;
             Sg[IX(L, c - SP, k0 - 2 + rr)] = fin[(size_t)rr * W + c];
         }
-        if (res != nullptr) {
+        if (res != nullptr || Q.rc != nullptr) {
+            // residual of the final state at the owned points; with the fused
+            // restriction it goes to a free buffer (where the neighbours' edge
+            // rows k0-1 and k1+1 arrive too) instead of global memory
+            T* rb = buf + (size_t)((cur_b + 1) % nbuf) * bsz;
 #pragma unroll
             for (int p = 0; p < P; p++) {
                 if (!act[p]) continue;
@@ -372,7 +418,58 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
                 acc = fma(cf[p][10], fin[xs + 1 - W], acc);
                 acc = fma(cf[p][11], fin[xs - 1 + W], acc);
                 acc = fma(cf[p][12], fin[xs + 1 + W], acc);
-                res[IX(L, i, kr + p)] = acc;
+                if (Q.rc == nullptr) {
+                    res[IX(L, i, kr + p)] = acc;
+                    continue;
+                }
+                rb[xs] = acc;
+                const int k = kr + p;
+                if (k == k0 && me > 0) {
+                    const int ok0 = 1 + (me - 1) * rpc;
+                    const uint32_t dst = smem_addr(rb + (size_t)(k - ok0 + 2) * W + cc);
+                    st_async(cluster_addr(dst, me - 1), acc, cluster_addr(smem_addr(&bar[3]), me - 1));
+                }
+                if (k == k1 && me < C - 1) {
+                    const int ok0 = 1 + (me + 1) * rpc;
+                    const uint32_t dst = smem_addr(rb + (size_t)(k - ok0 + 2) * W + cc);
+                    st_async(cluster_addr(dst, me + 1), acc, cluster_addr(smem_addr(&bar[3]), me + 1));
+                }
+            }
+        }
+        if (Q.rc != nullptr) {
+            int rto = 0;
+            if (C > 1) {
+                const int rexp = (((me > 0) ? cols : 0) + ((me < C - 1) ? cols : 0)) * (int)sizeof(T);
+                if (tid == 0) mbar_arrive_expect(smem_addr(&bar[3]), rexp);
+                __syncthreads();
+                int it = 0, w = 0;
+                while (!mbar_try_wait(smem_addr(&bar[3]), 0)) {
+                    if (++it > VISIT_WAIT_LIMIT) { w = 1; break; }
+                }
+                rto = __syncthreads_or(w);
+            } else {
+                __syncthreads();
+            }
+            if (rto) {
+                timed_out = true;
+                if (tid == 0) atomicExch(timeout_flag, 1);
+            } else {
+                // restrict (iterative_solver.f90:596-626; restrict9's terms and
+                // order, the repeated corner included) for the coarse rows K
+                // whose fine centre row 2K this CTA owns
+                const T* rb = buf + (size_t)((cur_b + 1) % nbuf) * bsz;
+                const int ncol = Q.Lr.a - 1;
+                const int K0 = max(1, (k0 + 1) / 2), K1 = min(Q.Lr.b - 1, k1 / 2);
+                for (int t = tid; t < (K1 - K0 + 1) * ncol; t += NT) {
+                    const int K = K0 + t / ncol, I = 1 + t % ncol;
+                    const T* q = rb + (size_t)(2 * K - k0 + 2) * W + (2 * I + SP);
+                    const T corners = (q[-W - 1] + q[W - 1] + q[W + 1] + q[W - 1]) / T(16);
+                    const T sides = (q[-1] + q[-W] + q[1] + q[W]) / T(8);
+                    const T centre = q[0] / T(4);
+                    Q.rc[IX(Q.Lr, I, K)] = corners + sides + centre;
+                }
+                if (Q.zc != nullptr)
+                    for (size_t t = (size_t)me * NT + tid; t < Q.zn; t += (size_t)C * NT) Q.zc[t] = T(0);
             }
         }
     }
@@ -548,7 +645,7 @@ static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const Visi
 template <typename T>
 static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* rhs, const T* dts, const T* ctab,
                    const T* cA, const T* cB, T* res, const double* cvals, const double* tvals, int nsweeps,
-                   int per_point, int Vbc, int* flag, int cfg) {
+                   int per_point, int Vbc, int* flag, int cfg, const VisitXfer<T>* x) {
     VisitShape sh;
     if (!visit_shape(L, nsweeps, sizeof(T) == sizeof(float), cfg, &sh)) return 1;
     if (per_point && sizeof(T) == sizeof(double) && ctab == nullptr) return 1;
@@ -558,6 +655,14 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
     Q.per_point = per_point;
     Q.Vbc = Vbc;
     Q.rpc = sh.rpc;
+    const VisitXfer<T> none;
+    const VisitXfer<T>& X = x ? *x : none;
+    Q.ec = X.ec;
+    Q.Lc = X.Lc;
+    Q.rc = X.rc;
+    Q.Lr = X.Lr;
+    Q.zc = X.rc ? X.zc : nullptr;
+    Q.zn = X.rc ? X.zn : 0;
     for (int n = 0; n < nsweeps; n++) {
         Q.c[n] = (T)cvals[n];
         Q.temp[n] = (T)tvals[n];
@@ -576,12 +681,13 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
 
 // Returns 0 if the level was handled here (caller skips the per-sweep path).
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
-                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag) {
+                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag,
+                         const VisitXfer<double>* x) {
     return visit_t<double>(s, lv.L, S, lv.coef, lv.rhs, lv.dt_stream, ctab, lv.cA, lv.cB, lv.res, cvals, tvals,
-                           nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg);
+                           nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x);
 }
 int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
-                           int nsweeps, int per_point, int Vbc, int* timeout_flag) {
+                           int nsweeps, int per_point, int Vbc, int* timeout_flag, const VisitXfer<float>* x) {
     return visit_t<float>(s, lv.L, S, lv.coef32, lv.rhs32, lv.dts32, nullptr, lv.cA32, lv.cB32, lv.res32, cvals,
-                          tvals, nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg);
+                          tvals, nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x);
 }

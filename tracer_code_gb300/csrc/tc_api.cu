@@ -377,8 +377,23 @@ static void sweep_factors(int Niter, int n, int dir, bool cheb_pp, double* c, do
     *c = (dir != 1 && !cheb_pp) ? 2.0 / (-lb - la + (lb - la) * *temp) : 1.0;
 }
 
-// iterate_stream (iterative_solver.f90:860-963), iterate_order=1
-void iterate_stream(Handle* h, int level, int dir) {
+// Would iterate_stream / iterate_stream32 smooth `level` in direction dir as
+// one cluster visit?  (the conditions under which launch_visit_cluster runs)
+static bool visit_fuses(Handle* h, int level, int dir) {
+    const Level& lv = h->lev[level];
+    const bool mixed = (h->p.solver_precision == 1);
+    if (!(h->fuse_visits && lv.fuse && level > 1 && level < h->grids && h->p.Nmulti <= 128)) return false;
+    if (!visit_cluster_fits(lv.L, h->p.Nmulti, mixed ? 1 : 0, lv.visit_cfg)) return false;
+    const bool pp = (dir != 1 && level == h->ratio_level);
+    return mixed || !pp || h->ctab_level == level;
+}
+
+// iterate_stream (iterative_solver.f90:860-963), iterate_order=1.
+// pro: first add the prolongation of level+1's correction (prolong);
+// rst: afterwards restrict the residual into level+1's RHS (restrict),
+// zeroing level+1's correction if rst_zero.  A cluster visit does both in
+// its own launch; otherwise they are separate kernels.
+void iterate_stream(Handle* h, int level, int dir, int pro = 0, int rst = 0, int rst_zero = 0) {
     Level& lv = h->lev[level];
     const int Niter = h->p.Nmulti;
     const bool cheb_pp = (level == h->ratio_level);
@@ -387,10 +402,24 @@ void iterate_stream(Handle* h, int level, int dir) {
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
         const int pp = (dir != 1 && cheb_pp) ? 1 : 0;
+        VisitXfer<double> x;
+        if (pro) {
+            x.ec = cur_err(h, level + 1);
+            x.Lc = h->lev[level + 1].L;
+        }
+        if (rst) {
+            x.rc = h->lev[level + 1].rhs;
+            x.Lr = h->lev[level + 1].L;
+            if (rst_zero) {
+                x.zc = cur_err(h, level + 1);
+                x.zn = h->lev[level + 1].L.plane;
+            }
+        }
         if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, tv, (h->ctab_level == level) ? h->ctab : nullptr,
-                                 Niter, pp, h->p.Vbc, &h->ds->visit_timeout) == 0)
+                                 Niter, pp, h->p.Vbc, &h->ds->visit_timeout, &x) == 0)
             return;
     }
+    if (pro) launch_prolong(h->st, h->lev[level + 1], lv, cur_err(h, level + 1), cur_err(h, level), h->p.Vbc);
     const int per_point = (dir != 1 && cheb_pp) ? 1 : 0;
     int flips = 0;
     for (int n = 1; n <= Niter;) {
@@ -413,27 +442,59 @@ void iterate_stream(Handle* h, int level, int dir) {
         lv.ecur = 1 - lv.ecur;
     }
     launch_residual(h->st, lv, lv.err[lv.ecur], h->rs, &h->ds->res_mag[level]);
+    if (rst)
+        launch_restrict_res(h->st, h->lev[level + 1], lv, lv.res, h->lev[level + 1].rhs,
+                            rst_zero ? cur_err(h, level + 1) : nullptr);
+}
+
+// Transfers of cycle step pp that the adjacent visits take over: the
+// restriction into the next step's level when this step's visit fuses and
+// the cycle goes down; the prolongation out of this step's level when the
+// next step's visit fuses and the cycle goes up.
+struct StepFusion {
+    int rst = 0, rst_zero = 0, pro_next = 0;
+};
+static StepFusion step_fusion(Handle* h, int pp) {
+    StepFusion f;
+    const int G = h->grids, level = h->multi[pp];
+    const int dir = (h->multi[pp + 1] > level) ? 0 : 1;
+    if (level < G && h->multi[pp + 1] == level + 1 && visit_fuses(h, level, dir)) {
+        f.rst = 1;
+        f.rst_zero = (level + 1 < G && h->p.mg_zero_coarse) ? 1 : 0;
+    }
+    if (pp + 1 <= h->nsteps && h->multi[pp + 1] == level - 1) {
+        const int nl = level - 1;
+        f.pro_next = visit_fuses(h, nl, (h->multi[pp + 2] > nl) ? 0 : 1) ? 1 : 0;
+    }
+    return f;
 }
 
 // Work of one multigrid cycle after the level-1 visit (p = 2..nsteps);
 // no host synchronisation inside, so it can be captured in a CUDA graph.
 void enqueue_cycle_rest(Handle* h) {
     const int G = h->grids;
+    bool restricted = false, pending_pro = false;
     for (int pp = 2; pp <= h->nsteps; pp++) {
         const int level = h->multi[pp];
         const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
         const bool zero = h->multi[pp - 1] < h->multi[pp] && level > 1 && level < G && h->p.mg_zero_coarse;
-        if (h->multi[pp - 1] < h->multi[pp] && level > 1)
+        if (h->multi[pp - 1] < h->multi[pp] && level > 1 && !restricted)
             launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs,
                                 zero ? cur_err(h, level) : nullptr);
+        const StepFusion f = step_fusion(h, pp);
         if (level < G) {
-            iterate_stream(h, level, dir);
+            iterate_stream(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
         } else {
             launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_err(h, G), h->p.Vbc);
         }
-        if (h->multi[pp + 1] < h->multi[pp])
-            launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
-                           h->p.Vbc);
+        restricted = f.rst != 0;
+        pending_pro = false;
+        if (h->multi[pp + 1] < h->multi[pp]) {
+            if (f.pro_next) pending_pro = true;
+            else
+                launch_prolong(h->st, h->lev[level], h->lev[level - 1], cur_err(h, level), cur_err(h, level - 1),
+                               h->p.Vbc);
+        }
     }
 }
 
@@ -442,7 +503,7 @@ float* cur_e32(Handle* h, int l) { return h->lev[l].e32[h->lev[l].e32cur]; }
 
 // iterate_stream on the FP32 correction of `level` (same sweeps and factors
 // as iterate_stream); level 1 skips the FP32 residual (its residual is FP64).
-void iterate_stream32(Handle* h, int level, int dir) {
+void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, int rst_zero = 0) {
     Level& lv = h->lev[level];
     const int Niter = h->p.Nmulti;
     const bool cheb_pp = (level == h->ratio_level);
@@ -450,10 +511,24 @@ void iterate_stream32(Handle* h, int level, int dir) {
     if (h->fuse_visits && lv.fuse && level > 1 && Niter <= 128) {
         double cv[128], tv[128];
         cheb_temps(Niter, dir, tv, cv);
+        VisitXfer<float> x;
+        if (pro) {
+            x.ec = cur_e32(h, level + 1);
+            x.Lc = h->lev[level + 1].L;
+        }
+        if (rst) {
+            x.rc = h->lev[level + 1].rhs32;
+            x.Lr = h->lev[level + 1].L;
+            if (rst_zero) {
+                x.zc = cur_e32(h, level + 1);
+                x.zn = h->lev[level + 1].L.plane;
+            }
+        }
         if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, tv, Niter, pp, h->p.Vbc,
-                                   &h->ds->visit_timeout) == 0)
+                                   &h->ds->visit_timeout, &x) == 0)
             return;
     }
+    if (pro) launch_prolong32(h->st, h->lev[level + 1], lv, cur_e32(h, level + 1), cur_e32(h, level), h->p.Vbc);
     int flips = 0;
     for (int n = 1; n <= Niter;) {
         // lv.blk sweeps per launch of the tiled smoother while that many
@@ -482,6 +557,9 @@ void iterate_stream32(Handle* h, int level, int dir) {
         lv.e32cur = 1 - lv.e32cur;
     }
     if (level > 1) launch_residual32(h->st, lv, cur_e32(h, level));
+    if (rst)
+        launch_restrict32(h->st, h->lev[level + 1], lv, lv.res32, h->lev[level + 1].rhs32,
+                          rst_zero ? cur_e32(h, level + 1) : nullptr);
 }
 
 // level-1 visit of the mixed solve: r = RHS - L psi (FP64) -> FP32 RHS,
@@ -497,6 +575,7 @@ void enqueue_l1_mixed(Handle* h, int dir) {
 // p = 2..nsteps of the mixed solve (enqueue_cycle_rest on FP32 corrections)
 void enqueue_rest_mixed(Handle* h, int) {
     const int G = h->grids;
+    bool restricted = false, pending_pro = false;
     for (int pp = 2; pp <= h->nsteps; pp++) {
         const int level = h->multi[pp];
         const int dir = (h->multi[pp + 1] > h->multi[pp]) ? 0 : 1;
@@ -504,14 +583,19 @@ void enqueue_rest_mixed(Handle* h, int) {
         float* zero = (down && level > 1 && level < G && h->p.mg_zero_coarse) ? cur_e32(h, level) : nullptr;
         if (down && level == 2)
             launch_restrict64to32(h->st, h->lev[2], h->lev[1], h->lev[1].res, h->lev[2].rhs32, zero);
-        else if (down && level > 2)
+        else if (down && level > 2 && !restricted)
             launch_restrict32(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res32, h->lev[level].rhs32,
                               zero);
-        if (level < G) iterate_stream32(h, level, dir);
+        const StepFusion f = step_fusion(h, pp);
+        if (level < G) iterate_stream32(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
         else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_e32(h, G), h->p.Vbc);
+        restricted = f.rst != 0;
+        pending_pro = false;
         if (h->multi[pp + 1] < h->multi[pp]) {
             if (level == 2)
                 launch_prolong_into64(h->st, h->lev[2], h->lev[1], cur_e32(h, 2), cur_err(h, 1), h->p.Vbc);
+            else if (f.pro_next)
+                pending_pro = true;
             else
                 launch_prolong32(h->st, h->lev[level], h->lev[level - 1], cur_e32(h, level), cur_e32(h, level - 1),
                                  h->p.Vbc);

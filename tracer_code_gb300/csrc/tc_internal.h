@@ -142,10 +142,25 @@ void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n)
 int visit_cluster_setup();
 int visit_cluster_fits(const Lay& L, int nsweeps, int fp32, int cfg = 0);
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab);
+// grid transfers a visit can do in the same launch (nullptr = none): add the
+// prolongation of the next coarser level's correction ec before the first
+// sweep; after the last, restrict the residual into the coarser RHS rc and
+// zero the coarser correction zc (zn values)
+template <typename T>
+struct VisitXfer {
+    const T* ec = nullptr;
+    Lay Lc{};
+    T* rc = nullptr;
+    Lay Lr{};
+    T* zc = nullptr;
+    size_t zn = 0;
+};
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
-                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag);
+                         const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag,
+                         const VisitXfer<double>* x = nullptr);
 int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
-                           int nsweeps, int per_point, int Vbc, int* timeout_flag);
+                           int nsweeps, int per_point, int Vbc, int* timeout_flag,
+                           const VisitXfer<float>* x = nullptr);
 
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
