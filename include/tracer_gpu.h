@@ -139,6 +139,13 @@ typedef struct tc_params {
      * correction before it is added (removes grid-scale noise that the
      * BF16 output carries; 0 = none). */
     int32_t learned_smooth;
+    /* No reference counterpart.  The tracer arrays are kept in the order of
+     * the corner control volume each tracer is counted in: tc_energy_time
+     * re-sorts them (a counting sort by cell) before its RK stages when
+     * tstep is a multiple of this interval (0 = never).  Results do not
+     * depend on it; every host-facing call keeps the reference's tracer
+     * order.  Default 10. */
+    int32_t tracer_sort_interval;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
@@ -285,6 +292,12 @@ tc_status tc_download_velocities(tc_handle* h, double* u, double* w);
  * smoothing on: Cnew, count_type, nempty, Cvis, Cbuoy, conduct are updated.
  * rtr/str are HOST arrays of ntr doubles. */
 tc_status tc_tracers_to_corners(tc_handle* h, const double* rtr, const double* str);
+
+/* Diagnostic (no reference counterpart): perm[j] (ntr int32) = the
+ * reference's index of the tracer in storage slot j on the device (the
+ * identity after an upload; the cell order after a re-sort, see
+ * tracer_sort_interval). */
+tc_status tc_tracer_order(tc_handle* h, int32_t* perm);
 
 /* Copies count_type (0:ntype, -span:nx+span, -span:nz+span) as int32. */
 tc_status tc_download_counts(tc_handle* h, int32_t* count_type);

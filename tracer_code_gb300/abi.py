@@ -71,6 +71,7 @@ class Params(C.Structure):
         ("delta_visT", C.c_double), ("yield_", C.c_double), ("yield_gradient", C.c_double),
         ("yield_depth", C.c_double), ("visC", _D4), ("delta_visC", _D4),
         ("mg_zero_coarse", C.c_int32), ("solver_precision", C.c_int32), ("learned_guess", C.c_int32), ("learned_smooth", C.c_int32),
+        ("tracer_sort_interval", C.c_int32),
     ]
 
     def copy(self) -> "Params":
@@ -133,6 +134,7 @@ def default_params() -> Params:
         p.delta_visC[t] = 2.0
     p.eig_ratio_min, p.ivis, p.visP, p.visT, p.delta_visT = 4.0, 2, 1.0, 3.0e4, 100.0
     p.yield_, p.yield_gradient, p.yield_depth = 15.0, 0.0, 0.1
+    p.tracer_sort_interval = 10
     return p
 
 

@@ -172,3 +172,144 @@ void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* cou
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
     k_counts_to_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, counts, nempty, C); tc_note_launch();
 }
+
+// ---- cell sort of the tracer arrays -------------------------------------------
+// The tracers are kept in the order of the corner control volume that
+// tracers_to_corners counts them in, so the warps of k_tracer_stage gather
+// from neighbouring grid rows and those of k_histogram meet few distinct
+// counters.  A counting sort: per-cell counts, an exclusive scan, and a
+// scatter that takes each tracer's slot with an atomic on its cell's offset
+// (the order inside a cell is left free: nothing the step computes depends on
+// it, every tracer is advanced on its own and the counts are integers).
+// perm[j] is the reference's index of the tracer stored at slot j.
+namespace {
+__device__ __forceinline__ int tracer_cell(const Lay& L, const Phys& P, double r, double s) {
+    int i = (int)round(r / P.dr), k = (int)round(s / P.ds);
+    i = min(max(i, 0), P.nx);
+    k = min(max(k, 0), P.nz);
+    return (int)IX(L, i, k);
+}
+
+__global__ void k_sort_count(Lay L, Phys P, int64_t ntr, const double* rr, const double* ss, int* cnt) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int key = (id < ntr) ? tracer_cell(L, P, ld_state(rr + id), ld_state(ss + id)) : -1;
+    const unsigned act = __activemask();
+    const unsigned peers = __match_any_sync(act, key);
+    if (key >= 0 && (int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(cnt + key, __popc(peers));
+}
+
+// exclusive scan of one 1024-element block in shared memory; returns the block total
+__device__ int block_exclusive_scan(int v, int* warp_tot, int* out_excl) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int n = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += n;
+    }
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        int t = (lane < (int)(blockDim.x >> 5)) ? warp_tot[lane] : 0;
+        int ti = t;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int n = __shfl_up_sync(0xffffffffu, ti, o);
+            if (lane >= o) ti += n;
+        }
+        warp_tot[lane] = ti - t;  // exclusive prefix of the warps
+        if (lane == 31) warp_tot[32] = ti;
+    }
+    __syncthreads();
+    *out_excl = warp_tot[wid] + incl - v;
+    const int tot = warp_tot[32];
+    __syncthreads();
+    return tot;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(const int* cnt, int n, int* bsum) {
+    __shared__ int wt[33];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    int ex;
+    const int tot = block_exclusive_scan(i < n ? cnt[i] : 0, wt, &ex);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = tot;
+}
+// one block: exclusive scan of the block totals, 1024 at a time with a carry
+__global__ void __launch_bounds__(1024) k_scan_bsums(int* bsum, int nb) {
+    __shared__ int wt[33];
+    int carry = 0;
+    for (int base = 0; base < nb; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = (i < nb) ? bsum[i] : 0;
+        int ex;
+        const int tot = block_exclusive_scan(v, wt, &ex);
+        if (i < nb) bsum[i] = carry + ex;
+        carry += tot;
+    }
+}
+__global__ void __launch_bounds__(1024) k_scan_final(const int* cnt, int n, const int* bsum, int* off) {
+    __shared__ int wt[33];
+    const int i = blockIdx.x * 1024 + threadIdx.x;
+    int ex;
+    block_exclusive_scan(i < n ? cnt[i] : 0, wt, &ex);
+    if (i < n) off[i] = bsum[blockIdx.x] + ex;
+}
+
+__global__ void k_sort_scatter(Lay L, Phys P, int64_t ntr, const double* rr, const double* ss, const int* tt,
+                               const int* perm, int* off, double* r2, double* s2, int* t2, int* p2) {
+    const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= ntr) return;
+    const double r = ld_state(rr + id), s = ld_state(ss + id);
+    const int pos = atomicAdd(off + tracer_cell(L, P, r, s), 1);
+    r2[pos] = r;
+    s2[pos] = s;
+    t2[pos] = ld_state(tt + id);
+    p2[pos] = ld_state(perm + id);
+}
+
+template <typename T>
+__global__ void k_perm_scatter(int64_t n, const int* perm, const T* in, T* out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[ld_state(perm + j)] = ld_state(in + j);
+}
+template <typename T>
+__global__ void k_perm_gather(int64_t n, const int* perm, const T* in, T* out) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) out[j] = ld_state(in + ld_state(perm + j));
+}
+__global__ void k_iota(int64_t n, int* p) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) p[j] = (int)j;
+}
+}  // namespace
+
+// cnt, off: L.plane ints each; bsum: (L.plane + 1023) / 1024 ints
+void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* rr, const double* ss,
+                         const int* tt, const int* perm, int* cnt, int* off, int* bsum, double* r2, double* s2,
+                         int* t2, int* p2) {
+    if (ntr <= 0) return;
+    const int n = (int)L.plane, nb = (n + 1023) / 1024;
+    const unsigned tb = (unsigned)((ntr + 255) / 256);
+    cudaMemsetAsync(cnt, 0, sizeof(int) * (size_t)n, s);
+    k_sort_count<<<tb, 256, 0, s>>>(L, P, ntr, rr, ss, cnt); tc_note_launch();
+    k_scan_blocks<<<nb, 1024, 0, s>>>(cnt, n, bsum); tc_note_launch();
+    k_scan_bsums<<<1, 1024, 0, s>>>(bsum, nb); tc_note_launch();
+    k_scan_final<<<nb, 1024, 0, s>>>(cnt, n, bsum, off); tc_note_launch();
+    k_sort_scatter<<<tb, 256, 0, s>>>(L, P, ntr, rr, ss, tt, perm, off, r2, s2, t2, p2); tc_note_launch();
+}
+void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out) {
+    if (n <= 0) return;
+    k_perm_scatter<double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, perm, in, out); tc_note_launch();
+}
+void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const int* in, int* out) {
+    if (n <= 0) return;
+    k_perm_scatter<int><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, perm, in, out); tc_note_launch();
+}
+void launch_perm_gather(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out) {
+    if (n <= 0) return;
+    k_perm_gather<double><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, perm, in, out); tc_note_launch();
+}
+void launch_iota(cudaStream_t s, int64_t n, int* p) {
+    if (n <= 0) return;
+    k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, p); tc_note_launch();
+}

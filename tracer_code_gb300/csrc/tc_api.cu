@@ -101,6 +101,10 @@ struct Handle {
     bool no_graphs = false;
     int cycles_acc = 0;  // W-cycles of all solves since tc_step began
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
+    // cell order of the tracer arrays: perm[j] = reference index of slot j
+    int* perm = nullptr;
+    int* itmp[2] = {nullptr, nullptr};  // scatter targets of ttype and perm
+    int *sort_cnt = nullptr, *sort_off = nullptr, *sort_bsum = nullptr;
     double* ctab = nullptr;    // per-point Chebyshev factors of the fused ratio level [Nmulti][(a-1)(b-1)]
     int ctab_level = 0;        // level the table was built for (0 = none)
     cudaError_t enq_err = cudaSuccess;  // first error of an enqueue-only helper (checked by its caller)
@@ -242,6 +246,36 @@ tc_status smoother_time(Handle* h) {
             if (++guard > h->loop_cap) return TC_ERR_LOOP_CAP;
         }
         h->n_comp[t] = nn;
+    }
+    return TC_OK;
+}
+
+// the tracer arrays in cell order (k_tracer.cu): positions, types and the
+// reference index move together; the RK temporaries take the old arrays
+void sort_tracers(Handle* h) {
+    launch_sort_tracers(h->st, h->L1, h->P, h->ntr, h->rtr, h->str, h->ttype, h->perm, h->sort_cnt, h->sort_off,
+                        h->sort_bsum, h->rtr1, h->str1, h->itmp[0], h->itmp[1]);
+    std::swap(h->rtr, h->rtr1);
+    std::swap(h->str, h->str1);
+    std::swap(h->ttype, h->itmp[0]);
+    std::swap(h->perm, h->itmp[1]);
+}
+
+// tracer arrays to host arrays in the reference's order (any may be null);
+// the copies are queued on the handle's stream
+tc_status download_tracers(Handle* h, double* rtr, double* str, int32_t* Ttype) {
+    const size_t n = (size_t)h->ntr;
+    if (rtr) {
+        launch_perm_scatter(h->st, h->ntr, h->perm, h->rtr, h->rtr2);
+        CK(cudaMemcpyAsync(rtr, h->rtr2, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    }
+    if (str) {
+        launch_perm_scatter(h->st, h->ntr, h->perm, h->str, h->str2);
+        CK(cudaMemcpyAsync(str, h->str2, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    }
+    if (Ttype) {
+        launch_perm_scatter(h->st, h->ntr, h->perm, h->ttype, h->itmp[0]);
+        CK(cudaMemcpyAsync(Ttype, h->itmp[0], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, h->st));
     }
     return TC_OK;
 }
@@ -776,6 +810,8 @@ tc_status energy_time(Handle* h) {
     TRY(check_flags(h));
     for (int t = 0; t < h->ntype; t++) copy_plane(h, h->C0[t], h->Cnew[t]);
     copy_plane(h, h->T0, h->T);
+    if (trc && h->ntr > 0 && h->p.tracer_sort_interval > 0 && h->tstep % h->p.tracer_sort_interval == 0)
+        sort_tracers(h);
     if (trc) { std::swap(h->rtr0, h->rtr); std::swap(h->str0, h->str); }
     auto derivs = [&]() {
         launch_derivatives(h->st, h->L1, h->P, h->u, h->du);
@@ -975,6 +1011,11 @@ tc_status create(Handle* h, const tc_params* in) {
         double** tr[] = {&h->rtr, &h->str, &h->rtr0, &h->str0, &h->rtr1, &h->str1, &h->rtr2, &h->str2};
         for (double** q : tr) TRY(dalloc_t(h, q, (size_t)h->ntr));
         TRY(dalloc_t(h, &h->ttype, (size_t)h->ntr));
+        TRY(dalloc_t(h, &h->perm, (size_t)h->ntr));
+        for (int q = 0; q < 2; q++) TRY(dalloc_t(h, &h->itmp[q], (size_t)h->ntr));
+        TRY(dalloc_t(h, &h->sort_cnt, pl));
+        TRY(dalloc_t(h, &h->sort_off, pl));
+        TRY(dalloc_t(h, &h->sort_bsum, (pl + 1023) / 1024));
     }
     const int ldab = 2 * h->kl + h->ku + 1;
     TRY(dalloc_t(h, &h->band, (size_t)ldab * h->ngrid_coarse));
@@ -1131,6 +1172,7 @@ tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF,
         CK(cudaMemcpyAsync(h->rtr, r, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemcpyAsync(h->str, s, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemcpyAsync(h->ttype, tt, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        launch_iota(h->st, h->ntr, h->perm);
     }
     CK(cudaMemsetAsync(h->ds, 0, sizeof(DevScalars), h->st));
     launch_enforce_T(h->st, h->L1, h->T, h->p.Tbot);
@@ -1213,6 +1255,7 @@ void tc_default_params(tc_params* p) {
     }
     p->eig_ratio_min = 4.0; p->ivis = 2; p->visP = 1.0; p->visT = 3.0e4; p->delta_visT = 100.0;
     p->yield = 15.0; p->yield_gradient = 0.0; p->yield_depth = 0.1;
+    p->tracer_sort_interval = 10;
 }
 
 void tc_abi_sizes(int32_t sizes[3]) {
@@ -1330,11 +1373,7 @@ tc_status tc_download_state(tc_handle* H, double* T, double* Cnew, double* SF, d
             for (size_t x = 0; x < ni * nk; x++) Cnew[x * h->ntype + t] = tmp[x];
         }
     }
-    if (h->p.comp == 1) {
-        if (rtr) CK(cudaMemcpyAsync(rtr, h->rtr, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
-        if (str) CK(cudaMemcpyAsync(str, h->str, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
-        if (Ttype) CK(cudaMemcpyAsync(Ttype, h->ttype, sizeof(int32_t) * h->ntr, cudaMemcpyDeviceToHost, h->st));
-    }
+    if (h->p.comp == 1) TRY(download_tracers(h, rtr, str, Ttype));
     CK(cudaStreamSynchronize(h->st));
     return TC_OK;
 }
@@ -1559,16 +1598,14 @@ tc_status tc_step_host(tc_handle* H, double* T, double* Cnew, double* SF, double
         CK(cudaMemcpyAsync(h->rtr, rtr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemcpyAsync(h->str, str, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemcpyAsync(h->ttype, Ttype, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        launch_iota(h->st, h->ntr, h->perm);
     }
     tc_status s = tc_step(H, row, cycles, dt_out);
     if (s != TC_OK) return s;
     TRY(get_field(h, T, h->T));
     TRY(get_field(h, SF, h->SF));
     if (h->ntype == 1) TRY(get_field(h, Cnew, h->Cnew[0]));
-    if (h->p.comp == 1) {
-        CK(cudaMemcpyAsync(rtr, h->rtr, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
-        CK(cudaMemcpyAsync(str, h->str, sizeof(double) * h->ntr, cudaMemcpyDeviceToHost, h->st));
-    }
+    if (h->p.comp == 1) TRY(download_tracers(h, rtr, str, nullptr));
     CK(cudaStreamSynchronize(h->st));
     return TC_OK;
 }
@@ -1665,10 +1702,23 @@ tc_status tc_tracers_to_corners(tc_handle* H, const double* rtr, const double* s
     if (!H || !rtr || !str) return TC_ERR_ARG;
     Handle* h = &H->h;
     if (h->p.comp != 1) return TC_ERR_UNSUPPORTED;
-    CK(cudaMemcpyAsync(h->rtr2, rtr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
-    CK(cudaMemcpyAsync(h->str2, str, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    // positions in the reference's order, gathered into the cell order of
+    // the tracer types
+    CK(cudaMemcpyAsync(h->rtr1, rtr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(h->str1, str, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
+    launch_perm_gather(h->st, h->ntr, h->perm, h->rtr1, h->rtr2);
+    launch_perm_gather(h->st, h->ntr, h->perm, h->str1, h->str2);
     TRY(tracers_to_corners(h, h->rtr2, h->str2, true));
     return check_flags(h);
+}
+
+tc_status tc_tracer_order(tc_handle* H, int32_t* perm) {
+    if (!H || !perm) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (h->ntr <= 0 || !h->perm) return TC_ERR_STATE;
+    CK(cudaMemcpyAsync(perm, h->perm, sizeof(int32_t) * (size_t)h->ntr, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
 }
 
 tc_status tc_download_counts(tc_handle* H, int32_t* count_type) {

@@ -222,5 +222,13 @@ void launch_tracer_stage(cudaStream_t s, const Lay& L, const Phys& P, int torder
                          const double* du, const double* dw, const DevScalars* ds);
 void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* r, const double* sv,
                       const int* ttype, int* counts, DevScalars* ds);
+// cell sort of the tracer arrays (k_tracer.cu): rr/ss/tt/perm -> r2/s2/t2/p2
+void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* rr, const double* ss,
+                         const int* tt, const int* perm, int* cnt, int* off, int* bsum, double* r2, double* s2,
+                         int* t2, int* p2);
+void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out);
+void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const int* in, int* out);
+void launch_perm_gather(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out);
+void launch_iota(cudaStream_t s, int64_t n, int* p);
 void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* counts, int* nempty,
                            double* const* Cnew);
