@@ -251,11 +251,20 @@ __global__ void __launch_bounds__(256, 1) k_sweep(Lay L, Range2 r, const double*
     store_stream(L, Sout, i, k, v, Vbc);
     pdl_done();
 }
+// one point per thread: the two-point kernel (k_sweep_x2<double>, 120 registers)
+// measured 18.3 against 8.5 us per level-1 sweep (half the resident warps)
+static constexpr bool kSweepPairs = false;
 void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
                   int per_point, double temp, int Vbc) {
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
-    launch_pdl(k_sweep, grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB,
-                                                  c_uniform, per_point, temp, Vbc); tc_note_launch();
+    if (kSweepPairs)
+        launch_pdl(k_sweep_x2<double>, grid_for_shape(r, lv.sweep_bx, 2 * lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by),
+                   0, s, lv.L, r, Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB, c_uniform, per_point, temp,
+                   Vbc);
+    else
+        launch_pdl(k_sweep, grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r,
+                   Sin, Sout, lv.coef, lv.rhs, lv.dt_stream, lv.cA, lv.cB, c_uniform, per_point, temp, Vbc);
+    tc_note_launch();
 }
 
 __global__ void __launch_bounds__(256, 1) k_residual(Lay L, Range2 r, const double* S, const double* __restrict__ coef,

@@ -59,86 +59,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
     pdl_done();
 }
 
-// k_sweep32 for two vertically adjacent points per thread (rows k, k+1):
-// the 18 stencil values of the pair are loaded once (13 per point alone),
-// and the two multiply-add chains interleave.  Same taps in the same order
-// per point as folded_residual, so the result equals k_sweep32's.
-__global__ void __launch_bounds__(256, 1) k_sweep32x2(Lay L, Range2 r, const float* Sin, float* Sout,
-                                                     const float* __restrict__ coef, const float* rhs,
-                                                     const float* __restrict__ dts, const float* __restrict__ cA,
-                                                     const float* __restrict__ cB, float c_uniform, int per_point,
-                                                     float temp, int Vbc) {
-    const int i = r.i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
-    const int k = r.k0 + 2 * (int)(blockIdx.y * blockDim.y + threadIdx.y);
-    bool act[2];
-    act[0] = (i <= r.i1) && (k <= r.k1);
-    act[1] = act[0] && (k + 1 <= r.k1);
-    const size_t ld = (size_t)L.ld, pl = L.plane;
-    const size_t x = act[0] ? IX(L, i, k) : 0;
-    float cf[2][TC_NCOEF], dt[2], ca[2], cb[2];
-#pragma unroll
-    for (int p = 0; p < 2; p++) {
-        const size_t xp = act[p] ? x + p * ld : x;
-#pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++) cf[p][d] = act[p] ? -__ldg(coef + xp + d * pl) : 0.f;
-        dt[p] = act[p] ? __ldg(dts + xp) : 0.f;
-        ca[p] = (act[p] && per_point) ? __ldg(cA + xp) : 1.f;
-        cb[p] = (act[p] && per_point) ? __ldg(cB + xp) : 0.f;
-    }
-    pdl_entry();
-    if (!act[0]) return;
-    // centre column rows k-2..k+3, columns i+-1 rows k-1..k+2, i+-2 rows k..k+1
-    const float* s = Sin + x;
-    float v0[6], vm1[4], vp1[4], vm2[2], vp2[2], rh[2];
-#pragma unroll
-    for (int q = 0; q < 6; q++) v0[q] = ld_state(s + (ptrdiff_t)(q - 2) * (ptrdiff_t)ld);
-#pragma unroll
-    for (int q = 0; q < 4; q++) {
-        vm1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld - 1);
-        vp1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld + 1);
-    }
-#pragma unroll
-    for (int q = 0; q < 2; q++) {
-        vm2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld - 2);
-        vp2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld + 2);
-        rh[q] = act[q] ? ld_state(rhs + x + q * ld) : 0.f;
-    }
-    float acc[2];
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][0], v0[p + 2], rh[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][1], vm1[p + 1], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][2], vp1[p + 1], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][3], vm2[p], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][4], vp2[p], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][5], v0[p + 1], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][6], v0[p + 3], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][7], v0[p], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][8], v0[p + 4], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][9], vm1[p], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][10], vp1[p], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][11], vm1[p + 2], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) acc[p] = fmaf(cf[p][12], vp1[p + 2], acc[p]);
-#pragma unroll
-    for (int p = 0; p < 2; p++) {
-        if (!act[p]) continue;
-        const float c = per_point ? 2.0f / (ca[p] + cb[p] * temp) : c_uniform;
-        store_stream<float>(L, Sout, i, k + p, fmaf(c * dt[p], acc[p], v0[p + 2]), Vbc);
-    }
-    pdl_done();
-}
-
 __global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* S, const float* __restrict__ coef,
                              const float* rhs, float* res) {
     RANGE_IK(r);
@@ -252,13 +172,13 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb) {
     }
 }
 
-static constexpr bool kSweep32Pairs = true;  // k_sweep32x2 (two points per thread) for the per-sweep FP32 smoother
+static constexpr bool kSweep32Pairs = true;  // k_sweep_x2 (two points per thread) for the per-sweep FP32 smoother
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc) {
     const Range2 r = interior(lv.L);
     if (kSweep32Pairs) {
         dim3 g = grid_for_shape(r, lv.sweep_bx, 2 * lv.sweep_by);
-        launch_pdl(k_sweep32x2, g, dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef32, lv.rhs32,
+        launch_pdl(k_sweep_x2<float>, g, dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef32, lv.rhs32,
                    lv.dts32, lv.cA32, lv.cB32, c_uniform, per_point, temp, Vbc);
     } else {
         launch_pdl(k_sweep32, grid_for_shape(r, lv.sweep_bx, lv.sweep_by), dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L,

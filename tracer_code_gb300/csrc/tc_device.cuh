@@ -240,3 +240,84 @@ inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, siz
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, kern, static_cast<Args&&>(args)...);
 }
+
+// One smoother sweep (k_sweep / k_sweep32) for two vertically adjacent
+// points per thread (rows k, k+1):
+// the 18 stencil values of the pair are loaded once (13 per point alone),
+// and the two multiply-add chains interleave.  Same taps in the same order
+// per point as folded_residual, so the result equals the one-point kernels'.
+template <typename T>
+__global__ void __launch_bounds__(256, 1) k_sweep_x2(Lay L, Range2 r, const T* Sin, T* Sout, const T* __restrict__ coef,
+                                                    const T* rhs, const T* __restrict__ dts,
+                                                    const T* __restrict__ cA, const T* __restrict__ cB, T c_uniform,
+                                                    int per_point, T temp, int Vbc) {
+    const int i = r.i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int k = r.k0 + 2 * (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    bool act[2];
+    act[0] = (i <= r.i1) && (k <= r.k1);
+    act[1] = act[0] && (k + 1 <= r.k1);
+    const size_t ld = (size_t)L.ld, pl = L.plane;
+    const size_t x = act[0] ? IX(L, i, k) : 0;
+    T cf[2][TC_NCOEF], dt[2], ca[2], cb[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const size_t xp = act[p] ? x + p * ld : x;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) cf[p][d] = act[p] ? -__ldg(coef + xp + d * pl) : T(0);
+        dt[p] = act[p] ? __ldg(dts + xp) : T(0);
+        ca[p] = (act[p] && per_point) ? __ldg(cA + xp) : T(1);
+        cb[p] = (act[p] && per_point) ? __ldg(cB + xp) : T(0);
+    }
+    pdl_entry();
+    if (!act[0]) return;
+    // centre column rows k-2..k+3, columns i+-1 rows k-1..k+2, i+-2 rows k..k+1
+    const T* s = Sin + x;
+    T v0[6], vm1[4], vp1[4], vm2[2], vp2[2], rh[2];
+#pragma unroll
+    for (int q = 0; q < 6; q++) v0[q] = ld_state(s + (ptrdiff_t)(q - 2) * (ptrdiff_t)ld);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        vm1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld - 1);
+        vp1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld + 1);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        vm2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld - 2);
+        vp2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld + 2);
+        rh[q] = act[q] ? ld_state(rhs + x + q * ld) : T(0);
+    }
+    T acc[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][0], v0[p + 2], rh[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][1], vm1[p + 1], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][2], vp1[p + 1], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][3], vm2[p], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][4], vp2[p], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][5], v0[p + 1], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][6], v0[p + 3], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][7], v0[p], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][8], v0[p + 4], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][9], vm1[p], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][10], vp1[p], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][11], vm1[p + 2], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) acc[p] = fma(cf[p][12], vp1[p + 2], acc[p]);
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        if (!act[p]) continue;
+        const T c = per_point ? T(2) / (ca[p] + cb[p] * temp) : c_uniform;
+        store_stream<T>(L, Sout, i, k + p, fma(c * dt[p], acc[p], v0[p + 2]), Vbc);
+    }
+    pdl_done();
+}
