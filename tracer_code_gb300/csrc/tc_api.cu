@@ -1012,6 +1012,7 @@ tc_status create(Handle* h, const tc_params* in) {
         for (double** q : tr) TRY(dalloc_t(h, q, (size_t)h->ntr));
         TRY(dalloc_t(h, &h->ttype, (size_t)h->ntr));
         TRY(dalloc_t(h, &h->perm, (size_t)h->ntr));
+        launch_iota(h->st, h->ntr, h->perm);  // a valid permutation before any upload
         for (int q = 0; q < 2; q++) TRY(dalloc_t(h, &h->itmp[q], (size_t)h->ntr));
         TRY(dalloc_t(h, &h->sort_cnt, pl));
         TRY(dalloc_t(h, &h->sort_off, pl));
