@@ -254,6 +254,14 @@ def sweep_roofline(sim, p, fp32: bool) -> dict:
                      "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s")}
 
 
+def replica_rate(units_per_rank: float, seconds_local: float, world: int, max_over_ranks) -> float:
+    """Whole-job throughput of N independent replicas: the units all ranks
+    processed over the slowest rank's time (each rank runs the same work, so
+    the units are world * units_per_rank).  max_over_ranks reduces a float
+    over the process group (identity for one rank)."""
+    return world * units_per_rank / max_over_ranks(seconds_local)
+
+
 def run_ours(args, rank: int, world: int, local_rank: int):
     import numpy as np
     import torch
@@ -287,7 +295,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         ms, solves, cycles, launches = timed_steps(sim, stream, args.steps, args.warmup, barrier)
     guess_used, guess_offered = learned.guess_stats(sim)
     ms_max = max_over_ranks(ms)
-    value = world * args.steps / (ms_max * 1e-3)
+    value = replica_rate(args.steps, ms * 1e-3, world, max_over_ranks)
     roof = sweep_roofline(sim, p, fp32=True)
     # end to end: the same steps through tc_step_host with pinned host state
     host = {}
@@ -306,7 +314,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     for _ in range(k_e2e):
         sim.step_host(host)
     torch.cuda.synchronize()
-    e2e_value = world * k_e2e / max_over_ranks(time.perf_counter() - t0)
+    e2e_value = replica_rate(k_e2e, time.perf_counter() - t0, world, max_over_ranks)
     sim.close()
     net.close()
     # the same mixed solver without the network
@@ -314,14 +322,14 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     simm = Simulation(pm, stream=stream.cuda_stream)
     simm.upload(st)
     msm, solvesm, _, _ = timed_steps(simm, stream, args.steps, args.warmup, barrier)
-    mixed_value = world * args.steps / (max_over_ranks(msm) * 1e-3)
+    mixed_value = replica_rate(args.steps, msm * 1e-3, world, max_over_ranks)
     simm.close()
     # comparison arm: plain FP64 multigrid on the same initial state
     pp = workload_params("plain")
     sim0 = Simulation(pp, stream=stream.cuda_stream)
     sim0.upload(st)
     ms0, solves0, cycles0, _ = timed_steps(sim0, stream, args.steps, args.warmup, barrier)
-    plain_value = world * args.steps / (max_over_ranks(ms0) * 1e-3)
+    plain_value = replica_rate(args.steps, ms0 * 1e-3, world, max_over_ranks)
     roof0 = sweep_roofline(sim0, pp, fp32=False)
     sim0.close()
     if rank == 0:
