@@ -293,6 +293,16 @@ tc_status tc_download_velocities(tc_handle* h, double* u, double* w);
  * rtr/str are HOST arrays of ntr doubles. */
 tc_status tc_tracers_to_corners(tc_handle* h, const double* rtr, const double* str);
 
+/* compute_strain_rate_invariant (momentum.f90:32-62): the strain-rate
+ * invariant of the current velocities (tc_compute_velocities first); the
+ * plastic viscosity (ivis = 3) uses it.  tc_stats computes it as well. */
+tc_status tc_compute_strain_rate_invariant(tc_handle* h);
+/* compute_viscosity (iterative_solver.f90:331-377) for one level: visf and
+ * the viscosity filter at level 1, restriction and filter below (levels in
+ * order, as multigrid calls them); updates the viscosity_smoother scalars
+ * that tc_stats reports (n_eta, eig_fine).  tc_multigrid calls it itself. */
+tc_status tc_compute_viscosity(tc_handle* h, int32_t level);
+
 /* Diagnostic (no reference counterpart): perm[j] (ntr int32) = the
  * reference's index of the tracer in storage slot j on the device (the
  * identity after an upload; the cell order after a re-sort, see

@@ -286,3 +286,5 @@ def test_blocked_sweeps_match_single_sweeps(gpu_lib, prec, ns, nx, nz, grids):
     assert np.array_equal(out[0][1], out[1][1])
     for a, b in zip(out[0][2], out[1][2]):
         assert np.array_equal(a, b)
+
+

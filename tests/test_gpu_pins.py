@@ -1,0 +1,50 @@
+"""Pins the GPU path itself to the reference's shipped outputs (the oracle's
+pins in test_oracle_pins.py, run through the C ABI on the device): from
+Trestart's T and SF, compute_velocities, compute_strain_rate_invariant,
+compute_viscosity(1) (visf with plastic yielding, ivis = 3, and the level-1
+viscosity filter) and stats reproduce stats.dat's and
+viscosity_smoother.dat's last rows to their 8 printed digits."""
+import pytest
+
+from tracer_code_gb300 import Simulation
+from tests.test_oracle_pins import _pin_params, _rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu_row(gpu_lib, golden):
+    g = Simulation(_pin_params(golden))
+    g.upload({"T": golden["T"], "SF": golden["SF"]})
+    g.compute_velocities()
+    g.compute_strain()
+    g.compute_viscosity(1)
+    row = g.stats()
+    g.close()
+    return row
+
+
+@pytest.mark.parametrize("col", ["Tavg", "vrms", "Nu", "Nu_bot", "RaT_avg", "mobility", "strain_max",
+                                 "q1", "q2", "q3", "q4"])
+def test_gpu_stats_row_matches_reference(gpu_row, golden, col):
+    ref = golden["stats_last"][col]
+    assert _rel(gpu_row[col], ref) < 6e-8, (col, gpu_row[col], ref)
+
+
+def test_gpu_viscosity_smoother_row_matches_reference(gpu_row, golden):
+    ref = golden["viscosity_smoother_last"]
+    assert gpu_row["n_eta"] == ref["n_eta"]
+    assert gpu_row["n_temp"] == ref["n_temp"]
+    assert _rel(gpu_row["eig_fine"], ref["eig_fine"]) < 6e-8
+
+
+def test_plastic_multigrid_is_reported_unsupported(gpu_lib, golden):
+    """The GPU multigrid implements the Newtonian branch; the shipped
+    plastic case (ivis = 3, non_Newtonian = 1) is refused, not run wrongly."""
+    from tracer_code_gb300 import TracerError
+    g = Simulation(_pin_params(golden))
+    g.upload({"T": golden["T"], "SF": golden["SF"]})
+    with pytest.raises(TracerError) as e:
+        g.multigrid()
+    assert e.value.status == 2  # TC_ERR_UNSUPPORTED
+    g.close()

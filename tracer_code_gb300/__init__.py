@@ -32,7 +32,7 @@ EXPORTS = [
     "tc_upload_state", "tc_download_state", "tc_set_clock", "tc_multigrid", "tc_compute_velocities", "tc_stats",
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
     "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
-    "tc_set_launch_shapes", "tc_tracer_order",
+    "tc_set_launch_shapes", "tc_tracer_order", "tc_compute_strain_rate_invariant", "tc_compute_viscosity",
 ]
 
 
@@ -82,6 +82,8 @@ def load_library(build_if_missing: bool = False):
         L.tc_autotune.argtypes = [vp, vp]
         L.tc_set_launch_shapes.argtypes = [vp, vp]
         L.tc_tracer_order.argtypes = [vp, vp]
+        L.tc_compute_strain_rate_invariant.argtypes = [vp]
+        L.tc_compute_viscosity.argtypes = [vp, C.c_int32]
         L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
@@ -239,6 +241,12 @@ class Simulation:
         out = (C.c_int32 * (3 * max(g - 1, 1)))()
         self._chk(self.L.tc_autotune(self.h, out), "autotune")
         return [(out[3 * i], out[3 * i + 1], out[3 * i + 2]) for i in range(g - 1)]
+
+    def compute_strain(self) -> None:
+        self._chk(self.L.tc_compute_strain_rate_invariant(self.h), "compute_strain_rate_invariant")
+
+    def compute_viscosity(self, level: int = 1) -> None:
+        self._chk(self.L.tc_compute_viscosity(self.h, level), "compute_viscosity")
 
     def tracer_order(self):
         """perm[j] = reference index of the tracer in device storage slot j."""

@@ -21,7 +21,8 @@
 // visf on the full ghost-padded level-1 box (momentum.f90:1-30; ivis 0,1,2,-1)
 // ---------------------------------------------------------------------------
 __global__ void k_visf1(Lay L, Phys P, Range2 r, double* __restrict__ vis, const double* __restrict__ Tvis, CPtrs C,
-                        const double* __restrict__ zg) {
+                        const double* __restrict__ zg, const double* __restrict__ T,
+                        const double* __restrict__ strain) {
     RANGE_IK(r);
     if (!inr) return;
     size_t x = IX(L, i, k);
@@ -33,6 +34,21 @@ __global__ void k_visf1(Lay L, Phys P, Range2 r, double* __restrict__ vis, const
         for (int j = 0; j < P.ntype; j++) d = d + C.p[j][x] * P.lnvisC[j];
         if (P.RaT != 0.0) v = exp(-Tvis[x] * P.lnvisT - d + (1.0 - zg[k]) * P.lnvisP);
         else v = exp(-d + (1.0 - zg[k]) * P.lnvisP);
+    } else if (P.ivis == 3) {
+        // diffusion creep visT**(-T), in parallel with plastic yielding
+        // (yield + yield_gradient*z)/strain in the top yield_depth; the
+        // strain rate at a ghost node is that of its mirror node
+        // (compute_strain_rate_invariant's ghost copies)
+        const double diffusion = pow(P.visT, -T[x]);
+        const int mi = (i < 0) ? -i : (i > L.a ? 2 * L.a - i : i);
+        const int mk = (k < 0) ? -k : (k > L.b ? 2 * L.b - k : k);
+        const double sr = strain[IX(L, mi, mk)];
+        if (zg[k] < (1.0 - P.yield_depth) || sr == 0.0) {
+            v = diffusion;
+        } else {
+            const double plastic = (P.yield + P.yield_gradient * zg[k]) / sr;
+            v = 1.0 / (1.0 / diffusion + 1.0 / plastic);
+        }
     } else if (P.ivis == -1) {
         v = exp((1.0 - zg[k]) * P.lnvisP);
     } else {
@@ -41,11 +57,11 @@ __global__ void k_visf1(Lay L, Phys P, Range2 r, double* __restrict__ vis, const
     vis[x] = v;
 }
 void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis, const double* Tvis,
-                        const double* const* Cvis, const double* zg) {
+                        const double* const* Cvis, const double* zg, const double* T, const double* strain) {
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
-    k_visf1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, vis, Tvis, C, zg); tc_note_launch();
+    k_visf1<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, vis, Tvis, C, zg, T, strain); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------

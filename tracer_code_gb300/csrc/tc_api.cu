@@ -370,7 +370,7 @@ tc_status smoother_vis(Handle* h, int level, int interpolate) {
 // compute_viscosity (iterative_solver.f90:331-377)
 tc_status compute_viscosity(Handle* h, int level) {
     if (level == 1) {
-        launch_visf_level1(h->st, h->L1, h->P, cur_vis(h, 1), h->Tvis, h->Cvis, h->zg);
+        launch_visf_level1(h->st, h->L1, h->P, cur_vis(h, 1), h->Tvis, h->Cvis, h->zg, h->T, h->strain);
         TRY(smoother_vis(h, 1, 0));
         return TC_OK;
     }
@@ -669,6 +669,17 @@ void enqueue_rest(Handle* h, int) { enqueue_cycle_rest(h); }
 // multigrid (iterative_solver.f90:79-173), Newtonian branch
 tc_status multigrid(Handle* h) {
     if (!h->uploaded) return TC_ERR_STATE;
+    if (h->p.non_Newtonian != 0 || h->p.ivis == 3) {
+        // the non-Newtonian iteration recomputes velocities, strain rate and
+        // every level's viscosity inside the W-cycle loop (iterative_solver.f90:
+        // 100-160); the GPU solve implements the Newtonian branch.  Plastic
+        // viscosity (ivis = 3) is the reference's non-Newtonian case: with
+        // non_Newtonian = 0 its own step does not finish (the CPU restatement
+        // reaches the filter loop cap in energy_time), so it is refused here;
+        // tc_compute_viscosity and tc_stats implement it
+        h->err = "non-Newtonian / plastic viscosity: the GPU multigrid implements the Newtonian branch";
+        return TC_ERR_UNSUPPORTED;
+    }
     const int G = h->grids;
     copy_plane(h, cur_err(h, 1), h->SF);
     launch_rhs1(h->st, h->L1, h->P, h->Tbuoy, h->Cbuoy, h->lev[1].rhs, h->rs, h->ds);
@@ -918,7 +929,7 @@ tc_status create(Handle* h, const tc_params* in) {
     tc_params& p = h->p;
     if (p.order != 2) { h->err = "the GPU path implements order=2"; return TC_ERR_UNSUPPORTED; }
     if (p.gridX != 0 || p.gridZ != 0) { h->err = "the GPU path implements uniform grids"; return TC_ERR_UNSUPPORTED; }
-    if (p.non_Newtonian != 0 || p.ivis == 3) { h->err = "the GPU path implements Newtonian viscosity"; return TC_ERR_UNSUPPORTED; }
+    if (p.ivis < -1 || p.ivis > 3) { h->err = "ivis must be -1..3"; return TC_ERR_ARG; }
     if (p.iterate_order != 1) { h->err = "iterate_order must be 1"; return TC_ERR_UNSUPPORTED; }
     if (p.RaT == 0.0) { h->err = "the GPU path implements thermal or thermochemical convection (RaT != 0)"; return TC_ERR_UNSUPPORTED; }
     if (p.torder != 2 && p.torder != 4) return TC_ERR_UNSUPPORTED;
@@ -979,6 +990,7 @@ tc_status create(Handle* h, const tc_params* in) {
     P.torder = p.torder; P.aspect = p.aspect; P.dr = s1.dr; P.ds = s1.ds; P.dr2 = s1.dr2; P.ds2 = s1.ds2;
     P.dro2 = 0.5 * s1.dr; P.dso2 = 0.5 * s1.ds; P.RaT = p.RaT;
     P.lnvisT = std::log(p.visT); P.lnvisP = std::log(p.visP); P.visT2 = p.visT * p.visT; P.H = p.H;
+    P.visT = p.visT; P.yield = p.yield; P.yield_gradient = p.yield_gradient; P.yield_depth = p.yield_depth;
     for (int t = 0; t < TC_MAX_TYPES; t++) {
         P.RaC[t] = p.RaC[t]; P.lnvisC[t] = (p.visC[t] > 0.0) ? std::log(p.visC[t]) : 0.0; P.Htype[t] = p.Htype[t];
         P.lncf[t] = (p.conduct_factor[t] > 0.0) ? std::log(1.0 / p.conduct_factor[t]) : 0.0;
@@ -1711,6 +1723,27 @@ tc_status tc_tracers_to_corners(tc_handle* H, const double* rtr, const double* s
     launch_perm_gather(h->st, h->ntr, h->perm, h->str1, h->str2);
     TRY(tracers_to_corners(h, h->rtr2, h->str2, true));
     return check_flags(h);
+}
+
+tc_status tc_compute_strain_rate_invariant(tc_handle* H) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    launch_strain(h->st, h->L1, h->P, h->u, h->w, h->strain);
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    return TC_OK;
+}
+
+tc_status tc_compute_viscosity(tc_handle* H, int32_t level) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    if (level < 1 || level > h->grids) return TC_ERR_ARG;
+    TRY(compute_viscosity(h, level));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    return TC_OK;
 }
 
 tc_status tc_tracer_order(tc_handle* H, int32_t* perm) {

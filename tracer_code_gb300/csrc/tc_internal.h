@@ -107,13 +107,14 @@ struct Phys {
     double lncf[TC_MAX_TYPES];   // log(1/conduct_factor)
     double courantT, courantC;
     double Tr_max, Ts_max, Trr_max, Tss_max;  // stability_RK4 scaled bounds (finest grid)
+    double visT, yield, yield_gradient, yield_depth;  // ivis = 3 (plastic)
 };
 
 // ---------------------------------------------------------------------------
 // launchers (k_mg.cu)
 // ---------------------------------------------------------------------------
 void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis, const double* Tvis,
-                        const double* const* Cvis, const double* zg);
+                        const double* const* Cvis, const double* zg, const double* T, const double* strain);
 void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_eig, int ivis, RedScratch rs,
                      DevScalars* ds);
 void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
