@@ -203,6 +203,46 @@ tc_status tc_upload_state(tc_handle* h, const double* T, const double* Cnew,
 tc_status tc_download_state(tc_handle* h, double* T, double* Cnew, double* SF,
                             double* rtr, double* str, int32_t* Ttype);
 
+/* The parameters the handle was created with (nx, nz as passed; tc_info has
+ * the optimized grid). */
+tc_status tc_get_params(const tc_handle* h, tc_params* p);
+
+/* Restart files in the reference's format: one gfortran unformatted
+ * sequential record each (4-byte little-endian length, payload, length;
+ * records of 2^31 bytes or more return TC_ERR_TOO_LARGE, files that do not
+ * hold exactly the expected record return TC_ERR_ARG).
+ *
+ * Trestart (print_restart main.f90:305-320, read by build_grid
+ * grid.f90:56-65): xg(-3:nx+3), zg(-3:nz+3), then T if `thermal` (RaT /= 0),
+ * then Cnew(1:ntype, field box) if ntype > 0 (comp = 1), then SF; T, SF on
+ * (-2:nx+2, -2:nz+2), i fastest.  T and Cnew may be NULL when not written. */
+tc_status tc_restart_write(const char* path, int32_t nx, int32_t nz, int32_t ntype, int32_t thermal,
+                           const double* xg, const double* zg, const double* T, const double* Cnew,
+                           const double* SF);
+tc_status tc_restart_read(const char* path, int32_t nx, int32_t nz, int32_t ntype, int32_t thermal,
+                          double* xg, double* zg, double* T, double* Cnew, double* SF);
+
+/* restart_tracers for compositional tracers with tracer = 0
+ * (main.f90:321-330, grid.f90:74-84): rtr(ntr), str(ntr), Ttype(ntr). */
+tc_status tc_restart_tracers_write(const char* path, int64_t ntr, const double* rtr, const double* str,
+                                   const int32_t* Ttype);
+tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype);
+
+/* build_grid's uniform coordinates with the ghost mirrors and exact end
+ * nodes (grid.f90:46-54, 97-108): xg(-3:nx+3), zg(-3:nz+3). */
+void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg);
+
+/* print_restart for a handle: downloads the state and writes Trestart (and
+ * restart_tracers when comp = 1 and `tracers` is not NULL), the coordinates
+ * from tc_restart_grid. */
+tc_status tc_write_restart(tc_handle* h, const char* trestart, const char* tracers);
+
+/* build_grid's restart branch for a handle: reads Trestart (and
+ * restart_tracers when comp = 1; then `tracers` must not be NULL) and
+ * uploads them with tc_upload_state.  The file's xg, zg are read and
+ * dropped: the GPU path uses the uniform grid of the handle. */
+tc_status tc_read_restart(tc_handle* h, const char* trestart, const char* tracers);
+
 /* Module clock: basics::tstep and basics::time, owned by the host loop. */
 tc_status tc_set_clock(tc_handle* h, int32_t tstep, double time);
 

@@ -14,10 +14,13 @@ Inputs (files of the reference repository):
                          (basics.f90:316-322)
   main.f90               the shipped inputs (parsed for the values the pin
                          needs, so none are typed in by hand)
-Outputs: tests/golden/trestart_200.npz and tests/golden/golden.json.
+Outputs: tests/golden/trestart_200.npz and tests/golden/golden.json (which
+also records the Trestart file's size and sha256, the byte-exact pin of the
+restart writer).
 """
 from __future__ import annotations
 
+import hashlib
 import json
 import os
 import re
@@ -81,6 +84,8 @@ def main(ref: str) -> None:
         "stats_dt": dt_rows[1] - dt_rows[0],
         "stats_rows": len(stats_rows),
         "print_digits": 8,
+        "trestart_bytes": os.path.getsize(os.path.join(ref, "Trestart")),
+        "trestart_sha256": hashlib.sha256(open(os.path.join(ref, "Trestart"), "rb").read()).hexdigest(),
     }
     np.savez_compressed(os.path.join(HERE, "trestart_200.npz"), xg=xg, zg=zg, T=T, SF=SF)
     with open(os.path.join(HERE, "golden.json"), "w") as f:

@@ -17,10 +17,10 @@ import numpy as np
 
 from .abi import (Info, Params, StatsRow, TracerError, config_1024x256, config_2048x512, config_plain_128,
                   default_params, scaled_config)
-from . import state
+from . import restart, state
 
 __all__ = ["Simulation", "Params", "TracerError", "default_params", "config_plain_128", "config_1024x256",
-           "config_2048x512", "scaled_config", "state", "load_library", "library_path"]
+           "config_2048x512", "scaled_config", "state", "restart", "load_library", "library_path"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libtracer_gpu.so")
@@ -33,6 +33,8 @@ EXPORTS = [
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
     "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
     "tc_set_launch_shapes", "tc_tracer_order", "tc_compute_strain_rate_invariant", "tc_compute_viscosity",
+    "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
+    "tc_restart_grid", "tc_write_restart", "tc_read_restart",
 ]
 
 
@@ -84,6 +86,16 @@ def load_library(build_if_missing: bool = False):
         L.tc_tracer_order.argtypes = [vp, vp]
         L.tc_compute_strain_rate_invariant.argtypes = [vp]
         L.tc_compute_viscosity.argtypes = [vp, C.c_int32]
+        L.tc_get_params.argtypes = [vp, C.POINTER(Params)]
+        i32, cs = C.c_int32, C.c_char_p
+        L.tc_restart_write.argtypes = [cs, i32, i32, i32, i32, vp, vp, vp, vp, vp]
+        L.tc_restart_read.argtypes = [cs, i32, i32, i32, i32, vp, vp, vp, vp, vp]
+        L.tc_restart_tracers_write.argtypes = [cs, C.c_int64, vp, vp, vp]
+        L.tc_restart_tracers_read.argtypes = [cs, C.c_int64, vp, vp, vp]
+        L.tc_restart_grid.argtypes = [i32, i32, C.c_double, vp, vp]
+        L.tc_restart_grid.restype = None
+        L.tc_write_restart.argtypes = [vp, cs, cs]
+        L.tc_read_restart.argtypes = [vp, cs, cs]
         L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
@@ -293,3 +305,13 @@ class Simulation:
         out = np.empty(self.field_shape() + (nt,), dtype=np.int32)
         self._chk(self.L.tc_download_counts(self.h, _ptr(out)), "download_counts")
         return out
+
+    def write_restart(self, trestart: str, tracers: str | None = None) -> None:
+        """print_restart (main.f90:301-330): Trestart and, for comp = 1, restart_tracers."""
+        self._chk(self.L.tc_write_restart(self.h, os.fsencode(trestart),
+                                          None if tracers is None else os.fsencode(tracers)), "write_restart")
+
+    def read_restart(self, trestart: str, tracers: str | None = None) -> None:
+        """build_grid's restart branch (grid.f90:55-96) followed by tc_upload_state."""
+        self._chk(self.L.tc_read_restart(self.h, os.fsencode(trestart),
+                                         None if tracers is None else os.fsencode(tracers)), "read_restart")

@@ -1355,6 +1355,12 @@ tc_status tc_get_info(const tc_handle* H, tc_info* info) {
     return TC_OK;
 }
 
+tc_status tc_get_params(const tc_handle* H, tc_params* p) {
+    if (!H || !p) return TC_ERR_ARG;
+    *p = H->h.p;
+    return TC_OK;
+}
+
 tc_status tc_set_stream(tc_handle* H, void* stream) {
     if (!H) return TC_ERR_ARG;
     Handle* h = &H->h;
