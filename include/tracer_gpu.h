@@ -292,7 +292,7 @@ tc_status tc_autotune(tc_handle* h, int32_t* choices);
 /* Applies launch shapes in tc_autotune's `choices` format (3 ints per level
  * 1..grids-1: sweep block x, block y, visit = 0 one launch per sweep / 1
  * default fused visit / 100*P + C / 1000 + n for n sweeps per launch of the
- * tiled smoother, n = 2, or 3 in the mixed solver), e.g. shapes tuned once on
+ * tiled smoother, n = 1..2, or 1..6 in the mixed solver), e.g. shapes tuned once on
  * another handle of the same grid and precision.  TC_ERR_ARG (nothing
  * changed) if a block has more than 256 threads or a visit shape does not fit
  * its level.  Shapes do not change the arithmetic. */
