@@ -228,6 +228,34 @@ tc_status tc_restart_tracers_write(const char* path, int64_t ntr, const double* 
                                    const int32_t* Ttype);
 tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype);
 
+/* The reference's text outputs as gfortran writes them (host only).
+ *
+ * tc_format_g: one real under the edit descriptor Gw.d (e = 0) or Gw.dEe
+ * into out[0..w] (w characters and a NUL); returns w, or -1 for arguments
+ * out of range (w 1..200, d 1..60, e 0..9).
+ *
+ * tc_format_stats_line: the stats.dat row of basics.f90:283-314 for
+ * local_time = 0 (the branches on comp, tracer and RaT = 0 included):
+ * '(12(g20.8))', '(12(g20.8),3(i6))', '(12(g20.8),3(i6),10(g20.8))', ... with
+ * Cavg and ent of types 1..ntype.  tc_format_vis_line: the
+ * viscosity_smoother.dat row of basics.f90:316-322 (empty when RaT = 0 and
+ * comp = 0, where the reference writes none).  Both write a NUL-terminated
+ * line without its newline; TC_ERR_TOO_LARGE if it does not fit in cap. */
+int32_t tc_format_g(double x, int32_t w, int32_t d, int32_t e, char* out);
+tc_status tc_format_stats_line(const tc_stats_row* row, int32_t comp, int32_t tracer, int32_t ntype, double RaT,
+                               char* buf, int32_t cap);
+tc_status tc_format_vis_line(const tc_stats_row* row, int32_t comp, int32_t ntype, double RaT, char* buf,
+                             int32_t cap);
+
+/* snapshots (main.f90:237-270): the T1xxxx file for the handle's current
+ * state, one '(9(g14.5E3),i6,20(g14.5E3))' line per node (xg, zg, T, SF, u,
+ * w, strain, vis, Tvis, nempty, Cnew(1:ntype), Cvis(1:ntype); the comp = 0
+ * and RaT = 0 forms as the reference has them), i outer, k inner, and a
+ * list-directed blank record after each i.  Call it where the reference
+ * calls snapshots: after tc_stats (strain and the level-1 viscosity are
+ * the ones stats used). */
+tc_status tc_write_snapshot(tc_handle* h, const char* path);
+
 /* build_grid's uniform coordinates with the ghost mirrors and exact end
  * nodes (grid.f90:46-54, 97-108): xg(-3:nx+3), zg(-3:nz+3). */
 void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg);
@@ -356,7 +384,7 @@ tc_status tc_download_counts(tc_handle* h, int32_t* count_type);
  * by the parity tests).  `name` is a reference array name: T, SF, Tvis, Tbuoy,
  * u, w, conduct, conduct_r, conduct_s, Cnew, Cvis, Cbuoy (type >= 1),
  * vis_grid, vis_x, vis_z, vis_xx, vis_zz, vis_xz, dt_stream, ratio, RHS,
- * error, residual, dt_vis (level >= 1), DERr_u, DERr_w, dts_array.  out
+ * error, residual, dt_vis (level >= 1), DERr_u, DERr_w, dts_array, strain.  out
  * receives the level's ghost-padded box (-span:nx_l+span, -span:nz_l+span)
  * in Fortran order; entries outside the reference array's own bounds are
  * unspecified. */

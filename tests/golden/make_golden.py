@@ -14,6 +14,9 @@ Inputs (files of the reference repository):
                          (basics.f90:316-322)
   main.f90               the shipped inputs (parsed for the values the pin
                          needs, so none are typed in by hand)
+  equalize.dat           '(g20.8,15(i10))' rows (composition.f90:568-574),
+                         kept verbatim with stats.dat's and
+                         viscosity_smoother.dat's rows for the text formatters
 Outputs: tests/golden/trestart_200.npz and tests/golden/golden.json (which
 also records the Trestart file's size and sha256, the byte-exact pin of the
 restart writer).
@@ -86,6 +89,9 @@ def main(ref: str) -> None:
         "print_digits": 8,
         "trestart_bytes": os.path.getsize(os.path.join(ref, "Trestart")),
         "trestart_sha256": hashlib.sha256(open(os.path.join(ref, "Trestart"), "rb").read()).hexdigest(),
+        # the shipped text rows verbatim (pins of the gfortran-style formatters)
+        "text_lines": {f: [l for l in open(os.path.join(ref, f)).read().split("\n") if l.strip()]
+                       for f in ("stats.dat", "viscosity_smoother.dat", "equalize.dat")},
     }
     np.savez_compressed(os.path.join(HERE, "trestart_200.npz"), xg=xg, zg=zg, T=T, SF=SF)
     with open(os.path.join(HERE, "golden.json"), "w") as f:

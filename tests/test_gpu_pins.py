@@ -3,7 +3,7 @@ pins in test_oracle_pins.py, run through the C ABI on the device): from
 Trestart's T and SF, compute_velocities, compute_strain_rate_invariant,
 compute_viscosity(1) (visf with plastic yielding, ivis = 3, and the level-1
 viscosity filter) and stats reproduce stats.dat's and
-viscosity_smoother.dat's last rows to their 8 printed digits."""
+viscosity_smoother.dat's last rows to their 8 printed digits, and as text."""
 import pytest
 
 from tracer_code_gb300 import Simulation
@@ -16,6 +16,7 @@ pytestmark = pytest.mark.gpu
 def gpu_row(gpu_lib, golden):
     g = Simulation(_pin_params(golden))
     g.upload({"T": golden["T"], "SF": golden["SF"]})
+    g.set_clock(0, float(golden["text_lines"]["stats.dat"][-1][:20]))
     g.compute_velocities()
     g.compute_strain()
     g.compute_viscosity(1)
@@ -36,6 +37,17 @@ def test_gpu_viscosity_smoother_row_matches_reference(gpu_row, golden):
     assert gpu_row["n_eta"] == ref["n_eta"]
     assert gpu_row["n_temp"] == ref["n_temp"]
     assert _rel(gpu_row["eig_fine"], ref["eig_fine"]) < 6e-8
+
+
+def test_gpu_rows_are_the_reference_text(gpu_row, golden):
+    """Written with the reference's formats, the GPU row is the shipped text:
+    stats.dat's twelve g20.8 fields (the tracer counts need restart_tracers,
+    which is not shipped) and viscosity_smoother.dat's whole row."""
+    from tracer_code_gb300 import textio
+    RaT = golden["inputs"]["RaT"]
+    line = golden["text_lines"]["stats.dat"][-1]
+    assert textio.stats_line(gpu_row, 0, 1, 0, RaT)[:240] == line[:240]
+    assert textio.vis_line(gpu_row, 0, 0, RaT) == golden["text_lines"]["viscosity_smoother.dat"][-1]
 
 
 def test_plastic_multigrid_is_reported_unsupported(gpu_lib, golden):

@@ -85,3 +85,22 @@ def test_restart_streamfunction_passes_reference_convergence_test(pinned, golden
     bad = o.residual(1, from_sf=True)
     assert bad / ref > 5 * tol
     o.set("SF", golden["SF"])
+
+
+def test_stats_and_viscosity_lines_match_reference_text(pinned, golden):
+    """The recomputed row, written with the reference's formats
+    (tc_format_stats_line / tc_format_vis_line), is the shipped text: the
+    twelve g20.8 fields of stats.dat's last row (its three tracer counts need
+    restart_tracers, which is not shipped) and the whole last row of
+    viscosity_smoother.dat."""
+    from tracer_code_gb300 import build as tcbuild
+    tcbuild.build()
+    from tracer_code_gb300 import textio
+    line = golden["text_lines"]["stats.dat"][-1]
+    row = pinned.stats()
+    row["time"] = float(line[:20])
+    assert textio.stats_line(row, 0, 1, 0, golden["inputs"]["RaT"])[:240] == line[:240]
+    sc = pinned.scalars()
+    vl = golden["text_lines"]["viscosity_smoother.dat"][-1]
+    r2 = {"time": float(vl[:20]), "n_eta": int(sc["n_eta"]), "eig_fine": sc["eig_fine"], "n_temp": int(sc["n_temp"])}
+    assert textio.vis_line(r2, 0, 0, golden["inputs"]["RaT"]) == vl

@@ -17,10 +17,10 @@ import numpy as np
 
 from .abi import (Info, Params, StatsRow, TracerError, config_1024x256, config_2048x512, config_plain_128,
                   default_params, scaled_config)
-from . import restart, state
+from . import restart, state, textio
 
 __all__ = ["Simulation", "Params", "TracerError", "default_params", "config_plain_128", "config_1024x256",
-           "config_2048x512", "scaled_config", "state", "restart", "load_library", "library_path"]
+           "config_2048x512", "scaled_config", "state", "restart", "textio", "load_library", "library_path"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "libtracer_gpu.so")
@@ -34,7 +34,8 @@ EXPORTS = [
     "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
     "tc_set_launch_shapes", "tc_tracer_order", "tc_compute_strain_rate_invariant", "tc_compute_viscosity",
     "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
-    "tc_restart_grid", "tc_write_restart", "tc_read_restart",
+    "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
+    "tc_format_vis_line", "tc_write_snapshot",
 ]
 
 
@@ -96,6 +97,11 @@ def load_library(build_if_missing: bool = False):
         L.tc_restart_grid.restype = None
         L.tc_write_restart.argtypes = [vp, cs, cs]
         L.tc_read_restart.argtypes = [vp, cs, cs]
+        L.tc_format_g.argtypes = [C.c_double, i32, i32, i32, C.c_char_p]
+        L.tc_format_g.restype = i32
+        L.tc_format_stats_line.argtypes = [C.POINTER(StatsRow), i32, i32, i32, C.c_double, C.c_char_p, i32]
+        L.tc_format_vis_line.argtypes = [C.POINTER(StatsRow), i32, i32, C.c_double, C.c_char_p, i32]
+        L.tc_write_snapshot.argtypes = [vp, cs]
         L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
@@ -315,3 +321,7 @@ class Simulation:
         """build_grid's restart branch (grid.f90:55-96) followed by tc_upload_state."""
         self._chk(self.L.tc_read_restart(self.h, os.fsencode(trestart),
                                          None if tracers is None else os.fsencode(tracers)), "read_restart")
+
+    def write_snapshot(self, path: str) -> None:
+        """snapshots (main.f90:237-270): the T1xxxx text file of the current state (call after stats)."""
+        self._chk(self.L.tc_write_snapshot(self.h, os.fsencode(path)), "write_snapshot")

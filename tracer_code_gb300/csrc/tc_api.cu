@@ -1812,6 +1812,7 @@ tc_status tc_debug_field(tc_handle* H, const char* name, int32_t level, int32_t 
         else if (n == "DERr_u") src = h->du;
         else if (n == "DERr_w") src = h->dw;
         else if (n == "dts_array") src = h->dts;
+        else if (n == "strain") src = h->strain;
         else if (n == "Cnew") src = ty(h->Cnew);
         else if (n == "Cvis") src = ty(h->Cvis);
         else if (n == "Cbuoy") src = ty(h->Cbuoy);
