@@ -43,7 +43,7 @@ extern "C" {
 #endif
 
 #define TC_MAX_TYPES 4
-#define TC_ABI_VERSION 2
+#define TC_ABI_VERSION 3
 
 /* Status codes.  Each reference `stop` site has its own code. */
 typedef enum tc_status {
@@ -67,7 +67,7 @@ typedef enum tc_status {
 /*
  * Inputs of main.f90:8-116 that the hot path reads.  Field names follow the
  * reference.  Fixed by this implementation (not parameters): Database=2,
- * iterate=1, local_time=0, tracer=0, equalize=0 (see tc_create).
+ * iterate=1, local_time=0, equalize=0 (see tc_create).
  */
 typedef struct tc_params {
     /* grid options (main.f90:9-21) */
@@ -146,6 +146,11 @@ typedef struct tc_params {
      * depend on it; every host-facing call keeps the reference's tracer
      * order.  Default 10. */
     int32_t tracer_sort_interval;
+    /* Temperature tracers (main.f90:56): 0 = T is a grid field advanced by
+     * energy_space; 1 = T is carried by the tracers (Ttr, Lagrangian
+     * conduction + heating by tracer_space, energy.f90:82-115) and the grid
+     * T is their per-volume mean (Tratio).  Works with comp = 0 or 1. */
+    int32_t tracer;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
@@ -203,6 +208,21 @@ tc_status tc_upload_state(tc_handle* h, const double* T, const double* Cnew,
 tc_status tc_download_state(tc_handle* h, double* T, double* Cnew, double* SF,
                             double* rtr, double* str, int32_t* Ttype);
 
+/* tc_upload_state with the tracers' temperatures Ttr(1:ntr), required when
+ * tracer = 1 (tc_upload_state then returns TC_ERR_ARG): build_grid's
+ * restart branch reads rtr, str[, Ttype], Ttr (grid.f90:74-84) and
+ * tracers_to_corners(rtr, str, Ttr, T) with smoothing off sets Tratio (the
+ * per-volume tracer mean; empty volumes keep T).  Ttype may be NULL when
+ * comp = 0 (all tracers ambient).  The per-volume sums of Ttr are exact
+ * (128-bit fixed point, rounded once), so Tratio does not depend on the
+ * order the tracers are summed in; the reference's FP64 sums depend on its
+ * OpenMP thread count and differ from it by a few ulps. */
+tc_status tc_upload_state_ex(tc_handle* h, const double* T, const double* Cnew, const double* SF,
+                             const double* rtr, const double* str, const int32_t* Ttype,
+                             const double* Ttr, int64_t ntr);
+/* Ttr(1:ntr) in the reference's tracer order (tracer = 1; TC_ERR_ARG otherwise). */
+tc_status tc_download_tracer_temperature(tc_handle* h, double* Ttr);
+
 /* The parameters the handle was created with (nx, nz as passed; tc_info has
  * the optimized grid). */
 tc_status tc_get_params(const tc_handle* h, tc_params* p);
@@ -222,11 +242,13 @@ tc_status tc_restart_write(const char* path, int32_t nx, int32_t nz, int32_t nty
 tc_status tc_restart_read(const char* path, int32_t nx, int32_t nz, int32_t ntype, int32_t thermal,
                           double* xg, double* zg, double* T, double* Cnew, double* SF);
 
-/* restart_tracers for compositional tracers with tracer = 0
- * (main.f90:321-330, grid.f90:74-84): rtr(ntr), str(ntr), Ttype(ntr). */
+/* restart_tracers (main.f90:321-330, grid.f90:74-84): rtr(ntr), str(ntr),
+ * then Ttype(ntr) when Ttype is not NULL (comp = 1) and Ttr(ntr) when Ttr
+ * is not NULL (tracer = 1); at least one of the two. */
 tc_status tc_restart_tracers_write(const char* path, int64_t ntr, const double* rtr, const double* str,
-                                   const int32_t* Ttype);
-tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype);
+                                   const int32_t* Ttype, const double* Ttr);
+tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype,
+                                  double* Ttr);
 
 /* The reference's text outputs as gfortran writes them (host only).
  *
@@ -261,13 +283,13 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path);
 void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg);
 
 /* print_restart for a handle: downloads the state and writes Trestart (and
- * restart_tracers when comp = 1 and `tracers` is not NULL), the coordinates
- * from tc_restart_grid. */
+ * restart_tracers when comp = 1 or tracer = 1 and `tracers` is not NULL),
+ * the coordinates from tc_restart_grid. */
 tc_status tc_write_restart(tc_handle* h, const char* trestart, const char* tracers);
 
 /* build_grid's restart branch for a handle: reads Trestart (and
- * restart_tracers when comp = 1; then `tracers` must not be NULL) and
- * uploads them with tc_upload_state.  The file's xg, zg are read and
+ * restart_tracers when comp = 1 or tracer = 1; then `tracers` must not be
+ * NULL) and uploads them with tc_upload_state_ex.  The file's xg, zg are read and
  * dropped: the GPU path uses the uniform grid of the handle. */
 tc_status tc_read_restart(tc_handle* h, const char* trestart, const char* tracers);
 
@@ -300,7 +322,9 @@ tc_status tc_step(tc_handle* h, tc_stats_row* row, int32_t* cycles, double* dt_o
  * Ttype in, runs tc_step, copies T, Cnew, SF, rtr, str back.  The arrays
  * must hold the state the previous call (or tc_download_state) returned;
  * after changing them, call tc_upload_state instead.  Any of row, cycles,
- * dt_out may be NULL.  No counterpart in the reference beyond tc_step. */
+ * dt_out may be NULL.  No counterpart in the reference beyond tc_step.
+ * Temperature tracers (tracer = 1) are refused (TC_ERR_UNSUPPORTED): Ttr is
+ * not among the arrays; step with tc_step and download Ttr instead. */
 tc_status tc_step_host(tc_handle* h, double* T, double* Cnew, double* SF, double* rtr, double* str,
                        const int32_t* Ttype, int64_t ntr, tc_stats_row* row, int32_t* cycles, double* dt_out);
 
@@ -384,7 +408,8 @@ tc_status tc_download_counts(tc_handle* h, int32_t* count_type);
  * by the parity tests).  `name` is a reference array name: T, SF, Tvis, Tbuoy,
  * u, w, conduct, conduct_r, conduct_s, Cnew, Cvis, Cbuoy (type >= 1),
  * vis_grid, vis_x, vis_z, vis_xx, vis_zz, vis_xz, dt_stream, ratio, RHS,
- * error, residual, dt_vis (level >= 1), DERr_u, DERr_w, dts_array, strain.  out
+ * error, residual, dt_vis (level >= 1), DERr_u, DERr_w, dts_array, strain,
+ * Tratio, tracer_space_array (tracer = 1).  out
  * receives the level's ghost-padded box (-span:nx_l+span, -span:nz_l+span)
  * in Fortran order; entries outside the reference array's own bounds are
  * unspecified. */

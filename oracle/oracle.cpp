@@ -14,7 +14,9 @@
 //   momentum.f90:1-76,532-551         visf, strain rate, compute_velocities
 //   composition.f90:669-998           tracers_to_corners, BCs, interpolate,
 //                                     compute_derivatives
-//   energy.f90 (all, tracer=0 branches) energy_time, energy_space, stability
+//   energy.f90 (all)                  energy_time (field T and temperature
+//                                     tracers), energy_space, tracer_space,
+//                                     extendT, stability
 //   basics.f90:112-418, grid.f90, main.f90:350-469 (FD_coefficients)
 //
 // The reference cannot be compiled here (it is Fortran and no Fortran
@@ -87,6 +89,30 @@ struct V1 {
 
 inline double sq(double x) { return x * x; }  // x**2.d0 folds to x*x in gfortran
 
+// Exact per-volume tracer temperature sums: x -> round-toward-zero(x * 2^64)
+// as a 128-bit integer, from the IEEE-754 fields (|x| >= 2^62 saturates,
+// NaN and values below 2^-64 count as 0); the sum back to double, rounded
+// to nearest once.  The GPU library computes the same integers.
+inline __int128 tracer_fixq(double x) {
+    uint64_t b;
+    std::memcpy(&b, &x, 8);
+    const int E = (int)((b >> 52) & 0x7ff);
+    if (E == 0x7ff && (b & 0xfffffffffffffULL)) return 0;  // NaN
+    const bool neg = (b >> 63) != 0;
+    unsigned __int128 v;
+    if (E == 0) v = 0;  // zero and subnormals: below 2^-64
+    else {
+        const uint64_t m = (b & 0xfffffffffffffULL) | (1ULL << 52);  // |x| = m * 2^(E-1075)
+        const int sh = E - 1011;                                   // |x| * 2^64 = m * 2^sh
+        if (sh > 73 || E == 0x7ff) v = (unsigned __int128)1 << 126;  // |x| >= 2^62
+        else if (sh >= 0) v = (unsigned __int128)m << sh;
+        else if (sh > -53) v = (unsigned __int128)(m >> (-sh));
+        else v = 0;
+    }
+    return neg ? -(__int128)v : (__int128)v;
+}
+inline double tracer_fixd(__int128 S) { return std::ldexp((double)S, -64); }
+
 // Scaled derivative eigenvalue bounds (module globals Tr_max ... Trrss_max).
 struct EigMax {
     double Tr, Trr, Trrr, Trrrr, Ts, Tss, Tsss, Tssss, Trs, Trrs, Trss, Trrss;
@@ -134,6 +160,11 @@ struct Oracle {
     std::vector<IArr> count_type;  // 0..ntype
     IArr nempty;
     std::vector<Arr> DERr_u, DERr_w;  // per derivative j=1..order-1 : (0:nx, -si:nz+si)
+    // temperature tracers (tracer = 1)
+    int tracer = 0;
+    std::vector<double> Ttr, Ttr0, Ttr1, Ttr2;
+    Arr Tratio, Textend, tsa;  // tsa = tracer_space_array (-si:nx+si, -si:nz+si)
+    std::vector<Arr> DERr_tracer;
     // module state
     double time = 0, dt = 0;
     int tstep = 0, kent = 0;
@@ -245,7 +276,7 @@ struct Oracle {
         Ax = std::pow(std::atan(p.spaceX * 0.5) - std::atan(p.spaceX * (-0.5)), -1.0);
         Az = std::pow(std::atan(p.spaceZ * 0.5) - std::atan(p.spaceZ * (-0.5)), -1.0);
         compute_factorials();
-        ntr = (p.comp == 1) ? (long)(nx + 1) * (nz + 1) * p.tpc : 0;
+        ntr = (p.comp == 1 || p.tracer == 1) ? (long)(nx + 1) * (nz + 1) * p.tpc : 0;
         dist_r = p.dist_factor * dr;
         dist_s = p.dist_factor * ds;
         nx_grid.assign(grids + 1, 0); nz_grid.assign(grids + 1, 0);
@@ -286,7 +317,7 @@ struct Oracle {
             Cnew[t].alloc(-s, nx + s, -s, nz + s); Cvis[t].alloc(-s, nx + s, -s, nz + s);
             Cbuoy[t].alloc(-s, nx + s, -s, nz + s);
         }
-        if (p.comp == 1) {
+        if (p.comp == 1 || p.tracer == 1) {
             count_type.assign(ntype + 1, IArr());
             for (int t = 0; t <= ntype; t++) count_type[t].alloc(-s, nx + s, -s, nz + s);
             nempty.alloc(-s, nx + s, -s, nz + s);
@@ -297,6 +328,15 @@ struct Oracle {
             DERr_u.assign(order, Arr()); DERr_w.assign(order, Arr());
             for (int j = 1; j <= order - 1; j++) {
                 DERr_u[j].alloc(0, nx, -si, nz + si); DERr_w[j].alloc(0, nx, -si, nz + si);
+            }
+            if (p.tracer == 1) {
+                Ttr.assign(ntr, 0); Ttr0.assign(ntr, 0); Ttr1.assign(ntr, 0);
+                if (p.torder > 2) Ttr2.assign(ntr, 0);
+                Tratio.alloc(-s, nx + s, -s, nz + s);
+                Textend.alloc(-spanT, nx + spanT, -spanT, nz + spanT);
+                tsa.alloc(-si, nx + si, -si, nz + si);
+                DERr_tracer.assign(order, Arr());
+                for (int j = 1; j <= order - 1; j++) DERr_tracer[j].alloc(0, nx, -si, nz + si);
             }
         }
         dt_vis.assign(grids + 1, Arr());
@@ -572,11 +612,13 @@ struct Oracle {
         if (p.order != 2 && p.order != 4) return TC_ERR_UNSUPPORTED;
         if (p.grids < 2 || p.grids > 6) return TC_ERR_ARG;
         if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
+        if (p.tracer != 0 && p.tracer != 1) return TC_ERR_ARG;
         if (p.iterate_order != 1) return TC_ERR_UNSUPPORTED;
         if (p.torder != 2 && p.torder != 4) return TC_ERR_UNSUPPORTED;
         order = p.order;
         nx = p.nx; nz = p.nz; grids = p.grids;
         comp = p.comp;
+        tracer = p.tracer;
         compute_smoothing_parameters();
         multigrid_setup();
         compute_basics();
@@ -1530,8 +1572,14 @@ struct Oracle {
         }
         return fin;
     }
-    // tracers_to_corners (composition.f90:669-790), comp=1, tracer=0
-    int tracers_to_corners(const std::vector<double>& rr, const std::vector<double>& ss) {
+    // tracers_to_corners (composition.f90:669-790).  With temperature tracers
+    // (Tt != nullptr) the per-volume sums of Ttr are exact: every Ttr enters
+    // as a 128-bit fixed-point integer (tracer_fixq) and the sum is rounded
+    // once (tracer_fixd), so the result does not depend on the summation
+    // order (the reference's depends on its OpenMP thread count).
+    int tracers_to_corners(const std::vector<double>& rr, const std::vector<double>& ss, const double* Tt = nullptr,
+                           const Arr* T0 = nullptr) {
+        if (Tt) Tratio = *T0;  // empty volumes keep T0
         for (int t = 0; t <= ntype; t++) count_type[t].fill(0);
         int nth = 1;
 #ifdef _OPENMP
@@ -1558,6 +1606,15 @@ struct Oracle {
             }
         }
         if (bad) return TC_ERR_TRACER_OUTSIDE;
+        std::vector<__int128> tsum;
+        if (Tt) {
+            tsum.assign((size_t)(nx + 1) * (nz + 1), 0);
+            for (long id = 0; id < ntr; id++) {
+                int i = (int)std::lround(rr[id] / dr);
+                int k = (int)std::lround(ss[id] / ds);
+                tsum[(size_t)i + (size_t)k * (nx + 1)] += tracer_fixq(Tt[id]);
+            }
+        }
         for (int r = 0; r < nth; r++)
             for (int t = 0; t <= ntype; t++) {
                 int* src = &work[((size_t)r * (ntype + 1) + t) * plane];
@@ -1587,11 +1644,52 @@ struct Oracle {
                         else if (ct == 0) C = 0.0;
                         else C = (double)ct / (double)ne;
                     }
+                if (Tt && ne > 0) Tratio(i, k) = tracer_fixd(tsum[(size_t)i + (size_t)k * (nx + 1)]) / (double)ne;
             }
-        for (int t = 0; t < ntype; t++) enforceBCs_comp(Cnew[t]);
-        if (smooth_vis == 1) { int st = smoother_time(); if (st) return st; }
+        if (comp == 1) {
+            for (int t = 0; t < ntype; t++) enforceBCs_comp(Cnew[t]);
+            if (smooth_vis == 1) { int st = smoother_time(); if (st) return st; }
+        }
+        if (Tt) {
+            enforceBCs(Tratio);
+            if (smooth_vis == 1) { int st = smoother_time_T(Tratio); if (st) return st; }
+        }
         load_conductivity_array();
         return TC_OK;
+    }
+
+    // extendT (energy.f90:478-499): Textend for the tracers' conduction term
+    void extendT(const Arr& T0) {
+        for (int i = 0; i <= nx; i++)
+            for (int k = 0; k <= nz; k++) Textend(i, k) = T0(i, k);
+        for (int i = 1; i <= spanT; i++)
+            for (int k = 0; k <= nz; k++) { Textend(-i, k) = Textend(i, k); Textend(nx + i, k) = Textend(nx - i, k); }
+        for (int k = 1; k <= spanT; k++)
+            for (int i = -spanT; i <= nx + spanT; i++) {
+                if (p.Tbot == 0) Textend(i, -k) = -(Textend(i, k) - 1.0) + 1.0;
+                else if (p.Tbot == 1) Textend(i, -k) = Textend(i, k);
+                Textend(i, nz + k) = -Textend(i, nz - k);
+            }
+        if (p.Tbot == 0)
+            for (int i = -spanT; i <= nx + spanT; i++) Textend(i, 0) = 1.0;
+        for (int i = -spanT; i <= nx + spanT; i++) Textend(i, nz) = 0.0;
+    }
+    // tracer_space (energy.f90:82-100): energy_space without advection, on Textend
+    double tracer_space(int i, int k) const {
+        double Tr = dotx(D1, span1, Textend, i, k) / dr, Ts = dotz(D1, span1, Textend, i, k) / ds;
+        double Trr = dotx(D2, span1, Textend, i, k) / dr2, Tss = dotz(D2, span1, Textend, i, k) / ds2;
+        double kx = conduct_r(i, k) / xr(i), kz = conduct_s(i, k) / zs(k);
+        double Tx = Tr / xr(i), Tz = Ts / zs(k);
+        double Txx = (Trr - Tx * xrr(i)) / sq(xr(i));
+        double Tzz = (Tss - Tz * zss(k)) / sq(zs(k));
+        return conduct(i, k) * (Txx + Tzz) + (kx * Tx + kz * Tz) + heating(i, k);
+    }
+    // load_tracer_space_array (energy.f90:102-115) + compute_derivatives of it
+    void load_tracer_space_array() {
+        extendT(Tratio);
+        for (int i = -span_interp; i <= nx + span_interp; i++)
+            for (int k = -span_interp; k <= nz + span_interp; k++) tsa(i, k) = tracer_space(i, k);
+        compute_derivatives(tsa, DERr_tracer);
     }
 
     // =====================================================================
@@ -1660,40 +1758,58 @@ struct Oracle {
                 else { T(i, k) = T(i, k) + 2.0 * temp; Tout(i, k) = T0(i, k) + factor * temp; }
             }
     }
-    // energy_time (energy.f90:117-453) for comp=1 or 0, tracer=0, local_time=0, equalize=0.
+    // energy_time (energy.f90:117-453) for comp = 0 or 1, tracer = 0 or 1,
+    // local_time = 0, equalize = 0.
     int energy_time() {
         int st = stability_RK4();
         if (st) return st;
         std::vector<Arr> C0 = Cnew;
-        Arr T0 = T, T1 = T, T2 = T;
-        bool trc = (comp == 1);
+        const bool tt = (tracer == 1);
+        const bool trc = (comp == 1) || tt;
+        const bool rat = (p.RaT != 0.0);
+        Arr T0 = tt ? Tratio : T;
+        Arr T1 = T, T2 = T;
+        if (tt) Ttr0 = Ttr;
         if (trc) { rtr0 = rtr; str0 = str; }
+        auto derivs = [&]() { compute_derivatives(u, DERr_u); compute_derivatives(w, DERr_w); };
+        // tracers_to_corners of a stage with temperature tracers, then tracer_space
+        auto t2c_T = [&](const std::vector<double>& rr, const std::vector<double>& ss, const std::vector<double>& Tt,
+                         bool reset_C) -> int {
+            if (reset_C && comp == 1) Cnew = C0;
+            int s2 = tracers_to_corners(rr, ss, Tt.data(), &T0);
+            if (s2) return s2;
+            load_tracer_space_array();
+            return TC_OK;
+        };
         // ---- stage 1 ----
-        if (p.RaT != 0.0) {
-            energy_stage(T0, 1, 0.5 * dt, T0, T1);
-            enforceBCs(T1);
+        if (rat) {
+            if (tt) load_tracer_space_array();
+            else { energy_stage(T0, 1, 0.5 * dt, T0, T1); enforceBCs(T1); }
         }
         if (trc) {
-            compute_derivatives(u, DERr_u);
-            compute_derivatives(w, DERr_w);
+            derivs();
             double dtstage = (p.torder == 2) ? dt : 0.5 * dt;
 #pragma omp parallel for schedule(static)
             for (long id = 0; id < ntr; id++) {
                 double tr = interpolate(rtr0[id], str0[id], DERr_u, u);
                 double ts = interpolate(rtr0[id], str0[id], DERr_w, w);
                 rtr[id] = tr; str[id] = ts;
+                double tT = 0.0;
+                if (tt) { tT = interpolate(rtr0[id], str0[id], DERr_tracer, tsa); Ttr[id] = tT; }
                 rtr1[id] = rtr0[id] + dtstage * tr;
                 str1[id] = str0[id] + dtstage * ts;
+                if (tt) Ttr1[id] = Ttr0[id] + dtstage * tT;
             }
         }
         // ---- stage 2 ----
+        if (tt) { st = t2c_T(rtr1, str1, Ttr1, false); if (st) return st; }
         if (p.RK_update == 1) {
-            if (trc) { st = tracers_to_corners(rtr1, str1); if (st) return st; }
-            st = smoother_time_T(T1); if (st) return st;
+            if (comp == 1 && !tt) { st = tracers_to_corners(rtr1, str1); if (st) return st; }
+            if (!tt) { st = smoother_time_T(T1); if (st) return st; }
             st = update_velocities(); if (st) return st;
-            if (trc) { compute_derivatives(u, DERr_u); compute_derivatives(w, DERr_w); }
+            if (trc) derivs();
         }
-        if (p.RaT != 0.0) {
+        if (rat && !tt) {
             energy_stage(T1, 2, 0.5 * dt, T0, T2);
             enforceBCs(T2);
         }
@@ -1703,26 +1819,32 @@ struct Oracle {
             for (long id = 0; id < ntr; id++) {
                 double tr = interpolate(rtr1[id], str1[id], DERr_u, u);
                 double ts = interpolate(rtr1[id], str1[id], DERr_w, w);
+                double tT = tt ? interpolate(rtr1[id], str1[id], DERr_tracer, tsa) : 0.0;
                 if (p.torder == 2) {
                     rtr[id] = rtr[id] + tr; str[id] = str[id] + ts;
+                    if (tt) Ttr[id] = Ttr[id] + tT;
                     rtr[id] = rtr0[id] + dtstage * rtr[id];
                     str[id] = str0[id] + dtstage * str[id];
+                    if (tt) Ttr[id] = Ttr0[id] + dtstage * Ttr[id];
                 } else {
                     rtr[id] = rtr[id] + 2.0 * tr; str[id] = str[id] + 2.0 * ts;
+                    if (tt) Ttr[id] = Ttr[id] + 2.0 * tT;
                     rtr2[id] = rtr0[id] + dtstage * tr;
                     str2[id] = str0[id] + dtstage * ts;
+                    if (tt) Ttr2[id] = Ttr0[id] + dtstage * tT;
                 }
             }
         }
         if (p.torder >= 3) {
             // ---- stage 3 ----
+            if (tt) { st = t2c_T(rtr2, str2, Ttr2, true); if (st) return st; }
             if (p.RK_update == 1) {
-                if (trc) { Cnew = C0; st = tracers_to_corners(rtr2, str2); if (st) return st; }
-                st = smoother_time_T(T2); if (st) return st;
+                if (comp == 1 && !tt) { Cnew = C0; st = tracers_to_corners(rtr2, str2); if (st) return st; }
+                if (!tt) { st = smoother_time_T(T2); if (st) return st; }
                 st = update_velocities(); if (st) return st;
-                if (trc) { compute_derivatives(u, DERr_u); compute_derivatives(w, DERr_w); }
+                if (trc) derivs();
             }
-            if (p.RaT != 0.0) {
+            if (rat && !tt) {
                 energy_stage(T2, 3, dt, T0, T1);
                 enforceBCs(T1);
             }
@@ -1736,16 +1858,22 @@ struct Oracle {
                     double ts = interpolate(rtr2[id], str2[id], DERr_w, w);
                     str[id] = str[id] + 2.0 * ts;
                     str1[id] = str0[id] + dtt * ts;
+                    if (tt) {
+                        double tT = interpolate(rtr2[id], str2[id], DERr_tracer, tsa);
+                        Ttr[id] = Ttr[id] + 2.0 * tT;
+                        Ttr1[id] = Ttr0[id] + dtt * tT;
+                    }
                 }
             }
             // ---- stage 4 ----
+            if (tt) { st = t2c_T(rtr1, str1, Ttr1, true); if (st) return st; }
             if (p.RK_update == 1) {
-                if (trc) { Cnew = C0; st = tracers_to_corners(rtr1, str1); if (st) return st; }
-                st = smoother_time_T(T1); if (st) return st;
+                if (comp == 1 && !tt) { Cnew = C0; st = tracers_to_corners(rtr1, str1); if (st) return st; }
+                if (!tt) { st = smoother_time_T(T1); if (st) return st; }
                 st = update_velocities(); if (st) return st;
-                if (trc) { compute_derivatives(u, DERr_u); compute_derivatives(w, DERr_w); }
+                if (trc) derivs();
             }
-            if (p.RaT != 0.0) {
+            if (rat && !tt) {
                 energy_stage(T1, 4, dt / 6.0, T0, T1);
                 enforceBCs(T);
             }
@@ -1757,12 +1885,18 @@ struct Oracle {
                     rtr[id] = rtr0[id] + dto6 * (rtr[id] + tr);
                     double ts = interpolate(rtr1[id], str1[id], DERr_w, w);
                     str[id] = str0[id] + dto6 * (str[id] + ts);
+                    if (tt) {
+                        double tT = interpolate(rtr1[id], str1[id], DERr_tracer, tsa);
+                        Ttr[id] = Ttr0[id] + dto6 * (Ttr[id] + tT);
+                    }
                 }
             }
         }
         // ---- wrap up ----
-        if (trc) { Cnew = C0; st = tracers_to_corners(rtr, str); if (st) return st; }
-        st = smoother_time_T(T); if (st) return st;
+        if (comp == 1) Cnew = C0;
+        if (trc) { st = tracers_to_corners(rtr, str, tt ? Ttr.data() : nullptr, &T0); if (st) return st; }
+        if (tt) T = Tratio;
+        else { st = smoother_time_T(T); if (st) return st; }
         return TC_OK;
     }
 
@@ -1808,6 +1942,8 @@ struct Oracle {
                 double fint = integrate2D([&](int i, int k) { return C(i, k); }, kent);
                 row->ent[t] = fint / p.aspect / mass[t];
             }
+        }
+        if (comp == 1 || tracer == 1) {
             int empty = 0, mn = 1 << 30, mx = -(1 << 30);
             for (int i = 0; i <= nx; i++)
                 for (int k = 0; k <= nz; k++) {
@@ -1850,9 +1986,10 @@ struct Oracle {
     // state I/O
     // =====================================================================
     int upload(const double* Tin, const double* Cin, const double* SFin, const double* rin, const double* sin,
-               const int32_t* tin, long n) {
+               const int32_t* tin, long n, const double* Ttr_in = nullptr) {
         if (!Tin || !SFin) return TC_ERR_ARG;
         if (comp == 1 && (n != ntr || !rin || !sin || !tin)) return TC_ERR_ARG;
+        if (tracer == 1 && (n != ntr || !rin || !sin || !Ttr_in)) return TC_ERR_ARG;
         std::memcpy(T.v.data(), Tin, T.v.size() * sizeof(double));
         std::memcpy(SF.v.data(), SFin, SF.v.size() * sizeof(double));
         size_t plane = T.v.size();
@@ -1865,12 +2002,13 @@ struct Oracle {
         for (int t = 0; t < ntype; t++) enforceBCs_comp(Cnew[t]);
         for (int l = 2; l <= grids; l++) error[l].fill(0.0);
         int st;
-        if (comp == 1) {
+        if (comp == 1 || tracer == 1) {
             std::memcpy(rtr.data(), rin, ntr * sizeof(double));
             std::memcpy(str.data(), sin, ntr * sizeof(double));
-            for (long i = 0; i < ntr; i++) Ttype[i] = tin[i];
+            for (long i = 0; i < ntr; i++) Ttype[i] = (comp == 1) ? tin[i] : 0;
+            if (tracer == 1) std::memcpy(Ttr.data(), Ttr_in, ntr * sizeof(double));
             smooth_vis = 0;
-            st = tracers_to_corners(rtr, str);
+            st = tracers_to_corners(rtr, str, tracer == 1 ? Ttr.data() : nullptr, &T);
             smooth_vis = 1;
             if (st) return st;
         }
@@ -1888,7 +2026,7 @@ struct Oracle {
             for (int t = 0; t < ntype; t++)
                 for (size_t x = 0; x < plane; x++) Cout[x * ntype + t] = Cnew[t].v[x];
         }
-        if (comp == 1) {
+        if (comp == 1 || tracer == 1) {
             if (rout) std::memcpy(rout, rtr.data(), ntr * sizeof(double));
             if (sout) std::memcpy(sout, str.data(), ntr * sizeof(double));
             if (tout) for (long i = 0; i < ntr; i++) tout[i] = Ttype[i];
@@ -1913,6 +2051,9 @@ struct Oracle {
         if (s == "conduct_s") return &conduct_s;
         if (s == "dts_array") return &dts_array;
         if (s == "residual") return &residual;
+        if (s == "Tratio") return tracer == 1 ? &Tratio : nullptr;
+        if (s == "Textend") return tracer == 1 ? &Textend : nullptr;
+        if (s == "tracer_space_array") return tracer == 1 ? &tsa : nullptr;
         if (s == "Cnew") return Ty(Cnew);
         if (s == "Cvis") return Ty(Cvis);
         if (s == "Cbuoy") return Ty(Cbuoy);
@@ -1962,6 +2103,16 @@ int tco_get_info(void* h, tc_info* info) {
 int tco_upload_state(void* h, const double* T, const double* C, const double* SF, const double* r,
                      const double* s, const int32_t* tt, int64_t n) {
     return ((Oracle*)h)->upload(T, C, SF, r, s, tt, (long)n);
+}
+int tco_upload_state_ex(void* h, const double* T, const double* C, const double* SF, const double* r,
+                        const double* s, const int32_t* tt, const double* Ttr, int64_t n) {
+    return ((Oracle*)h)->upload(T, C, SF, r, s, tt, (long)n, Ttr);
+}
+int tco_download_ttr(void* h, double* out) {
+    Oracle* o = (Oracle*)h;
+    if (o->tracer != 1 || !out) return TC_ERR_ARG;
+    std::memcpy(out, o->Ttr.data(), o->ntr * sizeof(double));
+    return TC_OK;
 }
 int tco_download_state(void* h, double* T, double* C, double* SF, double* r, double* s, int32_t* tt) {
     ((Oracle*)h)->download(T, C, SF, r, s, tt);

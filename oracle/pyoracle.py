@@ -46,6 +46,8 @@ def lib():
             L.tco_get_info.argtypes = [vp, C.POINTER(Info)]
             L.tco_upload_state.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64]
             L.tco_download_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+            L.tco_upload_state_ex.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
+            L.tco_download_ttr.argtypes = [vp, vp]
             L.tco_set_clock.argtypes = [vp, C.c_int32, C.c_double]
             L.tco_multigrid.argtypes = [vp, C.POINTER(C.c_int32)]
             L.tco_compute_velocities.argtypes = [vp]
@@ -137,6 +139,11 @@ class Oracle:
         s = None if s is None else np.ascontiguousarray(s, dtype=np.float64)
         t = None if t is None else np.ascontiguousarray(t, dtype=np.int32)
         n = 0 if r is None else r.size
+        if self.params.tracer == 1:
+            tt = np.ascontiguousarray(state["Ttr"], dtype=np.float64)
+            self._chk(self.L.tco_upload_state_ex(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t),
+                                                 _ptr(tt), n), "upload")
+            return
         self._chk(self.L.tco_upload_state(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t), n), "upload")
 
     def download(self) -> dict:
@@ -146,13 +153,19 @@ class Oracle:
         Cn = np.empty(shp + (nt,)) if nt else None
         out = {"T": T, "SF": SF}
         r = s = t = None
-        if self.params.comp == 1:
+        if self.params.comp == 1 or self.params.tracer == 1:
             r = np.empty(self.ntr); s = np.empty(self.ntr); t = np.empty(self.ntr, dtype=np.int32)
         self.L.tco_download_state(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t))
         if nt:
             out["Cnew"] = Cn
         if r is not None:
-            out.update(rtr=r, str=s, Ttype=t)
+            out.update(rtr=r, str=s)
+            if self.params.comp == 1:
+                out["Ttype"] = t
+        if self.params.tracer == 1:
+            tt = np.empty(self.ntr)
+            self._chk(self.L.tco_download_ttr(self.h, _ptr(tt)), "download_ttr")
+            out["Ttr"] = tt
         return out
 
     def set_clock(self, tstep: int, time: float):
@@ -186,7 +199,7 @@ class Oracle:
                                                 np.ascontiguousarray(s, np.float64)), "tracers_to_corners")
 
     def counts(self) -> np.ndarray:
-        nt = self.params.ntype + 1
+        nt = (self.params.ntype if self.params.comp == 1 else 0) + 1
         shp = self.field_shape()
         out = np.empty(shp + (nt,), dtype=np.int32)
         self.L.tco_download_counts(self.h, out.reshape(-1))

@@ -8,8 +8,9 @@ calls through the C ABI: no GPU needed.
   - the reader returns the shipped arrays and refuses files that do not
     hold exactly the expected record;
   - the comp = 1 layouts (Cnew between T and SF, type fastest; no T when
-    RaT = 0; restart_tracers = rtr, str, Ttype) round trip and have the
-    byte layout of one gfortran unformatted record.
+    RaT = 0; restart_tracers = rtr, str, Ttype) and the temperature-tracer
+    layouts (rtr, str[, Ttype], Ttr) round trip and have the byte layout of
+    one gfortran unformatted record.
 """
 import hashlib
 import os
@@ -108,6 +109,19 @@ def test_tracer_file_round_trip(rs, tmp_path):
     assert np.array_equal(d["rtr"], r) and np.array_equal(d["str"], s) and np.array_equal(d["Ttype"], t)
     with pytest.raises(TracerError):
         rs.read_tracers(p, n + 1)
+    # temperature tracers: rtr, str, Ttr (comp = 0) and rtr, str, Ttype, Ttr (comp = 1)
+    Tt = rng.random(n)
+    for with_type in (False, True):
+        rs.write_tracers(p, r, s, t if with_type else None, Tt)
+        b = record(p)
+        assert len(b) == (28 if with_type else 24) * n
+        assert np.array_equal(np.frombuffer(b[-8 * n:], "<f8"), Tt)
+        d = rs.read_tracers(p, n, Ttype=with_type, Ttr=True)
+        assert np.array_equal(d["Ttr"], Tt) and np.array_equal(d["rtr"], r)
+        if with_type:
+            assert np.array_equal(d["Ttype"], t)
+        with pytest.raises(TracerError):
+            rs.read_tracers(p, n, Ttype=not with_type, Ttr=True)
 
 
 def test_damaged_files_are_refused(rs, tmp_path):
@@ -145,8 +159,9 @@ def test_argument_checks(rs, tmp_path):
     assert L.tc_restart_write(q, 8, 4, 1, 1, ptr(xg), ptr(zg), ptr(sf), None, ptr(sf)) == ARG  # Cnew missing
     assert L.tc_restart_write(q, 8, 4, 0, 1, ptr(xg), ptr(zg), None, None, ptr(sf)) == ARG  # T missing
     assert L.tc_restart_write(q, 0, 4, 0, 0, ptr(xg), ptr(zg), None, None, ptr(sf)) == ARG
-    assert L.tc_restart_tracers_write(q, 0, ptr(xg), ptr(xg), None) == ARG
+    assert L.tc_restart_tracers_write(q, 0, ptr(xg), ptr(xg), ptr(xg), None) == ARG
+    assert L.tc_restart_tracers_write(q, 4, ptr(xg), ptr(xg), None, None) == ARG  # neither Ttype nor Ttr
     # a record of 2^31 bytes or more is refused before any array is touched
     big = 1 << 28
-    assert L.tc_restart_tracers_write(q, big, ptr(xg), ptr(xg), ptr(xg)) == TOO_LARGE
+    assert L.tc_restart_tracers_write(q, big, ptr(xg), ptr(xg), ptr(xg), None) == TOO_LARGE
     assert not os.path.exists(tmp_path / "x")

@@ -35,7 +35,7 @@ EXPORTS = [
     "tc_set_launch_shapes", "tc_tracer_order", "tc_compute_strain_rate_invariant", "tc_compute_viscosity",
     "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
     "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
-    "tc_format_vis_line", "tc_write_snapshot",
+    "tc_format_vis_line", "tc_write_snapshot", "tc_upload_state_ex", "tc_download_tracer_temperature",
 ]
 
 
@@ -68,6 +68,8 @@ def load_library(build_if_missing: bool = False):
         L.tc_set_stream.argtypes = [vp, vp]
         L.tc_upload_state.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int64]
         L.tc_download_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+        L.tc_upload_state_ex.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
+        L.tc_download_tracer_temperature.argtypes = [vp, vp]
         L.tc_set_clock.argtypes = [vp, C.c_int32, C.c_double]
         L.tc_multigrid.argtypes = [vp, C.POINTER(C.c_int32)]
         L.tc_compute_velocities.argtypes = [vp]
@@ -91,8 +93,8 @@ def load_library(build_if_missing: bool = False):
         i32, cs = C.c_int32, C.c_char_p
         L.tc_restart_write.argtypes = [cs, i32, i32, i32, i32, vp, vp, vp, vp, vp]
         L.tc_restart_read.argtypes = [cs, i32, i32, i32, i32, vp, vp, vp, vp, vp]
-        L.tc_restart_tracers_write.argtypes = [cs, C.c_int64, vp, vp, vp]
-        L.tc_restart_tracers_read.argtypes = [cs, C.c_int64, vp, vp, vp]
+        L.tc_restart_tracers_write.argtypes = [cs, C.c_int64, vp, vp, vp, vp]
+        L.tc_restart_tracers_read.argtypes = [cs, C.c_int64, vp, vp, vp, vp]
         L.tc_restart_grid.argtypes = [i32, i32, C.c_double, vp, vp]
         L.tc_restart_grid.restype = None
         L.tc_write_restart.argtypes = [vp, cs, cs]
@@ -193,6 +195,11 @@ class Simulation:
         s = None if s is None else np.ascontiguousarray(s, dtype=np.float64)
         t = None if t is None else np.ascontiguousarray(t, dtype=np.int32)
         n = 0 if r is None else r.size
+        if self.params.tracer == 1:
+            tt = np.ascontiguousarray(st["Ttr"], dtype=np.float64)
+            self._chk(self.L.tc_upload_state_ex(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t),
+                                                _ptr(tt), n), "upload")
+            return
         self._chk(self.L.tc_upload_state(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t), n), "upload")
 
     def download(self) -> dict:
@@ -201,15 +208,23 @@ class Simulation:
         nt = self.params.ntype if self.params.comp == 1 else 0
         Cn = np.empty(shp + (nt,)) if nt else None
         r = s = t = None
+        if self.params.comp == 1 or self.params.tracer == 1:
+            r = np.empty(self.ntr); s = np.empty(self.ntr)
         if self.params.comp == 1:
-            r = np.empty(self.ntr); s = np.empty(self.ntr); t = np.empty(self.ntr, dtype=np.int32)
+            t = np.empty(self.ntr, dtype=np.int32)
         self._chk(self.L.tc_download_state(self.h, _ptr(T), _ptr(Cn), _ptr(SF), _ptr(r), _ptr(s), _ptr(t)),
                   "download")
         out = {"T": T, "SF": SF}
         if nt:
             out["Cnew"] = Cn
         if r is not None:
-            out.update(rtr=r, str=s, Ttype=t)
+            out.update(rtr=r, str=s)
+        if t is not None:
+            out["Ttype"] = t
+        if self.params.tracer == 1:
+            tt = np.empty(self.ntr)
+            self._chk(self.L.tc_download_tracer_temperature(self.h, _ptr(tt)), "download_tracer_temperature")
+            out["Ttr"] = tt
         return out
 
     def set_clock(self, tstep: int, time: float):
@@ -307,7 +322,7 @@ class Simulation:
         return out
 
     def counts(self) -> np.ndarray:
-        nt = self.params.ntype + 1
+        nt = (self.params.ntype if self.params.comp == 1 else 0) + 1
         out = np.empty(self.field_shape() + (nt,), dtype=np.int32)
         self._chk(self.L.tc_download_counts(self.h, _ptr(out)), "download_counts")
         return out

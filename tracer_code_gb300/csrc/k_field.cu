@@ -467,7 +467,7 @@ void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const d
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
     k_stats_rows<<<(L.b + 1 + 63) / 64, 64, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows); tc_note_launch();
     k_stats_final<<<1, 32, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds); tc_note_launch();
-    if (P.comp == 1) {
+    if (P.comp == 1 || P.tracer == 1) {
         Range2 r{0, L.a, 0, L.b};
         k_nempty_init<<<1, 1, 0, s>>>(ds); tc_note_launch();
         k_nempty_stats<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, r, nempty, ds); tc_note_launch();

@@ -45,6 +45,16 @@ __device__ __forceinline__ double interp_taylor(const Lay& L, const Phys& P, con
     return fin;
 }
 
+// Temperature tracers (tracer = 1): the tracer_space value at the stage
+// position, interpolated like u and w, drives Ttr the way u drives rtr.
+struct TracerT {
+    const double* f;    // tracer_space_array (nullptr: no temperature tracers)
+    const double* der;  // its r-derivative table
+    const double* T0;   // Ttr0
+    double* acc;        // Ttr
+    double* out;        // Ttr1 / Ttr2 of the stage
+};
+
 // stage 1: (rin,sin)=(rtr0,str0) -> acc=k1, out=rtr1
 // stage 2: (rin,sin)=(rtr1,str1) -> RK2: acc=final rtr;  RK4: acc+=2k2, out=rtr2
 // stage 3: (rin,sin)=(rtr2,str2) -> acc+=2k3, out=rtr1
@@ -54,7 +64,7 @@ __global__ void k_tracer_stage(Lay L, Phys P, int torder, int stage, int64_t ntr
                                const double* __restrict__ s0, double* __restrict__ racc, double* __restrict__ sacc,
                                double* __restrict__ rout, double* __restrict__ sout, const double* __restrict__ u,
                                const double* __restrict__ w, const double* __restrict__ du,
-                               const double* __restrict__ dw, const DevScalars* __restrict__ ds) {
+                               const double* __restrict__ dw, const DevScalars* __restrict__ ds, TracerT tT) {
     int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= ntr) return;
     const double dt = ds->dt;
@@ -64,6 +74,27 @@ __global__ void k_tracer_stage(Lay L, Phys P, int torder, int stage, int64_t ntr
     if (!(r > 0.0 && r < P.aspect && s > 0.0 && s < 1.0)) return;
     const double tr = interp_taylor(L, P, u, du, r, s);
     const double ts = interp_taylor(L, P, w, dw, r, s);
+    if (tT.f) {
+        // energy.f90:213-223, 292-310, 371-375, 437-440
+        const double te = interp_taylor(L, P, tT.f, tT.der, r, s);
+        if (stage == 1) {
+            tT.acc[id] = te;
+            tT.out[id] = tT.T0[id] + ((torder == 2) ? dt : 0.5 * dt) * te;
+        } else if (stage == 2) {
+            if (torder == 2) {
+                const double a = tT.acc[id] + te;
+                tT.acc[id] = tT.T0[id] + (0.5 * dt) * a;
+            } else {
+                tT.acc[id] = tT.acc[id] + 2.0 * te;
+                tT.out[id] = tT.T0[id] + (0.5 * dt) * te;
+            }
+        } else if (stage == 3) {
+            tT.acc[id] = tT.acc[id] + 2.0 * te;
+            tT.out[id] = tT.T0[id] + dt * te;
+        } else {
+            tT.acc[id] = tT.T0[id] + (dt / 6.0) * (tT.acc[id] + te);
+        }
+    }
     if (stage == 1) {
         const double dtstage = (torder == 2) ? dt : 0.5 * dt;
         racc[id] = tr;
@@ -96,18 +127,77 @@ __global__ void k_tracer_stage(Lay L, Phys P, int torder, int stage, int64_t ntr
 void launch_tracer_stage(cudaStream_t s, const Lay& L, const Phys& P, int torder, int stage, int64_t ntr,
                          const double* rin, const double* sin, const double* r0, const double* s0, double* racc,
                          double* sacc, double* rout, double* sout, const double* u, const double* w,
-                         const double* du, const double* dw, const DevScalars* ds) {
+                         const double* du, const double* dw, const DevScalars* ds, const double* tsa,
+                         const double* dT, const double* Ttr0, double* Ttr, double* Tout) {
     if (ntr <= 0) return;
     unsigned nb = (unsigned)((ntr + 255) / 256);
+    const TracerT tT{tsa, dT, Ttr0, Ttr, Tout};
     k_tracer_stage<<<nb, 256, 0, s>>>(L, P, torder, stage, ntr, rin, sin, r0, s0, racc, sacc, rout, sout, u, w, du,
-                                      dw, ds); tc_note_launch();
+                                      dw, ds, tT); tc_note_launch();
+}
+
+// ---- exact per-volume sums of the tracer temperatures ------------------------
+// Each Ttr enters as round-toward-zero(Ttr * 2^64), a 128-bit integer built
+// from the IEEE-754 fields (|Ttr| >= 2^62 saturates, NaN and magnitudes
+// below 2^-64 count as 0); a volume's sum is a 128-bit integer kept as two
+// 64-bit words (the low word's atomic add reports its carry into the high
+// word), so it does not depend on the order the tracers arrive in; it is
+// rounded to double once.  The CPU restatement computes the same integers.
+__device__ __forceinline__ __int128 tracer_fixq(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int E = (int)((b >> 52) & 0x7ff);
+    if (E == 0x7ff && (b & 0xfffffffffffffULL)) return 0;
+    const bool neg = (b >> 63) != 0;
+    unsigned __int128 v;
+    if (E == 0) {
+        v = 0;
+    } else {
+        const unsigned long long m = (b & 0xfffffffffffffULL) | (1ULL << 52);  // |x| = m * 2^(E-1075)
+        const int sh = E - 1011;                                               // |x| * 2^64 = m * 2^sh
+        if (sh > 73 || E == 0x7ff) v = (unsigned __int128)1 << 126;
+        else if (sh >= 0) v = (unsigned __int128)m << sh;
+        else if (sh > -53) v = (unsigned __int128)(m >> (-sh));
+        else v = 0;
+    }
+    return neg ? -(__int128)v : (__int128)v;
+}
+__device__ __forceinline__ void tracer_add128(unsigned long long* lo, unsigned long long* hi, __int128 q) {
+    const unsigned __int128 u = (unsigned __int128)q;
+    const unsigned long long ql = (unsigned long long)u, qh = (unsigned long long)(u >> 64);
+    const unsigned long long old = atomicAdd(lo, ql);
+    const unsigned long long c = qh + ((old + ql < old) ? 1ULL : 0ULL);
+    if (c) atomicAdd(hi, c);
+}
+// the 128-bit sum * 2^-64 rounded to nearest (ties to even)
+__device__ __forceinline__ double tracer_fixd(unsigned long long lo, unsigned long long hi) {
+    const __int128 S = (__int128)(((unsigned __int128)hi << 64) | (unsigned __int128)lo);
+    if (S == 0) return 0.0;
+    const bool neg = S < 0;
+    unsigned __int128 m = neg ? (unsigned __int128)0 - (unsigned __int128)S : (unsigned __int128)S;
+    const unsigned long long mh = (unsigned long long)(m >> 64), ml = (unsigned long long)m;
+    const int nb = mh ? 128 - __clzll((long long)mh) : 64 - __clzll((long long)ml);
+    int e = 0;
+    if (nb > 53) {
+        const int drop = nb - 53;
+        const unsigned __int128 rem = m & (((unsigned __int128)1 << drop) - 1);
+        const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
+        m >>= drop;
+        e = drop;
+        if (rem > half || (rem == half && (m & 1))) {
+            m += 1;
+            if (m >> 53) { m >>= 1; e += 1; }
+        }
+    }
+    const double d = ldexp((double)(unsigned long long)m, e - 64);
+    return neg ? -d : d;
 }
 
 // histogram of tracers_to_corners (composition.f90:695-726): nint() rounds
 // half away from zero (CUDA round()).  Tracers of a warp that land in the
 // same counter are combined before one atomic (they are mostly cell-sorted).
 __global__ void k_histogram(Lay L, Phys P, int64_t ntr, const double* __restrict__ rr, const double* __restrict__ ss,
-                            const int* __restrict__ ttype, int* __restrict__ counts, int* __restrict__ flag) {
+                            const int* __restrict__ ttype, int* __restrict__ counts, int* __restrict__ flag,
+                            const double* __restrict__ Tt, unsigned long long* tlo, unsigned long long* thi) {
     int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     int key = -1;
     if (id < ntr) {
@@ -119,7 +209,10 @@ __global__ void k_histogram(Lay L, Phys P, int64_t ntr, const double* __restrict
             const int k = (int)round(s / P.ds);
             const int t = ttype[id];
             if (t < 0 || t > P.ntype || i < 0 || i > P.nx || k < 0 || k > P.nz) atomicOr(flag, 2);
-            else key = (int)((size_t)t * L.plane + IX(L, i, k));
+            else {
+                key = (int)((size_t)t * L.plane + IX(L, i, k));
+                if (Tt) tracer_add128(tlo + IX(L, i, k), thi + IX(L, i, k), tracer_fixq(Tt[id]));
+            }
         }
     }
     const unsigned act = __activemask();
@@ -128,16 +221,18 @@ __global__ void k_histogram(Lay L, Phys P, int64_t ntr, const double* __restrict
     if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(counts + key, __popc(peers));
 }
 void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* r, const double* sv,
-                      const int* ttype, int* counts, DevScalars* ds) {
+                      const int* ttype, int* counts, DevScalars* ds, const double* Tt, unsigned long long* tsum) {
     cudaMemsetAsync(counts, 0, sizeof(int) * L.plane * (size_t)(P.ntype + 1), s);
+    if (Tt) cudaMemsetAsync(tsum, 0, sizeof(unsigned long long) * 2 * L.plane, s);
     if (ntr <= 0) return;
     unsigned nb = (unsigned)((ntr + 255) / 256);
-    k_histogram<<<nb, 256, 0, s>>>(L, P, ntr, r, sv, ttype, counts, &ds->flag_outside); tc_note_launch();
+    k_histogram<<<nb, 256, 0, s>>>(L, P, ntr, r, sv, ttype, counts, &ds->flag_outside, Tt, Tt ? tsum : nullptr,
+                                   Tt ? tsum + L.plane : nullptr); tc_note_launch();
 }
 
 // ghost mirror of count_type, nempty and the tracer ratio (composition.f90:745-776)
 __global__ void k_counts_to_comp(Lay L, Phys P, Range2 r, int* __restrict__ counts, int* __restrict__ nempty,
-                                 CPtrsW Cn) {
+                                 CPtrsW Cn, const unsigned long long* __restrict__ tsum, double* __restrict__ Tratio) {
     RANGE_IK(r);
     if (!inr) return;
     const int nx = L.a, nz = L.b;
@@ -155,6 +250,7 @@ __global__ void k_counts_to_comp(Lay L, Phys P, Range2 r, int* __restrict__ coun
         ne += c;
     }
     nempty[x] = ne;
+    if (Tratio && inx && inz && ne > 0) Tratio[x] = tracer_fixd(tsum[x], tsum[L.plane + x]) / (double)ne;
     if (inx && inz && ne > 0)
         for (int t = 1; t <= P.ntype; t++) {
             int ct = counts[(size_t)t * L.plane + x];
@@ -166,11 +262,58 @@ __global__ void k_counts_to_comp(Lay L, Phys P, Range2 r, int* __restrict__ coun
         }
 }
 void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* counts, int* nempty,
-                           double* const* Cnew) {
+                           double* const* Cnew, const unsigned long long* tsum, double* Tratio) {
     CPtrsW C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
     Range2 r{-SP, L.a + SP, -SP, L.b + SP};
-    k_counts_to_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, counts, nempty, C); tc_note_launch();
+    k_counts_to_comp<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, counts, nempty, C, tsum, Tratio); tc_note_launch();
+}
+
+// extendT + tracer_space (energy.f90:478-499, 82-115) on (-1:nx+1, -1:nz+1):
+// energy_space without advection, on Tratio extended by extendT's mirrors
+// (antisymmetric about T=1 at the bottom for Tbot=0, symmetric for Tbot=1,
+// antisymmetric about 0 at the top; rows 0 and nz set to 1 and 0 last)
+__device__ __forceinline__ double textend(const Lay& L, const Phys& P, const double* __restrict__ Tr, int i, int k) {
+    const int nx = L.a, nz = L.b;
+    const int ii = (i < 0) ? -i : ((i > nx) ? 2 * nx - i : i);
+    if (k == nz) return 0.0;
+    if (k == 0 && P.Tbot == 0) return 1.0;
+    if (k >= 0 && k < nz) return Tr[IX(L, ii, k)];
+    if (k < 0) {
+        const double v = Tr[IX(L, ii, -k)];
+        return (P.Tbot == 0) ? -(v - 1.0) + 1.0 : v;
+    }
+    return -Tr[IX(L, ii, 2 * nz - k)];
+}
+__global__ void k_tracer_space(Lay L, Phys P, Range2 r, const double* __restrict__ Tr, const double* __restrict__ cd,
+                               const double* __restrict__ cr, const double* __restrict__ cs, CPtrs Cv,
+                               double* __restrict__ out) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    const double c = textend(L, P, Tr, i, k);
+    const double fm = textend(L, P, Tr, i - 1, k), fp = textend(L, P, Tr, i + 1, k);
+    const double gm = textend(L, P, Tr, i, k - 1), gp = textend(L, P, Tr, i, k + 1);
+    const double Trd = (-0.5 * fm + 0.5 * fp) / P.dr;
+    const double Tsd = (-0.5 * gm + 0.5 * gp) / P.ds;
+    const double Trr = (fm + -2.0 * c + fp) / P.dr2;
+    const double Tss = (gm + -2.0 * c + gp) / P.ds2;
+    double heat;
+    if (P.comp == 0) heat = P.H;
+    else {
+        double sC = 0.0;
+        for (int j = 0; j < P.ntype; j++) sC = sC + Cv.p[j][x];
+        heat = P.H * (1.0 - sC);
+        for (int j = 0; j < P.ntype; j++) heat = P.Htype[j] * Cv.p[j][x] + heat;
+    }
+    out[x] = cd[x] * (Trr + Tss) + (cr[x] * Trd + cs[x] * Tsd) + heat;
+}
+void launch_tracer_space(cudaStream_t s, const Lay& L, const Phys& P, const double* Tratio, const double* conduct,
+                         const double* conduct_r, const double* conduct_s, const double* const* Cvis, double* tsa) {
+    CPtrs C{};
+    for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cvis[j];
+    Range2 r{-1, L.a + 1, -1, L.b + 1};
+    k_tracer_space<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Tratio, conduct, conduct_r, conduct_s, C, tsa); tc_note_launch();
 }
 
 // ---- cell sort of the tracer arrays -------------------------------------------
@@ -256,7 +399,8 @@ __global__ void __launch_bounds__(1024) k_scan_final(const int* cnt, int n, cons
 }
 
 __global__ void k_sort_scatter(Lay L, Phys P, int64_t ntr, const double* rr, const double* ss, const int* tt,
-                               const int* perm, int* off, double* r2, double* s2, int* t2, int* p2) {
+                               const int* perm, int* off, double* r2, double* s2, int* t2, int* p2,
+                               const double* Tt, double* T2) {
     const int64_t id = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (id >= ntr) return;
     const double r = ld_state(rr + id), s = ld_state(ss + id);
@@ -265,6 +409,7 @@ __global__ void k_sort_scatter(Lay L, Phys P, int64_t ntr, const double* rr, con
     s2[pos] = s;
     t2[pos] = ld_state(tt + id);
     p2[pos] = ld_state(perm + id);
+    if (Tt) T2[pos] = ld_state(Tt + id);
 }
 
 template <typename T>
@@ -286,7 +431,7 @@ __global__ void k_iota(int64_t n, int* p) {
 // cnt, off: L.plane ints each; bsum: (L.plane + 1023) / 1024 ints
 void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* rr, const double* ss,
                          const int* tt, const int* perm, int* cnt, int* off, int* bsum, double* r2, double* s2,
-                         int* t2, int* p2) {
+                         int* t2, int* p2, const double* Tt, double* T2) {
     if (ntr <= 0) return;
     const int n = (int)L.plane, nb = (n + 1023) / 1024;
     const unsigned tb = (unsigned)((ntr + 255) / 256);
@@ -295,7 +440,7 @@ void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t nt
     k_scan_blocks<<<nb, 1024, 0, s>>>(cnt, n, bsum); tc_note_launch();
     k_scan_bsums<<<1, 1024, 0, s>>>(bsum, nb); tc_note_launch();
     k_scan_final<<<nb, 1024, 0, s>>>(cnt, n, bsum, off); tc_note_launch();
-    k_sort_scatter<<<tb, 256, 0, s>>>(L, P, ntr, rr, ss, tt, perm, off, r2, s2, t2, p2); tc_note_launch();
+    k_sort_scatter<<<tb, 256, 0, s>>>(L, P, ntr, rr, ss, tt, perm, off, r2, s2, t2, p2, Tt, T2); tc_note_launch();
 }
 void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out) {
     if (n <= 0) return;

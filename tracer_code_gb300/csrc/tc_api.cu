@@ -75,6 +75,11 @@ struct Handle {
     double *rtr = nullptr, *str = nullptr, *rtr0 = nullptr, *str0 = nullptr, *rtr1 = nullptr, *str1 = nullptr,
            *rtr2 = nullptr, *str2 = nullptr;
     int* ttype = nullptr;
+    // temperature tracers (tracer = 1): Ttr and its RK copies, the per-volume
+    // mean Tratio, tracer_space_array and its r-derivatives, the exact sums
+    double *Ttr = nullptr, *Ttr0 = nullptr, *Ttr1 = nullptr, *Ttr2 = nullptr;
+    double *Tratio = nullptr, *tsa = nullptr, *dT = nullptr;
+    unsigned long long* tsum = nullptr;
     double *band = nullptr, *rowb = nullptr, *bvec = nullptr, *ainv = nullptr;
     int* ipiv = nullptr;
     double* rows = nullptr;
@@ -254,7 +259,8 @@ tc_status smoother_time(Handle* h) {
 // reference index move together; the RK temporaries take the old arrays
 void sort_tracers(Handle* h) {
     launch_sort_tracers(h->st, h->L1, h->P, h->ntr, h->rtr, h->str, h->ttype, h->perm, h->sort_cnt, h->sort_off,
-                        h->sort_bsum, h->rtr1, h->str1, h->itmp[0], h->itmp[1]);
+                        h->sort_bsum, h->rtr1, h->str1, h->itmp[0], h->itmp[1], h->Ttr, h->Ttr1);
+    if (h->Ttr) std::swap(h->Ttr, h->Ttr1);
     std::swap(h->rtr, h->rtr1);
     std::swap(h->str, h->str1);
     std::swap(h->ttype, h->itmp[0]);
@@ -263,8 +269,12 @@ void sort_tracers(Handle* h) {
 
 // tracer arrays to host arrays in the reference's order (any may be null);
 // the copies are queued on the handle's stream
-tc_status download_tracers(Handle* h, double* rtr, double* str, int32_t* Ttype) {
+tc_status download_tracers(Handle* h, double* rtr, double* str, int32_t* Ttype, double* Ttr = nullptr) {
     const size_t n = (size_t)h->ntr;
+    if (Ttr && h->Ttr) {
+        launch_perm_scatter(h->st, h->ntr, h->perm, h->Ttr, h->Ttr2);
+        CK(cudaMemcpyAsync(Ttr, h->Ttr2, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
+    }
     if (rtr) {
         launch_perm_scatter(h->st, h->ntr, h->perm, h->rtr, h->rtr2);
         CK(cudaMemcpyAsync(rtr, h->rtr2, sizeof(double) * n, cudaMemcpyDeviceToHost, h->st));
@@ -280,12 +290,24 @@ tc_status download_tracers(Handle* h, double* rtr, double* str, int32_t* Ttype) 
     return TC_OK;
 }
 
-// tracers_to_corners (composition.f90:669-790), comp=1, tracer=0
-tc_status tracers_to_corners(Handle* h, const double* rr, const double* ss, bool smooth) {
-    launch_histogram(h->st, h->L1, h->P, h->ntr, rr, ss, h->ttype, h->counts, h->ds);
-    launch_counts_to_comp(h->st, h->L1, h->P, h->counts, h->nempty, h->Cnew);
-    for (int t = 0; t < h->ntype; t++) launch_enforce_comp(h->st, h->L1, h->Cnew[t], h->Cnew[t]);
-    if (smooth) TRY(smoother_time(h));
+// tracers_to_corners (composition.f90:669-790).  With temperature tracers
+// (Tt != nullptr) Tratio starts as T0 (kept in empty volumes) and takes the
+// exact per-volume mean of Tt elsewhere, then enforceBCs and, when
+// smoothing, smoother_time_T(Tratio).
+tc_status tracers_to_corners(Handle* h, const double* rr, const double* ss, bool smooth, const double* Tt = nullptr,
+                             const double* T0 = nullptr) {
+    if (Tt) copy_plane(h, h->Tratio, T0);
+    launch_histogram(h->st, h->L1, h->P, h->ntr, rr, ss, h->ttype, h->counts, h->ds, Tt, h->tsum);
+    launch_counts_to_comp(h->st, h->L1, h->P, h->counts, h->nempty, h->Cnew, Tt ? h->tsum : nullptr,
+                          Tt ? h->Tratio : nullptr);
+    if (h->p.comp == 1) {
+        for (int t = 0; t < h->ntype; t++) launch_enforce_comp(h->st, h->L1, h->Cnew[t], h->Cnew[t]);
+        if (smooth) TRY(smoother_time(h));
+    }
+    if (Tt) {
+        launch_enforce_T(h->st, h->L1, h->Tratio, h->p.Tbot);
+        if (smooth) TRY(smoother_time_T(h, h->Tratio));
+    }
     load_conductivity_array(h);
     return TC_OK;
 }
@@ -810,20 +832,24 @@ tc_status update_velocities(Handle* h) {
     return TC_OK;
 }
 
-// energy_time (energy.f90:117-453): field T, compositional tracers, local_time=0
+// energy_time (energy.f90:117-453): field T or temperature tracers,
+// compositional tracers, local_time=0
 tc_status energy_time(Handle* h) {
     if (!h->uploaded) return TC_ERR_STATE;
-    const bool trc = (h->p.comp == 1);
+    const bool tt = (h->p.tracer == 1);
+    const bool cmp = (h->p.comp == 1);
+    const bool trc = cmp || tt;
     const int torder = h->p.torder;
     const bool rat = (h->p.RaT != 0.0);
     launch_stability(h->st, h->L1, h->P, h->conduct, h->conduct_r, h->conduct_s, h->u, h->w, h->p.courant,
                      h->p.dt_manual, h->rs, h->ds);
     TRY(check_flags(h));
     for (int t = 0; t < h->ntype; t++) copy_plane(h, h->C0[t], h->Cnew[t]);
-    copy_plane(h, h->T0, h->T);
+    copy_plane(h, h->T0, tt ? h->Tratio : h->T);
     if (trc && h->ntr > 0 && h->p.tracer_sort_interval > 0 && h->tstep % h->p.tracer_sort_interval == 0)
         sort_tracers(h);
     if (trc) { std::swap(h->rtr0, h->rtr); std::swap(h->str0, h->str); }
+    if (tt) std::swap(h->Ttr0, h->Ttr);
     auto derivs = [&]() {
         launch_derivatives(h->st, h->L1, h->P, h->u, h->du);
         launch_derivatives(h->st, h->L1, h->P, h->w, h->dw);
@@ -834,51 +860,75 @@ tc_status energy_time(Handle* h) {
                             h->u, h->w, h->Cvis, h->ds);
         launch_enforce_T(h->st, h->L1, stage == 4 ? h->T : Tout, h->p.Tbot);
     };
+    // load_tracer_space_array + compute_derivatives(tracer_space_array)
+    auto tracer_space = [&]() {
+        launch_tracer_space(h->st, h->L1, h->P, h->Tratio, h->conduct, h->conduct_r, h->conduct_s, h->Cvis, h->tsa);
+        launch_derivatives(h->st, h->L1, h->P, h->tsa, h->dT);
+    };
+    // a stage's tracer update; Tout is the stage's Ttr1/Ttr2 (temperature tracers)
+    auto stage_tracers = [&](int stage, const double* rin, const double* sin, double* rout, double* sout,
+                             double* Tout) {
+        launch_tracer_stage(h->st, h->L1, h->P, torder, stage, h->ntr, rin, sin, h->rtr0, h->str0, h->rtr, h->str,
+                            rout, sout, h->u, h->w, h->du, h->dw, h->ds, tt ? h->tsa : nullptr, h->dT, h->Ttr0,
+                            h->Ttr, Tout);
+    };
     // ---- stage 1 ----
-    if (rat) stage_T(1, h->T0, h->T1);
+    if (rat) {
+        if (tt) tracer_space();
+        else stage_T(1, h->T0, h->T1);
+    }
     if (trc) {
         derivs();
-        launch_tracer_stage(h->st, h->L1, h->P, torder, 1, h->ntr, h->rtr0, h->str0, h->rtr0, h->str0, h->rtr, h->str,
-                            h->rtr1, h->str1, h->u, h->w, h->du, h->dw, h->ds);
+        stage_tracers(1, h->rtr0, h->str0, h->rtr1, h->str1, h->Ttr1);
     }
     // ---- stage 2 ----
+    if (tt) {
+        TRY(tracers_to_corners(h, h->rtr1, h->str1, true, h->Ttr1, h->T0));
+        tracer_space();
+    }
     if (h->p.RK_update == 1) {
-        if (trc) TRY(tracers_to_corners(h, h->rtr1, h->str1, true));
-        TRY(smoother_time_T(h, h->T1));
+        if (cmp && !tt) TRY(tracers_to_corners(h, h->rtr1, h->str1, true));
+        if (!tt) TRY(smoother_time_T(h, h->T1));
         TRY(update_velocities(h));
         if (trc) derivs();
     }
-    if (rat) stage_T(2, h->T1, h->T2);
-    if (trc)
-        launch_tracer_stage(h->st, h->L1, h->P, torder, 2, h->ntr, h->rtr1, h->str1, h->rtr0, h->str0, h->rtr, h->str,
-                            h->rtr2, h->str2, h->u, h->w, h->du, h->dw, h->ds);
+    if (rat && !tt) stage_T(2, h->T1, h->T2);
+    if (trc) stage_tracers(2, h->rtr1, h->str1, h->rtr2, h->str2, h->Ttr2);
     if (torder >= 3) {
         // ---- stage 3 ----
+        if (tt) {
+            if (cmp) restore_C();
+            TRY(tracers_to_corners(h, h->rtr2, h->str2, true, h->Ttr2, h->T0));
+            tracer_space();
+        }
         if (h->p.RK_update == 1) {
-            if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr2, h->str2, true)); }
-            TRY(smoother_time_T(h, h->T2));
+            if (cmp && !tt) { restore_C(); TRY(tracers_to_corners(h, h->rtr2, h->str2, true)); }
+            if (!tt) TRY(smoother_time_T(h, h->T2));
             TRY(update_velocities(h));
             if (trc) derivs();
         }
-        if (rat) stage_T(3, h->T2, h->T1);
-        if (trc)
-            launch_tracer_stage(h->st, h->L1, h->P, torder, 3, h->ntr, h->rtr2, h->str2, h->rtr0, h->str0, h->rtr,
-                                h->str, h->rtr1, h->str1, h->u, h->w, h->du, h->dw, h->ds);
+        if (rat && !tt) stage_T(3, h->T2, h->T1);
+        if (trc) stage_tracers(3, h->rtr2, h->str2, h->rtr1, h->str1, h->Ttr1);
         // ---- stage 4 ----
+        if (tt) {
+            if (cmp) restore_C();
+            TRY(tracers_to_corners(h, h->rtr1, h->str1, true, h->Ttr1, h->T0));
+            tracer_space();
+        }
         if (h->p.RK_update == 1) {
-            if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr1, h->str1, true)); }
-            TRY(smoother_time_T(h, h->T1));
+            if (cmp && !tt) { restore_C(); TRY(tracers_to_corners(h, h->rtr1, h->str1, true)); }
+            if (!tt) TRY(smoother_time_T(h, h->T1));
             TRY(update_velocities(h));
             if (trc) derivs();
         }
-        if (rat) stage_T(4, h->T1, h->T1);
-        if (trc)
-            launch_tracer_stage(h->st, h->L1, h->P, torder, 4, h->ntr, h->rtr1, h->str1, h->rtr0, h->str0, h->rtr,
-                                h->str, nullptr, nullptr, h->u, h->w, h->du, h->dw, h->ds);
+        if (rat && !tt) stage_T(4, h->T1, h->T1);
+        if (trc) stage_tracers(4, h->rtr1, h->str1, nullptr, nullptr, nullptr);
     }
     // ---- wrap up ----
-    if (trc) { restore_C(); TRY(tracers_to_corners(h, h->rtr, h->str, true)); }
-    TRY(smoother_time_T(h, h->T));
+    if (cmp) restore_C();
+    if (trc) TRY(tracers_to_corners(h, h->rtr, h->str, true, tt ? h->Ttr : nullptr, h->T0));
+    if (tt) copy_plane(h, h->T, h->Tratio);
+    else TRY(smoother_time_T(h, h->T));
     TRY(check_flags(h));
     h->dt = h->hs->dt;
     return TC_OK;
@@ -898,6 +948,8 @@ tc_status stats(Handle* h, tc_stats_row* row) {
         if (h->tstep == 0)
             for (int t = 0; t < h->ntype; t++) h->mass[t] = row->Cavg[t];
         for (int t = 0; t < h->ntype; t++) row->ent[t] = s.integ[4 + t] / asp / h->mass[t];
+    }
+    if (h->p.comp == 1 || h->p.tracer == 1) {
         row->empty_cells = s.empty_cells;
         row->tracer_min = s.nempty_min;
         row->tracer_max = s.nempty_max;
@@ -935,6 +987,8 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.torder != 2 && p.torder != 4) return TC_ERR_UNSUPPORTED;
     if (p.grids < 2 || p.grids > 6) return TC_ERR_ARG;
     if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
+    if (p.tracer != 0 && p.tracer != 1) return TC_ERR_ARG;
+    if (p.tracer == 1 && p.Tbot != 0 && p.Tbot != 1) { h->err = "temperature tracers need Tbot = 0 or 1"; return TC_ERR_ARG; }
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
     if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;
     if (p.learned_guess < 0 || p.learned_guess > 2 || p.learned_smooth < 0 || p.learned_smooth > 64) return TC_ERR_ARG;
@@ -972,7 +1026,7 @@ tc_status create(Handle* h, const tc_params* in) {
     tcs::LevSpacing s1;
     tcs::level_spacing(p.aspect, nx, nz, s1);
     h->grid_dr = s1.dr; h->grid_ds = s1.ds;
-    h->ntr = (p.comp == 1) ? (int64_t)(nx + 1) * (nz + 1) * p.tpc : 0;
+    h->ntr = (p.comp == 1 || p.tracer == 1) ? (int64_t)(nx + 1) * (nz + 1) * p.tpc : 0;
     const int nxc = nx >> (G - 1), nzc = nz >> (G - 1);
     h->ngrid_coarse = (nxc + 1) * (nzc + 1);
     tcs::coarse_bandwidth(nxc, nzc, 2, 1, h->kl, h->ku);
@@ -987,7 +1041,7 @@ tc_status create(Handle* h, const tc_params* in) {
     // ---- physics scalars ----
     Phys& P = h->P;
     P.nx = nx; P.nz = nz; P.ntype = h->ntype; P.comp = p.comp; P.ivis = p.ivis; P.Tbot = p.Tbot; P.Vbc = p.Vbc;
-    P.torder = p.torder; P.aspect = p.aspect; P.dr = s1.dr; P.ds = s1.ds; P.dr2 = s1.dr2; P.ds2 = s1.ds2;
+    P.torder = p.torder; P.tracer = p.tracer; P.aspect = p.aspect; P.dr = s1.dr; P.ds = s1.ds; P.dr2 = s1.dr2; P.ds2 = s1.ds2;
     P.dro2 = 0.5 * s1.dr; P.dso2 = 0.5 * s1.ds; P.RaT = p.RaT;
     P.lnvisT = std::log(p.visT); P.lnvisP = std::log(p.visP); P.visT2 = p.visT * p.visT; P.H = p.H;
     P.visT = p.visT; P.yield = p.yield; P.yield_gradient = p.yield_gradient; P.yield_depth = p.yield_depth;
@@ -1029,6 +1083,13 @@ tc_status create(Handle* h, const tc_params* in) {
         TRY(dalloc_t(h, &h->sort_cnt, pl));
         TRY(dalloc_t(h, &h->sort_off, pl));
         TRY(dalloc_t(h, &h->sort_bsum, (pl + 1023) / 1024));
+    }
+    if (p.tracer == 1 && h->ntr > 0) {
+        double** tq[] = {&h->Ttr, &h->Ttr0, &h->Ttr1, &h->Ttr2};
+        for (double** q : tq) TRY(dalloc_t(h, q, (size_t)h->ntr));
+        double** tf[] = {&h->Tratio, &h->tsa, &h->dT};
+        for (double** q : tf) TRY(dalloc_t(h, q, pl));
+        TRY(dalloc_t(h, &h->tsum, 2 * pl));
     }
     const int ldab = 2 * h->kl + h->ku + 1;
     TRY(dalloc_t(h, &h->band, (size_t)ldab * h->ngrid_coarse));
@@ -1164,9 +1225,13 @@ tc_status get_field(Handle* h, double* host, const double* dev) {
 }
 
 tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF, const double* r, const double* s,
-                 const int32_t* tt, int64_t n) {
+                 const int32_t* tt, int64_t n, const double* Ttr = nullptr) {
     if (!T || !SF) return TC_ERR_ARG;
     if (h->p.comp == 1 && (n != h->ntr || !r || !s || !tt)) return TC_ERR_ARG;
+    if (h->p.tracer == 1 && (n != h->ntr || !r || !s || !Ttr)) {
+        h->err = "temperature tracers need rtr, str and Ttr (tc_upload_state_ex)";
+        return TC_ERR_ARG;
+    }
     TRY(put_field(h, h->T, T));
     TRY(put_field(h, h->SF, SF));
     const size_t ni = (size_t)h->nx + 1 + 2 * SP, nk = (size_t)h->nz + 1 + 2 * SP;
@@ -1181,10 +1246,13 @@ tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF,
             CK(cudaMemsetAsync(h->Cnew[t], 0, sizeof(double) * h->L1.plane, h->st));
         }
     }
-    if (h->p.comp == 1) {
+    if (h->p.comp == 1 || h->p.tracer == 1) {
         CK(cudaMemcpyAsync(h->rtr, r, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         CK(cudaMemcpyAsync(h->str, s, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
-        CK(cudaMemcpyAsync(h->ttype, tt, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        if (h->p.comp == 1) CK(cudaMemcpyAsync(h->ttype, tt, sizeof(int32_t) * h->ntr, cudaMemcpyHostToDevice, h->st));
+        else CK(cudaMemsetAsync(h->ttype, 0, sizeof(int32_t) * h->ntr, h->st));  // all ambient
+        if (h->p.tracer == 1)
+            CK(cudaMemcpyAsync(h->Ttr, Ttr, sizeof(double) * h->ntr, cudaMemcpyHostToDevice, h->st));
         launch_iota(h->st, h->ntr, h->perm);
     }
     CK(cudaMemsetAsync(h->ds, 0, sizeof(DevScalars), h->st));
@@ -1194,7 +1262,8 @@ tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF,
     for (int l = 2; l <= h->grids; l++)
         for (int q = 0; q < 2; q++) CK(cudaMemsetAsync(h->lev[l].err[q], 0, sizeof(double) * h->lev[l].L.plane, h->st));
     h->uploaded = true;
-    if (h->p.comp == 1) TRY(tracers_to_corners(h, h->rtr, h->str, false));
+    if (h->p.comp == 1 || h->p.tracer == 1)
+        TRY(tracers_to_corners(h, h->rtr, h->str, false, h->p.tracer == 1 ? h->Ttr : nullptr, h->T));
     TRY(smoother_time_T(h, h->T));
     if (h->p.comp != 0) TRY(smoother_time(h));
     load_conductivity_array(h);
@@ -1377,6 +1446,21 @@ tc_status tc_upload_state(tc_handle* H, const double* T, const double* Cnew, con
     return upload(&H->h, T, Cnew, SF, rtr, str, Ttype, ntr);
 }
 
+tc_status tc_upload_state_ex(tc_handle* H, const double* T, const double* Cnew, const double* SF, const double* rtr,
+                             const double* str, const int32_t* Ttype, const double* Ttr, int64_t ntr) {
+    if (!H) return TC_ERR_ARG;
+    return upload(&H->h, T, Cnew, SF, rtr, str, Ttype, ntr, Ttr);
+}
+
+tc_status tc_download_tracer_temperature(tc_handle* H, double* Ttr) {
+    if (!H || !Ttr) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (h->p.tracer != 1 || !h->Ttr) return TC_ERR_ARG;
+    TRY(download_tracers(h, nullptr, nullptr, nullptr, Ttr));
+    CK(cudaStreamSynchronize(h->st));
+    return TC_OK;
+}
+
 tc_status tc_download_state(tc_handle* H, double* T, double* Cnew, double* SF, double* rtr, double* str,
                             int32_t* Ttype) {
     if (!H) return TC_ERR_ARG;
@@ -1392,7 +1476,7 @@ tc_status tc_download_state(tc_handle* H, double* T, double* Cnew, double* SF, d
             for (size_t x = 0; x < ni * nk; x++) Cnew[x * h->ntype + t] = tmp[x];
         }
     }
-    if (h->p.comp == 1) TRY(download_tracers(h, rtr, str, Ttype));
+    if (h->p.comp == 1 || h->p.tracer == 1) TRY(download_tracers(h, rtr, str, h->p.comp == 1 ? Ttype : nullptr));
     CK(cudaStreamSynchronize(h->st));
     return TC_OK;
 }
@@ -1609,6 +1693,10 @@ tc_status tc_step_host(tc_handle* H, double* T, double* Cnew, double* SF, double
     if (!H || !T || !SF) return TC_ERR_ARG;
     Handle* h = &H->h;
     if (!h->uploaded) return TC_ERR_STATE;
+    if (h->p.tracer == 1) {
+        h->err = "tc_step_host carries no tracer temperatures: use tc_step with tc_download_tracer_temperature";
+        return TC_ERR_UNSUPPORTED;
+    }
     if (h->p.comp == 1 && (ntr != h->ntr || !rtr || !str || !Ttype || !Cnew)) return TC_ERR_ARG;
     TRY(put_field(h, h->T, T));
     TRY(put_field(h, h->SF, SF));
@@ -1813,6 +1901,8 @@ tc_status tc_debug_field(tc_handle* H, const char* name, int32_t level, int32_t 
         else if (n == "DERr_w") src = h->dw;
         else if (n == "dts_array") src = h->dts;
         else if (n == "strain") src = h->strain;
+        else if (n == "Tratio") src = h->Tratio;
+        else if (n == "tracer_space_array") src = h->tsa;
         else if (n == "Cnew") src = ty(h->Cnew);
         else if (n == "Cvis") src = ty(h->Cvis);
         else if (n == "Cbuoy") src = ty(h->Cbuoy);

@@ -157,7 +157,7 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path) {
     const size_t vi = (size_t)nx + 3, nv = vi * ((size_t)nz + 3);
     std::vector<double> T(nf), SF(nf), C((size_t)(ntype ? ntype : 1) * nf), u(nv), w(nv), strain(nf), vis(nf),
         Tvis(nf), Cvis((size_t)(ntype ? ntype : 1) * nf), tmp(nf);
-    std::vector<int32_t> cnt(nf * (size_t)(p.ntype + 1));
+    std::vector<int32_t> cnt(nf * (size_t)(ntype + 1));
     st = tc_download_state(h, T.data(), ntype ? C.data() : nullptr, SF.data(), nullptr, nullptr, nullptr);
     if (st == TC_OK) st = tc_download_velocities(h, u.data(), w.data());
     if (st == TC_OK) st = tc_debug_field(h, "strain", 1, 0, strain.data());
@@ -167,7 +167,8 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path) {
         st = tc_debug_field(h, "Cvis", 1, t + 1, tmp.data());
         for (size_t q = 0; q < nf; q++) Cvis[q * ntype + t] = tmp[q];
     }
-    if (st == TC_OK && p.comp == 1) st = tc_download_counts(h, cnt.data());
+    const bool counted = (p.comp == 1 || p.tracer == 1);
+    if (st == TC_OK && counted) st = tc_download_counts(h, cnt.data());
     if (st != TC_OK) return st;
     std::vector<double> xg(nx + 7), zg(nz + 7);
     tc_restart_grid(nx, nz, p.aspect, xg.data(), zg.data());
@@ -181,8 +182,9 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path) {
             const size_t q = (size_t)(i + kSpan) + (size_t)(k + kSpan) * fi;
             const size_t qv = (size_t)(i + 1) + (size_t)(k + 1) * vi;
             int nempty = 0;
-            if (p.comp == 1)
-                for (int t = 0; t <= p.ntype; t++) nempty += cnt[q * (p.ntype + 1) + t];
+            const int nct = ntype + 1;  // count_type(0:ntype)
+            if (counted)
+                for (int t = 0; t < nct; t++) nempty += cnt[q * nct + t];
             line.clear();
             g(xg[i + 3]);
             g(zg[k + 3]);
@@ -191,10 +193,14 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path) {
                 g(SF[q]);
                 g(u[qv]);
                 g(w[qv]);
-                if (p.comp == 0) {
-                    // tracer = 0 on this path: xg, zg, T, SF, u, w, vis, Tvis
+                if (p.comp == 0 && p.tracer == 0) {
                     g(vis[q]);
                     g(Tvis[q]);
+                } else if (p.comp == 0) {
+                    g(strain[q]);
+                    g(vis[q]);
+                    g(Tvis[q]);
+                    fmt_i(line, nempty, 6);
                 } else {
                     g(strain[q]);
                     g(vis[q]);

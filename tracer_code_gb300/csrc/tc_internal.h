@@ -101,7 +101,7 @@ struct Level {
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
 struct Phys {
-    int nx, nz, ntype, comp, ivis, Tbot, Vbc, torder;
+    int nx, nz, ntype, comp, ivis, Tbot, Vbc, torder, tracer;
     double aspect, dr, ds, dr2, ds2, dro2, dso2;
     double RaT, RaC[TC_MAX_TYPES], lnvisT, lnvisP, lnvisC[TC_MAX_TYPES], visT2, H, Htype[TC_MAX_TYPES];
     double lncf[TC_MAX_TYPES];   // log(1/conduct_factor)
@@ -220,16 +220,24 @@ void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const d
 void launch_tracer_stage(cudaStream_t s, const Lay& L, const Phys& P, int torder, int stage, int64_t ntr,
                          const double* rin, const double* sin, const double* r0, const double* s0, double* racc,
                          double* sacc, double* rout, double* sout, const double* u, const double* w,
-                         const double* du, const double* dw, const DevScalars* ds);
+                         const double* du, const double* dw, const DevScalars* ds, const double* tsa = nullptr,
+                         const double* dT = nullptr, const double* Ttr0 = nullptr, double* Ttr = nullptr,
+                         double* Tout = nullptr);
+// counts per type and volume; with Tt (temperature tracers) also the exact
+// per-volume sums of Tt into tsum (2 x L.plane words: low, high)
 void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* r, const double* sv,
-                      const int* ttype, int* counts, DevScalars* ds);
-// cell sort of the tracer arrays (k_tracer.cu): rr/ss/tt/perm -> r2/s2/t2/p2
+                      const int* ttype, int* counts, DevScalars* ds, const double* Tt = nullptr,
+                      unsigned long long* tsum = nullptr);
+// cell sort of the tracer arrays (k_tracer.cu): rr/ss/tt/perm[/Tt] -> r2/s2/t2/p2[/T2]
 void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* rr, const double* ss,
                          const int* tt, const int* perm, int* cnt, int* off, int* bsum, double* r2, double* s2,
-                         int* t2, int* p2);
+                         int* t2, int* p2, const double* Tt = nullptr, double* T2 = nullptr);
+// extendT + tracer_space on (-1:nx+1, -1:nz+1) (temperature tracers)
+void launch_tracer_space(cudaStream_t s, const Lay& L, const Phys& P, const double* Tratio, const double* conduct,
+                         const double* conduct_r, const double* conduct_s, const double* const* Cvis, double* tsa);
 void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out);
 void launch_perm_scatter(cudaStream_t s, int64_t n, const int* perm, const int* in, int* out);
 void launch_perm_gather(cudaStream_t s, int64_t n, const int* perm, const double* in, double* out);
 void launch_iota(cudaStream_t s, int64_t n, int* p);
 void launch_counts_to_comp(cudaStream_t s, const Lay& L, const Phys& P, int* counts, int* nempty,
-                           double* const* Cnew);
+                           double* const* Cnew, const unsigned long long* tsum = nullptr, double* Tratio = nullptr);

@@ -7,9 +7,9 @@
 //                    xg(-3:nx+3), zg(-3:nz+3), [T], [Cnew(1:ntype,:,:)], SF
 //                    (T when RaT /= 0, Cnew when comp = 1; T, SF and Cnew on
 //                    the (-span:nx+span, -span:nz+span) box, i fastest)
-//   restart_tracers  print_restart (main.f90:321-330) / grid.f90:74-84 for
-//                    compositional tracers (tracer = 0): one record
-//                    rtr(ntr), str(ntr), Ttype(ntr)
+//   restart_tracers  print_restart (main.f90:321-330) / grid.f90:74-84: one
+//                    record rtr(ntr), str(ntr), then Ttype(ntr) (comp = 1)
+//                    and/or Ttr(ntr) (temperature tracers, tracer = 1)
 //
 // A gfortran unformatted sequential record is a 4-byte little-endian length,
 // the payload, and the same length again.  Records of 2^31 bytes or more
@@ -97,16 +97,23 @@ tc_status tc_restart_read(const char* path, int32_t nx, int32_t nz, int32_t ntyp
 }
 
 tc_status tc_restart_tracers_write(const char* path, int64_t ntr, const double* rtr, const double* str,
-                                   const int32_t* Ttype) {
-    if (!path || ntr < 1 || !rtr || !str || !Ttype) return TC_ERR_ARG;
+                                   const int32_t* Ttype, const double* Ttr) {
+    if (!path || ntr < 1 || !rtr || !str || (!Ttype && !Ttr)) return TC_ERR_ARG;
     const size_t n = (size_t)ntr;
-    return write_record(path, {{rtr, nullptr, 8 * n}, {str, nullptr, 8 * n}, {Ttype, nullptr, 4 * n}});
+    std::vector<Part> v = {{rtr, nullptr, 8 * n}, {str, nullptr, 8 * n}};
+    if (Ttype) v.push_back({Ttype, nullptr, 4 * n});
+    if (Ttr) v.push_back({Ttr, nullptr, 8 * n});
+    return write_record(path, v);
 }
 
-tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype) {
-    if (!path || ntr < 1 || !rtr || !str || !Ttype) return TC_ERR_ARG;
+tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, double* str, int32_t* Ttype,
+                                  double* Ttr) {
+    if (!path || ntr < 1 || !rtr || !str || (!Ttype && !Ttr)) return TC_ERR_ARG;
     const size_t n = (size_t)ntr;
-    return read_record(path, {{nullptr, rtr, 8 * n}, {nullptr, str, 8 * n}, {nullptr, Ttype, 4 * n}});
+    std::vector<Part> v = {{nullptr, rtr, 8 * n}, {nullptr, str, 8 * n}};
+    if (Ttype) v.push_back({nullptr, Ttype, 4 * n});
+    if (Ttr) v.push_back({nullptr, Ttr, 8 * n});
+    return read_record(path, v);
 }
 
 void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg) {
@@ -142,21 +149,24 @@ tc_status tc_write_restart(tc_handle* h, const char* trestart, const char* trace
     const int nx = info.nx, nz = info.nz, ntype = (p.comp == 1) ? p.ntype : 0;
     const size_t nf = field_count(nx, nz);
     std::vector<double> xg(nx + 1 + 2 * kSpanX), zg(nz + 1 + 2 * kSpanX), T(nf), SF(nf), C(nf * (ntype ? ntype : 1));
-    std::vector<double> r, st;
+    std::vector<double> r, st, Tt;
     std::vector<int32_t> tt;
-    const bool trc = (p.comp == 1 && info.ntr > 0);
+    const bool trc = ((p.comp == 1 || p.tracer == 1) && info.ntr > 0);
     if (trc) {
         r.resize((size_t)info.ntr);
         st.resize((size_t)info.ntr);
-        tt.resize((size_t)info.ntr);
+        if (p.comp == 1) tt.resize((size_t)info.ntr);
+        if (p.tracer == 1) Tt.resize((size_t)info.ntr);
     }
     s = tc_download_state(h, T.data(), ntype ? C.data() : nullptr, SF.data(), trc ? r.data() : nullptr,
-                          trc ? st.data() : nullptr, trc ? tt.data() : nullptr);
+                          trc ? st.data() : nullptr, tt.empty() ? nullptr : tt.data());
+    if (s == TC_OK && !Tt.empty()) s = tc_download_tracer_temperature(h, Tt.data());
     if (s != TC_OK) return s;
     tc_restart_grid(nx, nz, p.aspect, xg.data(), zg.data());
     s = tc_restart_write(trestart, nx, nz, ntype, p.RaT != 0.0, xg.data(), zg.data(), T.data(), C.data(), SF.data());
     if (s != TC_OK || !trc || !tracers) return s;
-    return tc_restart_tracers_write(tracers, info.ntr, r.data(), st.data(), tt.data());
+    return tc_restart_tracers_write(tracers, info.ntr, r.data(), st.data(), tt.empty() ? nullptr : tt.data(),
+                                    Tt.empty() ? nullptr : Tt.data());
 }
 
 tc_status tc_read_restart(tc_handle* h, const char* trestart, const char* tracers) {
@@ -172,19 +182,22 @@ tc_status tc_read_restart(tc_handle* h, const char* trestart, const char* tracer
     std::vector<double> xg(nx + 1 + 2 * kSpanX), zg(nz + 1 + 2 * kSpanX), T(nf, 0.0), SF(nf), C(nf * (ntype ? ntype : 1));
     s = tc_restart_read(trestart, nx, nz, ntype, p.RaT != 0.0, xg.data(), zg.data(), T.data(), C.data(), SF.data());
     if (s != TC_OK) return s;
-    const bool trc = (p.comp == 1 && info.ntr > 0);
-    std::vector<double> r, st;
+    const bool trc = ((p.comp == 1 || p.tracer == 1) && info.ntr > 0);
+    std::vector<double> r, st, Tt;
     std::vector<int32_t> tt;
     if (trc) {
         if (!tracers) return TC_ERR_ARG;
         r.resize((size_t)info.ntr);
         st.resize((size_t)info.ntr);
-        tt.resize((size_t)info.ntr);
-        s = tc_restart_tracers_read(tracers, info.ntr, r.data(), st.data(), tt.data());
+        if (p.comp == 1) tt.resize((size_t)info.ntr);
+        if (p.tracer == 1) Tt.resize((size_t)info.ntr);
+        s = tc_restart_tracers_read(tracers, info.ntr, r.data(), st.data(), tt.empty() ? nullptr : tt.data(),
+                                    Tt.empty() ? nullptr : Tt.data());
         if (s != TC_OK) return s;
     }
-    return tc_upload_state(h, T.data(), ntype ? C.data() : nullptr, SF.data(), trc ? r.data() : nullptr,
-                           trc ? st.data() : nullptr, trc ? tt.data() : nullptr, trc ? info.ntr : 0);
+    return tc_upload_state_ex(h, T.data(), ntype ? C.data() : nullptr, SF.data(), trc ? r.data() : nullptr,
+                              trc ? st.data() : nullptr, tt.empty() ? nullptr : tt.data(),
+                              Tt.empty() ? nullptr : Tt.data(), trc ? info.ntr : 0);
 }
 
 }  // extern "C"

@@ -69,22 +69,31 @@ def read_trestart(path, nx: int, nz: int, ntype: int = 0, thermal: bool = True) 
     return out
 
 
-def write_tracers(path, rtr, str_, Ttype) -> None:
-    """print_restart's restart_tracers record for tracer = 0 (main.f90:321-330)."""
+def write_tracers(path, rtr, str_, Ttype=None, Ttr=None) -> None:
+    """print_restart's restart_tracers record (main.f90:321-330): rtr, str,
+    then Ttype (comp = 1) and/or Ttr (tracer = 1)."""
     r = np.ascontiguousarray(rtr, np.float64)
     s = np.ascontiguousarray(str_, np.float64)
-    t = np.ascontiguousarray(Ttype, np.int32)
-    if not (r.size == s.size == t.size):
-        raise TracerError(1, "write_tracers", "rtr, str, Ttype must have one length")
-    st = _lib().tc_restart_tracers_write(os.fsencode(path), r.size, _p(r), _p(s), _p(t))
+    t = None if Ttype is None else np.ascontiguousarray(Ttype, np.int32)
+    tt = None if Ttr is None else np.ascontiguousarray(Ttr, np.float64)
+    if r.size != s.size or (t is not None and t.size != r.size) or (tt is not None and tt.size != r.size):
+        raise TracerError(1, "write_tracers", "rtr, str, Ttype, Ttr must have one length")
+    st = _lib().tc_restart_tracers_write(os.fsencode(path), r.size, _p(r), _p(s), _p(t), _p(tt))
     if st:
         raise TracerError(st, "write_tracers")
 
 
-def read_tracers(path, ntr: int) -> dict:
-    """build_grid's restart_tracers read for tracer = 0 (grid.f90:74-84)."""
-    r = np.empty(ntr); s = np.empty(ntr); t = np.empty(ntr, np.int32)
-    st = _lib().tc_restart_tracers_read(os.fsencode(path), ntr, _p(r), _p(s), _p(t))
+def read_tracers(path, ntr: int, Ttype: bool = True, Ttr: bool = False) -> dict:
+    """build_grid's restart_tracers read (grid.f90:74-84) for the given record layout."""
+    r = np.empty(ntr); s = np.empty(ntr)
+    t = np.empty(ntr, np.int32) if Ttype else None
+    tt = np.empty(ntr) if Ttr else None
+    st = _lib().tc_restart_tracers_read(os.fsencode(path), ntr, _p(r), _p(s), _p(t), _p(tt))
     if st:
         raise TracerError(st, "read_tracers")
-    return {"rtr": r, "str": s, "Ttype": t}
+    out = {"rtr": r, "str": s}
+    if Ttype:
+        out["Ttype"] = t
+    if Ttr:
+        out["Ttr"] = tt
+    return out

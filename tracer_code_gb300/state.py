@@ -8,7 +8,8 @@ initialize_tracers (composition.f90:593-639): ids run over corner control
 volumes with i outermost, then k, then the tpc tracers of that volume; each
 tracer sits at (i*dr, k*ds) + (U-1/2)*(dr, ds), clamped inside the walls by
 dist_r/dist_s; Ttype = composition(x, z) with initial_comp=0
-(initial_conditions.f90:149-158).
+(initial_conditions.f90:149-158); with temperature tracers, Ttr is the
+initial temperature profile at each tracer.
 """
 from __future__ import annotations
 
@@ -103,6 +104,18 @@ def initial_state(p: Params, seed: int = 1, nx: int | None = None, nz: int | Non
     T = initial_temperature(p, nx, nz)
     SF = np.zeros_like(T)
     st = {"T": T, "SF": SF, "Cnew": initial_composition(p, nx, nz)}
-    if p.comp == 1:
-        st["rtr"], st["str"], st["Ttype"] = initial_tracers(p, seed, nx, nz)
+    if p.comp == 1 or p.tracer == 1:
+        r, s, t = initial_tracers(p, seed, nx, nz)
+        st["rtr"], st["str"] = r, s
+        if p.comp == 1:
+            st["Ttype"] = t
+        if p.tracer == 1:
+            st["Ttr"] = initial_tracer_temperature(r, s)
     return st
+
+
+def initial_tracer_temperature(r: np.ndarray, s: np.ndarray) -> np.ndarray:
+    """Ttr = temperature(x, z) at each tracer (initialize_tracers,
+    composition.f90:630-633), with the grid's initial profile
+    (1 - z) + 0.01 cos(pi x) sin(pi z)."""
+    return np.ascontiguousarray((1.0 - s) + 0.01 * np.cos(np.pi * r) * np.sin(np.pi * s))
