@@ -78,7 +78,7 @@ typedef struct tc_params {
     double  spaceX, spaceZ, thickness;
     int32_t nbound;
     /* velocity solver options (main.f90:23-34) */
-    int32_t non_Newtonian;      /* GPU path: 0                                           */
+    int32_t non_Newtonian;      /* 1: viscosity rebuilt every W-cycle (FP64 solver only)  */
     int32_t iterate_order;      /* 1 = Richardson/Chebyshev smoother                     */
     double  tolerance;          /* relative L1 residual for multigrid convergence       */
     int32_t Nmulti;             /* smoother sweeps per level visit                        */

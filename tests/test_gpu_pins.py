@@ -3,7 +3,8 @@ pins in test_oracle_pins.py, run through the C ABI on the device): from
 Trestart's T and SF, compute_velocities, compute_strain_rate_invariant,
 compute_viscosity(1) (visf with plastic yielding, ivis = 3, and the level-1
 viscosity filter) and stats reproduce stats.dat's and
-viscosity_smoother.dat's last rows to their 8 printed digits, and as text."""
+viscosity_smoother.dat's last rows to their 8 printed digits, and as text;
+the shipped non-Newtonian solve restarts from Trestart as the oracle does."""
 import pytest
 
 from tracer_code_gb300 import Simulation
@@ -50,13 +51,21 @@ def test_gpu_rows_are_the_reference_text(gpu_row, golden):
     assert textio.vis_line(gpu_row, 0, 0, RaT) == golden["text_lines"]["viscosity_smoother.dat"][-1]
 
 
-def test_plastic_multigrid_is_reported_unsupported(gpu_lib, golden):
-    """The GPU multigrid implements the Newtonian branch; the shipped
-    plastic case (ivis = 3, non_Newtonian = 1) is refused, not run wrongly."""
-    from tracer_code_gb300 import TracerError
-    g = Simulation(_pin_params(golden))
-    g.upload({"T": golden["T"], "SF": golden["SF"]})
-    with pytest.raises(TracerError) as e:
-        g.multigrid()
-    assert e.value.status == 2  # TC_ERR_UNSUPPORTED
+def test_gpu_plastic_solve_from_trestart(gpu_lib, golden):
+    """The shipped configuration's non-Newtonian solve (ivis = 3 plastic
+    viscosity, non_Newtonian = 1, 2 levels) from Trestart: the stored
+    streamfunction is converged, so both sides stop after the first cycle
+    and the solution moves by no more than one cycle's smoothing, the same
+    on the GPU as in the CPU restatement."""
+    import numpy as np
+    from oracle.pyoracle import Oracle
+    p = _pin_params(golden)
+    g = Simulation(p)
+    o = Oracle(p)
+    for x in (g, o):
+        x.upload({"T": golden["T"], "SF": golden["SF"]})
+    qg, qo = g.multigrid(), o.multigrid()
+    assert qg == qo == 1
+    a, b = g.download()["SF"], o.download()["SF"]
+    assert np.abs(a - b).max() <= 1e-9 * np.abs(b).max()
     g.close()

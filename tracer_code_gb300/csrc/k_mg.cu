@@ -207,9 +207,11 @@ __global__ void k_level_coefs(Lay L, LevConst c, Range2 r, const double* __restr
     if (!inr) return;
     size_t x = IX(L, i, k);
     double v = V[x], ax = vx[x], az = vz[x], axx = vxx[x], azz = vzz[x], axz = vxz[x];
-    double eR, eI;
-    eig_pair(c, v, ax, az, axx, azz, axz, eR, eI);
-    dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
+    if (dts) {
+        double eR, eI;
+        eig_pair(c, v, ax, az, axx, azz, axz, eR, eI);
+        dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
+    }
     double g0 = axx - azz, g1 = v, g2 = 2.0 * v, g3 = 4.0 * axz, g4 = 2.0 * ax, g5 = 2.0 * az;
 #pragma unroll
     for (int d = 0; d < TC_NCOEF; d++) {
@@ -230,12 +232,12 @@ __global__ void k_level_coefs(Lay L, LevConst c, Range2 r, const double* __restr
     }
 }
 void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int ivis, double courant_stream,
-                        int cheb_level) {
+                        int cheb_level, bool with_dt) {
     (void)ivis;
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_level_coefs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
-                                                        lv.ratio, lv.dt_stream, lv.coef, lv.cA, lv.cB,
-                                                        courant_stream, cheb_level); tc_note_launch();
+                                                        lv.ratio, with_dt ? lv.dt_stream : nullptr, lv.coef, lv.cA,
+                                                        lv.cB, courant_stream, cheb_level); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------

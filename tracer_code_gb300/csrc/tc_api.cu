@@ -688,43 +688,61 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
 void enqueue_l1(Handle* h, int dir) { iterate_stream(h, 1, dir); }
 void enqueue_rest(Handle* h, int) { enqueue_cycle_rest(h); }
 
-// multigrid (iterative_solver.f90:79-173), Newtonian branch
+void compute_velocities(Handle* h);
+
+// multigrid (iterative_solver.f90:79-173).  Newtonian rheology
+// (non_Newtonian = 0): viscosities, level operators and the coarse LU once
+// per solve.  non_Newtonian = 1: every cycle starts from the current
+// correction (SF = error(1), velocities, strain rate) and rebuilds every
+// level's viscosity, local time steps and the coarse LU; after the level-1
+// visit the level-1 viscosity is brought up to date and the residual the
+// convergence test reads is taken with it (iterative_solver.f90:106-116,
+// 141-148).  The non-Newtonian iteration runs in FP64 without the learned
+// start and issues its launches directly (its level setup has host-side
+// loops between kernels).
 tc_status multigrid(Handle* h) {
     if (!h->uploaded) return TC_ERR_STATE;
-    if (h->p.non_Newtonian != 0 || h->p.ivis == 3) {
-        // the non-Newtonian iteration recomputes velocities, strain rate and
-        // every level's viscosity inside the W-cycle loop (iterative_solver.f90:
-        // 100-160); the GPU solve implements the Newtonian branch.  Plastic
-        // viscosity (ivis = 3) is the reference's non-Newtonian case: with
-        // non_Newtonian = 0 its own step does not finish (the CPU restatement
-        // reaches the filter loop cap in energy_time), so it is refused here;
-        // tc_compute_viscosity and tc_stats implement it
-        h->err = "non-Newtonian / plastic viscosity: the GPU multigrid implements the Newtonian branch";
-        return TC_ERR_UNSUPPORTED;
-    }
+    const bool nonN = (h->p.non_Newtonian == 1);
     const int G = h->grids;
+    const bool mixed = (h->p.solver_precision == 1);
     copy_plane(h, cur_err(h, 1), h->SF);
     launch_rhs1(h->st, h->L1, h->P, h->Tbuoy, h->Cbuoy, h->lev[1].rhs, h->rs, h->ds);
-    for (int l = 1; l <= G; l++) TRY(compute_viscosity(h, l));
-    for (int l = 1; l <= G; l++)
-        launch_level_coefs(h->st, h->lev[l], cur_vis(h, l), h->p.ivis, h->p.courant_stream, l == h->ratio_level ? 1 : 0);
-    const bool mixed = (h->p.solver_precision == 1);
-    if (mixed) {
-        for (int l = 1; l < G; l++) launch_level_to_f32(h->st, h->lev[l], l == h->ratio_level ? 1 : 0);
-    }
-    h->ctab_level = 0;
-    if (!mixed && h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
-        visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti, 0)) {
-        double cv[128], tv[128];
-        cheb_temps(h->p.Nmulti, 0, tv, cv);
-        launch_cheb_table(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab);
-        h->ctab_level = h->ratio_level;
-    }
-    if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) {
+    // compute_viscosity + iterate_local_time_steps of every level, in the
+    // folded form the sweeps read
+    auto level_setup = [&]() -> tc_status {
+        for (int l = 1; l <= G; l++) TRY(compute_viscosity(h, l));
+        for (int l = 1; l <= G; l++)
+            launch_level_coefs(h->st, h->lev[l], cur_vis(h, l), h->p.ivis, h->p.courant_stream,
+                               l == h->ratio_level ? 1 : 0);
+        if (mixed) {
+            for (int l = 1; l < G; l++) launch_level_to_f32(h->st, h->lev[l], l == h->ratio_level ? 1 : 0);
+        }
+        h->ctab_level = 0;
+        if (!mixed && h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
+            visit_cluster_fits(h->lev[h->ratio_level].L, h->p.Nmulti, 0)) {
+            double cv[128], tv[128];
+            cheb_temps(h->p.Nmulti, 0, tv, cv);
+            launch_cheb_table(h->st, h->lev[h->ratio_level], tv, h->p.Nmulti, h->ctab);
+            h->ctab_level = h->ratio_level;
+        }
+        return TC_OK;
+    };
+    // Compute_Matrix_coarse + DGBTRF (and the explicit inverse the coarse visits apply)
+    auto coarse_setup = [&]() {
         launch_coarse_build(h->st, h->lev[G], h->band, h->rowb, h->kl, h->ku, h->p.Vbc);
         launch_coarse_lu(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ds);
         launch_coarse_inverse(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ainv, h->bvec);
         h->lu_valid = true;
+    };
+    // SF = error(1); compute_velocities; compute_strain_rate_invariant
+    auto strain_from_correction = [&]() {
+        copy_plane(h, h->SF, cur_err(h, 1));
+        compute_velocities(h);
+        launch_strain(h->st, h->L1, h->P, h->u, h->w, h->strain);
+    };
+    if (!nonN) {
+        TRY(level_setup());
+        if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) coarse_setup();
     }
     CK(cudaMemsetAsync(&h->ds->visit_timeout, 0, sizeof(int), h->st));
     const size_t img = (size_t)h->nx * h->nz;
@@ -733,7 +751,7 @@ tc_status multigrid(Handle* h) {
         nn_fields_to_raw(h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1),
                          h->rec_raw + (size_t)h->rec_count * 3 * img);
     const int kGuessPatience = 8, kGuessProbe = 32;
-    bool try_guess = (h->p.learned_guess == 1 || h->p.learned_guess == 2) && h->net != nullptr;
+    bool try_guess = (h->p.learned_guess == 1 || h->p.learned_guess == 2) && h->net != nullptr && !nonN;
     if (try_guess && h->p.learned_guess == 1 && h->guess_reject_streak >= kGuessPatience &&
         (h->guess_solves % kGuessProbe) != 0)
         try_guess = false;
@@ -772,7 +790,7 @@ tc_status multigrid(Handle* h) {
     // follows it, then p=2..nsteps run unconditionally.
     const int dir1 = (h->multi[2] > h->multi[1]) ? 0 : 1;
     CycleGraphs& cg = *h->graphs;
-    const bool use_graphs = (h->st != nullptr) && !h->no_graphs;
+    const bool use_graphs = (h->st != nullptr) && !h->no_graphs && !nonN;
     void (*f_l1)(Handle*, int) = mixed ? enqueue_l1_mixed : enqueue_l1;
     void (*f_rest)(Handle*, int) = mixed ? enqueue_rest_mixed : enqueue_rest;
     h->enq_err = cudaSuccess;
@@ -790,10 +808,25 @@ tc_status multigrid(Handle* h) {
     }
     int q = 1;
     for (;;) {
+        if (nonN) {
+            strain_from_correction();
+            TRY(level_setup());
+            coarse_setup();
+        }
         if (use_graphs) { CK(cudaGraphLaunch(cg.l1, h->st)); tc_note_launch(cg.n_l1); }
         else f_l1(h, dir1);
         CK(h->enq_err);
+        if (nonN) {
+            // the level-1 viscosity of the new correction, its operator (the
+            // local time steps stay those of the cycle start) and the residual
+            strain_from_correction();
+            TRY(compute_viscosity(h, 1));
+            launch_level_coefs(h->st, h->lev[1], cur_vis(h, 1), h->p.ivis, h->p.courant_stream,
+                               h->ratio_level == 1 ? 1 : 0, false);
+            launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+        }
         TRY(sync_scalars(h));
+        if (nonN && h->hs->lu_info != 0) return TC_ERR_SINGULAR;
         if (h->hs->visit_timeout) {
             h->err = "fused smoother visit: neighbour wait exceeded its bound";
             return TC_ERR_DEVICE_TIMEOUT;
@@ -988,6 +1021,11 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.grids < 2 || p.grids > 6) return TC_ERR_ARG;
     if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
     if (p.tracer != 0 && p.tracer != 1) return TC_ERR_ARG;
+    if (p.non_Newtonian != 0 && p.non_Newtonian != 1) return TC_ERR_ARG;
+    if (p.non_Newtonian == 1 && (p.solver_precision != 0 || p.learned_guess != 0)) {
+        h->err = "the non-Newtonian iteration runs in FP64 without the learned start";
+        return TC_ERR_UNSUPPORTED;
+    }
     if (p.tracer == 1 && p.Tbot != 0 && p.Tbot != 1) { h->err = "temperature tracers need Tbot = 0 or 1"; return TC_ERR_ARG; }
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
     if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;

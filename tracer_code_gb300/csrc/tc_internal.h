@@ -122,7 +122,7 @@ void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, doubl
 void launch_restrict_vis(cudaStream_t s, const Level& coarse, const Level& fine, const double* vfine, double* vcoarse);
 void launch_vis_bcs_init(cudaStream_t s, const Level& coarse, double* v, int RaT_nonzero, double visT2);
 void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int ivis, double courant_stream,
-                        int cheb_level);
+                        int cheb_level, bool with_dt = true);
 void launch_sweep(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, double c_uniform,
                   int per_point, double temp, int Vbc);
 void launch_residual(cudaStream_t s, const Level& lv, const double* S, RedScratch rs, double* res_out);

@@ -95,7 +95,8 @@ def initial_composition(p: Params, nx: int | None = None, nz: int | None = None)
     ds = 1.0 / nz
     z = np.arange(-span, nz + span + 1, dtype=np.float64) * ds
     Cn = np.zeros((nz + 1 + 2 * span, nx + 1 + 2 * span, p.ntype), dtype=np.float64)
-    Cn[:, :, 0] = np.where(z <= p.dlayer, 1.0, 0.0)[:, None]
+    if p.ntype > 0:
+        Cn[:, :, 0] = np.where(z <= p.dlayer, 1.0, 0.0)[:, None]
     return np.ascontiguousarray(Cn)
 
 
