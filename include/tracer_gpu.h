@@ -43,7 +43,7 @@ extern "C" {
 #endif
 
 #define TC_MAX_TYPES 4
-#define TC_ABI_VERSION 3
+#define TC_ABI_VERSION 4
 
 /* Status codes.  Each reference `stop` site has its own code. */
 typedef enum tc_status {
@@ -60,14 +60,16 @@ typedef enum tc_status {
     TC_ERR_STATE = 10,           /* call order violated (e.g. step before upload)           */
     TC_ERR_SINGULAR = 11,        /* zero pivot in the coarsest-grid banded LU (DGBTRF INFO>0) */
     TC_ERR_TOO_LARGE = 12,       /* input larger than the fixed buffer of an allocation-free call */
-    TC_ERR_DEVICE_TIMEOUT = 13   /* a bounded wait inside a kernel gave up (the kernel returned; the
+    TC_ERR_DEVICE_TIMEOUT = 13,  /* a bounded wait inside a kernel gave up (the kernel returned; the
                                     handle's results are invalid, the CUDA context stays usable) */
+    TC_ERR_EQUALIZE = 14         /* "# of donor tracers found inconsistent with nfree value"
+                                    composition.f90:366-369 */
 } tc_status;
 
 /*
  * Inputs of main.f90:8-116 that the hot path reads.  Field names follow the
  * reference.  Fixed by this implementation (not parameters): Database=2,
- * iterate=1, local_time=0, equalize=0 (see tc_create).
+ * iterate=1, local_time=0 (see tc_create).
  */
 typedef struct tc_params {
     /* grid options (main.f90:9-21) */
@@ -151,6 +153,14 @@ typedef struct tc_params {
      * conduction + heating by tracer_space, energy.f90:82-115) and the grid
      * T is their per-volume mean (Tratio).  Works with comp = 0 or 1. */
     int32_t tracer;
+    /* Tracer repositioning, TRA (equalize_tracers, composition.f90:83-580;
+     * main.f90:55): 1 = before every energy_time, move the excess tracers of
+     * over-full control volumes to the poorest volumes by the reference's
+     * lottery.  Its random streams (mzran, one per OpenMP thread, seeded as
+     * basics.f90:198-212) and its work split follow the reference run with
+     * equalize_threads OpenMP threads (static schedule); 0 means 1. */
+    int32_t equalize;
+    int32_t equalize_threads;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
@@ -220,6 +230,13 @@ tc_status tc_download_state(tc_handle* h, double* T, double* Cnew, double* SF,
 tc_status tc_upload_state_ex(tc_handle* h, const double* T, const double* Cnew, const double* SF,
                              const double* rtr, const double* str, const int32_t* Ttype,
                              const double* Ttr, int64_t ntr);
+/* The equalize.dat values of the last tracer repositioning (equalize = 1,
+ * composition.f90:559-574): out[0] = n = ntype+1, then tpc_type(0:ntype)
+ * (tpc when comp = 0), minexcess(0:ntype), the sum of the deficits
+ * (nexcess <= 0), the tracers moved, nfree and count_display(0:ntype);
+ * *len = 0 when the last call found every volume on its target (the
+ * reference then writes no row).  TC_ERR_ARG if cap is too small. */
+tc_status tc_equalize_row(const tc_handle* h, int64_t* out, int32_t cap, int32_t* len);
 /* Ttr(1:ntr) in the reference's tracer order (tracer = 1; TC_ERR_ARG otherwise). */
 tc_status tc_download_tracer_temperature(tc_handle* h, double* Ttr);
 
@@ -264,6 +281,9 @@ tc_status tc_restart_tracers_read(const char* path, int64_t ntr, double* rtr, do
  * comp = 0, where the reference writes none).  Both write a NUL-terminated
  * line without its newline; TC_ERR_TOO_LARGE if it does not fit in cap. */
 int32_t tc_format_g(double x, int32_t w, int32_t d, int32_t e, char* out);
+/* The equalize.dat row '(g20.8,15(i10))' (composition.f90:568-574) of a
+ * tc_equalize_row result at `time`. */
+tc_status tc_format_equalize_line(double time, const int64_t* row, int32_t len, char* buf, int32_t cap);
 tc_status tc_format_stats_line(const tc_stats_row* row, int32_t comp, int32_t tracer, int32_t ntype, double RaT,
                                char* buf, int32_t cap);
 tc_status tc_format_vis_line(const tc_stats_row* row, int32_t comp, int32_t ntype, double RaT, char* buf,

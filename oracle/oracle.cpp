@@ -165,6 +165,13 @@ struct Oracle {
     std::vector<double> Ttr, Ttr0, Ttr1, Ttr2;
     Arr Tratio, Textend, tsa;  // tsa = tracer_space_array (-si:nx+si, -si:nz+si)
     std::vector<Arr> DERr_tracer;
+    // tracer repositioning (equalize = 1): the mzran state of each OpenMP
+    // thread of the reproduced run, Cinit, and the last equalize.dat row
+    int eq_T = 1;
+    std::vector<int32_t> sd_i, sd_j, sd_k, sd_n;
+    double Cinit[TC_MAX_TYPES] = {};
+    long nequalize = 0;
+    std::vector<int64_t> eq_row;  // see tco_equalize_row
     // module state
     double time = 0, dt = 0;
     int tstep = 0, kent = 0;
@@ -619,6 +626,11 @@ struct Oracle {
         nx = p.nx; nz = p.nz; grids = p.grids;
         comp = p.comp;
         tracer = p.tracer;
+        if (p.equalize != 0 && p.equalize != 1) return TC_ERR_ARG;
+        if (p.equalize == 1 && p.comp == 0 && p.tracer == 0) return TC_ERR_ARG;
+        eq_T = (p.equalize_threads > 0) ? p.equalize_threads : 1;
+        if (eq_T > 1024) return TC_ERR_ARG;
+        seed_ranks();
         compute_smoothing_parameters();
         multigrid_setup();
         compute_basics();
@@ -1758,11 +1770,357 @@ struct Oracle {
                 else { T(i, k) = T(i, k) + 2.0 * temp; Tout(i, k) = T0(i, k) + factor * temp; }
             }
     }
+    // =====================================================================
+    // tracer repositioning, TRA (composition.f90:7-580)
+    // =====================================================================
+    // initial mzran seeds of each OpenMP thread (basics.f90:198-212)
+    void seed_ranks() {
+        sd_i.assign(eq_T, 0); sd_j.assign(eq_T, 0); sd_k.assign(eq_T, 0); sd_n.assign(eq_T, 0);
+        sd_i[0] = 521288629; sd_j[0] = 362436069; sd_k[0] = 16163801; sd_n[0] = 1131199299;
+        for (int j = 1; j < eq_T; j++) {
+            int32_t r = sd_i[j - 1] - sd_k[j - 1];
+            if (r < 0) r += 2147483579;
+            sd_i[j] = sd_j[j - 1];
+            sd_j[j] = sd_k[j - 1];
+            sd_k[j] = r;
+            sd_n[j] = (int32_t)(69069u * (uint32_t)sd_n[j - 1] + 1013904243u);
+        }
+    }
+    // mzran (composition.f90:7-20); 32-bit integers wrap
+    double mzran(int rank) {
+        int32_t r = sd_i[rank] - sd_k[rank];
+        if (r < 0) r += 2147483579;
+        sd_i[rank] = sd_j[rank];
+        sd_j[rank] = sd_k[rank];
+        sd_k[rank] = r;
+        sd_n[rank] = (int32_t)(69069u * (uint32_t)sd_n[rank] + 1013904243u);
+        r = (int32_t)((uint32_t)r + (uint32_t)sd_n[rank]);
+        return 0.5 + (0.2328306e-9) * (double)r;
+    }
+    // shuffle_serial (composition.f90:22-34) on a(istart:N), `a` indexed absolutely
+    void shuffle_serial(int* a, int istart, int N, int rank) {
+        for (int i = istart; i <= N - 1; i++) {
+            const double ran = mzran(rank);
+            const int r = (int)std::floor(ran * (double)(N - i)) + i + 1;
+            std::swap(a[i], a[r]);
+        }
+    }
+    // iterations of thread t in a static-schedule OpenMP loop over N iterations
+    void omp_static(int N, int t, int& lo, int& cnt) const {
+        const int q = N / eq_T, r = N % eq_T;
+        if (t < r) { cnt = q + 1; lo = t * cnt; } else { cnt = q; lo = t * q + r; }
+    }
+    int minval_masked(const std::vector<int>& nex, int t, bool use_type) const {
+        int m = 2147483647;  // Fortran minval of an empty selection: HUGE
+        for (int i = 0; i <= nx; i++)
+            for (int k = 0; k <= nz; k++) {
+                const int v = nex[(size_t)i * (nz + 1) + k];
+                if (v > 0) continue;
+                if (use_type) {
+                    if (t == 0) {
+                        double sC = 0.0;
+                        for (int j = 0; j < ntype; j++) sC = sC + Cnew[j](i, k);
+                        if (sC != 0.0) continue;
+                    } else if (Cnew[t - 1](i, k) != 1.0) continue;
+                }
+                m = std::min(m, v);
+            }
+        return m;
+    }
+    int maxloc_type(int i, int k) {
+        int best = 0;
+        for (int t = 1; t <= ntype; t++)
+            if (count_type[t](i, k) > count_type[best](i, k)) best = t;
+        return best;
+    }
+    // equalize_tracers (composition.f90:83-580) with eq_T OpenMP threads
+    int equalize_tracers() {
+        const int NT = ntype + 1, NR = eq_T;
+        const size_t ncell = (size_t)(nx + 1) * (nz + 1);
+        auto C = [&](int i, int k) { return (size_t)i * (nz + 1) + k; };
+        std::vector<long> Nideal(NT, 0);
+        if (comp == 1) {
+            long s = 0;
+            for (int t = 1; t <= ntype; t++) { Nideal[t] = std::lround(Cinit[t - 1] * (double)ntr); s += Nideal[t]; }
+            Nideal[0] = ntr - s;
+        } else Nideal[0] = ntr;
+        // ---- excess tracers per corner volume ----
+        std::vector<int> nex(ncell, 0), tpc_type(NT, 0);
+        if (comp == 0) {
+            tpc_type[0] = p.tpc;
+            for (int i = 0; i <= nx; i++)
+                for (int k = 0; k <= nz; k++) nex[C(i, k)] = (nempty(i, k) > 0) ? nempty(i, k) - p.tpc : 0;
+        } else {
+            for (int t = 0; t <= ntype; t++) {
+                long cnt = 0, sum = 0;
+                for (int i = 0; i <= nx; i++)
+                    for (int k = 0; k <= nz; k++) {
+                        bool m;
+                        if (t == 0) {
+                            double sC = 0.0;
+                            for (int j = 0; j < ntype; j++) sC = sC + Cnew[j](i, k);
+                            m = (sC == 0.0);
+                        } else m = (Cnew[t - 1](i, k) == 1.0);
+                        if (m) { cnt++; sum += count_type[t](i, k); }
+                    }
+                tpc_type[t] = (cnt > 0) ? (int)std::lround((double)sum / (double)cnt) : 0;
+            }
+            for (int i = 0; i <= nx; i++)
+                for (int k = 0; k <= nz; k++) {
+                    nex[C(i, k)] = 0;
+                    for (int t = 0; t <= ntype; t++) {
+                        bool all = true;
+                        for (int a = -1; a <= 1 && all; a++)
+                            for (int b = -1; b <= 1 && all; b++)
+                                if (count_type[t](i + a, k + b) != nempty(i + a, k + b)) all = false;
+                        if (all && nempty(i, k) > 0) { nex[C(i, k)] = nempty(i, k) - tpc_type[t]; break; }
+                    }
+                }
+        }
+        long nfree = 0;
+        bool allzero = true;
+        for (size_t c = 0; c < ncell; c++) { if (nex[c] > 0) nfree += nex[c]; if (nex[c] != 0) allzero = false; }
+        eq_row.clear();
+        if (allzero) return TC_OK;
+        nequalize++;
+        // ---- tracer ids by corner volume, ascending, then shuffled ----
+        std::vector<long> off(ncell + 1, 0);
+        for (int i = 0; i <= nx; i++)
+            for (int k = 0; k <= nz; k++) off[C(i, k) + 1] = nempty(i, k);
+        for (size_t c = 0; c < ncell; c++) off[c + 1] += off[c];
+        std::vector<int> ids((size_t)off[ncell] + 1, 0), counter(ncell, 0);
+        for (long id = 0; id < ntr; id++) {
+            const int i = (int)std::lround(rtr[id] / dr), k = (int)std::lround(str[id] / ds);
+            const size_t c = C(i, k);
+            counter[c]++;
+            ids[(size_t)off[c] + counter[c] - 1] = (int)id + 1;  // Fortran ids
+        }
+        auto list = [&](size_t c) { return &ids[(size_t)off[c]] - 1; };  // list(c)[1..counter]
+        for (int t = 0; t < NR; t++) {
+            int lo, cnt;
+            omp_static(nx + 1, t, lo, cnt);
+            for (int i = lo; i < lo + cnt; i++)
+                for (int k = 0; k <= nz; k++) shuffle_serial(list(C(i, k)), 1, counter[C(i, k)], t);
+        }
+        // ---- temperature interpolant (temperature tracers) ----
+        Arr Tdumb;
+        std::vector<Arr> DERr_T;
+        if (tracer == 1) {
+            extendT(Tratio);
+            const int si = span_interp;
+            Tdumb.alloc(-si, nx + si, -si, nz + si);
+            for (int i = -si; i <= nx + si; i++)
+                for (int k = -si; k <= nz + si; k++) Tdumb(i, k) = Textend(i, k);
+            DERr_T.assign(order, Arr());
+            for (int j = 1; j <= order - 1; j++) DERr_T[j].alloc(0, nx, -si, nz + si);
+            compute_derivatives(Tdumb, DERr_T);
+        }
+        // ---- donor tracers ----
+        const size_t cap = (size_t)nfree + 1;
+        std::vector<int> donor((size_t)NR * NT * cap, 0);
+        auto D = [&](int rank, int t) { return &donor[((size_t)rank * NT + t) * cap]; };  // D(rank,t)[1..]
+        std::vector<int> isv((size_t)NR * NT, 0), isv2;
+        auto IS = [&](int rank, int t) -> int& { return isv[(size_t)rank * NT + t]; };
+        auto take = [&](size_t c, int rank, bool near_wall_only, bool near_wall) {
+            if (nex[c] <= 0) return;
+            for (int q = 1; q <= counter[c]; q++) {
+                const int ID = list(c)[q];
+                const double r = rtr[ID - 1], sv = str[ID - 1];
+                const bool nw = (sv < dist_s) || (sv > 1.0 - dist_s) || (r < dist_r) || (r > p.aspect - dist_r);
+                if (near_wall_only && nw != near_wall) continue;
+                const int t = Ttype[ID - 1];
+                IS(rank, t) = IS(rank, t) + 1;
+                D(rank, t)[IS(rank, t)] = ID;
+                nex[c] = nex[c] - 1;
+                if (nex[c] == 0) break;
+            }
+        };
+        auto edges = [&](bool near_wall) {
+            for (int i = 0; i <= nx; i += nx) {  // left and right columns, split over k
+                for (int t = 0; t < NR; t++) {
+                    int lo, cnt;
+                    omp_static(nz + 1, t, lo, cnt);
+                    for (int k = lo; k < lo + cnt; k++) take(C(i, k), t, true, near_wall);
+                }
+                if (nx == 0) break;
+            }
+            for (int k = 0; k <= nz; k += nz) {  // bottom and top rows, corners done, split over i
+                for (int t = 0; t < NR; t++) {
+                    int lo, cnt;
+                    omp_static(nx - 1, t, lo, cnt);
+                    for (int i = 1 + lo; i < 1 + lo + cnt; i++) take(C(i, k), t, true, near_wall);
+                }
+                if (nz == 0) break;
+            }
+        };
+        edges(true);
+        for (int t = 0; t < NR; t++)
+            for (int tt = 0; tt < NT; tt++) shuffle_serial(D(t, tt), 1, IS(t, tt), t);
+        isv2 = isv;
+        edges(false);
+        for (int t = 0; t < NR; t++) {  // interior volumes, split over i
+            int lo, cnt;
+            omp_static(nx - 1, t, lo, cnt);
+            for (int i = 1 + lo; i < 1 + lo + cnt; i++)
+                for (int k = 1; k <= nz - 1; k++) take(C(i, k), t, false, false);
+        }
+        std::vector<int> nfree_rank = isv;  // count(donor > 0) per rank and type
+        long found = 0;
+        for (int v : nfree_rank) found += v;
+        if (found != nfree) return TC_ERR_EQUALIZE;
+        for (int t = 0; t < NR; t++)
+            for (int tt = 0; tt < NT; tt++)
+                shuffle_serial(D(t, tt), isv2[(size_t)t * NT + tt] + 1, IS(t, tt), t);
+        // ---- lottery: donors to the poorest volumes ----
+        std::vector<int> nx_loop(nx + 1), nz_loop(nz + 1);
+        for (int i = 0; i <= nx; i++) nx_loop[i] = i;
+        for (int k = 0; k <= nz; k++) nz_loop[k] = k;
+        std::fill(isv.begin(), isv.end(), 0);
+        std::vector<long> tcount(NT, 0);
+        auto count_all = [&]() {
+            for (int t = 0; t < NT; t++) {
+                long s = 0;
+                for (int i = 0; i <= nx; i++)
+                    for (int k = 0; k <= nz; k++) s += count_type[t](i, k);
+                tcount[t] = s;
+            }
+        };
+        auto all_ideal = [&]() { for (int t = 0; t < NT; t++) if (tcount[t] != Nideal[t]) return false; return true; };
+        std::vector<int> minex(NT, 0);
+        auto minexcess = [&](bool reference_typo) {
+            minex[0] = (tpc_type[0] > 0) ? minval_masked(nex, 0, comp == 1) : 0;
+            for (int t = 1; t <= ntype; t++)
+                minex[t] = ((reference_typo ? tpc_type[0] : tpc_type[t]) > 0) ? minval_masked(nex, t, true) : 0;
+        };
+        auto place = [&](int rank, int t, int i, int k) -> int {
+            const double r = dr * (double)i, sv = ds * (double)k;
+            double pr = mzran(rank), ps = mzran(rank);
+            pr = (pr - 0.5) * dr;
+            ps = (ps - 0.5) * ds;
+            IS(rank, t) = IS(rank, t) + 1;
+            const int ID = D(rank, t)[IS(rank, t)];
+            double& R = rtr[ID - 1];
+            double& S = str[ID - 1];
+            R = r + pr;
+            S = sv + ps;
+            if (R <= 0.0) R = dist_r;
+            if (R >= p.aspect) R = p.aspect - dist_r;
+            if (S <= 0.0) S = dist_s;
+            if (S >= 1.0) S = 1.0 - dist_s;
+            return ID;
+        };
+        long sum_nfree = 0;
+        for (int v : nfree_rank) sum_nfree += v;
+        auto sum_isv = [&]() { long s = 0; for (int v : isv) s += v; return s; };
+        int escape = 0;
+        count_all();
+        if (all_ideal()) escape = 1;
+        int tt_priv[1024];  // each thread's private tt keeps its value across cells and passes
+        for (int t = 0; t < NR; t++) tt_priv[t] = 0;
+        for (;;) {
+            if (escape == 0) { count_all(); if (all_ideal()) escape = 1; }
+            minexcess(false);
+            bool allz = true;
+            for (int t = 0; t < NT; t++) if (minex[t] != 0) allz = false;
+            if (allz) break;
+            if (sum_isv() >= nfree) break;
+            isv2 = isv;
+            shuffle_serial(nx_loop.data(), 0, nx, 0);
+            shuffle_serial(nz_loop.data(), 0, nz, 0);
+            for (int rank = 0; rank < NR; rank++) {
+                int lo, cnt;
+                omp_static(nx + 1, rank, lo, cnt);
+                for (int ii = lo; ii < lo + cnt; ii++) {
+                    const int i = nx_loop[ii];
+                    for (int kk = 0; kk <= nz; kk++) {
+                        const int k = nz_loop[kk];
+                        const int type_save = maxloc_type(i, k);
+                        int& tt = tt_priv[rank];
+                        if (escape == 0) {
+                            for (int q = 0; q < NT; q++) if (tcount[q] > Nideal[q]) { tt = q; break; }
+                        } else tt = type_save;
+                        const size_t c = C(i, k);
+                        if (nex[c] == minex[type_save] && IS(rank, tt) < nfree_rank[(size_t)rank * NT + tt] && nex[c] < 0) {
+                            const int ID = place(rank, tt, i, k);
+                            if (comp == 1) Ttype[ID - 1] = type_save;
+                            count_type[tt](i, k) = count_type[tt](i, k) - 1;
+                            count_type[Ttype[ID - 1]](i, k) = count_type[Ttype[ID - 1]](i, k) + 1;
+                            nex[c] = nex[c] + 1;
+                        }
+                    }
+                }
+            }
+            if (isv == isv2) break;
+        }
+        // ---- remaining donors in serial, alternating between ranks ----
+        int rk = 0;
+        for (;;) {
+            minexcess(true);
+            bool allz = true;
+            for (int t = 0; t < NT; t++) if (minex[t] != 0) allz = false;
+            if (allz) break;
+            if (sum_isv() >= nfree) break;
+            isv2 = isv;
+            rk = 0;
+            shuffle_serial(nx_loop.data(), 0, nx, 0);
+            shuffle_serial(nz_loop.data(), 0, nz, 0);
+            for (int ii = 0; ii <= nx; ii++) {
+                const int i = nx_loop[ii];
+                for (int kk = 0; kk <= nz; kk++) {
+                    const int k = nz_loop[kk];
+                    const int tt = maxloc_type(i, k);
+                    long used = 0, avail = 0;
+                    for (int q = 0; q < NR; q++) { used += IS(q, tt); avail += nfree_rank[(size_t)q * NT + tt]; }
+                    const size_t c = C(i, k);
+                    if (nex[c] == minex[tt] && used < avail && nex[c] < 0) {
+                        for (;;) {
+                            rk = rk + 1;
+                            if (rk == NR) rk = 0;
+                            if (IS(rk, tt) < nfree_rank[(size_t)rk * NT + tt]) break;
+                        }
+                        const int ID = place(rk, tt, i, k);
+                        if (comp == 1) Ttype[ID - 1] = maxloc_type(i, k);
+                        nex[c] = nex[c] + 1;
+                    }
+                }
+            }
+            if (isv == isv2) break;
+        }
+        // ---- temperatures of the moved tracers ----
+        if (tracer == 1)
+            for (int t = 0; t < NR; t++)
+                for (int tt = 0; tt < NT; tt++)
+                    for (int q = 1; q <= IS(t, tt); q++) {
+                        const int ID = D(t, tt)[q];
+                        Ttr[ID - 1] = interpolate(rtr[ID - 1], str[ID - 1], DERr_T, Tdumb);
+                    }
+        // ---- the equalize.dat row (composition.f90:545-574) ----
+        if (comp == 0) minex[0] = minval_masked(nex, 0, false);
+        else for (int t = 0; t <= ntype; t++) minex[t] = minval_masked(nex, t, true);
+        long deficit = 0;
+        for (size_t c = 0; c < ncell; c++) if (nex[c] <= 0) deficit += nex[c];
+        eq_row.clear();
+        eq_row.push_back(NT);
+        for (int t = 0; t < NT; t++) eq_row.push_back(comp == 0 ? p.tpc : tpc_type[t]);
+        for (int t = 0; t < NT; t++) eq_row.push_back(minex[t]);
+        eq_row.push_back(deficit);
+        eq_row.push_back(sum_isv());
+        eq_row.push_back(nfree);
+        count_all();
+        for (int t = 0; t < NT; t++) eq_row.push_back(tcount[t]);
+        (void)sum_nfree;
+        smooth_vis = 0;
+        int st = tracers_to_corners(rtr, str, tracer == 1 ? Ttr.data() : nullptr, &T);
+        smooth_vis = 1;
+        return st;
+    }
+
     // energy_time (energy.f90:117-453) for comp = 0 or 1, tracer = 0 or 1,
     // local_time = 0, equalize = 0.
     int energy_time() {
         int st = stability_RK4();
         if (st) return st;
+        if (p.equalize == 1) { st = equalize_tracers(); if (st) return st; }
         std::vector<Arr> C0 = Cnew;
         const bool tt = (tracer == 1);
         const bool trc = (comp == 1) || tt;
@@ -1979,6 +2337,8 @@ struct Oracle {
         row->time = time;
         row->tstep = tstep;
         row->n_eta = n_eta; row->n_temp = n_temp; row->eig_fine = eig_fine;
+        if (time == 0.0 && p.equalize == 1)
+            for (int t = 0; t < ntype; t++) Cinit[t] = row->Cavg[t];
         for (int t = 0; t < TC_MAX_TYPES; t++) row->n_comp[t] = n_comp[t];
     }
 
@@ -2107,6 +2467,16 @@ int tco_upload_state(void* h, const double* T, const double* C, const double* SF
 int tco_upload_state_ex(void* h, const double* T, const double* C, const double* SF, const double* r,
                         const double* s, const int32_t* tt, const double* Ttr, int64_t n) {
     return ((Oracle*)h)->upload(T, C, SF, r, s, tt, (long)n, Ttr);
+}
+// the last equalize.dat row: n = ntype+1, then tpc_type[n], minexcess[n],
+// sum of deficits, tracers moved, nfree, count_display[n]; *len = 0 if the
+// last call found nothing to move
+int tco_equalize_row(void* h, int64_t* out, int32_t cap, int32_t* len) {
+    Oracle* o = (Oracle*)h;
+    if (!len || (int32_t)o->eq_row.size() > cap) return TC_ERR_ARG;
+    for (size_t q = 0; q < o->eq_row.size(); q++) out[q] = o->eq_row[q];
+    *len = (int32_t)o->eq_row.size();
+    return TC_OK;
 }
 int tco_download_ttr(void* h, double* out) {
     Oracle* o = (Oracle*)h;

@@ -48,6 +48,7 @@ def lib():
             L.tco_download_state.argtypes = [vp, vp, vp, vp, vp, vp, vp]
             L.tco_upload_state_ex.argtypes = [vp, vp, vp, vp, vp, vp, vp, vp, C.c_int64]
             L.tco_download_ttr.argtypes = [vp, vp]
+            L.tco_equalize_row.argtypes = [vp, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]
             L.tco_set_clock.argtypes = [vp, C.c_int32, C.c_double]
             L.tco_multigrid.argtypes = [vp, C.POINTER(C.c_int32)]
             L.tco_compute_velocities.argtypes = [vp]
@@ -293,3 +294,8 @@ class Oracle:
         rowb = np.empty(n)
         self.L.tco_coarse_matrix(self.h, band, rowb)
         return band.reshape(n, ldab), rowb
+
+    def equalize_row(self) -> list:
+        out = (C.c_int64 * 64)(); n = C.c_int32(0)
+        self._chk(self.L.tco_equalize_row(self.h, out, 64, C.byref(n)), "equalize_row")
+        return [int(out[q]) for q in range(n.value)]

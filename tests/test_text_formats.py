@@ -99,3 +99,12 @@ def test_branch_layouts(tio):
 ])
 def test_g_edit_rules(tio, x, w, d, e, want):
     assert tio.format_g(x, w, d, e) == want
+
+
+def test_shipped_equalize_rows_come_back_byte_for_byte(tio, golden):
+    """equalize.dat '(g20.8,15(i10))' (composition.f90:568-574), comp = 0:
+    time, tpc, minexcess(0), deficits, moved, nfree, count_display(0)."""
+    for line in golden["text_lines"]["equalize.dat"]:
+        f = fields(line, SPECS["equalize.dat"])
+        row = [1] + [int(v) for v in f[1:]]
+        assert tio.equalize_line(float(f[0]), row) == line

@@ -36,6 +36,7 @@ EXPORTS = [
     "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
     "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
     "tc_format_vis_line", "tc_write_snapshot", "tc_upload_state_ex", "tc_download_tracer_temperature",
+    "tc_equalize_row", "tc_format_equalize_line",
 ]
 
 
@@ -104,6 +105,8 @@ def load_library(build_if_missing: bool = False):
         L.tc_format_stats_line.argtypes = [C.POINTER(StatsRow), i32, i32, i32, C.c_double, C.c_char_p, i32]
         L.tc_format_vis_line.argtypes = [C.POINTER(StatsRow), i32, i32, C.c_double, C.c_char_p, i32]
         L.tc_write_snapshot.argtypes = [vp, cs]
+        L.tc_equalize_row.argtypes = [vp, C.POINTER(C.c_int64), i32, C.POINTER(i32)]
+        L.tc_format_equalize_line.argtypes = [C.c_double, C.POINTER(C.c_int64), i32, C.c_char_p, i32]
         L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
@@ -340,3 +343,9 @@ class Simulation:
     def write_snapshot(self, path: str) -> None:
         """snapshots (main.f90:237-270): the T1xxxx text file of the current state (call after stats)."""
         self._chk(self.L.tc_write_snapshot(self.h, os.fsencode(path)), "write_snapshot")
+
+    def equalize_row(self) -> list:
+        """The equalize.dat values of the last tracer repositioning (tc_equalize_row); [] if none."""
+        out = (C.c_int64 * 64)(); n = C.c_int32(0)
+        self._chk(self.L.tc_equalize_row(self.h, out, 64, C.byref(n)), "equalize_row")
+        return [int(out[q]) for q in range(n.value)]

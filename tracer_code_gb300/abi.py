@@ -25,6 +25,7 @@ STATUS = {
     11: "TC_ERR_SINGULAR",
     12: "TC_ERR_TOO_LARGE",
     13: "TC_ERR_DEVICE_TIMEOUT",
+    14: "TC_ERR_EQUALIZE",
 }
 
 # Reference `stop` messages that each status replaces.
@@ -33,6 +34,7 @@ STOP_MESSAGES = {
     4: "Multigrid Convergence Problem: Abnormally High Residual Detected -- stopping",
     5: "Tracer advected outside of domain - stopping",
     6: "Advective Eigenvalues Exceed Diffusive Eigenvalues -- this does not work for RK2",
+    14: "Error: # of donor tracers found inconsistent with nfree value",
 }
 
 
@@ -71,7 +73,8 @@ class Params(C.Structure):
         ("delta_visT", C.c_double), ("yield_", C.c_double), ("yield_gradient", C.c_double),
         ("yield_depth", C.c_double), ("visC", _D4), ("delta_visC", _D4),
         ("mg_zero_coarse", C.c_int32), ("solver_precision", C.c_int32), ("learned_guess", C.c_int32), ("learned_smooth", C.c_int32),
-        ("tracer_sort_interval", C.c_int32), ("tracer", C.c_int32),
+        ("tracer_sort_interval", C.c_int32), ("tracer", C.c_int32), ("equalize", C.c_int32),
+        ("equalize_threads", C.c_int32),
     ]
 
     def copy(self) -> "Params":

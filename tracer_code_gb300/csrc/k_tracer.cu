@@ -458,3 +458,587 @@ void launch_iota(cudaStream_t s, int64_t n, int* p) {
     if (n <= 0) return;
     k_iota<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, p); tc_note_launch();
 }
+
+// ---- tracer repositioning, TRA (composition.f90:7-580) ----------------------
+// The reference runs equalize_tracers with OpenMP threads, each drawing from
+// its own mzran stream over a static-schedule share of each loop; its result
+// depends on the thread count.  Here each of its NR threads is one GPU
+// thread: the per-volume shuffles run as NR threads over their shares, and
+// the donor search, the lottery passes and the serial remainder run in one
+// block whose first NR threads are the ranks (all threads take part in the
+// reductions between passes).  Every loop is bounded.
+namespace {
+
+__device__ __forceinline__ double eq_mzran(int* sd, int rank, int NR) {
+    int* si = sd;
+    int* sj = sd + NR;
+    int* sk = sd + 2 * NR;
+    int* sn = sd + 3 * NR;
+    int r = si[rank] - sk[rank];
+    if (r < 0) r += 2147483579;
+    si[rank] = sj[rank];
+    sj[rank] = sk[rank];
+    sk[rank] = r;
+    sn[rank] = (int)(69069u * (unsigned)sn[rank] + 1013904243u);
+    r = (int)((unsigned)r + (unsigned)sn[rank]);
+    return 0.5 + (0.2328306e-9) * (double)r;
+}
+// shuffle_serial on a(istart:N), `a` indexed absolutely
+__device__ void eq_shuffle(int* a, int istart, int N, int* sd, int rank, int NR) {
+    for (int i = istart; i <= N - 1; i++) {
+        const double ran = eq_mzran(sd, rank, NR);
+        const int r = (int)floor(ran * (double)(N - i)) + i + 1;
+        const int t = a[i];
+        a[i] = a[r];
+        a[r] = t;
+    }
+}
+// iterations [lo, lo+cnt) of thread t in a static OpenMP loop of N iterations
+__device__ __forceinline__ void eq_static(int N, int NR, int t, int& lo, int& cnt) {
+    const int q = N / NR, r = N % NR;
+    if (t < r) { cnt = q + 1; lo = t * cnt; } else { cnt = q; lo = t * q + r; }
+}
+
+struct EqDev {
+    Lay L;
+    int nx, nz, ntype, NT, NR, comp, tracer, tpc;
+    int64_t ntr;
+    double dr, ds, aspect, dist_r, dist_s;
+    int* counts;       // count_type (L1 planes per type)
+    const int* nempty; // L1
+    CPtrs C;           // Cnew per type (L1)
+    double* rtr;       // slot order
+    double* str;
+    int* ttype;
+    const int* perm;   // slot -> reference index
+    int* iperm;        // reference index -> slot
+    int* nex;          // (nx+1)*(nz+1), i-major
+    int* off;          // (nx+1)*(nz+1)+1
+    int* cur;          // per-volume cursors
+    int* ids;          // per-volume lists of reference ids (1-based)
+    int* sd;           // mzran state [4][NR]
+    int* donor;        // [NR][NT][cap]
+    int64_t cap;
+    int* isv;          // index_save [NR][NT]
+    int* isv2;
+    int* nfr;          // nfree_rank [NR][NT]
+    int* nx_loop;
+    int* nz_loop;
+    long long* sc;     // scalars, see EQ_*
+};
+enum { EQ_NFREE = 0, EQ_NONZERO, EQ_DEFICIT, EQ_MOVED, EQ_ERR, EQ_PASSES, EQ_TPC0, EQ_MIN0 = EQ_TPC0 + 8,
+       EQ_COUNT0 = EQ_MIN0 + 8, EQ_NIDEAL0 = EQ_COUNT0 + 8, EQ_TSUM0 = EQ_NIDEAL0 + 8, EQ_TCNT0 = EQ_TSUM0 + 8,
+       EQ_NSC = EQ_TCNT0 + 8 };
+
+__device__ __forceinline__ size_t eq_cell(const EqDev& E, int i, int k) { return (size_t)i * (E.nz + 1) + k; }
+__device__ __forceinline__ int eq_count(const EqDev& E, int t, int i, int k) {
+    return E.counts[(size_t)t * E.L.plane + IX(E.L, i, k)];
+}
+__device__ __forceinline__ bool eq_type_mask(const EqDev& E, int t, int i, int k) {
+    const size_t x = IX(E.L, i, k);
+    if (t == 0) {
+        double sC = 0.0;
+        for (int j = 0; j < E.ntype; j++) sC = sC + E.C.p[j][x];
+        return sC == 0.0;
+    }
+    return E.C.p[t - 1][x] == 1.0;
+}
+
+// tpc_type sums over the pure volumes (comp = 1): per type, count and count_type sum
+__global__ void k_eq_tpc(EqDev E) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    if (c >= ncell) return;
+    const int i = c / (E.nz + 1), k = c % (E.nz + 1);
+    for (int t = 0; t < E.NT; t++)
+        if (eq_type_mask(E, t, i, k)) {
+            atomicAdd((unsigned long long*)&E.sc[EQ_TCNT0 + t], 1ULL);
+            atomicAdd((unsigned long long*)&E.sc[EQ_TSUM0 + t], (unsigned long long)eq_count(E, t, i, k));
+        }
+}
+// nexcess (composition.f90:114-160), nfree and whether any volume is off its target
+__global__ void k_eq_nexcess(EqDev E) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    if (c >= ncell) return;
+    const int i = c / (E.nz + 1), k = c % (E.nz + 1);
+    const int ne = E.nempty[IX(E.L, i, k)];
+    int v = 0;
+    if (E.comp == 0) {
+        v = (ne > 0) ? ne - E.tpc : 0;
+    } else {
+        for (int t = 0; t < E.NT; t++) {
+            bool all = true;
+            for (int a = -1; a <= 1 && all; a++)
+                for (int b = -1; b <= 1 && all; b++)
+                    if (eq_count(E, t, i + a, k + b) != E.nempty[IX(E.L, i + a, k + b)]) all = false;
+            if (all && ne > 0) {
+                const long long n = E.sc[EQ_TCNT0 + t];
+                const int tp = (n > 0) ? (int)llround((double)E.sc[EQ_TSUM0 + t] / (double)n) : 0;
+                v = ne - tp;
+                break;
+            }
+        }
+    }
+    E.nex[c] = v;
+    if (v > 0) atomicAdd((unsigned long long*)&E.sc[EQ_NFREE], (unsigned long long)v);
+    if (v != 0) atomicOr((unsigned long long*)&E.sc[EQ_NONZERO], 1ULL);
+}
+// per-volume lists of reference ids: scatter, then ascending order in each list
+__global__ void k_eq_offsets_in(EqDev E, int* cnt) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    if (c >= ncell) return;
+    cnt[c] = E.nempty[IX(E.L, c / (E.nz + 1), c % (E.nz + 1))];
+    E.cur[c] = 0;
+}
+__global__ void k_eq_scatter(EqDev E) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= E.ntr) return;
+    const int id = E.perm[j];
+    E.iperm[id] = (int)j;
+    const int i = (int)round(E.rtr[j] / E.dr), k = (int)round(E.str[j] / E.ds);
+    const size_t c = eq_cell(E, i, k);
+    const int pos = atomicAdd(E.cur + c, 1);
+    E.ids[E.off[c] + pos] = id + 1;
+}
+__global__ void k_eq_sort_lists(EqDev E) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    if (c >= ncell) return;
+    int* a = E.ids + E.off[c];
+    const int n = E.off[c + 1] - E.off[c];
+    for (int p = 1; p < n; p++) {
+        const int v = a[p];
+        int q = p - 1;
+        while (q >= 0 && a[q] > v) { a[q + 1] = a[q]; q--; }
+        a[q + 1] = v;
+    }
+}
+// composition.f90:188-199: each rank shuffles the lists of its share of columns
+__global__ void k_eq_shuffle_lists(EqDev E) {
+    const int rank = blockIdx.x * blockDim.x + threadIdx.x;
+    if (rank >= E.NR) return;
+    int lo, cnt;
+    eq_static(E.nx + 1, E.NR, rank, lo, cnt);
+    for (int i = lo; i < lo + cnt; i++)
+        for (int k = 0; k <= E.nz; k++) {
+            const size_t c = eq_cell(E, i, k);
+            eq_shuffle(E.ids + E.off[c] - 1, 1, E.off[c + 1] - E.off[c], E.sd, rank, E.NR);
+        }
+}
+
+__device__ __forceinline__ int* eq_D(const EqDev& E, int rank, int t) {
+    return E.donor + ((size_t)rank * E.NT + t) * (size_t)E.cap;
+}
+// donors of one volume: the first nexcess ids of its list (near_wall: only
+// those within dist of a wall, or only those away from every wall)
+__device__ void eq_take(const EqDev& E, int i, int k, int rank, int mode) {
+    const size_t c = eq_cell(E, i, k);
+    if (E.nex[c] <= 0) return;
+    const int* a = E.ids + E.off[c] - 1;
+    const int n = E.off[c + 1] - E.off[c];
+    for (int q = 1; q <= n; q++) {
+        const int ID = a[q];
+        const int slot = E.iperm[ID - 1];
+        const double r = E.rtr[slot], s = E.str[slot];
+        const bool nw = (s < E.dist_s) || (s > 1.0 - E.dist_s) || (r < E.dist_r) || (r > E.aspect - E.dist_r);
+        if (mode == 1 && !nw) continue;
+        if (mode == 2 && nw) continue;
+        const int t = E.ttype[slot];
+        int& is = E.isv[rank * E.NT + t];
+        is = is + 1;
+        eq_D(E, rank, t)[is] = ID;
+        E.nex[c] = E.nex[c] - 1;
+        if (E.nex[c] == 0) break;
+    }
+}
+// composition.f90:226-334: the left and right columns split over k, then the
+// bottom and top rows (corners excluded) split over i; every thread of the
+// block calls it (threads >= NR only meet the barriers)
+__device__ void eq_edges(const EqDev& E, int rank, int mode) {
+    const bool isrank = rank < E.NR;
+    for (int i = 0; i <= E.nx; i += E.nx) {
+        int lo = 0, cnt = 0;
+        if (isrank) eq_static(E.nz + 1, E.NR, rank, lo, cnt);
+        for (int k = lo; k < lo + cnt; k++) eq_take(E, i, k, rank, mode);
+        __syncthreads();
+    }
+    for (int k = 0; k <= E.nz; k += E.nz) {
+        int lo = 0, cnt = 0;
+        if (isrank) eq_static(E.nx - 1, E.NR, rank, lo, cnt);
+        for (int i = 1 + lo; i < 1 + lo + cnt; i++) eq_take(E, i, k, rank, mode);
+        __syncthreads();
+    }
+}
+__device__ int eq_maxloc(const EqDev& E, int i, int k) {
+    int best = 0;
+    for (int t = 1; t < E.NT; t++)
+        if (eq_count(E, t, i, k) > eq_count(E, best, i, k)) best = t;
+    return best;
+}
+// block-wide minval of nexcess <= 0 over the volumes of type mask t
+// (use_type false: all volumes); HUGE when none
+__device__ int eq_minval(const EqDev& E, int t, bool use_type, int* red) {
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    int m = 2147483647;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int v = E.nex[c];
+        if (v > 0) continue;
+        if (use_type && !eq_type_mask(E, t, c / (E.nz + 1), c % (E.nz + 1))) continue;
+        m = min(m, v);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int r = 2147483647;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r = min(r, red[w]);
+        red[32] = r;
+    }
+    __syncthreads();
+    const int r = red[32];
+    __syncthreads();
+    return r;
+}
+__device__ long long eq_blocksum(long long v, long long* red) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        long long r = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) r += red[w];
+        red[32] = r;
+    }
+    __syncthreads();
+    const long long r = red[32];
+    __syncthreads();
+    return r;
+}
+__device__ void eq_tracer_counts(const EqDev& E, long long* tc, long long* red) {
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    for (int t = 0; t < E.NT; t++) {
+        long long s = 0;
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) s += eq_count(E, t, c / (E.nz + 1), c % (E.nz + 1));
+        tc[t] = eq_blocksum(s, red);
+    }
+}
+// places donor `rank`,`t`'s next id at a random point of corner volume (i,k)
+__device__ int eq_place(const EqDev& E, int rank, int t, int i, int k) {
+    const double r = E.dr * (double)i, s = E.ds * (double)k;
+    double pr = eq_mzran(E.sd, rank, E.NR), ps = eq_mzran(E.sd, rank, E.NR);
+    pr = (pr - 0.5) * E.dr;
+    ps = (ps - 0.5) * E.ds;
+    int& is = E.isv[rank * E.NT + t];
+    is = is + 1;
+    const int ID = eq_D(E, rank, t)[is];
+    const int slot = E.iperm[ID - 1];
+    double R = r + pr, S = s + ps;
+    if (R <= 0.0) R = E.dist_r;
+    if (R >= E.aspect) R = E.aspect - E.dist_r;
+    if (S <= 0.0) S = E.dist_s;
+    if (S >= 1.0) S = 1.0 - E.dist_s;
+    E.rtr[slot] = R;
+    E.str[slot] = S;
+    return ID;
+}
+
+// donor search, lottery and serial remainder (composition.f90:226-543) in
+// one block; threads < NR are the ranks
+__global__ void __launch_bounds__(1024) k_eq_main(EqDev E, int64_t nfree) {
+    __shared__ long long redl[33];
+    __shared__ int redi[33];
+    __shared__ long long tcount[8];
+    __shared__ int minex[8];
+    __shared__ int flags[4];  // 0: escape, 1: stop, 2: changed
+    const int rank = threadIdx.x;
+    const bool isrank = rank < E.NR;
+    const int NT = E.NT, NR = E.NR;
+    // ---- donors near the walls of edge volumes, shuffled per rank ----
+    eq_edges(E, rank, 1);
+    if (isrank)
+        for (int t = 0; t < NT; t++) eq_shuffle(eq_D(E, rank, t), 1, E.isv[rank * NT + t], E.sd, rank, NR);
+    __syncthreads();
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) E.isv2[q] = E.isv[q];
+    __syncthreads();
+    // ---- the rest of the edge volumes, then the interior volumes ----
+    eq_edges(E, rank, 2);
+    if (isrank) {
+        int lo, cnt;
+        eq_static(E.nx - 1, NR, rank, lo, cnt);
+        for (int i = 1 + lo; i < 1 + lo + cnt; i++)
+            for (int k = 1; k <= E.nz - 1; k++) eq_take(E, i, k, rank, 0);
+    }
+    __syncthreads();
+    long long found = 0;
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) {
+        E.nfr[q] = E.isv[q];
+        found += E.isv[q];
+    }
+    found = eq_blocksum(found, redl);
+    if (found != nfree) {
+        if (threadIdx.x == 0) E.sc[EQ_ERR] = 1;
+        return;
+    }
+    if (isrank)
+        for (int t = 0; t < NT; t++)
+            eq_shuffle(eq_D(E, rank, t), E.isv2[rank * NT + t] + 1, E.isv[rank * NT + t], E.sd, rank, NR);
+    __syncthreads();
+    // ---- lottery ----
+    for (int i = threadIdx.x; i <= E.nx; i += blockDim.x) E.nx_loop[i] = i;
+    for (int k = threadIdx.x; k <= E.nz; k += blockDim.x) E.nz_loop[k] = k;
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) E.isv[q] = 0;
+    __syncthreads();
+    eq_tracer_counts(E, tcount, redl);
+    if (threadIdx.x == 0) {
+        bool ideal = true;
+        for (int t = 0; t < NT; t++) if (tcount[t] != E.sc[EQ_NIDEAL0 + t]) ideal = false;
+        flags[0] = ideal ? 1 : 0;
+    }
+    __syncthreads();
+    const int tpc0 = (int)E.sc[EQ_TPC0];
+    long long passes = 0;
+    for (int pass = 0; pass < 1000000; pass++) {
+        if (flags[0] == 0) {
+            eq_tracer_counts(E, tcount, redl);
+            if (threadIdx.x == 0) {
+                bool ideal = true;
+                for (int t = 0; t < NT; t++) if (tcount[t] != E.sc[EQ_NIDEAL0 + t]) ideal = false;
+                if (ideal) flags[0] = 1;
+            }
+            __syncthreads();
+        }
+        {
+            const int m0 = (tpc0 > 0) ? eq_minval(E, 0, E.comp == 1, redi) : 0;
+            if (threadIdx.x == 0) minex[0] = m0;
+            for (int t = 1; t < NT; t++) {
+                const int mt = ((int)E.sc[EQ_TPC0 + t] > 0) ? eq_minval(E, t, true, redi) : 0;
+                if (threadIdx.x == 0) minex[t] = mt;
+            }
+        }
+        long long used = 0;
+        for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) used += E.isv[q];
+        used = eq_blocksum(used, redl);
+        if (threadIdx.x == 0) {
+            bool allz = true;
+            for (int t = 0; t < NT; t++) if (minex[t] != 0) allz = false;
+            flags[1] = (allz || used >= nfree) ? 1 : 0;
+            if (!flags[1]) {
+                eq_shuffle(E.nx_loop, 0, E.nx, E.sd, 0, NR);
+                eq_shuffle(E.nz_loop, 0, E.nz, E.sd, 0, NR);
+            }
+            flags[2] = 0;
+        }
+        __syncthreads();
+        if (flags[1]) break;
+        passes++;
+        if (isrank) {
+            int lo, cnt;
+            eq_static(E.nx + 1, NR, rank, lo, cnt);
+            int tt = 0;
+            for (int ii = lo; ii < lo + cnt; ii++) {
+                const int i = E.nx_loop[ii];
+                for (int kk = 0; kk <= E.nz; kk++) {
+                    const int k = E.nz_loop[kk];
+                    const int type_save = eq_maxloc(E, i, k);
+                    if (flags[0] == 0) {
+                        for (int q = 0; q < NT; q++)
+                            if (tcount[q] > E.sc[EQ_NIDEAL0 + q]) { tt = q; break; }
+                    } else {
+                        tt = type_save;
+                    }
+                    const size_t c = eq_cell(E, i, k);
+                    if (E.nex[c] == minex[type_save] && E.isv[rank * NT + tt] < E.nfr[rank * NT + tt] && E.nex[c] < 0) {
+                        const int ID = eq_place(E, rank, tt, i, k);
+                        const int slot = E.iperm[ID - 1];
+                        if (E.comp == 1) E.ttype[slot] = type_save;
+                        E.counts[(size_t)tt * E.L.plane + IX(E.L, i, k)] -= 1;
+                        E.counts[(size_t)E.ttype[slot] * E.L.plane + IX(E.L, i, k)] += 1;
+                        E.nex[c] = E.nex[c] + 1;
+                        flags[2] = 1;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (!flags[2]) break;
+        __syncthreads();
+    }
+    // ---- remaining donors, one thread, ranks in turn ----
+    for (int pass = 0; pass < 1000000; pass++) {
+        {
+            const int m0 = (tpc0 > 0) ? eq_minval(E, 0, E.comp == 1, redi) : 0;
+            if (threadIdx.x == 0) minex[0] = m0;
+            for (int t = 1; t < NT; t++) {
+                const int mt = (tpc0 > 0) ? eq_minval(E, t, true, redi) : 0;
+                if (threadIdx.x == 0) minex[t] = mt;
+            }
+        }
+        long long used = 0;
+        for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) used += E.isv[q];
+        used = eq_blocksum(used, redl);
+        if (threadIdx.x == 0) {
+            bool allz = true;
+            for (int t = 0; t < NT; t++) if (minex[t] != 0) allz = false;
+            flags[1] = (allz || used >= nfree) ? 1 : 0;
+            flags[2] = 0;
+            if (!flags[1]) {
+                int rk = 0;
+                eq_shuffle(E.nx_loop, 0, E.nx, E.sd, 0, NR);
+                eq_shuffle(E.nz_loop, 0, E.nz, E.sd, 0, NR);
+                for (int ii = 0; ii <= E.nx; ii++) {
+                    const int i = E.nx_loop[ii];
+                    for (int kk = 0; kk <= E.nz; kk++) {
+                        const int k = E.nz_loop[kk];
+                        const int tt = eq_maxloc(E, i, k);
+                        long long u = 0, a = 0;
+                        for (int q = 0; q < NR; q++) { u += E.isv[q * NT + tt]; a += E.nfr[q * NT + tt]; }
+                        const size_t c = eq_cell(E, i, k);
+                        if (E.nex[c] == minex[tt] && u < a && E.nex[c] < 0) {
+                            for (int g = 0; g < NR; g++) {
+                                rk = rk + 1;
+                                if (rk == NR) rk = 0;
+                                if (E.isv[rk * NT + tt] < E.nfr[rk * NT + tt]) break;
+                            }
+                            const int ID = eq_place(E, rk, tt, i, k);
+                            if (E.comp == 1) E.ttype[E.iperm[ID - 1]] = eq_maxloc(E, i, k);
+                            E.nex[c] = E.nex[c] + 1;
+                            flags[2] = 1;
+                        }
+                    }
+                }
+            }
+        }
+        __syncthreads();
+        if (flags[1] || !flags[2]) break;
+        __syncthreads();
+    }
+    // ---- the equalize.dat row ----
+    for (int t = 0; t < NT; t++) {
+        const int m = (E.comp == 0) ? eq_minval(E, 0, false, redi) : eq_minval(E, t, true, redi);
+        if (threadIdx.x == 0) E.sc[EQ_MIN0 + t] = m;
+    }
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    long long d = 0;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) if (E.nex[c] <= 0) d += E.nex[c];
+    d = eq_blocksum(d, redl);
+    long long used = 0;
+    for (int q = threadIdx.x; q < NR * NT; q += blockDim.x) used += E.isv[q];
+    used = eq_blocksum(used, redl);
+    eq_tracer_counts(E, tcount, redl);
+    if (threadIdx.x == 0) {
+        E.sc[EQ_DEFICIT] = d;
+        E.sc[EQ_MOVED] = used;
+        E.sc[EQ_PASSES] = passes;
+        for (int t = 0; t < NT; t++) E.sc[EQ_COUNT0 + t] = tcount[t];
+    }
+}
+
+// temperatures of the moved tracers from Textend (composition.f90:545-556)
+__global__ void k_eq_textend(Lay L, Phys P, const double* __restrict__ Tr, double* __restrict__ out) {
+    Range2 r{-1, L.a + 1, -1, L.b + 1};
+    RANGE_IK(r);
+    if (!inr) return;
+    out[IX(L, i, k)] = textend(L, P, Tr, i, k);
+}
+__global__ void k_eq_interp_T(Lay L, Phys P, EqDev E, const double* __restrict__ Td, const double* __restrict__ dTd,
+                              double* __restrict__ Ttr) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t per = (int64_t)E.cap;
+    if (g >= (int64_t)E.NR * E.NT * per) return;
+    const int rank = (int)(g / ((int64_t)E.NT * per));
+    const int t = (int)((g / per) % E.NT);
+    const int p = (int)(g % per);
+    if (p < 1 || p > E.isv[rank * E.NT + t]) return;
+    const int slot = E.iperm[eq_D(E, rank, t)[p] - 1];
+    Ttr[slot] = interp_taylor(L, P, Td, dTd, E.rtr[slot], E.str[slot]);
+}
+
+}  // namespace
+
+static EqDev eq_dev(const EqHost& H) {
+    EqDev E{};
+    E.L = H.L; E.nx = H.L.a; E.nz = H.L.b; E.ntype = H.ntype; E.NT = H.ntype + 1; E.NR = H.NR; E.comp = H.comp;
+    E.tracer = H.tracer; E.tpc = H.tpc; E.ntr = H.ntr; E.dr = H.P.dr; E.ds = H.P.ds; E.aspect = H.P.aspect;
+    E.dist_r = H.dist_r; E.dist_s = H.dist_s; E.counts = H.counts; E.nempty = H.nempty;
+    for (int j = 0; j < H.ntype && j < TC_MAX_TYPES; j++) E.C.p[j] = H.Cnew[j];
+    E.rtr = H.rtr; E.str = H.str; E.ttype = H.ttype; E.perm = H.perm; E.iperm = H.iperm; E.nex = H.nex;
+    E.off = H.off; E.cur = H.cur; E.ids = H.ids; E.sd = H.seeds; E.isv = H.isv; E.isv2 = H.isv2; E.nfr = H.nfr;
+    E.nx_loop = H.nx_loop; E.nz_loop = H.nz_loop; E.sc = H.sc;
+    return E;
+}
+__global__ void k_eq_set_total(int* off, int n, int64_t total) { off[n] = (int)total; }
+
+// equalize_tracers, first part (composition.f90:99-162): nexcess of every
+// corner volume; *nfree and whether any volume is off its target
+int launch_equalize_count(cudaStream_t s, const EqHost& H, int64_t* nfree, int* nonzero) {
+    EqDev E = eq_dev(H);
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    const unsigned cb = (unsigned)((ncell + 255) / 256);
+    long long hsc[EQ_NSC] = {};
+    for (int t = 0; t < E.NT; t++) hsc[EQ_NIDEAL0 + t] = H.Nideal[t];
+    cudaMemcpyAsync(H.sc, hsc, sizeof(hsc), cudaMemcpyHostToDevice, s);
+    if (E.comp == 1) { k_eq_tpc<<<cb, 256, 0, s>>>(E); tc_note_launch(); }
+    k_eq_nexcess<<<cb, 256, 0, s>>>(E); tc_note_launch();
+    cudaMemcpyAsync(hsc, H.sc, sizeof(hsc), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    *nfree = hsc[EQ_NFREE];
+    *nonzero = hsc[EQ_NONZERO] ? 1 : 0;
+    // tpc_type for the lottery's minexcess tests and the row
+    for (int t = 0; t < E.NT; t++) {
+        const long long n = hsc[EQ_TCNT0 + t];
+        hsc[EQ_TPC0 + t] = (E.comp == 0) ? (t == 0 ? E.tpc : 0)
+                                         : (n > 0 ? llround((double)hsc[EQ_TSUM0 + t] / (double)n) : 0);
+    }
+    cudaMemcpyAsync(H.sc + EQ_TPC0, hsc + EQ_TPC0, sizeof(long long) * 8, cudaMemcpyHostToDevice, s);
+    return 0;
+}
+
+// equalize_tracers, the rest (composition.f90:163-556) with `donor` holding
+// NR x NT x (nfree+1) ints; row receives the equalize.dat values (see
+// tc_equalize_row); returns 0, TC_ERR_EQUALIZE or -1 on a CUDA error
+int launch_equalize_move(cudaStream_t s, const EqHost& H, int64_t nfree, int* donor, int64_t* row, int* row_len) {
+    EqDev E = eq_dev(H);
+    E.cap = nfree + 1;
+    E.donor = donor;
+    const int ncell = (E.nx + 1) * (E.nz + 1);
+    const unsigned cb = (unsigned)((ncell + 255) / 256);
+    cudaMemsetAsync(E.donor, 0, sizeof(int) * (size_t)E.NR * E.NT * (size_t)E.cap, s);
+    cudaMemsetAsync(E.isv, 0, sizeof(int) * E.NR * E.NT, s);
+    cudaMemsetAsync(H.sc + EQ_ERR, 0, sizeof(long long), s);
+    // per-volume id lists, ascending, then shuffled by the ranks
+    k_eq_offsets_in<<<cb, 256, 0, s>>>(E, H.cnt); tc_note_launch();
+    const int nbk = (ncell + 1023) / 1024;
+    k_scan_blocks<<<nbk, 1024, 0, s>>>(H.cnt, ncell, H.bsum); tc_note_launch();
+    k_scan_bsums<<<1, 1024, 0, s>>>(H.bsum, nbk); tc_note_launch();
+    k_scan_final<<<nbk, 1024, 0, s>>>(H.cnt, ncell, H.bsum, E.off); tc_note_launch();
+    k_eq_set_total<<<1, 1, 0, s>>>(E.off, ncell, E.ntr); tc_note_launch();
+    const unsigned tb = (unsigned)((E.ntr + 255) / 256);
+    k_eq_scatter<<<tb, 256, 0, s>>>(E); tc_note_launch();
+    k_eq_sort_lists<<<cb, 256, 0, s>>>(E); tc_note_launch();
+    k_eq_shuffle_lists<<<(E.NR + 31) / 32, 32, 0, s>>>(E); tc_note_launch();
+    // donors, lottery, serial remainder
+    const int nb = (E.NR <= 256) ? 256 : ((E.NR + 31) / 32) * 32;
+    k_eq_main<<<1, nb, 0, s>>>(E, nfree); tc_note_launch();
+    if (E.tracer == 1) {
+        Range2 r{-1, E.L.a + 1, -1, E.L.b + 1};
+        k_eq_textend<<<grid_for(r), dim3(BX, BY), 0, s>>>(E.L, H.P, H.Tratio, H.Td); tc_note_launch();
+        launch_derivatives(s, E.L, H.P, H.Td, H.dTd);
+        const int64_t n = (int64_t)E.NR * E.NT * E.cap;
+        k_eq_interp_T<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(E.L, H.P, E, H.Td, H.dTd, H.Ttr); tc_note_launch();
+    }
+    long long hsc[EQ_NSC];
+    cudaMemcpyAsync(hsc, H.sc, sizeof(hsc), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    if (hsc[EQ_ERR]) return TC_ERR_EQUALIZE;
+    int n = 0;
+    row[n++] = E.NT;
+    for (int t = 0; t < E.NT; t++) row[n++] = hsc[EQ_TPC0 + t];
+    for (int t = 0; t < E.NT; t++) row[n++] = hsc[EQ_MIN0 + t];
+    row[n++] = hsc[EQ_DEFICIT];
+    row[n++] = hsc[EQ_MOVED];
+    row[n++] = nfree;
+    for (int t = 0; t < E.NT; t++) row[n++] = hsc[EQ_COUNT0 + t];
+    *row_len = n;
+    return 0;
+}

@@ -80,6 +80,19 @@ struct Handle {
     double *Ttr = nullptr, *Ttr0 = nullptr, *Ttr1 = nullptr, *Ttr2 = nullptr;
     double *Tratio = nullptr, *tsa = nullptr, *dT = nullptr;
     unsigned long long* tsum = nullptr;
+    // tracer repositioning (equalize = 1): index and list buffers, the mzran
+    // state of each reproduced OpenMP thread, the growable donor table,
+    // Cinit (stats at time 0) and the last equalize.dat row
+    int eq_NR = 1;
+    int *eq_iperm = nullptr, *eq_nex = nullptr, *eq_off = nullptr, *eq_cur = nullptr, *eq_ids = nullptr,
+        *eq_cnt = nullptr, *eq_seeds = nullptr, *eq_isv = nullptr, *eq_isv2 = nullptr, *eq_nfr = nullptr,
+        *eq_nxl = nullptr, *eq_nzl = nullptr, *eq_donor = nullptr;
+    size_t eq_donor_cap = 0;
+    long long* eq_sc = nullptr;
+    double *eq_Td = nullptr, *eq_dTd = nullptr;
+    double Cinit[TC_MAX_TYPES] = {};
+    long long nequalize = 0;
+    std::vector<int64_t> eq_row;
     double *band = nullptr, *rowb = nullptr, *bvec = nullptr, *ainv = nullptr;
     int* ipiv = nullptr;
     double* rows = nullptr;
@@ -865,6 +878,50 @@ tc_status update_velocities(Handle* h) {
     return TC_OK;
 }
 
+// equalize_tracers (composition.f90:83-580), then tracers_to_corners with
+// smoothing off (:576-578)
+tc_status equalize_tracers(Handle* h) {
+    EqHost H{};
+    H.L = h->L1; H.P = h->P; H.ntype = h->ntype; H.NR = h->eq_NR; H.comp = h->p.comp; H.tracer = h->p.tracer;
+    H.tpc = h->p.tpc; H.ntr = h->ntr; H.dist_r = h->p.dist_factor * h->P.dr; H.dist_s = h->p.dist_factor * h->P.ds;
+    if (h->p.comp == 1) {
+        long long sum = 0;
+        for (int t = 1; t <= h->ntype; t++) {
+            H.Nideal[t] = std::llround(h->Cinit[t - 1] * (double)h->ntr);
+            sum += H.Nideal[t];
+        }
+        H.Nideal[0] = h->ntr - sum;
+    } else {
+        H.Nideal[0] = h->ntr;
+    }
+    H.counts = h->counts; H.nempty = h->nempty; H.Cnew = h->Cnew; H.rtr = h->rtr; H.str = h->str;
+    H.ttype = h->ttype; H.perm = h->perm; H.iperm = h->eq_iperm; H.nex = h->eq_nex; H.off = h->eq_off;
+    H.cur = h->eq_cur; H.ids = h->eq_ids; H.cnt = h->eq_cnt; H.bsum = h->sort_bsum; H.seeds = h->eq_seeds;
+    H.isv = h->eq_isv; H.isv2 = h->eq_isv2; H.nfr = h->eq_nfr; H.nx_loop = h->eq_nxl; H.nz_loop = h->eq_nzl;
+    H.sc = h->eq_sc; H.Tratio = h->Tratio; H.Td = h->eq_Td; H.dTd = h->eq_dTd; H.Ttr = h->Ttr;
+    int64_t nfree = 0;
+    int nonzero = 0;
+    if (launch_equalize_count(h->st, H, &nfree, &nonzero) != 0) { CK(cudaGetLastError()); return TC_ERR_CUDA; }
+    h->eq_row.clear();
+    if (!nonzero) return TC_OK;
+    h->nequalize++;
+    const size_t need = (size_t)h->eq_NR * (size_t)(h->ntype + 1) * (size_t)(nfree + 1);
+    if (need > h->eq_donor_cap) {
+        if (h->eq_donor) cudaFree(h->eq_donor);
+        h->eq_donor = nullptr;
+        h->eq_donor_cap = 0;
+        CK(cudaMalloc((void**)&h->eq_donor, sizeof(int) * need));
+        h->eq_donor_cap = need;
+    }
+    int64_t row[64];
+    int len = 0;
+    const int st = launch_equalize_move(h->st, H, nfree, h->eq_donor, row, &len);
+    if (st == TC_ERR_EQUALIZE) return TC_ERR_EQUALIZE;
+    if (st != 0) { CK(cudaGetLastError()); return TC_ERR_CUDA; }
+    h->eq_row.assign(row, row + len);
+    return tracers_to_corners(h, h->rtr, h->str, false, h->p.tracer == 1 ? h->Ttr : nullptr, h->T);
+}
+
 // energy_time (energy.f90:117-453): field T or temperature tracers,
 // compositional tracers, local_time=0
 tc_status energy_time(Handle* h) {
@@ -877,6 +934,7 @@ tc_status energy_time(Handle* h) {
     launch_stability(h->st, h->L1, h->P, h->conduct, h->conduct_r, h->conduct_s, h->u, h->w, h->p.courant,
                      h->p.dt_manual, h->rs, h->ds);
     TRY(check_flags(h));
+    if (h->p.equalize == 1) TRY(equalize_tracers(h));
     for (int t = 0; t < h->ntype; t++) copy_plane(h, h->C0[t], h->Cnew[t]);
     copy_plane(h, h->T0, tt ? h->Tratio : h->T);
     if (trc && h->ntr > 0 && h->p.tracer_sort_interval > 0 && h->tstep % h->p.tracer_sort_interval == 0)
@@ -999,6 +1057,8 @@ tc_status stats(Handle* h, tc_stats_row* row) {
     }
     row->time = h->time;
     row->tstep = h->tstep;
+    if (h->time == 0.0 && h->p.equalize == 1)
+        for (int t = 0; t < h->ntype; t++) h->Cinit[t] = row->Cavg[t];
     row->n_eta = h->n_eta;
     row->n_temp = h->n_temp;
     row->eig_fine = h->eig_fine;
@@ -1022,6 +1082,9 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.comp == 1 && (p.ntype < 1 || p.ntype > TC_MAX_TYPES)) return TC_ERR_ARG;
     if (p.tracer != 0 && p.tracer != 1) return TC_ERR_ARG;
     if (p.non_Newtonian != 0 && p.non_Newtonian != 1) return TC_ERR_ARG;
+    if (p.equalize != 0 && p.equalize != 1) return TC_ERR_ARG;
+    if (p.equalize == 1 && p.comp == 0 && p.tracer == 0) { h->err = "equalize needs tracers"; return TC_ERR_ARG; }
+    if (p.equalize_threads < 0 || p.equalize_threads > 1024) return TC_ERR_ARG;
     if (p.non_Newtonian == 1 && (p.solver_precision != 0 || p.learned_guess != 0)) {
         h->err = "the non-Newtonian iteration runs in FP64 without the learned start";
         return TC_ERR_UNSUPPORTED;
@@ -1121,6 +1184,37 @@ tc_status create(Handle* h, const tc_params* in) {
         TRY(dalloc_t(h, &h->sort_cnt, pl));
         TRY(dalloc_t(h, &h->sort_off, pl));
         TRY(dalloc_t(h, &h->sort_bsum, (pl + 1023) / 1024));
+    }
+    if (p.equalize == 1 && h->ntr > 0) {
+        const int NR = (p.equalize_threads > 0) ? p.equalize_threads : 1;
+        const size_t nc = (size_t)(nx + 1) * (nz + 1);
+        h->eq_NR = NR;
+        TRY(dalloc_t(h, &h->eq_iperm, (size_t)h->ntr));
+        TRY(dalloc_t(h, &h->eq_ids, (size_t)h->ntr));
+        TRY(dalloc_t(h, &h->eq_nex, nc));
+        TRY(dalloc_t(h, &h->eq_off, nc + 1));
+        TRY(dalloc_t(h, &h->eq_cur, nc));
+        TRY(dalloc_t(h, &h->eq_cnt, nc));
+        TRY(dalloc_t(h, &h->eq_seeds, (size_t)4 * NR));
+        TRY(dalloc_t(h, &h->eq_isv, (size_t)NR * (h->ntype + 1)));
+        TRY(dalloc_t(h, &h->eq_isv2, (size_t)NR * (h->ntype + 1)));
+        TRY(dalloc_t(h, &h->eq_nfr, (size_t)NR * (h->ntype + 1)));
+        TRY(dalloc_t(h, &h->eq_nxl, (size_t)nx + 1));
+        TRY(dalloc_t(h, &h->eq_nzl, (size_t)nz + 1));
+        TRY(dalloc_t(h, &h->eq_sc, (size_t)64));
+        if (p.tracer == 1) { TRY(dalloc_t(h, &h->eq_Td, pl)); TRY(dalloc_t(h, &h->eq_dTd, pl)); }
+        // mzran seeds of each OpenMP thread (basics.f90:198-212), laid out [4][NR]
+        std::vector<int32_t> sd((size_t)4 * NR);
+        sd[0] = 521288629; sd[NR] = 362436069; sd[2 * NR] = 16163801; sd[3 * NR] = 1131199299;
+        for (int j = 1; j < NR; j++) {
+            int32_t r = sd[j - 1] - sd[2 * NR + j - 1];
+            if (r < 0) r += 2147483579;
+            sd[j] = sd[NR + j - 1];
+            sd[NR + j] = sd[2 * NR + j - 1];
+            sd[2 * NR + j] = r;
+            sd[3 * NR + j] = (int32_t)(69069u * (uint32_t)sd[3 * NR + j - 1] + 1013904243u);
+        }
+        CK(cudaMemcpy(h->eq_seeds, sd.data(), sizeof(int32_t) * sd.size(), cudaMemcpyHostToDevice));
     }
     if (p.tracer == 1 && h->ntr > 0) {
         double** tq[] = {&h->Ttr, &h->Ttr0, &h->Ttr1, &h->Ttr2};
@@ -1439,6 +1533,7 @@ tc_status tc_destroy(tc_handle* H) {
     Handle* h = &H->h;
     if (h->st) cudaStreamSynchronize(h->st);
     for (void* q : h->allocs) cudaFree(q);
+    if (h->eq_donor) cudaFree(h->eq_donor);
     if (h->hs) cudaFreeHost(h->hs);
     if (h->graphs) {
         if (h->graphs->l1) cudaGraphExecDestroy(h->graphs->l1);
@@ -1488,6 +1583,15 @@ tc_status tc_upload_state_ex(tc_handle* H, const double* T, const double* Cnew, 
                              const double* str, const int32_t* Ttype, const double* Ttr, int64_t ntr) {
     if (!H) return TC_ERR_ARG;
     return upload(&H->h, T, Cnew, SF, rtr, str, Ttype, ntr, Ttr);
+}
+
+tc_status tc_equalize_row(const tc_handle* H, int64_t* out, int32_t cap, int32_t* len) {
+    if (!H || !len) return TC_ERR_ARG;
+    const Handle* h = &H->h;
+    if ((int32_t)h->eq_row.size() > cap || (!out && !h->eq_row.empty())) return TC_ERR_ARG;
+    for (size_t q = 0; q < h->eq_row.size(); q++) out[q] = h->eq_row[q];
+    *len = (int32_t)h->eq_row.size();
+    return TC_OK;
 }
 
 tc_status tc_download_tracer_temperature(tc_handle* H, double* Ttr) {

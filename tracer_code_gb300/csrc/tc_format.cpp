@@ -4,6 +4,7 @@
 //   stats.dat               basics.f90:283-314 (local_time = 0 branches)
 //   viscosity_smoother.dat  basics.f90:316-322
 //   T1xxxx snapshots        snapshots, main.f90:237-270
+//   equalize.dat            equalize_tracers, composition.f90:568-574
 //
 // Fortran edit descriptors used there: Gw.d and Gw.dEe for reals, Iw for
 // integers; list-directed WRITE(u,*) " " for the blank line after each
@@ -141,6 +142,16 @@ tc_status tc_format_vis_line(const tc_stats_row* r, int32_t comp, int32_t ntype,
     if (RaT != 0.0) fmt_i(s, r->n_temp, 5);
     if (comp == 1)
         for (int t = 0; t < ntype; t++) fmt_i(s, r->n_comp[t], 5);
+    return finish(s, buf, cap);
+}
+
+tc_status tc_format_equalize_line(double time, const int64_t* row, int32_t len, char* buf, int32_t cap) {
+    if (!row || len < 1) return TC_ERR_ARG;
+    const int n = (int)row[0];
+    if (n < 1 || len != 4 + 3 * n) return TC_ERR_ARG;
+    std::string s;
+    fmt_g(s, time, 20, 8, 0);
+    for (int q = 1; q < len; q++) fmt_i(s, row[q], 10);
     return finish(s, buf, cap);
 }
 

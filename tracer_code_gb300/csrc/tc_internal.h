@@ -232,6 +232,27 @@ void launch_histogram(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, 
 void launch_sort_tracers(cudaStream_t s, const Lay& L, const Phys& P, int64_t ntr, const double* rr, const double* ss,
                          const int* tt, const int* perm, int* cnt, int* off, int* bsum, double* r2, double* s2,
                          int* t2, int* p2, const double* Tt = nullptr, double* T2 = nullptr);
+// tracer repositioning (equalize_tracers): device buffers and sizes of one call
+struct EqHost {
+    Lay L;
+    Phys P;
+    int ntype, NR, comp, tracer, tpc;
+    int64_t ntr;
+    double dist_r, dist_s;
+    long long Nideal[TC_MAX_TYPES + 1];
+    int* counts;          // count_type planes (modified by the lottery)
+    const int* nempty;
+    double* const* Cnew;
+    double *rtr, *str;    // slot order
+    int* ttype;
+    const int* perm;
+    int *iperm, *nex, *off, *cur, *ids, *cnt, *bsum, *seeds, *isv, *isv2, *nfr, *nx_loop, *nz_loop;
+    long long* sc;        // 64 scalars
+    const double* Tratio; // temperature tracers
+    double *Td, *dTd, *Ttr;
+};
+int launch_equalize_count(cudaStream_t s, const EqHost& H, int64_t* nfree, int* nonzero);
+int launch_equalize_move(cudaStream_t s, const EqHost& H, int64_t nfree, int* donor, int64_t* row, int* row_len);
 // extendT + tracer_space on (-1:nx+1, -1:nz+1) (temperature tracers)
 void launch_tracer_space(cudaStream_t s, const Lay& L, const Phys& P, const double* Tratio, const double* conduct,
                          const double* conduct_r, const double* conduct_s, const double* const* Cvis, double* tsa);

@@ -58,3 +58,13 @@ def vis_line(row, comp: int, ntype: int, RaT: float) -> str:
     if st:
         raise TracerError(st, "format_vis_line")
     return buf.value.decode()
+
+
+def equalize_line(time: float, row) -> str:
+    """The equalize.dat row (composition.f90:568-574) of a tc_equalize_row result."""
+    arr = (C.c_int64 * len(row))(*[int(v) for v in row])
+    buf = C.create_string_buffer(512)
+    st = _lib().tc_format_equalize_line(float(time), arr, len(row), buf, len(buf))
+    if st:
+        raise TracerError(st, "format_equalize_line")
+    return buf.value.decode()
