@@ -254,6 +254,65 @@ def sweep_roofline(sim, p, fp32: bool) -> dict:
                      "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s")}
 
 
+def shipped_params():
+    """The reference's own shipped main.f90 inputs (parsed from it into
+    tests/golden/golden.json): 200x200, aspect 1, 2 levels, tolerance 1e-3,
+    plastic viscosity (ivis 3) with the non-Newtonian iteration, temperature
+    tracers (30 per volume), tracer repositioning; TRA reproduces a
+    16-thread OpenMP run."""
+    from tracer_code_gb300 import default_params
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        inp = json.load(f)["inputs"]
+    p = default_params()
+    p.nx, p.nz, p.aspect, p.order = int(inp["nx"]), int(inp["nz"]), inp["aspect"], int(inp["order"])
+    p.comp, p.ntype, p.tracer, p.tpc = int(inp["comp"]), 0, int(inp["tracer"]), 30
+    p.equalize, p.equalize_threads = 1, 16
+    p.ivis, p.non_Newtonian = int(inp["ivis"]), int(inp["non_Newtonian"])
+    p.visT, p.visP, p.delta_visT = inp["visT"], inp["visP"], inp["delta_visT"]
+    p.yield_, p.yield_gradient, p.yield_depth = inp["yield"], inp["yield_gradient"], inp["yield_depth"]
+    p.RaT, p.tolerance, p.grids, p.Nmulti = inp["RaT"], inp["tolerance"], int(inp["grids"]), int(inp["Nmulti"])
+    p.eig_ratio, p.eig_ratio_min, p.vis_iter = inp["eig_ratio"], inp["eig_ratio_min"], int(inp["vis_iter"])
+    p.torder, p.courant, p.courantT = int(inp["torder"]), inp["courant"], inp["courantT"]
+    p.courant_stream, p.iterate_order, p.mingrid = inp["courant_stream"], int(inp["iterate_order"]), int(inp["mingrid"])
+    p.Tbot, p.Vbc = int(inp["Tbot"]), int(inp["Vbc"])
+    return p
+
+
+def shipped_config_rates(stream, steps: int, warmup: int, cpu: bool) -> dict:
+    """Timesteps/s of the reference's shipped configuration on this GPU (and,
+    for one step, the CPU restatement on the host cores) from a seeded state."""
+    import torch
+    from tracer_code_gb300 import Simulation, state
+    p = shipped_params()
+    st = state.initial_state(p, seed=1)
+    sim = Simulation(p, stream=stream.cuda_stream)
+    sim.upload(st)
+    for _ in range(warmup):
+        sim.step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    rows = [sim.step() for _ in range(steps)]
+    torch.cuda.synchronize()
+    gpu_s = (time.perf_counter() - t0) / steps
+    out = {"config": "reference main.f90 inputs: 200x200, comp=0, tracer=1 (30/volume), equalize=1 (16 threads), "
+                     "ivis=3, non_Newtonian=1, 2 levels, tolerance 1e-3; seeded synthetic state",
+           "gpu_timesteps_per_s": 1.0 / gpu_s, "cycles_per_step": [r[1] for r in rows],
+           "tracers_moved_last_step": (sim.equalize_row() or [0, 0, 0, 0, 0])[4]}
+    sim.close()
+    if cpu:
+        from oracle.pyoracle import Oracle
+        o = Oracle(p, threads=os.cpu_count() or 1)
+        o.upload(st)
+        o.step()
+        t0 = time.perf_counter()
+        o.step()
+        out["cpu_restatement_timesteps_per_s"] = 1.0 / (time.perf_counter() - t0)
+        out["cpu_cores"] = os.cpu_count() or 1
+        out["cpu_sample"] = "second step from the same state (the first moves no tracers)"
+        o.close()
+    return out
+
+
 def replica_rate(units_per_rank: float, seconds_local: float, world: int, max_over_ranks) -> float:
     """Whole-job throughput of N independent replicas: the units all ranks
     processed over the slowest rank's time (each rank runs the same work, so
@@ -332,6 +391,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     plain_value = replica_rate(args.steps, ms0 * 1e-3, world, max_over_ranks)
     roof0 = sweep_roofline(sim0, pp, fp32=False)
     sim0.close()
+    shipped = shipped_config_rates(stream, 3, 1, cpu=(rank == 0 and not args.no_cpu_baseline)) if rank == 0 else None
     if rank == 0:
         cfg = dict(workload_desc(p, "learned"), cycles_per_step=solves, warmup_cycles_per_step=cycles,
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
@@ -341,7 +401,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                         "cycles_per_step": solvesm},
                    plain_fp64={"timesteps_per_s": plain_value, "ms_per_step": ms0 / args.steps,
                                "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0},
-                   speedup_vs_plain_fp64=value / plain_value)
+                   speedup_vs_plain_fp64=value / plain_value,
+                   reference_shipped_config=shipped)
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",

@@ -14,6 +14,8 @@
 // xrr=...=0), which leaves every retained product and sum of the reference
 // unchanged.
 #include "tc_device.cuh"
+#include <cooperative_groups.h>
+namespace cg = cooperative_groups;
 
 #include <stdio.h>
 
@@ -507,9 +509,198 @@ __global__ void k_coarse_lu(double* __restrict__ ABg, int* __restrict__ ipiv, in
         for (size_t t = tid; t < tot; t += nth) ABg[t] = sm[t];
     if (tid == 0) *info_out = sInfo;
 }
+// The same factorisation for bands too large for one CTA's shared memory:
+// at step j only rows j..j+kl of columns j..j+KV are active (KV = kl+ku),
+// so that block is kept in the shared memory of a cluster of LU_CL CTAs,
+// columns dealt round-robin by (column mod (KV+1)) and rows by (row mod
+// (kl+1)).  The owner of column j searches the pivot, swaps and scales
+// column j and pushes the multipliers into every CTA's shared memory; after
+// one cluster barrier every CTA swaps and updates its own columns, writes
+// back row j of them and column j (its owner), and loads the row and column
+// that enter the block.  Each element sees the operations of dgbtf2 in the
+// same order as in k_coarse_lu.
+#define LU_CL 8
+__global__ void __launch_bounds__(512) k_coarse_lu_cl(double* __restrict__ ABg, int* __restrict__ ipiv, int n,
+                                                      int kl, int ku, int* info_out) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ double smw[];
+    const int ldab = 2 * kl + ku + 1, KV = ku + kl, R = kl + 1, C = KV + 1, Cq = (C + LU_CL - 1) / LU_CL;
+    double* Wl = smw;                       // [R][Cq]
+    double* buf = smw + (size_t)R * Cq;     // [2][R] multipliers of column j
+    __shared__ int sInfoPiv[2];             // pivot row offset * 2 + (pivot != 0), per step parity
+    __shared__ int sJP;
+    const int tid = threadIdx.x, nth = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nth >> 5;
+#define AB(rw, jc) ABg[(size_t)((rw) - 1) + (size_t)((jc) - 1) * ldab]
+    // dgbtf2's first loop: fill-in entries of columns ku+2..KV
+    if (rank == 0)
+        for (int jj = ku + 2; jj <= min(KV, n); jj++)
+            for (int i = KV - jj + 2 + tid; i <= kl; i += nth) AB(i, jj) = 0.0;
+    cl.sync();
+    // the block of step 1 (column 1+KV: rows 1..kl zeroed as dgbtf2 does at step 1)
+    for (int e = tid; e < R * Cq; e += nth) {
+        const int a = e / Cq, lc = e % Cq, cs = lc * LU_CL + rank;
+        if (cs >= C) continue;
+        // row 1+a sits in slot (1+a) mod R, column jc of 1..C in slot jc mod C
+        const int i = 1 + a, jc = (cs == 0) ? C : cs;
+        double v = 0.0;
+        if (i <= n && jc <= n) v = (jc == C && a < kl) ? 0.0 : AB(KV + 1 + i - jc, jc);
+        Wl[(size_t)(i % R) * Cq + lc] = v;
+    }
+    int JU = 1, info = 0;
+    // one value per thread of the row entering at the next step, loaded a step
+    // ahead (when every column of the block has its own thread)
+    const bool prefetch = (C <= nth);
+    double pf = 0.0;
+    int pf_lc = -1;
+    __syncthreads();
+    for (int j = 1; j <= n; j++) {
+        const int r0 = j % R, c0 = j % C;
+        auto RS = [&](int a) { const int v = r0 + a; return v >= R ? v - R : v; };
+        // local column index of absolute column j + c (owned by this CTA or -1)
+        auto LC = [&](int c) { int cs = c0 + c; if (cs >= C) cs -= C; return (cs % LU_CL == rank) ? cs / LU_CL : -1; };
+        if (j >= 2) {
+            // rows j..j+kl-1 of the column that enters (j+KV) are zeroed, row j+kl enters
+            const int jcn = j + KV;
+            if (jcn <= n) {
+                const int lc = LC(KV);
+                if (lc >= 0)
+                    for (int a = tid; a < kl; a += nth) Wl[(size_t)RS(a) * Cq + lc] = 0.0;
+            }
+            const int i = j + kl;
+            if (prefetch) {
+                if (pf_lc >= 0) Wl[(size_t)RS(kl) * Cq + pf_lc] = pf;
+            } else if (i <= n) {
+                for (int c = tid; c <= KV; c += nth) {
+                    const int lc = LC(c), jc = j + c;
+                    if (lc >= 0) Wl[(size_t)RS(kl) * Cq + lc] = (jc <= n) ? AB(KV + 1 + i - jc, jc) : 0.0;
+                }
+            }
+            __syncthreads();
+        }
+        if (prefetch) {
+            // row j+1+kl over columns j+1..j+1+KV, for step j+1
+            pf_lc = -1;
+            const int i1 = j + 1 + kl, c = tid;
+            if (j + 1 <= n && i1 <= n && c <= KV) {
+                int cs = c0 + 1 + c;
+                while (cs >= C) cs -= C;
+                if (cs % LU_CL == rank) {
+                    const int jc = j + 1 + c;
+                    pf_lc = cs / LU_CL;
+                    pf = (jc <= n) ? AB(KV + 1 + i1 - jc, jc) : 0.0;
+                }
+            }
+        }
+        const int KM = min(kl, n - j);
+        const int owner = c0 % LU_CL;
+        if (rank == owner) {
+            const int lc = c0 / LU_CL;
+            if (warp == 0) {
+                double best = -1.0;
+                int bi = 1 << 30;
+                for (int t = 1 + lane; t <= KM + 1; t += 32) {
+                    const double v = fabs(Wl[(size_t)RS(t - 1) * Cq + lc]);
+                    if (v > best) { best = v; bi = t; }
+                }
+                for (int off = 16; off > 0; off >>= 1) {
+                    const double ob = __shfl_down_sync(0xffffffffu, best, off);
+                    const int oi = __shfl_down_sync(0xffffffffu, bi, off);
+                    if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+                }
+                if (lane == 0) {
+                    sJP = bi;
+                    ipiv[j - 1] = bi + j - 1;
+                    const double pv = Wl[(size_t)RS(bi - 1) * Cq + lc];
+                    const int code = bi * 2 + (pv != 0.0 ? 1 : 0);
+                    if (pv != 0.0 && bi != 1) {
+                        Wl[(size_t)RS(bi - 1) * Cq + lc] = Wl[(size_t)RS(0) * Cq + lc];
+                        Wl[(size_t)RS(0) * Cq + lc] = pv;
+                    }
+                    for (int q = 0; q < LU_CL; q++) cl.map_shared_rank(sInfoPiv, q)[j & 1] = code;
+                }
+            }
+            __syncthreads();
+            if ((sInfoPiv[j & 1] & 1) && KM > 0) {
+                const double rcp = 1.0 / Wl[(size_t)RS(0) * Cq + lc];
+                for (int t = 1 + tid; t <= KM; t += nth) {
+                    const double v = rcp * Wl[(size_t)RS(t) * Cq + lc];
+                    Wl[(size_t)RS(t) * Cq + lc] = v;
+                    for (int q = 0; q < LU_CL; q++) cl.map_shared_rank(buf, q)[(j & 1) * R + t] = v;
+                }
+            }
+        }
+        cl.sync();  // multipliers and pivot of column j visible in every CTA
+        const int code = sInfoPiv[j & 1];
+        const int JP = code >> 1;
+        const bool nz = (code & 1) != 0;
+        if (nz) JU = max(JU, min(j + ku + JP - 1, n));
+        else if (info == 0) info = j;
+        if (nz) {
+            const double* mult = buf + (j & 1) * R;
+            // this CTA's columns of the block: local index lc holds slot lc*LU_CL+rank,
+            // i.e. column j + c with c = (slot - j) mod C
+            for (int lc = warp; lc < Cq; lc += nw) {
+                const int cs = lc * LU_CL + rank;
+                if (cs >= C) break;
+                int c = cs - c0;
+                if (c < 0) c += C;
+                if (c < 1 || c > JU - j) continue;
+                double* top = &Wl[(size_t)RS(0) * Cq + lc];
+                if (JP != 1 && lane == 0) {
+                    double* pr = &Wl[(size_t)RS(JP - 1) * Cq + lc];
+                    const double t0 = *pr;
+                    *pr = *top;
+                    *top = t0;
+                }
+                __syncwarp();
+                const double temp = -*top;
+                if (temp != 0.0)
+                    for (int t = 1 + lane; t <= KM; t += 32) {
+                        double* e = &Wl[(size_t)RS(t) * Cq + lc];
+                        *e = *e + mult[t] * temp;
+                    }
+            }
+        }
+        __syncthreads();
+        // write back column j (its owner) and row j (every CTA, its columns)
+        if (rank == owner) {
+            const int lc = c0 / LU_CL;
+            for (int a = tid; a <= kl; a += nth)
+                if (j + a <= n) AB(KV + 1 + a, j) = Wl[(size_t)RS(a) * Cq + lc];
+        }
+        for (int c = 1 + tid; c <= KV; c += nth) {
+            const int lc = LC(c), jc = j + c;
+            if (lc >= 0 && jc <= n) AB(KV + 1 - c, jc) = Wl[(size_t)RS(0) * Cq + lc];
+        }
+        __syncthreads();
+    }
+#undef AB
+    if (rank == 0 && tid == 0) *info_out = info;
+}
+
 void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, int ku, DevScalars* ds) {
     size_t bytes = sizeof(double) * (size_t)(2 * kl + ku + 1) * n;
     int in_smem = bytes <= 200 * 1024 ? 1 : 0;
+    const int R = kl + 1, C = kl + ku + 1, Cq = (C + LU_CL - 1) / LU_CL;
+    const size_t win = sizeof(double) * ((size_t)R * Cq + 2 * (size_t)R);
+    if (!in_smem && win <= 200 * 1024) {
+        cudaFuncSetAttribute(k_coarse_lu_cl, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)win);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(LU_CL, 1, 1);
+        cfg.blockDim = dim3(512, 1, 1);
+        cfg.dynamicSmemBytes = win;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = LU_CL;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, k_coarse_lu_cl, band, ipiv, n, kl, ku, &ds->lu_info); tc_note_launch();
+        return;
+    }
     size_t sm = in_smem ? bytes : 0;
     if (in_smem) cudaFuncSetAttribute(k_coarse_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info); tc_note_launch();
@@ -604,6 +795,155 @@ void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, co
     const int threads = 256;
     const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
     launch_pdl(k_coarse_apply, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
+}
+
+// Coarsest-level solve for coarse grids too large for an explicit inverse:
+// B = RowB .* RHS (Compute_coarse_vector), DGBTRS('N') with the band's LU
+// (row interchanges + unit-lower solve, then dtbsv), x to the interior
+// (Stream_grid_coarse with the stream BCs).  One block: the vector in shared
+// memory, one warp per substitution (the band is read once, from L2).
+#define CS_FW 8   // band rows below the diagonal per lane (kl <= 256) in the prefetched path
+#define CS_BW 16  // band rows above (kl + ku <= 512)
+template <typename TR>
+__global__ void __launch_bounds__(256) k_coarse_solve(Lay L, const double* __restrict__ ABg,
+                                                      const int* __restrict__ ipiv, const double* __restrict__ rowb,
+                                                      const TR* rhs, int n, int kl, int ku, TR* err, int Vbc) {
+    extern __shared__ double Bv[];
+    pdl_entry();
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int nzc = L.b, nxc = L.a, N = nzc + 1;
+    const int ldab = 2 * kl + ku + 1, KD = ku + kl + 1, K = kl + ku;
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int kq = q % N, iq = q / N;
+        Bv[q] = (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
+                    ? (double)ld_state(rhs + IX(L, iq, kq)) * __ldg(rowb + q)
+                    : 0.0;
+    }
+    __syncthreads();
+#define A_(rw, cl) ABg[(size_t)((rw) - 1) + (size_t)((cl) - 1) * ldab]
+    if (tid < 32 && kl <= 32 * CS_FW && K <= 32 * CS_BW) {
+        // the band column of the next step is loaded while this step runs
+        double nf[CS_FW];
+        int npiv = (n >= 2) ? __ldg(ipiv) : 0;
+        {
+            const int LM = min(kl, n - 1);
+#pragma unroll
+            for (int u = 0; u < CS_FW; u++) {
+                const int t = 1 + lane + 32 * u;
+                nf[u] = (n >= 2 && t <= LM) ? __ldg(&A_(KD + t, 1)) : 0.0;
+            }
+        }
+        for (int jj = 1; jj <= n - 1; jj++) {
+            const int LM = min(kl, n - jj);
+            double cf[CS_FW];
+#pragma unroll
+            for (int u = 0; u < CS_FW; u++) cf[u] = nf[u];
+            const int Lr = npiv;
+            if (jj + 1 <= n - 1) {
+                const int LM1 = min(kl, n - jj - 1);
+                npiv = __ldg(ipiv + jj);
+#pragma unroll
+                for (int u = 0; u < CS_FW; u++) {
+                    const int t = 1 + lane + 32 * u;
+                    nf[u] = (t <= LM1) ? __ldg(&A_(KD + t, jj + 1)) : 0.0;
+                }
+            }
+            if (Lr != jj) {
+                if (lane == 0) { const double t0 = Bv[Lr - 1]; Bv[Lr - 1] = Bv[jj - 1]; Bv[jj - 1] = t0; }
+                __syncwarp();
+            }
+            const double temp = -Bv[jj - 1];
+            if (temp != 0.0) {
+#pragma unroll
+                for (int u = 0; u < CS_FW; u++) {
+                    const int t = 1 + lane + 32 * u;
+                    if (t <= LM) Bv[jj + t - 1] = Bv[jj + t - 1] + cf[u] * temp;
+                }
+            }
+            __syncwarp();
+        }
+        double nb[CS_BW], nd = __ldg(&A_(K + 1, n));
+        {
+            const int jj = n, Lc = K + 1 - jj;
+#pragma unroll
+            for (int u = 0; u < CS_BW; u++) {
+                const int i = jj - 1 - lane - 32 * u;
+                nb[u] = (i >= max(1, jj - K)) ? __ldg(&A_(Lc + i, jj)) : 0.0;
+            }
+        }
+        for (int jj = n; jj >= 1; jj--) {
+            double cb[CS_BW];
+#pragma unroll
+            for (int u = 0; u < CS_BW; u++) cb[u] = nb[u];
+            const double dj = nd;
+            if (jj - 1 >= 1) {
+                const int j1 = jj - 1, Lc1 = K + 1 - j1;
+                nd = __ldg(&A_(K + 1, j1));
+#pragma unroll
+                for (int u = 0; u < CS_BW; u++) {
+                    const int i = j1 - 1 - lane - 32 * u;
+                    nb[u] = (i >= max(1, j1 - K)) ? __ldg(&A_(Lc1 + i, j1)) : 0.0;
+                }
+            }
+            const double bj = Bv[jj - 1];
+            if (bj != 0.0) {
+                const double temp = bj / dj;
+                __syncwarp();
+                if (lane == 0) Bv[jj - 1] = temp;
+#pragma unroll
+                for (int u = 0; u < CS_BW; u++) {
+                    const int i = jj - 1 - lane - 32 * u;
+                    if (i >= max(1, jj - K)) Bv[i - 1] = Bv[i - 1] - temp * cb[u];
+                }
+            }
+            __syncwarp();
+        }
+    } else if (tid < 32) {
+        for (int jj = 1; jj <= n - 1; jj++) {
+            const int LM = min(kl, n - jj);
+            const int Lr = __ldg(ipiv + jj - 1);
+            if (Lr != jj) {
+                if (lane == 0) { const double t0 = Bv[Lr - 1]; Bv[Lr - 1] = Bv[jj - 1]; Bv[jj - 1] = t0; }
+                __syncwarp();
+            }
+            const double temp = -Bv[jj - 1];
+            if (temp != 0.0)
+                for (int t = 1 + lane; t <= LM; t += 32) Bv[jj + t - 1] = Bv[jj + t - 1] + __ldg(&A_(KD + t, jj)) * temp;
+            __syncwarp();
+        }
+        for (int jj = n; jj >= 1; jj--) {
+            const double bj = Bv[jj - 1];
+            if (bj != 0.0) {
+                const int Lc = K + 1 - jj;
+                const double temp = bj / __ldg(&A_(K + 1, jj));
+                __syncwarp();
+                if (lane == 0) Bv[jj - 1] = temp;
+                for (int i = jj - 1 - lane; i >= max(1, jj - K); i -= 32) Bv[i - 1] = Bv[i - 1] - temp * __ldg(&A_(Lc + i, jj));
+            }
+            __syncwarp();
+        }
+    }
+#undef A_
+    __syncthreads();
+    for (int q = tid; q < n; q += blockDim.x) {
+        const int kq = q % N, iq = q / N;
+        if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1) store_stream<TR>(L, err, iq, kq, (TR)Bv[q], Vbc);
+    }
+    pdl_done();
+}
+void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                         int n, int kl, int ku, double* err, int Vbc) {
+    const size_t sm = sizeof(double) * (size_t)n;
+    cudaFuncSetAttribute(k_coarse_solve<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    launch_pdl(k_coarse_solve<double>, 1, 256, sm, s, lv.L, band, ipiv, rowb, (const double*)lv.rhs, n, kl, ku, err,
+               Vbc); tc_note_launch();
+}
+void launch_coarse_solve32(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                           int n, int kl, int ku, float* err, int Vbc) {
+    const size_t sm = sizeof(double) * (size_t)n;
+    cudaFuncSetAttribute(k_coarse_solve<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    launch_pdl(k_coarse_solve<float>, 1, 256, sm, s, lv.L, band, ipiv, rowb, (const float*)lv.rhs32, n, kl, ku, err,
+               Vbc); tc_note_launch();
 }
 
 __global__ void k_copy(double* dst, const double* src, size_t n) {

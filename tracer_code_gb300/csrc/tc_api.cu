@@ -48,6 +48,11 @@ namespace {
 const double kPi = 3.1415926535897932;
 
 struct CycleGraphs;
+// largest coarse grid (unknowns) solved through an explicit inverse (a
+// matrix-vector product per visit, n^2 doubles); larger ones use banded
+// substitution with the LU factors each visit
+constexpr int kCoarseInverseMax = 2048;
+
 struct Handle {
     tc_params p{};
     int nx = 0, nz = 0, grids = 0, nsteps = 0, ntype = 0;
@@ -94,6 +99,9 @@ struct Handle {
     long long nequalize = 0;
     std::vector<int64_t> eq_row;
     double *band = nullptr, *rowb = nullptr, *bvec = nullptr, *ainv = nullptr;
+    // coarse grids above kCoarseInverseMax unknowns are solved by banded
+    // substitution each visit instead of an explicit inverse
+    bool coarse_banded = false;
     int* ipiv = nullptr;
     double* rows = nullptr;
     RedScratch rs{};
@@ -554,7 +562,11 @@ void enqueue_cycle_rest(Handle* h) {
         if (level < G) {
             iterate_stream(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
         } else {
-            launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_err(h, G), h->p.Vbc);
+            if (h->coarse_banded)
+                launch_coarse_solve(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku,
+                                    cur_err(h, G), h->p.Vbc);
+            else
+                launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_err(h, G), h->p.Vbc);
         }
         restricted = f.rst != 0;
         pending_pro = false;
@@ -657,6 +669,9 @@ void enqueue_rest_mixed(Handle* h, int) {
                               zero);
         const StepFusion f = step_fusion(h, pp);
         if (level < G) iterate_stream32(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
+        else if (h->coarse_banded)
+            launch_coarse_solve32(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku,
+                                  cur_e32(h, G), h->p.Vbc);
         else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_e32(h, G), h->p.Vbc);
         restricted = f.rst != 0;
         pending_pro = false;
@@ -744,7 +759,8 @@ tc_status multigrid(Handle* h) {
     auto coarse_setup = [&]() {
         launch_coarse_build(h->st, h->lev[G], h->band, h->rowb, h->kl, h->ku, h->p.Vbc);
         launch_coarse_lu(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ds);
-        launch_coarse_inverse(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ainv, h->bvec);
+        if (!h->coarse_banded)
+            launch_coarse_inverse(h->st, h->band, h->ipiv, h->ngrid_coarse, h->kl, h->ku, h->ainv, h->bvec);
         h->lu_valid = true;
     };
     // SF = error(1); compute_velocities; compute_strain_rate_invariant
@@ -1226,8 +1242,11 @@ tc_status create(Handle* h, const tc_params* in) {
     const int ldab = 2 * h->kl + h->ku + 1;
     TRY(dalloc_t(h, &h->band, (size_t)ldab * h->ngrid_coarse));
     TRY(dalloc_t(h, &h->rowb, (size_t)h->ngrid_coarse));
-    TRY(dalloc_t(h, &h->ainv, (size_t)h->ngrid_coarse * h->ngrid_coarse));
-    TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
+    h->coarse_banded = h->ngrid_coarse > kCoarseInverseMax;
+    if (!h->coarse_banded) {
+        TRY(dalloc_t(h, &h->ainv, (size_t)h->ngrid_coarse * h->ngrid_coarse));
+        TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
+    }
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
     if (h->fuse_visits) TRY(dalloc_t(h, &h->ctab, (size_t)128 * 4096));
     TRY(dalloc_t(h, &h->rows, (size_t)8 * (nz + 1)));

@@ -135,6 +135,10 @@ void launch_coarse_build(cudaStream_t s, const Level& lv, double* band, double* 
 void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, int ku, DevScalars* ds);
 void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, int n, int kl, int ku, double* Ainv,
                            double* bscratch);
+void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                         int n, int kl, int ku, double* err, int Vbc);
+void launch_coarse_solve32(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
+                           int n, int kl, int ku, float* err, int Vbc);
 void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
                          int Vbc);
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n);
