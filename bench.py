@@ -481,6 +481,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-shipped", action="store_true",
+                    help="two timesteps of the reference's shipped configuration (for ncu)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling case: upload the workload, run one multigrid solve, exit")
     ap.add_argument("--solver", default="plain", choices=["plain", "mixed"],
@@ -510,6 +512,19 @@ def main():
         torch.cuda.synchronize()
         print(json.dumps({"profile_net": True, "loss": loss}), flush=True)
         net.close()
+        return
+    if args.profile_shipped:
+        from tracer_code_gb300 import Simulation, state
+        p = shipped_params()
+        sim = Simulation(p)
+        sim.upload(state.initial_state(p, seed=1))
+        out = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            row, q, dt = sim.step()
+            out.append({"cycles": q, "s": round(time.perf_counter() - t0, 4), "moved": (sim.equalize_row() or [0] * 5)[4]})
+        print(json.dumps({"profile_shipped": True, "steps": out}), flush=True)
+        sim.close()
         return
     if args.profile_solve:
         from tracer_code_gb300 import Simulation, state
