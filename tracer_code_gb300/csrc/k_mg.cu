@@ -768,33 +768,33 @@ void launch_coarse_inverse(cudaStream_t s, const double* band, const int* ipiv, 
 }
 
 // Coarsest-level solve as x = A^-1 (RowB .* RHS) (Compute_coarse_vector,
-// DGBTRS, Stream_grid_coarse): one warp per interior unknown, the boundary
-// unknowns are zero (walls); ghosts are written with the stream BCs.
+// DGBTRS, Stream_grid_coarse): one warp per interior unknown (the boundary
+// unknowns are zero: walls), the sum running over the interior unknowns
+// listed in cq (their coarse-level offsets in cx); ghosts are written with
+// the stream BCs.
 __global__ void k_coarse_apply(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
-                               const double* rhs, int n, double* err, int Vbc) {
+                               const double* rhs, int n, const int* __restrict__ cq, const int* __restrict__ cx,
+                               int m, double* err, int Vbc) {
     pdl_entry();
     const int lane = threadIdx.x & 31;
-    const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // 0-based row
-    if (pw >= n) return;
-    const int nzc = L.b, nxc = L.a, N = nzc + 1;
-    const int kp = pw % N, ip = pw / N;
-    if (ip < 1 || ip > nxc - 1 || kp < 1 || kp > nzc - 1) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= m) return;
+    const int pw = __ldg(cq + w), N = L.b + 1;
     const double* row = Ainv + (size_t)pw * n;
     double acc = 0.0;
-    for (int q = lane; q < n; q += 32) {
-        const int kq = q % N, iq = q / N;
-        if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
-            acc = fma(__ldg(row + q), ld_state(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+    for (int e = lane; e < m; e += 32) {
+        const int q = __ldg(cq + e);
+        acc = fma(__ldg(row + q), ld_state(rhs + __ldg(cx + e)) * __ldg(rowb + q), acc);
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) store_stream(L, err, ip, kp, acc, Vbc);
+    if (lane == 0) store_stream(L, err, pw / N, pw % N, acc, Vbc);
     pdl_done();
 }
-void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
-                         int Vbc) {
+void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n,
+                         const int* cq, const int* cx, int m, double* err, int Vbc) {
     const int threads = 256;
-    const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
-    launch_pdl(k_coarse_apply, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs, n, err, Vbc); tc_note_launch();
+    const unsigned nb = (unsigned)((m * 32 + threads - 1) / threads);
+    launch_pdl(k_coarse_apply, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs, n, cq, cx, m, err, Vbc); tc_note_launch();
 }
 
 // Coarsest-level solve for coarse grids too large for an explicit inverse:

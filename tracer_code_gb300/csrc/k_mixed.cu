@@ -138,24 +138,23 @@ __global__ void k_update64(Lay L, Range2 r, double* S, const float* e, int Vbc) 
 }
 
 // coarsest level: x = A^-1 (RowB .* rhs) in FP64 from the FP32 RHS, stored as FP32
+// (one warp per interior unknown; cq/cx list the interior unknowns)
 __global__ void k_coarse_apply32(Lay L, const double* __restrict__ Ainv, const double* __restrict__ rowb,
-                                 const float* rhs, int n, float* err, int Vbc) {
+                                 const float* rhs, int n, const int* __restrict__ cq, const int* __restrict__ cx,
+                                 int m, float* err, int Vbc) {
     pdl_entry();
     const int lane = threadIdx.x & 31;
-    const int pw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (pw >= n) return;
-    const int nzc = L.b, nxc = L.a, N = nzc + 1;
-    const int kp = pw % N, ip = pw / N;
-    if (ip < 1 || ip > nxc - 1 || kp < 1 || kp > nzc - 1) return;
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (w >= m) return;
+    const int pw = __ldg(cq + w), N = L.b + 1;
     const double* row = Ainv + (size_t)pw * n;
     double acc = 0.0;
-    for (int q = lane; q < n; q += 32) {
-        const int kq = q % N, iq = q / N;
-        if (iq >= 1 && iq <= nxc - 1 && kq >= 1 && kq <= nzc - 1)
-            acc = fma(__ldg(row + q), (double)ld_state(rhs + IX(L, iq, kq)) * __ldg(rowb + q), acc);
+    for (int e = lane; e < m; e += 32) {
+        const int q = __ldg(cq + e);
+        acc = fma(__ldg(row + q), (double)ld_state(rhs + __ldg(cx + e)) * __ldg(rowb + q), acc);
     }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (lane == 0) store_stream<float>(L, err, ip, kp, (float)acc, Vbc);
+    if (lane == 0) store_stream<float>(L, err, pw / N, pw % N, (float)acc, Vbc);
     pdl_done();
 }
 
@@ -231,9 +230,9 @@ void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e,
     launch_pdl(k_update64, grid_for(r), dim3(BX, BY), 0, s, lv.L, r, S, e, Vbc); tc_note_launch();
 }
 
-void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
-                           int Vbc) {
+void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n,
+                           const int* cq, const int* cx, int m, float* err, int Vbc) {
     const int threads = 256;
-    const unsigned nb = (unsigned)((n * 32 + threads - 1) / threads);
-    launch_pdl(k_coarse_apply32, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs32, n, err, Vbc); tc_note_launch();
+    const unsigned nb = (unsigned)((m * 32 + threads - 1) / threads);
+    launch_pdl(k_coarse_apply32, nb, threads, 0, s, lv.L, Ainv, rowb, lv.rhs32, n, cq, cx, m, err, Vbc); tc_note_launch();
 }

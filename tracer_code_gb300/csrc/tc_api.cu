@@ -102,6 +102,9 @@ struct Handle {
     // coarse grids above kCoarseInverseMax unknowns are solved by banded
     // substitution each visit instead of an explicit inverse
     bool coarse_banded = false;
+    // interior unknowns of the coarsest grid: index p and level offset
+    int *coarse_q = nullptr, *coarse_x = nullptr;
+    int coarse_m = 0;
     int* ipiv = nullptr;
     double* rows = nullptr;
     RedScratch rs{};
@@ -566,7 +569,8 @@ void enqueue_cycle_rest(Handle* h) {
                 launch_coarse_solve(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku,
                                     cur_err(h, G), h->p.Vbc);
             else
-                launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_err(h, G), h->p.Vbc);
+                launch_coarse_apply(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, h->coarse_q, h->coarse_x,
+                                    h->coarse_m, cur_err(h, G), h->p.Vbc);
         }
         restricted = f.rst != 0;
         pending_pro = false;
@@ -672,7 +676,8 @@ void enqueue_rest_mixed(Handle* h, int) {
         else if (h->coarse_banded)
             launch_coarse_solve32(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku,
                                   cur_e32(h, G), h->p.Vbc);
-        else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, cur_e32(h, G), h->p.Vbc);
+        else launch_coarse_apply32(h->st, h->lev[G], h->ainv, h->rowb, h->ngrid_coarse, h->coarse_q, h->coarse_x,
+                                   h->coarse_m, cur_e32(h, G), h->p.Vbc);
         restricted = f.rst != 0;
         pending_pro = false;
         if (h->multi[pp + 1] < h->multi[pp]) {
@@ -1246,6 +1251,19 @@ tc_status create(Handle* h, const tc_params* in) {
     if (!h->coarse_banded) {
         TRY(dalloc_t(h, &h->ainv, (size_t)h->ngrid_coarse * h->ngrid_coarse));
         TRY(dalloc_t(h, &h->bvec, (size_t)(h->ngrid_coarse + 8) * h->ngrid_coarse));
+        // interior unknowns p = i*(nzc+1) + k in increasing order, with their offsets
+        const Lay Lc = make_lay(nx >> (G - 1), nz >> (G - 1));
+        std::vector<int> cq, cx;
+        for (int i = 1; i <= Lc.a - 1; i++)
+            for (int k = 1; k <= Lc.b - 1; k++) {
+                cq.push_back(i * (Lc.b + 1) + k);
+                cx.push_back((int)IX(Lc, i, k));
+            }
+        h->coarse_m = (int)cq.size();
+        TRY(dalloc_t(h, &h->coarse_q, cq.size()));
+        TRY(dalloc_t(h, &h->coarse_x, cx.size()));
+        CK(cudaMemcpy(h->coarse_q, cq.data(), sizeof(int) * cq.size(), cudaMemcpyHostToDevice));
+        CK(cudaMemcpy(h->coarse_x, cx.data(), sizeof(int) * cx.size(), cudaMemcpyHostToDevice));
     }
     TRY(dalloc_t(h, &h->ipiv, (size_t)h->ngrid_coarse));
     if (h->fuse_visits) TRY(dalloc_t(h, &h->ctab, (size_t)128 * 4096));

@@ -139,8 +139,8 @@ void launch_coarse_solve(cudaStream_t s, const Level& lv, const double* band, co
                          int n, int kl, int ku, double* err, int Vbc);
 void launch_coarse_solve32(cudaStream_t s, const Level& lv, const double* band, const int* ipiv, const double* rowb,
                            int n, int kl, int ku, float* err, int Vbc);
-void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, double* err,
-                         int Vbc);
+void launch_coarse_apply(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n,
+                         const int* cq, const int* cx, int m, double* err, int Vbc);
 void launch_copy_plane(cudaStream_t s, double* dst, const double* src, size_t n);
 
 // (k_visit.cu) one whole smoother visit of a small level as one cluster launch
@@ -187,8 +187,8 @@ void launch_prolong_into64(cudaStream_t s, const Level& coarse, const Level& fin
                            int Vbc);
 void launch_residual_to32(cudaStream_t s, const Level& lv, const double* S, float* rhs32, float* zero = nullptr);
 void launch_update64(cudaStream_t s, const Level& lv, double* S, const float* e, int Vbc);
-void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n, float* err,
-                           int Vbc);
+void launch_coarse_apply32(cudaStream_t s, const Level& lv, const double* Ainv, const double* rowb, int n,
+                           const int* cq, const int* cx, int m, float* err, int Vbc);
 void launch_rhs1(cudaStream_t s, const Lay& L, const Phys& P, const double* Tbuoy, const double* const* Cbuoy,
                  double* rhs, RedScratch rs, DevScalars* ds);
 
