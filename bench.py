@@ -101,8 +101,8 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{index}.csv") if os.path.isdir(
-            os.path.join(ROOT, "gpurun_out")) else f"/tmp/tc_clocks_{os.getpid()}_{index}.csv"
+        out_dir = os.environ.get("TC_CLOCK_LOG_DIR", "/tmp")
+        self.path = os.path.join(out_dir, f"tc_clocks_{os.getpid()}_{index}.csv")
 
     def __enter__(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"

@@ -1,6 +1,6 @@
 // oracle.cpp -- CPU restatement of the reference hot path (TEST INFRASTRUCTURE).
 //
-// This file is the checker for the GB300 library, never part of it: only the
+// This file is test infrastructure for the GB300 library, never part of it: only the
 // tests, the smoke check and the CPU-baseline leg of the benchmark load the
 // shared object built from it.  It restates, routine by routine and in the
 // reference's own floating-point operation order, the Fortran/OpenMP code of

@@ -1,6 +1,6 @@
 """ctypes binding of the CPU oracle (TEST INFRASTRUCTURE ONLY).
 
-Only the tests, ``__graft_entry__.smoke()`` (as the checker) and the CPU
+Only the tests, ``__graft_entry__.smoke()`` (to compare against) and the CPU
 baseline leg of ``bench.py`` may import this module.  It exposes the same
 methods as ``tracer_code_gb300.Simulation`` so a parity test runs both on the
 same inputs.

@@ -1,7 +1,7 @@
 """GPU parity: the CUDA path (through its C ABI) against the CPU oracle on
 the same seeded inputs.
 
-Bit-exact where the benchmark spec asks for it (tracer positions, cell indices
+Bit-exact where the parity contract asks for it (tracer positions, cell indices
 and per-cell counts given identical velocities; the kernels that feed them),
 within stated tolerances elsewhere:
   - streamfunction: |SF_gpu - SF_cpu|_max <= 1e-9 |SF|_max, same cycle count,
