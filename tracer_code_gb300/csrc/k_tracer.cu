@@ -615,17 +615,53 @@ __global__ void k_eq_sort_lists(EqDev E) {
         a[q + 1] = v;
     }
 }
-// composition.f90:188-199: each rank shuffles the lists of its share of columns
+// mzran with the stream state held in registers (same draws as eq_mzran)
+struct EqMz {
+    int i, j, k, n;
+};
+__device__ __forceinline__ double eq_mz_next(EqMz& m) {
+    int r = m.i - m.k;
+    if (r < 0) r += 2147483579;
+    m.i = m.j;
+    m.j = m.k;
+    m.k = r;
+    m.n = (int)(69069u * (unsigned)m.n + 1013904243u);
+    r = (int)((unsigned)r + (unsigned)m.n);
+    return 0.5 + (0.2328306e-9) * (double)r;
+}
+// composition.f90:188-199: each rank shuffles the lists of its share of
+// columns; a list of up to 64 ids is shuffled in a thread-local copy
 __global__ void k_eq_shuffle_lists(EqDev E) {
     const int rank = blockIdx.x * blockDim.x + threadIdx.x;
     if (rank >= E.NR) return;
+    const int NR = E.NR;
+    EqMz m{E.sd[rank], E.sd[NR + rank], E.sd[2 * NR + rank], E.sd[3 * NR + rank]};
+    int loc[65];
     int lo, cnt;
-    eq_static(E.nx + 1, E.NR, rank, lo, cnt);
+    eq_static(E.nx + 1, NR, rank, lo, cnt);
     for (int i = lo; i < lo + cnt; i++)
         for (int k = 0; k <= E.nz; k++) {
             const size_t c = eq_cell(E, i, k);
-            eq_shuffle(E.ids + E.off[c] - 1, 1, E.off[c + 1] - E.off[c], E.sd, rank, E.NR);
+            int* a = E.ids + E.off[c] - 1;  // a[1..N]
+            const int N = E.off[c + 1] - E.off[c];
+            const bool small = N <= 64;
+            if (small)
+                for (int q = 1; q <= N; q++) loc[q] = a[q];
+            int* b = small ? loc : a;
+            for (int q = 1; q <= N - 1; q++) {
+                const double ran = eq_mz_next(m);
+                const int r = (int)floor(ran * (double)(N - q)) + q + 1;
+                const int t = b[q];
+                b[q] = b[r];
+                b[r] = t;
+            }
+            if (small)
+                for (int q = 1; q <= N; q++) a[q] = loc[q];
         }
+    E.sd[rank] = m.i;
+    E.sd[NR + rank] = m.j;
+    E.sd[2 * NR + rank] = m.k;
+    E.sd[3 * NR + rank] = m.n;
 }
 
 __device__ __forceinline__ int* eq_D(const EqDev& E, int rank, int t) {
