@@ -481,6 +481,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-step", metavar="NXxNZ", default=None,
+                    help="one timestep of the workload's physics on a smaller grid (for ncu), e.g. 512x128")
     ap.add_argument("--profile-shipped", action="store_true",
                     help="two timesteps of the reference's shipped configuration (for ncu)")
     ap.add_argument("--profile-solve", action="store_true",
@@ -512,6 +514,16 @@ def main():
         torch.cuda.synchronize()
         print(json.dumps({"profile_net": True, "loss": loss}), flush=True)
         net.close()
+        return
+    if args.profile_step:
+        from tracer_code_gb300 import Simulation, state, scaled_config
+        nx, nz = (int(v) for v in args.profile_step.lower().split("x"))
+        p = scaled_config(workload_params(args.solver), nx, nz)
+        sim = Simulation(p)
+        sim.upload(state.initial_state(p, seed=1))
+        row, q, dt = sim.step()
+        print(json.dumps({"profile_step": True, "grid": [nx, nz], "tracers": int(sim.ntr), "cycles": q}), flush=True)
+        sim.close()
         return
     if args.profile_shipped:
         from tracer_code_gb300 import Simulation, state
