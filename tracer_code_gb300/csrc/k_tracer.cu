@@ -10,39 +10,102 @@
 // therefore cell indices equal the CPU restatement bit for bit.
 #include "tc_device.cuh"
 
+// Cell indices of a tracer: int(x/h) and nint(x/h) of the correctly rounded
+// quotient, as composition.f90 takes them, without the FP64 division (on this
+// GPU the FP64 pipe, not memory, bounds the tracer kernels).  The 64 high bits
+// of the product of the significands of x and hinv = RN(1/h) give x*hinv in
+// fixed point with 64 fraction bits; for 0 < x/h < 2^21 this value, x/h and
+// RN(x/h) lie within 2^-30 of one another (hinv contributes 2^-53 relative, the
+// truncated product 2^-43 absolute, RN(x/h) 2^-53 relative).  When the fraction
+// is farther than 2^-24 from the boundary in question (an integer for int(),
+// a half-integer for nint()), RN(x/h) lies on the same side of it as the
+// fixed-point value and the index is read off the bits; otherwise, and for x
+// outside that range, the division is done.  Either way the result equals
+// that of the division.
+struct QuotFix {
+    unsigned long long ip, fr;  // integer part, fraction * 2^64
+    bool ok;
+};
+__device__ __forceinline__ QuotFix quot_fix(double x, double hinv) {
+    const unsigned long long bx = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long bh = (unsigned long long)__double_as_longlong(hinv);
+    const int ex = (int)(bx >> 52), eh = (int)(bh >> 52) & 0x7ff;   // ex includes the sign bit
+    const unsigned long long mx = ((bx & 0xfffffffffffffull) | (1ull << 52)) << 11;
+    const unsigned long long mh = ((bh & 0xfffffffffffffull) | (1ull << 52)) << 11;
+    const unsigned long long p = __umul64hi(mx, mh);    // in [2^62, 2^64)
+    const int sh = 2108 - ex - eh;                      // x*hinv = p / 2^sh
+    QuotFix q;
+    q.ok = ex > 0 && ex < 0x7ff && sh >= 43 && sh < 128;
+    if (sh >= 43 && sh < 64) {
+        q.ip = p >> sh;
+        q.fr = p << (64 - sh);
+    } else {
+        q.ip = 0;
+        q.fr = (sh >= 64 && sh < 128) ? (sh == 64 ? p : p >> (sh - 64)) : 0;
+    }
+    return q;
+}
+constexpr unsigned long long kQuotGuard = 1ull << 40;  // 2^-24 in fraction units
+__device__ __forceinline__ int quot_trunc(double x, double h, double hinv) {
+    const QuotFix q = quot_fix(x, hinv);
+    if (q.ok && q.fr > kQuotGuard && q.fr < 0ull - kQuotGuard) return (int)q.ip;
+    return (int)(x / h);
+}
+__device__ __forceinline__ int quot_nint(double x, double h, double hinv) {
+    const QuotFix q = quot_fix(x, hinv);
+    const unsigned long long half = 1ull << 63;
+    if (q.ok && (q.fr > half + kQuotGuard || q.fr < half - kQuotGuard)) return (int)q.ip + (q.fr > half ? 1 : 0);
+    return (int)round(x / h);
+}
+
 // interpolate (composition.f90:838-898) with order=2: one r-derivative table
-// DER(1,i,k) and a 3-point s-stencil; int() truncates, as in Fortran.
-__device__ __forceinline__ double interp_taylor(const Lay& L, const Phys& P, const double* __restrict__ f,
-                                                const double* __restrict__ der, double r, double s) {
-    const int i = (int)(r / P.dr);
-    const int k = (int)(s / P.ds);
+// DER(1,i,k) and a 3-point s-stencil; int() truncates, as in Fortran.  The
+// position part (cell, offsets, branch) is shared by every field
+// interpolated at the same point.
+struct TaylorPos {
+    int i, k;      // column of the r-Taylor step (i or i+1) and the s cell
+    double a1;     // r offset from that column
+    double hs;     // s offset (from k, or ds minus it on the upper branch)
+    bool slo;      // hs <= ds/2
+};
+__device__ __forceinline__ TaylorPos taylor_pos(const Phys& P, double r, double s) {
+    TaylorPos t;
+    const int i = quot_trunc(r, P.dr, P.rdr);
+    t.k = quot_trunc(s, P.ds, P.rds);
     double hr = r - (double)i * P.dr;
-    double fR0, fR1, fR2, fR3;  // jj = -1, 0, 1, 2
     if (hr <= P.dro2) {
-        const double a1 = hr / 1.0;
-        fR0 = __ldg(f + IX(L, i, k - 1)) + __ldg(der + IX(L, i, k - 1)) * a1;
-        fR1 = __ldg(f + IX(L, i, k)) + __ldg(der + IX(L, i, k)) * a1;
-        fR2 = __ldg(f + IX(L, i, k + 1)) + __ldg(der + IX(L, i, k + 1)) * a1;
-        fR3 = __ldg(f + IX(L, i, k + 2)) + __ldg(der + IX(L, i, k + 2)) * a1;
+        t.i = i;
+        t.a1 = hr / 1.0;
     } else {
         hr = P.dr - hr;
-        const double a1 = (-hr) / 1.0;
-        fR0 = __ldg(f + IX(L, i + 1, k - 1)) + __ldg(der + IX(L, i + 1, k - 1)) * a1;
-        fR1 = __ldg(f + IX(L, i + 1, k)) + __ldg(der + IX(L, i + 1, k)) * a1;
-        fR2 = __ldg(f + IX(L, i + 1, k + 1)) + __ldg(der + IX(L, i + 1, k + 1)) * a1;
-        fR3 = __ldg(f + IX(L, i + 1, k + 2)) + __ldg(der + IX(L, i + 1, k + 2)) * a1;
+        t.i = i + 1;
+        t.a1 = (-hr) / 1.0;
     }
-    double hs = s - (double)k * P.ds;
+    const double hs = s - (double)t.k * P.ds;
+    t.slo = hs <= P.dso2;
+    t.hs = t.slo ? hs : P.ds - hs;
+    return t;
+}
+__device__ __forceinline__ double taylor_eval(const Lay& L, const Phys& P, const double* __restrict__ f,
+                                              const double* __restrict__ der, const TaylorPos& t) {
+    const int i = t.i, k = t.k;
+    const double fR0 = __ldg(f + IX(L, i, k - 1)) + __ldg(der + IX(L, i, k - 1)) * t.a1;
+    const double fR1 = __ldg(f + IX(L, i, k)) + __ldg(der + IX(L, i, k)) * t.a1;
+    const double fR2 = __ldg(f + IX(L, i, k + 1)) + __ldg(der + IX(L, i, k + 1)) * t.a1;
+    const double fR3 = __ldg(f + IX(L, i, k + 2)) + __ldg(der + IX(L, i, k + 2)) * t.a1;
     double fin;
-    if (hs <= P.dso2) {
+    if (t.slo) {
         double DERs = (-0.5 * fR0 + 0.5 * fR2) / P.ds;
-        fin = fR1 + DERs * (hs / 1.0);
+        fin = fR1 + DERs * (t.hs / 1.0);
     } else {
-        hs = P.ds - hs;
         double DERs = (-0.5 * fR1 + 0.5 * fR3) / P.ds;
-        fin = fR2 + DERs * ((-hs) / 1.0);
+        fin = fR2 + DERs * ((-t.hs) / 1.0);
     }
     return fin;
+}
+__device__ __forceinline__ double interp_taylor(const Lay& L, const Phys& P, const double* __restrict__ f,
+                                                const double* __restrict__ der, double r, double s) {
+    return taylor_eval(L, P, f, der, taylor_pos(P, r, s));
 }
 
 // Temperature tracers (tracer = 1): the tracer_space value at the stage
@@ -72,11 +135,12 @@ __global__ void k_tracer_stage(Lay L, Phys P, int torder, int stage, int64_t ntr
     // positions outside the box were already reported by the histogram that
     // precedes every stage (the reference stops there); never index with them
     if (!(r > 0.0 && r < P.aspect && s > 0.0 && s < 1.0)) return;
-    const double tr = interp_taylor(L, P, u, du, r, s);
-    const double ts = interp_taylor(L, P, w, dw, r, s);
+    const TaylorPos tp = taylor_pos(P, r, s);
+    const double tr = taylor_eval(L, P, u, du, tp);
+    const double ts = taylor_eval(L, P, w, dw, tp);
     if (tT.f) {
         // energy.f90:213-223, 292-310, 371-375, 437-440
-        const double te = interp_taylor(L, P, tT.f, tT.der, r, s);
+        const double te = taylor_eval(L, P, tT.f, tT.der, tp);
         if (stage == 1) {
             tT.acc[id] = te;
             tT.out[id] = tT.T0[id] + ((torder == 2) ? dt : 0.5 * dt) * te;
@@ -205,8 +269,8 @@ __global__ void k_histogram(Lay L, Phys P, int64_t ntr, const double* __restrict
         if (r <= 0.0 || r >= P.aspect || s <= 0.0 || s >= 1.0) {
             atomicOr(flag, 1);
         } else {
-            const int i = (int)round(r / P.dr);
-            const int k = (int)round(s / P.ds);
+            const int i = quot_nint(r, P.dr, P.rdr);
+            const int k = quot_nint(s, P.ds, P.rds);
             const int t = ttype[id];
             if (t < 0 || t > P.ntype || i < 0 || i > P.nx || k < 0 || k > P.nz) atomicOr(flag, 2);
             else {
@@ -327,7 +391,7 @@ void launch_tracer_space(cudaStream_t s, const Lay& L, const Phys& P, const doub
 // perm[j] is the reference's index of the tracer stored at slot j.
 namespace {
 __device__ __forceinline__ int tracer_cell(const Lay& L, const Phys& P, double r, double s) {
-    int i = (int)round(r / P.dr), k = (int)round(s / P.ds);
+    int i = quot_nint(r, P.dr, P.rdr), k = quot_nint(s, P.ds, P.rds);
     i = min(max(i, 0), P.nx);
     k = min(max(k, 0), P.nz);
     return (int)IX(L, i, k);

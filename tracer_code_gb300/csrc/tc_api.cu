@@ -1165,6 +1165,7 @@ tc_status create(Handle* h, const tc_params* in) {
     P.nx = nx; P.nz = nz; P.ntype = h->ntype; P.comp = p.comp; P.ivis = p.ivis; P.Tbot = p.Tbot; P.Vbc = p.Vbc;
     P.torder = p.torder; P.tracer = p.tracer; P.aspect = p.aspect; P.dr = s1.dr; P.ds = s1.ds; P.dr2 = s1.dr2; P.ds2 = s1.ds2;
     P.dro2 = 0.5 * s1.dr; P.dso2 = 0.5 * s1.ds; P.RaT = p.RaT;
+    P.rdr = 1.0 / s1.dr; P.rds = 1.0 / s1.ds;
     P.lnvisT = std::log(p.visT); P.lnvisP = std::log(p.visP); P.visT2 = p.visT * p.visT; P.H = p.H;
     P.visT = p.visT; P.yield = p.yield; P.yield_gradient = p.yield_gradient; P.yield_depth = p.yield_depth;
     for (int t = 0; t < TC_MAX_TYPES; t++) {

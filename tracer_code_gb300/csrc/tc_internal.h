@@ -103,6 +103,7 @@ struct Level {
 struct Phys {
     int nx, nz, ntype, comp, ivis, Tbot, Vbc, torder, tracer;
     double aspect, dr, ds, dr2, ds2, dro2, dso2;
+    double rdr, rds;             // 1/dr, 1/ds rounded (tracer cell indices: quot_trunc, quot_nint)
     double RaT, RaC[TC_MAX_TYPES], lnvisT, lnvisP, lnvisC[TC_MAX_TYPES], visT2, H, Htype[TC_MAX_TYPES];
     double lncf[TC_MAX_TYPES];   // log(1/conduct_factor)
     double courantT, courantC;
