@@ -288,3 +288,40 @@ def test_blocked_sweeps_match_single_sweeps(gpu_lib, prec, ns, nx, nz, grids):
         assert np.array_equal(a, b)
 
 
+
+
+@pytest.mark.parametrize("mk", [case_128_like, case_1024_like])
+def test_energy_time_bitexact_with_tracers_on_cell_boundaries(gpu_lib, mk):
+    """Half of the tracers start where int(x/h) or nint(x/h) changes: exact
+    multiples and half multiples of dr and ds, and the doubles just below and
+    above them.  The GPU reads these cell indices off a fixed-point product
+    and divides only near such boundaries; positions, counts, C and T must
+    still equal the oracle's (which divides) bit for bit."""
+    p = mk()
+    p.RK_update = 0
+    st = fresh_state(p)
+    m = st["rtr"].size // 2
+    rng = np.random.default_rng(11)
+    kind = rng.integers(0, 6, m)
+    off = np.where(kind % 2 == 0, 0.0, 0.5)
+    side = kind // 2  # 0: on the boundary, 1: next double up, 2: next double down
+
+    def place(n, h):
+        x = (rng.integers(1, n, m).astype(np.float64) + off) * h
+        x = np.where(side == 1, np.nextafter(x, np.inf), x)
+        return np.where(side == 2, np.nextafter(x, -np.inf), x)
+
+    st["rtr"][:m] = place(p.nx, p.aspect / p.nx)
+    st["str"][:m] = place(p.nz, 1.0 / p.nz)
+    g, o = pair(p, st)
+    g.multigrid()
+    o.set("SF", g.download()["SF"])
+    g.compute_velocities()
+    o.compute_velocities()
+    assert g.energy_time() == o.energy_time()
+    a, b = g.download(), o.download()
+    assert np.array_equal(a["rtr"], b["rtr"])
+    assert np.array_equal(a["str"], b["str"])
+    assert np.array_equal(g.counts(), o.counts())
+    assert np.array_equal(a["Cnew"], b["Cnew"])
+    assert np.array_equal(a["T"], b["T"])
