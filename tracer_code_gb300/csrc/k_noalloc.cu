@@ -21,8 +21,15 @@
 // Set-up: the array's host-side name is only a stand-in, not a device
 // address, so the entry point looks up the device address once per device
 // (cudaGetSymbolAddress, with that device current) on its first call there
-// and caches it.  Make that first call on a device before capturing any
-// stream on it.
+// and caches it together with the device's current context.  A call that
+// finds another context current on that device (after cudaDeviceReset, or
+// when the primary context was released and created again, which may load
+// the module at another address) looks the address up again.  Make the first
+// call on a device before capturing any stream on it.
+//
+// Errors: the launches' own return codes and the stream synchronisation are
+// checked; the runtime's last-error state is neither read nor cleared, so an
+// error that the caller's own code left pending stays the caller's.
 //
 // The kernels are a variant of k_stats_rows / k_stats_final (k_field.cu)
 // that read the reference's own array layouts (no padding) and take their
@@ -173,23 +180,60 @@ __global__ void k_na_nempty(RefLayout R, const int* __restrict__ ne, NoAllocScra
 
 std::mutex g_na_mutex;
 NoAllocScratch* g_na_ptr[256] = {};
+void* g_na_ctx[256] = {};
 
-// Device address of the fixed array on the current device (looked up on the
-// first call per device, with that device current).
+// cuCtxGetCurrent from the driver, reached through the runtime so that the
+// library needs no link against libcuda.
+typedef int (*CtxGetCurrentFn)(void**);
+CtxGetCurrentFn g_ctx_get = nullptr;
+bool g_ctx_get_tried = false;
+
+// Device address of the fixed array on the current device: looked up on the
+// first call per device (with that device current) and again whenever the
+// device's current context differs from the one the address was found in.
 cudaError_t na_scratch(NoAllocScratch** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+    // make the runtime bind the device's primary context before reading it
+    e = cudaFree(nullptr);
+    if (e != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (g_na_ptr[dev] == nullptr) {
+    if (!g_ctx_get_tried) {
+        g_ctx_get_tried = true;
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            g_ctx_get = (CtxGetCurrentFn)fn;
+    }
+    void* ctx = nullptr;
+    if (g_ctx_get == nullptr || g_ctx_get(&ctx) != 0 || ctx == nullptr) {
+        // no context identity available: look the address up on every call
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, tc_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        *out = (NoAllocScratch*)p;
+        return cudaSuccess;
+    }
+    if (g_na_ptr[dev] == nullptr || g_na_ctx[dev] != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, tc_noalloc_scratch);
         if (e != cudaSuccess) return e;
         g_na_ptr[dev] = (NoAllocScratch*)p;
+        g_na_ctx[dev] = ctx;
     }
     *out = g_na_ptr[dev];
     return cudaSuccess;
+}
+
+// One launch whose status is its own return code (the runtime's last-error
+// state is left alone).
+template <typename... A>
+cudaError_t na_launch(void (*kern)(A...), dim3 grid, dim3 block, cudaStream_t st, A... args) {
+    void* argv[] = {(void*)&args...};
+    return cudaLaunchKernel((const void*)kern, grid, block, argv, 0, st);
 }
 
 }  // namespace
@@ -207,13 +251,19 @@ extern "C" tc_status tc_stats_noalloc(const double* T, const double* u, const do
     cudaStream_t st = (cudaStream_t)stream;
     RefLayout R{nx, nz, nx + 5, nx + 3, ntype};
     Consts c{aspect / (double)nx, 1.0 / (double)nz, RaT};
-    k_na_rows<<<(nz + 1 + 63) / 64, 64, 0, st>>>(R, c, T, u, w, conduct, vis, Cnew, S);
-    k_na_final<<<1, 32, 0, st>>>(R, c, kent, T, u, w, conduct, S);
-    if (ntype > 0) {
-        k_na_nempty_init<<<1, 1, 0, st>>>(S);
-        k_na_nempty<<<dim3((unsigned)((nx + 1 + 127) / 128), (unsigned)(nz + 1)), 128, 0, st>>>(R, nempty, S);
-    }
-    tc_note_launch(ntype > 0 ? 4 : 2);
+    // the tracer-count statistics follow the reference's rule: computed when
+    // comp = 1 or tracer = 1 (basics.f90:263-267), which the caller states by
+    // passing nempty (required with compositional types, NULL otherwise)
+    const bool counts = (nempty != nullptr);
+    cudaError_t e = na_launch(k_na_rows, dim3((unsigned)((nz + 1 + 63) / 64)), dim3(64), st, R, c, T, u, w, conduct,
+                              vis, Cnew, S);
+    if (e == cudaSuccess) e = na_launch(k_na_final, dim3(1), dim3(32), st, R, c, kent, T, u, w, conduct, S);
+    if (e == cudaSuccess && counts) e = na_launch(k_na_nempty_init, dim3(1), dim3(1), st, S);
+    if (e == cudaSuccess && counts)
+        e = na_launch(k_na_nempty, dim3((unsigned)((nx + 1 + 127) / 128), (unsigned)(nz + 1)), dim3(128), st, R,
+                      nempty, S);
+    if (e != cudaSuccess) return TC_ERR_CUDA;
+    tc_note_launch(counts ? 4 : 2);
     double integ[32];
     double smax = 0.0;
     int ints[3] = {0, 0, 0};
@@ -222,12 +272,12 @@ extern "C" tc_status tc_stats_noalloc(const double* T, const double* u, const do
         return TC_ERR_CUDA;
     if (cudaMemcpyAsync(ints, &S->nempty_min, sizeof(ints), cudaMemcpyDeviceToHost, st) != cudaSuccess)
         return TC_ERR_CUDA;
-    if (cudaStreamSynchronize(st) != cudaSuccess || cudaGetLastError() != cudaSuccess) return TC_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return TC_ERR_CUDA;
     std::memset(row, 0, sizeof(*row));
     // final divisions and roots exactly as stats (basics.f90:236-324)
     for (int t = 0; t < ntype; t++) row->Cavg[t] = integ[t] / aspect;
     for (int t = 0; t < ntype; t++) row->ent[t] = (mass && mass[t] != 0.0) ? integ[4 + t] / aspect / mass[t] : 0.0;
-    if (ntype > 0) {
+    if (counts) {
         row->tracer_min = ints[0];
         row->tracer_max = ints[1];
         row->empty_cells = ints[2];
