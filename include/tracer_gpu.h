@@ -16,9 +16,9 @@
  * This header replaces those four calls with handle-based entry points.  The
  * module state becomes an opaque handle (tc_handle) whose fields live in HBM;
  * host arrays cross the boundary only in tc_upload_state/tc_download_state.
- * A Fortran host binds these functions through ISO_C_BINDING (the binding
- * module is shown in INTEGRATION.md) and maps a non-zero status to `stop`,
- * which is what the reference does at each of its error sites.
+ * A Fortran host binds these functions through ISO_C_BINDING (one interface
+ * block per function in a small binding module) and maps a non-zero status
+ * to `stop`, which is what the reference does at each of its error sites.
  *
  * Array conventions (identical to the reference's allocations, basics.f90:37-110):
  *   - FP64, Fortran column-major (i, the horizontal index, fastest);
@@ -161,6 +161,18 @@ typedef struct tc_params {
      * equalize_threads OpenMP threads (static schedule); 0 means 1. */
     int32_t equalize;
     int32_t equalize_threads;
+    /* No reference counterpart.  1 = evaluate the bottom of each W-cycle --
+     * the smoothing of level grids-1 and the coarsest direct solves between
+     * a restriction into level grids-1 and the prolongation out of it -- as
+     * one matrix-vector product with that sub-cycle's exact linear map,
+     * built once per multigrid call (one column per interior unknown of
+     * level grids-1).  Same iterates in exact arithmetic; only rounding
+     * differs.  Needs mg_zero_coarse = 1 (otherwise the sub-cycle also
+     * depends on the previous corrections), non_Newtonian = 0, grids >= 3,
+     * at most 1024 interior unknowns on level grids-1 and a coarsest grid
+     * solved by its explicit inverse; where these do not hold the cycle runs
+     * as with 0.  0 = sweep by sweep (default). */
+    int32_t mg_coarse_matrix;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat
@@ -395,6 +407,11 @@ tc_status tc_time_sweep(tc_handle* h, int32_t level, int32_t nsweeps, double* ms
  * and writes the mean milliseconds per visit.  The level's correction arrays
  * are left changed; the next tc_multigrid starts from SF as always. */
 tc_status tc_time_visit(tc_handle* h, int32_t level, int32_t reps, double* ms_per_visit);
+/* With mg_coarse_matrix in effect: times `reps` back-to-back products with
+ * the bottom-of-cycle matrix of the pattern with k coarsest solves (one
+ * kernel each) and writes the mean milliseconds per product.
+ * TC_ERR_UNSUPPORTED if the handle has no such matrix. */
+tc_status tc_time_subcycle(tc_handle* h, int32_t k, int32_t reps, double* ms_per_apply);
 int64_t tc_kernel_launches(void);
 
 /* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */
@@ -447,7 +464,10 @@ void tc_abi_sizes(int32_t sizes[3]);
  * same row as tc_stats (basics.f90:236-324) from device arrays the caller
  * owns, in the reference's layouts: T, conduct, vis (vis_grid of level 1)
  * and nempty on (-2:nx+2, -2:nz+2); u, w on (-1:nx+1, -1:nz+1); Cnew on
- * (1:ntype, -2:nx+2, -2:nz+2).  Uniform grid, order 2.  kent and mass
+ * (1:ntype, -2:nx+2, -2:nz+2).  Uniform grid, order 2.  Pass nempty when the
+ * run has compositional or temperature tracers (comp = 1 or tracer = 1, the
+ * rule of basics.f90:263-267: empty_cells, tracer_min and tracer_max are then
+ * filled) and NULL otherwise; it is required when ntype > 0.  kent and mass
  * (host array, may be NULL: ent = 0) are the entrainment inputs of stats;
  * time, tstep and the smoother counters of the row are left 0.  Work is
  * issued on `stream` (a cudaStream_t, NULL = legacy default) and the call
@@ -456,8 +476,11 @@ void tc_abi_sizes(int32_t sizes[3]);
  * 229,712 bytes that every GPU loading this library holds until exit, which
  * limits nz to TC_NOALLOC_MAX_NZ (larger nz returns TC_ERR_TOO_LARGE).  The
  * first call on a device looks up that array's device address (with the
- * device current) and should come before any stream capture on it.  All
- * calls share the array: calls whose work overlaps on the GPU race. */
+ * device current) and should come before any stream capture on it; the
+ * address is looked up again when the device's context changed (after
+ * cudaDeviceReset).  All calls share the array: calls whose work overlaps on
+ * the GPU race.  Launch failures are read from the launches' return codes;
+ * the runtime's last-error state is left as the caller left it. */
 #define TC_NOALLOC_MAX_NZ 4096
 tc_status tc_stats_noalloc(const double* T, const double* u, const double* w, const double* conduct,
                            const double* vis, const double* Cnew, const int32_t* nempty, int32_t nx, int32_t nz,

@@ -1,0 +1,263 @@
+// k_subcycle.cu -- the bottom of the W-cycle as a precomputed matrix.
+//
+// In the reference's W-cycles (multigrid_cycle.f90:9-92) every descent into
+// level S = grids-1 runs, until the cycle returns to level S-1:
+//
+//     k times: smooth S (Nmulti sweeps, Chebyshev going down), residual,
+//              restrict into the coarsest level G, direct solve on G,
+//              prolong the coarse correction and add it to S's correction;
+//     then:    smooth S (Nmulti sweeps, Richardson going up)
+//
+// with k = 1 or 2 (grids = 6: "5 6 5" and "5 6 5 6 5").  When a level's
+// correction restarts from zero at every new restricted residual
+// (mg_zero_coarse = 1) and the operators are fixed for the solve (Newtonian
+// rheology), this is a fixed linear map e_S = M_k r_S of the restricted
+// residual r_S: the sweeps, the residual, the transfers and the direct solve
+// are all linear.  M_k (n_S x n_S, n_S the interior unknowns of S) is built
+// in FP64 once per multigrid call by running the sub-cycle on the n_S unit
+// vectors, one CTA per column, with the same per-point arithmetic as the
+// FP64 smoother kernels (k_sweep, k_residual, restrict9, k_coarse_apply,
+// k_prolong) in shared memory; each descent then costs one matrix-vector
+// product instead of (2k+1) x Nmulti latency-bound sweeps and k coarse
+// solves.  In exact arithmetic the cycle is unchanged; only the
+// summation order of the bottom correction differs.  This is the same step
+// the coarsest level takes already (an explicit inverse of the banded
+// matrix instead of DGBTRS per visit, iterative_solver.f90:138-142).
+#include "tc_device.cuh"
+
+namespace {
+
+constexpr int kThreads = 512;
+constexpr int kPPT = 2;  // interior points of level S per thread (n_S <= 1024)
+
+template <typename T>
+struct SubArgs {
+    Lay LS, LG;
+    const T* coef;  // level S folded operator (TC_NCOEF planes), pseudo-time step, Chebyshev denominators
+    const T* dts;
+    const T* cA;
+    const T* cB;
+    const T* tab;  // [4][nsweeps]: c and temp of the sweeps of a downward visit, then of an upward one
+    int nsweeps, per_point_down;
+    const double* Ainv;  // coarsest level: explicit inverse, row scaling, interior unknown lists
+    const double* rowb;
+    const int* cq;
+    const int* cx;
+    int n, m;
+    int Vbc, kmax, nS;
+    T* M[4];  // outputs for k = 1..4 (null: not needed)
+};
+
+// shared-memory versions of the stencil helpers (same terms in the same order)
+template <typename T>
+__device__ __forceinline__ T sm_restrict9(const T* in, const Lay& F, int ii, int kk) {
+    T corners = (in[IX(F, ii - 1, kk - 1)] + in[IX(F, ii - 1, kk + 1)] + in[IX(F, ii + 1, kk + 1)] +
+                 in[IX(F, ii - 1, kk + 1)]) / T(16);
+    T sides = (in[IX(F, ii - 1, kk)] + in[IX(F, ii, kk - 1)] + in[IX(F, ii + 1, kk)] + in[IX(F, ii, kk + 1)]) / T(8);
+    T centre = in[IX(F, ii, kk)] / T(4);
+    return corners + sides + centre;
+}
+
+template <typename T>
+__device__ __forceinline__ T sm_prolong(const Lay& C, const T* ec, int i, int k) {
+    const bool ie = (i % 2) == 0, ke = (k % 2) == 0;
+    if (ie && ke) return ec[IX(C, i / 2, k / 2)];
+    if (ie) return (ec[IX(C, i / 2, (k - 1) / 2)] + ec[IX(C, i / 2, (k + 1) / 2)]) / T(2);
+    if (ke) return (ec[IX(C, (i - 1) / 2, k / 2)] + ec[IX(C, (i + 1) / 2, k / 2)]) / T(2);
+    return (ec[IX(C, (i - 1) / 2, (k - 1) / 2)] + ec[IX(C, (i + 1) / 2, (k - 1) / 2)] +
+            ec[IX(C, (i + 1) / 2, (k + 1) / 2)] + ec[IX(C, (i - 1) / 2, (k + 1) / 2)]) / T(4);
+}
+
+// rhs - L S at x, the 13 taps in folded_residual's order
+template <typename T>
+__device__ __forceinline__ T sm_apply(const Lay& L, const T* S, size_t x, const T* c, T rhs) {
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    T acc = rhs;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) acc = fma(-c[d], S[(ptrdiff_t)x + off[d]], acc);
+    return acc;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* P0 = reinterpret_cast<T*>(smem_raw);
+    T* P1 = P0 + A.LS.plane;
+    T* P2 = P1 + A.LS.plane;
+    T* R = P2 + A.LS.plane;
+    T* RG = R + A.LS.plane;
+    T* EG = RG + A.LG.plane;
+    const int tid = threadIdx.x;
+    const int nS = A.nS;
+    const int a1 = A.LS.a - 1;
+    const int j = blockIdx.x;  // column: interior point j of level S (i fastest)
+    const size_t total = 4 * A.LS.plane + 2 * A.LG.plane;
+    for (size_t t = tid; t < total; t += blockDim.x) P0[t] = T(0);
+    // this thread's points of level S, their operator, dt and Chebyshev denominators in registers
+    int pi[kPPT], pk[kPPT];
+    size_t px[kPPT];
+    bool pa[kPPT];
+    T cf[kPPT][TC_NCOEF], dt[kPPT], ca[kPPT], cb[kPPT];
+#pragma unroll
+    for (int q = 0; q < kPPT; q++) {
+        const int p = tid + q * kThreads;
+        pa[q] = p < nS;
+        pi[q] = pa[q] ? 1 + p % a1 : 1;
+        pk[q] = pa[q] ? 1 + p / a1 : 1;
+        px[q] = IX(A.LS, pi[q], pk[q]);
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) cf[q][d] = pa[q] ? __ldg(A.coef + px[q] + d * A.LS.plane) : T(0);
+        dt[q] = pa[q] ? __ldg(A.dts + px[q]) : T(0);
+        ca[q] = (pa[q] && A.per_point_down) ? __ldg(A.cA + px[q]) : T(1);
+        cb[q] = (pa[q] && A.per_point_down) ? __ldg(A.cB + px[q]) : T(0);
+    }
+    __syncthreads();
+    if (tid == 0) R[IX(A.LS, 1 + j % a1, 1 + j / a1)] = T(1);
+    __syncthreads();
+    // one visit of Nmulti sweeps from Sa (ping-pong with Sb); returns the plane holding the result
+    auto visit = [&](T* Sa, T* Sb, int up) -> T* {
+        const T* cv = A.tab + (up ? 2 : 0) * A.nsweeps;
+        const T* tv = cv + A.nsweeps;
+        const bool pp = !up && A.per_point_down;
+        for (int n = 0; n < A.nsweeps; n++) {
+            const T cu = __ldg(cv + n), temp = __ldg(tv + n);
+#pragma unroll
+            for (int q = 0; q < kPPT; q++) {
+                if (!pa[q]) continue;
+                const T res = sm_apply(A.LS, Sa, px[q], cf[q], R[px[q]]);
+                const T c = pp ? T(2) / (ca[q] + cb[q] * temp) : cu;
+                store_stream<T>(A.LS, Sb, pi[q], pk[q], fma(c * dt[q], res, Sa[px[q]]), A.Vbc);
+            }
+            __syncthreads();
+            T* t = Sa;
+            Sa = Sb;
+            Sb = t;
+        }
+        return Sa;
+    };
+    const int lane = tid & 31, warp = tid >> 5, nwarps = kThreads / 32;
+    const int NG = A.LG.b + 1;
+    for (int blk = 1; blk <= A.kmax; blk++) {
+        // smooth S going down; the result back in P0
+        T* e = visit(P0, P1, 0);
+        if (e != P0) {
+            for (size_t t = tid; t < A.LS.plane; t += blockDim.x) P0[t] = e[t];
+            __syncthreads();
+        }
+        // residual into P1, restricted into the coarsest RHS
+#pragma unroll
+        for (int q = 0; q < kPPT; q++)
+            if (pa[q]) P1[px[q]] = sm_apply(A.LS, P0, px[q], cf[q], R[px[q]]);
+        __syncthreads();
+        for (int c = tid; c < (A.LG.a - 1) * (A.LG.b - 1); c += blockDim.x) {
+            const int ic = 1 + c % (A.LG.a - 1), kc = 1 + c / (A.LG.a - 1);
+            RG[IX(A.LG, ic, kc)] = sm_restrict9(P1, A.LS, 2 * ic, 2 * kc);
+        }
+        __syncthreads();
+        // direct solve x = A^-1 (RowB .* rhs): one warp per unknown, lane-strided sum and shuffle tree
+        for (int w = warp; w < A.m; w += nwarps) {
+            const int pw = __ldg(A.cq + w);
+            const double* row = A.Ainv + (size_t)pw * A.n;
+            double acc = 0.0;
+            for (int e2 = lane; e2 < A.m; e2 += 32) {
+                const int q = __ldg(A.cq + e2);
+                acc = fma(__ldg(row + q), (double)RG[__ldg(A.cx + e2)] * __ldg(A.rowb + q), acc);
+            }
+            for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+            if (lane == 0) store_stream<T>(A.LG, EG, pw / NG, pw % NG, (T)acc, A.Vbc);
+        }
+        __syncthreads();
+        // prolong the coarse correction and add it to S's
+#pragma unroll
+        for (int q = 0; q < kPPT; q++)
+            if (pa[q]) store_stream<T>(A.LS, P0, pi[q], pk[q], P0[px[q]] + sm_prolong<T>(A.LG, EG, pi[q], pk[q]), A.Vbc);
+        __syncthreads();
+        T* out = A.M[blk - 1];
+        if (out != nullptr) {
+            // this pattern ends here: smooth S going up from a copy, column j of M_blk
+            for (size_t t = tid; t < A.LS.plane; t += blockDim.x) P1[t] = P0[t];
+            __syncthreads();
+            T* f = visit(P1, P2, 1);
+            for (int p = tid; p < nS; p += blockDim.x)
+                out[(size_t)p * nS + j] = f[IX(A.LS, 1 + p % a1, 1 + p / a1)];
+            __syncthreads();
+        }
+    }
+}
+
+// e_S = M r_S: one warp per interior unknown p of level S (lane-strided sum
+// in FP64, shuffle tree), written with the stream BCs' ghost copies.  The
+// matrix is FP64 in both solvers: the product cancels strongly (the sum of
+// the terms' magnitudes is far above the result), so FP32 entries would
+// perturb the correction by far more than the FP32 sweeps they replace
+// (measured: 4e-4 of the level-1 correction after one W-cycle, against
+// 5e-13 with FP64 entries).  The mixed solve's FP32 RHS and correction are
+// converted at the load and the store.
+template <typename TV>
+__global__ void __launch_bounds__(256) k_subcycle_apply(Lay L, const double* __restrict__ M, const TV* rhs, TV* err,
+                                                        int nS, int Vbc) {
+    pdl_entry();
+    const int lane = threadIdx.x & 31;
+    const int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (p >= nS) return;
+    const int a1 = L.a - 1;
+    const double* row = M + (size_t)p * nS;
+    double acc = 0.0;
+    for (int jj = lane; jj < nS; jj += 32)
+        acc = fma(__ldg(row + jj), (double)ld_state(rhs + IX(L, 1 + jj % a1, 1 + jj / a1)), acc);
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if (lane == 0) store_stream<TV>(L, err, 1 + p % a1, 1 + p / a1, (TV)acc, Vbc);
+    pdl_done();
+}
+
+template <typename T>
+size_t build_smem(const Lay& LS, const Lay& LG) {
+    return sizeof(T) * (4 * LS.plane + 2 * LG.plane);
+}
+
+template <typename T>
+int launch_build(cudaStream_t s, const SubArgs<T>& A) {
+    const size_t smem = build_smem<T>(A.LS, A.LG);
+    if (A.nS > kThreads * kPPT || smem > 200 * 1024) return -1;
+    if (cudaFuncSetAttribute(k_subcycle_build<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return -1;
+    k_subcycle_build<T><<<A.nS, kThreads, smem, s>>>(A);
+    tc_note_launch();
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace
+
+int subcycle_fits(const Lay& LS, const Lay& LG) {
+    const int nS = (LS.a - 1) * (LS.b - 1);
+    return (nS <= kThreads * kPPT && build_smem<double>(LS, LG) <= 200 * 1024) ? 1 : 0;
+}
+
+// The matrices are built in FP64 from the level's FP64 operator in both
+// solvers (in the mixed solve the FP32 smoother's coefficients are roundings
+// of the same FP64 ones).
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, int nsweeps,
+                          int per_point_down, const double* Ainv, const double* rowb, const int* cq, const int* cx,
+                          int n, int m, int Vbc, int kmax, double* const* M) {
+    if (kmax < 1 || kmax > 4) return -1;
+    SubArgs<double> A{};
+    A.LS = S.L; A.LG = G.L;
+    A.coef = S.coef; A.dts = S.dt_stream; A.cA = S.cA; A.cB = S.cB;
+    A.tab = tab; A.nsweeps = nsweeps; A.per_point_down = per_point_down;
+    A.Ainv = Ainv; A.rowb = rowb; A.cq = cq; A.cx = cx; A.n = n; A.m = m;
+    A.Vbc = Vbc; A.kmax = kmax; A.nS = (S.L.a - 1) * (S.L.b - 1);
+    for (int k = 0; k < 4; k++) A.M[k] = M[k];
+    return launch_build(s, A);
+}
+
+void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc) {
+    const int nS = (S.L.a - 1) * (S.L.b - 1);
+    const unsigned nb = (unsigned)((nS * 32 + 255) / 256);
+    if (fp32)
+        launch_pdl(k_subcycle_apply<float>, nb, 256, 0, s, S.L, M, (const float*)S.rhs32, (float*)err, nS, Vbc);
+    else
+        launch_pdl(k_subcycle_apply<double>, nb, 256, 0, s, S.L, M, (const double*)S.rhs, (double*)err, nS, Vbc);
+    tc_note_launch();
+}

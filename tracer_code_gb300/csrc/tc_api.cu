@@ -19,6 +19,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <algorithm>
 
 #include <atomic>
 #include <thread>
@@ -151,6 +152,16 @@ struct Handle {
     // training-sample recorder (caller-owned device buffers)
     float *rec_raw = nullptr, *rec_sf = nullptr;
     int rec_cap = 0, rec_count = 0;
+    // bottom of the W-cycle as precomputed matrices (mg_coarse_matrix = 1):
+    // sub_k[pp] = coarse solves of the pattern that starts at cycle step pp
+    // (a step entering level grids-1 from above; 0 elsewhere), sub_end[pp]
+    // its last step; subM[k-1] = M_k (FP32 in the mixed solve); sub_tab =
+    // the c and temp tables of a downward and an upward visit
+    bool sub_on = false, sub_valid = false;
+    int sub_kmax = 0;
+    std::vector<int> sub_k, sub_end;
+    double* subM[4] = {nullptr, nullptr, nullptr, nullptr};
+    double* sub_tab = nullptr;
 };
 
 #define CK(call)                                                      \
@@ -561,8 +572,16 @@ void enqueue_cycle_rest(Handle* h) {
         if (h->multi[pp - 1] < h->multi[pp] && level > 1 && !restricted)
             launch_restrict_res(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res, h->lev[level].rhs,
                                 zero ? cur_err(h, level) : nullptr);
+        // the sub-cycle below level grids-1 entered here: one product with its
+        // matrix, then continue with the step that leaves level grids-1
+        const int sub = h->sub_on ? h->sub_k[pp] : 0;
+        if (sub) {
+            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 0, cur_err(h, level), h->p.Vbc);
+            pp = h->sub_end[pp];
+        }
         const StepFusion f = step_fusion(h, pp);
-        if (level < G) {
+        if (sub) {
+        } else if (level < G) {
             iterate_stream(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
         } else {
             if (h->coarse_banded)
@@ -671,8 +690,14 @@ void enqueue_rest_mixed(Handle* h, int) {
         else if (down && level > 2 && !restricted)
             launch_restrict32(h->st, h->lev[level], h->lev[level - 1], h->lev[level - 1].res32, h->lev[level].rhs32,
                               zero);
+        const int sub = h->sub_on ? h->sub_k[pp] : 0;
+        if (sub) {
+            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 1, cur_e32(h, level), h->p.Vbc);
+            pp = h->sub_end[pp];
+        }
         const StepFusion f = step_fusion(h, pp);
-        if (level < G) iterate_stream32(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
+        if (sub) {
+        } else if (level < G) iterate_stream32(h, level, dir, pending_pro ? 1 : 0, f.rst, f.rst_zero);
         else if (h->coarse_banded)
             launch_coarse_solve32(h->st, h->lev[G], h->band, h->ipiv, h->rowb, h->ngrid_coarse, h->kl, h->ku,
                                   cur_e32(h, G), h->p.Vbc);
@@ -774,9 +799,32 @@ tc_status multigrid(Handle* h) {
         compute_velocities(h);
         launch_strain(h->st, h->L1, h->P, h->u, h->w, h->strain);
     };
+    // the bottom of the W-cycle as matrices M_k (k_subcycle.cu): the level
+    // grids-1 sweep tables of a downward and an upward visit, then one CTA
+    // per column runs the sub-cycle on a unit vector
+    auto subcycle_setup = [&]() -> tc_status {
+        const int S = G - 1, Nm = h->p.Nmulti;
+        const bool cheb_pp = (S == h->ratio_level);
+        std::vector<double> tv((size_t)4 * Nm);
+        for (int dir = 0; dir < 2; dir++)
+            for (int n = 1; n <= Nm; n++)
+                sweep_factors(Nm, n, dir, cheb_pp, &tv[(size_t)(2 * dir) * Nm + n - 1],
+                              &tv[(size_t)(2 * dir + 1) * Nm + n - 1]);
+        CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
+        if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_tab, Nm, cheb_pp ? 1 : 0,
+                                  h->ainv, h->rowb, h->coarse_q, h->coarse_x, h->ngrid_coarse, h->coarse_m,
+                                  h->p.Vbc, h->sub_kmax, h->subM) != 0) {
+            h->err = "k_subcycle_build: launch failed";
+            return TC_ERR_CUDA;
+        }
+        h->sub_valid = true;
+        return TC_OK;
+    };
     if (!nonN) {
         TRY(level_setup());
-        if (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid) coarse_setup();
+        const bool rebuild = (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid);
+        if (rebuild) coarse_setup();
+        if (h->sub_on && (rebuild || !h->sub_valid)) TRY(subcycle_setup());
     }
     CK(cudaMemsetAsync(&h->ds->visit_timeout, 0, sizeof(int), h->st));
     const size_t img = (size_t)h->nx * h->nz;
@@ -1352,6 +1400,39 @@ tc_status create(Handle* h, const tc_params* in) {
             for (int i = 0; i <= lv.L.a; i++)
                 for (int k = 1; k <= lv.L.b - 1; k++) hv[IX(lv.L, i, k)] = dtv;
             CK(cudaMemcpy(lv.dt_vis, hv.data(), lp * sizeof(double), cudaMemcpyHostToDevice));
+        }
+    }
+    // the bottom of the W-cycle as precomputed matrices
+    if (p.mg_coarse_matrix == 1 && p.mg_zero_coarse == 1 && p.non_Newtonian == 0 && G >= 3 && !h->coarse_banded &&
+        subcycle_fits(h->lev[G - 1].L, h->lev[G].L)) {
+        const int S = G - 1;
+        h->sub_k.assign(h->nsteps + 2, 0);
+        h->sub_end.assign(h->nsteps + 2, 0);
+        bool need[5] = {false, false, false, false, false};
+        bool ok = true;
+        for (int pp = 2; pp <= h->nsteps && ok; pp++) {
+            if (h->multi[pp] != S || h->multi[pp - 1] != S - 1) continue;
+            int k = 0, q = pp;
+            while (q + 1 <= h->nsteps + 1 && h->multi[q + 1] >= S) {
+                q++;
+                if (h->multi[q] == G) k++;
+            }
+            // the pattern must be S (G S)^k and end before the cycle does
+            for (int t = pp; t <= q; t++)
+                if (h->multi[t] != ((t - pp) % 2 == 0 ? S : G)) ok = false;
+            if (q > h->nsteps || h->multi[q] != S || k < 1 || k > 4) ok = false;
+            if (!ok) break;
+            h->sub_k[pp] = k;
+            h->sub_end[pp] = q;
+            need[k] = true;
+            h->sub_kmax = std::max(h->sub_kmax, k);
+        }
+        if (ok && h->sub_kmax > 0) {
+            const size_t nS = (size_t)(h->lev[S].L.a - 1) * (h->lev[S].L.b - 1);
+            for (int k = 1; k <= 4; k++)
+                if (need[k]) TRY(dalloc_t(h, &h->subM[k - 1], nS * nS));
+            TRY(dalloc_t(h, &h->sub_tab, 4 * (size_t)p.Nmulti));
+            h->sub_on = true;
         }
     }
     // stability_RK4_smoother: dts_array
@@ -1966,6 +2047,31 @@ tc_status tc_time_visit(tc_handle* H, int32_t level, int32_t reps, double* ms_pe
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_visit = (double)ms / reps;
+    return TC_OK;
+}
+
+tc_status tc_time_subcycle(tc_handle* H, int32_t k, int32_t reps, double* ms_per_apply) {
+    if (!H || !ms_per_apply || reps < 1 || k < 1 || k > 4) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (!h->uploaded) return TC_ERR_STATE;
+    if (!h->sub_on || h->subM[k - 1] == nullptr) return TC_ERR_UNSUPPORTED;
+    const int S = h->grids - 1;
+    const bool mixed = (h->p.solver_precision == 1);
+    void* err = mixed ? (void*)cur_e32(h, S) : (void*)cur_err(h, S);
+    auto apply = [&]() { launch_subcycle_apply(h->st, h->lev[S], h->subM[k - 1], mixed ? 1 : 0, err, h->p.Vbc); };
+    apply();
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, h->st));
+    for (int n = 0; n < reps; n++) apply();
+    CK(cudaEventRecord(e1, h->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms_per_apply = (double)ms / reps;
     return TC_OK;
 }
 

@@ -168,6 +168,18 @@ int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const doub
                            int nsweeps, int per_point, int Vbc, int* timeout_flag,
                            const VisitXfer<float>* x = nullptr);
 
+// (k_subcycle.cu) the bottom of the W-cycle (smoothing of level S = grids-1
+// and the coarsest solves between a restriction into S and the prolongation
+// out of it) as precomputed FP64 n_S x n_S matrices M_k, k = coarse solves
+// of the pattern; M[k-1] null where no pattern has k coarse solves.  The
+// apply reads the level's RHS and writes its correction in the solver's
+// precision (fp32: rhs32 / e32).
+int subcycle_fits(const Lay& LS, const Lay& LG);
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, int nsweeps,
+                          int per_point_down, const double* Ainv, const double* rowb, const int* cq, const int* cx,
+                          int n, int m, int Vbc, int kmax, double* const* M);
+void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc);
+
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
