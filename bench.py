@@ -15,10 +15,13 @@ Prints one JSON line (rank 0) with the contract keys plus roofline,
 cpu_baseline, e2e, clocks and gpu_launches.
 
 reference: the CPU restatement of the reference (oracle/, OpenMP on all host
-cores) on the same workload; each step is a bounded sample (two multigrid
-calls capped at 2 and 24 W-cycles, one RK step without re-solves, one
-tracer-ratio pass) from which the full timestep time is assembled with the
-workload's cycle count.
+cores) on the same workload.  Its timed steps are whole timesteps from the
+seeded initial state (every multigrid solve to the 1e-8 test, cycles
+counted, four RK stages, four tracer-ratio passes), measured with a wall
+clock.  A whole CPU timestep takes about a minute, so the arm times as many
+of the K requested steps as fit REF_BUDGET_S (at least one) and reports the
+number it timed in "steps" (the request in "steps_requested"); its W warm-up
+steps are bounded (one W-cycle each on a separate copy of the state).
 """
 from __future__ import annotations
 
@@ -35,11 +38,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "timesteps/s 1024x256 grid, 6.5M tracers: learned+mixed vs plain MG @ 1e-8 resid"
 UNIT = "timesteps/s"
-# Average W-cycles per timestep (4 solves) of this workload, measured on the
-# GPU arm over its first steps (same algorithm, same tolerance); used only to
-# assemble the CPU reference arm's timestep from its bounded sample when it
-# runs without the GPU arm in the same process.
-CYCLES_PER_STEP_DEFAULT = 228.0
+# wall-clock budget of the reference arm's timed whole CPU timesteps (s): it
+# stops after the step that crosses it (so at least one step is timed)
+REF_BUDGET_S = 150.0
 # W-cycle caps of the two CPU multigrid calls of one bounded sample (their
 # difference gives the time per cycle, about 10 s of CPU work per sample)
 CPU_SAMPLE_CYCLES = (2, 24)
@@ -55,13 +56,15 @@ def workload_params(solver: str = "plain"):
     from tracer_code_gb300 import config_1024x256
     p = config_1024x256()
     p.mg_zero_coarse = 1
+    p.mg_coarse_matrix = 1
     p.solver_precision = 1 if solver == "mixed" else 0
     return p
 
 
 SOLVER_DESC = {
     "plain": "plain FP64 multigrid (W-cycle, Chebyshev-Richardson smoother, banded LU coarse solve), "
-             "coarse corrections restart from zero (mg_zero_coarse=1)",
+             "coarse corrections restart from zero (mg_zero_coarse=1); the bottom of each W-cycle (level-5 "
+             "visits and coarsest solves) applied as its precomputed exact linear map (mg_coarse_matrix=1)",
     "mixed": "mixed-precision multigrid: the same W-cycle with FP32 smoother, residuals and transfers on levels "
              "1..grids-1 inside FP64 defect correction (FP64 level-1 residual, streamfunction and updates, FP64 "
              "coarse solve), same 1e-8 test",
@@ -192,26 +195,51 @@ def cpu_sample(p, threads: int, cycles_per_step: float, seed: int = 1) -> dict:
 
 
 def run_reference(args, rank: int, world: int):
+    """The reference arm: whole CPU timesteps of the restatement on all host
+    cores, timed with a wall clock (rank 0 only; other ranks do no work)."""
     if rank != 0:
         return
+    from oracle.pyoracle import Oracle
+    from tracer_code_gb300 import TracerError, state
     p = workload_params()
     threads = os.cpu_count() or 1
-    samples = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_sample(p, threads, CYCLES_PER_STEP_DEFAULT)
-        if i >= args.warmup:
-            samples.append(r)
-    step_s = statistics.mean(r["step_s"] for r in samples)
-    value = 1.0 / step_s
+    st = state.initial_state(p, seed=1)
+    # bounded warm-up steps (thread pool, first touch): one W-cycle each on a copy
+    q = p.copy()
+    q.max_cycles = 1
+    ow = Oracle(q, threads=threads)
+    ow.upload(st)
+    for _ in range(args.warmup):
+        try:
+            ow.multigrid()
+        except TracerError as e:
+            if e.status != 3:
+                raise
+    ow.close()
+    o = Oracle(p, threads=threads)
+    o.upload(st)
+    times, cycles = [], []
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _, qc, _ = o.step()
+        times.append(time.perf_counter() - t0)
+        cycles.append(int(qc))
+        if time.perf_counter() - t_all >= REF_BUDGET_S:
+            break
+    o.close()
+    total = sum(times)
+    value = len(times) / total
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_desc(p, "plain"),
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
+        "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(workload_desc(p, "plain"), mg_zero_coarse=p.mg_zero_coarse),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"per step: CPU restatement multigrid capped at {CPU_SAMPLE_CYCLES[0]} and {CPU_SAMPLE_CYCLES[1]} W-cycles, one RK4 step "
-                                   f"without re-solves, one tracer-ratio pass; timestep assembled as "
-                                   f"4*fixed + {CYCLES_PER_STEP_DEFAULT:g} cycles + RK + 3 ratio passes",
-                         "parts": samples[-1]},
+                         "sample": f"{len(times)} whole timesteps of the CPU restatement from the seeded initial "
+                                   f"state (every solve to the 1e-8 test), wall clock; W-cycles per step {cycles}; "
+                                   f"steps timed = those of the {args.steps} requested that fit {REF_BUDGET_S:g} s",
+                         "step_s": times, "cycles_per_step": cycles},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -235,6 +263,141 @@ def timed_steps(sim, stream, steps: int, warmup: int, barrier):
     torch.cuda.synchronize()
     barrier()
     return e0.elapsed_time(e1), cyc, warm, Simulation.kernel_launches() - n0
+
+
+# the reference's 6-level W-cycle (multigrid_cycle.f90:91-92), steps p = 1..42
+W_TABLE6 = [1, 2, 3, 4, 5, 6, 5, 6, 5, 4, 5, 6, 5, 4, 3, 4, 5, 6, 5, 4, 3, 2, 3, 4, 5, 6, 5, 4, 3, 4, 5, 6, 5, 4,
+            5, 6, 5, 6, 5, 4, 3, 2]
+
+
+def visits_per_cycle(grids: int) -> dict:
+    if grids != 6:
+        raise ValueError("the bench workload runs 6 levels")
+    return {l: W_TABLE6.count(l) for l in range(1, grids + 1)}
+
+
+def bottom_patterns(grids: int) -> dict:
+    """Descents into level grids-1 per W-cycle, keyed by the coarsest solves
+    each makes before the cycle leaves level grids-1 again."""
+    t = W_TABLE6 if grids == 6 else None
+    if t is None:
+        raise ValueError("the bench workload runs 6 levels")
+    S, out = grids - 1, {}
+    n = len(t)
+    for i in range(n):
+        if t[i] == S and t[i - 1] == S - 1:
+            k, j = 0, i
+            while t[(j + 1) % n] >= S:
+                j += 1
+                k += t[j % n] == grids
+            out[k] = out.get(k, 0) + 1
+    return out
+
+
+def level_points(p, level: int) -> int:
+    f = 2 ** (level - 1)
+    return (p.nx // f - 1) * (p.nz // f - 1)
+
+
+def cycle_profile(sim, p, fp32: bool) -> dict:
+    """Per-level share of one W-cycle, timed live on the library's stream:
+    each level's whole smoother visit (tc_time_visit: its kernels, replayed
+    back to back) times its visits per cycle; the level whose visits take
+    the largest share holds the dominant kernel.  Algorithmic bytes of a
+    visit = Nmulti sweeps x (88 B FP64 | 44 B FP32) x interior points."""
+    from tracer_code_gb300 import Simulation
+    visits = visits_per_cycle(p.grids)
+    bsweep = 44.0 if fp32 else 88.0
+    rows = []
+    matrix = bool(getattr(p, "mg_coarse_matrix", 0))
+    top = p.grids - 1 if matrix else p.grids
+    for lvl in range(1, top):
+        reps = 3 if lvl == 1 else 20
+        n0 = Simulation.kernel_launches()
+        ms = sim.time_visit(lvl, reps)
+        launches = (Simulation.kernel_launches() - n0) / (reps + 1)
+        pts = level_points(p, lvl)
+        rows.append({"level": lvl, "points": pts, "visits_per_cycle": visits[lvl], "ms_per_visit": ms,
+                     "launches_per_visit": launches, "ms_per_cycle": ms * visits[lvl],
+                     "alg_bytes_per_visit": p.Nmulti * bsweep * pts})
+    bottom = None
+    if matrix:
+        # level grids-1 and the coarsest solves: one product per descent
+        S = p.grids - 1
+        pat = bottom_patterns(p.grids)
+        nS = level_points(p, S)
+        ms = {k: sim.time_subcycle(k, 50) for k in pat}
+        es = 4.0 if fp32 else 8.0
+        bottom = {"level": S, "points": nS, "products_per_cycle": pat,
+                  "ms_per_product": ms, "ms_per_cycle": sum(pat[k] * ms[k] for k in pat),
+                  "alg_bytes_per_product": es * nS * nS + 2 * es * nS,
+                  "replaces": f"{visits[S]} visits of level {S} and {visits[p.grids]} coarsest solves per cycle"}
+        rows.append({"level": S, "points": nS, "visits_per_cycle": sum(pat.values()),
+                     "ms_per_visit": bottom["ms_per_cycle"] / sum(pat.values()), "launches_per_visit": 1.0,
+                     "ms_per_cycle": bottom["ms_per_cycle"],
+                     "alg_bytes_per_visit": bottom["alg_bytes_per_product"], "matrix": True})
+    tot = sum(r["ms_per_cycle"] for r in rows)
+    for r in rows:
+        r["share_of_smoothing"] = r["ms_per_cycle"] / tot
+    return {"levels": rows, "coarse_solves_per_cycle": 0 if matrix else visits[p.grids], "bottom_matrix": bottom}
+
+
+def dominant_roofline(sim, p, prof: dict, fp32: bool) -> dict:
+    """Roofline of the kernel that takes the largest share of a W-cycle: at
+    level 1 the per-sweep smoother launch (70 per visit), below it the
+    level's visit (one cluster launch per visit where it fuses)."""
+    peak, src = peaks()
+    dom = max(prof["levels"], key=lambda r: r["ms_per_cycle"])
+    lvl, pts = dom["level"], dom["points"]
+    if lvl == 1:
+        return sweep_roofline(sim, p, fp32) | {"share_of_smoothing": dom["share_of_smoothing"]}
+    per_launch_ms = dom["ms_per_visit"] / max(dom["launches_per_visit"], 1.0)
+    alg = dom["alg_bytes_per_visit"] / max(dom["launches_per_visit"], 1.0)
+    achieved = alg / (per_launch_ms * 1e-3) / 1e9
+    if dom.get("matrix"):
+        return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "kernel": f"k_subcycle_apply (level {lvl}, {pts}x{pts} matrix)",
+                "alg_bytes_per_launch": alg, "kernel_ms": per_launch_ms,
+                "share_of_smoothing": dom["share_of_smoothing"],
+                "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured" else "fallback"}
+    fused = abs(dom["launches_per_visit"] - 1.0) < 1e-9
+    kname = ("k_visit_cluster" if fused else "smoother launches") + f"<{'float' if fp32 else 'double'}>"
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": None,
+            "kernel": f"{kname} (level {lvl}, {pts} points, {p.Nmulti} sweeps per launch)" if fused else
+                      f"{kname} (level {lvl}, {pts} points)",
+            "alg_bytes_per_launch": alg, "kernel_ms": per_launch_ms,
+            "share_of_smoothing": dom["share_of_smoothing"],
+            "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured" else "fallback 6.8 TB/s",
+            "note": "latency bound: the level lives in the shared memory and registers of one thread-block "
+                    "cluster for the whole visit, so each sweep costs one compute-exchange-wait chain; "
+                    "achieved = the sweeps' algorithmic bytes over the launch time (traffic null: the level "
+                    "is read from HBM once per visit)"}
+
+
+def step_roofline(p, prof: dict, cycles_per_step: float, ms_per_step: float, fp32: bool) -> dict:
+    """Whole-timestep algorithmic bytes (model of the per-unit figures above)
+    over the measured step time: smoother sweeps, residuals (72 B/pt), the
+    FP64 level-1 bridges of the mixed solve, tracer RK stages (64 B/tracer)
+    and tracer-ratio passes (20 B/tracer + 20 B/volume)."""
+    peak, _ = peaks()
+    bsweep = 44.0 if fp32 else 88.0
+    per_cycle = 0.0
+    for r in prof["levels"]:
+        if r.get("matrix"):
+            per_cycle += r["visits_per_cycle"] * r["alg_bytes_per_visit"]
+        else:
+            per_cycle += r["visits_per_cycle"] * (p.Nmulti * bsweep + (36.0 if fp32 else 72.0)) * r["points"]
+    if fp32:
+        per_cycle += (72.0 + 24.0 + 72.0) * level_points(p, 1)  # residual_to32, update64, FP64 residual
+    ntr = (p.nx + 1) * (p.nz + 1) * p.tpc
+    vols = (p.nx + 1) * (p.nz + 1)
+    tracer = 4 * 64.0 * ntr + 4 * (20.0 * ntr + 20.0 * vols)
+    total = cycles_per_step * per_cycle + tracer
+    achieved = total / (ms_per_step * 1e-3) / 1e9
+    return {"alg_bytes_per_step": total, "multigrid_bytes_per_cycle": per_cycle, "tracer_bytes_per_step": tracer,
+            "cycles_per_step": cycles_per_step, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak}
 
 
 def sweep_roofline(sim, p, fp32: bool) -> dict:
@@ -355,7 +518,10 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     guess_used, guess_offered = learned.guess_stats(sim)
     ms_max = max_over_ranks(ms)
     value = replica_rate(args.steps, ms * 1e-3, world, max_over_ranks)
-    roof = sweep_roofline(sim, p, fp32=True)
+    prof = cycle_profile(sim, p, fp32=True)
+    roof = dominant_roofline(sim, p, prof, fp32=True)
+    roof_l1 = sweep_roofline(sim, p, fp32=True)
+    step_roof = step_roofline(p, prof, statistics.mean(solves), ms_max / args.steps, fp32=True)
     # end to end: the same steps through tc_step_host with pinned host state
     host = {}
     dl = sim.download()
@@ -366,7 +532,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         host[key][...] = a
     h2d = sum(host[k].nbytes for k in ("T", "SF", "Cnew", "rtr", "str", "Ttype"))
     d2h = sum(host[k].nbytes for k in ("T", "SF", "Cnew", "rtr", "str"))
-    k_e2e = max(1, min(args.steps, 3))
+    k_e2e = args.steps
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -389,18 +555,28 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     sim0.upload(st)
     ms0, solves0, cycles0, _ = timed_steps(sim0, stream, args.steps, args.warmup, barrier)
     plain_value = replica_rate(args.steps, ms0 * 1e-3, world, max_over_ranks)
-    roof0 = sweep_roofline(sim0, pp, fp32=False)
+    prof0 = cycle_profile(sim0, pp, fp32=False)
+    roof0 = dominant_roofline(sim0, pp, prof0, fp32=False)
+    roof0_l1 = sweep_roofline(sim0, pp, fp32=False)
+    step_roof0 = step_roofline(pp, prof0, statistics.mean(solves0), ms0 / args.steps, fp32=False)
     sim0.close()
     shipped = shipped_config_rates(stream, 3, 1, cpu=(rank == 0 and not args.no_cpu_baseline)) if rank == 0 else None
     if rank == 0:
-        cfg = dict(workload_desc(p, "learned"), cycles_per_step=solves, warmup_cycles_per_step=cycles,
+        cfg = dict(workload_desc(p, "learned"), mg_zero_coarse=p.mg_zero_coarse,
+                   mg_zero_coarse_note="coarse-level corrections restart from zero when a level receives a new "
+                                       "restricted residual (the reference keeps them; with 6 levels its W-cycle "
+                                       "stalls on this workload); both arms and the CPU reference arm use it",
+                   cycles_per_step=solves, warmup_cycles_per_step=cycles,
+                   w_cycle_profile=prof, level1_sweep_roofline=roof_l1, step_roofline=step_roof,
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
                    learned_guess={"weights": os.path.relpath(GUESS_WEIGHTS, ROOT), "solves_offered": guess_offered,
                                   "solves_started_from_guess": guess_used},
                    mixed_without_guess={"timesteps_per_s": mixed_value, "ms_per_step": msm / args.steps,
                                         "cycles_per_step": solvesm},
                    plain_fp64={"timesteps_per_s": plain_value, "ms_per_step": ms0 / args.steps,
-                               "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0},
+                               "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0,
+                               "level1_sweep_roofline": roof0_l1, "step_roofline": step_roof0,
+                               "w_cycle_profile": prof0},
                    speedup_vs_plain_fp64=value / plain_value,
                    reference_shipped_config=shipped)
         line = {
