@@ -1445,9 +1445,13 @@ struct Oracle {
     }
     int last_cycles = 0;
     int cycles_acc = 0;
+    // level-1 residual ratio after each level-1 visit of the last multigrid
+    // call (the quantity the convergence test compares with the tolerance)
+    std::vector<double> res_trace;
     // multigrid (iterative_solver.f90:79-173)
     int multigrid() {
         int st;
+        res_trace.clear();
         error[1] = SF;
         compute_RHS(1);
         compute_reference_residual(1);
@@ -1499,6 +1503,7 @@ struct Oracle {
                         st = compute_viscosity(1); if (st) return st;
                         st = compute_residual(1, error[1], pp); if (st) return st;
                     }
+                    res_trace.push_back(residual_mag[1] / res_ref[1]);
                     if (residual_mag[1] / res_ref[1] <= p.tolerance) { conv = true; break; }
                 }
                 if (multi[pp + 1] < multi[pp]) prolong(level);
@@ -2490,6 +2495,13 @@ int tco_download_state(void* h, double* T, double* C, double* SF, double* r, dou
 }
 int tco_set_clock(void* h, int32_t tstep, double time) {
     Oracle* o = (Oracle*)h; o->tstep = tstep; o->time = time; return TC_OK;
+}
+// copies up to cap entries of the last multigrid call's residual trace; returns its length
+int tco_residual_trace(void* h, double* out, int32_t cap) {
+    const Oracle* o = (const Oracle*)h;
+    const int n = (int)o->res_trace.size();
+    for (int i = 0; i < n && i < cap; i++) out[i] = o->res_trace[i];
+    return n;
 }
 int tco_multigrid(void* h, int32_t* cycles) {
     Oracle* o = (Oracle*)h;

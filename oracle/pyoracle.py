@@ -51,6 +51,8 @@ def lib():
             L.tco_equalize_row.argtypes = [vp, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]
             L.tco_set_clock.argtypes = [vp, C.c_int32, C.c_double]
             L.tco_multigrid.argtypes = [vp, C.POINTER(C.c_int32)]
+            L.tco_residual_trace.argtypes = [vp, dp, C.c_int32]
+            L.tco_residual_trace.restype = C.c_int
             L.tco_compute_velocities.argtypes = [vp]
             L.tco_stats.argtypes = [vp, C.POINTER(StatsRow)]
             L.tco_energy_time.argtypes = [vp, C.POINTER(C.c_double)]
@@ -176,6 +178,12 @@ class Oracle:
         q = C.c_int32(0)
         self._chk(self.L.tco_multigrid(self.h, C.byref(q)), "multigrid")
         return q.value
+
+    def residual_trace(self) -> np.ndarray:
+        """Level-1 residual ratio after each W-cycle of the last multigrid call."""
+        buf = np.zeros(4096)
+        n = self.L.tco_residual_trace(self.h, buf, buf.size)
+        return buf[:min(n, buf.size)].copy()
 
     def compute_velocities(self):
         self.L.tco_compute_velocities(self.h)

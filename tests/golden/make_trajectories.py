@@ -7,12 +7,15 @@ fixtures are committed, the oracle is not needed at test time):
   traj_1024x256.json   the 1024x256 case (aspect 4, Ra 1e7, B 0.8,
                        eta = exp(-ln(1e4) T) x 10 in enriched material,
                        25 tracers per cell, 6 levels, coarse corrections
-                       restarting from zero): 5 steps
+                       restarting from zero): 20 steps; its per-volume
+                       counts after the last step go to
+                       traj_1024x256_counts.npz
 
 Each file holds, per step, the stats.dat row (Nu, Vrms, Tavg, Nu_bot,
 Cavg, empty_cells, tracer_min, tracer_max), the W-cycles of the step and dt,
-with the seeded initial state's seed, and after the last step a checksum
-of the per-volume tracer counts.
+with the seeded initial state's seed, a checksum of the per-volume tracer
+counts after every step, and after the last step the counts' sum and
+checksum.
 
     python tests/golden/make_trajectories.py [128|1024]
 """
@@ -40,7 +43,12 @@ def case(name: str):
         return config_plain_128(), 100, "traj_128x128.json"
     p = config_1024x256()
     p.mg_zero_coarse = 1
-    return p, 5, "traj_1024x256.json"
+    return p, 20, "traj_1024x256.json"
+
+
+def checksum(counts: np.ndarray) -> int:
+    c = counts.astype(np.int64).ravel()
+    return int((c * (np.arange(c.size) % 9973 + 1)).sum())
 
 
 def run(name: str, seed: int = 1) -> None:
@@ -53,15 +61,17 @@ def run(name: str, seed: int = 1) -> None:
         row, q, dt = o.step()
         r = {k: row[k] for k in KEYS}
         r["Cavg"] = row["Cavg"][0]
-        r.update(cycles=int(q), dt=float(dt))
+        r.update(cycles=int(q), dt=float(dt), counts_checksum=checksum(o.counts()))
         rows.append(r)
         print(name, n, q, row["Nu"], row["vrms"], round(time.time() - t0, 1), flush=True)
     counts = o.counts()
     out = {"case": name, "nx": p.nx, "nz": p.nz, "tpc": p.tpc, "seed": seed, "steps": steps, "rows": rows,
            "counts_sum": int(counts.sum()),
-           "counts_checksum": int((counts.astype(np.int64).ravel() * (np.arange(counts.size) % 9973 + 1)).sum())}
+           "counts_checksum": checksum(counts)}
     with open(os.path.join(HERE, fname), "w") as f:
         json.dump(out, f, indent=1)
+    if name != "128":
+        np.savez_compressed(os.path.join(HERE, fname.replace(".json", "_counts.npz")), counts=counts.astype(np.int16))
     print("wrote", fname)
 
 

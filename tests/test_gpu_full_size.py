@@ -1,17 +1,25 @@
-"""The largest configuration at its full size: 2048x512 cells, 40 tracers per
-cell (42,045,480 tracers), Ra = 1e8, viscosity contrast 1e6 (T) x 30 (C).
-The reference's multigrid does not converge on this case (nor does the CPU
-oracle's), so the tracer path is checked on its own, through properties that
-do not depend on the size: from a convection-cell streamfunction and one
+"""The configurations at their full size.
+
+2048x512 cells, 40 tracers per cell (42,045,480 tracers), Ra = 1e8,
+viscosity contrast 1e6 (T) x 30 (C): the reference's multigrid does not
+converge on this case (nor does the CPU oracle's), so the tracer path is
+checked on its own: from a convection-cell streamfunction and one
 energy_time with that velocity field held (RK_update = 0), every tracer
 stays inside the box, the per-volume counts equal a host recount of the
 downloaded positions (nint of r/dr and s/ds, per type), and C is the count
 ratio in every volume that holds tracers.
+
+Both full-size configurations (1024x256 with 25 tracers per cell and its
+multigrid-solved streamfunction; 2048x512 with the convection cell) against
+the CPU oracle from the same state: one energy_time with the velocity field
+held gives the same tracer positions, per-volume counts, C and T bit for
+bit (the velocities, the Taylor interpolation, the RK updates and the cell
+indices are the reference's arithmetic on both sides).
 """
 import numpy as np
 import pytest
 
-from tracer_code_gb300 import Simulation, config_2048x512, state
+from tracer_code_gb300 import Simulation, config_1024x256, config_2048x512, state
 
 pytestmark = pytest.mark.gpu
 
@@ -52,3 +60,45 @@ def test_full_size_tracer_step_keeps_counts_and_ratio(gpu_lib):
     held = ne > 0
     want = np.where(ct == ne, 1.0, np.where(ct == 0, 0.0, ct / np.maximum(ne, 1)))
     assert np.array_equal(C[held], want[held])
+
+
+def _cell_sf(p):
+    x = np.arange(-SP, p.nx + SP + 1) * (p.aspect / p.nx)
+    z = np.arange(-SP, p.nz + SP + 1) * (1.0 / p.nz)
+    return np.ascontiguousarray(1.0e3 * np.sin(np.pi * z)[:, None] * np.sin(np.pi * x / p.aspect)[None, :])
+
+
+@pytest.mark.parametrize("size", ["1024x256", "2048x512"])
+def test_full_size_energy_time_bitexact_against_oracle(gpu_lib, size):
+    from oracle.pyoracle import Oracle
+    if size == "1024x256":
+        p = config_1024x256()
+        p.mg_zero_coarse = 1
+    else:
+        p = config_2048x512()
+    p.RK_update = 0
+    st = state.initial_state(p, seed=1)
+    if size == "2048x512":
+        st["SF"] = _cell_sf(p)
+    g = Simulation(p)
+    g.upload(st)
+    o = Oracle(p)
+    o.upload(st)
+    if size == "1024x256":
+        g.multigrid()
+        o.set("SF", g.download()["SF"])
+    g.compute_velocities()
+    o.compute_velocities()
+    dtg = g.energy_time()
+    dto = o.energy_time()
+    assert dtg == dto
+    a, b = g.download(), o.download()
+    cg, co = g.counts(), o.counts()
+    g.close()
+    o.close()
+    moved = int(np.count_nonzero(a["rtr"] != st["rtr"]))
+    print(f"{size}: {a['rtr'].size} tracers, {moved} moved in r; dt = {dtg:.6e}")
+    assert moved > 0
+    for key in ("rtr", "str", "Cnew", "T"):
+        assert np.array_equal(a[key], b[key]), key
+    assert np.array_equal(cg, co)
