@@ -68,9 +68,13 @@ SOLVER_DESC = {
     "mixed": "mixed-precision multigrid: the same W-cycle with FP32 smoother, residuals and transfers on levels "
              "1..grids-1 inside FP64 defect correction (FP64 level-1 residual, streamfunction and updates, FP64 "
              "coarse solve), same 1e-8 test",
-    "learned": "learned + mixed: the mixed-precision multigrid, each solve offered the encoder-decoder's initial "
-               "guess (BF16 tcgen05 network trained at 512x128) and started from it when its level-1 residual is "
-               "below the previous streamfunction's; same 1e-8 test",
+    "learned": "learned + mixed: the mixed-precision multigrid with the encoder-decoder (BF16 tcgen05 network "
+               "trained at 512x128) supplying its predicted change of each solve as (a) the start, scaled to the "
+               "residual-minimising multiple (learned_guess=3), and (b) one of two directions of a correction after "
+               "every level-1 visit, the other being psi's change over the last W-cycle, with coefficients "
+               "minimising the L1-weighted residual (cycle_correction=2); same 1e-8 test",
+    "corr": "mixed + cycle correction without the network: the same correction after every level-1 visit along "
+            "psi's change over the last W-cycle only (cycle_correction=1); same 1e-8 test",
 }
 GUESS_WEIGHTS = os.path.join(ROOT, "tracer_code_gb300", "weights", "guess_512x128.npy")
 
@@ -504,9 +508,11 @@ def run_ours(args, rank: int, world: int, local_rank: int):
         return float(t.item())
 
     from tracer_code_gb300 import learned
-    # headline arm: mixed-precision solver with the learned initial guess
+    # headline arm: mixed-precision solver with the learned start and the
+    # learned coarse-level correction
     p = workload_params("mixed")
-    p.learned_guess = 1
+    p.learned_guess = 3
+    p.cycle_correction = 2
     st = state.initial_state(p, seed=1 + rank)
     sim = Simulation(p, stream=stream.cuda_stream)
     net = learned.Net(1, p.nz, p.nx, stream=stream.cuda_stream)
@@ -542,7 +548,15 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     e2e_value = replica_rate(k_e2e, time.perf_counter() - t0, world, max_over_ranks)
     sim.close()
     net.close()
-    # the same mixed solver without the network
+    # ablation: the same correction without the network's direction
+    pc = workload_params("mixed")
+    pc.cycle_correction = 1
+    simc = Simulation(pc, stream=stream.cuda_stream)
+    simc.upload(st)
+    msc, solvesc, _, _ = timed_steps(simc, stream, args.steps, args.warmup, barrier)
+    corr_value = replica_rate(args.steps, msc * 1e-3, world, max_over_ranks)
+    simc.close()
+    # the same mixed solver without the network and without the correction
     pm = workload_params("mixed")
     simm = Simulation(pm, stream=stream.cuda_stream)
     simm.upload(st)
@@ -571,8 +585,13 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
                    learned_guess={"weights": os.path.relpath(GUESS_WEIGHTS, ROOT), "solves_offered": guess_offered,
                                   "solves_started_from_guess": guess_used},
+                   cycle_correction_without_network={"timesteps_per_s": corr_value, "ms_per_step": msc / args.steps,
+                                                     "cycles_per_step": solvesc, "solver": SOLVER_DESC["corr"]},
                    mixed_without_guess={"timesteps_per_s": mixed_value, "ms_per_step": msm / args.steps,
-                                        "cycles_per_step": solvesm},
+                                        "cycles_per_step": solvesm,
+                                        "solver": "the mixed-precision multigrid alone (no network, no correction)"},
+                   learned_gain={"cycles_vs_mixed_alone": sum(solves) / max(sum(solvesm), 1),
+                                 "cycles_vs_correction_without_network": sum(solves) / max(sum(solvesc), 1)},
                    plain_fp64={"timesteps_per_s": plain_value, "ms_per_step": ms0 / args.steps,
                                "cycles_per_step": solves0, "solver": SOLVER_DESC["plain"], "roofline": roof0,
                                "level1_sweep_roofline": roof0_l1, "step_roofline": step_roof0,

@@ -135,6 +135,11 @@ typedef struct tc_params {
      * below that of the previous streamfunction; after 8 rejections in a row
      * the guess is offered on every 32nd solve only, until it is taken again
      * (the plain start is used alone meanwhile); 2 = always from the guess;
+     * 3 = from the previous streamfunction plus the multiple of the
+     * network's predicted change that minimises the residual's 2-norm:
+     * alpha = <A d, r> / <A d, A d> with d = guess - SF and r = RHS - A SF,
+     * so the start's residual never exceeds the previous streamfunction's
+     * (alpha near 0 when the prediction does not help);
      * 0 = always from the previous streamfunction. */
     int32_t learned_guess;
     /* Passes of a separable (1,2,1)/4 filter applied to the network's
@@ -173,6 +178,18 @@ typedef struct tc_params {
      * solved by its explicit inverse; where these do not hold the cycle runs
      * as with 0.  0 = sweep by sweep (default). */
     int32_t mg_coarse_matrix;
+    /* No reference counterpart: a correction after every level-1 visit.
+     * 0 = none (the reference's cycle).  1 = the minimal-residual correction
+     * of the level-1 streamfunction along its change over the last W-cycle
+     * (psi now minus psi after the previous correction).  2 = the learned
+     * coarse-level correction: the minimal-residual correction on the
+     * two-dimensional space spanned by that change and the attached
+     * network's predicted change of the solve (formed once per multigrid
+     * call); it needs an attached network (without one it acts as 1).  The
+     * correction never raises the residual's 2-norm, the convergence test is
+     * the reference's and is taken after it, so the solution meets the same
+     * tolerance; cycle counts differ.  Not with non_Newtonian = 1. */
+    int32_t cycle_correction;
 } tc_params;
 
 /* One row of stats.dat (basics.f90:283-314) plus viscosity_smoother.dat

@@ -2496,6 +2496,12 @@ int tco_download_state(void* h, double* T, double* C, double* SF, double* r, dou
 int tco_set_clock(void* h, int32_t tstep, double time) {
     Oracle* o = (Oracle*)h; o->tstep = tstep; o->time = time; return TC_OK;
 }
+// W-cycle cap of later multigrid calls (tests that step a solve cycle by cycle)
+int tco_set_max_cycles(void* h, int32_t n) {
+    if (n < 1) return TC_ERR_ARG;
+    ((Oracle*)h)->p.max_cycles = n;
+    return TC_OK;
+}
 // copies up to cap entries of the last multigrid call's residual trace; returns its length
 int tco_residual_trace(void* h, double* out, int32_t cap) {
     const Oracle* o = (const Oracle*)h;

@@ -51,6 +51,7 @@ def lib():
             L.tco_equalize_row.argtypes = [vp, C.POINTER(C.c_int64), C.c_int32, C.POINTER(C.c_int32)]
             L.tco_set_clock.argtypes = [vp, C.c_int32, C.c_double]
             L.tco_multigrid.argtypes = [vp, C.POINTER(C.c_int32)]
+            L.tco_set_max_cycles.argtypes = [vp, C.c_int32]
             L.tco_residual_trace.argtypes = [vp, dp, C.c_int32]
             L.tco_residual_trace.restype = C.c_int
             L.tco_compute_velocities.argtypes = [vp]
@@ -178,6 +179,9 @@ class Oracle:
         q = C.c_int32(0)
         self._chk(self.L.tco_multigrid(self.h, C.byref(q)), "multigrid")
         return q.value
+
+    def set_max_cycles(self, n: int):
+        self._chk(self.L.tco_set_max_cycles(self.h, n), "set_max_cycles")
 
     def residual_trace(self) -> np.ndarray:
         """Level-1 residual ratio after each W-cycle of the last multigrid call."""

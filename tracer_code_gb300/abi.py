@@ -74,7 +74,7 @@ class Params(C.Structure):
         ("yield_depth", C.c_double), ("visC", _D4), ("delta_visC", _D4),
         ("mg_zero_coarse", C.c_int32), ("solver_precision", C.c_int32), ("learned_guess", C.c_int32), ("learned_smooth", C.c_int32),
         ("tracer_sort_interval", C.c_int32), ("tracer", C.c_int32), ("equalize", C.c_int32),
-        ("equalize_threads", C.c_int32), ("mg_coarse_matrix", C.c_int32),
+        ("equalize_threads", C.c_int32), ("mg_coarse_matrix", C.c_int32), ("cycle_correction", C.c_int32),
     ]
 
     def copy(self) -> "Params":

@@ -1,0 +1,202 @@
+// k_accel.cu -- residual-minimising corrections of the level-1
+// streamfunction along a few directions: the learned start and the
+// correction after every level-1 visit (the learned coarse-level correction).
+//
+// Given the current streamfunction psi (level 1, FP64), its RHS and the
+// folded operator A, and directions v_1..v_m (m <= 2), the correction
+//
+//     psi <- psi + sum_j alpha_j v_j,   G alpha = b,
+//     G_ij = sum w (A v_i)(A v_j),   b_i = sum w (A v_i) r,   r = RHS - A psi,
+//     w = 1 / |r|                                        (interior sums)
+//
+// minimises the weighted 2-norm sum w (r - sum_j alpha_j A v_j)^2, which at
+// alpha = 0 equals the L1 norm of the residual -- the norm of the
+// reference's convergence test (iterative_solver.f90:147-156) -- and is one
+// reweighted least-squares step towards its minimum over psi + span{v_j}.
+// The plain 2-norm (w = 1) and the energy-norm Galerkin step do not work
+// here: at 1024x256 with a 1e5 viscosity contrast the W-cycle lowers the L1
+// residual but not its 2-norm, and both steps drove alpha to -1 (cancelling
+// each cycle) and stalled the solve; pseudo-time-step weights stalled too.
+// The directions used:
+//
+//   DNN   the network's predicted solution change (its guess minus the
+//         streamfunction it started from), formed once per multigrid call;
+//   DK    psi's change over the last W-cycle, psi - psi_prev (psi_prev = psi
+//         after the previous correction).
+//
+// One kernel forms A v_j and the residual at every interior point and the
+// sums (deterministic block partials, fixed-order fold by the last block),
+// whose last block also solves the 2x2 (or 1x1) system into the device
+// scalars; a second kernel applies the update with the stream BCs' ghost
+// copies and, for DK, records psi_prev.  No host synchronisation, so both
+// run inside the W-cycle's CUDA graph.  Safeguards: a direction with
+// A v = 0, or a 2x2 system whose determinant is below 1e-12 of the product
+// of its diagonal (nearly parallel directions), drops to the 1x1 system of
+// the first direction (or to no correction).
+#include "tc_device.cuh"
+
+namespace {
+
+constexpr int kNV = 6;  // sums: G11, G12, G21 (= G12), G22, b1, b2
+
+// direction value at offset y: DK = psi - psi_prev, DNN = dnn
+__device__ __forceinline__ double dir_at(int kind, const double* psi, const double* prev, const double* dnn, size_t y) {
+    return kind == TC_ACCEL_DK ? ld_state(psi + y) - ld_state(prev + y) : ld_state(dnn + y);
+}
+
+// grid-stride over the interior points (a fixed number of blocks keeps the
+// final fold short: each of the six sums is folded by its own warp)
+__global__ void __launch_bounds__(256) k_accel_dots(Lay L, const double* __restrict__ coef, const double* rhs,
+                                                    const double* psi, const double* prev, const double* dnn, int k1,
+                                                    int k2, RedScratch rs, DevScalars* ds) {
+    pdl_entry();
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    const int a1i = L.a - 1, npts = (L.a - 1) * (L.b - 1);
+    const bool useq = (k1 == TC_ACCEL_DK || k2 == TC_ACCEL_DK), usen = (k1 == TC_ACCEL_DNN || k2 == TC_ACCEL_DNN);
+    double s[kNV] = {0, 0, 0, 0, 0, 0};
+    for (int pnt = blockIdx.x * blockDim.x + threadIdx.x; pnt < npts; pnt += gridDim.x * blockDim.x) {
+        const size_t x = IX(L, 1 + pnt % a1i, 1 + pnt / a1i);
+        // A psi, A v1, A v2 from one load of each tap
+        double ap = 0.0, a1 = 0.0, a2 = 0.0;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) {
+            const double c = __ldg(coef + x + d * L.plane);
+            const size_t y = (size_t)((ptrdiff_t)x + off[d]);
+            const double p = ld_state(psi + y);
+            const double q = useq ? ld_state(prev + y) : 0.0;
+            const double n = usen ? ld_state(dnn + y) : 0.0;
+            ap = fma(c, p, ap);
+            a1 = fma(c, (k1 == TC_ACCEL_DK) ? p - q : n, a1);
+            if (k2 != TC_ACCEL_NONE) a2 = fma(c, (k2 == TC_ACCEL_DK) ? p - q : n, a2);
+        }
+        const double res = ld_state(rhs + x) - ap;
+        // w = 1/|r| (a weight: single-precision reciprocal is enough)
+        const float fr = fabsf((float)res);
+        const double w = (fr > 0.0f) ? (double)(1.0f / fr) : 0.0;
+        const double wa1 = w * a1, wa2 = w * a2;
+        s[0] += wa1 * a1;
+        s[1] += wa1 * a2;
+        s[3] += wa2 * a2;
+        s[4] += wa1 * res;
+        s[5] += wa2 * res;
+    }
+    s[2] = s[1];
+    // block sums (warp shuffle, then one warp over the warps' partials)
+    __shared__ double sh[kNV][32];
+    __shared__ bool last;
+    const int tid = threadIdx.x;
+    const int nth = blockDim.x;
+    const int bid = blockIdx.x;
+    const int nb = gridDim.x;
+#pragma unroll
+    for (int q = 0; q < kNV; q++) {
+        double v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) sh[q][tid >> 5] = v;
+    }
+    __syncthreads();
+    if (tid < 32) {
+#pragma unroll
+        for (int q = 0; q < kNV; q++) {
+            double v = (tid < ((nth + 31) >> 5)) ? sh[q][tid] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (tid == 0) rs.part[(size_t)q * nb + bid] = v;
+        }
+        if (tid == 0) {
+            __threadfence();
+            const unsigned int t = atomicAdd(rs.count, 1u);
+            last = (t == (unsigned int)(nb - 1));
+        }
+    }
+    __syncthreads();
+    if (last) {
+        __threadfence();
+        // warp q folds sum q over the blocks (lane-strided, fixed order)
+        __shared__ double tot[kNV];
+        const int wq = tid >> 5, lane = tid & 31;
+        if (wq < kNV) {
+            double v = 0.0;
+            for (int b = lane; b < nb; b += 32) v += __ldcg(rs.part + (size_t)wq * nb + b);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) tot[wq] = v;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double al1 = 0.0, al2 = 0.0;
+            const double g11 = tot[0], g12 = tot[1], g21 = tot[2], g22 = tot[3], b1 = tot[4], b2 = tot[5];
+            bool done = false;
+            if (k2 != TC_ACCEL_NONE && g11 > 0.0 && g22 > 0.0) {
+                const double det = g11 * g22 - g12 * g21;
+                if (fabs(det) > 1e-12 * g11 * g22) {
+                    al1 = (b1 * g22 - g12 * b2) / det;
+                    al2 = (g11 * b2 - g21 * b1) / det;
+                    done = true;
+                }
+            }
+            if (!done) {
+                // one direction: the first if usable, else the second
+                if (g11 > 0.0) al1 = b1 / g11;
+                else if (k2 != TC_ACCEL_NONE && g22 > 0.0) al2 = b2 / g22;
+            }
+            ds->acc_alpha[0] = al1;
+            ds->acc_alpha[1] = al2;
+            *rs.count = 0u;
+        }
+    }
+    pdl_done();
+}
+
+__global__ void k_accel_update(Lay L, Range2 r, double* psi, double* prev, const double* dnn, int k1, int k2,
+                               const DevScalars* ds, int record_prev, int Vbc) {
+    pdl_entry();
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    const double al1 = __ldcg(&ds->acc_alpha[0]), al2 = __ldcg(&ds->acc_alpha[1]);
+    const double p0 = ld_state(psi + x);
+    const double v1 = dir_at(k1, psi, prev, dnn, x);
+    const double v2 = (k2 != TC_ACCEL_NONE) ? dir_at(k2, psi, prev, dnn, x) : 0.0;
+    const double pn = p0 + al1 * v1 + al2 * v2;
+    store_stream<double>(L, psi, i, k, pn, Vbc);
+    if (record_prev) store_stream<double>(L, prev, i, k, pn, Vbc);
+    pdl_done();
+}
+
+// dst = a - b over the whole plane (ghosts included: both follow the same
+// linear mirror rule, so the difference does too)
+__global__ void k_plane_diff(double* dst, const double* a, const double* b, size_t n) {
+    pdl_entry();
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        dst[t] = ld_state(a + t) - ld_state(b + t);
+    pdl_done();
+}
+
+}  // namespace
+
+void launch_accel(cudaStream_t s, const Level& l1, double* psi, double* prev, const double* dnn, int k1, int k2,
+                  int record_prev, RedScratch rs, DevScalars* ds, int Vbc) {
+    Range2 r{1, l1.L.a - 1, 1, l1.L.b - 1};
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    const int npts = (l1.L.a - 1) * (l1.L.b - 1);
+    int nb = (npts + 255) / 256;
+    if (nb > 2 * nsm) nb = 2 * nsm;
+    launch_pdl(k_accel_dots, dim3((unsigned)nb), dim3(256), 0, s, l1.L, (const double*)l1.coef,
+               (const double*)l1.rhs, (const double*)psi, (const double*)prev, dnn, k1, k2, rs, ds);
+    launch_pdl(k_accel_update, grid_for(r), dim3(BX, BY), 0, s, l1.L, r, psi, prev, dnn, k1, k2,
+               (const DevScalars*)ds, record_prev, Vbc);
+    tc_note_launch(2);
+}
+
+void launch_plane_diff(cudaStream_t s, double* dst, const double* a, const double* b, size_t n) {
+    int nb = (int)((n + 255) / 256);
+    if (nb > 2048) nb = 2048;
+    launch_pdl(k_plane_diff, dim3((unsigned)nb), dim3(256), 0, s, dst, a, b, n);
+    tc_note_launch();
+}

@@ -162,6 +162,10 @@ struct Handle {
     std::vector<int> sub_k, sub_end;
     double* subM[4] = {nullptr, nullptr, nullptr, nullptr};
     double* sub_tab = nullptr;
+    // corrections of psi (k_accel.cu): psi after the previous correction,
+    // the network's predicted change of the current solve
+    double *acc_prev = nullptr, *acc_dnn = nullptr;
+    bool acc_dnn_on = false;  // the current solve has a network direction
 };
 
 #define CK(call)                                                      \
@@ -560,6 +564,22 @@ static StepFusion step_fusion(Handle* h, int pp) {
     return f;
 }
 
+// cycle_correction: the minimal-residual correction of the level-1
+// streamfunction after each level-1 visit, along the change of psi since the
+// previous one (one whole W-cycle: coarse-grid correction and smoothing)
+// and, with cycle_correction = 2, the network's direction.  It runs at the
+// smoothed point of the cycle: right after the coarse-grid correction (level
+// 1 has no second visit in the reference's tables) psi carries the
+// prolongation's high-frequency error, which dominates the residual, and a
+// step there tends to cancel the cycle.  The residual the convergence test
+// reads is taken after the correction.
+void enqueue_cycle_correction(Handle* h) {
+    if (h->p.cycle_correction == 0 || h->acc_prev == nullptr) return;
+    const int k2 = (h->p.cycle_correction == 2 && h->acc_dnn_on) ? TC_ACCEL_DNN : TC_ACCEL_NONE;
+    launch_accel(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->acc_dnn, TC_ACCEL_DK, k2, 1, h->rs, h->ds,
+                 h->p.Vbc);
+}
+
 // Work of one multigrid cycle after the level-1 visit (p = 2..nsteps);
 // no host synchronisation inside, so it can be captured in a CUDA graph.
 void enqueue_cycle_rest(Handle* h) {
@@ -673,6 +693,7 @@ void enqueue_l1_mixed(Handle* h, int dir) {
     launch_residual_to32(h->st, l1, cur_err(h, 1), l1.rhs32, cur_e32(h, 1));
     iterate_stream32(h, 1, dir);
     launch_update64(h->st, l1, cur_err(h, 1), cur_e32(h, 1), h->p.Vbc);
+    enqueue_cycle_correction(h);
     launch_residual(h->st, l1, cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
 }
 
@@ -721,7 +742,7 @@ void enqueue_rest_mixed(Handle* h, int) {
 struct CycleGraphs {
     cudaGraphExec_t l1 = nullptr, rest = nullptr;
     long long n_l1 = 0, n_rest = 0;  // kernel nodes per graph
-    int ratio_level = -1, zero = -1, dir1 = -1;
+    int ratio_level = -1, zero = -1, dir1 = -1, dnn = -1;
     cudaStream_t st = nullptr;
 };
 
@@ -743,7 +764,13 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
     if (e != cudaSuccess) { h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return TC_ERR_CUDA; }
     return TC_OK;
 }
-void enqueue_l1(Handle* h, int dir) { iterate_stream(h, 1, dir); }
+void enqueue_l1(Handle* h, int dir) {
+    iterate_stream(h, 1, dir);
+    if (h->p.cycle_correction != 0 && h->acc_prev != nullptr) {
+        enqueue_cycle_correction(h);
+        launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+    }
+}
 void enqueue_rest(Handle* h, int) { enqueue_cycle_rest(h); }
 
 void compute_velocities(Handle* h);
@@ -849,7 +876,36 @@ tc_status multigrid(Handle* h) {
         launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
         launch_residual(h->st, h->lev[1], h->guess, h->rs, &h->ds->res_mag[0]);
     }
+    // the network's predicted change of this solve, d = guess - SF
+    // (learned_guess = 3: the start SF + alpha d, alpha residual-minimising;
+    // cycle_correction = 2: d spans the correction with each cycle's own)
+    h->acc_dnn_on = h->net != nullptr && !nonN && h->acc_dnn != nullptr &&
+                    (h->p.learned_guess == 3 || h->p.cycle_correction == 2);
+    if (h->acc_dnn_on) {
+        if (nn_guess(h->net, h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
+                     h->p.Vbc, h->p.learned_smooth) != 0) {
+            h->err = "learned guess: network forward failed";
+            return TC_ERR_CUDA;
+        }
+        launch_plane_diff(h->st, h->acc_dnn, h->guess, cur_err(h, 1), h->L1.plane);
+        if (h->p.learned_guess == 3)
+            launch_accel(h->st, h->lev[1], cur_err(h, 1), nullptr, h->acc_dnn, TC_ACCEL_DNN, TC_ACCEL_NONE, 0, h->rs,
+                         h->ds, h->p.Vbc);
+    }
     TRY(sync_scalars(h));
+    if (h->acc_dnn_on) {
+        int f = 0;
+        CK(cudaMemcpy(&f, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToHost));
+        if (f) {
+            h->err = "learned guess: a convolution's bounded wait gave up";
+            return TC_ERR_DEVICE_TIMEOUT;
+        }
+        if (h->p.learned_guess == 3) {
+            h->guess_offered++;
+            if (h->hs->acc_alpha[0] != 0.0) h->guess_used++;
+        }
+    }
+    if (h->p.cycle_correction != 0 && h->acc_prev != nullptr && !nonN) copy_plane(h, h->acc_prev, cur_err(h, 1));
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     if (try_guess) {
         int f = 0;
@@ -877,7 +933,7 @@ tc_status multigrid(Handle* h) {
     void (*f_rest)(Handle*, int) = mixed ? enqueue_rest_mixed : enqueue_rest;
     h->enq_err = cudaSuccess;
     if (use_graphs && (cg.l1 == nullptr || cg.ratio_level != h->ratio_level || cg.zero != h->p.mg_zero_coarse ||
-                       cg.dir1 != dir1 || cg.st != h->st)) {
+                       cg.dir1 != dir1 || cg.st != h->st || cg.dnn != (h->acc_dnn_on ? 1 : 0))) {
         if (cg.l1) cudaGraphExecDestroy(cg.l1);
         if (cg.rest) cudaGraphExecDestroy(cg.rest);
         cg.l1 = cg.rest = nullptr;
@@ -887,6 +943,7 @@ tc_status multigrid(Handle* h) {
         cg.zero = h->p.mg_zero_coarse;
         cg.dir1 = dir1;
         cg.st = h->st;
+        cg.dnn = h->acc_dnn_on ? 1 : 0;
     }
     int q = 1;
     for (;;) {
@@ -1161,7 +1218,12 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.tracer == 1 && p.Tbot != 0 && p.Tbot != 1) { h->err = "temperature tracers need Tbot = 0 or 1"; return TC_ERR_ARG; }
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
     if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;
-    if (p.learned_guess < 0 || p.learned_guess > 2 || p.learned_smooth < 0 || p.learned_smooth > 64) return TC_ERR_ARG;
+    if (p.learned_guess < 0 || p.learned_guess > 3 || p.learned_smooth < 0 || p.learned_smooth > 64) return TC_ERR_ARG;
+    if (p.cycle_correction < 0 || p.cycle_correction > 2) return TC_ERR_ARG;
+    if (p.non_Newtonian == 1 && p.cycle_correction != 0) {
+        h->err = "the cycle correction runs on Newtonian solves";
+        return TC_ERR_UNSUPPORTED;
+    }
     h->nx = p.nx; h->nz = p.nz; h->grids = p.grids;
     {
         const long nb = (long)((p.nx + 2 + BX - 1) / BX) * (long)((p.nz + 2 + BY - 1) / BY);
@@ -1434,6 +1496,11 @@ tc_status create(Handle* h, const tc_params* in) {
             TRY(dalloc_t(h, &h->sub_tab, 4 * (size_t)p.Nmulti));
             h->sub_on = true;
         }
+    }
+    // corrections after the level-1 visit: psi at the previous one, the network's direction
+    if (p.cycle_correction != 0 || p.learned_guess == 3) {
+        if (p.cycle_correction != 0) TRY(dalloc_t(h, &h->acc_prev, pl));
+        TRY(dalloc_t(h, &h->acc_dnn, pl));
     }
     // stability_RK4_smoother: dts_array
     {

@@ -65,6 +65,7 @@ struct DevScalars {
     int    lu_info;          // first zero pivot of the coarse LU (0 = none)
     int    visit_timeout;    // a fused visit's bounded neighbour wait gave up
     int    pad;
+    double acc_alpha[2];     // coefficients of the last correction of psi (k_accel.cu)
 };
 
 // Reduction scratch: per-block partials plus a completion counter.
@@ -179,6 +180,15 @@ int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const 
                           int per_point_down, const double* Ainv, const double* rowb, const int* cq, const int* cx,
                           int n, int m, int Vbc, int kmax, double* const* M);
 void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc);
+
+// (k_accel.cu) residual-minimising correction of the level-1 streamfunction along up to
+// two directions: TC_ACCEL_DK = psi - prev (the last W-cycle's correction),
+// TC_ACCEL_DNN = dnn (the network's predicted change); record_prev: prev =
+// the corrected psi afterwards
+enum { TC_ACCEL_NONE = 0, TC_ACCEL_DK = 1, TC_ACCEL_DNN = 2 };
+void launch_accel(cudaStream_t s, const Level& l1, double* psi, double* prev, const double* dnn, int k1, int k2,
+                  int record_prev, RedScratch rs, DevScalars* ds, int Vbc);
+void launch_plane_diff(cudaStream_t s, double* dst, const double* a, const double* b, size_t n);
 
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
