@@ -429,6 +429,13 @@ tc_status tc_time_visit(tc_handle* h, int32_t level, int32_t reps, double* ms_pe
  * kernel each) and writes the mean milliseconds per product.
  * TC_ERR_UNSUPPORTED if the handle has no such matrix. */
 tc_status tc_time_subcycle(tc_handle* h, int32_t k, int32_t reps, double* ms_per_apply);
+/* Timeout-path test (no counterpart in the reference).  With on != 0 every
+ * fused cluster visit of the handle first waits, with a bounded poll, for a
+ * device word that nothing sets, before it issues any sweep or write to
+ * another CTA; the poll runs out, the visit takes its timeout exit and the
+ * next tc_multigrid returns TC_ERR_DEVICE_TIMEOUT.  on = 0 restores normal
+ * visits; the handle then solves as before. */
+tc_status tc_debug_wait_test(tc_handle* h, int32_t on);
 int64_t tc_kernel_launches(void);
 
 /* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */

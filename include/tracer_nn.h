@@ -39,6 +39,14 @@ typedef struct tc_net tc_net;
 tc_status tcnn_create(int32_t nb_max, int32_t H, int32_t W, uint64_t seed, tc_net** out);
 tc_status tcnn_destroy(tc_net* net);
 tc_status tcnn_set_stream(tc_net* net, void* stream);
+/* Timeout-path test (no counterpart in the reference).  With on != 0 every
+ * 3x3 convolution of the network first waits, with a bounded poll, for a
+ * device word that nothing sets, after allocating its tensor memory and
+ * before issuing any copy; the poll runs out, the convolution reports
+ * failure, frees its tensor memory and returns, and a solve that uses the
+ * network returns TC_ERR_DEVICE_TIMEOUT.  on = 0 restores normal
+ * convolutions. */
+tc_status tcnn_debug_wait_test(tc_net* net, int32_t on);
 int64_t tcnn_param_count(const tc_net* net);
 /* Flat FP32 parameter / gradient vectors (layer by layer: W[cout][9][cin],
  * b[cout]; head w[32], b). */

@@ -21,7 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtracer_gpu.so")
 
-SOURCES = ["k_mg.cu", "k_visit.cu", "k_sweepblk.cu", "k_mixed.cu", "k_conv.cu", "k_nn.cu", "tc_nn_api.cu", "k_field.cu", "k_tracer.cu", "k_noalloc.cu", "k_subcycle.cu", "k_accel.cu", "tc_api.cu", "tc_setup.cpp", "tc_restart.cpp", "tc_format.cpp"]
+SOURCES = ["k_mg.cu", "k_visit.cu", "k_sweepblk.cu", "k_mixed.cu", "k_conv.cu", "k_nn.cu", "tc_nn_api.cu", "k_field.cu", "k_tracer.cu", "k_noalloc.cu", "k_subcycle.cu", "k_accel.cu", "k_loop.cu", "tc_api.cu", "tc_setup.cpp", "tc_restart.cpp", "tc_format.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

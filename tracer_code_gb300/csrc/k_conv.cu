@@ -36,6 +36,11 @@ struct ConvArgs {
     const float* bias;           // [N] or null
     __nv_bfloat16* out;
     int* fail;
+    // timeout-path test (null in use): after allocating its TMEM and before
+    // issuing any copy the kernel waits, bounded, for this device word to
+    // become non-zero; nothing sets it, so the wait runs out and the kernel
+    // reports failure, frees its TMEM and returns
+    const int* test_flag;
 };
 
 template <int N>
@@ -75,8 +80,19 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_base;
+    if (a.test_flag != nullptr) {
+        if (tid == 0) {
+            long it = 0;
+            while (*(volatile const int*)a.test_flag == 0 && ++it <= (1l << 14)) {
+            }
+            bad = 1;
+        }
+        __syncthreads();
+    }
 
-    if (tid == 0) {
+    if (bad) {
+        // (timeout-path test: no copy issued, nothing to wait for)
+    } else if (tid == 0) {
         // producer: stage s of step i holds tap i / nchunk, channel chunk i % nchunk
         for (int i = 0; i < nsteps; i++) {
             const int s = i % kStages;
@@ -110,7 +126,7 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
     __syncthreads();  // roles finished; `bad` visible to every thread
     // epilogue: warp w holds pixels 32w..32w+31 of the tile (warp-uniform
     // decision, the TMEM loads are warp-collective)
-    const bool ok = __all_sync(0xffffffffu, mbar_wait(&done, 0) ? 1 : 0) != 0;
+    const bool ok = !bad && __all_sync(0xffffffffu, mbar_wait(&done, 0) ? 1 : 0) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int m = warp * 32 + lane;
     const int px = x0 + m % a.bx, py = y0 + m / a.bx;
@@ -170,7 +186,7 @@ using namespace nn;
 // with cout_tot channels.
 int conv3x3_launch(cudaStream_t s, const __nv_bfloat16* x, int nb, int H, int W, int cin_tot, int cin_off, int cin,
                    const __nv_bfloat16* wpack, const float* bias, int N, int relu, __nv_bfloat16* out, int cout_tot,
-                   int cout_off, int cout_store, int* fail) {
+                   int cout_off, int cout_store, int* fail, const int* test_flag) {
     if (cin % 16 || cin_off % 8 || cout_off % 8 || cout_store % 8 || cout_store > N) return 1;
     if (!(N == 32 || N == 64 || N == 128 || N == 256)) return 1;
     const int bx = W < 128 ? W : 128;
@@ -192,7 +208,7 @@ int conv3x3_launch(cudaStream_t s, const __nv_bfloat16* x, int nb, int H, int W,
     a.nb = nb; a.H = H; a.W = W; a.bx = bx; a.by = by;
     a.cin = cin; a.cin_off = cin_off; a.kc = conv_kc(cin);
     a.cout_store = cout_store; a.cout_off = cout_off; a.cout_tot = cout_tot;
-    a.relu = relu; a.wpack = wpack; a.bias = bias; a.out = out; a.fail = fail;
+    a.relu = relu; a.wpack = wpack; a.bias = bias; a.out = out; a.fail = fail; a.test_flag = test_flag;
     const int smem = kStages * (a.kc * 256 + N * a.kc * 2);
     const unsigned grid = (unsigned)(nb * (H / by) * (W / bx));
     switch (N) {

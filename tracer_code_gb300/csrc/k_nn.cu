@@ -407,6 +407,8 @@ struct tc_net_impl {
     float *out = nullptr, *dout = nullptr, *tgt = nullptr, *stats = nullptr, *part = nullptr, *lossp = nullptr;
     size_t part_len = 0;
     int* fail = nullptr;
+    int* never = nullptr;      // a word that stays 0 (timeout-path test)
+    bool wait_test = false;    // tcnn_debug_wait_test: convs wait on `never` first
     std::vector<void*> allocs;
     std::string err;
 };
@@ -433,7 +435,7 @@ int conv_fwd(tc_net_impl* n, int l, int nb, View in, View out) {
     const int H = n->H >> s.lev, W = n->W >> s.lev;
     const int cin_p = (l == 0) ? 16 : s.cin;
     return conv3x3_launch(n->st, in.p, nb, H, W, in.ctot, in.off, cin_p, n->wpf[l], n->p + n->boff[l], npow(s.cout),
-                          1, out.p, out.ctot, out.off, s.cout, n->fail);
+                          1, out.p, out.ctot, out.off, s.cout, n->fail, n->wait_test ? n->never : nullptr);
 }
 
 // backward of layer l given dY (view, same shape as its output) and Y:
@@ -457,7 +459,7 @@ int conv_bwd(tc_net_impl* n, int l, int nb, View X, View Y, View dY, View dX) {
     k_reduce_parts<<<nblk(s.cout), 256, 0, n->st>>>(pb, nchunk, (size_t)s.cout, n->g + n->boff[l]); tc_note_launch();
     if (l == 0) return 0;
     return conv3x3_launch(n->st, n->dZ, nb, H, W, s.cout, 0, s.cout, n->wpb[l], nullptr, npow(s.cin), 0, dX.p,
-                          dX.ctot, dX.off, s.cin, n->fail);
+                          dX.ctot, dX.off, s.cin, n->fail, n->wait_test ? n->never : nullptr);
 }
 
 void pack_all(tc_net_impl* n) {
@@ -480,6 +482,8 @@ void pack_all(tc_net_impl* n) {
 int net_forward(tc_net_impl* n, int nb) {
     const int H = n->H, W = n->W;
     int r = 0;
+    // the failure flag reports this pass (and a backward pass that follows it)
+    if (cudaMemsetAsync(n->fail, 0, sizeof(int), n->st) != cudaSuccess) return 1;
     r |= conv_fwd(n, 0, nb, V(n->x16, 16, 0, 16), V(n->A0, 32, 0, 32));
     r |= conv_fwd(n, 1, nb, V(n->A0, 32, 0, 32), V(n->U0, 96, 64, 32));
     k_pool<<<nblk(px_at(n, 1, nb) * 32), 256, 0, n->st>>>(V(n->U0, 96, 64, 32), nb, H, W, V(n->P0, 32, 0, 32));
@@ -604,7 +608,8 @@ int net_create(tc_net_impl* n, int nbmax, int H, int W, uint64_t seed) {
         if (!nalloc(n, b.a, b.n) || !nalloc(n, b.d, b.n)) return 2;
     if (!nalloc(n, &n->x16, p0 * 16) || !nalloc(n, &n->dZ, p0 * 32)) return 2;
     if (!nalloc(n, &n->out, p0) || !nalloc(n, &n->dout, p0) || !nalloc(n, &n->tgt, p0) ||
-        !nalloc(n, &n->stats, (size_t)4 * nbmax) || !nalloc(n, &n->lossp, 4096) || !nalloc(n, &n->fail, 4))
+        !nalloc(n, &n->stats, (size_t)4 * nbmax) || !nalloc(n, &n->lossp, 4096) || !nalloc(n, &n->fail, 4) ||
+        !nalloc(n, &n->never, 4))
         return 2;
     // weight-gradient partials: the largest chunks * (cout*9*cin + cout) over layers
     size_t mx = 0;
@@ -747,6 +752,7 @@ float* net_grads(tc_net_impl* n) { return n->g; }
 float* net_out(tc_net_impl* n) { return n->out; }
 int net_nbmax(const tc_net_impl* n) { return n->nbmax; }
 int* net_fail(tc_net_impl* n) { return n->fail; }
+void net_set_wait_test(tc_net_impl* n, bool on) { n->wait_test = on; }
 size_t net_npx(const tc_net_impl* n, int nb) { return (size_t)nb * n->H * n->W; }
 int net_repack(tc_net_impl* n) {
     pack_all(n);

@@ -41,6 +41,8 @@ namespace cg = cooperative_groups;
 #define VISIT_MAX_CLUSTER 16
 #define VISIT_SMEM_MAX (96 * 1024)
 #define VISIT_WAIT_LIMIT (1 << 20)
+// polls of the timeout-path test's word (VisitParams.test_flag)
+#define VISIT_TEST_WAIT_LIMIT (1 << 14)
 
 template <typename T>
 struct VisitParams {
@@ -55,6 +57,11 @@ struct VisitParams {
     Lay Lr;
     T* zc;        // with the restriction: the coarser correction set to zero (zn values)
     size_t zn;
+    // timeout-path test (null in solves): before its first sweep the visit
+    // waits, bounded, for this device word to become non-zero; nothing sets
+    // it, so the wait runs out and the visit takes its timeout exit having
+    // issued no remote write
+    const int* test_flag;
 };
 
 // bilinear prolongation of the coarse correction at fine point (i,k): the
@@ -254,6 +261,16 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
     int phase = 0;  // bit q: parity of mbarrier q's current phase
     int cur_b = 0;
     bool timed_out = false;
+    if (Q.test_flag != nullptr) {
+        int gave_up = 0;
+        if (tid == 0) {
+            int it = 0;
+            while (*(volatile const int*)Q.test_flag == 0 && ++it <= VISIT_TEST_WAIT_LIMIT) {
+            }
+            gave_up = 1;
+        }
+        timed_out = __syncthreads_or(gave_up) != 0;
+    }
     const size_t tab_base = (size_t)(i - 1) + (size_t)(kr - 1) * cols;
     // table prefetch ring (FP64 per-point level): factors of sweeps n, n+1
     T pre0[P], pre1[P];
@@ -263,7 +280,7 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
         pre0[p] = (ld && Q.nsweeps > 0) ? __ldg(ctab + tab_base + (size_t)p * cols) : T(0);
         pre1[p] = (ld && Q.nsweeps > 1) ? __ldg(ctab + (size_t)npl + tab_base + (size_t)p * cols) : T(0);
     }
-    for (int n = 0; n < Q.nsweeps; n++) {
+    for (int n = 0; n < Q.nsweeps && !timed_out; n++) {
         const int nxt_b = (cur_b + 1 == nbuf) ? 0 : cur_b + 1;
         const T* cur = buf + (size_t)cur_b * bsz;
         T* nxt = buf + (size_t)nxt_b * bsz;
@@ -645,7 +662,7 @@ static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const Visi
 template <typename T>
 static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* rhs, const T* dts, const T* ctab,
                    const T* cA, const T* cB, T* res, const double* cvals, const double* tvals, int nsweeps,
-                   int per_point, int Vbc, int* flag, int cfg, const VisitXfer<T>* x) {
+                   int per_point, int Vbc, int* flag, int cfg, const VisitXfer<T>* x, const int* test_flag) {
     VisitShape sh;
     if (!visit_shape(L, nsweeps, sizeof(T) == sizeof(float), cfg, &sh)) return 1;
     if (per_point && sizeof(T) == sizeof(double) && ctab == nullptr) return 1;
@@ -663,6 +680,7 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
     Q.Lr = X.Lr;
     Q.zc = X.rc ? X.zc : nullptr;
     Q.zn = X.rc ? X.zn : 0;
+    Q.test_flag = test_flag;
     for (int n = 0; n < nsweeps; n++) {
         Q.c[n] = (T)cvals[n];
         Q.temp[n] = (T)tvals[n];
@@ -682,12 +700,13 @@ static int visit_t(cudaStream_t s, const Lay& L, T* S, const T* coef, const T* r
 // Returns 0 if the level was handled here (caller skips the per-sweep path).
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
                          const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag,
-                         const VisitXfer<double>* x) {
+                         const VisitXfer<double>* x, const int* test_flag) {
     return visit_t<double>(s, lv.L, S, lv.coef, lv.rhs, lv.dt_stream, ctab, lv.cA, lv.cB, lv.res, cvals, tvals,
-                           nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x);
+                           nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x, test_flag);
 }
 int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
-                           int nsweeps, int per_point, int Vbc, int* timeout_flag, const VisitXfer<float>* x) {
+                           int nsweeps, int per_point, int Vbc, int* timeout_flag, const VisitXfer<float>* x,
+                           const int* test_flag) {
     return visit_t<float>(s, lv.L, S, lv.coef32, lv.rhs32, lv.dts32, nullptr, lv.cA32, lv.cB32, lv.res32, cvals,
-                          tvals, nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x);
+                          tvals, nsweeps, per_point, Vbc, timeout_flag, lv.visit_cfg, x, test_flag);
 }

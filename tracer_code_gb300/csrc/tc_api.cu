@@ -129,6 +129,8 @@ struct Handle {
     std::string err;
     CycleGraphs* graphs = nullptr;
     bool no_graphs = false;
+    bool no_device_loop = false;  // convergence loop on the host (one read per W-cycle)
+    bool wait_test = false;       // tc_debug_wait_test: fused visits wait on a word nothing sets
     int cycles_acc = 0;  // W-cycles of all solves since tc_step began
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
     // cell order of the tracer arrays: perm[j] = reference index of slot j
@@ -511,7 +513,8 @@ void iterate_stream(Handle* h, int level, int dir, int pro = 0, int rst = 0, int
             }
         }
         if (launch_visit_cluster(h->st, lv, lv.err[lv.ecur], cv, tv, (h->ctab_level == level) ? h->ctab : nullptr,
-                                 Niter, pp, h->p.Vbc, &h->ds->visit_timeout, &x) == 0)
+                                 Niter, pp, h->p.Vbc, &h->ds->visit_timeout, &x,
+                                 h->wait_test ? &h->ds->never_set : nullptr) == 0)
             return;
     }
     if (pro) launch_prolong(h->st, h->lev[level + 1], lv, cur_err(h, level + 1), cur_err(h, level), h->p.Vbc);
@@ -649,7 +652,7 @@ void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, i
             }
         }
         if (launch_visit_cluster32(h->st, lv, cur_e32(h, level), cv, tv, Niter, pp, h->p.Vbc,
-                                   &h->ds->visit_timeout, &x) == 0)
+                                   &h->ds->visit_timeout, &x, h->wait_test ? &h->ds->never_set : nullptr) == 0)
             return;
     }
     if (pro) launch_prolong32(h->st, h->lev[level + 1], lv, cur_e32(h, level + 1), cur_e32(h, level), h->p.Vbc);
@@ -742,6 +745,11 @@ void enqueue_rest_mixed(Handle* h, int) {
 struct CycleGraphs {
     cudaGraphExec_t l1 = nullptr, rest = nullptr;
     long long n_l1 = 0, n_rest = 0;  // kernel nodes per graph
+    // the whole solve with its convergence loop on the device (k_loop.cu):
+    // kernels before the WHILE node and in its body
+    cudaGraphExec_t loop = nullptr;
+    long long n_pre = 0, n_body = 0;
+    bool loop_failed = false;  // the driver refused the conditional node: host loop
     int ratio_level = -1, zero = -1, dir1 = -1, dnn = -1;
     cudaStream_t st = nullptr;
 };
@@ -764,6 +772,84 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
     if (e != cudaSuccess) { h->err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e); return TC_ERR_CUDA; }
     return TC_OK;
 }
+// The solve as one graph: [init, level-1 visit, check] then a WHILE node
+// whose body is [rest of the cycle, level-1 visit, check]; both parts are
+// filled by stream capture (cudaStreamBeginCaptureToGraph).  Returns false
+// (with the stream out of capture and no error left pending) when the
+// driver does not take the conditional node.
+bool build_loop_graph(Handle* h, void (*f_l1)(Handle*, int), void (*f_rest)(Handle*, int), int dir1,
+                      cudaGraphExec_t* out, long long* n_pre, long long* n_body) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle cond;
+    if (cudaGraphConditionalHandleCreate(&cond, g, 0, 0) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        return false;
+    }
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    long long before = t_launches;
+    h->enq_err = cudaSuccess;
+    if (cudaStreamBeginCaptureToGraph(h->st, g, nullptr, nullptr, 0, mode) != cudaSuccess) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        return false;
+    }
+    launch_cycle_init(h->st, h->ds);
+    f_l1(h, dir1);
+    launch_cycle_check(h->st, h->ds, h->p.tolerance, h->p.max_cycles, cond);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    bool ok = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &capg, &deps, nullptr, &nd) == cudaSuccess &&
+              cs == cudaStreamCaptureStatusActive &&
+              cudaGraphAddNode(&wn, capg, deps, nullptr, nd, &np) == cudaSuccess &&
+              cudaStreamUpdateCaptureDependencies(h->st, &wn, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+                  cudaSuccess;
+    cudaGraph_t g2 = nullptr;
+    const bool ended = cudaStreamEndCapture(h->st, &g2) == cudaSuccess;
+    *n_pre = t_launches - before;
+    g_launches.fetch_sub(*n_pre);
+    t_launches = before;
+    if (!ok || !ended || h->enq_err != cudaSuccess) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        h->enq_err = cudaSuccess;
+        return false;
+    }
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    before = t_launches;
+    ok = cudaStreamBeginCaptureToGraph(h->st, body, nullptr, nullptr, 0, mode) == cudaSuccess;
+    if (ok) {
+        f_rest(h, 0);
+        f_l1(h, dir1);
+        launch_cycle_check(h->st, h->ds, h->p.tolerance, h->p.max_cycles, cond);
+        cudaGraph_t b2 = nullptr;
+        ok = cudaStreamEndCapture(h->st, &b2) == cudaSuccess;
+    }
+    *n_body = t_launches - before;
+    g_launches.fetch_sub(*n_body);
+    t_launches = before;
+    cudaGraphExec_t ge = nullptr;
+    if (ok && h->enq_err == cudaSuccess) ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+    else ok = false;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        h->enq_err = cudaSuccess;
+        return false;
+    }
+    *out = ge;
+    return true;
+}
+
 void enqueue_l1(Handle* h, int dir) {
     iterate_stream(h, 1, dir);
     if (h->p.cycle_correction != 0 && h->acc_prev != nullptr) {
@@ -936,9 +1022,13 @@ tc_status multigrid(Handle* h) {
                        cg.dir1 != dir1 || cg.st != h->st || cg.dnn != (h->acc_dnn_on ? 1 : 0))) {
         if (cg.l1) cudaGraphExecDestroy(cg.l1);
         if (cg.rest) cudaGraphExecDestroy(cg.rest);
-        cg.l1 = cg.rest = nullptr;
+        if (cg.loop) cudaGraphExecDestroy(cg.loop);
+        cg.l1 = cg.rest = cg.loop = nullptr;
         TRY(capture(h, &cg.l1, f_l1, dir1, &cg.n_l1));
         TRY(capture(h, &cg.rest, f_rest, 0, &cg.n_rest));
+        if (!cg.loop_failed && !h->no_device_loop &&
+            !build_loop_graph(h, f_l1, f_rest, dir1, &cg.loop, &cg.n_pre, &cg.n_body))
+            cg.loop_failed = true;
         cg.ratio_level = h->ratio_level;
         cg.zero = h->p.mg_zero_coarse;
         cg.dir1 = dir1;
@@ -946,7 +1036,23 @@ tc_status multigrid(Handle* h) {
         cg.dnn = h->acc_dnn_on ? 1 : 0;
     }
     int q = 1;
-    for (;;) {
+    if (use_graphs && cg.loop != nullptr) {
+        // the whole convergence loop on the device; one host read per solve
+        CK(cudaGraphLaunch(cg.loop, h->st));
+        TRY(sync_scalars(h));
+        q = h->hs->cyc_q;
+        const int st = h->hs->cyc_status;
+        const long long bodies = (st == TC_ERR_MG_CYCLES) ? q - 2 : q - 1;
+        tc_note_launch(cg.n_pre + (bodies > 0 ? bodies : 0) * cg.n_body);
+        if (h->hs->visit_timeout || st == TC_ERR_DEVICE_TIMEOUT) {
+            h->err = "fused smoother visit: neighbour wait exceeded its bound";
+            return TC_ERR_DEVICE_TIMEOUT;
+        }
+        if (st == TC_ERR_MG_RESIDUAL) return TC_ERR_MG_RESIDUAL;
+        if (st == TC_ERR_MG_CYCLES) { h->last_cycles = q; return TC_ERR_MG_CYCLES; }
+        if (st != 0) return (tc_status)st;
+    }
+    for (; !(use_graphs && cg.loop != nullptr);) {
         if (nonN) {
             strain_from_correction();
             TRY(level_setup());
@@ -1292,6 +1398,7 @@ tc_status create(Handle* h, const tc_params* in) {
     h->own_stream = true;
     h->graphs = new CycleGraphs();
     h->no_graphs = (std::getenv("TC_NO_GRAPHS") != nullptr);
+    h->no_device_loop = (std::getenv("TC_HOST_LOOP") != nullptr);
     h->fuse_visits = (std::getenv("TC_NO_FUSED_VISITS") == nullptr) && visit_cluster_setup() > 0;
     // ---- allocations ----
     h->L1 = make_lay(nx, nz);
@@ -1724,6 +1831,7 @@ tc_status tc_destroy(tc_handle* H) {
     if (h->graphs) {
         if (h->graphs->l1) cudaGraphExecDestroy(h->graphs->l1);
         if (h->graphs->rest) cudaGraphExecDestroy(h->graphs->rest);
+        if (h->graphs->loop) cudaGraphExecDestroy(h->graphs->loop);
         delete h->graphs;
     }
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
@@ -1952,7 +2060,8 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
     CycleGraphs& cg = *h->graphs;
     if (cg.l1) cudaGraphExecDestroy(cg.l1);
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
-    cg.l1 = cg.rest = nullptr;
+    if (cg.loop) cudaGraphExecDestroy(cg.loop);
+    cg.l1 = cg.rest = cg.loop = nullptr;
     return TC_OK;
 }
 
@@ -1983,7 +2092,8 @@ tc_status tc_set_launch_shapes(tc_handle* H, const int32_t* choices) {
     CycleGraphs& cg = *h->graphs;
     if (cg.l1) cudaGraphExecDestroy(cg.l1);
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
-    cg.l1 = cg.rest = nullptr;
+    if (cg.loop) cudaGraphExecDestroy(cg.loop);
+    cg.l1 = cg.rest = cg.loop = nullptr;
     return TC_OK;
 }
 
@@ -2139,6 +2249,19 @@ tc_status tc_time_subcycle(tc_handle* H, int32_t k, int32_t reps, double* ms_per
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *ms_per_apply = (double)ms / reps;
+    return TC_OK;
+}
+
+tc_status tc_debug_wait_test(tc_handle* H, int32_t on) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    h->wait_test = (on != 0);
+    // the cycle graphs bake in the visits' parameters: capture again
+    CycleGraphs& cg = *h->graphs;
+    if (cg.l1) cudaGraphExecDestroy(cg.l1);
+    if (cg.rest) cudaGraphExecDestroy(cg.rest);
+    if (cg.loop) cudaGraphExecDestroy(cg.loop);
+    cg.l1 = cg.rest = cg.loop = nullptr;
     return TC_OK;
 }
 

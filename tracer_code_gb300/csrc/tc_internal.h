@@ -66,6 +66,10 @@ struct DevScalars {
     int    visit_timeout;    // a fused visit's bounded neighbour wait gave up
     int    pad;
     double acc_alpha[2];     // coefficients of the last correction of psi (k_accel.cu)
+    int    cyc_q;            // W-cycle count of the device-side multigrid loop (k_loop.cu)
+    int    cyc_status;       // its stop reason: 0 converged, else the tc_status
+    int    never_set;        // stays 0: the word the timeout-path tests wait on
+    int    pad2;
 };
 
 // Reduction scratch: per-block partials plus a completion counter.
@@ -162,12 +166,13 @@ struct VisitXfer {
     T* zc = nullptr;
     size_t zn = 0;
 };
+// test_flag: the timeout-path test (tc_debug_wait_test); null in solves
 int launch_visit_cluster(cudaStream_t s, const Level& lv, double* S, const double* cvals, const double* tvals,
                          const double* ctab, int nsweeps, int per_point, int Vbc, int* timeout_flag,
-                         const VisitXfer<double>* x = nullptr);
+                         const VisitXfer<double>* x = nullptr, const int* test_flag = nullptr);
 int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const double* cvals, const double* tvals,
                            int nsweeps, int per_point, int Vbc, int* timeout_flag,
-                           const VisitXfer<float>* x = nullptr);
+                           const VisitXfer<float>* x = nullptr, const int* test_flag = nullptr);
 
 // (k_subcycle.cu) the bottom of the W-cycle (smoothing of level S = grids-1
 // and the coarsest solves between a restriction into S and the prolongation
@@ -189,6 +194,13 @@ enum { TC_ACCEL_NONE = 0, TC_ACCEL_DK = 1, TC_ACCEL_DNN = 2 };
 void launch_accel(cudaStream_t s, const Level& l1, double* psi, double* prev, const double* dnn, int k1, int k2,
                   int record_prev, RedScratch rs, DevScalars* ds, int Vbc);
 void launch_plane_diff(cudaStream_t s, double* dst, const double* a, const double* b, size_t n);
+
+// (k_loop.cu) the multigrid convergence loop on the device: the cycle counter
+// and the reference's tests after each level-1 visit, setting the condition
+// of the CUDA-graph WHILE node that repeats the cycle
+void launch_cycle_init(cudaStream_t s, DevScalars* ds);
+void launch_cycle_check(cudaStream_t s, DevScalars* ds, double tolerance, int max_cycles,
+                        cudaGraphConditionalHandle cond);
 
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);

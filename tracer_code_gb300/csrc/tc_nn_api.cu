@@ -21,6 +21,7 @@ float* net_grads(tc_net_impl* n);
 float* net_out(tc_net_impl* n);
 int net_nbmax(const tc_net_impl* n);
 int* net_fail(tc_net_impl* n);
+void net_set_wait_test(tc_net_impl* n, bool on);
 int net_repack(tc_net_impl* n);
 size_t net_npx(const tc_net_impl* n, int nb);
 int net_loss_value(tc_net_impl* n, float* host);
@@ -60,6 +61,11 @@ tc_status tcnn_destroy(tc_net* net) {
     net_destroy(net->impl);
     net_delete(net->impl);
     delete net;
+    return TC_OK;
+}
+tc_status tcnn_debug_wait_test(tc_net* net, int32_t on) {
+    if (!net) return TC_ERR_ARG;
+    net_set_wait_test(net->impl, on != 0);
     return TC_OK;
 }
 tc_status tcnn_set_stream(tc_net* net, void* stream) {

@@ -24,6 +24,7 @@ def _lib():
         L.tcnn_create.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_uint64, C.POINTER(vp)]
         L.tcnn_destroy.argtypes = [vp]
         L.tcnn_set_stream.argtypes = [vp, vp]
+        L.tcnn_debug_wait_test.argtypes = [vp, C.c_int32]
         L.tcnn_param_count.argtypes = [vp]
         L.tcnn_param_count.restype = C.c_int64
         L.tcnn_get_params.argtypes = [vp, vp]
@@ -96,6 +97,10 @@ class Net:
         _chk(self.L.tcnn_loss_backward(self.h, C.c_void_p(raw_ptr), C.c_void_p(sf_new_ptr), nb, C.byref(loss)),
              "tcnn_loss_backward")
         return float(loss.value)
+
+    def debug_wait_test(self, on: bool):
+        """Timeout-path test: every convolution waits on a word nothing sets (tcnn_debug_wait_test)."""
+        _chk(self.L.tcnn_debug_wait_test(self.h, 1 if on else 0), "tcnn_debug_wait_test")
 
     def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8):
         _chk(self.L.tcnn_adam(self.h, lr, beta1, beta2, eps), "tcnn_adam")
