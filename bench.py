@@ -519,6 +519,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     net.load(GUESS_WEIGHTS)
     learned.attach(sim, net)
     sim.upload(st)
+    shapes = sim.autotune()  # launch shapes per level, timed on this GPU (tc_autotune)
     with ClockSampler(local_rank) as clk:
         ms, solves, cycles, launches = timed_steps(sim, stream, args.steps, args.warmup, barrier)
     guess_used, guess_offered = learned.guess_stats(sim)
@@ -553,6 +554,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     pc.cycle_correction = 1
     simc = Simulation(pc, stream=stream.cuda_stream)
     simc.upload(st)
+    simc.autotune()
     msc, solvesc, _, _ = timed_steps(simc, stream, args.steps, args.warmup, barrier)
     corr_value = replica_rate(args.steps, msc * 1e-3, world, max_over_ranks)
     simc.close()
@@ -560,6 +562,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     pm = workload_params("mixed")
     simm = Simulation(pm, stream=stream.cuda_stream)
     simm.upload(st)
+    simm.autotune()
     msm, solvesm, _, _ = timed_steps(simm, stream, args.steps, args.warmup, barrier)
     mixed_value = replica_rate(args.steps, msm * 1e-3, world, max_over_ranks)
     simm.close()
@@ -567,6 +570,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     pp = workload_params("plain")
     sim0 = Simulation(pp, stream=stream.cuda_stream)
     sim0.upload(st)
+    sim0.autotune()
     ms0, solves0, cycles0, _ = timed_steps(sim0, stream, args.steps, args.warmup, barrier)
     plain_value = replica_rate(args.steps, ms0 * 1e-3, world, max_over_ranks)
     prof0 = cycle_profile(sim0, pp, fp32=False)
@@ -580,6 +584,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                    mg_zero_coarse_note="coarse-level corrections restart from zero when a level receives a new "
                                        "restricted residual (the reference keeps them; with 6 levels its W-cycle "
                                        "stalls on this workload); both arms and the CPU reference arm use it",
+                   launch_shapes={"tuned_by": "tc_autotune on this GPU, every arm",
+                                  "per_level_block_x_block_y_visit": shapes},
                    cycles_per_step=solves, warmup_cycles_per_step=cycles,
                    w_cycle_profile=prof, level1_sweep_roofline=roof_l1, step_roofline=step_roof,
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),

@@ -38,6 +38,7 @@ struct SubArgs {
     const T* cA;
     const T* cB;
     const T* tab;  // [4][nsweeps]: c and temp of the sweeps of a downward visit, then of an upward one
+    const T* ctab; // per-point Chebyshev factors 2/(cA + cB temp_n) of a downward visit, [nsweeps][nS]
     int nsweeps, per_point_down;
     const double* Ainv;  // coarsest level: explicit inverse, row scaling, interior unknown lists
     const double* rowb;
@@ -98,7 +99,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
     int pi[kPPT], pk[kPPT];
     size_t px[kPPT];
     bool pa[kPPT];
-    T cf[kPPT][TC_NCOEF], dt[kPPT], ca[kPPT], cb[kPPT];
+    T cf[kPPT][TC_NCOEF], dt[kPPT];
 #pragma unroll
     for (int q = 0; q < kPPT; q++) {
         const int p = tid + q * kThreads;
@@ -109,8 +110,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
 #pragma unroll
         for (int d = 0; d < TC_NCOEF; d++) cf[q][d] = pa[q] ? __ldg(A.coef + px[q] + d * A.LS.plane) : T(0);
         dt[q] = pa[q] ? __ldg(A.dts + px[q]) : T(0);
-        ca[q] = (pa[q] && A.per_point_down) ? __ldg(A.cA + px[q]) : T(1);
-        cb[q] = (pa[q] && A.per_point_down) ? __ldg(A.cB + px[q]) : T(0);
     }
     __syncthreads();
     if (tid == 0) R[IX(A.LS, 1 + j % a1, 1 + j / a1)] = T(1);
@@ -118,15 +117,16 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
     // one visit of Nmulti sweeps from Sa (ping-pong with Sb); returns the plane holding the result
     auto visit = [&](T* Sa, T* Sb, int up) -> T* {
         const T* cv = A.tab + (up ? 2 : 0) * A.nsweeps;
-        const T* tv = cv + A.nsweeps;
         const bool pp = !up && A.per_point_down;
         for (int n = 0; n < A.nsweeps; n++) {
-            const T cu = __ldg(cv + n), temp = __ldg(tv + n);
+            const T cu = __ldg(cv + n);
 #pragma unroll
             for (int q = 0; q < kPPT; q++) {
                 if (!pa[q]) continue;
                 const T res = sm_apply(A.LS, Sa, px[q], cf[q], R[px[q]]);
-                const T c = pp ? T(2) / (ca[q] + cb[q] * temp) : cu;
+                // the per-point factor from the table (the same correctly rounded
+                // division as k_sweep's, done once per solve)
+                const T c = pp ? __ldg(A.ctab + (size_t)n * nS + tid + q * kThreads) : cu;
                 store_stream<T>(A.LS, Sb, pi[q], pk[q], fma(c * dt[q], res, Sa[px[q]]), A.Vbc);
             }
             __syncthreads();
@@ -238,14 +238,15 @@ int subcycle_fits(const Lay& LS, const Lay& LG) {
 // The matrices are built in FP64 from the level's FP64 operator in both
 // solvers (in the mixed solve the FP32 smoother's coefficients are roundings
 // of the same FP64 ones).
-int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, int nsweeps,
-                          int per_point_down, const double* Ainv, const double* rowb, const int* cq, const int* cx,
-                          int n, int m, int Vbc, int kmax, double* const* M) {
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, const double* ctab,
+                          int nsweeps, int per_point_down, const double* Ainv, const double* rowb, const int* cq,
+                          const int* cx, int n, int m, int Vbc, int kmax, double* const* M) {
+    if (per_point_down && ctab == nullptr) return -1;
     if (kmax < 1 || kmax > 4) return -1;
     SubArgs<double> A{};
     A.LS = S.L; A.LG = G.L;
     A.coef = S.coef; A.dts = S.dt_stream; A.cA = S.cA; A.cB = S.cB;
-    A.tab = tab; A.nsweeps = nsweeps; A.per_point_down = per_point_down;
+    A.tab = tab; A.ctab = ctab; A.nsweeps = nsweeps; A.per_point_down = per_point_down;
     A.Ainv = Ainv; A.rowb = rowb; A.cq = cq; A.cx = cx; A.n = n; A.m = m;
     A.Vbc = Vbc; A.kmax = kmax; A.nS = (S.L.a - 1) * (S.L.b - 1);
     for (int k = 0; k < 4; k++) A.M[k] = M[k];

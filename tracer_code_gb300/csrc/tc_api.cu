@@ -164,6 +164,7 @@ struct Handle {
     std::vector<int> sub_k, sub_end;
     double* subM[4] = {nullptr, nullptr, nullptr, nullptr};
     double* sub_tab = nullptr;
+    double* sub_ctab = nullptr;  // per-point Chebyshev factors of level grids-1 [Nmulti][n_S]
     // corrections of psi (k_accel.cu): psi after the previous correction,
     // the network's predicted change of the current solve
     double *acc_prev = nullptr, *acc_dnn = nullptr;
@@ -924,7 +925,8 @@ tc_status multigrid(Handle* h) {
                 sweep_factors(Nm, n, dir, cheb_pp, &tv[(size_t)(2 * dir) * Nm + n - 1],
                               &tv[(size_t)(2 * dir + 1) * Nm + n - 1]);
         CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
-        if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_tab, Nm, cheb_pp ? 1 : 0,
+        if (cheb_pp) launch_cheb_table(h->st, h->lev[S], tv.data() + Nm, Nm, h->sub_ctab);
+        if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_tab, h->sub_ctab, Nm, cheb_pp ? 1 : 0,
                                   h->ainv, h->rowb, h->coarse_q, h->coarse_x, h->ngrid_coarse, h->coarse_m,
                                   h->p.Vbc, h->sub_kmax, h->subM) != 0) {
             h->err = "k_subcycle_build: launch failed";
@@ -1573,6 +1575,7 @@ tc_status create(Handle* h, const tc_params* in) {
     }
     // the bottom of the W-cycle as precomputed matrices
     if (p.mg_coarse_matrix == 1 && p.mg_zero_coarse == 1 && p.non_Newtonian == 0 && G >= 3 && !h->coarse_banded &&
+        p.Nmulti <= 128 &&
         subcycle_fits(h->lev[G - 1].L, h->lev[G].L)) {
         const int S = G - 1;
         h->sub_k.assign(h->nsteps + 2, 0);
@@ -1601,6 +1604,7 @@ tc_status create(Handle* h, const tc_params* in) {
             for (int k = 1; k <= 4; k++)
                 if (need[k]) TRY(dalloc_t(h, &h->subM[k - 1], nS * nS));
             TRY(dalloc_t(h, &h->sub_tab, 4 * (size_t)p.Nmulti));
+            TRY(dalloc_t(h, &h->sub_ctab, (size_t)p.Nmulti * nS));
             h->sub_on = true;
         }
     }

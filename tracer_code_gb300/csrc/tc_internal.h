@@ -181,9 +181,9 @@ int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const doub
 // apply reads the level's RHS and writes its correction in the solver's
 // precision (fp32: rhs32 / e32).
 int subcycle_fits(const Lay& LS, const Lay& LG);
-int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, int nsweeps,
-                          int per_point_down, const double* Ainv, const double* rowb, const int* cq, const int* cx,
-                          int n, int m, int Vbc, int kmax, double* const* M);
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, const double* ctab,
+                          int nsweeps, int per_point_down, const double* Ainv, const double* rowb, const int* cq,
+                          const int* cx, int n, int m, int Vbc, int kmax, double* const* M);
 void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc);
 
 // (k_accel.cu) residual-minimising correction of the level-1 streamfunction along up to
