@@ -135,6 +135,9 @@ __device__ __forceinline__ void st_async(uint32_t raddr, double v, uint32_t rbar
 __device__ __forceinline__ void mbar_init(uint32_t a, int count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
 }
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(a) : "memory");
+}
 __device__ __forceinline__ void mbar_arrive_expect(uint32_t a, int bytes) {
     asm volatile("{ .reg .b64 st; mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1; }" ::"r"(a), "r"(bytes)
                  : "memory");
@@ -250,7 +253,9 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
     }
     if (tid == 0 && C > 1) {
         // 0-2: the sweep buffers; 3: the residual rows of the fused restriction
-        for (int q = 0; q < 4; q++) mbar_init(smem_addr(&bar[q]), 1);
+        // sweep buffers: one arrival per warp (its values stored) plus the
+        // halo bytes; the residual rows: one arrival plus their bytes
+        for (int q = 0; q < 4; q++) mbar_init(smem_addr(&bar[q]), q < 3 ? NT / 32 : 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     // bytes this CTA receives per sweep: its halo rows that other CTAs own
@@ -388,19 +393,29 @@ __global__ void __launch_bounds__(NT, 1) k_visit_cluster(VisitParams<T> Q, T* Sg
             }
         }
         if (C > 1) {
-            if (tid == 0) mbar_arrive_expect(smem_addr(&bar[nxt_b]), expect);
-            __syncthreads();
-            int it = 0, to = 0;
-            while (!mbar_try_wait(smem_addr(&bar[nxt_b]), (phase >> nxt_b) & 1)) {
-                if (++it > VISIT_WAIT_LIMIT) { to = 1; break; }
+            // the phase completes when every warp has stored its values (one
+            // arrival per warp after __syncwarp) and the halo bytes of the
+            // neighbours have landed; no block-wide barrier per sweep
+            const uint32_t nb = smem_addr(&bar[nxt_b]);
+            __syncwarp();
+            if (tid == 0) mbar_arrive_expect(nb, expect);
+            else if ((tid & 31) == 0) mbar_arrive(nb);
+            int it = 0;
+            bool to = false;
+            while (!mbar_try_wait(nb, (phase >> nxt_b) & 1)) {
+                if (++it > VISIT_WAIT_LIMIT) { to = true; break; }
             }
             phase ^= 1 << nxt_b;
-            if (__syncthreads_or(to)) { timed_out = true; break; }
+            if (to) { timed_out = true; break; }
         } else {
             __syncthreads();
         }
         cur_b = nxt_b;
     }
+    // one decision for the whole CTA: a thread that gave up leaves its loop
+    // at once, the others give up at their next wait (its warp no longer
+    // arrives), so every thread gets here
+    timed_out = __syncthreads_or(timed_out ? 1 : 0) != 0;
     if (timed_out) {
         if (tid == 0) atomicExch(timeout_flag, 1);
     } else {
