@@ -185,10 +185,18 @@ typedef struct tc_params {
      * coarse-level correction: the minimal-residual correction on the
      * two-dimensional space spanned by that change and the attached
      * network's predicted change of the solve (formed once per multigrid
-     * call); it needs an attached network (without one it acts as 1).  The
-     * correction never raises the residual's 2-norm, the convergence test is
-     * the reference's and is taken after it, so the solution meets the same
-     * tolerance; cycle counts differ.  Not with non_Newtonian = 1. */
+     * call); it needs an attached network (without one it acts as 1).
+     * 3 = the windowed correction: the minimiser over psi + the span of the
+     * changes of the last four W-cycles (each stored with its image under
+     * the operator; a change nearly in the span of the newer ones is
+     * dropped), a Krylov acceleration of the W-cycle restarted at every
+     * multigrid call.  4 = 3 with the network's direction added to the span
+     * (without a network it acts as 3).  The coefficients minimise the
+     * residual weighted by 1/|r| (one reweighted least-squares step towards
+     * its L1 norm, the norm of the convergence test); the convergence test
+     * is the reference's and is taken after the correction, so the solution
+     * meets the same tolerance; cycle counts differ.  Not with
+     * non_Newtonian = 1. */
     int32_t cycle_correction;
 } tc_params;
 
@@ -436,6 +444,13 @@ tc_status tc_time_subcycle(tc_handle* h, int32_t k, int32_t reps, double* ms_per
  * next tc_multigrid returns TC_ERR_DEVICE_TIMEOUT.  on = 0 restores normal
  * visits; the handle then solves as before. */
 tc_status tc_debug_wait_test(tc_handle* h, int32_t on);
+/* Level-1 FP32 smoother of the mixed solve (no counterpart in the reference).
+ * By default it forms the 13 folded coefficients from five FP32 viscosity
+ * fields inside each sweep; with fields = 0 it reads the 13 coefficient
+ * planes rounded from FP64 instead (the same taps and factors; only the
+ * coefficients' rounding differs).  For tests that compare the two;
+ * TC_ERR_UNSUPPORTED when the handle has no field sweep (FP64 solve). */
+tc_status tc_debug_sweep_fields(tc_handle* h, int32_t fields);
 int64_t tc_kernel_launches(void);
 
 /* Copies u, w ((-span_interp:nx+span_interp, ...) each) to the host. */

@@ -90,3 +90,64 @@ def test_mixed_steps_against_fp64_oracle(gpu_lib):
     a, b = g.download(), o.download()
     assert np.abs(a["rtr"] - b["rtr"]).max() <= 1e-8
     assert np.abs(a["str"] - b["str"]).max() <= 1e-8
+
+
+def _capped_correction(p, st, fields=None):
+    # two W-cycles at most: the level-1 correction after the first cycle's
+    # coarse work and the second cycle's level-1 visit
+    from tracer_code_gb300 import TracerError
+    q = p.copy()
+    q.tolerance, q.max_cycles = 1e-300, 2
+    g = Simulation(q)
+    g.upload(st)
+    if fields is not None:
+        g.debug_sweep_fields(fields)
+    with pytest.raises(TracerError):
+        g.multigrid()
+    e1 = g.get("error", 1)
+    g.close()
+    return e1
+
+
+def test_level1_field_sweep(gpu_lib):
+    """The level-1 FP32 sweep that forms its coefficients from five FP32
+    viscosity fields is as close to the FP64 cycle as the sweep over the
+    13 coefficient planes rounded from FP64, and the full solves meet the
+    oracle's residual test with W-cycle counts within 10% (+1) of each
+    other."""
+    p = case_1024_like(nx=256, nz=64, grids=5, tpc=3)
+    p.mg_zero_coarse = 1
+    st = fresh_state(p, seed=7)
+    a = _capped_correction(p, st)
+    m = _mixed(p)
+    ef = _capped_correction(m, st, fields=True)
+    ep = _capped_correction(m, st, fields=False)
+    scale = np.abs(a).max()
+    df, dp = np.abs(ef - a).max() / scale, np.abs(ep - a).max() / scale
+    print(f"one cycle against FP64: field sweep {df:.3e}, coefficient planes {dp:.3e}")
+    assert df <= 2.0 * dp + 1e-12
+    cyc, sf = {}, {}
+    for fields in (True, False):
+        g = Simulation(m)
+        g.upload(st)
+        g.debug_sweep_fields(fields)
+        cyc[fields] = g.multigrid()
+        sf[fields] = g.download()["SF"]
+        g.close()
+    print(f"W-cycles: field sweep {cyc[True]}, coefficient planes {cyc[False]}")
+    assert abs(cyc[True] - cyc[False]) <= 0.1 * cyc[False] + 1
+    o = Oracle(p)
+    o.upload(st)
+    o.compute_viscosity(1)
+    assert _residual_ratio(o, sf[True]) <= p.tolerance
+    o.close()
+
+
+def test_field_sweep_toggle_needs_mixed(gpu_lib):
+    from tracer_code_gb300 import TracerError
+    p = case_128_like()
+    g = Simulation(p)
+    g.upload(fresh_state(p, seed=1))
+    with pytest.raises(TracerError):
+        g.debug_sweep_fields(False)
+    g.close()

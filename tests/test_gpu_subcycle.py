@@ -10,8 +10,9 @@ up to rounding:
   - after one W-cycle and the next level-1 visit from the same start (a solve
     capped at two cycles), the level-1 correction equals the sweep path's to
     1e-12 of its largest value (FP64); in the mixed solve (FP32 smoother,
-    the matrix kept in FP64) it is at least as close to the FP64 one as the
-    FP32 sweep path's is;
+    the matrix built in FP32 from the FP32 operator, products summed in
+    FP64) it is at least as close to the FP64 one as the FP32 sweep path's
+    is (3.7e-5 against 1.9e-4 measured on this case);
   - full solves take the same W-cycles as the oracle (FP64) and meet the
     oracle's residual test (both precisions); SF agrees with the oracle's to
     1e-9 of its largest value (FP64);
@@ -19,8 +20,7 @@ up to rounding:
   - at 1024x256 with the workload's physics (6 levels) one solve each way
     takes the same cycles in FP64; in the mixed solve the count moves with
     the FP32 rounding either way (53 and 58 measured at 1024x256 for the
-    sweep and matrix paths, whose one-cycle deviations from the FP64 cycle
-    are 1.9e-4 and 1.5e-4), so it is held within 15%.
+    sweep and matrix paths), so it is held within 15%.
 """
 import numpy as np
 import pytest

@@ -31,7 +31,7 @@ EXPORTS = [
     "tc_default_params", "tc_abi_sizes", "tc_create", "tc_destroy", "tc_get_info", "tc_set_stream",
     "tc_upload_state", "tc_download_state", "tc_set_clock", "tc_multigrid", "tc_compute_velocities", "tc_stats",
     "tc_energy_time", "tc_step", "tc_download_velocities", "tc_tracers_to_corners", "tc_download_counts",
-    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_time_subcycle", "tc_debug_wait_test", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
+    "tc_last_error", "tc_debug_field", "tc_step_host", "tc_time_sweep", "tc_time_visit", "tc_time_subcycle", "tc_debug_wait_test", "tc_debug_sweep_fields", "tc_kernel_launches", "tc_autotune", "tc_ensemble_step",
     "tc_set_launch_shapes", "tc_tracer_order", "tc_compute_strain_rate_invariant", "tc_compute_viscosity",
     "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
     "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
@@ -87,6 +87,7 @@ def load_library(build_if_missing: bool = False):
         L.tc_time_visit.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
         L.tc_time_subcycle.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_double)]
         L.tc_debug_wait_test.argtypes = [vp, C.c_int32]
+        L.tc_debug_sweep_fields.argtypes = [vp, C.c_int32]
         L.tc_autotune.argtypes = [vp, vp]
         L.tc_set_launch_shapes.argtypes = [vp, vp]
         L.tc_tracer_order.argtypes = [vp, vp]
@@ -312,6 +313,11 @@ class Simulation:
     def debug_wait_test(self, on: bool) -> None:
         """Timeout-path test: fused visits wait on a word nothing sets (tc_debug_wait_test)."""
         self._chk(self.L.tc_debug_wait_test(self.h, 1 if on else 0), "debug_wait_test")
+
+    def debug_sweep_fields(self, fields: bool) -> None:
+        """Level-1 FP32 sweep from the five viscosity fields (default) or from
+        the 13 coefficient planes (tc_debug_sweep_fields)."""
+        self._chk(self.L.tc_debug_sweep_fields(self.h, 1 if fields else 0), "debug_sweep_fields")
 
     @staticmethod
     def kernel_launches() -> int:

@@ -172,7 +172,208 @@ __global__ void k_plane_diff(double* dst, const double* a, const double* b, size
     pdl_done();
 }
 
+// ---- windowed correction ---------------------------------------------------
+// Directions j = 0..nd-1: j = 0 the newest change (written to slot
+// (head + 1) % TC_WIN this launch), j = 1..nold the stored changes from the
+// newest back, then the network's direction.  Sums: the upper triangle of
+// G (kWT entries, row-major) and b.
+constexpr int kWD = TC_WIN + 1;               // directions at most
+constexpr int kWT = kWD * (kWD + 1) / 2;      // Gram entries
+constexpr int kWS = kWT + kWD;                // sums
+
+__device__ __forceinline__ int win_slot(int head, int back) { return (head - back + 2 * TC_WIN) % TC_WIN; }
+
+__global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restrict__ coef, const double* rhs,
+                                                  const double* psi, const double* prev, double* P, double* AP,
+                                                  const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds) {
+    pdl_entry();
+    const int n = __ldcg(&ds->win_n), head = __ldcg(&ds->win_head);
+    const int nold = min(n, TC_WIN - 1);
+    const int nd = 1 + nold + (use_dnn ? 1 : 0);
+    const int snew = (n == 0) ? 0 : (head + 1) % TC_WIN;
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    const int a1i = L.a - 1, npts = (L.a - 1) * (L.b - 1);
+    double s[kWS];
+#pragma unroll
+    for (int q = 0; q < kWS; q++) s[q] = 0.0;
+    for (int pnt = blockIdx.x * blockDim.x + threadIdx.x; pnt < npts; pnt += gridDim.x * blockDim.x) {
+        const size_t x = IX(L, 1 + pnt % a1i, 1 + pnt / a1i);
+        double ap = 0.0, ad = 0.0, an = 0.0;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) {
+            const double c = __ldg(coef + x + d * L.plane);
+            const size_t y = (size_t)((ptrdiff_t)x + off[d]);
+            const double p = ld_state(psi + y);
+            ap = fma(c, p, ap);
+            ad = fma(c, p - ld_state(prev + y), ad);
+            if (use_dnn) an = fma(c, ld_state(dnn + y), an);
+        }
+        P[(size_t)snew * L.plane + x] = ld_state(psi + x) - ld_state(prev + x);
+        AP[(size_t)snew * L.plane + x] = ad;
+        const double res = ld_state(rhs + x) - ap;
+        double v[kWD];
+        v[0] = ad;
+#pragma unroll
+        for (int j = 1; j < kWD; j++) {
+            if (j <= nold) v[j] = ld_state(AP + (size_t)win_slot(snew, j) * L.plane + x);
+            else v[j] = (use_dnn && j == nold + 1) ? an : 0.0;
+        }
+        // w = 1/|r| (a weight: single-precision reciprocal is enough)
+        const float fr = fabsf((float)res);
+        const double w = (fr > 0.0f) ? (double)(1.0f / fr) : 0.0;
+        int t = 0;
+#pragma unroll
+        for (int i = 0; i < kWD; i++) {
+            const double wi = w * v[i];
+#pragma unroll
+            for (int j = i; j < kWD; j++) s[t++] += wi * v[j];
+            s[kWT + i] += wi * res;
+        }
+    }
+    // block sums (warp shuffle, then one warp over the warps' partials)
+    __shared__ double sh[kWS][8];
+    __shared__ bool last;
+    const int tid = threadIdx.x, bid = blockIdx.x, nb = gridDim.x;
+#pragma unroll
+    for (int q = 0; q < kWS; q++) {
+        double v = s[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) sh[q][tid >> 5] = v;
+    }
+    __syncthreads();
+    if (tid < 32) {
+        for (int q = 0; q < kWS; q++) {
+            double v = (tid < (int)(blockDim.x >> 5)) ? sh[q][tid] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (tid == 0) rs.part[(size_t)q * nb + bid] = v;
+        }
+        if (tid == 0) {
+            __threadfence();
+            const unsigned int t = atomicAdd(rs.count, 1u);
+            last = (t == (unsigned int)(nb - 1));
+        }
+    }
+    __syncthreads();
+    if (!last) {
+        pdl_done();
+        return;
+    }
+    __threadfence();
+    // warp w folds sums w, w + 8, ... over the blocks (lane-strided, fixed order)
+    __shared__ double tot[kWS];
+    {
+        const int wq = tid >> 5, lane = tid & 31;
+        for (int q = wq; q < kWS; q += (int)(blockDim.x >> 5)) {
+            double v = 0.0;
+            for (int b = lane; b < nb; b += 32) v += __ldcg(rs.part + (size_t)q * nb + b);
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if (lane == 0) tot[q] = v;
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        // LDL^T of G in direction order, dropping a direction whose pivot
+        // falls below 1e-10 of its diagonal (nearly in the span of the kept
+        // ones) or whose diagonal is not positive; then G beta = b on the
+        // kept directions
+        double G[kWD][kWD], Lm[kWD][kWD], D[kWD], y[kWD], beta[kWD];
+        bool keep[kWD];
+        int t = 0;
+        for (int i = 0; i < kWD; i++)
+            for (int j = i; j < kWD; j++) {
+                G[i][j] = tot[t];
+                G[j][i] = tot[t];
+                t++;
+            }
+        for (int i = 0; i < kWD; i++) {
+            keep[i] = false;
+            D[i] = 0.0;
+            beta[i] = 0.0;
+            for (int j = 0; j < kWD; j++) Lm[i][j] = 0.0;
+        }
+        for (int j = 0; j < nd; j++) {
+            double dj = G[j][j];
+            for (int k = 0; k < j; k++)
+                if (keep[k]) dj -= Lm[j][k] * Lm[j][k] * D[k];
+            if (!(G[j][j] > 0.0) || !(dj > 1e-10 * G[j][j])) continue;
+            keep[j] = true;
+            D[j] = dj;
+            Lm[j][j] = 1.0;
+            for (int i = j + 1; i < nd; i++) {
+                double v = G[i][j];
+                for (int k = 0; k < j; k++)
+                    if (keep[k]) v -= Lm[i][k] * Lm[j][k] * D[k];
+                Lm[i][j] = v / dj;
+            }
+        }
+        for (int i = 0; i < nd; i++) {
+            if (!keep[i]) continue;
+            double v = tot[kWT + i];
+            for (int k = 0; k < i; k++)
+                if (keep[k]) v -= Lm[i][k] * y[k];
+            y[i] = v;
+        }
+        for (int i = nd - 1; i >= 0; i--) {
+            if (!keep[i]) continue;
+            double v = y[i] / D[i];
+            for (int k = i + 1; k < nd; k++)
+                if (keep[k]) v -= Lm[k][i] * beta[k];
+            beta[i] = v;
+        }
+        for (int i = 0; i < kWD; i++) ds->win_beta[i] = beta[i];
+        ds->win_nd = nd;
+        ds->win_head = snew;
+        ds->win_n = min(n + 1, TC_WIN);
+        *rs.count = 0u;
+    }
+    pdl_done();
+}
+
+// psi += sum_j beta_j v_j (ghosts by the stream BCs); prev = the new psi
+__global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const double* P, const double* dnn,
+                             int use_dnn, const DevScalars* ds, int Vbc) {
+    pdl_entry();
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k);
+    const int nd = __ldcg(&ds->win_nd), head = __ldcg(&ds->win_head);
+    const int nold = nd - 1 - (use_dnn ? 1 : 0);
+    double pn = ld_state(psi + x);
+    for (int j = 0; j <= nold; j++) {
+        const double b = __ldcg(&ds->win_beta[j]);
+        if (b != 0.0) pn += b * ld_state(P + (size_t)win_slot(head, j) * L.plane + x);
+    }
+    if (use_dnn) {
+        const double b = __ldcg(&ds->win_beta[nd - 1]);
+        if (b != 0.0) pn += b * ld_state(dnn + x);
+    }
+    store_stream<double>(L, psi, i, k, pn, Vbc);
+    store_stream<double>(L, prev, i, k, pn, Vbc);
+    pdl_done();
+}
+
 }  // namespace
+
+void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* prev, double* P, double* AP,
+                         const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds, int Vbc) {
+    Range2 r{1, l1.L.a - 1, 1, l1.L.b - 1};
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    const int npts = (l1.L.a - 1) * (l1.L.b - 1);
+    int nb = (npts + 255) / 256;
+    if (nb > 2 * nsm) nb = 2 * nsm;
+    launch_pdl(k_win_dots, dim3((unsigned)nb), dim3(256), 0, s, l1.L, (const double*)l1.coef,
+               (const double*)l1.rhs, (const double*)psi, (const double*)prev, P, AP, dnn, use_dnn, rs, ds);
+    launch_pdl(k_win_update, grid_for(r), dim3(BX, BY), 0, s, l1.L, r, psi, prev, (const double*)P, dnn, use_dnn,
+               (const DevScalars*)ds, Vbc);
+    tc_note_launch(2);
+}
 
 void launch_accel(cudaStream_t s, const Level& l1, double* psi, double* prev, const double* dnn, int k1, int k2,
                   int record_prev, RedScratch rs, DevScalars* ds, int Vbc) {

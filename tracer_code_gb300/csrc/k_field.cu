@@ -351,89 +351,157 @@ void launch_strain(cudaStream_t s, const Lay& L, const Phys& P, const double* u,
 // [13] Nu denominator, [14] Nu_bot numerator, [15..18] q1..q4
 // ---------------------------------------------------------------------------
 #define NROWINT 7
-__global__ void k_stats_rows(Lay L, Phys P, const double* __restrict__ T, const double* __restrict__ u,
-                             const double* __restrict__ w, const double* __restrict__ cd,
-                             const double* __restrict__ vis, CPtrs Cn, double* __restrict__ rows) {
-    int k = blockIdx.x * blockDim.x + threadIdx.x;
-    const int nx = L.a, nz = L.b;
-    if (k > nz) return;
-    const int nrow = NROWINT;
-    // integrands: 0..ntype-1 C, then 4: u^2+w^2, 5: T, 6: RaT/conduct/vis
-    double acc[NROWINT];
-    for (int q = 0; q < nrow; q++) acc[q] = 0.0;
-    auto f = [&](int q, int i) -> double {
-        size_t x = IX(L, i, k);
-        if (q < 4) return (q < P.ntype) ? Cn.p[q][x] : 0.0;
-        if (q == 4) return u[x] * u[x] + w[x] * w[x];
-        if (q == 5) return T[x];
-        return P.RaT / cd[x] / vis[x];
-    };
-    for (int q = 0; q < nrow; q++) {
-        if (q < 4 && q >= P.ntype) continue;
-        if (q >= 5 && P.RaT == 0.0) continue;
-        double fint = 0.0;
-        double fprev = f(q, 0);
-        for (int i = 0; i <= nx - 1; i++) {
-            double fn = f(q, i + 1);
-            fint = fint + 0.5 * (fprev * 1.0 + fn * 1.0) * P.dr;
-            fprev = fn;
-        }
-        acc[q] = fint;
-    }
-    for (int q = 0; q < nrow; q++) rows[(size_t)q * (nz + 1) + k] = acc[q];
+// The integrands are evaluated in parallel into shared memory, CH columns at
+// a time; one thread per running sum then adds them serially with the
+// reference's expression, so every sum takes the same operations in the same
+// order as the serial loop (the values are the same doubles).
+constexpr int kStatCH = 512;
+constexpr int kStatThreads = 256;
+
+// integrand q at (i, k): 0..3 C by type, 4 u^2+w^2, 5 T, 6 RaT/conduct/vis
+__device__ __forceinline__ double stat_integrand(const Lay& L, const Phys& P, const double* __restrict__ T,
+                                                 const double* __restrict__ u, const double* __restrict__ w,
+                                                 const double* __restrict__ cd, const double* __restrict__ vis,
+                                                 const CPtrs& Cn, int q, int i, int k) {
+    const size_t x = IX(L, i, k);
+    if (q < 4) return (q < P.ntype) ? Cn.p[q][x] : 0.0;
+    if (q == 4) return u[x] * u[x] + w[x] * w[x];
+    if (q == 5) return T[x];
+    return P.RaT / cd[x] / vis[x];
 }
-__global__ void k_stats_final(Lay L, Phys P, int kent, const double* __restrict__ rows,
-                              const double* __restrict__ T, const double* __restrict__ u,
-                              const double* __restrict__ w, const double* __restrict__ cd,
-                              const double* __restrict__ st, DevScalars* ds) {
+__device__ __forceinline__ bool stat_row_active(const Phys& P, int q) {
+    if (q < 4 && q >= P.ntype) return false;
+    if (q >= 5 && P.RaT == 0.0) return false;
+    return true;
+}
+
+// integrate1Dx of every row k (basics.f90 trapezoid, left to right): one
+// block per row
+__global__ void __launch_bounds__(kStatThreads) k_stats_rows(Lay L, Phys P, const double* __restrict__ T,
+                                                             const double* __restrict__ u,
+                                                             const double* __restrict__ w,
+                                                             const double* __restrict__ cd,
+                                                             const double* __restrict__ vis, CPtrs Cn,
+                                                             double* __restrict__ rows) {
+    __shared__ double fv[NROWINT][kStatCH + 1];
+    const int k = blockIdx.x;
+    const int nx = L.a, nz = L.b;
+    const int t = threadIdx.x;
+    double fint = 0.0;
+    for (int c0 = 0; c0 < nx; c0 += kStatCH) {
+        const int n = min(kStatCH, nx - c0);  // sums over i = c0..c0+n-1 use f(c0..c0+n)
+        for (int e = t; e < NROWINT * (n + 1); e += blockDim.x) {
+            const int q = e / (n + 1), j = e % (n + 1);
+            fv[q][j] = stat_row_active(P, q) ? stat_integrand(L, P, T, u, w, cd, vis, Cn, q, c0 + j, k) : 0.0;
+        }
+        __syncthreads();
+        if (t < NROWINT && stat_row_active(P, t)) {
+            double fprev = fv[t][0];
+            for (int j = 0; j < n; j++) {
+                const double fn = fv[t][j + 1];
+                fint = fint + 0.5 * (fprev * 1.0 + fn * 1.0) * P.dr;
+                fprev = fn;
+            }
+        }
+        __syncthreads();
+    }
+    if (t < NROWINT) rows[(size_t)t * (nz + 1) + k] = stat_row_active(P, t) ? fint : 0.0;
+}
+
+// integrate1Dz of the row integrals (from k = 0, and from kent for the C
+// types), the top-row and Nusselt integrals along x, the corner fluxes and
+// the top-row strain maximum.  One block.
+__global__ void __launch_bounds__(kStatThreads) k_stats_final(Lay L, Phys P, int kent,
+                                                              const double* __restrict__ rows,
+                                                              const double* __restrict__ T,
+                                                              const double* __restrict__ u,
+                                                              const double* __restrict__ w,
+                                                              const double* __restrict__ cd,
+                                                              const double* __restrict__ st, DevScalars* ds) {
+    __shared__ double fv[NROWINT][kStatCH + 1];
+    __shared__ double red[kStatThreads / 32];
     const int nx = L.a, nz = L.b;
     const int t = threadIdx.x;
     const size_t ld = (size_t)L.ld;
-    // threads 0..6: z-integrals of the row integrals; 7..10: from kent for C types
-    if (t < NROWINT + 4) {
-        int q = (t < NROWINT) ? t : (t - NROWINT);
-        int k0 = (t < NROWINT) ? 0 : kent;
-        bool active = true;
+    // z-integrals: thread t < NROWINT sums row t from k = 0; thread
+    // NROWINT + q (q < 4) sums C type q from kent
+    {
+        const int q = (t < NROWINT) ? t : t - NROWINT;
+        const int k0 = (t < NROWINT) ? 0 : kent;
+        bool active = (t < NROWINT + 4);
         if (q < 4 && q >= P.ntype) active = false;
         if (t >= NROWINT && q >= 4) active = false;
+        double fint = 0.0;
+        for (int c0 = 0; c0 < nz; c0 += kStatCH) {
+            const int n = min(kStatCH, nz - c0);
+            for (int e = t; e < NROWINT * (n + 1); e += blockDim.x) {
+                const int qq = e / (n + 1), j = e % (n + 1);
+                fv[qq][j] = rows[(size_t)qq * (nz + 1) + c0 + j];
+            }
+            __syncthreads();
+            if (active) {
+                for (int j = 0; j < n; j++) {
+                    if (c0 + j < k0) continue;
+                    fint = fint + 0.5 * (fv[q][j] * 1.0 + fv[q][j + 1] * 1.0) * P.ds;
+                }
+            }
+            __syncthreads();
+        }
         if (active) {
-            const double* f = rows + (size_t)q * (nz + 1);
-            double fint = 0.0;
-            for (int k = k0; k <= nz - 1; k++) fint = fint + 0.5 * (f[k] * 1.0 + f[k + 1] * 1.0) * P.ds;
-            int slot = (t < NROWINT) ? ((q < 4) ? q : (q - 4 + 8)) : (4 + q);
+            const int slot = (t < NROWINT) ? ((q < 4) ? q : (q - 4 + 8)) : (4 + q);
             ds->integ[slot] = fint;
         }
-    } else if (t == 16) {
-        // top-row mobility integrand and the Nusselt integrands
-        double a = 0.0, b = 0.0, c = 0.0, m = 0.0;
-        auto top = [&](int i) { size_t x = IX(L, i, nz); return u[x] * u[x] + w[x] * w[x]; };
-        auto Tzs = [&](int i) { size_t x = IX(L, i, nz); return (-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0; };
-        auto Tzb = [&](int i) { size_t x = IX(L, i, 0); return (-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0; };
-        for (int i = 0; i <= nx - 1; i++) {
-            m = m + 0.5 * (top(i) * 1.0 + top(i + 1) * 1.0) * P.dr;
-            if (P.RaT != 0.0) {
-                double ai = -cd[IX(L, i, nz)] * Tzs(i), ai1 = -cd[IX(L, i + 1, nz)] * Tzs(i + 1);
-                a = a + 0.5 * (ai * 1.0 + ai1 * 1.0) * P.dr;
-                double bi = T[IX(L, i, 0)], bi1 = T[IX(L, i + 1, 0)];
-                b = b + 0.5 * (bi * 1.0 + bi1 * 1.0) * P.dr;
-                double ci = -cd[IX(L, i, 0)] * Tzb(i), ci1 = -cd[IX(L, i + 1, 0)] * Tzb(i + 1);
-                c = c + 0.5 * (ci * 1.0 + ci1 * 1.0) * P.dr;
+    }
+    // top-row mobility integrand and the Nusselt integrands: values 0 top(i),
+    // 1 -cd*dT/dz at the top, 2 T at the bottom, 3 -cd*dT/dz at the bottom;
+    // thread j < 4 keeps sum j
+    {
+        const bool rat = (P.RaT != 0.0);
+        double acc = 0.0;
+        for (int c0 = 0; c0 < nx; c0 += kStatCH) {
+            const int n = min(kStatCH, nx - c0);
+            for (int e = t; e < 4 * (n + 1); e += blockDim.x) {
+                const int q = e / (n + 1), i = c0 + e % (n + 1);
+                double v = 0.0;
+                if (q == 0) {
+                    const size_t x = IX(L, i, nz);
+                    v = u[x] * u[x] + w[x] * w[x];
+                } else if (rat && q == 1) {
+                    const size_t x = IX(L, i, nz);
+                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0);
+                } else if (rat && q == 2) {
+                    v = T[IX(L, i, 0)];
+                } else if (rat && q == 3) {
+                    const size_t x = IX(L, i, 0);
+                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0);
+                }
+                fv[q][e % (n + 1)] = v;
             }
+            __syncthreads();
+            if (t < 4 && (t == 0 || rat)) {
+                for (int j = 0; j < n; j++) acc = acc + 0.5 * (fv[t][j] * 1.0 + fv[t][j + 1] * 1.0) * P.dr;
+            }
+            __syncthreads();
         }
-        ds->integ[11] = m;
-        ds->integ[12] = a;
-        ds->integ[13] = b;
-        ds->integ[14] = c;
-        if (P.RaT != 0.0) {
-            auto dz = [&](int i, int kk) { size_t x = IX(L, i, kk); return -0.5 * T[x - ld] + 0.5 * T[x + ld]; };
-            ds->integ[15] = -(cd[IX(L, 0, nz)] * dz(0, nz)) / P.ds / 1.0;
-            ds->integ[16] = -(cd[IX(L, nx, nz)] * dz(nx, nz)) / P.ds / 1.0;
-            ds->integ[17] = -(cd[IX(L, nx, 0)] * dz(nx, 0)) / P.ds / 1.0;
-            ds->integ[18] = -(cd[IX(L, 0, 0)] * dz(0, 0)) / P.ds / 1.0;
-        }
-        double smax = -INFINITY;
-        for (int i = 0; i <= nx; i++) smax = fmax(smax, st[IX(L, i, nz)]);
-        ds->strain_max = smax;
+        if (t < 4) ds->integ[11 + t] = acc;
+    }
+    if (t == 0 && P.RaT != 0.0) {
+        auto dz = [&](int i, int kk) { size_t x = IX(L, i, kk); return -0.5 * T[x - ld] + 0.5 * T[x + ld]; };
+        ds->integ[15] = -(cd[IX(L, 0, nz)] * dz(0, nz)) / P.ds / 1.0;
+        ds->integ[16] = -(cd[IX(L, nx, nz)] * dz(nx, nz)) / P.ds / 1.0;
+        ds->integ[17] = -(cd[IX(L, nx, 0)] * dz(nx, 0)) / P.ds / 1.0;
+        ds->integ[18] = -(cd[IX(L, 0, 0)] * dz(0, 0)) / P.ds / 1.0;
+    }
+    // top-row strain maximum (fmax is exact and order-free)
+    double smax = -INFINITY;
+    for (int i = t; i <= nx; i += blockDim.x) smax = fmax(smax, st[IX(L, i, nz)]);
+    for (int o = 16; o > 0; o >>= 1) smax = fmax(smax, __shfl_down_sync(0xffffffffu, smax, o));
+    if ((t & 31) == 0) red[t >> 5] = smax;
+    __syncthreads();
+    if (t == 0) {
+        double m = -INFINITY;
+        for (int j = 0; j < (int)(blockDim.x >> 5); j++) m = fmax(m, red[j]);
+        ds->strain_max = m;
     }
 }
 __global__ void k_nempty_stats(Lay L, Range2 r, const int* __restrict__ ne, DevScalars* ds) {
@@ -465,8 +533,8 @@ void launch_stats(cudaStream_t s, const Lay& L, const Phys& P, int kent, const d
                   const double* const* Cnew, const int* nempty, double* rows, DevScalars* ds) {
     CPtrs C{};
     for (int j = 0; j < P.ntype && j < TC_MAX_TYPES; j++) C.p[j] = Cnew[j];
-    k_stats_rows<<<(L.b + 1 + 63) / 64, 64, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows); tc_note_launch();
-    k_stats_final<<<1, 32, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds); tc_note_launch();
+    k_stats_rows<<<L.b + 1, kStatThreads, 0, s>>>(L, P, T, u, w, conduct, vis, C, rows); tc_note_launch();
+    k_stats_final<<<1, kStatThreads, 0, s>>>(L, P, kent, rows, T, u, w, conduct, strain, ds); tc_note_launch();
     if (P.comp == 1 || P.tracer == 1) {
         Range2 r{0, L.a, 0, L.b};
         k_nempty_init<<<1, 1, 0, s>>>(ds); tc_note_launch();

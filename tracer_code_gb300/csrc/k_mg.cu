@@ -94,11 +94,18 @@ __global__ void k_vis_grad(Lay L, LevConst c, Range2 r, const double* __restrict
         } else {
             const size_t ld = (size_t)L.ld;
             double v0 = V[x], vm = V[x - 1], vp = V[x + 1], vzm = V[x - ld], vzp = V[x + ld];
-            double vis_r = (-0.5 * vm + 0.5 * vp) / c.dr;
-            double vis_rr = (vm + -2.0 * v0 + vp) / c.dr2;
-            double vis_s = (-0.5 * vzm + 0.5 * vzp) / c.ds;
-            double vis_ss = (vzm + -2.0 * v0 + vzp) / c.ds2;
-            double vis_rs = (0.25 * V[x - 1 - ld] + -0.25 * V[x + 1 - ld] + -0.25 * V[x - 1 + ld] + 0.25 * V[x + 1 + ld]) / c.drds;
+            const double nr = -0.5 * vm + 0.5 * vp, nrr = vm + -2.0 * v0 + vp;
+            const double ns = -0.5 * vzm + 0.5 * vzp, nss = vzm + -2.0 * v0 + vzp;
+            const double nrs =
+                0.25 * V[x - 1 - ld] + -0.25 * V[x + 1 - ld] + -0.25 * V[x - 1 + ld] + 0.25 * V[x + 1 + ld];
+            // power-of-two spacings: the products equal the quotients exactly
+            double vis_r, vis_rr, vis_s, vis_ss, vis_rs;
+            if (c.recip) {
+                vis_r = nr * c.rdr; vis_rr = nrr * c.rdr2; vis_s = ns * c.rds; vis_ss = nss * c.rds2;
+                vis_rs = nrs * c.rdrds;
+            } else {
+                vis_r = nr / c.dr; vis_rr = nrr / c.dr2; vis_s = ns / c.ds; vis_ss = nss / c.ds2; vis_rs = nrs / c.drds;
+            }
             vx[x] = vis_r; vz[x] = vis_s; vxx[x] = vis_rr; vzz[x] = vis_ss; vxz[x] = vis_rs;
             if (do_eig) {
                 double eR, eI;
@@ -127,8 +134,10 @@ __global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restr
     const size_t ld = (size_t)L.ld;
     size_t x = IX(L, i, k);
     double v0 = Vin[x];
-    double Trr = (Vin[x - 1] + -2.0 * v0 + Vin[x + 1]) / cc.dr2;
-    double Tss = (Vin[x - ld] + -2.0 * v0 + Vin[x + ld]) / cc.ds2;
+    const double nrr = Vin[x - 1] + -2.0 * v0 + Vin[x + 1], nss = Vin[x - ld] + -2.0 * v0 + Vin[x + ld];
+    // power-of-two spacings: the products equal the quotients exactly
+    const double Trr = cc.recip ? nrr * cc.rdr2 : nrr / cc.dr2;
+    const double Tss = cc.recip ? nss * cc.rds2 : nss / cc.ds2;
     double temp = Trr + Tss;
     double dts = dtv[x] * 0.99;
     double v = v0 + c * dts * temp;

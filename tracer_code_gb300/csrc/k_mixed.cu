@@ -59,6 +59,109 @@ __global__ void __launch_bounds__(256, 1) k_sweep32(Lay L, Range2 r, const float
     pdl_done();
 }
 
+// Level-1 FP32 sweep that forms its 13 coefficients from the five viscosity
+// fields in registers (42 multiply-adds per point, the structural zeros of
+// the stencil skipped) instead of reading 13 coefficient planes: 24 B of
+// coefficient and dt data per point where the folded planes take 56 B.
+// Two points per thread (rows k, k+1) share their vertical taps; the taps
+// and their order are k_sweep_x2's, so only the coefficients' rounding
+// differs from the folded FP32 sweep (FP32 sums of FP32-rounded fields
+// instead of FP32 roundings of FP64 sums).
+__global__ void __launch_bounds__(256, 1) k_sweep_g32(Lay L, Range2 r, FoldG32 F, const float* Sin, float* Sout,
+                                                      const float* __restrict__ g, const float* rhs,
+                                                      const float* __restrict__ dts, const float* __restrict__ cA,
+                                                      const float* __restrict__ cB, float c_uniform, int per_point,
+                                                      float temp, int Vbc) {
+    constexpr unsigned kMask[TC_NCOEF] = TC_FOLD_G32_MASK;
+    const int i = r.i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
+    const int k = r.k0 + 2 * (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    bool act[2];
+    act[0] = (i <= r.i1) && (k <= r.k1);
+    act[1] = act[0] && (k + 1 <= r.k1);
+    const size_t ld = (size_t)L.ld, pl = L.plane;
+    const size_t x = act[0] ? IX(L, i, k) : 0;
+    float cf[2][TC_NCOEF], dt[2], ca[2], cb[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        const size_t xp = act[p] ? x + p * ld : x;
+        float G[5];
+#pragma unroll
+        for (int j = 0; j < 5; j++) G[j] = act[p] ? __ldg(g + xp + j * pl) : 0.f;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) {
+            float c = 0.f;
+            bool first = true;
+#pragma unroll
+            for (int j = 0; j < 5; j++) {
+                if (!((kMask[d] >> j) & 1u)) continue;
+                c = first ? G[j] * F.w[d][j] : fmaf(G[j], F.w[d][j], c);
+                first = false;
+            }
+            cf[p][d] = -c;
+        }
+        dt[p] = act[p] ? __ldg(dts + xp) : 0.f;
+        ca[p] = (act[p] && per_point) ? __ldg(cA + xp) : 1.f;
+        cb[p] = (act[p] && per_point) ? __ldg(cB + xp) : 0.f;
+    }
+    pdl_entry();
+    if (!act[0]) return;
+    // centre column rows k-2..k+3, columns i+-1 rows k-1..k+2, i+-2 rows k..k+1
+    const float* s = Sin + x;
+    float v0[6], vm1[4], vp1[4], vm2[2], vp2[2], rh[2];
+#pragma unroll
+    for (int q = 0; q < 6; q++) v0[q] = ld_state(s + (ptrdiff_t)(q - 2) * (ptrdiff_t)ld);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        vm1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld - 1);
+        vp1[q] = ld_state(s + (ptrdiff_t)(q - 1) * (ptrdiff_t)ld + 1);
+    }
+#pragma unroll
+    for (int q = 0; q < 2; q++) {
+        vm2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld - 2);
+        vp2[q] = ld_state(s + (ptrdiff_t)q * (ptrdiff_t)ld + 2);
+        rh[q] = act[q] ? ld_state(rhs + x + q * ld) : 0.f;
+    }
+    // the folded operator's tap order (fold_apply)
+    float acc[2];
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        float a = fmaf(cf[p][0], v0[p + 2], rh[p]);
+        a = fmaf(cf[p][1], vm1[p + 1], a);
+        a = fmaf(cf[p][2], vp1[p + 1], a);
+        a = fmaf(cf[p][3], vm2[p], a);
+        a = fmaf(cf[p][4], vp2[p], a);
+        a = fmaf(cf[p][5], v0[p + 1], a);
+        a = fmaf(cf[p][6], v0[p + 3], a);
+        a = fmaf(cf[p][7], v0[p], a);
+        a = fmaf(cf[p][8], v0[p + 4], a);
+        a = fmaf(cf[p][9], vm1[p], a);
+        a = fmaf(cf[p][10], vp1[p], a);
+        a = fmaf(cf[p][11], vm1[p + 2], a);
+        acc[p] = fmaf(cf[p][12], vp1[p + 2], a);
+    }
+#pragma unroll
+    for (int p = 0; p < 2; p++) {
+        if (!act[p]) continue;
+        const float c = per_point ? 2.0f / (ca[p] + cb[p] * temp) : c_uniform;
+        store_stream<float>(L, Sout, i, k + p, fmaf(c * dt[p], acc[p], v0[p + 2]), Vbc);
+    }
+    pdl_done();
+}
+
+// the five fields G of k_sweep_g32 at the interior points, rounded to FP32
+__global__ void k_level_g32(Lay L, Range2 r, const double* __restrict__ V, const double* __restrict__ vx,
+                            const double* __restrict__ vz, const double* __restrict__ vxx,
+                            const double* __restrict__ vzz, const double* __restrict__ vxz, float* __restrict__ g) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const size_t x = IX(L, i, k), pl = L.plane;
+    g[x] = (float)(vxx[x] - vzz[x]);
+    g[x + pl] = (float)V[x];
+    g[x + 2 * pl] = (float)vxz[x];
+    g[x + 3 * pl] = (float)vx[x];
+    g[x + 4 * pl] = (float)vz[x];
+}
+
 __global__ void __launch_bounds__(256, 1) k_residual32(Lay L, Range2 r, const float* S, const float* __restrict__ coef,
                              const float* rhs, float* res) {
     RANGE_IK(r);
@@ -171,11 +274,39 @@ void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb) {
     }
 }
 
+// Weights of k_sweep_g32 from the level's FP64 fold basis: g = (G0, G1, 2 G1,
+// 4 G2, 2 G3, 2 G4) in k_level_coefs, so w = (f0, f1 + 2 f2, 4 f3, 2 f4, 2 f5)
+// (formed in FP64, then rounded).  False when an entry outside the mask is
+// not exactly zero.
+bool fold_g32_weights(const LevConst& c, FoldG32* out) {
+    const unsigned mask[TC_NCOEF] = TC_FOLD_G32_MASK;
+    for (int d = 0; d < TC_NCOEF; d++) {
+        const double* f = c.fold[d];
+        const double w[5] = {f[0], f[1] + 2.0 * f[2], 4.0 * f[3], 2.0 * f[4], 2.0 * f[5]};
+        for (int j = 0; j < 5; j++) {
+            if (!((mask[d] >> j) & 1u) && w[j] != 0.0) return false;
+            out->w[d][j] = (float)w[j];
+        }
+    }
+    return true;
+}
+
+void launch_level_g32(cudaStream_t s, const Level& lv, const double* vis) {
+    const Range2 r = interior(lv.L);
+    k_level_g32<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz, lv.g32);
+    tc_note_launch();
+}
+
 static constexpr bool kSweep32Pairs = true;  // k_sweep_x2 (two points per thread) for the per-sweep FP32 smoother
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc) {
     const Range2 r = interior(lv.L);
-    if (kSweep32Pairs) {
+    if (lv.g32 != nullptr && lv.use_g32) {
+        dim3 g = grid_for_shape(r, lv.sweep_bx, 2 * lv.sweep_by);
+        launch_pdl(k_sweep_g32, g, dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, lv.gw, Sin, Sout,
+                   (const float*)lv.g32, (const float*)lv.rhs32, (const float*)lv.dts32, (const float*)lv.cA32,
+                   (const float*)lv.cB32, c_uniform, per_point, temp, Vbc);
+    } else if (kSweep32Pairs) {
         dim3 g = grid_for_shape(r, lv.sweep_bx, 2 * lv.sweep_by);
         launch_pdl(k_sweep_x2<float>, g, dim3(lv.sweep_bx, lv.sweep_by), 0, s, lv.L, r, Sin, Sout, lv.coef32, lv.rhs32,
                    lv.dts32, lv.cA32, lv.cB32, c_uniform, per_point, temp, Vbc);

@@ -14,10 +14,11 @@
 // rheology), this is a fixed linear map e_S = M_k r_S of the restricted
 // residual r_S: the sweeps, the residual, the transfers and the direct solve
 // are all linear.  M_k (n_S x n_S, n_S the interior unknowns of S) is built
-// in FP64 once per multigrid call by running the sub-cycle on the n_S unit
-// vectors, one CTA per column, with the same per-point arithmetic as the
-// FP64 smoother kernels (k_sweep, k_residual, restrict9, k_coarse_apply,
-// k_prolong) in shared memory; each descent then costs one matrix-vector
+// once per multigrid call by running the sub-cycle on the n_S unit vectors,
+// one CTA per column, with the per-point arithmetic of the solver's smoother
+// kernels (k_sweep, k_residual, restrict9, k_coarse_apply, k_prolong; FP64,
+// or in the mixed solve FP32 from its FP32 operator with the coarsest solve
+// in FP64) in shared memory; each descent then costs one matrix-vector
 // product instead of (2k+1) x Nmulti latency-bound sweeps and k coarse
 // solves.  In exact arithmetic the cycle is unchanged; only the
 // summation order of the bottom correction differs.  This is the same step
@@ -188,24 +189,46 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
 
 // e_S = M r_S: one warp per interior unknown p of level S (lane-strided sum
 // in FP64, shuffle tree), written with the stream BCs' ghost copies.  The
-// matrix is FP64 in both solvers: the product cancels strongly (the sum of
-// the terms' magnitudes is far above the result), so FP32 entries would
-// perturb the correction by far more than the FP32 sweeps they replace
-// (measured: 4e-4 of the level-1 correction after one W-cycle, against
-// 5e-13 with FP64 entries).  The mixed solve's FP32 RHS and correction are
-// converted at the load and the store.
-template <typename TV>
-__global__ void __launch_bounds__(256) k_subcycle_apply(Lay L, const double* __restrict__ M, const TV* rhs, TV* err,
+// product cancels strongly (the sum of the terms' magnitudes is far above
+// the result), so it is summed in FP64 whatever the entries' type: FP64
+// entries in the FP64 solve (the level-1 correction after one W-cycle within
+// 5e-13 of the sweep path's), FP32 entries built from the FP32 operator in
+// the mixed solve (after one W-cycle 3.7e-5 from the FP64 cycle's, where the
+// FP32 sweeps give 1.9e-4).  The mixed
+// solve's FP32 RHS and correction are converted at the load and the store.
+//
+// The matrix is fixed for the solve, so each warp loads its row into
+// registers before waiting for the previous kernel; the RHS is then staged
+// once per block in shared memory as FP64 (one conversion and one index
+// computation per entry and block, not per entry and row).
+template <typename TM, typename TV>
+__global__ void __launch_bounds__(256) k_subcycle_apply(Lay L, const TM* __restrict__ M, const TV* rhs, TV* err,
                                                         int nS, int Vbc) {
-    pdl_entry();
+    constexpr int kPerLane = kThreads * kPPT / 32;  // nS <= kThreads * kPPT
+    __shared__ double r[kThreads * kPPT];
     const int lane = threadIdx.x & 31;
     const int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (p >= nS) return;
     const int a1 = L.a - 1;
-    const double* row = M + (size_t)p * nS;
+    TM m[kPerLane];
+    {
+        const TM* row = M + (size_t)(p < nS ? p : 0) * nS;
+#pragma unroll
+        for (int q = 0; q < kPerLane; q++) {
+            const int jj = lane + 32 * q;
+            m[q] = (p < nS && jj < nS) ? __ldg(row + jj) : TM(0);
+        }
+    }
+    pdl_entry();
+    for (int jj = threadIdx.x; jj < nS; jj += blockDim.x)
+        r[jj] = (double)ld_state(rhs + IX(L, 1 + jj % a1, 1 + jj / a1));
+    __syncthreads();
+    if (p >= nS) return;
     double acc = 0.0;
-    for (int jj = lane; jj < nS; jj += 32)
-        acc = fma(__ldg(row + jj), (double)ld_state(rhs + IX(L, 1 + jj % a1, 1 + jj / a1)), acc);
+#pragma unroll
+    for (int q = 0; q < kPerLane; q++) {
+        const int jj = lane + 32 * q;
+        if (jj < nS) acc = fma((double)m[q], r[jj], acc);
+    }
     for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
     if (lane == 0) store_stream<TV>(L, err, 1 + p % a1, 1 + p / a1, (TV)acc, Vbc);
     pdl_done();
@@ -235,30 +258,50 @@ int subcycle_fits(const Lay& LS, const Lay& LG) {
     return (nS <= kThreads * kPPT && build_smem<double>(LS, LG) <= 200 * 1024) ? 1 : 0;
 }
 
-// The matrices are built in FP64 from the level's FP64 operator in both
-// solvers (in the mixed solve the FP32 smoother's coefficients are roundings
-// of the same FP64 ones).
-int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, const double* ctab,
-                          int nsweeps, int per_point_down, const double* Ainv, const double* rowb, const int* cq,
-                          const int* cx, int n, int m, int Vbc, int kmax, double* const* M) {
+// fp32 = 0: the matrices in FP64 from the level's FP64 operator (tab, ctab
+// and M FP64).  fp32 = 1 (the mixed solve): in FP32 from its FP32 operator,
+// the arithmetic of its FP32 smoother (tab, ctab and M FP32; the coarsest
+// solve FP64 as in k_coarse_apply32).
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, int fp32, const void* tab,
+                          const void* ctab, int nsweeps, int per_point_down, const double* Ainv, const double* rowb,
+                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M) {
     if (per_point_down && ctab == nullptr) return -1;
     if (kmax < 1 || kmax > 4) return -1;
+    if (fp32) {
+        SubArgs<float> A{};
+        A.LS = S.L; A.LG = G.L;
+        A.coef = S.coef32; A.dts = S.dts32; A.cA = S.cA32; A.cB = S.cB32;
+        A.tab = (const float*)tab; A.ctab = (const float*)ctab; A.nsweeps = nsweeps;
+        A.per_point_down = per_point_down;
+        A.Ainv = Ainv; A.rowb = rowb; A.cq = cq; A.cx = cx; A.n = n; A.m = m;
+        A.Vbc = Vbc; A.kmax = kmax; A.nS = (S.L.a - 1) * (S.L.b - 1);
+        for (int k = 0; k < 4; k++) A.M[k] = (float*)M[k];
+        return launch_build(s, A);
+    }
     SubArgs<double> A{};
     A.LS = S.L; A.LG = G.L;
     A.coef = S.coef; A.dts = S.dt_stream; A.cA = S.cA; A.cB = S.cB;
-    A.tab = tab; A.ctab = ctab; A.nsweeps = nsweeps; A.per_point_down = per_point_down;
+    A.tab = (const double*)tab; A.ctab = (const double*)ctab; A.nsweeps = nsweeps;
+    A.per_point_down = per_point_down;
     A.Ainv = Ainv; A.rowb = rowb; A.cq = cq; A.cx = cx; A.n = n; A.m = m;
     A.Vbc = Vbc; A.kmax = kmax; A.nS = (S.L.a - 1) * (S.L.b - 1);
-    for (int k = 0; k < 4; k++) A.M[k] = M[k];
+    for (int k = 0; k < 4; k++) A.M[k] = (double*)M[k];
     return launch_build(s, A);
 }
 
-void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc) {
+// e_S = M r_S in the solver's precision (fp32: FP32 RHS and correction);
+// m32: the matrix is FP32; the products are summed in FP64 either way
+void launch_subcycle_apply(cudaStream_t s, const Level& S, const void* M, int fp32, int m32, void* err, int Vbc) {
     const int nS = (S.L.a - 1) * (S.L.b - 1);
     const unsigned nb = (unsigned)((nS * 32 + 255) / 256);
-    if (fp32)
-        launch_pdl(k_subcycle_apply<float>, nb, 256, 0, s, S.L, M, (const float*)S.rhs32, (float*)err, nS, Vbc);
+    if (fp32 && m32)
+        launch_pdl(k_subcycle_apply<float, float>, nb, 256, 0, s, S.L, (const float*)M, (const float*)S.rhs32,
+                   (float*)err, nS, Vbc);
+    else if (fp32)
+        launch_pdl(k_subcycle_apply<double, float>, nb, 256, 0, s, S.L, (const double*)M, (const float*)S.rhs32,
+                   (float*)err, nS, Vbc);
     else
-        launch_pdl(k_subcycle_apply<double>, nb, 256, 0, s, S.L, M, (const double*)S.rhs, (double*)err, nS, Vbc);
+        launch_pdl(k_subcycle_apply<double, double>, nb, 256, 0, s, S.L, (const double*)M, (const double*)S.rhs,
+                   (double*)err, nS, Vbc);
     tc_note_launch();
 }

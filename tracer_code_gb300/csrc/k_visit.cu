@@ -644,6 +644,10 @@ static void cheb_table_t(cudaStream_t s, const Lay& L, const double* tvals, int 
 void launch_cheb_table(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, double* tab) {
     cheb_table_t<double>(s, lv.L, tvals, nsweeps, lv.cA, lv.cB, tab);
 }
+// the FP32 smoother's per-point factors 2/(cA + cB*temp) in FP32 (temps rounded to float)
+void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab) {
+    cheb_table_t<float>(s, lv.L, tvals, nsweeps, lv.cA32, lv.cB32, tab);
+}
 
 template <typename T, int P, int NT>
 static cudaError_t visit_launch(const VisitShape& sh, cudaStream_t s, const VisitParams<T>& Q, T* S, const T* coef,

@@ -160,6 +160,7 @@ struct Handle {
     // its last step; subM[k-1] = M_k (FP32 in the mixed solve); sub_tab =
     // the c and temp tables of a downward and an upward visit
     bool sub_on = false, sub_valid = false;
+    bool sub_m32 = false;  // the matrices are built and held in FP32 (mixed solve)
     int sub_kmax = 0;
     std::vector<int> sub_k, sub_end;
     double* subM[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -168,6 +169,7 @@ struct Handle {
     // corrections of psi (k_accel.cu): psi after the previous correction,
     // the network's predicted change of the current solve
     double *acc_prev = nullptr, *acc_dnn = nullptr;
+    double *win_p = nullptr, *win_ap = nullptr;  // windowed correction: TC_WIN changes and their images
     bool acc_dnn_on = false;  // the current solve has a network direction
 };
 
@@ -579,6 +581,11 @@ static StepFusion step_fusion(Handle* h, int pp) {
 // reads is taken after the correction.
 void enqueue_cycle_correction(Handle* h) {
     if (h->p.cycle_correction == 0 || h->acc_prev == nullptr) return;
+    if (h->p.cycle_correction >= 3) {
+        launch_accel_window(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->win_p, h->win_ap, h->acc_dnn,
+                            (h->p.cycle_correction == 4 && h->acc_dnn_on) ? 1 : 0, h->rs, h->ds, h->p.Vbc);
+        return;
+    }
     const int k2 = (h->p.cycle_correction == 2 && h->acc_dnn_on) ? TC_ACCEL_DNN : TC_ACCEL_NONE;
     launch_accel(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->acc_dnn, TC_ACCEL_DK, k2, 1, h->rs, h->ds,
                  h->p.Vbc);
@@ -600,7 +607,7 @@ void enqueue_cycle_rest(Handle* h) {
         // matrix, then continue with the step that leaves level grids-1
         const int sub = h->sub_on ? h->sub_k[pp] : 0;
         if (sub) {
-            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 0, cur_err(h, level), h->p.Vbc);
+            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 0, 0, cur_err(h, level), h->p.Vbc);
             pp = h->sub_end[pp];
         }
         const StepFusion f = step_fusion(h, pp);
@@ -660,8 +667,10 @@ void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, i
     int flips = 0;
     for (int n = 1; n <= Niter;) {
         // lv.blk sweeps per launch of the tiled smoother while that many
-        // remain, then single sweeps of it (lv.blk = 0: k_sweep32)
-        const int ns = (lv.blk >= 1 && n + lv.blk - 1 <= Niter) ? lv.blk : (lv.blk >= 1 ? 1 : 0);
+        // remain, then single sweeps of it (lv.blk = 0: k_sweep32; a level
+        // swept from its viscosity fields, g32, is always swept that way)
+        const int blk = (lv.g32 && lv.use_g32) ? 0 : lv.blk;
+        const int ns = (blk >= 1 && n + blk - 1 <= Niter) ? blk : (blk >= 1 ? 1 : 0);
         float cs[6], ts[6];
         for (int j = 0; j < (ns > 0 ? ns : 1); j++) {
             double c, temp;
@@ -717,7 +726,8 @@ void enqueue_rest_mixed(Handle* h, int) {
                               zero);
         const int sub = h->sub_on ? h->sub_k[pp] : 0;
         if (sub) {
-            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 1, cur_e32(h, level), h->p.Vbc);
+            launch_subcycle_apply(h->st, h->lev[level], h->subM[sub - 1], 1, h->sub_m32 ? 1 : 0, cur_e32(h, level),
+                                  h->p.Vbc);
             pp = h->sub_end[pp];
         }
         const StepFusion f = step_fusion(h, pp);
@@ -888,6 +898,7 @@ tc_status multigrid(Handle* h) {
                                l == h->ratio_level ? 1 : 0);
         if (mixed) {
             for (int l = 1; l < G; l++) launch_level_to_f32(h->st, h->lev[l], l == h->ratio_level ? 1 : 0);
+            if (h->lev[1].g32) launch_level_g32(h->st, h->lev[1], cur_vis(h, 1));
         }
         h->ctab_level = 0;
         if (!mixed && h->ctab && h->ratio_level > 1 && h->p.Nmulti <= 128 &&
@@ -924,11 +935,18 @@ tc_status multigrid(Handle* h) {
             for (int n = 1; n <= Nm; n++)
                 sweep_factors(Nm, n, dir, cheb_pp, &tv[(size_t)(2 * dir) * Nm + n - 1],
                               &tv[(size_t)(2 * dir + 1) * Nm + n - 1]);
-        CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
-        if (cheb_pp) launch_cheb_table(h->st, h->lev[S], tv.data() + Nm, Nm, h->sub_ctab);
-        if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_tab, h->sub_ctab, Nm, cheb_pp ? 1 : 0,
+        if (h->sub_m32) {
+            std::vector<float> tf(tv.begin(), tv.end());
+            CK(cudaMemcpyAsync(h->sub_tab, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, h->st));
+            if (cheb_pp) launch_cheb_table32(h->st, h->lev[S], tv.data() + Nm, Nm, (float*)h->sub_ctab);
+        } else {
+            CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
+            if (cheb_pp) launch_cheb_table(h->st, h->lev[S], tv.data() + Nm, Nm, h->sub_ctab);
+        }
+        if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_m32 ? 1 : 0, h->sub_tab, h->sub_ctab, Nm,
+                                  cheb_pp ? 1 : 0,
                                   h->ainv, h->rowb, h->coarse_q, h->coarse_x, h->ngrid_coarse, h->coarse_m,
-                                  h->p.Vbc, h->sub_kmax, h->subM) != 0) {
+                                  h->p.Vbc, h->sub_kmax, (void* const*)h->subM) != 0) {
             h->err = "k_subcycle_build: launch failed";
             return TC_ERR_CUDA;
         }
@@ -968,7 +986,7 @@ tc_status multigrid(Handle* h) {
     // (learned_guess = 3: the start SF + alpha d, alpha residual-minimising;
     // cycle_correction = 2: d spans the correction with each cycle's own)
     h->acc_dnn_on = h->net != nullptr && !nonN && h->acc_dnn != nullptr &&
-                    (h->p.learned_guess == 3 || h->p.cycle_correction == 2);
+                    (h->p.learned_guess == 3 || h->p.cycle_correction == 2 || h->p.cycle_correction == 4);
     if (h->acc_dnn_on) {
         if (nn_guess(h->net, h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
                      h->p.Vbc, h->p.learned_smooth) != 0) {
@@ -993,7 +1011,10 @@ tc_status multigrid(Handle* h) {
             if (h->hs->acc_alpha[0] != 0.0) h->guess_used++;
         }
     }
-    if (h->p.cycle_correction != 0 && h->acc_prev != nullptr && !nonN) copy_plane(h, h->acc_prev, cur_err(h, 1));
+    if (h->p.cycle_correction != 0 && h->acc_prev != nullptr && !nonN) {
+        copy_plane(h, h->acc_prev, cur_err(h, 1));
+        CK(cudaMemsetAsync(&h->ds->win_n, 0, sizeof(int), h->st));  // a new window per solve
+    }
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     if (try_guess) {
         int f = 0;
@@ -1327,7 +1348,7 @@ tc_status create(Handle* h, const tc_params* in) {
     if (p.Nmulti < 1 || p.max_cycles < 1 || p.nx < 8 || p.nz < 8 || p.aspect <= 0.0) return TC_ERR_ARG;
     if (p.solver_precision != 0 && p.solver_precision != 1) return TC_ERR_ARG;
     if (p.learned_guess < 0 || p.learned_guess > 3 || p.learned_smooth < 0 || p.learned_smooth > 64) return TC_ERR_ARG;
-    if (p.cycle_correction < 0 || p.cycle_correction > 2) return TC_ERR_ARG;
+    if (p.cycle_correction < 0 || p.cycle_correction > 4) return TC_ERR_ARG;
     if (p.non_Newtonian == 1 && p.cycle_correction != 0) {
         h->err = "the cycle correction runs on Newtonian solves";
         return TC_ERR_UNSUPPORTED;
@@ -1526,6 +1547,7 @@ tc_status create(Handle* h, const tc_params* in) {
         lv.coef32 = lv.dts32 = lv.cA32 = lv.cB32 = lv.rhs32 = lv.res32 = nullptr;
         lv.e32[0] = lv.e32[1] = nullptr;
         lv.e32cur = 0;
+        lv.g32 = nullptr;
         if (p.solver_precision == 1) {
             TRY(dalloc_t(h, &lv.coef32, lp * TC_NCOEF));
             float** f32[] = {&lv.dts32, &lv.cA32, &lv.cB32, &lv.rhs32, &lv.res32, &lv.e32[0], &lv.e32[1]};
@@ -1536,6 +1558,11 @@ tc_status create(Handle* h, const tc_params* in) {
         LevConst& c = lv.c;
         c.dr = s.dr; c.ds = s.ds; c.dr2 = s.dr2; c.ds2 = s.ds2; c.dr3 = s.dr3; c.ds3 = s.ds3; c.dr4 = s.dr4;
         c.ds4 = s.ds4; c.drds = s.drds; c.drds2 = s.drds2; c.dr2ds = s.dr2ds; c.dr2ds2 = s.dr2ds2;
+        {
+            auto pow2 = [](double v) { int e; return v > 0.0 && std::frexp(v, &e) == 0.5; };
+            c.recip = (pow2(c.dr) && pow2(c.ds) && pow2(c.dr2) && pow2(c.ds2) && pow2(c.drds)) ? 1 : 0;
+            c.rdr = 1.0 / c.dr; c.rds = 1.0 / c.ds; c.rdr2 = 1.0 / c.dr2; c.rds2 = 1.0 / c.ds2; c.rdrds = 1.0 / c.drds;
+        }
         // scaled bounds (test_eigenvalues / iterate_local_time_steps preamble)
         const double Ts = h->eb.Tr / s.ds, Tss = -h->eb.Trr / s.ds2, Tsss = h->eb.Trrr / s.ds3,
                      Tssss = h->eb.Trrrr / s.ds4, Trr = -h->eb.Trr / s.dr2, Trrr = h->eb.Trrr / s.dr3,
@@ -1560,6 +1587,13 @@ tc_status create(Handle* h, const tc_params* in) {
             c.fold[d][3] = Srs;
             c.fold[d][4] = Srrr + Srss;
             c.fold[d][5] = Ssss + Srrs;
+        }
+        // level 1 of the mixed solve sweeps from the five viscosity fields
+        // (k_sweep_g32) when the stencil's structural zeros hold
+        lv.use_g32 = 0;
+        if (p.solver_precision == 1 && l == 1 && fold_g32_weights(c, &lv.gw)) {
+            TRY(dalloc_t(h, &lv.g32, lp * 5));
+            lv.use_g32 = 1;
         }
         // stability_vis_smoother (uniform: eI = 0)
         {
@@ -1605,12 +1639,17 @@ tc_status create(Handle* h, const tc_params* in) {
                 if (need[k]) TRY(dalloc_t(h, &h->subM[k - 1], nS * nS));
             TRY(dalloc_t(h, &h->sub_tab, 4 * (size_t)p.Nmulti));
             TRY(dalloc_t(h, &h->sub_ctab, (size_t)p.Nmulti * nS));
+            h->sub_m32 = (p.solver_precision == 1);
             h->sub_on = true;
         }
     }
     // corrections after the level-1 visit: psi at the previous one, the network's direction
     if (p.cycle_correction != 0 || p.learned_guess == 3) {
         if (p.cycle_correction != 0) TRY(dalloc_t(h, &h->acc_prev, pl));
+        if (p.cycle_correction >= 3) {
+            TRY(dalloc_t(h, &h->win_p, pl * TC_WIN));
+            TRY(dalloc_t(h, &h->win_ap, pl * TC_WIN));
+        }
         TRY(dalloc_t(h, &h->acc_dnn, pl));
     }
     // stability_RK4_smoother: dts_array
@@ -2025,7 +2064,7 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         lv.visit_cfg = 0;
         double best_v = 1e30;
         int best_blk = 0;
-        for (int blk = 0; blk <= (mixed ? 6 : 2); blk++) {
+        for (int blk = 0; blk <= (mixed ? ((lv.g32 && lv.use_g32) ? 0 : 6) : 2); blk++) {
             lv.blk = blk;
             double ms = 0;
             TRY(time_visits(&ms));
@@ -2239,7 +2278,9 @@ tc_status tc_time_subcycle(tc_handle* H, int32_t k, int32_t reps, double* ms_per
     const int S = h->grids - 1;
     const bool mixed = (h->p.solver_precision == 1);
     void* err = mixed ? (void*)cur_e32(h, S) : (void*)cur_err(h, S);
-    auto apply = [&]() { launch_subcycle_apply(h->st, h->lev[S], h->subM[k - 1], mixed ? 1 : 0, err, h->p.Vbc); };
+    auto apply = [&]() {
+        launch_subcycle_apply(h->st, h->lev[S], h->subM[k - 1], mixed ? 1 : 0, h->sub_m32 ? 1 : 0, err, h->p.Vbc);
+    };
     apply();
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
@@ -2261,6 +2302,19 @@ tc_status tc_debug_wait_test(tc_handle* H, int32_t on) {
     Handle* h = &H->h;
     h->wait_test = (on != 0);
     // the cycle graphs bake in the visits' parameters: capture again
+    CycleGraphs& cg = *h->graphs;
+    if (cg.l1) cudaGraphExecDestroy(cg.l1);
+    if (cg.rest) cudaGraphExecDestroy(cg.rest);
+    if (cg.loop) cudaGraphExecDestroy(cg.loop);
+    cg.l1 = cg.rest = cg.loop = nullptr;
+    return TC_OK;
+}
+
+tc_status tc_debug_sweep_fields(tc_handle* H, int32_t fields) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    if (h->lev[1].g32 == nullptr) return TC_ERR_UNSUPPORTED;
+    h->lev[1].use_g32 = fields ? 1 : 0;
     CycleGraphs& cg = *h->graphs;
     if (cg.l1) cudaGraphExecDestroy(cg.l1);
     if (cg.rest) cudaGraphExecDestroy(cg.rest);

@@ -21,6 +21,7 @@
 #define TC_MAXLEV 6
 #define TC_NCOEF 13
 #define TC_MAX_RED_BLOCKS 8192
+#define TC_WIN 4  // W-cycle changes kept by the windowed correction
 
 // 13-point stencil offsets used by the folded operator, in this order.
 #define TC_OFFSETS_DI {0, -1, 1, -2, 2, 0, 0, 0, 0, -1, 1, -1, 1}
@@ -47,6 +48,11 @@ struct LevConst {
     // folded-operator basis: for each offset d, (Srr-Sss, Srrrr+Sssss, Srrss, Srs, Srrr+Srss, Ssss+Srrs)
     double fold[TC_NCOEF][6];
     double dtvis_scale;  // unused placeholder
+    // reciprocals of dr, ds, dr2, ds2, drds; recip = 1 when all five spacings
+    // are powers of two, so that x * (1/h) equals x / h exactly and the
+    // viscosity-filter kernels multiply instead of dividing
+    double rdr, rds, rdr2, rds2, rdrds;
+    int recip;
 };
 
 // Scalars that kernels produce and the host reads back.
@@ -70,6 +76,11 @@ struct DevScalars {
     int    cyc_status;       // its stop reason: 0 converged, else the tc_status
     int    never_set;        // stays 0: the word the timeout-path tests wait on
     int    pad2;
+    // windowed correction (cycle_correction 3/4, k_accel.cu): coefficients of
+    // the last correction (newest change first, the network's direction
+    // last), stored changes, slot of the newest, directions used
+    double win_beta[TC_WIN + 1];
+    int    win_n, win_head, win_nd, win_pad;
 };
 
 // Reduction scratch: per-block partials plus a completion counter.
@@ -77,6 +88,16 @@ struct RedScratch {
     double* part;         // [4][TC_MAX_RED_BLOCKS]
     unsigned int* count;  // [8]
 };
+
+// FP32 fold weights: coefficient d = sum_j w[d][j] G_j over the fields
+// G = (eta_xx - eta_zz, eta, eta_xz, eta_x, eta_z); the entries outside
+// kFoldG32Mask are zero for every uniform-grid stencil (checked on the host)
+struct FoldG32 {
+    float w[TC_NCOEF][5];
+};
+// tap d of the folded operator (centre, x offsets -1 1 -2 2, z offsets, the
+// four diagonals) uses field j where bit j of the mask is set
+#define TC_FOLD_G32_MASK {0x03u, 0x0bu, 0x0bu, 0x0bu, 0x0bu, 0x13u, 0x13u, 0x13u, 0x13u, 0x1eu, 0x1eu, 0x1eu, 0x1eu}
 
 struct Level {
     Lay L;
@@ -96,6 +117,13 @@ struct Level {
     float *coef32, *dts32, *cA32, *cB32, *rhs32, *res32;
     float* e32[2];
     int e32cur;
+    // level 1 of the mixed solve: the five viscosity fields the folded
+    // coefficients are made of (eta_xx - eta_zz, eta, eta_xz, eta_x, eta_z) in
+    // FP32, and the fold weights that turn them into the 13 coefficients
+    // inside the sweep (null: the sweep reads coef32)
+    float* g32;
+    FoldG32 gw;
+    int use_g32;  // 1: the level's per-sweep FP32 smoother reads g32
     // launch configuration of this level's smoother, set by tc_autotune
     // (defaults: 32x8 blocks; fused visits wherever they fit)
     int sweep_bx, sweep_by;
@@ -181,10 +209,11 @@ int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const doub
 // apply reads the level's RHS and writes its correction in the solver's
 // precision (fp32: rhs32 / e32).
 int subcycle_fits(const Lay& LS, const Lay& LG);
-int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, const double* tab, const double* ctab,
-                          int nsweeps, int per_point_down, const double* Ainv, const double* rowb, const int* cq,
-                          const int* cx, int n, int m, int Vbc, int kmax, double* const* M);
-void launch_subcycle_apply(cudaStream_t s, const Level& S, const double* M, int fp32, void* err, int Vbc);
+int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, int fp32, const void* tab,
+                          const void* ctab, int nsweeps, int per_point_down, const double* Ainv, const double* rowb,
+                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M);
+void launch_subcycle_apply(cudaStream_t s, const Level& S, const void* M, int fp32, int m32, void* err, int Vbc);
+void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab);
 
 // (k_accel.cu) residual-minimising correction of the level-1 streamfunction along up to
 // two directions: TC_ACCEL_DK = psi - prev (the last W-cycle's correction),
@@ -194,6 +223,13 @@ enum { TC_ACCEL_NONE = 0, TC_ACCEL_DK = 1, TC_ACCEL_DNN = 2 };
 void launch_accel(cudaStream_t s, const Level& l1, double* psi, double* prev, const double* dnn, int k1, int k2,
                   int record_prev, RedScratch rs, DevScalars* ds, int Vbc);
 void launch_plane_diff(cudaStream_t s, double* dst, const double* a, const double* b, size_t n);
+// windowed correction: the change d = psi - prev of the last W-cycle joins
+// a window of the last TC_WIN changes (P, their images A d in AP; slots in
+// ring order, ds->win_n / win_head), and psi moves to the minimiser of the
+// L1-weighted residual over psi + span{window, dnn (when use_dnn)}; prev =
+// the corrected psi.  ds->win_n = 0 starts a new window.
+void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* prev, double* P, double* AP,
+                         const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds, int Vbc);
 
 // (k_loop.cu) the multigrid convergence loop on the device: the cycle counter
 // and the reference's tests after each level-1 visit, setting the condition
@@ -204,6 +240,8 @@ void launch_cycle_check(cudaStream_t s, DevScalars* ds, double tolerance, int ma
 
 // (k_mixed.cu) FP32 multigrid of the mixed-precision solve and its FP64 bridges
 void launch_level_to_f32(cudaStream_t s, const Level& lv, int cheb);
+void launch_level_g32(cudaStream_t s, const Level& lv, const double* vis);
+bool fold_g32_weights(const LevConst& c, FoldG32* out);
 void launch_sweep32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, float c_uniform, int per_point,
                     float temp, int Vbc);
 void launch_residual32(cudaStream_t s, const Level& lv, const float* S);
