@@ -70,11 +70,14 @@ SOLVER_DESC = {
              "coarse solve), same 1e-8 test",
     "learned": "learned + mixed: the mixed-precision multigrid with the encoder-decoder (BF16 tcgen05 network "
                "trained at 512x128) supplying its predicted change of each solve as (a) the start, scaled to the "
-               "residual-minimising multiple (learned_guess=3), and (b) one of two directions of a correction after "
-               "every level-1 visit, the other being psi's change over the last W-cycle, with coefficients "
-               "minimising the L1-weighted residual (cycle_correction=2); same 1e-8 test",
-    "corr": "mixed + cycle correction without the network: the same correction after every level-1 visit along "
-            "psi's change over the last W-cycle only (cycle_correction=1); same 1e-8 test",
+               "residual-minimising multiple (learned_guess=3), and (b) a direction of the correction after every "
+               "level-1 visit, whose other directions are psi's changes over the last four W-cycles (a windowed "
+               "Krylov acceleration of the W-cycle), with coefficients minimising the L1-weighted residual "
+               "(cycle_correction=4); same 1e-8 test",
+    "corr": "mixed + windowed correction without the network: the same correction after every level-1 visit "
+            "over psi's changes of the last four W-cycles only (cycle_correction=3); same 1e-8 test",
+    "corr1": "mixed + one-direction correction: the correction after every level-1 visit along psi's change "
+             "over the last W-cycle only (cycle_correction=1); same 1e-8 test",
 }
 GUESS_WEIGHTS = os.path.join(ROOT, "tracer_code_gb300", "weights", "guess_512x128.npy")
 
@@ -382,8 +385,9 @@ def dominant_roofline(sim, p, prof: dict, fp32: bool) -> dict:
 def step_roofline(p, prof: dict, cycles_per_step: float, ms_per_step: float, fp32: bool) -> dict:
     """Whole-timestep algorithmic bytes (model of the per-unit figures above)
     over the measured step time: smoother sweeps, residuals (72 B/pt), the
-    FP64 level-1 bridges of the mixed solve, tracer RK stages (64 B/tracer)
-    and tracer-ratio passes (20 B/tracer + 20 B/volume)."""
+    FP64 level-1 bridges of the mixed solve, the correction after each
+    level-1 visit, tracer RK stages (64 B/tracer) and tracer-ratio passes
+    (20 B/tracer + 20 B/volume)."""
     peak, _ = peaks()
     bsweep = 44.0 if fp32 else 88.0
     per_cycle = 0.0
@@ -394,6 +398,15 @@ def step_roofline(p, prof: dict, cycles_per_step: float, ms_per_step: float, fp3
             per_cycle += r["visits_per_cycle"] * (p.Nmulti * bsweep + (36.0 if fp32 else 72.0)) * r["points"]
     if fp32:
         per_cycle += (72.0 + 24.0 + 72.0) * level_points(p, 1)  # residual_to32, update64, FP64 residual
+    cc = int(getattr(p, "cycle_correction", 0))
+    if cc >= 3:
+        # windowed correction: 13 FP64 coefficients, psi, prev, RHS, three
+        # stored images and the network direction read, the new change and
+        # its image written; then four changes, the direction and psi read,
+        # psi and prev written
+        per_cycle += (104.0 + 24.0 + 24.0 + 16.0 + 48.0 + 16.0) * level_points(p, 1)
+    elif cc >= 1:
+        per_cycle += (104.0 + 32.0 + 40.0) * level_points(p, 1)
     ntr = (p.nx + 1) * (p.nz + 1) * p.tpc
     vols = (p.nx + 1) * (p.nz + 1)
     tracer = 4 * 64.0 * ntr + 4 * (20.0 * ntr + 20.0 * vols)
@@ -512,7 +525,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     # learned coarse-level correction
     p = workload_params("mixed")
     p.learned_guess = 3
-    p.cycle_correction = 2
+    p.cycle_correction = 4
     st = state.initial_state(p, seed=1 + rank)
     sim = Simulation(p, stream=stream.cuda_stream)
     net = learned.Net(1, p.nz, p.nx, stream=stream.cuda_stream)
@@ -549,15 +562,24 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     e2e_value = replica_rate(k_e2e, time.perf_counter() - t0, world, max_over_ranks)
     sim.close()
     net.close()
-    # ablation: the same correction without the network's direction
+    # ablations: the same windowed correction without the network's
+    # direction, and the one-direction correction
     pc = workload_params("mixed")
-    pc.cycle_correction = 1
+    pc.cycle_correction = 3
     simc = Simulation(pc, stream=stream.cuda_stream)
     simc.upload(st)
     simc.autotune()
     msc, solvesc, _, _ = timed_steps(simc, stream, args.steps, args.warmup, barrier)
     corr_value = replica_rate(args.steps, msc * 1e-3, world, max_over_ranks)
     simc.close()
+    pc1 = workload_params("mixed")
+    pc1.cycle_correction = 1
+    simc1 = Simulation(pc1, stream=stream.cuda_stream)
+    simc1.upload(st)
+    simc1.autotune()
+    msc1, solvesc1, _, _ = timed_steps(simc1, stream, args.steps, args.warmup, barrier)
+    corr1_value = replica_rate(args.steps, msc1 * 1e-3, world, max_over_ranks)
+    simc1.close()
     # the same mixed solver without the network and without the correction
     pm = workload_params("mixed")
     simm = Simulation(pm, stream=stream.cuda_stream)
@@ -593,6 +615,8 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                   "solves_started_from_guess": guess_used},
                    cycle_correction_without_network={"timesteps_per_s": corr_value, "ms_per_step": msc / args.steps,
                                                      "cycles_per_step": solvesc, "solver": SOLVER_DESC["corr"]},
+                   one_direction_correction={"timesteps_per_s": corr1_value, "ms_per_step": msc1 / args.steps,
+                                             "cycles_per_step": solvesc1, "solver": SOLVER_DESC["corr1"]},
                    mixed_without_guess={"timesteps_per_s": mixed_value, "ms_per_step": msm / args.steps,
                                         "cycles_per_step": solvesm,
                                         "solver": "the mixed-precision multigrid alone (no network, no correction)"},

@@ -13,14 +13,17 @@
     residual test keeps the plain start in practice);
   - the correction after every level-1 visit (cycle_correction 1: along
     psi's change over the last W-cycle; 2: also along the network's
-    predicted change, the learned coarse-level correction) and the
-    residual-minimising learned start (learned_guess 3) keep every solve at
-    the reference's tolerance, checked by the oracle's residual test, in
-    FP64 and mixed precision, with no more W-cycles than without them;
-  - on the 1024x256 workload the learned + mixed solver takes strictly
-    fewer W-cycles than the mixed solver alone; the counts of the ablation
-    without the network's direction are printed next to them (the share of
-    the gain that the network itself brings).
+    predicted change, the learned coarse-level correction; 3: over the
+    changes of the last four W-cycles; 4: those and the network's change)
+    and the residual-minimising learned start (learned_guess 3) keep every
+    solve at the reference's tolerance, checked by the oracle's residual
+    test, in FP64 and mixed precision, with no more W-cycles than without
+    them;
+  - on the 1024x256 workload the learned + mixed solver (windowed
+    correction with the network's direction) takes strictly fewer W-cycles
+    than the mixed solver alone and than the one-direction correction; the
+    counts of the ablation without the network's direction are printed next
+    to them (the share of the gain that the network itself brings).
 """
 import os
 
@@ -138,7 +141,7 @@ def _attach_trained(sim, p):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("cc,lg", [(1, 0), (2, 3)])
+@pytest.mark.parametrize("cc,lg", [(1, 0), (2, 3), (3, 0), (4, 3)])
 def test_cycle_correction_meets_tolerance(gpu_lib, prec, cc, lg):
     from oracle.pyoracle import Oracle
     from tests.cases import case_1024_like, fresh_state
@@ -150,7 +153,7 @@ def test_cycle_correction_meets_tolerance(gpu_lib, prec, cc, lg):
         q = p.copy()
         q.cycle_correction, q.learned_guess = (cc, lg) if use else (0, 0)
         sim = Simulation(q)
-        net = _attach_trained(sim, q) if use and cc == 2 else None
+        net = _attach_trained(sim, q) if use and cc in (2, 4) else None
         sim.upload(st)
         cyc[use] = sim.multigrid()
         sf = sim.download()["SF"]
@@ -177,11 +180,12 @@ def test_learned_correction_on_workload(gpu_lib):
     p.mg_zero_coarse, p.mg_coarse_matrix, p.solver_precision = 1, 1, 1
     st = state.initial_state(p, seed=1)
     runs = {}
-    for name, cc, lg in (("mixed", 0, 0), ("correction without network", 1, 0), ("learned + mixed", 2, 3)):
+    for name, cc, lg in (("mixed", 0, 0), ("one-direction correction", 1, 0),
+                         ("windowed correction without network", 3, 0), ("learned + mixed", 4, 3)):
         q = p.copy()
         q.cycle_correction, q.learned_guess = cc, lg
         sim = Simulation(q)
-        net = _attach_trained(sim, q) if cc == 2 else None
+        net = _attach_trained(sim, q) if cc in (2, 4) else None
         sim.upload(st)
         out = [sim.step() for _ in range(3)]
         runs[name] = ([c for _, c, _ in out], out[-1][0])
@@ -192,5 +196,6 @@ def test_learned_correction_on_workload(gpu_lib):
         print(f"1024x256 mixed, 3 steps, {name}: W-cycles {c} (total {sum(c)})")
     base, learned_run = runs["mixed"], runs["learned + mixed"]
     assert sum(learned_run[0]) < sum(base[0])
+    assert sum(learned_run[0]) < sum(runs["one-direction correction"][0])
     for key in ("Nu", "vrms", "Tavg"):
         assert abs(learned_run[1][key] - base[1][key]) <= 1e-6 * abs(base[1][key]), key
