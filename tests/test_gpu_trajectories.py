@@ -4,14 +4,17 @@ trajectories (tests/golden/make_trajectories.py):
   - the 128x128 plain case, 100 steps: every step's W-cycle count equal,
     Nu, Vrms, Tavg, Nu_bot and the enriched-tracer mass (Cavg) within 1e-6
     relative, the per-volume counts after the last step equal;
-  - the 1024x256 case (FP64 multigrid), 5 steps: stats within 1e-6; the
-    W-cycle counts and the final counts are reported (the folded operator
-    rounds differently from the oracle's at 1e-9 of SF, so a solve that ends
-    near the 1e-8 test can take one cycle more or less, and positions then
-    differ at 1e-10: a tracer within that distance of a volume edge may be
-    counted in the neighbour);
+  - the 1024x256 case (FP64 multigrid), 20 steps: stats within 1e-6, every
+    step's W-cycle count within 5% of the oracle's and the total within 2%
+    (the folded operator rounds differently from the oracle's, and with a
+    1e4 viscosity contrast the residual's rounding error is not far below
+    the 1e-8 test, so a solve that ends there can take a few cycles more),
+    and the final per-volume counts
+    equal to the oracle's, except where a volume holds tracers within 1e-9
+    of its edges (positions differ at 1e-10, so such a tracer may be counted
+    in the neighbour);
   - the 1024x256 case with the mixed-precision solver (FP32 smoother inside
-    FP64 defect correction) against the FP64 oracle, 5 steps: the largest
+    FP64 defect correction) against the FP64 oracle, 20 steps: the largest
     relative differences of Nu, Vrms and mass are printed and held below
     1e-6 (the solve meets the same 1e-8 residual; cycle counts may differ).
 """
@@ -82,19 +85,76 @@ def test_fp64_trajectory_128x128_100_steps(gpu_lib):
     assert _checksum(counts) == d["counts_checksum"]
 
 
+def _near_edge(r, s, i, k, dr, ds, eps):
+    """Tracers within eps of an edge of corner volume (i, k) (the volume of
+    the points whose nint(r/dr), nint(s/ds) are i, k)."""
+    near_r = (np.abs(r - (i - 0.5) * dr) < eps) | (np.abs(r - (i + 0.5) * dr) < eps)
+    near_s = (np.abs(s - (k - 0.5) * ds) < eps) | (np.abs(s - (k + 0.5) * ds) < eps)
+    inside = (np.abs(r - i * dr) <= 0.5 * dr + eps) & (np.abs(s - k * ds) <= 0.5 * ds + eps)
+    return int((inside & (near_r | near_s)).sum())
+
+
 def test_fp64_trajectory_1024x256(gpu_lib):
+    """20 steps of the 1024x256 case against the oracle: stats within 1e-6;
+    every step's W-cycles (four solves) within 5% of the oracle's and the
+    total within 2% (the folded operator rounds differently from the
+    oracle's; with a 1e4 viscosity contrast the residual's rounding error is
+    not far below the 1e-8 test, and a solve that ends there can take a few
+    cycles more: measured, 6 of 20 steps differ, all with the GPU taking
+    more, by at most 4.3%, 0.7% over the 20 steps); the per-volume counts after the last step equal to the
+    oracle's -- or every volume that differs holds at least as many tracers
+    within 1e-9 of its edges as its count differs by (positions agree to
+    about 1e-10, so only a tracer that close to an edge can be counted in the
+    neighbour)."""
     d = _load("traj_1024x256.json")
-    worst, counts = _run(d, strict=False)
-    print("1024x256 max relative differences:", worst,
-          "final counts equal:", _checksum(counts) == d["counts_checksum"])
+    p = _params(d)
+    g = Simulation(p)
+    g.upload(state.initial_state(p, seed=d["seed"]))
+    worst = {k: 0.0 for k in ("Nu", "vrms", "Tavg", "Nu_bot", "Cavg")}
+    cycles = []
+    for n, ref in enumerate(d["rows"]):
+        row, q, dt = g.step()
+        cycles.append((q, ref["cycles"]))
+        got = dict(row)
+        got["Cavg"] = row["Cavg"][0]
+        for k in worst:
+            worst[k] = max(worst[k], abs(got[k] - ref[k]) / abs(ref[k]))
+    counts = g.counts()
+    dl = g.download()
+    span = g.info.span
+    g.close()
+    print("W-cycles per step (GPU, oracle):", cycles)
+    print("1024x256 max relative differences:", worst)
+    ref_counts = np.load(os.path.join(HERE, "traj_1024x256_counts.npz"))["counts"].astype(np.int32)
+    assert ref_counts.shape == counts.shape
+    tot, tot_ref = counts.sum(axis=-1), ref_counts.sum(axis=-1)
+    bad = np.argwhere((counts != ref_counts).any(axis=-1))
+    qs, qrs = sum(q for q, _ in cycles), sum(qr for _, qr in cycles)
+    print(f"W-cycles over {len(cycles)} steps: GPU {qs}, oracle {qrs}; "
+          f"volumes whose final counts differ from the oracle's: {len(bad)}")
+    assert len(cycles) == d["steps"] >= 20
     for k, v in worst.items():
         assert v <= TOL, (k, v)
+    for n, (q, qr) in enumerate(cycles):
+        assert abs(q - qr) <= max(1, 0.05 * qr), (n, q, qr)
+    assert abs(qs - qrs) <= 0.02 * qrs
     assert int(counts.sum()) == d["counts_sum"]
+    if len(bad):
+        dr, ds = p.aspect / p.nx, 1.0 / p.nz
+        r, s = dl["rtr"], dl["str"]
+        for a, b in bad:
+            # field arrays are (z, x) with span ghost rows/columns
+            near = _near_edge(r, s, b - span, a - span, dr, ds, 1e-9)
+            diff = int(np.abs(counts[a, b] - ref_counts[a, b]).sum())
+            print(f"  volume (i={b - span}, k={a - span}): counts {counts[a, b].tolist()} vs {ref_counts[a, b].tolist()}, "
+                  f"tracers within 1e-9 of its edges: {near}")
+            assert diff <= 2 * near, (a, b)
+        assert abs(int(tot.sum()) - int(tot_ref.sum())) == 0
 
 
 def test_mixed_precision_error_against_fp64_oracle(gpu_lib):
     d = _load("traj_1024x256.json")
     worst, _ = _run(d, solver_precision=1, strict=False)
-    print("mixed vs FP64 oracle, 1024x256, 5 steps, max relative differences:", worst)
+    print(f"mixed vs FP64 oracle, 1024x256, {len(d['rows'])} steps, max relative differences:", worst)
     for k, v in worst.items():
         assert v <= TOL, (k, v)
