@@ -712,8 +712,9 @@ def main():
                     help="two timesteps of the reference's shipped configuration (for ncu)")
     ap.add_argument("--profile-solve", action="store_true",
                     help="profiling case: upload the workload, run one multigrid solve, exit")
-    ap.add_argument("--solver", default="plain", choices=["plain", "mixed"],
-                    help="solver of --profile-solve")
+    ap.add_argument("--solver", default="plain", choices=["plain", "mixed", "learned"],
+                    help="solver of --profile-solve / --profile-step (learned: the headline arm's, with the "
+                         "committed network)")
     ap.add_argument("--profile-net", action="store_true",
                     help="profiling case: one guess-network forward and backward on one 1024x256 image, exit")
     ap.add_argument("--ensemble", type=int, default=0, metavar="N",
@@ -743,7 +744,9 @@ def main():
     if args.profile_step:
         from tracer_code_gb300 import Simulation, state, scaled_config
         nx, nz = (int(v) for v in args.profile_step.lower().split("x"))
-        p = scaled_config(workload_params(args.solver), nx, nz)
+        p = scaled_config(workload_params("mixed" if args.solver == "learned" else args.solver), nx, nz)
+        if args.solver == "learned":
+            p.cycle_correction = 3  # the headline's correction (the network is trained for 1024x256 inputs)
         sim = Simulation(p)
         sim.upload(state.initial_state(p, seed=1))
         row, q, dt = sim.step()
@@ -764,15 +767,24 @@ def main():
         sim.close()
         return
     if args.profile_solve:
-        from tracer_code_gb300 import Simulation, state
-        p = workload_params(args.solver)
+        from tracer_code_gb300 import Simulation, state, learned
+        p = workload_params("mixed" if args.solver == "learned" else args.solver)
+        net = None
+        if args.solver == "learned":
+            p.learned_guess, p.cycle_correction = 3, 4
         sim = Simulation(p)
+        if args.solver == "learned":
+            net = learned.Net(1, p.nz, p.nx)
+            net.load(GUESS_WEIGHTS)
+            learned.attach(sim, net)
         sim.upload(state.initial_state(p, seed=1))
         n0 = Simulation.kernel_launches()
         q = sim.multigrid()
-        print(json.dumps({"profile_solve": True, "cycles": q, "launches_before_solve": n0,
+        print(json.dumps({"profile_solve": True, "solver": args.solver, "cycles": q, "launches_before_solve": n0,
                           "launches_in_solve": Simulation.kernel_launches() - n0}), flush=True)
         sim.close()
+        if net:
+            net.close()
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

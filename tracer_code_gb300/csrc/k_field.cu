@@ -114,9 +114,10 @@ void launch_smooth_T_step(cudaStream_t s, const Lay& L, const Phys& P, const dou
 
 // one step of smoother_time (smoother.f90:287-341) for one type
 __global__ void k_smooth_C(Lay L, Phys P, Range2 r, const double* __restrict__ Cin, double* __restrict__ Cout,
-                           const double* __restrict__ dts, double c) {
+                           const double* __restrict__ dts, double c, const double* cdev) {
     RANGE_IK(r);
     if (!inr) return;
+    if (cdev) c = *cdev;  // the factor the device-side filter loop chose
     size_t x = IX(L, i, k);
     double temp = lap5(Cin, x, (size_t)L.ld, P.dr2, P.ds2);
     double d = dts[x] * P.courantC;
@@ -126,9 +127,9 @@ __global__ void k_smooth_C(Lay L, Phys P, Range2 r, const double* __restrict__ C
     Cout[x] = v;
 }
 void launch_smooth_C_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Cin, double* Cout,
-                          const double* dts, double c) {
+                          const double* dts, double c, const double* cdev) {
     Range2 r{0, L.a, 0, L.b};
-    k_smooth_C<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Cin, Cout, dts, c); tc_note_launch();
+    k_smooth_C<<<grid_for(r), dim3(BX, BY), 0, s>>>(L, P, r, Cin, Cout, dts, c, cdev); tc_note_launch();
 }
 
 // load_conductivity_array (energy.f90:31-58)

@@ -128,9 +128,10 @@ void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_
 // one Chebyshev step of smoother_vis with viscosityBCs fused
 // ---------------------------------------------------------------------------
 __global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restrict__ Vin, double* __restrict__ Vout,
-                             const double* __restrict__ dtv, double c, int RaTnz, double visT2) {
+                             const double* __restrict__ dtv, double c, const double* cdev, int RaTnz, double visT2) {
     RANGE_IK(r);
     if (!inr) return;
+    if (cdev) c = *cdev;  // the factor the device-side filter loop chose
     const size_t ld = (size_t)L.ld;
     size_t x = IX(L, i, k);
     double v0 = Vin[x];
@@ -160,9 +161,11 @@ __global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restr
     }
 }
 void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
-                       int kmax, int RaT_nonzero, double visT2) {
+                       int kmax, int RaT_nonzero, double visT2, const double* cdev) {
     Range2 r{0, lv.L.a, kmin, kmax};
-    k_vis_smooth<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vin, vout, lv.dt_vis, c, RaT_nonzero, visT2); tc_note_launch();
+    k_vis_smooth<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vin, vout, lv.dt_vis, c, cdev, RaT_nonzero,
+                                                       visT2);
+    tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------

@@ -28,8 +28,16 @@
 
 namespace {
 
-constexpr int kThreads = 512;
-constexpr int kPPT = 2;  // interior points of level S per thread (n_S <= 1024)
+constexpr int kMaxS = 1024;  // interior points of level S at most
+// build CTA: FP32 one point per thread on 1024 threads (32 warps to hide the
+// sweeps' latencies); FP64 two points per thread on 512 (its registers)
+template <typename T>
+struct BuildShape {
+    static constexpr int threads = sizeof(T) == sizeof(float) ? 1024 : 512;
+    static constexpr int ppt = kMaxS / threads;
+};
+constexpr int kThreads = 512;  // the product kernel's block
+constexpr int kPPT = 2;
 
 template <typename T>
 struct SubArgs {
@@ -82,7 +90,8 @@ __device__ __forceinline__ T sm_apply(const Lay& L, const T* S, size_t x, const 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
+__global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(SubArgs<T> A) {
+    constexpr int kThreads = BuildShape<T>::threads, kPPT = BuildShape<T>::ppt;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* P0 = reinterpret_cast<T*>(smem_raw);
     T* P1 = P0 + A.LS.plane;
@@ -119,15 +128,30 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
     auto visit = [&](T* Sa, T* Sb, int up) -> T* {
         const T* cv = A.tab + (up ? 2 : 0) * A.nsweeps;
         const bool pp = !up && A.per_point_down;
+        // the sweep's factors are loaded one sweep ahead (their latency is
+        // not on the sweep-to-sweep path)
+        T cnext[kPPT];
+        T cunext = __ldg(cv);
+#pragma unroll
+        for (int q = 0; q < kPPT; q++) cnext[q] = (pp && pa[q]) ? __ldg(A.ctab + tid + q * kThreads) : T(0);
         for (int n = 0; n < A.nsweeps; n++) {
-            const T cu = __ldg(cv + n);
+            const T cu = cunext;
+            T cpp[kPPT];
+#pragma unroll
+            for (int q = 0; q < kPPT; q++) cpp[q] = cnext[q];
+            if (n + 1 < A.nsweeps) {
+                cunext = __ldg(cv + n + 1);
+#pragma unroll
+                for (int q = 0; q < kPPT; q++)
+                    if (pp && pa[q]) cnext[q] = __ldg(A.ctab + (size_t)(n + 1) * nS + tid + q * kThreads);
+            }
 #pragma unroll
             for (int q = 0; q < kPPT; q++) {
                 if (!pa[q]) continue;
                 const T res = sm_apply(A.LS, Sa, px[q], cf[q], R[px[q]]);
                 // the per-point factor from the table (the same correctly rounded
                 // division as k_sweep's, done once per solve)
-                const T c = pp ? __ldg(A.ctab + (size_t)n * nS + tid + q * kThreads) : cu;
+                const T c = pp ? cpp[q] : cu;
                 store_stream<T>(A.LS, Sb, pi[q], pk[q], fma(c * dt[q], res, Sa[px[q]]), A.Vbc);
             }
             __syncthreads();
@@ -204,8 +228,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_subcycle_build(SubArgs<T> A) {
 template <typename TM, typename TV>
 __global__ void __launch_bounds__(256) k_subcycle_apply(Lay L, const TM* __restrict__ M, const TV* rhs, TV* err,
                                                         int nS, int Vbc) {
-    constexpr int kPerLane = kThreads * kPPT / 32;  // nS <= kThreads * kPPT
-    __shared__ double r[kThreads * kPPT];
+    constexpr int kPerLane = kMaxS / 32;  // nS <= kMaxS
+    __shared__ double r[kMaxS];
     const int lane = threadIdx.x & 31;
     const int p = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int a1 = L.a - 1;
@@ -242,11 +266,11 @@ size_t build_smem(const Lay& LS, const Lay& LG) {
 template <typename T>
 int launch_build(cudaStream_t s, const SubArgs<T>& A) {
     const size_t smem = build_smem<T>(A.LS, A.LG);
-    if (A.nS > kThreads * kPPT || smem > 200 * 1024) return -1;
+    if (A.nS > kMaxS || smem > 200 * 1024) return -1;
     if (cudaFuncSetAttribute(k_subcycle_build<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return -1;
-    k_subcycle_build<T><<<A.nS, kThreads, smem, s>>>(A);
+    k_subcycle_build<T><<<A.nS, BuildShape<T>::threads, smem, s>>>(A);
     tc_note_launch();
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -255,7 +279,7 @@ int launch_build(cudaStream_t s, const SubArgs<T>& A) {
 
 int subcycle_fits(const Lay& LS, const Lay& LG) {
     const int nS = (LS.a - 1) * (LS.b - 1);
-    return (nS <= kThreads * kPPT && build_smem<double>(LS, LG) <= 200 * 1024) ? 1 : 0;
+    return (nS <= kMaxS && build_smem<double>(LS, LG) <= 200 * 1024) ? 1 : 0;
 }
 
 // fp32 = 0: the matrices in FP64 from the level's FP64 operator (tab, ctab

@@ -22,6 +22,8 @@
 #include <algorithm>
 
 #include <atomic>
+#include <functional>
+#include <map>
 #include <thread>
 
 static std::atomic<long long> g_launches{0};
@@ -129,7 +131,15 @@ struct Handle {
     std::string err;
     CycleGraphs* graphs = nullptr;
     bool no_graphs = false;
-    bool no_device_loop = false;  // convergence loop on the host (one read per W-cycle)
+    bool no_device_loop = false;  // convergence and filter loops on the host (one read per pass)
+    // filter loops as cached WHILE graphs (k_loop.cu), keyed by loop kind,
+    // level / type and the interpolate flag; their factor tables on the
+    // device: [option-1 first phase 6][option-1 second phase 6][option 0
+    // vis_iter][C Niter 10][C Niter 1]
+    std::map<int, cudaGraphExec_t> flt_graphs;
+    bool flt_failed = false;
+    bool flt_dev_state = false;  // the filter counters and Nvis_store/nn_store live on the device
+    double* flt_tab = nullptr;
     bool wait_test = false;       // tc_debug_wait_test: fused visits wait on a word nothing sets
     int cycles_acc = 0;  // W-cycles of all solves since tc_step began
     bool fuse_visits = false;  // small levels smoothed by one cluster launch per visit
@@ -229,8 +239,143 @@ tc_status sync_scalars(Handle* h) {
     CK(cudaMemcpyAsync(h->hs, h->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
     CK(cudaStreamSynchronize(h->st));
     CK(cudaGetLastError());
+    if (h->hs->flt_launches != 0) {
+        // kernels the filter loops' WHILE bodies ran since the last read
+        tc_note_launch((long long)h->hs->flt_launches);
+        CK(cudaMemsetAsync(&h->ds->flt_launches, 0, sizeof(unsigned long long), h->st));
+    }
+    if (h->hs->flt_status != 0) {
+        const int st = h->hs->flt_status;
+        CK(cudaMemsetAsync(&h->ds->flt_status, 0, sizeof(int), h->st));
+        h->hs->flt_status = 0;
+        return (tc_status)st;
+    }
+    if (h->flt_dev_state) {
+        h->n_temp = h->hs->n_temp;
+        h->n_eta = h->hs->n_eta;
+        h->eig_fine = h->hs->eig_fine;
+        for (int t = 0; t < TC_MAX_TYPES; t++) h->n_comp[t] = h->hs->n_comp[t];
+        h->Nvis_store = h->hs->vis_nvis_store;
+        h->nn_store = h->hs->vis_nn_store;
+    }
     return TC_OK;
 }
+
+// A graph of pre(cond) followed by a WHILE node on cond whose body is
+// body(cond), captured from the handle's stream; the kernels of body are
+// counted by the check kernels, not here.  False when the driver refuses.
+bool build_while_graph(Handle* h, const std::function<void(cudaGraphConditionalHandle)>& pre,
+                       const std::function<void(cudaGraphConditionalHandle)>& body, cudaGraphExec_t* out) {
+    cudaGraph_t g = nullptr;
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) return false;
+    cudaGraphConditionalHandle cond;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    const long long before = t_launches;
+    bool ok = cudaGraphConditionalHandleCreate(&cond, g, 0, 0) == cudaSuccess &&
+              cudaStreamBeginCaptureToGraph(h->st, g, nullptr, nullptr, 0, mode) == cudaSuccess;
+    if (!ok) {
+        cudaGraphDestroy(g);
+        cudaGetLastError();
+        return false;
+    }
+    h->enq_err = cudaSuccess;
+    pre(cond);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    ok = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &capg, &deps, nullptr, &nd) == cudaSuccess &&
+         cs == cudaStreamCaptureStatusActive && cudaGraphAddNode(&wn, capg, deps, nullptr, nd, &np) == cudaSuccess &&
+         cudaStreamUpdateCaptureDependencies(h->st, &wn, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+             cudaSuccess;
+    cudaGraph_t g2 = nullptr;
+    const bool ended = cudaStreamEndCapture(h->st, &g2) == cudaSuccess;
+    if (ok && ended && h->enq_err == cudaSuccess) {
+        cudaGraph_t bg = np.conditional.phGraph_out[0];
+        ok = cudaStreamBeginCaptureToGraph(h->st, bg, nullptr, nullptr, 0, mode) == cudaSuccess;
+        if (ok) {
+            body(cond);
+            cudaGraph_t b2 = nullptr;
+            ok = cudaStreamEndCapture(h->st, &b2) == cudaSuccess && h->enq_err == cudaSuccess;
+        }
+    } else {
+        ok = false;
+    }
+    // the kernels were counted at capture; the graph's launches count them
+    g_launches.fetch_sub(t_launches - before);
+    t_launches = before;
+    cudaGraphExec_t ge = nullptr;
+    if (ok) ok = cudaGraphInstantiate(&ge, g, 0) == cudaSuccess;
+    cudaGraphDestroy(g);
+    h->enq_err = cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        return false;
+    }
+    *out = ge;
+    return true;
+}
+
+// The cached filter graph `key`, built by make() on first use; null when
+// graphs are off or the driver refused one (from then on the host loops
+// run, after the device's filter state was read back).
+cudaGraphExec_t filter_graph(Handle* h, int key, const std::function<bool(cudaGraphExec_t*)>& make) {
+    if (h->flt_failed || h->no_graphs || h->no_device_loop) return nullptr;
+    auto it = h->flt_graphs.find(key);
+    if (it != h->flt_graphs.end()) return it->second;
+    cudaGraphExec_t ge = nullptr;
+    if (!make(&ge)) {
+        h->flt_failed = true;
+        return nullptr;
+    }
+    h->flt_graphs[key] = ge;
+    return ge;
+}
+
+// Reads the device's filter state back into the handle (before a host
+// loop runs after the device ones did).
+tc_status filter_state_to_host(Handle* h) {
+    if (!h->flt_dev_state) return TC_OK;
+    TRY(sync_scalars(h));
+    h->flt_dev_state = false;
+    return TC_OK;
+}
+
+// Launches a filter graph (n_pre kernels before its WHILE node), first
+// handing the module scalars over to the device.
+tc_status launch_filter_graph(Handle* h, cudaGraphExec_t ge, int n_pre) {
+    if (!h->flt_dev_state) {
+        DevScalars init{};
+        init.vis_nvis_store = h->Nvis_store;
+        init.vis_nn_store = h->nn_store;
+        init.n_eta = h->n_eta;
+        init.n_temp = h->n_temp;
+        init.eig_fine = h->eig_fine;
+        for (int t = 0; t < TC_MAX_TYPES; t++) init.n_comp[t] = h->n_comp[t];
+        // eig_fine to the end of DevScalars: the filter state (counters,
+        // status and launch count zero)
+        const size_t o0 = offsetof(DevScalars, eig_fine), o1 = sizeof(DevScalars);
+        CK(cudaMemcpyAsync((char*)h->ds + o0, (const char*)&init + o0, o1 - o0, cudaMemcpyHostToDevice, h->st));
+        CK(cudaStreamSynchronize(h->st));
+        h->flt_dev_state = true;
+    }
+    CK(cudaGraphLaunch(ge, h->st));
+    tc_note_launch(n_pre);
+    return TC_OK;
+}
+
+// filter graph keys: kind * 1000 + level or type * 10 + interpolate
+enum { kFltT = 1, kFltC = 2, kFltVis = 3 };
+// factor-table offsets in h->flt_tab
+constexpr int kTabVisA1 = 0, kTabVisB = 6, kTabVis0 = 12;
+inline int tab_c10(const Handle* h) { return kTabVis0 + h->p.vis_iter; }
+inline int tab_c1(const Handle* h) { return kTabVis0 + h->p.vis_iter + 10; }
 
 // ---------------------------------------------------------------------------
 // boundary-condition and copy helpers
@@ -249,6 +394,27 @@ tc_status smoother_time_T(Handle* h, const double* Tin) {
     copy_plane(h, h->Tvis, Tin);
     copy_plane(h, h->Tbuoy, Tin);
     if (h->p.RaT == 0.0) return TC_OK;
+    // on the device: [smoothness, test] then WHILE {step, BCs, copy back,
+    // smoothness, test}; Tvis keeps its buffer (Tvis2 is the step's target)
+    cudaGraphExec_t ge = filter_graph(h, kFltT * 1000, [&](cudaGraphExec_t* out) {
+        return build_while_graph(
+            h,
+            [&](cudaGraphConditionalHandle c) {
+                launch_tflt_init(h->st, h->ds);
+                launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
+                launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
+            },
+            [&](cudaGraphConditionalHandle c) {
+                launch_smooth_T_step(h->st, h->L1, h->P, h->Tvis, h->Tvis2, h->dts);
+                launch_enforce_T(h->st, h->L1, h->Tvis2, h->p.Tbot);
+                copy_plane(h, h->Tvis, h->Tvis2);
+                launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
+                launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
+            },
+            out);
+    });
+    if (ge) return launch_filter_graph(h, ge, 3);
+    TRY(filter_state_to_host(h));
     int n = 0;
     for (;;) {
         launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
@@ -271,6 +437,39 @@ tc_status smoother_time(Handle* h) {
         copy_plane(h, h->Cvis[t], h->Cnew[t]);
         copy_plane(h, h->Cbuoy[t], h->Cnew[t]);
     }
+    // on the device, per type: [init, smoothness, test] then WHILE {step
+    // with the factor the test chose, BCs, copy back, smoothness, test};
+    // every type's graph is built before any runs
+    std::vector<cudaGraphExec_t> ges(h->ntype, nullptr);
+    bool dev = true;
+    for (int t = 0; t < h->ntype && dev; t++) {
+        ges[t] = filter_graph(h, kFltC * 1000 + t * 10, [&](cudaGraphExec_t* out) {
+            const double* tab = h->flt_tab;
+            return build_while_graph(
+                h,
+                [&](cudaGraphConditionalHandle c) {
+                    launch_cflt_init(h->st, h->ds, t == 0 ? 1 : 0);
+                    launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
+                    launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4,
+                                      c);
+                },
+                [&](cudaGraphConditionalHandle c) {
+                    launch_smooth_C_step(h->st, h->L1, h->P, h->Cvis[t], h->Cvis2[t], h->dts, 0.0, &h->ds->flt_c);
+                    launch_enforce_comp(h->st, h->L1, h->Cvis2[t], h->Cvis[t]);
+                    copy_plane(h, h->Cvis[t], h->Cvis2[t]);
+                    launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
+                    launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4,
+                                      c);
+                },
+                out);
+        });
+        dev = ges[t] != nullptr;
+    }
+    if (dev) {
+        for (int t = 0; t < h->ntype; t++) TRY(launch_filter_graph(h, ges[t], 3));
+        return TC_OK;
+    }
+    TRY(filter_state_to_host(h));
     for (int t = 0; t < h->ntype; t++) {
         int nn = 0;
         bool trigger = false;
@@ -383,6 +582,49 @@ tc_status smoother_vis(Handle* h, int level, int interpolate) {
     const int RaTnz = (h->p.RaT != 0.0) ? 1 : 0;
     const double visT2 = h->p.visT * h->p.visT;
     (void)a;
+    // on the device: [copy, init, grad_eig, test] then WHILE {step with the
+    // factor the test chose, copy back, grad_eig, test}; vis[vcur] keeps its
+    // buffer
+    {
+        VisFltArgs fa{};
+        fa.option = option;
+        fa.interpolate = interpolate;
+        fa.ivis0 = (h->p.ivis == 0) ? 1 : 0;
+        fa.niter0 = Niter;
+        fa.eig_ratio_min = h->p.eig_ratio_min;
+        fa.eig_ratio = h->p.eig_ratio;
+        fa.cap = h->loop_cap;
+        fa.tabA = h->flt_tab + (option == 1 ? kTabVisA1 : kTabVis0);
+        fa.tabB = h->flt_tab + kTabVisB;
+        const int reset = (interpolate == 0 || level == 1) ? 1 : 0;
+        double* cur = lv.vis[lv.vcur];
+        double* oth = lv.vis[1 - lv.vcur];
+        const size_t by = sizeof(double) * lv.L.plane;
+        cudaGraphExec_t ge = filter_graph(h, kFltVis * 1000 + level * 10 + interpolate, [&](cudaGraphExec_t* out) {
+            return build_while_graph(
+                h,
+                [&](cudaGraphConditionalHandle c) {
+                    if (cudaMemcpyAsync(oth, cur, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+                        h->enq_err = cudaErrorUnknown;
+                    launch_vflt_init(h->st, h->ds, reset, fa);
+                    launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
+                    launch_vflt_check(h->st, h->ds, fa, 3, c);
+                },
+                [&](cudaGraphConditionalHandle c) {
+                    launch_vis_smooth(h->st, lv, cur, oth, 0.0, kmin, kmax, RaTnz, visT2, &h->ds->flt_c);
+                    if (cudaMemcpyAsync(cur, oth, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+                        h->enq_err = cudaErrorUnknown;
+                    launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
+                    launch_vflt_check(h->st, h->ds, fa, 3, c);
+                },
+                out);
+        });
+        if (ge) {
+            h->ratio_level = (h->p.ivis != 0) ? level : 0;  // grad_eig's, run at least once
+            return launch_filter_graph(h, ge, 3);
+        }
+        TRY(filter_state_to_host(h));
+    }
     // the buffer that smoothing writes must already hold the rows it leaves unchanged
     CK(cudaMemcpyAsync(lv.vis[1 - lv.vcur], lv.vis[lv.vcur], sizeof(double) * lv.L.plane, cudaMemcpyDeviceToDevice,
                        h->st));
@@ -1362,6 +1604,7 @@ tc_status create(Handle* h, const tc_params* in) {
     // compute_smoothing_parameters (multigrid_cycle.f90:131-173)
     if (p.ivis == 0 || p.RaT == 0.0) h->delta_T = 2.0;
     else h->delta_T = (p.visT != 1.0) ? std::log(p.delta_visT) / std::log(p.visT) : 2.0;
+    if (p.vis_iter < 1) { h->err = "vis_iter must be >= 1"; return TC_ERR_ARG; }
     for (int t = 0; t < TC_MAX_TYPES; t++) h->delta_C[t] = 2.0;
     if (p.comp == 1) {
         for (int t = 0; t < p.ntype; t++)
@@ -1652,6 +1895,24 @@ tc_status create(Handle* h, const tc_params* in) {
         }
         TRY(dalloc_t(h, &h->acc_dnn, pl));
     }
+    // Chebyshev factors of the filter loops (smoother.f90: the same
+    // expressions the host loops evaluate), for the device-side loops
+    {
+        auto cheb = [](int Niter, int n, double lb, double la) {
+            const int ntemp = Niter - n + 1;
+            return 2.0 / (-lb - la + (lb - la) * std::cos((double)(2 * ntemp - 1) * kPi / (double)(2 * Niter)));
+        };
+        std::vector<double> tb((size_t)kTabVis0 + p.vis_iter + 11);
+        for (int n = 1; n <= 6; n++) {
+            tb[kTabVisA1 + n - 1] = cheb(6, n, -5.0, -2.0);
+            tb[kTabVisB + n - 1] = cheb(6, n, -2.0, -1.0);
+        }
+        for (int n = 1; n <= p.vis_iter; n++) tb[kTabVis0 + n - 1] = cheb(p.vis_iter, n, -2.0, -1.0);
+        for (int n = 1; n <= 10; n++) tb[tab_c10(h) + n - 1] = cheb(10, n, -5.0, -1.0);
+        tb[tab_c1(h)] = cheb(1, 1, -5.0, -1.0);
+        TRY(dalloc_t(h, &h->flt_tab, tb.size()));
+        CK(cudaMemcpy(h->flt_tab, tb.data(), sizeof(double) * tb.size(), cudaMemcpyHostToDevice));
+    }
     // stability_RK4_smoother: dts_array
     {
         const double Tr_max = h->eb.Tr / s1.dr, Ts_max = h->eb.Tr / s1.ds;
@@ -1877,6 +2138,8 @@ tc_status tc_destroy(tc_handle* H) {
         if (h->graphs->loop) cudaGraphExecDestroy(h->graphs->loop);
         delete h->graphs;
     }
+    for (auto& kv : h->flt_graphs)
+        if (kv.second) cudaGraphExecDestroy(kv.second);
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     delete H;
     return TC_OK;

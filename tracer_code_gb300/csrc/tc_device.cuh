@@ -90,8 +90,17 @@ __device__ __forceinline__ void reduce_to(int op, double v, double* part, unsign
         __threadfence();
         if (tid < 32) {
             double x = red_identity(op);
-            // lane-strided partial folds in fixed order, then a fixed tree
-            for (int b = tid; b < nb; b += 32) x = red_apply(op, x, __ldcg(part + b));
+            // lane-strided partial folds in fixed order, then a fixed tree;
+            // eight loads in flight per lane (the fold order is unchanged)
+            int b = tid;
+            for (; b + 32 * 7 < nb; b += 32 * 8) {
+                double t[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) t[u] = __ldcg(part + b + 32 * u);
+#pragma unroll
+                for (int u = 0; u < 8; u++) x = red_apply(op, x, t[u]);
+            }
+            for (; b < nb; b += 32) x = red_apply(op, x, __ldcg(part + b));
             for (int off = 16; off > 0; off >>= 1) x = red_apply(op, x, __shfl_down_sync(0xffffffffu, x, off));
             if (tid == 0) {
                 if (op == RED_SUM) x = x / scale_div1 / scale_div2;

@@ -81,6 +81,25 @@ struct DevScalars {
     // last), stored changes, slot of the newest, directions used
     double win_beta[TC_WIN + 1];
     int    win_n, win_head, win_nd, win_pad;
+    // filter loops on the device (k_loop.cu): the factor of the next
+    // smoothing step, the loop counters, the counts and the fine-level
+    // eigenvalue ratio they report, and TC_ERR_LOOP_CAP when a loop hit
+    // its cap
+    double flt_c;
+    double eig_fine;
+    int    flt_n, flt_nn, flt_niter, flt_phase, flt_guard, flt_status;
+    int    vis_nvis_store, vis_nn_store, n_eta, n_temp;
+    int    n_comp[TC_MAX_TYPES];
+    unsigned long long flt_launches;  // kernels run by the loops' WHILE bodies (the host adds them to its count)
+};
+
+// Arguments of the viscosity filter's device check (smoother_vis's tests)
+struct VisFltArgs {
+    int option, interpolate, ivis0, niter0;
+    double eig_ratio_min, eig_ratio;
+    long long cap;
+    const double* tabA;  // factors of the first phase, by inner index 1..niter0
+    const double* tabB;  // option 1 after the first outer pass (Niter 6, lb -2, la -1)
 };
 
 // Reduction scratch: per-block partials plus a completion counter.
@@ -151,8 +170,9 @@ void launch_visf_level1(cudaStream_t s, const Lay& L, const Phys& P, double* vis
                         const double* const* Cvis, const double* zg, const double* T, const double* strain);
 void launch_vis_grad(cudaStream_t s, const Level& lv, const double* vis, int do_eig, int ivis, RedScratch rs,
                      DevScalars* ds);
+// cdev: when non-null the factor is read from the device (filter loop graph)
 void launch_vis_smooth(cudaStream_t s, const Level& lv, const double* vin, double* vout, double c, int kmin,
-                       int kmax, int RaT_nonzero, double visT2);
+                       int kmax, int RaT_nonzero, double visT2, const double* cdev = nullptr);
 void launch_restrict_vis(cudaStream_t s, const Level& coarse, const Level& fine, const double* vfine, double* vcoarse);
 void launch_vis_bcs_init(cudaStream_t s, const Level& coarse, double* v, int RaT_nonzero, double visT2);
 void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int ivis, double courant_stream,
@@ -235,6 +255,19 @@ void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* p
 // and the reference's tests after each level-1 visit, setting the condition
 // of the CUDA-graph WHILE node that repeats the cycle
 void launch_cycle_init(cudaStream_t s, DevScalars* ds);
+// filter loops as WHILE graphs: smoother_time_T, smoother_time (one type),
+// smoother_vis; each check follows a smoothness / grad_eig reduction and
+// sets the condition (1: smooth once more and test again)
+// (body: kernels in the WHILE body, added to ds->flt_launches per pass)
+void launch_tflt_init(cudaStream_t s, DevScalars* ds);
+void launch_tflt_check(cudaStream_t s, DevScalars* ds, double delta, long long cap, int body,
+                       cudaGraphConditionalHandle cond);
+void launch_cflt_init(cudaStream_t s, DevScalars* ds, int first_type);
+void launch_cflt_check(cudaStream_t s, DevScalars* ds, int type, double delta, long long cap, const double* tab10,
+                       const double* tab1, int body, cudaGraphConditionalHandle cond);
+void launch_vflt_init(cudaStream_t s, DevScalars* ds, int reset_store, const VisFltArgs& a);
+void launch_vflt_check(cudaStream_t s, DevScalars* ds, const VisFltArgs& a, int body,
+                       cudaGraphConditionalHandle cond);
 void launch_cycle_check(cudaStream_t s, DevScalars* ds, double tolerance, int max_cycles,
                         cudaGraphConditionalHandle cond);
 
@@ -274,7 +307,7 @@ void launch_smoothness(cudaStream_t s, const Lay& L, const double* f, RedScratch
 void launch_smooth_T_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Tin, double* Tout,
                           const double* dts);
 void launch_smooth_C_step(cudaStream_t s, const Lay& L, const Phys& P, const double* Cin, double* Cout,
-                          const double* dts, double c);
+                          const double* dts, double c, const double* cdev = nullptr);
 void launch_conductivity(cudaStream_t s, const Lay& L, const Phys& P, const double* const* Cvis, double* conduct,
                          double* conduct_r, double* conduct_s);
 void launch_velocities(cudaStream_t s, const Lay& L, const Phys& P, const double* SF, double* u, double* w);
