@@ -29,7 +29,14 @@ def test_128x128_trajectory_prefix_is_the_oracle():
 
 
 def test_1024x256_trajectory_is_complete():
+    import numpy as np
     with open(os.path.join(HERE, "traj_1024x256.json")) as f:
         d = json.load(f)
-    assert d["steps"] == len(d["rows"]) == 5 and d["nx"] == 1024 and d["nz"] == 256
+    assert d["steps"] == len(d["rows"]) == 20 and d["nx"] == 1024 and d["nz"] == 256
     assert d["counts_sum"] >= (d["nx"] + 1) * (d["nz"] + 1) * d["tpc"]  # interior plus mirrored ghosts
+    # the final per-volume counts file matches the recorded sum and checksum
+    counts = np.load(os.path.join(HERE, "traj_1024x256_counts.npz"))["counts"].astype(np.int64)
+    assert int(counts.sum()) == d["counts_sum"]
+    c = counts.ravel()
+    assert int((c * (np.arange(c.size) % 9973 + 1)).sum()) == d["counts_checksum"]
+    assert d["rows"][-1]["counts_checksum"] == d["counts_checksum"]
