@@ -173,63 +173,98 @@ __global__ void k_plane_diff(double* dst, const double* a, const double* b, size
 }
 
 // ---- windowed correction ---------------------------------------------------
-// Directions j = 0..nd-1: j = 0 the newest change (written to slot
-// (head + 1) % TC_WIN this launch), j = 1..nold the stored changes from the
-// newest back, then the network's direction.  Sums: the upper triangle of
-// G (kWT entries, row-major) and b.
+// Directions j = 0..nd-1: j = 0 the newest change d = psi - prev (written to
+// slot (head + 1) % TC_WIN this launch), j = 1..nold the stored changes from
+// the newest back, then the network's direction.  Sums: the upper triangle
+// of G (kWT entries, row-major over kWD) and b.
+//
+// One stencil application per cycle: with rp = RHS - A prev (kept from the
+// previous correction, see k_win_update) and r = RHS - A psi, the newest
+// direction's image is A d = rp - r, and the network direction's image A dnn
+// is formed once per solve (k_win_init).
 constexpr int kWD = TC_WIN + 1;               // directions at most
 constexpr int kWT = kWD * (kWD + 1) / 2;      // Gram entries
 constexpr int kWS = kWT + kWD;                // sums
 
 __device__ __forceinline__ int win_slot(int head, int back) { return (head - back + 2 * TC_WIN) % TC_WIN; }
 
+// rp = RHS - A prev and, with a network direction, A dnn (interior points)
+__global__ void k_win_init(Lay L, Range2 r, const double* __restrict__ coef, const double* rhs, const double* prev,
+                           const double* dnn, double* rp, double* adnn) {
+    RANGE_IK(r);
+    if (!inr) return;
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    const size_t x = IX(L, i, k);
+    double ap = 0.0, an = 0.0;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) {
+        const double c = __ldg(coef + x + d * L.plane);
+        const size_t y = (size_t)((ptrdiff_t)x + off[d]);
+        ap = fma(c, ld_state(prev + y), ap);
+        if (adnn) an = fma(c, ld_state(dnn + y), an);
+    }
+    rp[x] = ld_state(rhs + x) - ap;
+    if (adnn) adnn[x] = an;
+}
+
+// the grid-stride sums for ND directions
+template <int ND>
+__device__ __forceinline__ void win_sums(const Lay& L, const double* __restrict__ coef, const double* rhs,
+                                         const double* psi, const double* prev, const double* rp, double* P,
+                                         double* AP, double* rn, const double* adnn, int snew, int nold,
+                                         double* s) {
+    const ptrdiff_t ld = (ptrdiff_t)L.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    const int a1i = L.a - 1, npts = (L.a - 1) * (L.b - 1);
+    for (int pnt = blockIdx.x * blockDim.x + threadIdx.x; pnt < npts; pnt += gridDim.x * blockDim.x) {
+        const size_t x = IX(L, 1 + pnt % a1i, 1 + pnt / a1i);
+        double ap = 0.0;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++)
+            ap = fma(__ldg(coef + x + d * L.plane), ld_state(psi + (size_t)((ptrdiff_t)x + off[d])), ap);
+        const double res = ld_state(rhs + x) - ap;
+        double v[ND];
+        v[0] = ld_state(rp + x) - res;  // A (psi - prev)
+        P[(size_t)snew * L.plane + x] = ld_state(psi + x) - ld_state(prev + x);
+        AP[(size_t)snew * L.plane + x] = v[0];
+        rn[x] = res;
+#pragma unroll
+        for (int j = 1; j < ND; j++)
+            v[j] = (j <= nold) ? ld_state(AP + (size_t)win_slot(snew, j) * L.plane + x) : ld_state(adnn + x);
+        // w = 1/|r| (a weight: single-precision reciprocal is enough)
+        const float fr = fabsf((float)res);
+        const double w = (fr > 0.0f) ? (double)(1.0f / fr) : 0.0;
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            const double wi = w * v[i];
+            const int row = i * kWD - i * (i - 1) / 2;  // upper-triangle start of row i over kWD
+#pragma unroll
+            for (int j = i; j < ND; j++) s[row + (j - i)] += wi * v[j];
+            s[kWT + i] += wi * res;
+        }
+    }
+}
+
 __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restrict__ coef, const double* rhs,
-                                                  const double* psi, const double* prev, double* P, double* AP,
-                                                  const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds) {
+                                                  const double* psi, const double* prev, const double* rp, double* P,
+                                                  double* AP, double* rn, const double* adnn, int use_dnn,
+                                                  RedScratch rs, DevScalars* ds) {
     pdl_entry();
     const int n = __ldcg(&ds->win_n), head = __ldcg(&ds->win_head);
     const int nold = min(n, TC_WIN - 1);
     const int nd = 1 + nold + (use_dnn ? 1 : 0);
     const int snew = (n == 0) ? 0 : (head + 1) % TC_WIN;
-    const ptrdiff_t ld = (ptrdiff_t)L.ld;
-    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
-    const int a1i = L.a - 1, npts = (L.a - 1) * (L.b - 1);
     double s[kWS];
 #pragma unroll
     for (int q = 0; q < kWS; q++) s[q] = 0.0;
-    for (int pnt = blockIdx.x * blockDim.x + threadIdx.x; pnt < npts; pnt += gridDim.x * blockDim.x) {
-        const size_t x = IX(L, 1 + pnt % a1i, 1 + pnt / a1i);
-        double ap = 0.0, ad = 0.0, an = 0.0;
-#pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++) {
-            const double c = __ldg(coef + x + d * L.plane);
-            const size_t y = (size_t)((ptrdiff_t)x + off[d]);
-            const double p = ld_state(psi + y);
-            ap = fma(c, p, ap);
-            ad = fma(c, p - ld_state(prev + y), ad);
-            if (use_dnn) an = fma(c, ld_state(dnn + y), an);
-        }
-        P[(size_t)snew * L.plane + x] = ld_state(psi + x) - ld_state(prev + x);
-        AP[(size_t)snew * L.plane + x] = ad;
-        const double res = ld_state(rhs + x) - ap;
-        double v[kWD];
-        v[0] = ad;
-#pragma unroll
-        for (int j = 1; j < kWD; j++) {
-            if (j <= nold) v[j] = ld_state(AP + (size_t)win_slot(snew, j) * L.plane + x);
-            else v[j] = (use_dnn && j == nold + 1) ? an : 0.0;
-        }
-        // w = 1/|r| (a weight: single-precision reciprocal is enough)
-        const float fr = fabsf((float)res);
-        const double w = (fr > 0.0f) ? (double)(1.0f / fr) : 0.0;
-        int t = 0;
-#pragma unroll
-        for (int i = 0; i < kWD; i++) {
-            const double wi = w * v[i];
-#pragma unroll
-            for (int j = i; j < kWD; j++) s[t++] += wi * v[j];
-            s[kWT + i] += wi * res;
-        }
+    // the direction count is the same for the whole grid
+    switch (nd) {
+        case 1: win_sums<1>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
+        case 2: win_sums<2>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
+        case 3: win_sums<3>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
+        case 4: win_sums<4>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
+        default: win_sums<kWD>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
     }
     // block sums (warp shuffle, then one warp over the warps' partials)
     __shared__ double sh[kWS][8];
@@ -290,6 +325,7 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
             keep[i] = false;
             D[i] = 0.0;
             beta[i] = 0.0;
+            y[i] = 0.0;
             for (int j = 0; j < kWD; j++) Lm[i][j] = 0.0;
         }
         for (int j = 0; j < nd; j++) {
@@ -330,33 +366,53 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
     pdl_done();
 }
 
-// psi += sum_j beta_j v_j (ghosts by the stream BCs); prev = the new psi
-__global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const double* P, const double* dnn,
-                             int use_dnn, const DevScalars* ds, int Vbc) {
+// psi += sum_j beta_j v_j (ghosts by the stream BCs); prev = the new psi;
+// rp = r - sum_j beta_j A v_j, the residual of the new psi by linearity
+// (from this cycle's directly computed r, so rounding does not accumulate)
+__global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const double* P, const double* AP,
+                             const double* rn, double* rp, const double* dnn, const double* adnn, int use_dnn,
+                             const DevScalars* ds, int Vbc) {
     pdl_entry();
     RANGE_IK(r);
     if (!inr) return;
     const size_t x = IX(L, i, k);
     const int nd = __ldcg(&ds->win_nd), head = __ldcg(&ds->win_head);
     const int nold = nd - 1 - (use_dnn ? 1 : 0);
-    double pn = ld_state(psi + x);
+    double pn = ld_state(psi + x), rr = ld_state(rn + x);
     for (int j = 0; j <= nold; j++) {
         const double b = __ldcg(&ds->win_beta[j]);
-        if (b != 0.0) pn += b * ld_state(P + (size_t)win_slot(head, j) * L.plane + x);
+        if (b != 0.0) {
+            const size_t o = (size_t)win_slot(head, j) * L.plane + x;
+            pn += b * ld_state(P + o);
+            rr -= b * ld_state(AP + o);
+        }
     }
     if (use_dnn) {
         const double b = __ldcg(&ds->win_beta[nd - 1]);
-        if (b != 0.0) pn += b * ld_state(dnn + x);
+        if (b != 0.0) {
+            pn += b * ld_state(dnn + x);
+            rr -= b * ld_state(adnn + x);
+        }
     }
     store_stream<double>(L, psi, i, k, pn, Vbc);
     store_stream<double>(L, prev, i, k, pn, Vbc);
+    rp[x] = rr;
     pdl_done();
 }
 
 }  // namespace
 
+void launch_accel_window_init(cudaStream_t s, const Level& l1, const double* prev, const double* dnn, double* rp,
+                              double* adnn) {
+    Range2 r{1, l1.L.a - 1, 1, l1.L.b - 1};
+    k_win_init<<<grid_for(r), dim3(BX, BY), 0, s>>>(l1.L, r, (const double*)l1.coef, (const double*)l1.rhs, prev,
+                                                   dnn, rp, adnn);
+    tc_note_launch();
+}
+
 void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* prev, double* P, double* AP,
-                         const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds, int Vbc) {
+                         double* rn, double* rp, const double* dnn, const double* adnn, int use_dnn, RedScratch rs,
+                         DevScalars* ds, int Vbc) {
     Range2 r{1, l1.L.a - 1, 1, l1.L.b - 1};
     static int nsm = 0;
     if (nsm == 0) {
@@ -369,9 +425,10 @@ void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* p
     int nb = (npts + 255) / 256;
     if (nb > 2 * nsm) nb = 2 * nsm;
     launch_pdl(k_win_dots, dim3((unsigned)nb), dim3(256), 0, s, l1.L, (const double*)l1.coef,
-               (const double*)l1.rhs, (const double*)psi, (const double*)prev, P, AP, dnn, use_dnn, rs, ds);
-    launch_pdl(k_win_update, grid_for(r), dim3(BX, BY), 0, s, l1.L, r, psi, prev, (const double*)P, dnn, use_dnn,
-               (const DevScalars*)ds, Vbc);
+               (const double*)l1.rhs, (const double*)psi, (const double*)prev, (const double*)rp, P, AP, rn, adnn,
+               use_dnn, rs, ds);
+    launch_pdl(k_win_update, grid_for(r), dim3(BX, BY), 0, s, l1.L, r, psi, prev, (const double*)P,
+               (const double*)AP, (const double*)rn, rp, dnn, adnn, use_dnn, (const DevScalars*)ds, Vbc);
     tc_note_launch(2);
 }
 

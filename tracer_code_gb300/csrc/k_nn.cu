@@ -316,18 +316,21 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
 
 // ---- inputs ---------------------------------------------------------------------------
 // per-image statistics of the three raw channels (raw[n][3][H][W]):
-// st[n] = {mean c0, std c0, rms c1, rms c2}
-__global__ void __launch_bounds__(256) k_stats(const float* __restrict__ raw, int H, int W, float* __restrict__ st) {
+// st[n] = {mean c0, std c0, rms c1, rms c2}.  kStatParts blocks per image
+// write FP64 partial sums; one warp per image folds them in block order.
+constexpr int kStatParts = 64;
+__global__ void __launch_bounds__(256) k_stats_part(const float* __restrict__ raw, int H, int W,
+                                                    double* __restrict__ part) {
     __shared__ double red[8][4];
-    const int n = blockIdx.x;
+    const int n = blockIdx.y, b = blockIdx.x;
     const size_t hw = (size_t)H * W;
     const float* r = raw + (size_t)n * 3 * hw;
     double s0 = 0, q0 = 0, q1 = 0, q2 = 0;
-    for (size_t p = threadIdx.x; p < hw; p += blockDim.x) {
-        const double a = r[p], b = r[hw + p], c = r[2 * hw + p];
+    for (size_t p = (size_t)b * blockDim.x + threadIdx.x; p < hw; p += (size_t)kStatParts * blockDim.x) {
+        const double a = r[p], bb = r[hw + p], c = r[2 * hw + p];
         s0 += a;
         q0 += a * a;
-        q1 += b * b;
+        q1 += bb * bb;
         q2 += c * c;
     }
     double v[4] = {s0, q0, q1, q2};
@@ -336,10 +339,23 @@ __global__ void __launch_bounds__(256) k_stats(const float* __restrict__ raw, in
         if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k] = v[k];
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double t[4] = {0, 0, 0, 0};
-        for (int w = 0; w < 8; w++)
-            for (int k = 0; k < 4; k++) t[k] += red[w][k];
+    if (threadIdx.x < 4) {
+        double t = 0;
+        for (int w = 0; w < 8; w++) t += red[w][threadIdx.x];
+        part[((size_t)n * kStatParts + b) * 4 + threadIdx.x] = t;
+    }
+}
+__global__ void k_stats_fin(const double* __restrict__ part, int H, int W, float* __restrict__ st) {
+    const int n = blockIdx.x, lane = threadIdx.x;
+    const double hw = (double)H * W;
+    double t[4];
+    for (int k = 0; k < 4; k++) {
+        double v = 0;
+        for (int b = lane; b < kStatParts; b += 32) v += part[((size_t)n * kStatParts + b) * 4 + k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        t[k] = v;
+    }
+    if (lane == 0) {
         const double mean = t[0] / hw, var = t[1] / hw - mean * mean;
         st[4 * n + 0] = (float)mean;
         st[4 * n + 1] = (float)sqrt(var > 1e-12 ? var : 1e-12);
@@ -405,6 +421,7 @@ struct tc_net_impl {
          *dA2 = nullptr, *dU2 = nullptr, *dP2 = nullptr, *dA3 = nullptr, *dB3 = nullptr, *dD2a = nullptr,
          *dD2b = nullptr, *dD1a = nullptr, *dD1b = nullptr, *dD0a = nullptr, *dD0b = nullptr, *dZ = nullptr;
     float *out = nullptr, *dout = nullptr, *tgt = nullptr, *stats = nullptr, *part = nullptr, *lossp = nullptr;
+    double* statp = nullptr;   // per-block partial sums of the input statistics
     size_t part_len = 0;
     int* fail = nullptr;
     int* never = nullptr;      // a word that stays 0 (timeout-path test)
@@ -608,7 +625,8 @@ int net_create(tc_net_impl* n, int nbmax, int H, int W, uint64_t seed) {
         if (!nalloc(n, b.a, b.n) || !nalloc(n, b.d, b.n)) return 2;
     if (!nalloc(n, &n->x16, p0 * 16) || !nalloc(n, &n->dZ, p0 * 32)) return 2;
     if (!nalloc(n, &n->out, p0) || !nalloc(n, &n->dout, p0) || !nalloc(n, &n->tgt, p0) ||
-        !nalloc(n, &n->stats, (size_t)4 * nbmax) || !nalloc(n, &n->lossp, 4096) || !nalloc(n, &n->fail, 4) ||
+        !nalloc(n, &n->stats, (size_t)4 * nbmax) || !nalloc(n, &n->statp, (size_t)4 * kStatParts * nbmax) ||
+        !nalloc(n, &n->lossp, 4096) || !nalloc(n, &n->fail, 4) ||
         !nalloc(n, &n->never, 4))
         return 2;
     // weight-gradient partials: the largest chunks * (cout*9*cin + cout) over layers
@@ -627,9 +645,10 @@ int net_create(tc_net_impl* n, int nbmax, int H, int W, uint64_t seed) {
 }
 
 void net_prepare(tc_net_impl* n, const float* raw, int nb) {
-    k_stats<<<nb, 256, 0, n->st>>>(raw, n->H, n->W, n->stats);
+    k_stats_part<<<dim3(kStatParts, nb), 256, 0, n->st>>>(raw, n->H, n->W, n->statp);
+    k_stats_fin<<<nb, 32, 0, n->st>>>(n->statp, n->H, n->W, n->stats);
     k_input<<<nblk((size_t)nb * n->H * n->W), 256, 0, n->st>>>(raw, n->stats, nb, n->H, n->W, n->x16);
-    tc_note_launch(2);
+    tc_note_launch(3);
 }
 
 int net_loss(tc_net_impl* n, const float* raw, const float* sf_new, int nb, float* loss_host) {

@@ -180,6 +180,7 @@ struct Handle {
     // the network's predicted change of the current solve
     double *acc_prev = nullptr, *acc_dnn = nullptr;
     double *win_p = nullptr, *win_ap = nullptr;  // windowed correction: TC_WIN changes and their images
+    double *win_rn = nullptr, *win_rp = nullptr, *win_adnn = nullptr;  // r of psi, of prev; A dnn
     bool acc_dnn_on = false;  // the current solve has a network direction
 };
 
@@ -824,8 +825,9 @@ static StepFusion step_fusion(Handle* h, int pp) {
 void enqueue_cycle_correction(Handle* h) {
     if (h->p.cycle_correction == 0 || h->acc_prev == nullptr) return;
     if (h->p.cycle_correction >= 3) {
-        launch_accel_window(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->win_p, h->win_ap, h->acc_dnn,
-                            (h->p.cycle_correction == 4 && h->acc_dnn_on) ? 1 : 0, h->rs, h->ds, h->p.Vbc);
+        launch_accel_window(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->win_p, h->win_ap, h->win_rn,
+                            h->win_rp, h->acc_dnn, h->win_adnn, (h->p.cycle_correction == 4 && h->acc_dnn_on) ? 1 : 0,
+                            h->rs, h->ds, h->p.Vbc);
         return;
     }
     const int k2 = (h->p.cycle_correction == 2 && h->acc_dnn_on) ? TC_ACCEL_DNN : TC_ACCEL_NONE;
@@ -1255,7 +1257,13 @@ tc_status multigrid(Handle* h) {
     }
     if (h->p.cycle_correction != 0 && h->acc_prev != nullptr && !nonN) {
         copy_plane(h, h->acc_prev, cur_err(h, 1));
-        CK(cudaMemsetAsync(&h->ds->win_n, 0, sizeof(int), h->st));  // a new window per solve
+        if (h->p.cycle_correction >= 3) {
+            // a new window per solve: the start's residual and the network direction's image
+            CK(cudaMemsetAsync(&h->ds->win_n, 0, sizeof(int), h->st));
+            const bool dnn = (h->p.cycle_correction == 4 && h->acc_dnn_on);
+            launch_accel_window_init(h->st, h->lev[1], h->acc_prev, dnn ? h->acc_dnn : nullptr, h->win_rp,
+                                     dnn ? h->win_adnn : nullptr);
+        }
     }
     if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     if (try_guess) {
@@ -1892,6 +1900,9 @@ tc_status create(Handle* h, const tc_params* in) {
         if (p.cycle_correction >= 3) {
             TRY(dalloc_t(h, &h->win_p, pl * TC_WIN));
             TRY(dalloc_t(h, &h->win_ap, pl * TC_WIN));
+            TRY(dalloc_t(h, &h->win_rn, pl));
+            TRY(dalloc_t(h, &h->win_rp, pl));
+            TRY(dalloc_t(h, &h->win_adnn, pl));
         }
         TRY(dalloc_t(h, &h->acc_dnn, pl));
     }

@@ -248,8 +248,14 @@ void launch_plane_diff(cudaStream_t s, double* dst, const double* a, const doubl
 // ring order, ds->win_n / win_head), and psi moves to the minimiser of the
 // L1-weighted residual over psi + span{window, dnn (when use_dnn)}; prev =
 // the corrected psi.  ds->win_n = 0 starts a new window.
+// rn: this cycle's residual RHS - A psi (written); rp: RHS - A prev (read,
+// then replaced by the corrected psi's, by linearity); adnn = A dnn.
+// launch_accel_window_init forms rp for the solve's start and adnn.
 void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* prev, double* P, double* AP,
-                         const double* dnn, int use_dnn, RedScratch rs, DevScalars* ds, int Vbc);
+                         double* rn, double* rp, const double* dnn, const double* adnn, int use_dnn, RedScratch rs,
+                         DevScalars* ds, int Vbc);
+void launch_accel_window_init(cudaStream_t s, const Level& l1, const double* prev, const double* dnn, double* rp,
+                              double* adnn);
 
 // (k_loop.cu) the multigrid convergence loop on the device: the cycle counter
 // and the reference's tests after each level-1 visit, setting the condition
