@@ -151,3 +151,31 @@ def test_field_sweep_toggle_needs_mixed(gpu_lib):
     with pytest.raises(TracerError):
         g.debug_sweep_fields(False)
     g.close()
+
+
+@pytest.mark.parametrize("nx,nz", [(256, 64), (200, 72)])
+def test_level1_tiled_field_sweeps_bit_exact(gpu_lib, nx, nz):
+    """Two or three level-1 field sweeps per launch (k_sweep_gblk, 64x16
+    tiles with recomputed halos, coefficients in shared memory) give the
+    one-sweep-per-launch result bit for bit, on grids whose interior is not
+    a multiple of the tile (partial tiles at the far walls)."""
+    p = _mixed(case_1024_like(nx=nx, nz=nz, grids=4, tpc=3))
+    p.mg_zero_coarse = 1
+    st = fresh_state(p, seed=11)
+    g0 = Simulation(p)
+    g0.upload(st)
+    base = g0.autotune()
+    g0.close()
+    sf = {}
+    for blk in (0, 2, 3):
+        shapes = [list(c) for c in base]
+        shapes[0][2] = 1000 + blk if blk else 0
+        g = Simulation(p)
+        g.upload(st)
+        g.set_launch_shapes(shapes)
+        q = g.multigrid()
+        sf[blk] = (q, g.download()["SF"])
+        g.close()
+    for blk in (2, 3):
+        assert sf[blk][0] == sf[0][0], (blk, sf[blk][0], sf[0][0])
+        assert np.array_equal(sf[blk][1], sf[0][1]), blk

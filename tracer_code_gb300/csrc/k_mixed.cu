@@ -72,7 +72,6 @@ __global__ void __launch_bounds__(256, 1) k_sweep_g32(Lay L, Range2 r, FoldG32 F
                                                       const float* __restrict__ dts, const float* __restrict__ cA,
                                                       const float* __restrict__ cB, float c_uniform, int per_point,
                                                       float temp, int Vbc) {
-    constexpr unsigned kMask[TC_NCOEF] = TC_FOLD_G32_MASK;
     const int i = r.i0 + (int)(blockIdx.x * blockDim.x + threadIdx.x);
     const int k = r.k0 + 2 * (int)(blockIdx.y * blockDim.y + threadIdx.y);
     bool act[2];
@@ -87,18 +86,7 @@ __global__ void __launch_bounds__(256, 1) k_sweep_g32(Lay L, Range2 r, FoldG32 F
         float G[5];
 #pragma unroll
         for (int j = 0; j < 5; j++) G[j] = act[p] ? __ldg(g + xp + j * pl) : 0.f;
-#pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++) {
-            float c = 0.f;
-            bool first = true;
-#pragma unroll
-            for (int j = 0; j < 5; j++) {
-                if (!((kMask[d] >> j) & 1u)) continue;
-                c = first ? G[j] * F.w[d][j] : fmaf(G[j], F.w[d][j], c);
-                first = false;
-            }
-            cf[p][d] = -c;
-        }
+        fold_from_fields(F, G, cf[p]);
         dt[p] = act[p] ? __ldg(dts + xp) : 0.f;
         ca[p] = (act[p] && per_point) ? __ldg(cA + xp) : 1.f;
         cb[p] = (act[p] && per_point) ? __ldg(cB + xp) : 0.f;

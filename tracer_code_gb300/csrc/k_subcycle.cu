@@ -89,6 +89,35 @@ __device__ __forceinline__ T sm_apply(const Lay& L, const T* S, size_t x, const 
     return acc;
 }
 
+// The ghost copies store_stream writes for interior point (i, k) besides the
+// point itself (at most three when a, b >= 2 SP + 1): their plane offsets and
+// signs, in store_stream's order, so that a sweep of the build writes
+// v, then sg[g] * v at idx[g] -- the same values, without re-deriving them.
+template <typename T>
+__device__ __forceinline__ int ghost_targets(const Lay& L, int i, int k, int Vbc, int* idx, T* sg) {
+    const int a = L.a, b = L.b;
+    int gi[2] = {i, 0};
+    T si[2] = {T(1), T(-1)};
+    int ng = 1;
+    if (i <= SP) gi[ng++] = -i;
+    else if (i >= a - SP) gi[ng++] = 2 * a - i;
+    int gk[2] = {k, 0};
+    const T zsgn = (Vbc == 1) ? T(1) : T(-1);
+    T sk[2] = {T(1), zsgn};
+    int nk = 1;
+    if (k <= SP) gk[nk++] = -k;
+    else if (k >= b - SP) gk[nk++] = 2 * b - k;
+    int n = 0;
+    for (int u = 0; u < nk; u++)
+        for (int t = 0; t < ng; t++) {
+            if (u == 0 && t == 0) continue;
+            idx[n] = (int)IX(L, gi[t], gk[u]);
+            sg[n] = si[t] * sk[u];
+            n++;
+        }
+    return n;
+}
+
 template <typename T>
 __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(SubArgs<T> A) {
     constexpr int kThreads = BuildShape<T>::threads, kPPT = BuildShape<T>::ppt;
@@ -105,25 +134,43 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
     const int j = blockIdx.x;  // column: interior point j of level S (i fastest)
     const size_t total = 4 * A.LS.plane + 2 * A.LG.plane;
     for (size_t t = tid; t < total; t += blockDim.x) P0[t] = T(0);
-    // this thread's points of level S, their operator, dt and Chebyshev denominators in registers
+    // this thread's points of level S, their operator, dt, ghost copies and
+    // RHS (the unit vector of column j) in registers
     int pi[kPPT], pk[kPPT];
     size_t px[kPPT];
     bool pa[kPPT];
-    T cf[kPPT][TC_NCOEF], dt[kPPT];
+    T cf[kPPT][TC_NCOEF], dt[kPPT], rq[kPPT];
+    int gn[kPPT], gidx[kPPT][3];
+    T gsg[kPPT][3];
+    // threads in rows of rpad slots (a1 rounded up to whole warps) when
+    // that many fit, so that no warp's taps straddle two rows (which puts
+    // two lanes on one shared-memory bank); else a1 slots per row
+    const int b1 = A.LS.b - 1;
+    const int rpad = (((a1 + 31) & ~31) * b1 <= kThreads * kPPT) ? ((a1 + 31) & ~31) : a1;
+    int pidx[kPPT];  // interior point index (i fastest over a1), the matrix's row order
 #pragma unroll
     for (int q = 0; q < kPPT; q++) {
-        const int p = tid + q * kThreads;
-        pa[q] = p < nS;
-        pi[q] = pa[q] ? 1 + p % a1 : 1;
-        pk[q] = pa[q] ? 1 + p / a1 : 1;
+        const int slot = tid + q * kThreads, si = slot % rpad, sk = slot / rpad;
+        pa[q] = si < a1 && sk < b1;
+        pi[q] = pa[q] ? 1 + si : 1;
+        pk[q] = pa[q] ? 1 + sk : 1;
+        pidx[q] = pa[q] ? sk * a1 + si : 0;
+        const int p = pidx[q];
         px[q] = IX(A.LS, pi[q], pk[q]);
 #pragma unroll
         for (int d = 0; d < TC_NCOEF; d++) cf[q][d] = pa[q] ? __ldg(A.coef + px[q] + d * A.LS.plane) : T(0);
         dt[q] = pa[q] ? __ldg(A.dts + px[q]) : T(0);
+        rq[q] = (pa[q] && p == j) ? T(1) : T(0);
+        gn[q] = pa[q] ? ghost_targets<T>(A.LS, pi[q], pk[q], A.Vbc, gidx[q], gsg[q]) : 0;
     }
     __syncthreads();
     if (tid == 0) R[IX(A.LS, 1 + j % a1, 1 + j / a1)] = T(1);
     __syncthreads();
+    // store_stream of v at this thread's point q into S
+    auto put = [&](T* S, int q, T v) {
+        S[px[q]] = v;
+        for (int g = 0; g < gn[q]; g++) S[gidx[q][g]] = gsg[q][g] * v;
+    };
     // one visit of Nmulti sweeps from Sa (ping-pong with Sb); returns the plane holding the result
     auto visit = [&](T* Sa, T* Sb, int up) -> T* {
         const T* cv = A.tab + (up ? 2 : 0) * A.nsweeps;
@@ -133,7 +180,7 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
         T cnext[kPPT];
         T cunext = __ldg(cv);
 #pragma unroll
-        for (int q = 0; q < kPPT; q++) cnext[q] = (pp && pa[q]) ? __ldg(A.ctab + tid + q * kThreads) : T(0);
+        for (int q = 0; q < kPPT; q++) cnext[q] = (pp && pa[q]) ? __ldg(A.ctab + pidx[q]) : T(0);
         for (int n = 0; n < A.nsweeps; n++) {
             const T cu = cunext;
             T cpp[kPPT];
@@ -143,16 +190,16 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
                 cunext = __ldg(cv + n + 1);
 #pragma unroll
                 for (int q = 0; q < kPPT; q++)
-                    if (pp && pa[q]) cnext[q] = __ldg(A.ctab + (size_t)(n + 1) * nS + tid + q * kThreads);
+                    if (pp && pa[q]) cnext[q] = __ldg(A.ctab + (size_t)(n + 1) * nS + pidx[q]);
             }
 #pragma unroll
             for (int q = 0; q < kPPT; q++) {
                 if (!pa[q]) continue;
-                const T res = sm_apply(A.LS, Sa, px[q], cf[q], R[px[q]]);
+                const T res = sm_apply(A.LS, Sa, px[q], cf[q], rq[q]);
                 // the per-point factor from the table (the same correctly rounded
                 // division as k_sweep's, done once per solve)
                 const T c = pp ? cpp[q] : cu;
-                store_stream<T>(A.LS, Sb, pi[q], pk[q], fma(c * dt[q], res, Sa[px[q]]), A.Vbc);
+                put(Sb, q, fma(c * dt[q], res, Sa[px[q]]));
             }
             __syncthreads();
             T* t = Sa;
@@ -173,7 +220,7 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
         // residual into P1, restricted into the coarsest RHS
 #pragma unroll
         for (int q = 0; q < kPPT; q++)
-            if (pa[q]) P1[px[q]] = sm_apply(A.LS, P0, px[q], cf[q], R[px[q]]);
+            if (pa[q]) P1[px[q]] = sm_apply(A.LS, P0, px[q], cf[q], rq[q]);
         __syncthreads();
         for (int c = tid; c < (A.LG.a - 1) * (A.LG.b - 1); c += blockDim.x) {
             const int ic = 1 + c % (A.LG.a - 1), kc = 1 + c / (A.LG.a - 1);
@@ -196,7 +243,7 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
         // prolong the coarse correction and add it to S's
 #pragma unroll
         for (int q = 0; q < kPPT; q++)
-            if (pa[q]) store_stream<T>(A.LS, P0, pi[q], pk[q], P0[px[q]] + sm_prolong<T>(A.LG, EG, pi[q], pk[q]), A.Vbc);
+            if (pa[q]) put(P0, q, P0[px[q]] + sm_prolong<T>(A.LG, EG, pi[q], pk[q]));
         __syncthreads();
         T* out = A.M[blk - 1];
         if (out != nullptr) {
@@ -278,6 +325,7 @@ int launch_build(cudaStream_t s, const SubArgs<T>& A) {
 }  // namespace
 
 int subcycle_fits(const Lay& LS, const Lay& LG) {
+    if (LS.a < 2 * SP + 1 || LS.b < 2 * SP + 1) return 0;  // at most one mirror per direction (ghost_targets)
     const int nS = (LS.a - 1) * (LS.b - 1);
     return (nS <= kMaxS && build_smem<double>(LS, LG) <= 200 * 1024) ? 1 : 0;
 }

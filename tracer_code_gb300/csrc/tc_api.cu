@@ -912,8 +912,10 @@ void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, i
     for (int n = 1; n <= Niter;) {
         // lv.blk sweeps per launch of the tiled smoother while that many
         // remain, then single sweeps of it (lv.blk = 0: k_sweep32; a level
-        // swept from its viscosity fields, g32, is always swept that way)
-        const int blk = (lv.g32 && lv.use_g32) ? 0 : lv.blk;
+        // swept from its viscosity fields, g32: lv.blk = 2 or 3 sweeps per
+        // k_sweep_gblk launch, the rest as single k_sweep_g32 sweeps)
+        const bool gf = lv.g32 && lv.use_g32;
+        const int blk = gf ? ((lv.blk == 2 || lv.blk == 3) ? lv.blk : 0) : lv.blk;
         const int ns = (blk >= 1 && n + blk - 1 <= Niter) ? blk : (blk >= 1 ? 1 : 0);
         float cs[6], ts[6];
         for (int j = 0; j < (ns > 0 ? ns : 1); j++) {
@@ -922,8 +924,10 @@ void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, i
             cs[j] = (float)c;
             ts[j] = (float)temp;
         }
-        if (ns > 0 &&
-            launch_sweep_blk32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], ns, cs, ts, pp, h->p.Vbc)) {
+        if (ns > 0 && (gf ? launch_sweep_gblk32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], ns, cs, ts, pp,
+                                                 h->p.Vbc)
+                          : launch_sweep_blk32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], ns, cs, ts, pp,
+                                               h->p.Vbc))) {
             n += ns;
         } else {
             launch_sweep32(h->st, lv, lv.e32[lv.e32cur], lv.e32[1 - lv.e32cur], cs[0], pp, ts[0], h->p.Vbc);
@@ -2338,7 +2342,9 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
         lv.visit_cfg = 0;
         double best_v = 1e30;
         int best_blk = 0;
-        for (int blk = 0; blk <= (mixed ? ((lv.g32 && lv.use_g32) ? 0 : 6) : 2); blk++) {
+        const bool gf = lv.g32 && lv.use_g32;
+        for (int blk = 0; blk <= (mixed ? (gf ? 3 : 6) : 2); blk++) {
+            if (gf && blk == 1) continue;  // field sweeps: 0 (one per launch), 2 or 3 per launch
             lv.blk = blk;
             double ms = 0;
             TRY(time_visits(&ms));
@@ -2526,21 +2532,20 @@ tc_status tc_time_visit(tc_handle* H, int32_t level, int32_t reps, double* ms_pe
         else if (mixed) iterate_stream32(h, level, 0);
         else iterate_stream(h, level, 0);
     };
+    // one visit launched directly (counted), then reps visits captured in a
+    // CUDA graph and replayed, as the solver runs them (per-launch host
+    // overhead would otherwise dominate the many-launch visits)
     h->enq_err = cudaSuccess;
+    const long long n0 = t_launches;
     visit();
-    cudaEvent_t e0, e1;
-    CK(cudaEventCreate(&e0));
-    CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, h->st));
-    for (int n = 0; n < reps; n++) visit();
-    CK(cudaEventRecord(e1, h->st));
-    CK(cudaEventSynchronize(e1));
     CK(h->enq_err);
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, e0, e1));
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    *ms_per_visit = (double)ms / reps;
+    const long long per_visit = t_launches - n0;
+    double ms = 0.0;
+    TRY(graph_time(h, [&]() {
+        for (int n = 0; n < reps; n++) visit();
+    }, &ms));
+    tc_note_launch(per_visit * reps);
+    *ms_per_visit = ms / reps;
     return TC_OK;
 }
 

@@ -196,6 +196,25 @@ __device__ __forceinline__ T fold_apply(const Lay& L, const T* S, size_t x, cons
     return acc;
 }
 
+// the 13 folded FP32 coefficients, negated, from the five viscosity fields G
+// (eta_xx - eta_zz, eta, eta_xz, eta_x, eta_z) and the weights of FoldG32:
+// per tap the masked fields in order, first a product, then multiply-adds
+__device__ __forceinline__ void fold_from_fields(const FoldG32& F, const float* G, float* cf) {
+    constexpr unsigned kMask[TC_NCOEF] = TC_FOLD_G32_MASK;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) {
+        float c = 0.f;
+        bool first = true;
+#pragma unroll
+        for (int j = 0; j < 5; j++) {
+            if (!((kMask[d] >> j) & 1u)) continue;
+            c = first ? G[j] * F.w[d][j] : fmaf(G[j], F.w[d][j], c);
+            first = false;
+        }
+        cf[d] = -c;
+    }
+}
+
 // writes v at interior (i,k) and the ghost/mirror copies enforceBCs_stream
 // derives from it (Vbc=0: antisymmetric rows; Vbc=1: symmetric rows)
 template <typename T>

@@ -290,6 +290,10 @@ bool launch_sweep_blk32(cudaStream_t s, const Level& lv, const float* Sin, float
 bool launch_sweep_blk64(cudaStream_t s, const Level& lv, const double* Sin, double* Sout, int ns, const double* c,
                         const double* temp, int per_point, int Vbc);
 int sweep_blk_tiles(const Lay& L);  // CTAs of one launch of the tiled smoother
+// ns = 2 or 3 sweeps of the level-1 field sweep (k_sweep_g32) per launch
+// (k_sweep_gblk); false when the level has no fields or ns is not built
+bool launch_sweep_gblk32(cudaStream_t s, const Level& lv, const float* Sin, float* Sout, int ns, const float* c,
+                         const float* temp, int per_point, int Vbc);
 void launch_restrict32(cudaStream_t s, const Level& coarse, const Level& fine, const float* rf, float* rhs_c,
                        float* zero = nullptr);
 void launch_restrict64to32(cudaStream_t s, const Level& coarse, const Level& fine, const double* rf, float* rhs_c,
