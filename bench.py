@@ -46,10 +46,10 @@ REF_BUDGET_S = 150.0
 CPU_SAMPLE_CYCLES = (2, 24)
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the level-1
 # smoother kernels from one ncu capture each (cold cache; the FP64 kernel in
-# profiles/multigrid_solve_1024x256.md, the FP32 one in
-# profiles/k_sweep32_1024x256.md).
+# profiles/multigrid_solve_1024x256.md, the FP32 field sweep k_sweep_g32 in
+# profiles/k_sweep_g32_1024x256.md).
 SWEEP_DRAM_BYTES = 34.0e6
-SWEEP32_DRAM_BYTES = 17.26e6
+SWEEP32_DRAM_BYTES = 8.65e6
 
 
 def workload_params(solver: str = "plain"):
@@ -426,11 +426,13 @@ def sweep_roofline(sim, p, fp32: bool) -> dict:
     peak, src = peaks()
     return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": SWEEP32_DRAM_BYTES if fp32 else SWEEP_DRAM_BYTES,
-            "kernel": ("k_sweep32" if fp32 else "k_sweep") + f" (level 1, {ni}x{nk} points)",
+            "kernel": ("k_sweep_g32" if fp32 else "k_sweep") + f" (level 1, {ni}x{nk} points)",
             "alg_bytes_per_launch": alg_bytes, "kernel_ms": sweep_ms,
             "peak_source": f"{src} (MEASURED_PEAKS.json hbm_gbs burst)" if src == "measured" else "fallback 6.8 TB/s",
-            "note": ("FP32: 44 B/pt (13 coefficients + RHS + dt + psi in/out at half width, per the FP64 88 B/pt "
-                     "count); level-1 FP32 working set 17.8 MB is L2-resident between sweeps" if fp32 else
+            "note": ("FP32: 44 B/pt algorithmic (the FP64 88 B/pt count at half width); the field sweep reads five "
+                     "viscosity fields, dt, RHS and psi (a cold launch reads 8.65 MB = 33 B/pt from DRAM) and forms "
+                     "the 13 coefficients in registers; between sweeps the level-1 FP32 working set is L2-resident"
+                     if fp32 else
                      "FP64-pipe bound on GB300: 15 FP64 ops/point/sweep at 1.2 TFLOP/s")}
 
 

@@ -219,19 +219,29 @@ __device__ __forceinline__ void win_sums(const Lay& L, const double* __restrict_
     const int a1i = L.a - 1, npts = (L.a - 1) * (L.b - 1);
     for (int pnt = blockIdx.x * blockDim.x + threadIdx.x; pnt < npts; pnt += gridDim.x * blockDim.x) {
         const size_t x = IX(L, 1 + pnt % a1i, 1 + pnt / a1i);
+        // all loads first (coefficients, taps, the stored images), then the arithmetic
+        double cf[TC_NCOEF], tp[TC_NCOEF];
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) {
+            cf[d] = __ldg(coef + x + d * L.plane);
+            tp[d] = ld_state(psi + (size_t)((ptrdiff_t)x + off[d]));
+        }
+        double old[ND > 1 ? ND - 1 : 1];
+#pragma unroll
+        for (int j = 1; j < ND; j++)
+            old[j - 1] = (j <= nold) ? ld_state(AP + (size_t)win_slot(snew, j) * L.plane + x) : ld_state(adnn + x);
+        const double rhsx = ld_state(rhs + x), rpx = ld_state(rp + x), px0 = ld_state(prev + x);
         double ap = 0.0;
 #pragma unroll
-        for (int d = 0; d < TC_NCOEF; d++)
-            ap = fma(__ldg(coef + x + d * L.plane), ld_state(psi + (size_t)((ptrdiff_t)x + off[d])), ap);
-        const double res = ld_state(rhs + x) - ap;
+        for (int d = 0; d < TC_NCOEF; d++) ap = fma(cf[d], tp[d], ap);
+        const double res = rhsx - ap;
         double v[ND];
-        v[0] = ld_state(rp + x) - res;  // A (psi - prev)
-        P[(size_t)snew * L.plane + x] = ld_state(psi + x) - ld_state(prev + x);
+        v[0] = rpx - res;  // A (psi - prev)
+        P[(size_t)snew * L.plane + x] = tp[0] - px0;
         AP[(size_t)snew * L.plane + x] = v[0];
         rn[x] = res;
 #pragma unroll
-        for (int j = 1; j < ND; j++)
-            v[j] = (j <= nold) ? ld_state(AP + (size_t)win_slot(snew, j) * L.plane + x) : ld_state(adnn + x);
+        for (int j = 1; j < ND; j++) v[j] = old[j - 1];
         // w = 1/|r| (a weight: single-precision reciprocal is enough)
         const float fr = fabsf((float)res);
         const double w = (fr > 0.0f) ? (double)(1.0f / fr) : 0.0;
@@ -267,7 +277,7 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
         default: win_sums<kWD>(L, coef, rhs, psi, prev, rp, P, AP, rn, adnn, snew, nold, s); break;
     }
     // block sums (warp shuffle, then one warp over the warps' partials)
-    __shared__ double sh[kWS][8];
+    __shared__ double sh[kWS][16];
     __shared__ bool last;
     const int tid = threadIdx.x, bid = blockIdx.x, nb = gridDim.x;
 #pragma unroll
@@ -301,7 +311,16 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
         const int wq = tid >> 5, lane = tid & 31;
         for (int q = wq; q < kWS; q += (int)(blockDim.x >> 5)) {
             double v = 0.0;
-            for (int b = lane; b < nb; b += 32) v += __ldcg(rs.part + (size_t)q * nb + b);
+            const double* pq = rs.part + (size_t)q * nb;
+            int b = lane;
+            for (; b + 32 * 7 < nb; b += 32 * 8) {
+                double t[8];
+#pragma unroll
+                for (int u = 0; u < 8; u++) t[u] = __ldcg(pq + b + 32 * u);
+#pragma unroll
+                for (int u = 0; u < 8; u++) v += t[u];
+            }
+            for (; b < nb; b += 32) v += __ldcg(pq + b);
             for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
             if (lane == 0) tot[q] = v;
         }
@@ -368,35 +387,53 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
 
 // psi += sum_j beta_j v_j (ghosts by the stream BCs); prev = the new psi;
 // rp = r - sum_j beta_j A v_j, the residual of the new psi by linearity
-// (from this cycle's directly computed r, so rounding does not accumulate)
+// (from this cycle's directly computed r, so rounding does not accumulate),
+// also written to the level's residual plane with its mean |.| (the value
+// the convergence test reads, as the residual kernel would give it up to
+// rounding)
 __global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const double* P, const double* AP,
                              const double* rn, double* rp, const double* dnn, const double* adnn, int use_dnn,
-                             const DevScalars* ds, int Vbc) {
+                             const DevScalars* ds, int Vbc, double* res, RedScratch rs, double* res_out,
+                             double div1, double div2) {
     pdl_entry();
     RANGE_IK(r);
-    if (!inr) return;
+    double mag = 0.0;
+    if (inr) {
     const size_t x = IX(L, i, k);
     const int nd = __ldcg(&ds->win_nd), head = __ldcg(&ds->win_head);
     const int nold = nd - 1 - (use_dnn ? 1 : 0);
-    double pn = ld_state(psi + x), rr = ld_state(rn + x);
-    for (int j = 0; j <= nold; j++) {
-        const double b = __ldcg(&ds->win_beta[j]);
-        if (b != 0.0) {
+    double beta[kWD], pv[kWD], av[kWD];
+#pragma unroll
+    for (int j = 0; j < kWD; j++) beta[j] = __ldcg(&ds->win_beta[j]);
+    // every used direction's values loaded before the sums (a zero beta
+    // adds nothing); the network's direction sits in the last used slot
+#pragma unroll
+    for (int j = 0; j < kWD; j++) {
+        pv[j] = 0.0;
+        av[j] = 0.0;
+        if (j <= nold) {
             const size_t o = (size_t)win_slot(head, j) * L.plane + x;
-            pn += b * ld_state(P + o);
-            rr -= b * ld_state(AP + o);
+            pv[j] = ld_state(P + o);
+            av[j] = ld_state(AP + o);
+        } else if (use_dnn && j == nd - 1) {
+            pv[j] = ld_state(dnn + x);
+            av[j] = ld_state(adnn + x);
         }
     }
-    if (use_dnn) {
-        const double b = __ldcg(&ds->win_beta[nd - 1]);
-        if (b != 0.0) {
-            pn += b * ld_state(dnn + x);
-            rr -= b * ld_state(adnn + x);
-        }
+    double pn = ld_state(psi + x), rr = ld_state(rn + x);
+#pragma unroll
+    for (int j = 0; j < kWD; j++) {
+        if (j >= nd) break;
+        pn += beta[j] * pv[j];
+        rr -= beta[j] * av[j];
     }
     store_stream<double>(L, psi, i, k, pn, Vbc);
     store_stream<double>(L, prev, i, k, pn, Vbc);
     rp[x] = rr;
+    res[x] = rr;
+    mag = fabs(rr);
+    }
+    reduce_to(RED_SUM, mag, rs.part, rs.count, res_out, div1, div2);
     pdl_done();
 }
 
@@ -422,13 +459,20 @@ void launch_accel_window(cudaStream_t s, const Level& l1, double* psi, double* p
         if (nsm <= 0) nsm = 1;
     }
     const int npts = (l1.L.a - 1) * (l1.L.b - 1);
+    // grid-stride over the points with one wave of CTAs (three per SM: the
+    // kernel's launch bounds), so that the block sums and their fold stay few
+    // one CTA of 256 threads per SM, grid-stride over the points: the block
+    // sums of the up to 20 FP64 products cost per thread, so few threads with
+    // several points each are fastest (measured at 1024x256: 1 x SMs 306 us per
+    // level-1 visit, 2 x 317, 3 x 326, 6 x 358; 512 threads 317)
     int nb = (npts + 255) / 256;
-    if (nb > 2 * nsm) nb = 2 * nsm;
+    if (nb > nsm) nb = nsm;
     launch_pdl(k_win_dots, dim3((unsigned)nb), dim3(256), 0, s, l1.L, (const double*)l1.coef,
                (const double*)l1.rhs, (const double*)psi, (const double*)prev, (const double*)rp, P, AP, rn, adnn,
                use_dnn, rs, ds);
     launch_pdl(k_win_update, grid_for(r), dim3(BX, BY), 0, s, l1.L, r, psi, prev, (const double*)P,
-               (const double*)AP, (const double*)rn, rp, dnn, adnn, use_dnn, (const DevScalars*)ds, Vbc);
+               (const double*)AP, (const double*)rn, rp, dnn, adnn, use_dnn, (const DevScalars*)ds, Vbc, l1.res, rs,
+               &ds->res_mag[1], (double)(l1.L.a - 1), (double)(l1.L.b - 1));
     tc_note_launch(2);
 }
 

@@ -822,17 +822,20 @@ static StepFusion step_fusion(Handle* h, int pp) {
 // prolongation's high-frequency error, which dominates the residual, and a
 // step there tends to cancel the cycle.  The residual the convergence test
 // reads is taken after the correction.
-void enqueue_cycle_correction(Handle* h) {
-    if (h->p.cycle_correction == 0 || h->acc_prev == nullptr) return;
+// returns true when the correction wrote the level-1 residual and its mean
+// (the windowed correction), false when the residual kernel must follow
+bool enqueue_cycle_correction(Handle* h) {
+    if (h->p.cycle_correction == 0 || h->acc_prev == nullptr) return false;
     if (h->p.cycle_correction >= 3) {
         launch_accel_window(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->win_p, h->win_ap, h->win_rn,
                             h->win_rp, h->acc_dnn, h->win_adnn, (h->p.cycle_correction == 4 && h->acc_dnn_on) ? 1 : 0,
                             h->rs, h->ds, h->p.Vbc);
-        return;
+        return true;
     }
     const int k2 = (h->p.cycle_correction == 2 && h->acc_dnn_on) ? TC_ACCEL_DNN : TC_ACCEL_NONE;
     launch_accel(h->st, h->lev[1], cur_err(h, 1), h->acc_prev, h->acc_dnn, TC_ACCEL_DK, k2, 1, h->rs, h->ds,
                  h->p.Vbc);
+    return false;
 }
 
 // Work of one multigrid cycle after the level-1 visit (p = 2..nsteps);
@@ -954,8 +957,7 @@ void enqueue_l1_mixed(Handle* h, int dir) {
     launch_residual_to32(h->st, l1, cur_err(h, 1), l1.rhs32, cur_e32(h, 1));
     iterate_stream32(h, 1, dir);
     launch_update64(h->st, l1, cur_err(h, 1), cur_e32(h, 1), h->p.Vbc);
-    enqueue_cycle_correction(h);
-    launch_residual(h->st, l1, cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+    if (!enqueue_cycle_correction(h)) launch_residual(h->st, l1, cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
 }
 
 // p = 2..nsteps of the mixed solve (enqueue_cycle_rest on FP32 corrections)
@@ -1112,8 +1114,7 @@ bool build_loop_graph(Handle* h, void (*f_l1)(Handle*, int), void (*f_rest)(Hand
 void enqueue_l1(Handle* h, int dir) {
     iterate_stream(h, 1, dir);
     if (h->p.cycle_correction != 0 && h->acc_prev != nullptr) {
-        enqueue_cycle_correction(h);
-        launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
+        if (!enqueue_cycle_correction(h)) launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
     }
 }
 void enqueue_rest(Handle* h, int) { enqueue_cycle_rest(h); }
