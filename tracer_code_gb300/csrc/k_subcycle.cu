@@ -36,8 +36,6 @@ struct BuildShape {
     static constexpr int threads = sizeof(T) == sizeof(float) ? 1024 : 512;
     static constexpr int ppt = kMaxS / threads;
 };
-constexpr int kThreads = 512;  // the product kernel's block
-constexpr int kPPT = 2;
 
 template <typename T>
 struct SubArgs {
@@ -258,6 +256,183 @@ __global__ void __launch_bounds__(BuildShape<T>::threads, 1) k_subcycle_build(Su
     }
 }
 
+// ---- FP32 build, four columns per CTA --------------------------------------------
+// The mixed solve's build (k_subcycle_build<float>'s arithmetic per column)
+// on four unit vectors at once: every shared-memory plane holds the four
+// columns' values of a point in one float4, so a sweep's 13 tap loads serve
+// four columns, and the coefficients, ghost targets and factors are shared.
+// The coarsest solve uses the compact FP32 inverse Ac (Ac[e][e2] = A^-1 at
+// the interior unknowns cq[e], cq[e2], times the row scale rowb[cq[e2]]):
+// the matrix is stored in FP32 anyway, and an FP64 solve of 945 x 2
+// right-hand sides costs about 150 us of the FP64 pipe per build.
+__device__ __forceinline__ float4 f4_fma(float c, float4 v, float4 a) {
+    return make_float4(fmaf(c, v.x, a.x), fmaf(c, v.y, a.y), fmaf(c, v.z, a.z), fmaf(c, v.w, a.w));
+}
+__device__ __forceinline__ float4 f4_scale(float c, float4 v) { return make_float4(c * v.x, c * v.y, c * v.z, c * v.w); }
+__device__ __forceinline__ float4 f4_add(float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+__device__ __forceinline__ float4 f4_div(float4 a, float d) { return make_float4(a.x / d, a.y / d, a.z / d, a.w / d); }
+
+// sm_restrict9 per component (same terms, same order)
+__device__ __forceinline__ float4 sm_restrict9_4(const float4* in, const Lay& F, int ii, int kk) {
+    const float4 c0 = in[IX(F, ii - 1, kk - 1)], c1 = in[IX(F, ii - 1, kk + 1)], c2 = in[IX(F, ii + 1, kk + 1)],
+                 c3 = in[IX(F, ii - 1, kk + 1)];
+    const float4 s0 = in[IX(F, ii - 1, kk)], s1 = in[IX(F, ii, kk - 1)], s2 = in[IX(F, ii + 1, kk)],
+                 s3 = in[IX(F, ii, kk + 1)];
+    const float4 cc = in[IX(F, ii, kk)];
+    const float4 corners = f4_div(f4_add(f4_add(f4_add(c0, c1), c2), c3), 16.f);
+    const float4 sides = f4_div(f4_add(f4_add(f4_add(s0, s1), s2), s3), 8.f);
+    const float4 centre = f4_div(cc, 4.f);
+    return f4_add(f4_add(corners, sides), centre);
+}
+// sm_prolong per component
+__device__ __forceinline__ float4 sm_prolong4(const Lay& C, const float4* ec, int i, int k) {
+    const bool ie = (i % 2) == 0, ke = (k % 2) == 0;
+    if (ie && ke) return ec[IX(C, i / 2, k / 2)];
+    if (ie) return f4_div(f4_add(ec[IX(C, i / 2, (k - 1) / 2)], ec[IX(C, i / 2, (k + 1) / 2)]), 2.f);
+    if (ke) return f4_div(f4_add(ec[IX(C, (i - 1) / 2, k / 2)], ec[IX(C, (i + 1) / 2, k / 2)]), 2.f);
+    return f4_div(f4_add(f4_add(f4_add(ec[IX(C, (i - 1) / 2, (k - 1) / 2)], ec[IX(C, (i + 1) / 2, (k - 1) / 2)]),
+                                ec[IX(C, (i + 1) / 2, (k + 1) / 2)]),
+                         ec[IX(C, (i - 1) / 2, (k + 1) / 2)]),
+                  4.f);
+}
+// store_stream per component
+__device__ __forceinline__ void store_stream4(const Lay& L, float4* S, int i, int k, float4 v, int Vbc) {
+    int idx[3];
+    float sg[3];
+    const int n = ghost_targets<float>(L, i, k, Vbc, idx, sg);
+    S[IX(L, i, k)] = v;
+    for (int g = 0; g < n; g++) S[idx[g]] = f4_scale(sg[g], v);
+}
+
+__global__ void __launch_bounds__(1024, 1) k_subcycle_build4(SubArgs<float> A, const float* __restrict__ Ac) {
+    constexpr int kThreads = 1024;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float4* P0 = reinterpret_cast<float4*>(smem_raw);
+    float4* P1 = P0 + A.LS.plane;
+    float4* P2 = P1 + A.LS.plane;
+    float4* RG = P2 + A.LS.plane;
+    float4* EG = RG + A.LG.plane;
+    const int tid = threadIdx.x;
+    const int nS = A.nS;
+    const int a1 = A.LS.a - 1, b1 = A.LS.b - 1;
+    const int j0 = blockIdx.x * 4;  // columns j0 .. j0 + 3 (those below nS)
+    const size_t total = 3 * A.LS.plane + 2 * A.LG.plane;
+    for (size_t t = tid; t < total; t += blockDim.x) P0[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const int rpad = (((a1 + 31) & ~31) * b1 <= kThreads) ? ((a1 + 31) & ~31) : a1;
+    const int si = tid % rpad, sk = tid / rpad;
+    const bool pa = si < a1 && sk < b1;
+    const int pi = pa ? 1 + si : 1, pk = pa ? 1 + sk : 1;
+    const int pidx = pa ? sk * a1 + si : 0;
+    const size_t px = IX(A.LS, pi, pk);
+    float cf[TC_NCOEF], dt;
+#pragma unroll
+    for (int d = 0; d < TC_NCOEF; d++) cf[d] = pa ? __ldg(A.coef + px + d * A.LS.plane) : 0.f;
+    dt = pa ? __ldg(A.dts + px) : 0.f;
+    const float4 rq = make_float4(pa && pidx == j0 ? 1.f : 0.f, pa && pidx == j0 + 1 ? 1.f : 0.f,
+                                  pa && pidx == j0 + 2 ? 1.f : 0.f, pa && pidx == j0 + 3 ? 1.f : 0.f);
+    int gidx[3];
+    float gsg[3];
+    const int gn = pa ? ghost_targets<float>(A.LS, pi, pk, A.Vbc, gidx, gsg) : 0;
+    __syncthreads();
+    auto put = [&](float4* S, float4 v) {
+        S[px] = v;
+        for (int g = 0; g < gn; g++) S[gidx[g]] = f4_scale(gsg[g], v);
+    };
+    const ptrdiff_t ld = (ptrdiff_t)A.LS.ld;
+    const ptrdiff_t off[TC_NCOEF] = {0, -1, 1, -2, 2, -ld, ld, -2 * ld, 2 * ld, -1 - ld, 1 - ld, -1 + ld, 1 + ld};
+    // rhs - L S at this thread's point, per column (sm_apply's order)
+    auto apply = [&](const float4* S, float4 rhs) {
+        float4 acc = rhs;
+#pragma unroll
+        for (int d = 0; d < TC_NCOEF; d++) acc = f4_fma(-cf[d], S[(ptrdiff_t)px + off[d]], acc);
+        return acc;
+    };
+    auto visit = [&](float4* Sa, float4* Sb, int up) -> float4* {
+        const float* cv = A.tab + (up ? 2 : 0) * A.nsweeps;
+        const bool pp = !up && A.per_point_down;
+        float cunext = __ldg(cv);
+        float cnext = (pp && pa) ? __ldg(A.ctab + pidx) : 0.f;
+        for (int n = 0; n < A.nsweeps; n++) {
+            const float cu = cunext, cpp = cnext;
+            if (n + 1 < A.nsweeps) {
+                cunext = __ldg(cv + n + 1);
+                if (pp && pa) cnext = __ldg(A.ctab + (size_t)(n + 1) * nS + pidx);
+            }
+            if (pa) {
+                const float4 res = apply(Sa, rq);
+                const float c = pp ? cpp : cu;
+                const float cd = c * dt;
+                const float4 s0 = Sa[px];
+                put(Sb, make_float4(fmaf(cd, res.x, s0.x), fmaf(cd, res.y, s0.y), fmaf(cd, res.z, s0.z),
+                                    fmaf(cd, res.w, s0.w)));
+            }
+            __syncthreads();
+            float4* t = Sa;
+            Sa = Sb;
+            Sb = t;
+        }
+        return Sa;
+    };
+    const int lane = tid & 31, warp = tid >> 5, nwarps = kThreads / 32;
+    const int NG = A.LG.b + 1;
+    for (int blk = 1; blk <= A.kmax; blk++) {
+        float4* e = visit(P0, P1, 0);
+        if (e != P0) {
+            for (size_t t = tid; t < A.LS.plane; t += blockDim.x) P0[t] = e[t];
+            __syncthreads();
+        }
+        if (pa) P1[px] = apply(P0, rq);
+        __syncthreads();
+        for (int c = tid; c < (A.LG.a - 1) * (A.LG.b - 1); c += blockDim.x) {
+            const int ic = 1 + c % (A.LG.a - 1), kc = 1 + c / (A.LG.a - 1);
+            RG[IX(A.LG, ic, kc)] = sm_restrict9_4(P1, A.LS, 2 * ic, 2 * kc);
+        }
+        __syncthreads();
+        // coarsest solve x = Ac RG (one warp per unknown, lane-strided, shuffle tree)
+        for (int w = warp; w < A.m; w += nwarps) {
+            const int pw = __ldg(A.cq + w);
+            const float* row = Ac + (size_t)w * A.m;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int e2 = lane; e2 < A.m; e2 += 32) acc = f4_fma(__ldg(row + e2), RG[__ldg(A.cx + e2)], acc);
+            for (int o = 16; o > 0; o >>= 1) {
+                acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+                acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+                acc.z += __shfl_down_sync(0xffffffffu, acc.z, o);
+                acc.w += __shfl_down_sync(0xffffffffu, acc.w, o);
+            }
+            if (lane == 0) store_stream4(A.LG, EG, pw / NG, pw % NG, acc, A.Vbc);
+        }
+        __syncthreads();
+        if (pa) put(P0, f4_add(P0[px], sm_prolong4(A.LG, EG, pi, pk)));
+        __syncthreads();
+        float* out = A.M[blk - 1];
+        if (out != nullptr) {
+            for (size_t t = tid; t < A.LS.plane; t += blockDim.x) P1[t] = P0[t];
+            __syncthreads();
+            const float4* f = visit(P1, P2, 1);
+            for (int p = tid; p < nS; p += blockDim.x) {
+                const float4 v = f[IX(A.LS, 1 + p % a1, 1 + p / a1)];
+                float* o = out + (size_t)p * nS + j0;
+                o[0] = v.x;
+                if (j0 + 1 < nS) o[1] = v.y;
+                if (j0 + 2 < nS) o[2] = v.z;
+                if (j0 + 3 < nS) o[3] = v.w;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Ac[e][e2] = Ainv[cq[e] * n + cq[e2]] * rowb[cq[e2]], rounded to FP32
+__global__ void k_coarse_compact32(const double* __restrict__ Ainv, const double* __restrict__ rowb,
+                                   const int* __restrict__ cq, int m, int n, float* __restrict__ Ac) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m * m) return;
+    const int e = t / m, e2 = t % m;
+    const int q = cq[e2];
+    Ac[t] = (float)(Ainv[(size_t)cq[e] * n + q] * rowb[q]);
+}
+
 // e_S = M r_S: one warp per interior unknown p of level S (lane-strided sum
 // in FP64, shuffle tree), written with the stream BCs' ghost copies.  The
 // product cancels strongly (the sum of the terms' magnitudes is far above
@@ -310,6 +485,20 @@ size_t build_smem(const Lay& LS, const Lay& LG) {
     return sizeof(T) * (4 * LS.plane + 2 * LG.plane);
 }
 
+int launch_build4(cudaStream_t s, const SubArgs<float>& A, float* Ac) {
+    const size_t smem = sizeof(float4) * (3 * A.LS.plane + 2 * A.LG.plane);
+    if (A.nS > kMaxS || smem > 200 * 1024 || Ac == nullptr) return -1;
+    const int mm = A.m * A.m;
+    k_coarse_compact32<<<(mm + 255) / 256, 256, 0, s>>>(A.Ainv, A.rowb, A.cq, A.m, A.n, Ac);
+    tc_note_launch();
+    if (cudaFuncSetAttribute(k_subcycle_build4, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+        return -1;
+    k_subcycle_build4<<<(A.nS + 3) / 4, 1024, smem, s>>>(A, Ac);
+    tc_note_launch();
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
 template <typename T>
 int launch_build(cudaStream_t s, const SubArgs<T>& A) {
     const size_t smem = build_smem<T>(A.LS, A.LG);
@@ -336,7 +525,7 @@ int subcycle_fits(const Lay& LS, const Lay& LG) {
 // solve FP64 as in k_coarse_apply32).
 int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, int fp32, const void* tab,
                           const void* ctab, int nsweeps, int per_point_down, const double* Ainv, const double* rowb,
-                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M) {
+                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M, float* Ac) {
     if (per_point_down && ctab == nullptr) return -1;
     if (kmax < 1 || kmax > 4) return -1;
     if (fp32) {
@@ -348,6 +537,7 @@ int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, int fp
         A.Ainv = Ainv; A.rowb = rowb; A.cq = cq; A.cx = cx; A.n = n; A.m = m;
         A.Vbc = Vbc; A.kmax = kmax; A.nS = (S.L.a - 1) * (S.L.b - 1);
         for (int k = 0; k < 4; k++) A.M[k] = (float*)M[k];
+        if (Ac != nullptr) return launch_build4(s, A, Ac);
         return launch_build(s, A);
     }
     SubArgs<double> A{};

@@ -171,6 +171,7 @@ struct Handle {
     // the c and temp tables of a downward and an upward visit
     bool sub_on = false, sub_valid = false;
     bool sub_m32 = false;  // the matrices are built and held in FP32 (mixed solve)
+    float* sub_ac = nullptr;  // the FP32 build's compact coarse inverse (coarse_m^2)
     int sub_kmax = 0;
     std::vector<int> sub_k, sub_end;
     double* subM[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -1195,7 +1196,7 @@ tc_status multigrid(Handle* h) {
         if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_m32 ? 1 : 0, h->sub_tab, h->sub_ctab, Nm,
                                   cheb_pp ? 1 : 0,
                                   h->ainv, h->rowb, h->coarse_q, h->coarse_x, h->ngrid_coarse, h->coarse_m,
-                                  h->p.Vbc, h->sub_kmax, (void* const*)h->subM) != 0) {
+                                  h->p.Vbc, h->sub_kmax, (void* const*)h->subM, h->sub_ac) != 0) {
             h->err = "k_subcycle_build: launch failed";
             return TC_ERR_CUDA;
         }
@@ -1896,6 +1897,7 @@ tc_status create(Handle* h, const tc_params* in) {
             TRY(dalloc_t(h, &h->sub_tab, 4 * (size_t)p.Nmulti));
             TRY(dalloc_t(h, &h->sub_ctab, (size_t)p.Nmulti * nS));
             h->sub_m32 = (p.solver_precision == 1);
+            if (h->sub_m32) TRY(dalloc_t(h, &h->sub_ac, (size_t)h->coarse_m * h->coarse_m));
             h->sub_on = true;
         }
     }

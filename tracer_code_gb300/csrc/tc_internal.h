@@ -231,7 +231,8 @@ int launch_visit_cluster32(cudaStream_t s, const Level& lv, float* S, const doub
 int subcycle_fits(const Lay& LS, const Lay& LG);
 int launch_subcycle_build(cudaStream_t s, const Level& S, const Level& G, int fp32, const void* tab,
                           const void* ctab, int nsweeps, int per_point_down, const double* Ainv, const double* rowb,
-                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M);
+                          const int* cq, const int* cx, int n, int m, int Vbc, int kmax, void* const* M,
+                          float* Ac = nullptr);  // Ac: FP32 build with a compact FP32 coarse inverse (m x m)
 void launch_subcycle_apply(cudaStream_t s, const Level& S, const void* M, int fp32, int m32, void* err, int Vbc);
 void launch_cheb_table32(cudaStream_t s, const Level& lv, const double* tvals, int nsweeps, float* tab);
 
