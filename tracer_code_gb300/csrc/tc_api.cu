@@ -914,13 +914,13 @@ void iterate_stream32(Handle* h, int level, int dir, int pro = 0, int rst = 0, i
     if (pro) launch_prolong32(h->st, h->lev[level + 1], lv, cur_e32(h, level + 1), cur_e32(h, level), h->p.Vbc);
     int flips = 0;
     for (int n = 1; n <= Niter;) {
-        // lv.blk sweeps per launch of the tiled smoother while that many
-        // remain, then single sweeps of it (lv.blk = 0: k_sweep32; a level
-        // swept from its viscosity fields, g32: lv.blk = 2 or 3 sweeps per
-        // k_sweep_gblk launch, the rest as single k_sweep_g32 sweeps)
+        // lv.blk sweeps per launch of the tiled smoother, the remainder of the
+        // visit in one last launch (lv.blk = 0: k_sweep32; a level swept from
+        // its viscosity fields, g32: lv.blk = 2 or 3 sweeps per k_sweep_gblk
+        // launch, a remainder of one as a k_sweep_g32 sweep)
         const bool gf = lv.g32 && lv.use_g32;
         const int blk = gf ? ((lv.blk == 2 || lv.blk == 3) ? lv.blk : 0) : lv.blk;
-        const int ns = (blk >= 1 && n + blk - 1 <= Niter) ? blk : (blk >= 1 ? 1 : 0);
+        const int ns = (blk >= 1) ? std::min(blk, Niter - n + 1) : 0;
         float cs[6], ts[6];
         for (int j = 0; j < (ns > 0 ? ns : 1); j++) {
             double c, temp;
