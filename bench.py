@@ -655,8 +655,9 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 
 
 def run_ensemble(args):
-    """Batched ensemble: args.ensemble cases (tracer_code_gb300.ensemble.case_params), mixed solver,
-    learned guess and autotuned launch shapes per case, stepped together by tc_ensemble_step."""
+    """Batched ensemble: args.ensemble cases (tracer_code_gb300.ensemble.case_params), mixed solver with
+    the bottom-of-cycle matrix, the learned start and the windowed correction with the network's
+    direction, autotuned launch shapes per case, stepped together by tc_ensemble_step."""
     import torch
     from tracer_code_gb300.ensemble import Ensemble, case_params
     t0 = time.time()
@@ -690,6 +691,8 @@ def run_ensemble(args):
         "dtype": "f32+f64", "data": "synthetic (seeded per case)",
         "config": {"workload": f"{args.ensemble} independent cases, grids {sizes}, 10-25 tracers/cell, "
                                f"Ra 1e5-1e7, B 0.2-1.0, viscosity contrast 1e2-1e5",
+                   "solver": "mixed precision, bottom-of-cycle matrix, learned start (learned_guess=3) and "
+                             "windowed correction with the network's direction (cycle_correction=4)",
                    "tracers_total": ntr, "cases_timed": len(active),
                    "cases_stopped_in_warmup": {str(k): v for k, v in sorted(ens.stopped.items())},
                    "per_case_timesteps_per_s": args.steps / el,

@@ -717,7 +717,7 @@ void launch_coarse_lu(cudaStream_t s, double* band, int* ipiv, int n, int kl, in
     if (in_smem) cudaFuncSetAttribute(k_coarse_lu, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     // 512 threads: the rank-1 updates keep one SM's FP64 pipe busy (574 us
     // for the 217-unknown coarse grid of 1024x256; 606 / 668 / 888 us / 1.30 ms
-    // with 256 / 128 / 64 / 32 threads)
+    // with 256 / 128 / 64 / 32 threads, 775 us on the 8-CTA cluster variant)
     k_coarse_lu<<<1, 512, sm, s>>>(band, ipiv, n, kl, ku, in_smem, &ds->lu_info); tc_note_launch();
 }
 

@@ -5,7 +5,8 @@ tc_step on every case with the cases' work issued concurrently by a pool of
 host threads, so the GPU executes the cases side by side (the small cases'
 latency-bound smoother launches fill SMs the large cases leave idle).  Each
 case may carry the learned initial guess (its own network instance, since a
-network holds one image's activations).
+network holds one image's activations); with a network the cases use the
+learned start and the network's direction in their correction.
 """
 from __future__ import annotations
 
@@ -21,7 +22,8 @@ def case_params(i: int, seed: int = 1):
     """Case i of the 64-case mix: grids 256x64 / 512x128 / 1024x256 in turn,
     10..25 tracers per cell, Ra log-uniform in 1e5..1e7, B uniform in
     0.2..1.0, viscosity contrast log-uniform in 1e2..1e5, mixed precision,
-    coarse corrections from zero; drawn from a generator seeded by (seed, i)."""
+    coarse corrections from zero, the bottom-of-cycle matrix and the windowed
+    correction; drawn from a generator seeded by (seed, i)."""
     rng = np.random.default_rng([seed, i])
     sizes = [(256, 64, 4), (512, 128, 5), (1024, 256, 6)]
     nx, nz, grids = sizes[i % 3]
@@ -33,7 +35,9 @@ def case_params(i: int, seed: int = 1):
     p.RaC[0] = rng.uniform(0.2, 1.0) * ra
     p.visT = 10.0 ** rng.uniform(2.0, 5.0)
     p.mg_zero_coarse = 1
+    p.mg_coarse_matrix = 1
     p.solver_precision = 1
+    p.cycle_correction = 3
     return p
 
 
@@ -48,7 +52,10 @@ class Ensemble:
         for i, p in enumerate(params):
             q = p.copy()
             if weights is not None:
-                q.learned_guess = 1
+                # the learned start and the network's direction in the correction
+                q.learned_guess = 3
+                if q.cycle_correction in (1, 3):
+                    q.cycle_correction += 1
             sim = Simulation(q)
             if weights is not None:
                 net = learned.Net(1, q.nz, q.nx)
