@@ -132,18 +132,20 @@ __global__ void k_pool_bwd_add(View dout, int nb, int H, int W, View din) {
     }
 }
 // out (full resolution view) = nearest upsampling of in (half resolution)
+// nearest upsampling, eight channels (16 bytes) per thread: channel counts,
+// offsets and totals are multiples of 8
 __global__ void k_up(View in, int nb, int H, int W, View out) {
-    const int c = in.c, h = H / 2, w = W / 2;
-    const size_t total = (size_t)nb * H * W * c;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        const int ch = (int)(t % c);
-        size_t q = t / c;
-        const int x = (int)(q % W);
+    const int c8 = in.c / 8, h = H / 2, w = W / 2;
+    const int total = nb * H * W * c8;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+        const int ch = (t % c8) * 8;
+        int q = t / c8;
+        const int x = q % W;
         q /= W;
-        const int y = (int)(q % H);
-        const int n = (int)(q / H);
-        out.p[(((size_t)n * H + y) * W + x) * out.ctot + out.off + ch] =
-            in.p[(((size_t)n * h + y / 2) * w + x / 2) * in.ctot + in.off + ch];
+        const int y = q % H;
+        const int n = q / H;
+        *reinterpret_cast<uint4*>(out.p + (((size_t)n * H + y) * W + x) * out.ctot + out.off + ch) =
+            *reinterpret_cast<const uint4*>(in.p + (((size_t)n * h + y / 2) * w + x / 2) * in.ctot + in.off + ch);
     }
 }
 // dIn (half resolution) = sum over each 2x2 block of dOut (full resolution view)
@@ -514,15 +516,15 @@ int net_forward(tc_net_impl* n, int nb) {
                                                            V(n->P2, 128, 0, 128));
     r |= conv_fwd(n, 6, nb, V(n->P2, 128, 0, 128), V(n->A3, 128, 0, 128));
     r |= conv_fwd(n, 7, nb, V(n->A3, 128, 0, 128), V(n->B3, 128, 0, 128));
-    k_up<<<nblk(px_at(n, 2, nb) * 128), 256, 0, n->st>>>(V(n->B3, 128, 0, 128), nb, H / 4, W / 4,
+    k_up<<<nblk(px_at(n, 2, nb) * 16), 256, 0, n->st>>>(V(n->B3, 128, 0, 128), nb, H / 4, W / 4,
                                                          V(n->U2, 256, 0, 128));
     r |= conv_fwd(n, 8, nb, V(n->U2, 256, 0, 256), V(n->D2a, 128, 0, 128));
     r |= conv_fwd(n, 9, nb, V(n->D2a, 128, 0, 128), V(n->D2b, 128, 0, 128));
-    k_up<<<nblk(px_at(n, 1, nb) * 128), 256, 0, n->st>>>(V(n->D2b, 128, 0, 128), nb, H / 2, W / 2,
+    k_up<<<nblk(px_at(n, 1, nb) * 16), 256, 0, n->st>>>(V(n->D2b, 128, 0, 128), nb, H / 2, W / 2,
                                                          V(n->U1, 192, 0, 128));
     r |= conv_fwd(n, 10, nb, V(n->U1, 192, 0, 192), V(n->D1a, 64, 0, 64));
     r |= conv_fwd(n, 11, nb, V(n->D1a, 64, 0, 64), V(n->D1b, 64, 0, 64));
-    k_up<<<nblk(px_at(n, 0, nb) * 64), 256, 0, n->st>>>(V(n->D1b, 64, 0, 64), nb, H, W, V(n->U0, 96, 0, 64));
+    k_up<<<nblk(px_at(n, 0, nb) * 8), 256, 0, n->st>>>(V(n->D1b, 64, 0, 64), nb, H, W, V(n->U0, 96, 0, 64));
     r |= conv_fwd(n, 12, nb, V(n->U0, 96, 0, 96), V(n->D0a, 32, 0, 32));
     r |= conv_fwd(n, 13, nb, V(n->D0a, 32, 0, 32), V(n->D0b, 32, 0, 32));
     k_head<<<nblk(px_at(n, 0, nb)), 256, 0, n->st>>>(n->D0b, n->p + n->head_off, px_at(n, 0, nb), n->out);
