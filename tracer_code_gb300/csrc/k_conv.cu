@@ -8,13 +8,12 @@
 // offset (out-of-image rows and columns are zero-filled by the TMA unit,
 // which is the convolution's zero padding), the weight operand is one bulk
 // copy of a pre-packed [KC/8][N][8] slab.  A four-stage ring of shared
-// buffers overlaps the copies with the MMAs: thread 0 issues the copies,
-// thread 32 the tcgen05.mma instructions (KC/16 per stage) and commits each
-// stage's release and, at the end, the accumulator's completion; then the
-// four warps read their 32 TMEM lanes (pixels), add the bias, apply ReLU and
-// store BF16 at a channel offset of the output tensor (so a layer can write
-// into one half of a concatenation buffer).  Every wait is bounded; past the
-// bound the kernel records a failure flag and skips its remaining work.
+// buffers overlaps the copies with the MMAs (KC/16 tcgen05.mma per stage);
+// the epilogue reads the accumulator's TMEM lanes (pixels), adds the bias,
+// applies ReLU and stores BF16 at a channel offset of the output tensor (so
+// a layer can write into one half of a concatenation buffer).  Every wait is
+// bounded; past the bound the kernel records a failure flag and skips its
+// remaining work.
 #include "nn_conv.cuh"
 #include "tc_nn.h"
 
@@ -43,37 +42,50 @@ struct ConvArgs {
     const int* test_flag;
 };
 
+// ---- the kernel: persistent and warp-specialised ---------------------------------
+// Each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ... with its
+// TMEM, barriers and stage ring set up once: warp 0 (one lane) issues the
+// copies of every tile's K stages into the ring, warp 1 (one lane) the MMAs
+// into one of two TMEM accumulators (tile j into buffer j % 2), and warps 2-5
+// run the epilogue of tile j while the MMAs of tile j + 1 proceed (warp w reads
+// TMEM lanes 32 (w % 4) .. + 31, i.e. pixels 32 (w % 4) .. + 31 of the tile).
+// accf[b]: the MMAs of the tile in buffer b are done; acce[b]: the epilogue
+// warps have read buffer b (four arrivals).  Same per-tile arithmetic as
+// k_conv3x3 (the same MMAs in the same order, the same epilogue); every wait
+// is bounded, past the bound the kernel records a failure and stops issuing.
+__device__ __forceinline__ void mbar_arrive1(uint64_t* b) {
+    asm volatile("{ .reg .b64 st; mbarrier.arrive.shared::cta.b64 st, [%0]; }" ::"r"(saddr(b)) : "memory");
+}
+
 template <int N>
-__global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
+__global__ void __launch_bounds__(192, 1) k_conv3x3p(const __grid_constant__ CUtensorMap xmap, ConvArgs a) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], done;
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages], accf[2], acce[2];
     __shared__ uint32_t tmem_base;
     __shared__ int bad;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int a_bytes = a.kc * 256;        // 128 rows x kc channels x 2 B
+    const int a_bytes = a.kc * 256;
     const int b_bytes = N * a.kc * 2;
     const int st_bytes = a_bytes + b_bytes;
     const int nchunk = a.cin / a.kc, nsteps = 9 * nchunk;
-    // tile coordinates
     const int tiles_x = a.W / a.bx, tiles_y = a.H / a.by;
-    int t = blockIdx.x;
-    const int tx = t % tiles_x;
-    t /= tiles_x;
-    const int ty = t % tiles_y;
-    const int n = t / tiles_y;
-    const int x0 = tx * a.bx, y0 = ty * a.by;
+    const int ntiles = a.nb * tiles_x * tiles_y;
+    const int my_tiles = (blockIdx.x < (unsigned)ntiles) ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     if (tid == 0) {
         bad = 0;
         for (int s = 0; s < kStages; s++) {
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(&done, 1);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&accf[b], 1);
+            mbar_init(&acce[b], 4);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tmem_base)),
-                     "r"(N));
+                     "r"(2 * N));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -89,66 +101,98 @@ __global__ void __launch_bounds__(128, 1) k_conv3x3(const __grid_constant__ CUte
         }
         __syncthreads();
     }
-
+    auto tile_origin = [&](int j, int& x0, int& y0, int& n) {
+        int t = (int)blockIdx.x + j * (int)gridDim.x;
+        const int tx = t % tiles_x;
+        t /= tiles_x;
+        const int ty = t % tiles_y;
+        n = t / tiles_y;
+        x0 = tx * a.bx;
+        y0 = ty * a.by;
+    };
+    bool fail = false;
     if (bad) {
         // (timeout-path test: no copy issued, nothing to wait for)
-    } else if (tid == 0) {
-        // producer: stage s of step i holds tap i / nchunk, channel chunk i % nchunk
-        for (int i = 0; i < nsteps; i++) {
-            const int s = i % kStages;
-            if (i >= kStages && !mbar_wait(&empty[s], ((i / kStages) - 1) & 1)) { bad = 1; break; }
-            const int tap = i / nchunk, ch = i % nchunk;
-            const int dy = tap / 3 - 1, dx = tap % 3 - 1;
-            unsigned char* As = smem + (size_t)s * st_bytes;
-            unsigned char* Bs = As + a_bytes;
-            mbar_expect_tx(&full[s], (uint32_t)st_bytes);
-            for (int j = 0; j < a.kc / 8; j++)
-                tma_load4(As + j * 2048, &xmap, a.cin_off + ch * a.kc + j * 8, x0 + dx, y0 + dy, n, &full[s]);
-            bulk_load(Bs, a.wpack + (size_t)i * N * a.kc, (uint32_t)b_bytes, &full[s]);
+    } else if (warp == 0) {
+        if (lane == 0) {
+            // producer: global stage g = j * nsteps + i of tile j, tap i / nchunk, chunk i % nchunk
+            for (int j = 0; j < my_tiles && !fail; j++) {
+                int x0, y0, n;
+                tile_origin(j, x0, y0, n);
+                for (int i = 0; i < nsteps; i++) {
+                    const int g = j * nsteps + i, s = g % kStages;
+                    if (g >= kStages && !mbar_wait(&empty[s], ((g / kStages) - 1) & 1)) { fail = true; break; }
+                    const int tap = i / nchunk, ch = i % nchunk;
+                    const int dy = tap / 3 - 1, dx = tap % 3 - 1;
+                    unsigned char* As = smem + (size_t)s * st_bytes;
+                    unsigned char* Bs = As + a_bytes;
+                    mbar_expect_tx(&full[s], (uint32_t)st_bytes);
+                    for (int q = 0; q < a.kc / 8; q++)
+                        tma_load4(As + q * 2048, &xmap, a.cin_off + ch * a.kc + q * 8, x0 + dx, y0 + dy, n, &full[s]);
+                    bulk_load(Bs, a.wpack + (size_t)i * N * a.kc, (uint32_t)b_bytes, &full[s]);
+                }
+            }
         }
-    } else if (tid == 32) {
-        // MMA issuer
-        constexpr uint32_t idesc = idesc_bf16(128, N);
-        for (int i = 0; i < nsteps; i++) {
-            const int s = i % kStages;
-            if (!mbar_wait(&full[s], (i / kStages) & 1)) { bad = 1; break; }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            constexpr uint32_t idesc = idesc_bf16(128, N);
+            for (int j = 0; j < my_tiles && !fail; j++) {
+                const int b = j & 1;
+                // the epilogue of tile j - 2 has read buffer b
+                if (j >= 2 && !mbar_wait(&acce[b], ((j >> 1) - 1) & 1)) { fail = true; break; }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t acc = tmem + (uint32_t)(b * N);
+                for (int i = 0; i < nsteps; i++) {
+                    const int g = j * nsteps + i, s = g % kStages;
+                    if (!mbar_wait(&full[s], (g / kStages) & 1)) { fail = true; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t As = saddr(smem + (size_t)s * st_bytes), Bs = As + a_bytes;
+                    for (int kk = 0; kk < a.kc / 16; kk++) {
+                        const uint64_t ad = smem_desc(As + kk * 2 * 2048, 2048, 128);
+                        const uint64_t bd = smem_desc(Bs + kk * 2 * N * 16, N * 16, 128);
+                        umma_bf16(acc, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+                    }
+                    umma_commit(&empty[s]);
+                }
+                if (fail) break;
+                umma_commit(&accf[b]);
+            }
+        }
+    } else {
+        // epilogue warps 2..5: TMEM lane quarter q = warp % 4
+        const int q = warp & 3;
+        for (int j = 0; j < my_tiles; j++) {
+            const int b = j & 1;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(&accf[b], (j >> 1) & 1) ? 1 : 0) != 0;
+            if (!ok) { fail = true; break; }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t As = saddr(smem + (size_t)s * st_bytes), Bs = As + a_bytes;
-            for (int kk = 0; kk < a.kc / 16; kk++) {
-                const uint64_t ad = smem_desc(As + kk * 2 * 2048, 2048, 128);
-                const uint64_t bd = smem_desc(Bs + kk * 2 * N * 16, N * 16, 128);
-                umma_bf16(tmem, ad, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
-            }
-            umma_commit(&empty[s]);
-        }
-        umma_commit(&done);
-    }
-    __syncthreads();  // roles finished; `bad` visible to every thread
-    // epilogue: warp w holds pixels 32w..32w+31 of the tile (warp-uniform
-    // decision, the TMEM loads are warp-collective)
-    const bool ok = !bad && __all_sync(0xffffffffu, mbar_wait(&done, 0) ? 1 : 0) != 0;
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int m = warp * 32 + lane;
-    const int px = x0 + m % a.bx, py = y0 + m / a.bx;
-    if (ok && !bad) {
-        __nv_bfloat16* op = a.out + (((size_t)n * a.H + py) * a.W + px) * a.cout_tot + a.cout_off;
-        for (int c0 = 0; c0 < a.cout_store; c0 += 8) {
-            float v[8];
-            tmem_ld8(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            __align__(16) __nv_bfloat16 o[8];
+            int x0, y0, n;
+            tile_origin(j, x0, y0, n);
+            const int m = q * 32 + lane;
+            const int px = x0 + m % a.bx, py = y0 + m / a.bx;
+            __nv_bfloat16* op = a.out + (((size_t)n * a.H + py) * a.W + px) * a.cout_tot + a.cout_off;
+            for (int c0 = 0; c0 < a.cout_store; c0 += 8) {
+                float v[8];
+                tmem_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(b * N + c0), v);
+                __align__(16) __nv_bfloat16 o[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) {
-                float y = v[j] + (a.bias ? __ldg(a.bias + c0 + j) : 0.f);
-                if (a.relu) y = fmaxf(y, 0.f);
-                o[j] = __float2bfloat16(y);
+                for (int jj = 0; jj < 8; jj++) {
+                    float y = v[jj] + (a.bias ? __ldg(a.bias + c0 + jj) : 0.f);
+                    if (a.relu) y = fmaxf(y, 0.f);
+                    o[jj] = __float2bfloat16(y);
+                }
+                *reinterpret_cast<uint4*>(op + c0) = *reinterpret_cast<const uint4*>(o);
             }
-            *reinterpret_cast<uint4*>(op + c0) = *reinterpret_cast<const uint4*>(o);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&acce[b]);
         }
     }
-    if ((!ok || bad) && lane == 0) atomicExch(a.fail, 1);
+    if (fail) atomicExch(&bad, 1);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(N));
+    if (bad && tid == 0) atomicExch(a.fail, 1);
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * N));
 }
 
 // ---- host ---------------------------------------------------------------------
@@ -170,11 +214,27 @@ static bool conv_attr() {
     static bool done = false;
     if (!done) {
         const int smax = kStages * (64 * 256 + N * 64 * 2);
-        if (cudaFuncSetAttribute(k_conv3x3<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess)
+        if (cudaFuncSetAttribute(k_conv3x3p<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax) != cudaSuccess)
             return false;
         done = true;
     }
     return true;
+}
+
+// CTAs of the persistent convolution: two per SM while two double-buffered
+// accumulators fit the SM's 512 TMEM columns (one for N = 256)
+template <int N>
+static unsigned conv_grid(int ntiles) {
+    static int nsm = 0;
+    if (nsm == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
+    }
+    const int per_sm = (4 * N <= 512) ? 2 : 1;
+    const int g = nsm * per_sm;
+    return (unsigned)(ntiles < g ? ntiles : g);
 }
 
 }  // namespace nn
@@ -210,12 +270,18 @@ int conv3x3_launch(cudaStream_t s, const __nv_bfloat16* x, int nb, int H, int W,
     a.cout_store = cout_store; a.cout_off = cout_off; a.cout_tot = cout_tot;
     a.relu = relu; a.wpack = wpack; a.bias = bias; a.out = out; a.fail = fail; a.test_flag = test_flag;
     const int smem = kStages * (a.kc * 256 + N * a.kc * 2);
-    const unsigned grid = (unsigned)(nb * (H / by) * (W / bx));
+    const int ntiles = nb * (H / by) * (W / bx);
     switch (N) {
-        case 32: if (!conv_attr<32>()) return 4; k_conv3x3<32><<<grid, 128, smem, s>>>(map, a); break;
-        case 64: if (!conv_attr<64>()) return 4; k_conv3x3<64><<<grid, 128, smem, s>>>(map, a); break;
-        case 128: if (!conv_attr<128>()) return 4; k_conv3x3<128><<<grid, 128, smem, s>>>(map, a); break;
-        default: if (!conv_attr<256>()) return 4; k_conv3x3<256><<<grid, 128, smem, s>>>(map, a); break;
+        case 32: if (!conv_attr<32>()) return 4; k_conv3x3p<32><<<conv_grid<32>(ntiles), 192, smem, s>>>(map, a); break;
+        case 64: if (!conv_attr<64>()) return 4; k_conv3x3p<64><<<conv_grid<64>(ntiles), 192, smem, s>>>(map, a); break;
+        case 128:
+            if (!conv_attr<128>()) return 4;
+            k_conv3x3p<128><<<conv_grid<128>(ntiles), 192, smem, s>>>(map, a);
+            break;
+        default:
+            if (!conv_attr<256>()) return 4;
+            k_conv3x3p<256><<<conv_grid<256>(ntiles), 192, smem, s>>>(map, a);
+            break;
     }
     tc_note_launch();
     return cudaGetLastError() == cudaSuccess ? 0 : 5;
