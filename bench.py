@@ -535,9 +535,23 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     learned.attach(sim, net)
     sim.upload(st)
     shapes = sim.autotune()  # launch shapes per level, timed on this GPU (tc_autotune)
+    sim.set_step_graph(args.step_graph)
     with ClockSampler(local_rank) as clk:
         ms, solves, cycles, launches = timed_steps(sim, stream, args.steps, args.warmup, barrier)
     guess_used, guess_offered = learned.guess_stats(sim)
+    # the same handle with every timestep as one graph launch (the other mode)
+    sim.set_step_graph(not args.step_graph)
+    g0 = sim.step_graph_info()[0]
+    # untimed steps up to and including the next tracer sort, so that both of
+    # the step's graphs (with and without the sort) are captured untimed
+    t = args.warmup + args.steps
+    ival = max(int(p.tracer_sort_interval), 1)
+    w_other = max(2, (ival - t % ival) % ival + 1)
+    msg, solvesg, _, _ = timed_steps(sim, stream, args.steps, w_other, barrier)
+    other_mode = {"timesteps_per_s": replica_rate(args.steps, msg * 1e-3, world, max_over_ranks),
+                  "ms_per_step": msg / args.steps, "cycles_per_step": solvesg,
+                  "steps_as_one_graph_launch": sim.step_graph_info()[0] - g0}
+    sim.set_step_graph(args.step_graph)
     ms_max = max_over_ranks(ms)
     value = replica_rate(args.steps, ms * 1e-3, world, max_over_ranks)
     prof = cycle_profile(sim, p, fp32=True)
@@ -571,6 +585,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     simc = Simulation(pc, stream=stream.cuda_stream)
     simc.upload(st)
     simc.autotune()
+    simc.set_step_graph(args.step_graph)
     msc, solvesc, _, _ = timed_steps(simc, stream, args.steps, args.warmup, barrier)
     corr_value = replica_rate(args.steps, msc * 1e-3, world, max_over_ranks)
     simc.close()
@@ -579,6 +594,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     simc1 = Simulation(pc1, stream=stream.cuda_stream)
     simc1.upload(st)
     simc1.autotune()
+    simc1.set_step_graph(args.step_graph)
     msc1, solvesc1, _, _ = timed_steps(simc1, stream, args.steps, args.warmup, barrier)
     corr1_value = replica_rate(args.steps, msc1 * 1e-3, world, max_over_ranks)
     simc1.close()
@@ -587,6 +603,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     simm = Simulation(pm, stream=stream.cuda_stream)
     simm.upload(st)
     simm.autotune()
+    simm.set_step_graph(args.step_graph)
     msm, solvesm, _, _ = timed_steps(simm, stream, args.steps, args.warmup, barrier)
     mixed_value = replica_rate(args.steps, msm * 1e-3, world, max_over_ranks)
     simm.close()
@@ -595,6 +612,7 @@ def run_ours(args, rank: int, world: int, local_rank: int):
     sim0 = Simulation(pp, stream=stream.cuda_stream)
     sim0.upload(st)
     sim0.autotune()
+    sim0.set_step_graph(args.step_graph)
     ms0, solves0, cycles0, _ = timed_steps(sim0, stream, args.steps, args.warmup, barrier)
     plain_value = replica_rate(args.steps, ms0 * 1e-3, world, max_over_ranks)
     prof0 = cycle_profile(sim0, pp, fp32=False)
@@ -610,6 +628,15 @@ def run_ours(args, rank: int, world: int, local_rank: int):
                                        "stalls on this workload); both arms and the CPU reference arm use it",
                    launch_shapes={"tuned_by": "tc_autotune on this GPU, every arm",
                                   "per_level_block_x_block_y_visit": shapes},
+                   step_graph={"timed_arms_as_one_graph_launch_per_step": bool(args.step_graph),
+                               ("eager_steps" if args.step_graph else "graph_steps"): dict(
+                                   other_mode, note="the headline arm's handle, continued for another "
+                                                    f"{args.steps} timed steps after {w_other} untimed ones"),
+                               "note": "a graph step (tc_set_step_graph) is the whole timestep as one CUDA graph "
+                                       "launch, its convergence and filter loops conditional WHILE nodes and "
+                                       "the host's reads of the step's scalars made once after it; its results "
+                                       "equal the eager step's bit for bit.  The eager step (default) reads "
+                                       "the scalars once per solve, filter call and stop test"},
                    cycles_per_step=solves, warmup_cycles_per_step=cycles,
                    w_cycle_profile=prof, level1_sweep_roofline=roof_l1, step_roofline=step_roof,
                    tracer_rk_stages_per_s=value * 4 * ((p.nx + 1) * (p.nz + 1) * p.tpc),
@@ -657,17 +684,27 @@ def run_ours(args, rank: int, world: int, local_rank: int):
 def run_ensemble(args):
     """Batched ensemble: args.ensemble cases (tracer_code_gb300.ensemble.case_params), mixed solver with
     the bottom-of-cycle matrix, the learned start and the windowed correction with the network's
-    direction, autotuned launch shapes per case, stepped together by tc_ensemble_step."""
+    direction, autotuned launch shapes per case, stepped together by one graph launch per step
+    (tc_ensemble_run)."""
     import torch
     from tracer_code_gb300.ensemble import Ensemble, case_params
     t0 = time.time()
     params = [case_params(i) for i in range(args.ensemble)]
-    ens = Ensemble(params, weights=GUESS_WEIGHTS, autotune=True)
+    ens = Ensemble(params, weights=GUESS_WEIGHTS, autotune=True, graph=not args.no_step_graph)
     setup_s = time.time() - t0
     # cases whose run stops (tracers leaving the domain, a diverging solve:
     # the reference's `stop` sites) stop during the warm-up and are left out
     for _ in range(args.warmup):
         ens.step(strict=False)
+    # a case that stopped in the last warm-up step changes the case list, so
+    # the next step captures a new ensemble graph: take that step untimed too
+    extra_warmup = 0
+    while extra_warmup < 5:
+        before = list(ens.active)
+        ens.step(strict=False)
+        extra_warmup += 1
+        if ens.active == before:
+            break
     torch.cuda.synchronize()
     active = list(ens.active)
     t1 = time.perf_counter()
@@ -679,6 +716,7 @@ def run_ensemble(args):
     el = time.perf_counter() - t1
     if ens.active != active:
         raise RuntimeError(f"cases stopped inside the timed steps: {sorted(set(active) - set(ens.active))}")
+    graph_steps, pool_steps = ens.graph_info()
     ntr = sum(ens.ntr[i] for i in active)
     sizes = {}
     for p in params:
@@ -697,8 +735,16 @@ def run_ensemble(args):
                    "cases_stopped_in_warmup": {str(k): v for k, v in sorted(ens.stopped.items())},
                    "per_case_timesteps_per_s": args.steps / el,
                    "cycles_per_step_per_case": cyc, "setup_s": setup_s,
-                   "execution": "one handle and stream per case, tc_step issued by a host thread pool "
-                                "(tc_ensemble_step); per-case CUDA graphs; launch shapes from tc_autotune"},
+                   "execution": ("one CUDA graph launch per ensemble timestep (tc_ensemble_run): every case's "
+                                 "captured step, with its convergence and filter loops as conditional WHILE "
+                                 "nodes, is a branch of one graph forked onto the cases' streams; the first "
+                                 "step, and steps after a case stops, run tc_step per case from a host thread "
+                                 "pool; launch shapes from tc_autotune")
+                                if not args.no_step_graph else
+                                "one handle and stream per case, tc_step issued by a host thread pool "
+                                "(tc_ensemble_step); launch shapes from tc_autotune",
+                   "steps_as_one_graph_launch": graph_steps, "steps_by_thread_pool": pool_steps,
+                   "extra_warmup_steps": extra_warmup},
     }
     ens.close()
     print(json.dumps(line), flush=True)
@@ -711,6 +757,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--step-graph", action="store_true",
+                    help="time the single-case arms with every timestep as one CUDA graph launch")
+    ap.add_argument("--no-step-graph", action="store_true",
+                    help="ensemble: step the cases from a host thread pool instead of one graph launch per step")
     ap.add_argument("--profile-step", metavar="NXxNZ", default=None,
                     help="one timestep of the workload's physics on a smaller grid (for ncu), e.g. 512x128")
     ap.add_argument("--profile-shipped", action="store_true",

@@ -417,6 +417,40 @@ tc_status tc_set_launch_shapes(tc_handle* h, const int32_t* choices);
 tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc_stats_row* rows, int32_t* cycles,
                            double* dts, tc_status* status);
 
+/* The timestep as one CUDA graph launch (no reference counterpart; the
+ * reference's main.f90 time loop calls the same subroutines one by one).
+ * tc_set_step_graph(h, 1): from the handle's second step on, tc_step
+ * captures the whole step (multigrid with its convergence loop and the
+ * filter loops as conditional WHILE nodes, velocities, stats, energy_time)
+ * once per tracer-sort flag and then launches it once per step with one
+ * synchronisation; the reads of the device scalars the step makes (cycle
+ * counts, stop tests, the stats row, dt) are recorded into pinned memory by
+ * the graph and processed after it, in the eager step's order, so results,
+ * status codes and the stats row are those of the eager step (state after a
+ * failing step may differ: a graph step runs to its end).  Steps that need a
+ * host decision run eagerly: the first step, non_Newtonian = 1, equalize =
+ * 1, learned_guess 1 or 2, a solve recorder, the host loops.  A capture the
+ * driver refuses switches the handle back to eager steps (state 2).
+ * tc_step_graph_info: steps run as one graph, state 0 off / 1 on / 2
+ * refused. */
+tc_status tc_set_step_graph(tc_handle* h, int32_t on);
+tc_status tc_step_graph_info(const tc_handle* h, int64_t* graph_steps, int32_t* state);
+
+/* An ensemble stepped by one graph launch per timestep: every case's
+ * captured step is a branch of one graph forked from the ensemble's own
+ * stream onto the cases' streams and joined back; graphs are cached by the
+ * case list (at most four).  tc_ensemble_run takes the cases of this step
+ * (the same contract as tc_ensemble_step, whose thread pool of nthreads
+ * threads runs a step whenever a case is not ready for a captured step);
+ * the handles must outlive the ensemble object.  tc_ensemble_info: steps
+ * run as one launch and steps run by the thread pool. */
+typedef struct tc_ensemble tc_ensemble;
+tc_status tc_ensemble_create(int32_t nthreads, tc_ensemble** out);
+tc_status tc_ensemble_run(tc_ensemble* e, tc_handle* const* hs, int32_t n, tc_stats_row* rows, int32_t* cycles,
+                          double* dts, tc_status* status);
+tc_status tc_ensemble_info(const tc_ensemble* e, int64_t* graph_steps, int64_t* eager_steps);
+tc_status tc_ensemble_destroy(tc_ensemble* e);
+
 /* Diagnostics (no counterpart in the reference).  tc_time_sweep times
  * `nsweeps` back-to-back launches of the multigrid smoother kernel of `level`
  * (the FP32 one under solver_precision = 1), replayed as one CUDA graph as

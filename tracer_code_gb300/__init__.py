@@ -36,7 +36,8 @@ EXPORTS = [
     "tc_get_params", "tc_restart_write", "tc_restart_read", "tc_restart_tracers_write", "tc_restart_tracers_read",
     "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
     "tc_format_vis_line", "tc_write_snapshot", "tc_upload_state_ex", "tc_download_tracer_temperature",
-    "tc_equalize_row", "tc_format_equalize_line",
+    "tc_equalize_row", "tc_format_equalize_line", "tc_set_step_graph", "tc_step_graph_info",
+    "tc_ensemble_create", "tc_ensemble_run", "tc_ensemble_info", "tc_ensemble_destroy",
 ]
 
 
@@ -111,6 +112,12 @@ def load_library(build_if_missing: bool = False):
         L.tc_equalize_row.argtypes = [vp, C.POINTER(C.c_int64), i32, C.POINTER(i32)]
         L.tc_format_equalize_line.argtypes = [C.c_double, C.POINTER(C.c_int64), i32, C.c_char_p, i32]
         L.tc_ensemble_step.argtypes = [C.POINTER(vp), C.c_int32, C.c_int32, vp, vp, vp, vp]
+        L.tc_set_step_graph.argtypes = [vp, C.c_int32]
+        L.tc_step_graph_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int32)]
+        L.tc_ensemble_create.argtypes = [C.c_int32, C.POINTER(vp)]
+        L.tc_ensemble_run.argtypes = [vp, C.POINTER(vp), C.c_int32, vp, vp, vp, vp]
+        L.tc_ensemble_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+        L.tc_ensemble_destroy.argtypes = [vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]
@@ -258,6 +265,17 @@ class Simulation:
         row = StatsRow(); q = C.c_int32(0); dt = C.c_double(0)
         self._chk(self.L.tc_step(self.h, C.byref(row), C.byref(q), C.byref(dt)), "step")
         return row.as_dict(), q.value, dt.value
+
+    def set_step_graph(self, on: bool = True) -> None:
+        """From the next ready step on, each tc_step is one captured graph
+        launch (tc_set_step_graph)."""
+        self._chk(self.L.tc_set_step_graph(self.h, 1 if on else 0), "set_step_graph")
+
+    def step_graph_info(self):
+        """(steps run as one graph launch, state 0 off / 1 on / 2 refused)."""
+        n = C.c_int64(0); st = C.c_int32(0)
+        self._chk(self.L.tc_step_graph_info(self.h, C.byref(n), C.byref(st)), "step_graph_info")
+        return n.value, st.value
 
     def step_host(self, st: dict):
         """tc_step_host on host arrays (pinned for end-to-end timing); st is

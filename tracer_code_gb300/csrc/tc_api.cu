@@ -183,6 +183,31 @@ struct Handle {
     double *win_p = nullptr, *win_ap = nullptr;  // windowed correction: TC_WIN changes and their images
     double *win_rn = nullptr, *win_rp = nullptr, *win_adnn = nullptr;  // r of psi, of prev; A dnn
     bool acc_dnn_on = false;  // the current solve has a network direction
+    // whole-step graphs (tc_set_step_graph, tc_ensemble_*): while a step is
+    // captured, each point where the host would read the device scalars
+    // instead records them into hsnap[k] (a copy node of the graph) and
+    // queues its host work in `deferred`, which runs after every launch of
+    // the graph in the order the eager step would have run it; the WHILE
+    // bodies of the step's loops are captured on body_st
+    bool capturing = false;
+    cudaStream_t body_st = nullptr;
+    DevScalars* hsnap = nullptr;  // pinned, kMaxSnap entries
+    int nsnap = 0;
+    std::vector<std::function<tc_status()>> deferred;
+    bool step_graph = false, step_graph_failed = false;
+    std::map<int, struct StepGraph*> step_graphs;  // by whether the step sorts the tracers
+    tc_stats_row stats_row{};                      // the row the last stats read formed
+    long long sub_tab_key = -1;                    // the sweep tables now in sub_tab
+    long long graph_steps = 0;                     // steps run as one graph launch
+    long long epoch = 0;  // bumped whenever a captured step would be stale (launch shapes, network, stream)
+};
+
+constexpr int kMaxSnap = 64;
+
+struct StepGraph {
+    cudaGraphExec_t ge = nullptr;
+    std::vector<std::function<tc_status()>> post;  // host work after the launch, in order
+    long long n_static = 0;                        // kernel nodes outside the WHILE bodies
 };
 
 #define CK(call)                                                      \
@@ -236,19 +261,18 @@ Lay make_lay(int a, int b) {
     return L;
 }
 
-// Synchronise and fetch the device scalars; reports sticky kernel faults.
-tc_status sync_scalars(Handle* h) {
-    CK(cudaMemcpyAsync(h->hs, h->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
-    CK(cudaStreamSynchronize(h->st));
-    CK(cudaGetLastError());
+// The host's side of a read of the device scalars (already in *h->hs): the
+// kernels the filter loops' WHILE bodies ran since the last read, their
+// status and the module scalars they keep on the device.  `reset` clears
+// the device's counters (a captured step clears them inside its graph).
+tc_status scalars_to_host(Handle* h, bool reset) {
     if (h->hs->flt_launches != 0) {
-        // kernels the filter loops' WHILE bodies ran since the last read
         tc_note_launch((long long)h->hs->flt_launches);
-        CK(cudaMemsetAsync(&h->ds->flt_launches, 0, sizeof(unsigned long long), h->st));
+        if (reset) CK(cudaMemsetAsync(&h->ds->flt_launches, 0, sizeof(unsigned long long), h->st));
     }
     if (h->hs->flt_status != 0) {
         const int st = h->hs->flt_status;
-        CK(cudaMemsetAsync(&h->ds->flt_status, 0, sizeof(int), h->st));
+        if (reset) CK(cudaMemsetAsync(&h->ds->flt_status, 0, sizeof(int), h->st));
         h->hs->flt_status = 0;
         return (tc_status)st;
     }
@@ -261,6 +285,86 @@ tc_status sync_scalars(Handle* h) {
         h->nn_store = h->hs->vis_nn_store;
     }
     return TC_OK;
+}
+
+// Synchronise and fetch the device scalars; reports sticky kernel faults.
+tc_status sync_scalars(Handle* h) {
+    CK(cudaMemcpyAsync(h->hs, h->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    return scalars_to_host(h, true);
+}
+
+// A point where the step reads the device scalars and then runs `post` on
+// them.  Eager: synchronise, read, run post now.  While a step is captured:
+// the graph copies the scalars into the next pinned snapshot and clears the
+// filter counters, and post runs after each launch of the graph.
+tc_status sync_point(Handle* h, std::function<tc_status()> post) {
+    if (!h->capturing) {
+        TRY(sync_scalars(h));
+        return post ? post() : TC_OK;
+    }
+    if (h->nsnap >= kMaxSnap) {
+        if (h->enq_err == cudaSuccess) h->enq_err = cudaErrorInvalidValue;
+        return TC_OK;
+    }
+    const int k = h->nsnap++;
+    CKV(cudaMemcpyAsync(h->hsnap + k, h->ds, sizeof(DevScalars), cudaMemcpyDeviceToHost, h->st));
+    CKV(cudaMemsetAsync(&h->ds->flt_launches, 0, sizeof(unsigned long long), h->st));
+    CKV(cudaMemsetAsync(&h->ds->flt_status, 0, sizeof(int), h->st));
+    h->deferred.push_back([h, k, post]() -> tc_status {
+        *h->hs = h->hsnap[k];
+        TRY(scalars_to_host(h, false));
+        return post ? post() : TC_OK;
+    });
+    return TC_OK;
+}
+
+// Inside a step being captured on h->st: pre(cond), then a WHILE node on
+// cond whose body(cond) is captured on body_st into the node's body graph.
+// The body's kernels are taken out of the launch count (*n_body holds them).
+// False (with h->enq_err set) when the driver refuses.
+bool emit_while(Handle* h, const std::function<void(cudaGraphConditionalHandle)>& pre,
+                const std::function<void(cudaGraphConditionalHandle)>& body, long long* n_body) {
+    *n_body = 0;
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t capg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    cudaGraphConditionalHandle cond;
+    bool ok = cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &capg, &deps, nullptr, &nd) == cudaSuccess &&
+              cs == cudaStreamCaptureStatusActive && cudaGraphConditionalHandleCreate(&cond, capg, 0, 0) == cudaSuccess;
+    if (ok) {
+        pre(cond);
+        ok = h->enq_err == cudaSuccess;
+    }
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t wn = nullptr;
+    ok = ok && cudaStreamGetCaptureInfo(h->st, &cs, nullptr, &capg, &deps, nullptr, &nd) == cudaSuccess &&
+         cs == cudaStreamCaptureStatusActive && cudaGraphAddNode(&wn, capg, deps, nullptr, nd, &np) == cudaSuccess &&
+         cudaStreamUpdateCaptureDependencies(h->st, &wn, nullptr, 1, cudaStreamSetCaptureDependencies) == cudaSuccess;
+    if (ok) {
+        cudaStream_t keep = h->st;
+        const long long before = t_launches;
+        h->st = h->body_st;
+        ok = cudaStreamBeginCaptureToGraph(h->st, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                           cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+            body(cond);
+            cudaGraph_t b2 = nullptr;
+            ok = cudaStreamEndCapture(h->st, &b2) == cudaSuccess && h->enq_err == cudaSuccess;
+        }
+        h->st = keep;
+        *n_body = t_launches - before;
+        g_launches.fetch_sub(*n_body);
+        t_launches = before;
+    }
+    if (!ok && h->enq_err == cudaSuccess) h->enq_err = cudaErrorStreamCaptureUnsupported;
+    return ok;
 }
 
 // A graph of pre(cond) followed by a WHILE node on cond whose body is
@@ -398,23 +502,25 @@ tc_status smoother_time_T(Handle* h, const double* Tin) {
     if (h->p.RaT == 0.0) return TC_OK;
     // on the device: [smoothness, test] then WHILE {step, BCs, copy back,
     // smoothness, test}; Tvis keeps its buffer (Tvis2 is the step's target)
-    cudaGraphExec_t ge = filter_graph(h, kFltT * 1000, [&](cudaGraphExec_t* out) {
-        return build_while_graph(
-            h,
-            [&](cudaGraphConditionalHandle c) {
-                launch_tflt_init(h->st, h->ds);
-                launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
-                launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
-            },
-            [&](cudaGraphConditionalHandle c) {
-                launch_smooth_T_step(h->st, h->L1, h->P, h->Tvis, h->Tvis2, h->dts);
-                launch_enforce_T(h->st, h->L1, h->Tvis2, h->p.Tbot);
-                copy_plane(h, h->Tvis, h->Tvis2);
-                launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
-                launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
-            },
-            out);
-    });
+    auto pre = [&](cudaGraphConditionalHandle c) {
+        launch_tflt_init(h->st, h->ds);
+        launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
+        launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
+    };
+    auto body = [&](cudaGraphConditionalHandle c) {
+        launch_smooth_T_step(h->st, h->L1, h->P, h->Tvis, h->Tvis2, h->dts);
+        launch_enforce_T(h->st, h->L1, h->Tvis2, h->p.Tbot);
+        copy_plane(h, h->Tvis, h->Tvis2);
+        launch_smoothness(h->st, h->L1, h->Tvis, h->rs, h->ds);
+        launch_tflt_check(h->st, h->ds, h->delta_T, h->loop_cap, 4, c);
+    };
+    if (h->capturing) {
+        long long nb;
+        emit_while(h, pre, body, &nb);  // the body's kernels are counted on the device
+        return TC_OK;
+    }
+    cudaGraphExec_t ge =
+        filter_graph(h, kFltT * 1000, [&](cudaGraphExec_t* out) { return build_while_graph(h, pre, body, out); });
     if (ge) return launch_filter_graph(h, ge, 3);
     TRY(filter_state_to_host(h));
     int n = 0;
@@ -445,28 +551,29 @@ tc_status smoother_time(Handle* h) {
     std::vector<cudaGraphExec_t> ges(h->ntype, nullptr);
     bool dev = true;
     for (int t = 0; t < h->ntype && dev; t++) {
-        ges[t] = filter_graph(h, kFltC * 1000 + t * 10, [&](cudaGraphExec_t* out) {
-            const double* tab = h->flt_tab;
-            return build_while_graph(
-                h,
-                [&](cudaGraphConditionalHandle c) {
-                    launch_cflt_init(h->st, h->ds, t == 0 ? 1 : 0);
-                    launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
-                    launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4,
-                                      c);
-                },
-                [&](cudaGraphConditionalHandle c) {
-                    launch_smooth_C_step(h->st, h->L1, h->P, h->Cvis[t], h->Cvis2[t], h->dts, 0.0, &h->ds->flt_c);
-                    launch_enforce_comp(h->st, h->L1, h->Cvis2[t], h->Cvis[t]);
-                    copy_plane(h, h->Cvis[t], h->Cvis2[t]);
-                    launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
-                    launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4,
-                                      c);
-                },
-                out);
-        });
+        const double* tab = h->flt_tab;
+        auto pre = [&](cudaGraphConditionalHandle c) {
+            launch_cflt_init(h->st, h->ds, t == 0 ? 1 : 0);
+            launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
+            launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4, c);
+        };
+        auto body = [&](cudaGraphConditionalHandle c) {
+            launch_smooth_C_step(h->st, h->L1, h->P, h->Cvis[t], h->Cvis2[t], h->dts, 0.0, &h->ds->flt_c);
+            launch_enforce_comp(h->st, h->L1, h->Cvis2[t], h->Cvis[t]);
+            copy_plane(h, h->Cvis[t], h->Cvis2[t]);
+            launch_smoothness(h->st, h->L1, h->Cvis[t], h->rs, h->ds);
+            launch_cflt_check(h->st, h->ds, t, h->delta_C[t], h->loop_cap, tab + tab_c10(h), tab + tab_c1(h), 4, c);
+        };
+        if (h->capturing) {
+            long long nb;
+            emit_while(h, pre, body, &nb);
+            continue;
+        }
+        ges[t] = filter_graph(h, kFltC * 1000 + t * 10,
+                              [&](cudaGraphExec_t* out) { return build_while_graph(h, pre, body, out); });
         dev = ges[t] != nullptr;
     }
+    if (h->capturing) return TC_OK;
     if (dev) {
         for (int t = 0; t < h->ntype; t++) TRY(launch_filter_graph(h, ges[t], 3));
         return TC_OK;
@@ -501,15 +608,25 @@ tc_status smoother_time(Handle* h) {
 }
 
 // the tracer arrays in cell order (k_tracer.cu): positions, types and the
-// reference index move together; the RK temporaries take the old arrays
-void sort_tracers(Handle* h) {
+// reference index move together.  The sort writes into the RK temporaries
+// and is copied back, so every tracer buffer keeps its role from step to
+// step (a captured step graph bakes the buffers in).
+tc_status sort_tracers(Handle* h) {
     launch_sort_tracers(h->st, h->L1, h->P, h->ntr, h->rtr, h->str, h->ttype, h->perm, h->sort_cnt, h->sort_off,
                         h->sort_bsum, h->rtr1, h->str1, h->itmp[0], h->itmp[1], h->Ttr, h->Ttr1);
-    if (h->Ttr) std::swap(h->Ttr, h->Ttr1);
-    std::swap(h->rtr, h->rtr1);
-    std::swap(h->str, h->str1);
-    std::swap(h->ttype, h->itmp[0]);
-    std::swap(h->perm, h->itmp[1]);
+    const size_t n = (size_t)h->ntr;
+    CK(cudaMemcpyAsync(h->rtr, h->rtr1, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->str, h->str1, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->ttype, h->itmp[0], sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(h->perm, h->itmp[1], sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, h->st));
+    if (h->Ttr) CK(cudaMemcpyAsync(h->Ttr, h->Ttr1, sizeof(double) * n, cudaMemcpyDeviceToDevice, h->st));
+    return TC_OK;
+}
+
+// energy_time sorts the tracers at the start of this step
+bool sorts_this_step(const Handle* h) {
+    const bool trc = (h->p.comp == 1) || (h->p.tracer == 1);
+    return trc && h->ntr > 0 && h->p.tracer_sort_interval > 0 && h->tstep % h->p.tracer_sort_interval == 0;
 }
 
 // tracer arrays to host arrays in the reference's order (any may be null);
@@ -602,25 +719,28 @@ tc_status smoother_vis(Handle* h, int level, int interpolate) {
         double* cur = lv.vis[lv.vcur];
         double* oth = lv.vis[1 - lv.vcur];
         const size_t by = sizeof(double) * lv.L.plane;
-        cudaGraphExec_t ge = filter_graph(h, kFltVis * 1000 + level * 10 + interpolate, [&](cudaGraphExec_t* out) {
-            return build_while_graph(
-                h,
-                [&](cudaGraphConditionalHandle c) {
-                    if (cudaMemcpyAsync(oth, cur, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
-                        h->enq_err = cudaErrorUnknown;
-                    launch_vflt_init(h->st, h->ds, reset, fa);
-                    launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
-                    launch_vflt_check(h->st, h->ds, fa, 3, c);
-                },
-                [&](cudaGraphConditionalHandle c) {
-                    launch_vis_smooth(h->st, lv, cur, oth, 0.0, kmin, kmax, RaTnz, visT2, &h->ds->flt_c);
-                    if (cudaMemcpyAsync(cur, oth, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
-                        h->enq_err = cudaErrorUnknown;
-                    launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
-                    launch_vflt_check(h->st, h->ds, fa, 3, c);
-                },
-                out);
-        });
+        auto pre = [&](cudaGraphConditionalHandle c) {
+            if (cudaMemcpyAsync(oth, cur, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+                h->enq_err = cudaErrorUnknown;
+            launch_vflt_init(h->st, h->ds, reset, fa);
+            launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
+            launch_vflt_check(h->st, h->ds, fa, 3, c);
+        };
+        auto body = [&](cudaGraphConditionalHandle c) {
+            launch_vis_smooth(h->st, lv, cur, oth, 0.0, kmin, kmax, RaTnz, visT2, &h->ds->flt_c);
+            if (cudaMemcpyAsync(cur, oth, by, cudaMemcpyDeviceToDevice, h->st) != cudaSuccess)
+                h->enq_err = cudaErrorUnknown;
+            launch_vis_grad(h->st, lv, cur, 1, h->p.ivis, h->rs, h->ds);
+            launch_vflt_check(h->st, h->ds, fa, 3, c);
+        };
+        if (h->capturing) {
+            long long nb;
+            emit_while(h, pre, body, &nb);
+            h->ratio_level = (h->p.ivis != 0) ? level : 0;
+            return TC_OK;
+        }
+        cudaGraphExec_t ge = filter_graph(h, kFltVis * 1000 + level * 10 + interpolate,
+                                          [&](cudaGraphExec_t* out) { return build_while_graph(h, pre, body, out); });
         if (ge) {
             h->ratio_level = (h->p.ivis != 0) ? level : 0;  // grad_eig's, run at least once
             return launch_filter_graph(h, ge, 3);
@@ -1132,6 +1252,26 @@ void compute_velocities(Handle* h);
 // 141-148).  The non-Newtonian iteration runs in FP64 without the learned
 // start and issues its launches directly (its level setup has host-side
 // loops between kernels).
+// The device-side convergence loop's outcome after a read of the scalars:
+// its W-cycle count and stop reason (iterative_solver.f90:147-156); the
+// kernels it ran are n_pre before the WHILE node and n_body per pass.
+tc_status loop_result(Handle* h, long long n_pre, long long n_body) {
+    const int q = h->hs->cyc_q;
+    const int st = h->hs->cyc_status;
+    const long long bodies = (st == TC_ERR_MG_CYCLES) ? q - 2 : q - 1;
+    tc_note_launch(n_pre + (bodies > 0 ? bodies : 0) * n_body);
+    if (h->hs->visit_timeout || st == TC_ERR_DEVICE_TIMEOUT) {
+        h->err = "fused smoother visit: neighbour wait exceeded its bound";
+        return TC_ERR_DEVICE_TIMEOUT;
+    }
+    if (st == TC_ERR_MG_RESIDUAL) return TC_ERR_MG_RESIDUAL;
+    h->last_cycles = q;
+    if (st == TC_ERR_MG_CYCLES) return TC_ERR_MG_CYCLES;
+    if (st != 0) return (tc_status)st;
+    h->cycles_acc += q;
+    return TC_OK;
+}
+
 tc_status multigrid(Handle* h) {
     if (!h->uploaded) return TC_ERR_STATE;
     const bool nonN = (h->p.non_Newtonian == 1);
@@ -1185,13 +1325,26 @@ tc_status multigrid(Handle* h) {
             for (int n = 1; n <= Nm; n++)
                 sweep_factors(Nm, n, dir, cheb_pp, &tv[(size_t)(2 * dir) * Nm + n - 1],
                               &tv[(size_t)(2 * dir + 1) * Nm + n - 1]);
-        if (h->sub_m32) {
-            std::vector<float> tf(tv.begin(), tv.end());
-            CK(cudaMemcpyAsync(h->sub_tab, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, h->st));
-            if (cheb_pp) launch_cheb_table32(h->st, h->lev[S], tv.data() + Nm, Nm, (float*)h->sub_ctab);
-        } else {
-            CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
-            if (cheb_pp) launch_cheb_table(h->st, h->lev[S], tv.data() + Nm, Nm, h->sub_ctab);
+        // the sweep tables depend on Nmulti and the Chebyshev flag only: uploaded
+        // once (a captured step cannot copy from pageable host memory)
+        const long long key = (long long)Nm * 4 + (cheb_pp ? 2 : 0) + (h->sub_m32 ? 1 : 0);
+        if (h->sub_tab_key != key) {
+            if (h->capturing) {
+                if (h->enq_err == cudaSuccess) h->enq_err = cudaErrorStreamCaptureUnsupported;
+                return TC_OK;
+            }
+            if (h->sub_m32) {
+                std::vector<float> tf(tv.begin(), tv.end());
+                CK(cudaMemcpyAsync(h->sub_tab, tf.data(), sizeof(float) * tf.size(), cudaMemcpyHostToDevice, h->st));
+            } else {
+                CK(cudaMemcpyAsync(h->sub_tab, tv.data(), sizeof(double) * tv.size(), cudaMemcpyHostToDevice, h->st));
+            }
+            CK(cudaStreamSynchronize(h->st));
+            h->sub_tab_key = key;
+        }
+        if (cheb_pp) {
+            if (h->sub_m32) launch_cheb_table32(h->st, h->lev[S], tv.data() + Nm, Nm, (float*)h->sub_ctab);
+            else launch_cheb_table(h->st, h->lev[S], tv.data() + Nm, Nm, h->sub_ctab);
         }
         if (launch_subcycle_build(h->st, h->lev[S], h->lev[G], h->sub_m32 ? 1 : 0, h->sub_tab, h->sub_ctab, Nm,
                                   cheb_pp ? 1 : 0,
@@ -1229,6 +1382,7 @@ tc_status multigrid(Handle* h) {
             h->err = "learned guess: network forward failed";
             return TC_ERR_CUDA;
         }
+        CK(cudaMemcpyAsync(&h->ds->net_fail, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToDevice, h->st));
         launch_residual(h->st, h->lev[1], cur_err(h, 1), h->rs, &h->ds->res_mag[1]);
         launch_residual(h->st, h->lev[1], h->guess, h->rs, &h->ds->res_mag[0]);
     }
@@ -1243,24 +1397,29 @@ tc_status multigrid(Handle* h) {
             h->err = "learned guess: network forward failed";
             return TC_ERR_CUDA;
         }
+        CK(cudaMemcpyAsync(&h->ds->net_fail, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToDevice, h->st));
         launch_plane_diff(h->st, h->acc_dnn, h->guess, cur_err(h, 1), h->L1.plane);
         if (h->p.learned_guess == 3)
             launch_accel(h->st, h->lev[1], cur_err(h, 1), nullptr, h->acc_dnn, TC_ACCEL_DNN, TC_ACCEL_NONE, 0, h->rs,
                          h->ds, h->p.Vbc);
     }
-    TRY(sync_scalars(h));
-    if (h->acc_dnn_on) {
-        int f = 0;
-        CK(cudaMemcpy(&f, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToHost));
-        if (f) {
-            h->err = "learned guess: a convolution's bounded wait gave up";
-            return TC_ERR_DEVICE_TIMEOUT;
+    // the start's read: the network's wait flag, the learned start's
+    // bookkeeping and the coarse LU's pivot test
+    const bool dnn_on = h->acc_dnn_on, lg3 = (h->p.learned_guess == 3);
+    TRY(sync_point(h, [h, dnn_on, lg3]() -> tc_status {
+        if (dnn_on) {
+            if (h->hs->net_fail) {
+                h->err = "learned guess: a convolution's bounded wait gave up";
+                return TC_ERR_DEVICE_TIMEOUT;
+            }
+            if (lg3) {
+                h->guess_offered++;
+                if (h->hs->acc_alpha[0] != 0.0) h->guess_used++;
+            }
         }
-        if (h->p.learned_guess == 3) {
-            h->guess_offered++;
-            if (h->hs->acc_alpha[0] != 0.0) h->guess_used++;
-        }
-    }
+        if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
+        return TC_OK;
+    }));
     if (h->p.cycle_correction != 0 && h->acc_prev != nullptr && !nonN) {
         copy_plane(h, h->acc_prev, cur_err(h, 1));
         if (h->p.cycle_correction >= 3) {
@@ -1271,11 +1430,8 @@ tc_status multigrid(Handle* h) {
                                      dnn ? h->win_adnn : nullptr);
         }
     }
-    if (h->hs->lu_info != 0) return TC_ERR_SINGULAR;
     if (try_guess) {
-        int f = 0;
-        CK(cudaMemcpy(&f, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToHost));
-        if (f) {
+        if (h->hs->net_fail) {
             h->err = "learned guess: a convolution's bounded wait gave up";
             return TC_ERR_DEVICE_TIMEOUT;
         }
@@ -1296,6 +1452,27 @@ tc_status multigrid(Handle* h) {
     const bool use_graphs = (h->st != nullptr) && !h->no_graphs && !nonN;
     void (*f_l1)(Handle*, int) = mixed ? enqueue_l1_mixed : enqueue_l1;
     void (*f_rest)(Handle*, int) = mixed ? enqueue_rest_mixed : enqueue_rest;
+    if (h->capturing) {
+        // inside a captured step: the convergence loop as this step's own
+        // WHILE node, its result read after the step
+        long long n_body = 0;
+        emit_while(
+            h,
+            [&](cudaGraphConditionalHandle c) {
+                launch_cycle_init(h->st, h->ds);
+                f_l1(h, dir1);
+                launch_cycle_check(h->st, h->ds, h->p.tolerance, h->p.max_cycles, c);
+            },
+            [&](cudaGraphConditionalHandle c) {
+                f_rest(h, 0);
+                f_l1(h, dir1);
+                launch_cycle_check(h->st, h->ds, h->p.tolerance, h->p.max_cycles, c);
+            },
+            &n_body);
+        TRY(sync_point(h, [h, n_body]() { return loop_result(h, 0, n_body); }));
+        copy_plane(h, h->SF, cur_err(h, 1));
+        return TC_OK;
+    }
     h->enq_err = cudaSuccess;
     if (use_graphs && (cg.l1 == nullptr || cg.ratio_level != h->ratio_level || cg.zero != h->p.mg_zero_coarse ||
                        cg.dir1 != dir1 || cg.st != h->st || cg.dnn != (h->acc_dnn_on ? 1 : 0))) {
@@ -1318,20 +1495,15 @@ tc_status multigrid(Handle* h) {
     if (use_graphs && cg.loop != nullptr) {
         // the whole convergence loop on the device; one host read per solve
         CK(cudaGraphLaunch(cg.loop, h->st));
-        TRY(sync_scalars(h));
-        q = h->hs->cyc_q;
-        const int st = h->hs->cyc_status;
-        const long long bodies = (st == TC_ERR_MG_CYCLES) ? q - 2 : q - 1;
-        tc_note_launch(cg.n_pre + (bodies > 0 ? bodies : 0) * cg.n_body);
-        if (h->hs->visit_timeout || st == TC_ERR_DEVICE_TIMEOUT) {
-            h->err = "fused smoother visit: neighbour wait exceeded its bound";
-            return TC_ERR_DEVICE_TIMEOUT;
+        TRY(sync_point(h, [h, &cg]() { return loop_result(h, cg.n_pre, cg.n_body); }));
+        copy_plane(h, h->SF, cur_err(h, 1));
+        if (rec) {
+            nn_field_to_img(h->st, h->lev[1].L, h->SF, h->rec_sf + (size_t)h->rec_count * img);
+            h->rec_count++;
         }
-        if (st == TC_ERR_MG_RESIDUAL) return TC_ERR_MG_RESIDUAL;
-        if (st == TC_ERR_MG_CYCLES) { h->last_cycles = q; return TC_ERR_MG_CYCLES; }
-        if (st != 0) return (tc_status)st;
+        return TC_OK;
     }
-    for (; !(use_graphs && cg.loop != nullptr);) {
+    for (;;) {
         if (nonN) {
             strain_from_correction();
             TRY(level_setup());
@@ -1376,11 +1548,15 @@ tc_status multigrid(Handle* h) {
 
 void compute_velocities(Handle* h) { launch_velocities(h->st, h->L1, h->P, h->SF, h->u, h->w); }
 
-tc_status check_flags(Handle* h) {
-    TRY(sync_scalars(h));
+// the tracer and RK2 stop tests of the reference (energy.f90) on the last read
+tc_status flags_result(Handle* h) {
     if (h->hs->flag_outside) return TC_ERR_TRACER_OUTSIDE;
     if (h->hs->flag_rk2) return TC_ERR_RK2_STABILITY;
     return TC_OK;
+}
+
+tc_status check_flags(Handle* h) {
+    return sync_point(h, [h]() { return flags_result(h); });
 }
 
 tc_status update_velocities(Handle* h) {
@@ -1448,10 +1624,15 @@ tc_status energy_time(Handle* h) {
     if (h->p.equalize == 1) TRY(equalize_tracers(h));
     for (int t = 0; t < h->ntype; t++) copy_plane(h, h->C0[t], h->Cnew[t]);
     copy_plane(h, h->T0, tt ? h->Tratio : h->T);
-    if (trc && h->ntr > 0 && h->p.tracer_sort_interval > 0 && h->tstep % h->p.tracer_sort_interval == 0)
-        sort_tracers(h);
-    if (trc) { std::swap(h->rtr0, h->rtr); std::swap(h->str0, h->str); }
-    if (tt) std::swap(h->Ttr0, h->Ttr);
+    if (sorts_this_step(h)) TRY(sort_tracers(h));
+    // the step's start positions (and temperatures); rtr, str and Ttr are
+    // the RK accumulators, which stage 1 writes first
+    const size_t nb = sizeof(double) * (size_t)h->ntr;
+    if (trc && h->ntr > 0) {
+        CK(cudaMemcpyAsync(h->rtr0, h->rtr, nb, cudaMemcpyDeviceToDevice, h->st));
+        CK(cudaMemcpyAsync(h->str0, h->str, nb, cudaMemcpyDeviceToDevice, h->st));
+    }
+    if (tt && h->ntr > 0) CK(cudaMemcpyAsync(h->Ttr0, h->Ttr, nb, cudaMemcpyDeviceToDevice, h->st));
     auto derivs = [&]() {
         launch_derivatives(h->st, h->L1, h->P, h->u, h->du);
         launch_derivatives(h->st, h->L1, h->P, h->w, h->dw);
@@ -1531,19 +1712,29 @@ tc_status energy_time(Handle* h) {
     if (trc) TRY(tracers_to_corners(h, h->rtr, h->str, true, tt ? h->Ttr : nullptr, h->T0));
     if (tt) copy_plane(h, h->T, h->Tratio);
     else TRY(smoother_time_T(h, h->T));
-    TRY(check_flags(h));
-    h->dt = h->hs->dt;
-    return TC_OK;
+    return sync_point(h, [h]() {
+        TRY(flags_result(h));
+        h->dt = h->hs->dt;
+        return TC_OK;
+    });
 }
 
 // stats (basics.f90:236-324)
+tc_status stats_row(Handle* h, tc_stats_row* row);
+
 tc_status stats(Handle* h, tc_stats_row* row) {
-    std::memset(row, 0, sizeof(*row));
-    const double asp = h->p.aspect;
     launch_strain(h->st, h->L1, h->P, h->u, h->w, h->strain);
     launch_stats(h->st, h->L1, h->P, h->kent, h->T, h->u, h->w, h->conduct, cur_vis(h, 1), h->strain, h->Cnew,
                  h->nempty, h->rows, h->ds);
-    TRY(sync_scalars(h));
+    TRY(sync_point(h, [h]() { return stats_row(h, &h->stats_row); }));
+    if (!h->capturing && row) *row = h->stats_row;
+    return TC_OK;
+}
+
+// the stats.dat row from the last read of the device scalars
+tc_status stats_row(Handle* h, tc_stats_row* row) {
+    std::memset(row, 0, sizeof(*row));
+    const double asp = h->p.aspect;
     const DevScalars& s = *h->hs;
     if (h->p.comp == 1) {
         for (int t = 0; t < h->ntype; t++) row->Cavg[t] = s.integ[t] / asp;
@@ -2018,6 +2209,135 @@ tc_status upload(Handle* h, const double* T, const double* Cn, const double* SF,
     return TC_OK;
 }
 
+// ---------------------------------------------------------------------------
+// the whole timestep as one graph launch
+// ---------------------------------------------------------------------------
+void drop_step_graphs(Handle* h) {
+    for (auto& kv : h->step_graphs) {
+        if (kv.second && kv.second->ge) cudaGraphExecDestroy(kv.second->ge);
+        delete kv.second;
+    }
+    h->step_graphs.clear();
+    h->epoch++;
+}
+
+// The step can run as one captured graph: every loop of it on the device,
+// no host branch on a device value, and everything the first step builds
+// (cycle and filter graphs, coarse factors, sub-cycle tables) in place.
+// `own`: the handle's own step graph (tc_set_step_graph) rather than an
+// ensemble's.
+bool step_graph_ready(const Handle* h, bool own) {
+    if ((own && !h->step_graph) || h->step_graph_failed || !h->uploaded || h->st == nullptr) return false;
+    if (h->no_graphs || h->no_device_loop || h->flt_failed || !h->flt_dev_state || h->wait_test) return false;
+    if (h->p.non_Newtonian == 1 || h->p.equalize == 1) return false;
+    if (h->p.learned_guess == 1 || h->p.learned_guess == 2) return false;
+    if (h->rec_raw && h->rec_count < h->rec_cap) return false;
+    if (h->tstep < 1 || h->time == 0.0 || !h->lu_valid || (h->sub_on && !h->sub_valid)) return false;
+    return h->graphs != nullptr && h->graphs->loop != nullptr;
+}
+
+// what a captured step needs before its capture begins (allocations are
+// not allowed inside one)
+tc_status step_graph_prepare(Handle* h) {
+    if (!h->hsnap) CK(cudaMallocHost((void**)&h->hsnap, sizeof(DevScalars) * kMaxSnap));
+    if (!h->body_st) CK(cudaStreamCreateWithFlags(&h->body_st, cudaStreamNonBlocking));
+    return TC_OK;
+}
+
+// One step (multigrid, velocities, stats, energy_time; the order of tc_step)
+// enqueued on h->st, which is capturing; the host work that follows each
+// launch goes to sg->post, the kernels outside the WHILE bodies to
+// sg->n_static.
+tc_status capture_step(Handle* h, StepGraph* sg) {
+    const long long before = t_launches;
+    h->deferred.clear();
+    h->nsnap = 0;
+    h->enq_err = cudaSuccess;
+    h->capturing = true;
+    tc_status s = multigrid(h);
+    if (s == TC_OK) {
+        compute_velocities(h);
+        s = stats(h, nullptr);
+    }
+    if (s == TC_OK) s = energy_time(h);
+    h->capturing = false;
+    sg->n_static = t_launches - before;
+    g_launches.fetch_sub(sg->n_static);
+    t_launches = before;
+    sg->post = std::move(h->deferred);
+    h->deferred.clear();
+    if (s == TC_OK && h->enq_err != cudaSuccess) s = TC_ERR_CUDA;
+    h->enq_err = cudaSuccess;
+    return s;
+}
+
+tc_status build_step_graph(Handle* h, StepGraph** out) {
+    TRY(step_graph_prepare(h));
+    StepGraph* sg = new StepGraph();
+    if (cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        delete sg;
+        cudaGetLastError();
+        return TC_ERR_CUDA;
+    }
+    tc_status s = capture_step(h, sg);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (s == TC_OK && (e != cudaSuccess || g == nullptr)) s = TC_ERR_CUDA;
+    if (s == TC_OK && cudaGraphInstantiate(&sg->ge, g, 0) != cudaSuccess) s = TC_ERR_CUDA;
+    if (g) cudaGraphDestroy(g);
+    if (s != TC_OK) {
+        delete sg;
+        cudaGetLastError();
+        return s;
+    }
+    *out = sg;
+    return TC_OK;
+}
+
+// The host's part of a step after its graph ran: the deferred reads in the
+// eager step's order (the first error stops them, as it stops that step),
+// then the outputs and the clock.
+tc_status finish_step(Handle* h, const StepGraph& sg, tc_stats_row* row, int32_t* cycles, double* dt_out) {
+    tc_status s = TC_OK;
+    for (const auto& f : sg.post) {
+        s = f();
+        if (s != TC_OK) break;
+    }
+    h->graph_steps++;
+    if (cycles) *cycles = (s == TC_OK || h->cycles_acc > 0) ? h->cycles_acc : h->last_cycles;
+    if (s != TC_OK) return s;
+    if (row) *row = h->stats_row;
+    if (dt_out) *dt_out = h->dt;
+    h->time = h->time + h->dt;
+    h->tstep += 1;
+    return TC_OK;
+}
+
+// tc_step as one graph launch: the step's graph for this sort flag (captured
+// on first use), one synchronisation, then the deferred host work.  False in
+// *ran when the step must run eagerly (a capture the driver refused).
+tc_status step_as_graph(Handle* h, tc_stats_row* row, int32_t* cycles, double* dt_out, bool* ran) {
+    *ran = false;
+    const int key = sorts_this_step(h) ? 1 : 0;
+    StepGraph* sg = nullptr;
+    auto it = h->step_graphs.find(key);
+    if (it != h->step_graphs.end()) {
+        sg = it->second;
+    } else if (build_step_graph(h, &sg) == TC_OK) {
+        h->step_graphs[key] = sg;
+    } else {
+        h->step_graph_failed = true;
+        return TC_OK;
+    }
+    *ran = true;
+    h->cycles_acc = 0;
+    CK(cudaGraphLaunch(sg->ge, h->st));
+    tc_note_launch(sg->n_static);
+    CK(cudaStreamSynchronize(h->st));
+    CK(cudaGetLastError());
+    return finish_step(h, *sg, row, cycles, dt_out);
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -2062,6 +2382,83 @@ tc_status graph_time(Handle* h, F&& fn, double* ms_out) {
     cudaGraphExecDestroy(ge);
     *ms_out = ms;
     return TC_OK;
+}
+}  // namespace
+
+// An ensemble whose timestep is one graph launch: the cases' captured steps
+// as independent branches of one graph (fork from a root stream onto every
+// case's stream, join back), cached by the case list, each case's
+// configuration epoch and sort flag.
+struct tc_ensemble {
+    struct Entry {
+        std::vector<tc_handle*> hs;
+        std::vector<long long> epochs;
+        std::vector<int> sorts;
+        cudaGraphExec_t ge = nullptr;
+        std::vector<StepGraph> cases;
+        long long n_static = 0;
+    };
+    int nthreads = 1;
+    int device = 0;
+    cudaStream_t root = nullptr;
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    std::vector<Entry*> cache;  // most recent last, at most kCache
+    long long graph_steps = 0, eager_steps = 0;
+    bool failed = false;
+    static constexpr size_t kCache = 4;
+};
+
+namespace {
+void drop_entry(tc_ensemble::Entry* en) {
+    if (en->ge) cudaGraphExecDestroy(en->ge);
+    delete en;
+}
+
+tc_ensemble::Entry* build_entry(tc_ensemble* e, tc_handle* const* hs, int n) {
+    auto* en = new tc_ensemble::Entry();
+    en->hs.assign(hs, hs + n);
+    en->cases.resize((size_t)n);
+    for (int i = 0; i < n; i++) {
+        Handle* h = &hs[i]->h;
+        if (step_graph_prepare(h) != TC_OK) {
+            drop_entry(en);
+            return nullptr;
+        }
+        en->epochs.push_back(h->epoch);
+        en->sorts.push_back(sorts_this_step(h) ? 1 : 0);
+    }
+    while (e->join.size() < (size_t)n) {
+        cudaEvent_t ev = nullptr;
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) {
+            drop_entry(en);
+            return nullptr;
+        }
+        e->join.push_back(ev);
+    }
+    if (cudaStreamBeginCapture(e->root, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        drop_entry(en);
+        return nullptr;
+    }
+    bool ok = cudaEventRecord(e->fork, e->root) == cudaSuccess;
+    for (int i = 0; i < n && ok; i++) {
+        Handle* h = &hs[i]->h;
+        ok = cudaStreamWaitEvent(h->st, e->fork, 0) == cudaSuccess && capture_step(h, &en->cases[(size_t)i]) == TC_OK;
+        en->n_static += en->cases[(size_t)i].n_static;
+        ok = ok && cudaEventRecord(e->join[(size_t)i], h->st) == cudaSuccess &&
+             cudaStreamWaitEvent(e->root, e->join[(size_t)i], 0) == cudaSuccess;
+    }
+    cudaGraph_t g = nullptr;
+    const cudaError_t ee = cudaStreamEndCapture(e->root, &g);
+    ok = ok && ee == cudaSuccess && g != nullptr && cudaGraphInstantiate(&en->ge, g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        drop_entry(en);
+        return nullptr;
+    }
+    return en;
 }
 }  // namespace
 
@@ -2121,6 +2518,7 @@ tc_status tc_attach_net(tc_handle* H, tc_net* net) {
         if (!h->nn_raw) TRY(dalloc_t(h, &h->nn_raw, (size_t)3 * h->nx * h->nz));
     }
     h->net = n;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2131,6 +2529,7 @@ tc_status tc_record_solves(tc_handle* H, float* raw, float* sf_new, int32_t capa
     h->rec_sf = capacity > 0 ? sf_new : nullptr;
     h->rec_cap = capacity;
     h->rec_count = 0;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2158,6 +2557,9 @@ tc_status tc_destroy(tc_handle* H) {
     }
     for (auto& kv : h->flt_graphs)
         if (kv.second) cudaGraphExecDestroy(kv.second);
+    drop_step_graphs(h);
+    if (h->hsnap) cudaFreeHost(h->hsnap);
+    if (h->body_st) cudaStreamDestroy(h->body_st);
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     delete H;
     return TC_OK;
@@ -2188,6 +2590,7 @@ tc_status tc_set_stream(tc_handle* H, void* stream) {
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     h->own_stream = false;
     h->st = (cudaStream_t)stream;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2278,6 +2681,11 @@ tc_status tc_energy_time(tc_handle* H, double* dt_out) {
 tc_status tc_step(tc_handle* H, tc_stats_row* row, int32_t* cycles, double* dt_out) {
     if (!H) return TC_ERR_ARG;
     Handle* h = &H->h;
+    if (step_graph_ready(h, true)) {
+        bool ran = false;
+        const tc_status s = step_as_graph(h, row, cycles, dt_out, &ran);
+        if (ran || s != TC_OK) return s;
+    }
     h->cycles_acc = 0;
     tc_status s = multigrid(h);
     if (cycles) *cycles = h->last_cycles;
@@ -2388,6 +2796,7 @@ tc_status tc_autotune(tc_handle* H, int32_t* choices) {
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
     if (cg.loop) cudaGraphExecDestroy(cg.loop);
     cg.l1 = cg.rest = cg.loop = nullptr;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2420,6 +2829,7 @@ tc_status tc_set_launch_shapes(tc_handle* H, const int32_t* choices) {
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
     if (cg.loop) cudaGraphExecDestroy(cg.loop);
     cg.l1 = cg.rest = cg.loop = nullptr;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2450,6 +2860,108 @@ tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc
         if (first == TC_OK && st[(size_t)i] != TC_OK) first = st[(size_t)i];
     }
     return first;
+}
+
+tc_status tc_set_step_graph(tc_handle* H, int32_t on) {
+    if (!H) return TC_ERR_ARG;
+    Handle* h = &H->h;
+    h->step_graph = (on != 0);
+    h->step_graph_failed = false;
+    if (!h->step_graph) drop_step_graphs(h);
+    return TC_OK;
+}
+
+tc_status tc_step_graph_info(const tc_handle* H, int64_t* graph_steps, int32_t* state) {
+    if (!H) return TC_ERR_ARG;
+    const Handle* h = &H->h;
+    if (graph_steps) *graph_steps = h->graph_steps;
+    if (state) *state = h->step_graph_failed ? 2 : (h->step_graph ? 1 : 0);
+    return TC_OK;
+}
+
+tc_status tc_ensemble_create(int32_t nthreads, tc_ensemble** out) {
+    if (!out || nthreads < 1) return TC_ERR_ARG;
+    auto* e = new tc_ensemble();
+    e->nthreads = nthreads;
+    cudaGetDevice(&e->device);
+    if (cudaStreamCreateWithFlags(&e->root, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess) {
+        tc_ensemble_destroy(e);
+        return TC_ERR_CUDA;
+    }
+    *out = e;
+    return TC_OK;
+}
+
+tc_status tc_ensemble_run(tc_ensemble* e, tc_handle* const* hs, int32_t n, tc_stats_row* rows, int32_t* cycles,
+                          double* dts, tc_status* status) {
+    if (!e || !hs || n < 1) return TC_ERR_ARG;
+    bool ready = !e->failed;
+    for (int i = 0; i < n; i++) {
+        if (!hs[i]) return TC_ERR_ARG;
+        ready = ready && step_graph_ready(&hs[i]->h, false) && hs[i]->h.device == e->device;
+    }
+    tc_ensemble::Entry* en = nullptr;
+    if (ready) {
+        const std::vector<tc_handle*> key(hs, hs + n);
+        for (auto* c : e->cache) {
+            if (c->hs != key) continue;
+            bool same = true;
+            for (int i = 0; i < n && same; i++)
+                same = c->epochs[(size_t)i] == hs[i]->h.epoch &&
+                       c->sorts[(size_t)i] == (sorts_this_step(&hs[i]->h) ? 1 : 0);
+            if (same) en = c;
+        }
+        if (!en) {
+            cudaSetDevice(e->device);
+            en = build_entry(e, hs, n);
+            if (en) {
+                e->cache.push_back(en);
+                if (e->cache.size() > tc_ensemble::kCache) {
+                    drop_entry(e->cache.front());
+                    e->cache.erase(e->cache.begin());
+                }
+            } else {
+                e->failed = true;  // the driver refused the capture: the thread pool from now on
+            }
+        }
+    }
+    if (!en) {
+        e->eager_steps++;
+        return tc_ensemble_step(hs, n, e->nthreads, rows, cycles, dts, status);
+    }
+    for (int i = 0; i < n; i++) hs[i]->h.cycles_acc = 0;
+    cudaSetDevice(e->device);
+    if (cudaGraphLaunch(en->ge, e->root) != cudaSuccess) return TC_ERR_CUDA;
+    tc_note_launch(en->n_static);
+    if (cudaStreamSynchronize(e->root) != cudaSuccess || cudaGetLastError() != cudaSuccess) return TC_ERR_CUDA;
+    tc_status first = TC_OK;
+    for (int i = 0; i < n; i++) {
+        const tc_status s = finish_step(&hs[i]->h, en->cases[(size_t)i], rows ? &rows[i] : nullptr,
+                                        cycles ? &cycles[i] : nullptr, dts ? &dts[i] : nullptr);
+        if (status) status[i] = s;
+        if (first == TC_OK && s != TC_OK) first = s;
+    }
+    e->graph_steps++;
+    return first;
+}
+
+tc_status tc_ensemble_info(const tc_ensemble* e, int64_t* graph_steps, int64_t* eager_steps) {
+    if (!e) return TC_ERR_ARG;
+    if (graph_steps) *graph_steps = e->graph_steps;
+    if (eager_steps) *eager_steps = e->eager_steps;
+    return TC_OK;
+}
+
+tc_status tc_ensemble_destroy(tc_ensemble* e) {
+    if (!e) return TC_OK;
+    if (e->root) cudaStreamSynchronize(e->root);
+    for (auto* c : e->cache) drop_entry(c);
+    for (auto ev : e->join) cudaEventDestroy(ev);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->root) cudaStreamDestroy(e->root);
+    delete e;
+    return TC_OK;
 }
 
 tc_status tc_step_host(tc_handle* H, double* T, double* Cnew, double* SF, double* rtr, double* str,
@@ -2589,6 +3101,7 @@ tc_status tc_debug_wait_test(tc_handle* H, int32_t on) {
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
     if (cg.loop) cudaGraphExecDestroy(cg.loop);
     cg.l1 = cg.rest = cg.loop = nullptr;
+    drop_step_graphs(h);
     return TC_OK;
 }
 
@@ -2602,6 +3115,7 @@ tc_status tc_debug_sweep_fields(tc_handle* H, int32_t fields) {
     if (cg.rest) cudaGraphExecDestroy(cg.rest);
     if (cg.loop) cudaGraphExecDestroy(cg.loop);
     cg.l1 = cg.rest = cg.loop = nullptr;
+    drop_step_graphs(h);
     return TC_OK;
 }
 

@@ -75,7 +75,7 @@ struct DevScalars {
     int    cyc_q;            // W-cycle count of the device-side multigrid loop (k_loop.cu)
     int    cyc_status;       // its stop reason: 0 converged, else the tc_status
     int    never_set;        // stays 0: the word the timeout-path tests wait on
-    int    pad2;
+    int    net_fail;         // the network's bounded-wait flag, copied after each forward pass
     // windowed correction (cycle_correction 3/4, k_accel.cu): coefficients of
     // the last correction (newest change first, the network's direction
     // last), stored changes, slot of the newest, directions used

@@ -1,12 +1,16 @@
-"""Ensemble of independent cases stepped together (tc_ensemble_step).
+"""Ensemble of independent cases stepped together (tc_ensemble_run,
+tc_ensemble_step).
 
-Each case is its own handle on its own CUDA stream; one ensemble step runs
-tc_step on every case with the cases' work issued concurrently by a pool of
-host threads, so the GPU executes the cases side by side (the small cases'
-latency-bound smoother launches fill SMs the large cases leave idle).  Each
-case may carry the learned initial guess (its own network instance, since a
-network holds one image's activations); with a network the cases use the
-learned start and the network's direction in their correction.
+Each case is its own handle on its own CUDA stream.  With graph=True (the
+default) one ensemble step is one CUDA graph launch: every case's captured
+timestep is a branch of one graph, so the GPU executes the cases side by
+side (the small cases' latency-bound smoother launches fill SMs the large
+cases leave idle) with one host synchronisation per step; the first step,
+and any step a case is not ready to capture, runs tc_step on every case
+from a pool of host threads instead.  Each case may carry the learned
+initial guess (its own network instance, since a network holds one image's
+activations); with a network the cases use the learned start and the
+network's direction in their correction.
 """
 from __future__ import annotations
 
@@ -43,9 +47,16 @@ def case_params(i: int, seed: int = 1):
 
 class Ensemble:
     def __init__(self, params: list, seeds: list | None = None, weights: str | None = None,
-                 autotune: bool = True):
+                 autotune: bool = True, graph: bool = True, nthreads: int | None = None):
         from . import learned
         self.L = load_library()
+        self.graph = None
+        if graph:
+            e = C.c_void_p()
+            r = self.L.tc_ensemble_create(nthreads or len(params), C.byref(e))
+            if r != 0:
+                raise TracerError(r, "tc_ensemble_create")
+            self.graph = e
         self.sims = []
         self.nets = []
         self.params = params
@@ -98,8 +109,12 @@ class Ensemble:
         cyc = (C.c_int32 * n)()
         dts = (C.c_double * n)()
         st = (C.c_int32 * n)()
-        r = self.L.tc_ensemble_step(hs, n, nthreads or n, C.cast(rows, C.c_void_p), C.cast(cyc, C.c_void_p),
-                                    C.cast(dts, C.c_void_p), C.cast(st, C.c_void_p))
+        if self.graph is not None:
+            r = self.L.tc_ensemble_run(self.graph, hs, n, C.cast(rows, C.c_void_p), C.cast(cyc, C.c_void_p),
+                                       C.cast(dts, C.c_void_p), C.cast(st, C.c_void_p))
+        else:
+            r = self.L.tc_ensemble_step(hs, n, nthreads or n, C.cast(rows, C.c_void_p), C.cast(cyc, C.c_void_p),
+                                        C.cast(dts, C.c_void_p), C.cast(st, C.c_void_p))
         if r != 0 and strict:
             bad = [(idx[j], STATUS.get(st[j], st[j])) for j in range(n) if st[j] != 0]
             raise TracerError(r, f"tc_ensemble_step: {bad}")
@@ -111,7 +126,18 @@ class Ensemble:
             rows_o[i], cyc_o[i], dt_o[i] = rows[j].as_dict(), cyc[j], dts[j]
         return rows_o, cyc_o, dt_o
 
+    def graph_info(self):
+        """(steps run as one graph launch, steps run by the thread pool)."""
+        if self.graph is None:
+            return 0, 0
+        g = C.c_int64(0); e = C.c_int64(0)
+        self.L.tc_ensemble_info(self.graph, C.byref(g), C.byref(e))
+        return g.value, e.value
+
     def close(self):
+        if self.graph is not None:
+            self.L.tc_ensemble_destroy(self.graph)
+            self.graph = None
         for s in self.sims:
             s.close()
         for nt in self.nets:
