@@ -9,9 +9,11 @@
 // :32-62, compute_velocities :532-551), composition.f90 (enforceBCs_comp
 // :792-803, velocityBCs :806-836, compute_derivatives :900-919) and basics.f90
 // (stats :236-324, integrate2D / integrate1Dx / integrate1Dz :341-403).
-// Uniform grid metrics: xr=zs=1, xrr=zss=0.  Every kernel keeps the
-// reference's operation order (no FMA contraction), so with identical inputs
-// its output equals the CPU restatement bit for bit.
+// On a uniform grid the metrics are xr = zs = 1, xrr = zss = 0 and the
+// kernels skip them; on a stretched grid (P.M.on) they apply them as the
+// reference does.  Every kernel keeps the reference's operation order (no
+// FMA contraction), so with identical inputs its output equals the CPU
+// restatement bit for bit.
 #include "tc_device.cuh"
 
 // enforceBCs (energy.f90:455-475): every ghost / boundary-row value as a
@@ -95,6 +97,19 @@ __device__ __forceinline__ double lap5(const double* __restrict__ T, size_t x, s
     double Tss = (T[x - ld] + -2.0 * c + T[x + ld]) / ds2;
     return Trr + Tss;
 }
+// smoother_space (smoother.f90:122-140) at node (i, k), stretched or uniform
+__device__ __forceinline__ double smoother_space(const Phys& P, const double* __restrict__ T, size_t x, size_t ld,
+                                                 int i, int k) {
+    if (!P.M.on) return lap5(T, x, ld, P.dr2, P.ds2);
+    const double c = T[x];
+    const double Tr = (-0.5 * T[x - 1] + 0.5 * T[x + 1]) / P.dr, Ts = (-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds;
+    const double Trr = (T[x - 1] + -2.0 * c + T[x + 1]) / P.dr2, Tss = (T[x - ld] + -2.0 * c + T[x + ld]) / P.ds2;
+    const double x1 = mt(P.M.xr, i), z1 = mt(P.M.zs, k);
+    const double Tx = Tr / x1, Tz = Ts / z1;
+    const double Txx = (Trr - Tx * mt(P.M.xrr, i)) / (x1 * x1);
+    const double Tzz = (Tss - Tz * mt(P.M.zss, k)) / (z1 * z1);
+    return Txx + Tzz;
+}
 
 // one Richardson step of smoother_time_T (smoother.f90:343-377)
 __global__ void k_smooth_T(Lay L, Phys P, Range2 r, const double* __restrict__ Tin, double* __restrict__ Tout,
@@ -102,7 +117,7 @@ __global__ void k_smooth_T(Lay L, Phys P, Range2 r, const double* __restrict__ T
     RANGE_IK(r);
     if (!inr) return;
     size_t x = IX(L, i, k);
-    double temp = lap5(Tin, x, (size_t)L.ld, P.dr2, P.ds2);
+    double temp = smoother_space(P, Tin, x, (size_t)L.ld, i, k);
     double d = dts[x] * P.courantT;
     Tout[x] = Tin[x] + d * temp;
 }
@@ -119,7 +134,7 @@ __global__ void k_smooth_C(Lay L, Phys P, Range2 r, const double* __restrict__ C
     if (!inr) return;
     if (cdev) c = *cdev;  // the factor the device-side filter loop chose
     size_t x = IX(L, i, k);
-    double temp = lap5(Cin, x, (size_t)L.ld, P.dr2, P.ds2);
+    double temp = smoother_space(P, Cin, x, (size_t)L.ld, i, k);
     double d = dts[x] * P.courantC;
     double v = Cin[x] + c * d * temp;
     if (v < 0.0) v = 0.0;
@@ -168,11 +183,13 @@ void launch_conductivity(cudaStream_t s, const Lay& L, const Phys& P, const doub
 __device__ __forceinline__ double uf_(const Lay& L, const Phys& P, const double* SF, int i, int k) {
     const size_t ld = (size_t)L.ld;
     size_t x = IX(L, i, k);
-    return (-0.5 * SF[x - ld] + 0.5 * SF[x + ld]) / P.ds;
+    const double SFs = (-0.5 * SF[x - ld] + 0.5 * SF[x + ld]) / P.ds;
+    return P.M.on ? SFs / mt(P.M.zs, k) : SFs;
 }
 __device__ __forceinline__ double wf_(const Lay& L, const Phys& P, const double* SF, int i, int k) {
     size_t x = IX(L, i, k);
-    return -((-0.5 * SF[x - 1] + 0.5 * SF[x + 1]) / P.dr);
+    const double SFr = (-0.5 * SF[x - 1] + 0.5 * SF[x + 1]) / P.dr;
+    return -(P.M.on ? SFr / mt(P.M.xr, i) : SFr);
 }
 __global__ void k_velocities(Lay L, Phys P, Range2 r, const double* __restrict__ SF, double* __restrict__ u,
                              double* __restrict__ w) {
@@ -233,7 +250,17 @@ __global__ void k_stab(Lay L, Phys P, Range2 r, const double* __restrict__ cd, c
     double v = -INFINITY;
     if (inr) {
         size_t x = IX(L, i, k);
-        if (which == 0) {
+        if (P.M.on) {
+            // eigA / eigD on a stretched grid (energy.f90:686-706)
+            const double x1 = mt(P.M.xr, i), z1 = mt(P.M.zs, k);
+            if (which == 0) {
+                double ax = -(cd[x] * mt(P.M.xrr, i) / mt(P.M.xr3, i)) - u[x] / x1 + cr[x] / (x1 * x1);
+                double az = -(cd[x] * mt(P.M.zss, k) / mt(P.M.zs3, k)) - w[x] / z1 + cs[x] / (z1 * z1);
+                v = fabs(ax) * P.Tr_max + fabs(az) * P.Ts_max;
+            } else {
+                v = cd[x] * (fabs(P.Trr_max / (x1 * x1)) + fabs(P.Tss_max / (z1 * z1)));
+            }
+        } else if (which == 0) {
             double ax = -(cd[x] * 0.0) - u[x] + cr[x];
             double az = -(cd[x] * 0.0) - w[x] + cs[x];
             v = fabs(ax) * P.Tr_max + fabs(az) * P.Ts_max;
@@ -298,7 +325,19 @@ __global__ void k_energy(Lay L, Phys P, Range2 r, int stage, const double* __res
         heat = P.H * (1.0 - sC);
         for (int j = 0; j < P.ntype; j++) heat = P.Htype[j] * Cv.p[j][x] + heat;
     }
-    double temp = cd[x] * (Trr + Tss) + (kx * Tr + kz * Ts) - u[x] * Tr - w[x] * Ts + heat;
+    double temp;
+    if (P.M.on) {
+        // energy_space on a stretched grid (energy.f90:60-80)
+        const double x1 = mt(P.M.xr, i), z1 = mt(P.M.zs, k);
+        kx = kx / x1;
+        kz = kz / z1;
+        const double Tx = Tr / x1, Tz = Ts / z1;
+        const double Txx = (Trr - Tx * mt(P.M.xrr, i)) / (x1 * x1);
+        const double Tzz = (Tss - Tz * mt(P.M.zss, k)) / (z1 * z1);
+        temp = cd[x] * (Txx + Tzz) + (kx * Tx + kz * Tz) - u[x] * Tx - w[x] * Tz + heat;
+    } else {
+        temp = cd[x] * (Trr + Tss) + (kx * Tr + kz * Ts) - u[x] * Tr - w[x] * Ts + heat;
+    }
     const double dt = ds->dt;
     if (stage == 1) {
         T[x] = temp;
@@ -335,6 +374,11 @@ __global__ void k_strain(Lay L, Phys P, Range2 r, const double* __restrict__ u, 
     double us = (-0.5 * u[x - ld] + 0.5 * u[x + ld]) / P.ds;
     double wr = (-0.5 * w[x - 1] + 0.5 * w[x + 1]) / P.dr;
     double ws = (-0.5 * w[x - ld] + 0.5 * w[x + ld]) / P.ds;
+    if (P.M.on) {
+        // ux = ur / xr, uz = us / zs, wx = wr / xr, wz = ws / zs (momentum.f90:45-48)
+        const double x1 = mt(P.M.xr, i), z1 = mt(P.M.zs, k);
+        ur = ur / x1; us = us / z1; wr = wr / x1; ws = ws / z1;
+    }
     double q = 0.5 * (2.0 * (ur * ur + ws * ws) + (us + wr) * (us + wr));
     st[x] = sqrt(q);
 }
@@ -398,10 +442,13 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_rows(Lay L, Phys P, cons
         __syncthreads();
         if (t < NROWINT && stat_row_active(P, t)) {
             double fprev = fv[t][0];
+            double xprev = P.M.on ? mt(P.M.xr, c0) : 1.0;
             for (int j = 0; j < n; j++) {
                 const double fn = fv[t][j + 1];
-                fint = fint + 0.5 * (fprev * 1.0 + fn * 1.0) * P.dr;
+                const double xn = P.M.on ? mt(P.M.xr, c0 + j + 1) : 1.0;
+                fint = fint + 0.5 * (fprev * xprev + fn * xn) * P.dr;
                 fprev = fn;
+                xprev = xn;
             }
         }
         __syncthreads();
@@ -443,7 +490,8 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_final(Lay L, Phys P, int
             if (active) {
                 for (int j = 0; j < n; j++) {
                     if (c0 + j < k0) continue;
-                    fint = fint + 0.5 * (fv[q][j] * 1.0 + fv[q][j + 1] * 1.0) * P.ds;
+                    const double za = P.M.on ? mt(P.M.zs, c0 + j) : 1.0, zb = P.M.on ? mt(P.M.zs, c0 + j + 1) : 1.0;
+                    fint = fint + 0.5 * (fv[q][j] * za + fv[q][j + 1] * zb) * P.ds;
                 }
             }
             __syncthreads();
@@ -458,6 +506,7 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_final(Lay L, Phys P, int
     // thread j < 4 keeps sum j
     {
         const bool rat = (P.RaT != 0.0);
+        const double zs_top = P.M.on ? mt(P.M.zs, nz) : 1.0, zs_bot = P.M.on ? mt(P.M.zs, 0) : 1.0;
         double acc = 0.0;
         for (int c0 = 0; c0 < nx; c0 += kStatCH) {
             const int n = min(kStatCH, nx - c0);
@@ -469,18 +518,21 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_final(Lay L, Phys P, int
                     v = u[x] * u[x] + w[x] * w[x];
                 } else if (rat && q == 1) {
                     const size_t x = IX(L, i, nz);
-                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0);
+                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / zs_top);
                 } else if (rat && q == 2) {
                     v = T[IX(L, i, 0)];
                 } else if (rat && q == 3) {
                     const size_t x = IX(L, i, 0);
-                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / 1.0);
+                    v = -cd[x] * ((-0.5 * T[x - ld] + 0.5 * T[x + ld]) / P.ds / zs_bot);
                 }
                 fv[q][e % (n + 1)] = v;
             }
             __syncthreads();
             if (t < 4 && (t == 0 || rat)) {
-                for (int j = 0; j < n; j++) acc = acc + 0.5 * (fv[t][j] * 1.0 + fv[t][j + 1] * 1.0) * P.dr;
+                for (int j = 0; j < n; j++) {
+                    const double xa = P.M.on ? mt(P.M.xr, c0 + j) : 1.0, xb = P.M.on ? mt(P.M.xr, c0 + j + 1) : 1.0;
+                    acc = acc + 0.5 * (fv[t][j] * xa + fv[t][j + 1] * xb) * P.dr;
+                }
             }
             __syncthreads();
         }
@@ -488,10 +540,11 @@ __global__ void __launch_bounds__(kStatThreads) k_stats_final(Lay L, Phys P, int
     }
     if (t == 0 && P.RaT != 0.0) {
         auto dz = [&](int i, int kk) { size_t x = IX(L, i, kk); return -0.5 * T[x - ld] + 0.5 * T[x + ld]; };
-        ds->integ[15] = -(cd[IX(L, 0, nz)] * dz(0, nz)) / P.ds / 1.0;
-        ds->integ[16] = -(cd[IX(L, nx, nz)] * dz(nx, nz)) / P.ds / 1.0;
-        ds->integ[17] = -(cd[IX(L, nx, 0)] * dz(nx, 0)) / P.ds / 1.0;
-        ds->integ[18] = -(cd[IX(L, 0, 0)] * dz(0, 0)) / P.ds / 1.0;
+        const double zt = P.M.on ? mt(P.M.zs, nz) : 1.0, zb = P.M.on ? mt(P.M.zs, 0) : 1.0;
+        ds->integ[15] = -(cd[IX(L, 0, nz)] * dz(0, nz)) / P.ds / zt;
+        ds->integ[16] = -(cd[IX(L, nx, nz)] * dz(nx, nz)) / P.ds / zt;
+        ds->integ[17] = -(cd[IX(L, nx, 0)] * dz(nx, 0)) / P.ds / zb;
+        ds->integ[18] = -(cd[IX(L, 0, 0)] * dz(0, 0)) / P.ds / zb;
     }
     // top-row strain maximum (fmax is exact and order-free)
     double smax = -INFINITY;

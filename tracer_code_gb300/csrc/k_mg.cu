@@ -81,6 +81,51 @@ __device__ __forceinline__ void eig_pair(const LevConst& c, double v, double vx,
     eI = fabs(t5) + fabs(t6);
 }
 
+// eigI / eigR of a stretched-grid level at node (i, k) (iterative_solver.f90:
+// 750-857), the reference's expressions in its order; the level's node i is
+// fine node i * mf
+__device__ void eig_pair_metric(const LevConst& c, int i, int k, double v, double vx, double vz, double vxx,
+                                double vzz, double vxz, double& eR, double& eI) {
+    const int i1 = i * c.mf, k1 = k * c.mf;
+    const Metric& M = c.M;
+    const double x1 = mt(M.xr, i1), x2 = mt(M.xrr, i1), x3 = mt(M.xrrr, i1), x4 = mt(M.xrrrr, i1);
+    const double x13 = mt(M.xr3, i1), x14 = mt(M.xr4, i1);
+    const double z1 = mt(M.zs, k1), z2 = mt(M.zss, k1), z3 = mt(M.zsss, k1), z4 = mt(M.zssss, k1);
+    const double z13 = mt(M.zs3, k1), z14 = mt(M.zs4, k1);
+    const EigScaled& e = c.e;
+    {
+        const double Sr = e.Tr, Ss = e.Ts, Srr = 0.0, Sss = 0.0, Srrr = e.Trrr, Ssss = e.Tsss, Srrrr = 0.0,
+                     Sssss = 0.0, Srs = 0.0, Srrs = e.Trrs, Srss = e.Trss, Srrss = 0.0;
+        const double Sx = Sr / x1, Sz = Ss / z1;
+        const double Sxx = (Srr + fabs(Sx * x2)) / (x1 * x1);
+        const double Szz = (Sss + fabs(Sz * z2)) / (z1 * z1);
+        const double Sxxx = (Srrr + fabs(3.0 * Sxx * x1 * x2) + fabs(Sx * x3)) / fabs(x13);
+        const double Szzz = (Ssss + fabs(3.0 * Szz * z1 * z2) + fabs(Sz * z3)) / fabs(z13);
+        const double Sxxxx =
+            (Srrrr + fabs(6.0 * Sxxx * x2 * (x1 * x1)) + (fabs(3.0 * (x2 * x2) + 4.0 * x1 * x3) * fabs(Sxx)) +
+             fabs(Sx * x4)) / x14;
+        const double Szzzz =
+            (Sssss + fabs(6.0 * Szzz * z2 * (z1 * z1)) + (fabs(3.0 * (z2 * z2) + 4.0 * z1 * z3) * fabs(Szz)) +
+             fabs(Sz * z4)) / z14;
+        const double Sxz = Srs / x1 / z1;
+        const double Sxxz = (Srrs + fabs(Sxz * z1 * x2)) / fabs(z1) / (x1 * x1);
+        const double Sxzz = (Srss + fabs(Sxz * x1 * z2)) / fabs(x1) / (z1 * z1);
+        const double Sxxzz = (Srrss + fabs(Sxzz * x2) * (z1 * z1) + fabs(Sxxz * z2) * (x1 * x1) +
+                              fabs(Sxz * x2 * z2)) / ((x1 * z1) * (x1 * z1));
+        const double t1 = (vxx + vzz) * (Sxx + Szz);
+        const double t2 = v * (Sxxxx + Szzzz);
+        const double t3 = 2.0 * v * Sxxzz;
+        const double t4 = 4.0 * vxz * Sxz;
+        const double t5 = 2.0 * vx * (Sxxx + Sxzz);
+        const double t6 = 2.0 * vz * (Szzz + Sxxz);
+        eI = fabs(t1) + fabs(t2) + fabs(t3) + fabs(t4) + fabs(t5) + fabs(t6);
+    }
+    {
+        const double q[12] = {0.0, e.Trr, 0.0, e.Trrrr, 0.0, e.Tss, 0.0, e.Tssss, e.Trs, 0.0, 0.0, e.Trrss};
+        eR = -stream_op_metric(q, x1, x2, x3, x4, x13, x14, z1, z2, z3, z4, z13, z14, v, vx, vz, vxx, vzz, vxz);
+    }
+}
+
 __global__ void k_vis_grad(Lay L, LevConst c, Range2 r, const double* __restrict__ V, double* __restrict__ vx,
                            double* __restrict__ vz, double* __restrict__ vxx, double* __restrict__ vzz,
                            double* __restrict__ vxz, double* __restrict__ ratio, int do_eig, int ivis,
@@ -106,12 +151,28 @@ __global__ void k_vis_grad(Lay L, LevConst c, Range2 r, const double* __restrict
             } else {
                 vis_r = nr / c.dr; vis_rr = nrr / c.dr2; vis_s = ns / c.ds; vis_ss = nss / c.ds2; vis_rs = nrs / c.drds;
             }
-            vx[x] = vis_r; vz[x] = vis_s; vxx[x] = vis_rr; vzz[x] = vis_ss; vxz[x] = vis_rs;
-            if (do_eig) {
-                double eR, eI;
-                eig_pair(c, v0, vis_r, vis_s, vis_rr, vis_ss, vis_rs, eR, eI);
-                rat = fabs(eR / eI);
-                ratio[x] = rat;
+            if (c.M.on) {
+                // viscosity_gradients on a stretched grid (iterative_solver.f90:320-324)
+                const int ii = i * c.mf, kk = k * c.mf;
+                const double x1 = mt(c.M.xr, ii), x2 = mt(c.M.xrr, ii), z1 = mt(c.M.zs, kk), z2 = mt(c.M.zss, kk);
+                const double ax = vis_r / x1, az = vis_s / z1;
+                const double axx = (vis_rr - ax * x2) / (x1 * x1), azz = (vis_ss - az * z2) / (z1 * z1);
+                const double axz = vis_rs / x1 / z1;
+                vx[x] = ax; vz[x] = az; vxx[x] = axx; vzz[x] = azz; vxz[x] = axz;
+                if (do_eig) {
+                    double eR, eI;
+                    eig_pair_metric(c, i, k, v0, ax, az, axx, azz, axz, eR, eI);
+                    rat = fabs(eR / eI);
+                    ratio[x] = rat;
+                }
+            } else {
+                vx[x] = vis_r; vz[x] = vis_s; vxx[x] = vis_rr; vzz[x] = vis_ss; vxz[x] = vis_rs;
+                if (do_eig) {
+                    double eR, eI;
+                    eig_pair(c, v0, vis_r, vis_s, vis_rr, vis_ss, vis_rs, eR, eI);
+                    rat = fabs(eR / eI);
+                    ratio[x] = rat;
+                }
             }
         }
     }
@@ -139,7 +200,19 @@ __global__ void k_vis_smooth(Lay L, LevConst cc, Range2 r, const double* __restr
     // power-of-two spacings: the products equal the quotients exactly
     const double Trr = cc.recip ? nrr * cc.rdr2 : nrr / cc.dr2;
     const double Tss = cc.recip ? nss * cc.rds2 : nss / cc.ds2;
-    double temp = Trr + Tss;
+    double temp;
+    if (cc.M.on) {
+        // vis_space on a stretched grid (smoother.f90:142-164)
+        const double nr = -0.5 * Vin[x - 1] + 0.5 * Vin[x + 1], ns = -0.5 * Vin[x - ld] + 0.5 * Vin[x + ld];
+        const double Tr = cc.recip ? nr * cc.rdr : nr / cc.dr, Ts = cc.recip ? ns * cc.rds : ns / cc.ds;
+        const int i1 = i * cc.mf, k1 = k * cc.mf;
+        const double x1 = mt(cc.M.xr, i1), x2 = mt(cc.M.xrr, i1), z1 = mt(cc.M.zs, k1), z2 = mt(cc.M.zss, k1);
+        const double Tx = Tr / x1, Tz = Ts / z1;
+        const double Txx = (Trr - Tx * x2) / (x1 * x1), Tzz = (Tss - Tz * z2) / (z1 * z1);
+        temp = Txx + Tzz;
+    } else {
+        temp = Trr + Tss;
+    }
     double dts = dtv[x] * 0.99;
     double v = v0 + c * dts * temp;
     Vout[x] = v;
@@ -216,26 +289,47 @@ __global__ void k_level_coefs(Lay L, LevConst c, Range2 r, const double* __restr
                               const double* __restrict__ vz, const double* __restrict__ vxx,
                               const double* __restrict__ vzz, const double* __restrict__ vxz,
                               const double* __restrict__ ratio, double* __restrict__ dts, double* __restrict__ coef,
-                              double* __restrict__ cA, double* __restrict__ cB, double courant_stream, int cheb) {
+                              double* __restrict__ cA, double* __restrict__ cB, double courant_stream, int cheb,
+                              MetricFold mw) {
     RANGE_IK(r);
     if (!inr) return;
     size_t x = IX(L, i, k);
     double v = V[x], ax = vx[x], az = vz[x], axx = vxx[x], azz = vzz[x], axz = vxz[x];
-    if (dts) {
-        double eR, eI;
-        eig_pair(c, v, ax, az, axx, azz, axz, eR, eI);
-        dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
-    }
-    double g0 = axx - azz, g1 = v, g2 = 2.0 * v, g3 = 4.0 * axz, g4 = 2.0 * ax, g5 = 2.0 * az;
+    if (c.M.on) {
+        // stretched grid: each tap's coefficient is the operator applied to
+        // that tap alone (stream_space with build = 1, iterative_solver.f90:
+        // 456-561), and the local time step from the metric eigenvalues
+        if (dts) {
+            double eR, eI;
+            eig_pair_metric(c, i, k, v, ax, az, axx, azz, axz, eR, eI);
+            dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
+        }
+        const int i1 = i * c.mf, k1 = k * c.mf;
+        const Metric& M = c.M;
+        const double x1 = mt(M.xr, i1), x2 = mt(M.xrr, i1), x3 = mt(M.xrrr, i1), x4 = mt(M.xrrrr, i1);
+        const double x13 = mt(M.xr3, i1), x14 = mt(M.xr4, i1);
+        const double z1 = mt(M.zs, k1), z2 = mt(M.zss, k1), z3 = mt(M.zsss, k1), z4 = mt(M.zssss, k1);
+        const double z13 = mt(M.zs3, k1), z14 = mt(M.zs4, k1);
+        for (int d = 0; d < TC_NCOEF; d++)
+            coef[(size_t)d * L.plane + x] = stream_op_metric(mw.w[d], x1, x2, x3, x4, x13, x14, z1, z2, z3, z4, z13,
+                                                             z14, v, ax, az, axx, azz, axz);
+    } else {
+        if (dts) {
+            double eR, eI;
+            eig_pair(c, v, ax, az, axx, azz, axz, eR, eI);
+            dts[x] = -courant_stream * 2.0 * eR / (eR * eR + eI * eI);
+        }
+        double g0 = axx - azz, g1 = v, g2 = 2.0 * v, g3 = 4.0 * axz, g4 = 2.0 * ax, g5 = 2.0 * az;
 #pragma unroll
-    for (int d = 0; d < TC_NCOEF; d++) {
-        double A = g0 * c.fold[d][0];
-        A = fma(g1, c.fold[d][1], A);
-        A = fma(g2, c.fold[d][2], A);
-        A = fma(g3, c.fold[d][3], A);
-        A = fma(g4, c.fold[d][4], A);
-        A = fma(g5, c.fold[d][5], A);
-        coef[(size_t)d * L.plane + x] = A;
+        for (int d = 0; d < TC_NCOEF; d++) {
+            double A = g0 * c.fold[d][0];
+            A = fma(g1, c.fold[d][1], A);
+            A = fma(g2, c.fold[d][2], A);
+            A = fma(g3, c.fold[d][3], A);
+            A = fma(g4, c.fold[d][4], A);
+            A = fma(g5, c.fold[d][5], A);
+            coef[(size_t)d * L.plane + x] = A;
+        }
     }
     if (cheb) {
         double rr = ratio[x];
@@ -251,7 +345,7 @@ void launch_level_coefs(cudaStream_t s, const Level& lv, const double* vis, int 
     Range2 r{1, lv.L.a - 1, 1, lv.L.b - 1};
     k_level_coefs<<<grid_for(r), dim3(BX, BY), 0, s>>>(lv.L, lv.c, r, vis, lv.vx, lv.vz, lv.vxx, lv.vzz, lv.vxz,
                                                         lv.ratio, with_dt ? lv.dt_stream : nullptr, lv.coef, lv.cA,
-                                                        lv.cB, courant_stream, cheb_level); tc_note_launch();
+                                                        lv.cB, courant_stream, cheb_level, lv.mfold); tc_note_launch();
 }
 
 // ---------------------------------------------------------------------------
@@ -982,13 +1076,17 @@ __global__ void k_rhs1(Lay L, Phys P, Range2 r, const double* __restrict__ Tb, C
     if (inr) {
         size_t x = IX(L, i, k);
         double R = 0.0;
+        // dx/dr at node i (1 on a uniform grid, where the division is skipped)
+        const double x1 = P.M.on ? mt(P.M.xr, i) : 1.0;
         if (P.RaT != 0.0) {
             double Tr = (-0.5 * Tb[x - 1] + 0.5 * Tb[x + 1]) / P.dr;
+            if (P.M.on) Tr = Tr / x1;
             R = P.RaT * Tr;
         }
         if (P.comp == 1)
             for (int j = 0; j < P.ntype; j++) {
                 double Cr = (-0.5 * Cb.p[j][x - 1] + 0.5 * Cb.p[j][x + 1]) / P.dr;
+                if (P.M.on) Cr = Cr / x1;
                 R = R - P.RaC[j] * Cr;
             }
         rhs[x] = R;

@@ -1775,7 +1775,15 @@ tc_status create(Handle* h, const tc_params* in) {
     h->p = *in;
     tc_params& p = h->p;
     if (p.order != 2) { h->err = "the GPU path implements order=2"; return TC_ERR_UNSUPPORTED; }
-    if (p.gridX != 0 || p.gridZ != 0) { h->err = "the GPU path implements uniform grids"; return TC_ERR_UNSUPPORTED; }
+    if (p.gridX < 0 || p.gridX > 2 || p.gridZ < 0 || p.gridZ > 2) { h->err = "gridX and gridZ must be 0..2"; return TC_ERR_ARG; }
+    if ((p.gridX != 0 || p.gridZ != 0) && (p.comp == 1 || p.tracer == 1)) {
+        h->err = "stretched grids are implemented for the field-temperature path (comp = 0, tracer = 0)";
+        return TC_ERR_UNSUPPORTED;
+    }
+    if (p.gridZ == 2 && (p.nbound < 2 || p.nz - 2 * p.nbound + 2 <= 0)) {
+        h->err = "gridZ = 2 needs 2 <= nbound and nz > 2 nbound - 2";
+        return TC_ERR_ARG;
+    }
     if (p.ivis < -1 || p.ivis > 3) { h->err = "ivis must be -1..3"; return TC_ERR_ARG; }
     if (p.iterate_order != 1) { h->err = "iterate_order must be 1"; return TC_ERR_UNSUPPORTED; }
     if (p.RaT == 0.0) { h->err = "the GPU path implements thermal or thermochemical convection (RaT != 0)"; return TC_ERR_UNSUPPORTED; }
@@ -1843,10 +1851,14 @@ tc_status create(Handle* h, const tc_params* in) {
     tcs::FD fd;
     tcs::fd_coefficients(2, fd);
     tcs::derivative_eigenvalues(fd, 1, h->eb);
-    // entrainment_setup (composition.f90:582-591), uniform zgrid
+    // build_grid (grid.f90): coordinates and metrics
+    tcs::GridMetrics gm;
+    tcs::grid_metrics(p.aspect, nx, nz, p.gridX, p.gridZ, p.spaceX, p.spaceZ, p.thickness, p.nbound, fd, gm);
+    const bool stretched = (p.gridX != 0 || p.gridZ != 0);
+    // entrainment_setup (composition.f90:582-591)
     h->kent = 0;
     for (int k = 0; k <= nz; k++)
-        if (s1.ds * (double)k <= p.dent) h->kent = k;
+        if (gm.zg[(size_t)(k + gm.pad)] <= p.dent) h->kent = k;
     // ---- physics scalars ----
     Phys& P = h->P;
     P.nx = nx; P.nz = nz; P.ntype = h->ntype; P.comp = p.comp; P.ivis = p.ivis; P.Tbot = p.Tbot; P.Vbc = p.Vbc;
@@ -1862,6 +1874,8 @@ tc_status create(Handle* h, const tc_params* in) {
     P.courantT = p.courantT; P.courantC = p.courantC;
     P.Tr_max = h->eb.Tr / s1.dr; P.Ts_max = h->eb.Tr / s1.ds;
     P.Trr_max = -h->eb.Trr / s1.dr2; P.Tss_max = -h->eb.Trr / s1.ds2;
+    P.M = Metric{};
+    P.M.on = stretched ? 1 : 0;
     // ---- stream ----
     cudaGetDevice(&h->device);
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
@@ -1963,6 +1977,23 @@ tc_status create(Handle* h, const tc_params* in) {
     e = cudaMallocHost((void**)&h->hs, sizeof(DevScalars));
     if (e != cudaSuccess) { h->err = cudaGetErrorString(e); return TC_ERR_ALLOC; }
     std::memset(h->hs, 0, sizeof(DevScalars));
+    if (stretched) {
+        // the metric arrays, each over fine index -pad..n+pad
+        const std::vector<double>* xs[6] = {&gm.xr, &gm.xrr, &gm.xrrr, &gm.xrrrr, &gm.xr3, &gm.xr4};
+        const std::vector<double>* zs_[6] = {&gm.zs, &gm.zss, &gm.zsss, &gm.zssss, &gm.zs3, &gm.zs4};
+        const double** xd[6] = {&P.M.xr, &P.M.xrr, &P.M.xrrr, &P.M.xrrrr, &P.M.xr3, &P.M.xr4};
+        const double** zd[6] = {&P.M.zs, &P.M.zss, &P.M.zsss, &P.M.zssss, &P.M.zs3, &P.M.zs4};
+        for (int q = 0; q < 6; q++) {
+            double* dx = nullptr;
+            double* dz = nullptr;
+            TRY(dalloc_t(h, &dx, xs[q]->size()));
+            TRY(dalloc_t(h, &dz, zs_[q]->size()));
+            CK(cudaMemcpy(dx, xs[q]->data(), sizeof(double) * xs[q]->size(), cudaMemcpyHostToDevice));
+            CK(cudaMemcpy(dz, zs_[q]->data(), sizeof(double) * zs_[q]->size(), cudaMemcpyHostToDevice));
+            *xd[q] = dx;
+            *zd[q] = dz;
+        }
+    }
     // ---- levels ----
     const int odi[TC_NCOEF] = TC_OFFSETS_DI, odk[TC_NCOEF] = TC_OFFSETS_DK;
     auto Dv = [&](const double* D, int j) { return (j < -3 || j > 3) ? 0.0 : D[j + 3]; };
@@ -2019,6 +2050,9 @@ tc_status create(Handle* h, const tc_params* in) {
         (void)Ts;
         c.eK1 = Trr - Tss; c.eK2 = Trrrr + Tssss; c.eTrrss = Trrss; c.eTrs = Trs;
         c.eK5 = Trrr + Trss; c.eK6 = Tsss + Trrs;
+        c.M = P.M;
+        c.mf = 1 << (l - 1);
+        c.e = EigScaled{h->eb.Tr / s.dr, Ts, Trr, Tss, Trrr, Tsss, Trrrr, Tssss, Trs, Trrs, Trss, Trrss};
         for (int d = 0; d < TC_NCOEF; d++) {
             const int di = odi[d], dk = odk[d];
             double Srr = 0, Sss = 0, Srrr = 0, Ssss = 0, Srrrr = 0, Sssss = 0;
@@ -2035,23 +2069,33 @@ tc_status create(Handle* h, const tc_params* in) {
             c.fold[d][3] = Srs;
             c.fold[d][4] = Srrr + Srss;
             c.fold[d][5] = Ssss + Srrs;
+            // the same single-tap derivatives unreduced (stream_space, build = 1)
+            const double Sr = (dk == 0) ? Dv(fd.D1, di) / s.dr : 0.0;
+            const double Ss = (di == 0) ? Dv(fd.D1, dk) / s.ds : 0.0;
+            const double q[12] = {Sr, Srr, Srrr, Srrrr, Ss, Sss, Ssss, Sssss, Srs, Srrs, Srss, Srrss};
+            for (int j = 0; j < 12; j++) lv.mfold.w[d][j] = q[j];
         }
         // level 1 of the mixed solve sweeps from the five viscosity fields
         // (k_sweep_g32) when the stencil's structural zeros hold
         lv.use_g32 = 0;
-        if (p.solver_precision == 1 && l == 1 && fold_g32_weights(c, &lv.gw)) {
+        if (p.solver_precision == 1 && l == 1 && !stretched && fold_g32_weights(c, &lv.gw)) {
             TRY(dalloc_t(h, &lv.g32, lp * 5));
             lv.use_g32 = 1;
         }
-        // stability_vis_smoother (uniform: eI = 0)
+        // stability_vis_smoother (smoother.f90:465-508); uniform: eI = 0
         {
             const double Trr_l = -h->eb.Trr / s.dr2, Tss_l = -h->eb.Trr / s.ds2;
-            const double eR = std::fabs(Trr_l / 1.0) + std::fabs(Tss_l / 1.0);
-            const double eI = std::fabs(0.0 / 1.0) * (h->eb.Tr / s.dr) + std::fabs(0.0 / 1.0) * (h->eb.Tr / s.ds);
-            const double dtv = 2.0 * eR / (eR * eR + eI * eI);
+            const double Tr_l = h->eb.Tr / s.dr, Ts_l = h->eb.Tr / s.ds;
             std::vector<double> hv(lp, 0.0);
             for (int i = 0; i <= lv.L.a; i++)
-                for (int k = 1; k <= lv.L.b - 1; k++) hv[IX(lv.L, i, k)] = dtv;
+                for (int k = 1; k <= lv.L.b - 1; k++) {
+                    const int i1 = i * c.mf + gm.pad, k1 = k * c.mf + gm.pad;
+                    const double x1 = gm.xr[(size_t)i1], x2 = gm.xrr[(size_t)i1];
+                    const double z1 = gm.zs[(size_t)k1], z2 = gm.zss[(size_t)k1];
+                    const double eR = std::fabs(Trr_l / (x1 * x1)) + std::fabs(Tss_l / (z1 * z1));
+                    const double eI = std::fabs(x2 / gm.xr3[(size_t)i1]) * Tr_l + std::fabs(z2 / gm.zs3[(size_t)k1]) * Ts_l;
+                    hv[IX(lv.L, i, k)] = 2.0 * eR / (eR * eR + eI * eI);
+                }
             CK(cudaMemcpy(lv.dt_vis, hv.data(), lp * sizeof(double), cudaMemcpyHostToDevice));
         }
     }
@@ -2122,27 +2166,26 @@ tc_status create(Handle* h, const tc_params* in) {
         TRY(dalloc_t(h, &h->flt_tab, tb.size()));
         CK(cudaMemcpy(h->flt_tab, tb.data(), sizeof(double) * tb.size(), cudaMemcpyHostToDevice));
     }
-    // stability_RK4_smoother: dts_array
+    // stability_RK4_smoother: dts_array (smoother.f90:423-462)
     {
         const double Tr_max = h->eb.Tr / s1.dr, Ts_max = h->eb.Tr / s1.ds;
         const double Trr_max = -h->eb.Trr / s1.dr2, Tss_max = -h->eb.Trr / s1.ds2;
-        const double eR = std::fabs(Trr_max / 1.0) + std::fabs(Tss_max / 1.0);
-        const double eI = std::fabs(0.0 / 1.0) * Tr_max + std::fabs(0.0 / 1.0) * Ts_max;
-        const double v = 2.0 * eR / (eR * eR + eI * eI);
         std::vector<double> hv(pl, 0.0);
         for (int i = 0; i <= nx; i++)
-            for (int k = 0; k <= nz; k++) hv[IX(h->L1, i, k)] = v;
+            for (int k = 0; k <= nz; k++) {
+                const size_t i1 = (size_t)(i + gm.pad), k1 = (size_t)(k + gm.pad);
+                const double x1 = gm.xr[i1], z1 = gm.zs[k1];
+                const double eR = std::fabs(Trr_max / (x1 * x1)) + std::fabs(Tss_max / (z1 * z1));
+                const double eI = std::fabs(gm.xrr[i1] / gm.xr3[i1]) * Tr_max + std::fabs(gm.zss[k1] / gm.zs3[k1]) * Ts_max;
+                hv[IX(h->L1, i, k)] = 2.0 * eR / (eR * eR + eI * eI);
+            }
         CK(cudaMemcpy(h->dts, hv.data(), pl * sizeof(double), cudaMemcpyHostToDevice));
     }
-    // zg (grid.f90:46-109, restart=0 coordinates, uniform)
+    // zg (grid.f90:46-109, restart=0 coordinates)
     {
-        std::vector<double> z((size_t)nz + 1 + 2 * (SP + 1));
-        auto Z = [&](int k) -> double& { return z[(size_t)(k + SP + 1)]; };
-        for (int k = 0; k <= nz; k++) Z(k) = s1.ds * (double)k;
-        for (int k = 1; k <= SP + 1; k++) { Z(-k) = -Z(k); Z(nz + k) = 1.0 - Z(nz - k) + 1.0; }
-        Z(0) = 0.0; Z(nz) = 1.0;
-        CK(cudaMemcpy(h->zg, z.data(), z.size() * sizeof(double), cudaMemcpyHostToDevice));
-        h->zg += SP + 1;  // kernels index zg[k], k >= -3
+        static_assert(SP + 1 == 3, "zg is indexed k + 3");
+        CK(cudaMemcpy(h->zg, gm.zg.data(), gm.zg.size() * sizeof(double), cudaMemcpyHostToDevice));
+        h->zg += gm.pad;  // kernels index zg[k], k >= -3
     }
     CK(cudaDeviceSynchronize());
     return TC_OK;

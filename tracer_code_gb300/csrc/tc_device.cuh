@@ -19,6 +19,42 @@ struct Range2 {
     int i0, i1, k0, k1;  // inclusive
 };
 
+// metric array a at fine node n (Metric in tc_internal.h)
+__device__ __forceinline__ double mt(const double* a, int n) { return a[n + TC_MPAD]; }
+
+// The streamfunction operator of iterative_solver.f90 stream_space on a
+// stretched grid, given the computational derivatives q = (Sr, Srr, Srrr,
+// Srrrr, Ss, Sss, Ssss, Sssss, Srs, Srrs, Srss, Srrss) at a node whose
+// metrics are x1..x4 (xr..xrrrr), x13 = xr**3, x14 = xr**4 and likewise for z,
+// and whose viscosity and its x/z derivatives are v, vx, vz, vxx, vzz, vxz;
+// the reference's expressions in its order.
+__device__ __forceinline__ double stream_op_metric(const double* q, double x1, double x2, double x3, double x4,
+                                                   double x13, double x14, double z1, double z2, double z3,
+                                                   double z4, double z13, double z14, double v, double vx, double vz,
+                                                   double vxx, double vzz, double vxz) {
+    const double Sr = q[0], Srr = q[1], Srrr = q[2], Srrrr = q[3], Ss = q[4], Sss = q[5], Ssss = q[6],
+                 Sssss = q[7], Srs = q[8], Srrs = q[9], Srss = q[10], Srrss = q[11];
+    const double Sx = Sr / x1, Sz = Ss / z1;
+    const double Sxx = (Srr - Sx * x2) / (x1 * x1);
+    const double Szz = (Sss - Sz * z2) / (z1 * z1);
+    const double Sxxx = (Srrr - 3.0 * Sxx * x1 * x2 - Sx * x3) / x13;
+    const double Szzz = (Ssss - 3.0 * Szz * z1 * z2 - Sz * z3) / z13;
+    const double Sxxxx = (Srrrr - 6.0 * Sxxx * x2 * (x1 * x1) - (3.0 * (x2 * x2) + 4.0 * x1 * x3) * Sxx - Sx * x4) / x14;
+    const double Szzzz = (Sssss - 6.0 * Szzz * z2 * (z1 * z1) - (3.0 * (z2 * z2) + 4.0 * z1 * z3) * Szz - Sz * z4) / z14;
+    const double Sxz = Srs / x1 / z1;
+    const double Sxxz = (Srrs - Sxz * z1 * x2) / z1 / (x1 * x1);
+    const double Sxzz = (Srss - Sxz * x1 * z2) / x1 / (z1 * z1);
+    const double Sxxzz =
+        (Srrss - Sxzz * x2 * (z1 * z1) - Sxxz * z2 * (x1 * x1) - Sxz * x2 * z2) / ((x1 * z1) * (x1 * z1));
+    const double t1 = (vxx - vzz) * (Sxx - Szz);
+    const double t2 = v * (Sxxxx + Szzzz);
+    const double t3 = 2.0 * v * Sxxzz;
+    const double t4 = 4.0 * vxz * Sxz;
+    const double t5 = 2.0 * vx * (Sxxx + Sxzz);
+    const double t6 = 2.0 * vz * (Szzz + Sxxz);
+    return t1 + t2 + t3 + t4 + t5 + t6;
+}
+
 inline dim3 grid_for(const Range2& r) {
     int ni = r.i1 - r.i0 + 1, nk = r.k1 - r.k0 + 1;
     if (ni < 1) ni = 1;

@@ -40,6 +40,24 @@ inline
 #endif
 size_t IX(const Lay& L, int i, int k) { return (size_t)(i + SP) + (size_t)(k + SP) * (size_t)L.ld; }
 
+// Metrics of a stretched grid (grid.f90 build_grid): dx/dr and its
+// r-derivatives at fine node i, with xr3 = xr**3 and xr4 = xr**4 as the host
+// evaluates them, and dz/ds likewise at fine row k; every array is indexed
+// [i + TC_MPAD] for i = -TC_MPAD..n+TC_MPAD.  on = 0: a uniform grid (xr = zs
+// = 1, the others 0), where the kernels take their uniform-grid form.
+#define TC_MPAD 3
+struct Metric {
+    const double *xr, *xrr, *xrrr, *xrrrr, *xr3, *xr4;
+    const double *zs, *zss, *zsss, *zssss, *zs3, *zs4;
+    int on;
+};
+
+// scaled eigenvalue bounds of one level (the reference's test_eigenvalues /
+// iterate_local_time_steps preamble), for the stretched-grid eigenvalues
+struct EigScaled {
+    double Tr, Ts, Trr, Tss, Trrr, Tsss, Trrrr, Tssss, Trs, Trrs, Trss, Trrss;
+};
+
 // Per-level constants (grid spacings and scaled eigenvalue bounds).
 struct LevConst {
     double dr, ds, dr2, ds2, dr3, ds3, dr4, ds4, drds, drds2, dr2ds, dr2ds2;
@@ -53,6 +71,19 @@ struct LevConst {
     // viscosity-filter kernels multiply instead of dividing
     double rdr, rds, rdr2, rds2, rdrds;
     int recip;
+    // stretched grids: the metrics, this level's stride into the fine grid
+    // (node i of the level is fine node i * mf) and the unreduced bounds
+    Metric M;
+    int mf;
+    EigScaled e;
+};
+
+// Stretched-grid operator: the 13 tap coefficients are sum_q w[d][q] a_q(i,k)
+// over the computational derivatives q = (Sr, Srr, Srrr, Srrrr, Ss, Sss, Ssss,
+// Sssss, Srs, Srrs, Srss, Srrss), w[d][q] = the FD weight of q at tap d over
+// its spacing, a_q = the coefficient of q in the operator at (i, k)
+struct MetricFold {
+    double w[TC_NCOEF][12];
 };
 
 // Scalars that kernels produce and the host reads back.
@@ -149,6 +180,7 @@ struct Level {
     int fuse;       // 1 = one cluster launch per visit when the level fits, 0 = one launch per sweep
     int visit_cfg;  // shape of the fused visit: 0 = default, else 100*points per strip + CTAs
     int blk;        // when not fused: 0 = one k_sweep / k_sweep32 launch per sweep, n = n sweeps per k_sweep_blk launch
+    MetricFold mfold;  // stretched grids: the tap weights of the computational derivatives
 };
 
 // Host-side scalars of the physics configuration, passed by value to kernels.
@@ -161,6 +193,7 @@ struct Phys {
     double courantT, courantC;
     double Tr_max, Ts_max, Trr_max, Tss_max;  // stability_RK4 scaled bounds (finest grid)
     double visT, yield, yield_gradient, yield_depth;  // ivis = 3 (plastic)
+    Metric M;                                         // stretched-grid metrics (M.on = 0: uniform)
 };
 
 // ---------------------------------------------------------------------------

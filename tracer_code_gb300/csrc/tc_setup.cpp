@@ -202,4 +202,75 @@ void coarse_bandwidth(int nxc, int nzc, int span, int span1, int& kl, int& ku) {
     }
 }
 
+// xgrid / zgrid (grid.f90:1-35)
+static double xgrid(double r, double aspect, int gridX, double spaceX, double Ax) {
+    if (gridX == 1) return aspect * (Ax * std::atan(spaceX * (r / aspect - 0.5)) + 0.5);
+    return r;
+}
+static double zgrid(double s, int nz, double ds, int gridZ, double spaceZ, double thickness, int nbound,
+                    double Az) {
+    if (gridZ == 1) return Az * std::atan(spaceZ * (s - 0.5)) + 0.5;
+    if (gridZ == 2) {
+        const double dzin = (1.0 - 2.0 * thickness) / (double)(nz - 2 * nbound + 2);
+        const double s1 = (double)(nbound - 1) * ds, s2 = 1.0 - s1;
+        const double scale = thickness / (std::exp(spaceZ * s1) - 1.0);
+        if (s < s1) return scale * (std::exp(spaceZ * s) - 1.0);
+        if (s > s2) return 1.0 - scale * (std::exp(-spaceZ * (s - 1.0)) - 1.0);
+        return thickness + (s - s1) * dzin / ds;
+    }
+    return s;
+}
+
+void grid_metrics(double aspect, int nx, int nz, int gridX, int gridZ, double spaceX, double spaceZ,
+                  double thickness, int nbound, const FD& fd, GridMetrics& g) {
+    const int P = g.pad, span = 2, span1 = 1, si = 1;
+    LevSpacing sp;
+    level_spacing(aspect, nx, nz, sp);
+    const double dr = sp.dr, ds = sp.ds;
+    // basics.f90:140-141
+    const double Ax = std::pow(std::atan(spaceX * 0.5) - std::atan(spaceX * (-0.5)), -1.0);
+    const double Az = std::pow(std::atan(spaceZ * 0.5) - std::atan(spaceZ * (-0.5)), -1.0);
+    auto alloc = [&](std::vector<double>& v, int n) { v.assign((size_t)n + 1 + 2 * P, 0.0); };
+    for (auto* v : {&g.xg, &g.xr, &g.xrr, &g.xrrr, &g.xrrrr, &g.xr3, &g.xr4}) alloc(*v, nx);
+    for (auto* v : {&g.zg, &g.zs, &g.zss, &g.zsss, &g.zssss, &g.zs3, &g.zs4}) alloc(*v, nz);
+    auto X = [&](std::vector<double>& v, int i) -> double& { return v[(size_t)(i + P)]; };
+    for (int i = 0; i <= nx; i++) X(g.xg, i) = xgrid(dr * (double)i, aspect, gridX, spaceX, Ax);
+    for (int k = 0; k <= nz; k++) X(g.zg, k) = zgrid(ds * (double)k, nz, ds, gridZ, spaceZ, thickness, nbound, Az);
+    for (int i = 1; i <= span + si; i++) {
+        X(g.xg, -i) = -X(g.xg, i);
+        X(g.xg, nx + i) = aspect - X(g.xg, nx - i) + aspect;
+    }
+    for (int k = 1; k <= span + si; k++) {
+        X(g.zg, -k) = -X(g.zg, k);
+        X(g.zg, nz + k) = 1.0 - X(g.zg, nz - k) + 1.0;
+    }
+    X(g.xg, 0) = 0.0; X(g.zg, 0) = 0.0; X(g.xg, nx) = aspect; X(g.zg, nz) = 1.0;
+    // dot_product(D(-sp:sp), f(c-sp:c+sp)) in index order
+    auto dot = [&](const double* D, int sp_, std::vector<double>& f, int c) {
+        double s = 0.0;
+        for (int j = -sp_; j <= sp_; j++) s = s + D[j + 3] * X(f, c + j);
+        return s;
+    };
+    for (int i = 0; i <= nx; i++) {
+        X(g.xrrr, i) = gridX != 0 ? dot(fd.D3, span, g.xg, i) / sp.dr3 : 0.0;
+        X(g.xrrrr, i) = gridX != 0 ? dot(fd.D4, span, g.xg, i) / sp.dr4 : 0.0;
+    }
+    for (int i = -si; i <= nx + si; i++) {
+        X(g.xr, i) = gridX != 0 ? dot(fd.D1, span1, g.xg, i) / dr : 1.0;
+        X(g.xrr, i) = gridX != 0 ? dot(fd.D2, span1, g.xg, i) / sp.dr2 : 0.0;
+        X(g.xr3, i) = std::pow(X(g.xr, i), 3.0);
+        X(g.xr4, i) = std::pow(X(g.xr, i), 4.0);
+    }
+    for (int k = 0; k <= nz; k++) {
+        X(g.zsss, k) = gridZ != 0 ? dot(fd.D3, span, g.zg, k) / sp.ds3 : 0.0;
+        X(g.zssss, k) = gridZ != 0 ? dot(fd.D4, span, g.zg, k) / sp.ds4 : 0.0;
+    }
+    for (int k = -si; k <= nz + si; k++) {
+        X(g.zs, k) = gridZ != 0 ? dot(fd.D1, span1, g.zg, k) / ds : 1.0;
+        X(g.zss, k) = gridZ != 0 ? dot(fd.D2, span1, g.zg, k) / sp.ds2 : 0.0;
+        X(g.zs3, k) = std::pow(X(g.zs, k), 3.0);
+        X(g.zs4, k) = std::pow(X(g.zs, k), 4.0);
+    }
+}
+
 }  // namespace tcs

@@ -23,4 +23,17 @@ double pw(double x, int n);
 void level_spacing(double aspect, int nxl, int nzl, LevSpacing& s);
 void coarse_bandwidth(int nxc, int nzc, int span, int span1, int& kl, int& ku);
 
+// build_grid (grid.f90): node coordinates xg(i) = xgrid(i dr), zg(k) =
+// zgrid(k ds) with the mirrored ghosts, and the metrics xr, xrr (D1, D2 over
+// span1), xrrr, xrrrr (D3, D4 over span) and likewise for z, plus xr**3,
+// xr**4, zs**3, zs**4 as libm pow evaluates them.  Every vector holds index
+// -pad..n+pad at [i + pad].  gridX: 0 uniform, 1 arctan, 2 uniform through
+// the metric path; gridZ: 0 uniform, 1 arctan, 2 boundary layers.
+struct GridMetrics {
+    int pad = 3;
+    std::vector<double> xg, zg, xr, xrr, xrrr, xrrrr, xr3, xr4, zs, zss, zsss, zssss, zs3, zs4;
+};
+void grid_metrics(double aspect, int nx, int nz, int gridX, int gridZ, double spaceX, double spaceZ,
+                  double thickness, int nbound, const FD& fd, GridMetrics& g);
+
 }  // namespace tcs

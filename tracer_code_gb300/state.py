@@ -45,16 +45,44 @@ def sizes(p: Params, nx: int | None = None, nz: int | None = None):
     return nx, nz, span
 
 
-def initial_temperature(p: Params, nx: int | None = None, nz: int | None = None) -> np.ndarray:
-    """T0 = (1 - z) + 0.01 cos(pi x) sin(pi z) on (-span:nx+span, -span:nz+span),
-    Fortran order (returned array has shape (nz+1+2span, nx+1+2span), i
-    fastest in memory).  T(:,0)=1, T(:,nz)=0 as in basics.f90:230-231; ghosts
-    are filled by enforceBCs at upload."""
+def grid_coordinates(p: Params, nx: int | None = None, nz: int | None = None):
+    """Node coordinates x(i) = xgrid(i dr), i = -span..nx+span, and z(k) =
+    zgrid(k ds) (grid.f90:1-35; Ax, Az as basics.f90:140-141): uniform for
+    gridX/gridZ = 0 (and gridX = 2), arctan stretching for 1, boundary layers
+    of nbound nodes and total thickness `thickness` for gridZ = 2."""
     nx, nz, span = sizes(p, nx, nz)
     dr = p.aspect / nx
     ds = 1.0 / nz
-    x = np.arange(-span, nx + span + 1, dtype=np.float64) * dr
-    z = np.arange(-span, nz + span + 1, dtype=np.float64) * ds
+    r = np.arange(-span, nx + span + 1, dtype=np.float64) * dr
+    s = np.arange(-span, nz + span + 1, dtype=np.float64) * ds
+    if p.gridX == 1:
+        ax = 1.0 / (np.arctan(p.spaceX * 0.5) - np.arctan(p.spaceX * -0.5))
+        x = p.aspect * (ax * np.arctan(p.spaceX * (r / p.aspect - 0.5)) + 0.5)
+    else:
+        x = r
+    if p.gridZ == 1:
+        az = 1.0 / (np.arctan(p.spaceZ * 0.5) - np.arctan(p.spaceZ * -0.5))
+        z = az * np.arctan(p.spaceZ * (s - 0.5)) + 0.5
+    elif p.gridZ == 2:
+        dzin = (1.0 - 2.0 * p.thickness) / (nz - 2 * p.nbound + 2)
+        s1 = (p.nbound - 1) * ds
+        s2 = 1.0 - s1
+        scale = p.thickness / (np.exp(p.spaceZ * s1) - 1.0)
+        z = np.where(s < s1, scale * (np.exp(p.spaceZ * s) - 1.0),
+                     np.where(s > s2, 1.0 - scale * (np.exp(-p.spaceZ * (s - 1.0)) - 1.0),
+                              p.thickness + (s - s1) * dzin / ds))
+    else:
+        z = s
+    return x, z
+
+
+def initial_temperature(p: Params, nx: int | None = None, nz: int | None = None) -> np.ndarray:
+    """T0 = (1 - z) + 0.01 cos(pi x) sin(pi z) at the node coordinates on
+    (-span:nx+span, -span:nz+span), Fortran order (returned array has shape
+    (nz+1+2span, nx+1+2span), i fastest in memory).  T(:,0)=1, T(:,nz)=0 as in
+    basics.f90:230-231; ghosts are filled by enforceBCs at upload."""
+    nx, nz, span = sizes(p, nx, nz)
+    x, z = grid_coordinates(p, nx, nz)
     T = (1.0 - z)[:, None] + 0.01 * np.cos(np.pi * x)[None, :] * np.sin(np.pi * z)[:, None]
     T[span + 0, :] = 1.0
     T[span + nz, :] = 0.0
