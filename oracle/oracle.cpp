@@ -142,6 +142,7 @@ struct Oracle {
            Tsss_base = 0, Tssss_base = 0, Trs_base = 0, Trrss_base = 0, Trss_base = 0, Trrs_base = 0;
     // ---- grid ----
     V1 xg, zg, xr, xrr, xrrr, xrrrr, zs, zss, zsss, zssss;
+    std::vector<V1> DERxr, DERzs;  // (1:order-1, 0:n): compute_metric_interpolator_derivatives
     // ---- fields ----
     Arr T, SF, Tvis, Tbuoy, u, w, vis, strain, conduct, conduct_r, conduct_s, dts_array;
     std::vector<Arr> Cnew, Cvis, Cbuoy;  // per type (index tt-1)
@@ -318,6 +319,8 @@ struct Oracle {
         xg.alloc(-(s + si), nx + s + si); zg.alloc(-(s + si), nz + s + si);
         xr.alloc(-si, nx + si); xrr.alloc(-si, nx + si); xrrr.alloc(0, nx); xrrrr.alloc(0, nx);
         zs.alloc(-si, nz + si); zss.alloc(-si, nz + si); zsss.alloc(0, nz); zssss.alloc(0, nz);
+        DERxr.assign(order, V1()); DERzs.assign(order, V1());
+        for (int j = 1; j <= order - 1; j++) { DERxr[j].alloc(0, nx); DERzs[j].alloc(0, nz); }
         ntype = p.comp == 1 ? p.ntype : 0;
         Cnew.assign(ntype, Arr()); Cvis.assign(ntype, Arr()); Cbuoy.assign(ntype, Arr());
         for (int t = 0; t < ntype; t++) {
@@ -503,6 +506,57 @@ struct Oracle {
             if (p.gridZ != 0) { zs(k) = dotD(D1, span1, zg, k) / ds; zss(k) = dotD(D2, span1, zg, k) / ds2; }
             else { zs(k) = 1.0; zss(k) = 0.0; }
         }
+        // compute_metric_interpolator_derivatives (composition.f90:921-936);
+        // the reference calls it for comp = 1 only (grid.f90:146), here for
+        // every case so that temperature tracers read defined values
+        for (int jj = 1; jj <= order - 1; jj++) {
+            for (int i = 0; i <= nx; i++) DERxr[jj](i) = dotD(D[jj], span_interp, xr, i) / dr_power[jj];
+            for (int k = 0; k <= nz; k++) DERzs[jj](k) = dotD(D[jj], span_interp, zs, k) / ds_power[jj];
+        }
+    }
+    // interpolate_xr / interpolate_zs (composition.f90:938-998): the metric at
+    // a tracer position by the forward or backward Taylor step of interpolate
+    double interpolate_xr(double r) const {
+        if (p.gridX == 0) return 1.0;
+        const int i = (int)(r / dr);
+        double hr = r - (double)i * dr;
+        double x;
+        if (hr <= dro2) {
+            x = xr(i);
+            for (int j = 1; j <= order - 1; j++) x = x + DERxr[j](i) * (pw(hr, j) / factorial[j]);
+        } else {
+            hr = dr - hr;
+            x = xr(i + 1);
+            for (int j = 1; j <= order - 1; j++) x = x + DERxr[j](i + 1) * (pw(-hr, j) / factorial[j]);
+        }
+        return x;
+    }
+    double interpolate_zs(double s) const {
+        if (p.gridZ == 0) return 1.0;
+        const int k = (int)(s / ds);
+        double hs = s - (double)k * ds;
+        double z;
+        if (hs <= dso2) {
+            z = zs(k);
+            for (int j = 1; j <= order - 1; j++) z = z + DERzs[j](k) * (pw(hs, j) / factorial[j]);
+        } else {
+            hs = ds - hs;
+            z = zs(k + 1);
+            for (int j = 1; j <= order - 1; j++) z = z + DERzs[j](k + 1) * (pw(-hs, j) / factorial[j]);
+        }
+        return z;
+    }
+    // the tracer's computational velocity at (r, s): u / xr and w / zs with
+    // the interpolated metrics on stretched axes (energy.f90:194-203)
+    double tr_vel(double r, double s) const {
+        double t = interpolate(r, s, DERr_u, u);
+        if (p.gridX != 0) t = t / interpolate_xr(r);
+        return t;
+    }
+    double ts_vel(double r, double s) const {
+        double t = interpolate(r, s, DERr_w, w);
+        if (p.gridZ != 0) t = t / interpolate_zs(s);
+        return t;
     }
 
     // derivative_eigenvalues (energy.f90:501-598).  T_test uses CMPLX without
@@ -2154,8 +2208,8 @@ struct Oracle {
             double dtstage = (p.torder == 2) ? dt : 0.5 * dt;
 #pragma omp parallel for schedule(static)
             for (long id = 0; id < ntr; id++) {
-                double tr = interpolate(rtr0[id], str0[id], DERr_u, u);
-                double ts = interpolate(rtr0[id], str0[id], DERr_w, w);
+                double tr = tr_vel(rtr0[id], str0[id]);
+                double ts = ts_vel(rtr0[id], str0[id]);
                 rtr[id] = tr; str[id] = ts;
                 double tT = 0.0;
                 if (tt) { tT = interpolate(rtr0[id], str0[id], DERr_tracer, tsa); Ttr[id] = tT; }
@@ -2180,8 +2234,8 @@ struct Oracle {
             double dtstage = 0.5 * dt;
 #pragma omp parallel for schedule(static)
             for (long id = 0; id < ntr; id++) {
-                double tr = interpolate(rtr1[id], str1[id], DERr_u, u);
-                double ts = interpolate(rtr1[id], str1[id], DERr_w, w);
+                double tr = tr_vel(rtr1[id], str1[id]);
+                double ts = ts_vel(rtr1[id], str1[id]);
                 double tT = tt ? interpolate(rtr1[id], str1[id], DERr_tracer, tsa) : 0.0;
                 if (p.torder == 2) {
                     rtr[id] = rtr[id] + tr; str[id] = str[id] + ts;
@@ -2215,10 +2269,10 @@ struct Oracle {
                 double dtt = dt;
 #pragma omp parallel for schedule(static)
                 for (long id = 0; id < ntr; id++) {
-                    double tr = interpolate(rtr2[id], str2[id], DERr_u, u);
+                    double tr = tr_vel(rtr2[id], str2[id]);
                     rtr[id] = rtr[id] + 2.0 * tr;
                     rtr1[id] = rtr0[id] + dtt * tr;
-                    double ts = interpolate(rtr2[id], str2[id], DERr_w, w);
+                    double ts = ts_vel(rtr2[id], str2[id]);
                     str[id] = str[id] + 2.0 * ts;
                     str1[id] = str0[id] + dtt * ts;
                     if (tt) {
@@ -2244,9 +2298,9 @@ struct Oracle {
                 double dto6 = dt / 6.0;
 #pragma omp parallel for schedule(static)
                 for (long id = 0; id < ntr; id++) {
-                    double tr = interpolate(rtr1[id], str1[id], DERr_u, u);
+                    double tr = tr_vel(rtr1[id], str1[id]);
                     rtr[id] = rtr0[id] + dto6 * (rtr[id] + tr);
-                    double ts = interpolate(rtr1[id], str1[id], DERr_w, w);
+                    double ts = ts_vel(rtr1[id], str1[id]);
                     str[id] = str0[id] + dto6 * (str[id] + ts);
                     if (tt) {
                         double tT = interpolate(rtr1[id], str1[id], DERr_tracer, tsa);

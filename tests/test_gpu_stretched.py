@@ -12,8 +12,10 @@ against the oracle on the same seeded inputs:
     oracle's operator; the mixed solver passes it too;
   - five timesteps: the stats.dat quantities within 1e-6 and the temperature
     within 1e-8;
-  - compositional or temperature tracers on a stretched grid are refused
-    (the tracer metric interpolation is not built).
+  - compositional and temperature tracers: velocities divided by the metric
+    interpolated at the tracer (interpolate_xr / interpolate_zs), positions,
+    counts, C, T and Ttr bit for bit given identical velocities, positions
+    within 1e-10 after full steps.
 """
 import numpy as np
 import pytest
@@ -111,10 +113,64 @@ def test_stretched_steps_parity(gpu_lib, gx, gz):
     assert np.abs(Tg - To).max() <= 1e-8
 
 
-@pytest.mark.parametrize("comp,tracer", [(1, 0), (0, 1)])
-def test_stretched_grid_with_tracers_is_refused(gpu_lib, comp, tracer):
-    p = stretched(1, 2)
-    p.comp, p.tracer = comp, tracer
-    with pytest.raises(TracerError) as e:
-        Simulation(p)
-    assert e.value.status == 2  # TC_ERR_UNSUPPORTED
+def tracer_case(gx, gz, comp, tracer):
+    p = stretched(gx, gz)
+    p.comp, p.tracer, p.tpc = comp, tracer, 4
+    p.RaC[0] = 0.5 * p.RaT if comp else 0.0
+    return p
+
+
+@pytest.mark.parametrize("gx,gz,comp,tracer", [(1, 0, 1, 0), (1, 1, 0, 1), (0, 1, 0, 1)])
+def test_stretched_tracers_bitexact_given_identical_velocities(gpu_lib, gx, gz, comp, tracer):
+    """RK_update = 0: one velocity field for all four stages, so both sides
+    divide identically interpolated velocities by identically interpolated
+    metrics: positions, counts, C and T bit for bit."""
+    p = tracer_case(gx, gz, comp, tracer)
+    p.RK_update = 0
+    g, o = pair(p)
+    g.multigrid()
+    o.set("SF", g.download()["SF"])
+    g.compute_velocities()
+    o.compute_velocities()
+    assert g.energy_time() == o.energy_time()
+    a, b = g.download(), o.download()
+    for k in ("rtr", "str", "T"):
+        assert np.array_equal(a[k], b[k]), k
+    assert np.array_equal(g.counts(), o.counts())
+    if comp:
+        assert np.array_equal(a["Cnew"], b["Cnew"])
+    if tracer:
+        assert np.array_equal(a["Ttr"], b["Ttr"])
+
+
+@pytest.mark.parametrize("gx,gz,comp,tracer", [(1, 0, 1, 0), (1, 1, 0, 1)])
+def test_stretched_tracer_steps_parity(gpu_lib, gx, gz, comp, tracer):
+    p = tracer_case(gx, gz, comp, tracer)
+    g, o = pair(p)
+    for n in range(3):
+        rg, qg, _ = g.step()
+        ro, qo, _ = o.step()
+        assert abs(qg - qo) <= 1, n
+        for k in ("Nu", "vrms", "Tavg"):
+            assert rg[k] == pytest.approx(ro[k], rel=1e-6), (n, k)
+        if comp:
+            assert rg["Cavg"][0] == pytest.approx(ro["Cavg"][0], rel=1e-6)
+    a, b = g.download(), o.download()
+    assert np.abs(a["rtr"] - b["rtr"]).max() <= 1e-10
+    assert np.abs(a["str"] - b["str"]).max() <= 1e-10
+
+
+def test_stretched_dense_layer_stops_as_the_oracle_does(gpu_lib):
+    """comp = 1 with the arctan z-stretching: the oracle's W-cycle stops with
+    TC_ERR_MG_RESIDUAL in the first steps; the GPU path stops there too."""
+    p = tracer_case(1, 1, 1, 0)
+    g, o = pair(p)
+    stop = {}
+    for side, sim in (("gpu", g), ("oracle", o)):
+        try:
+            for n in range(3):
+                sim.step()
+            stop[side] = None
+        except TracerError as e:
+            stop[side] = (n, e.status)
+    assert stop["oracle"] is not None and stop["gpu"] == stop["oracle"]

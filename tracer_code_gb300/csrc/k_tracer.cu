@@ -136,8 +136,15 @@ __global__ void k_tracer_stage(Lay L, Phys P, int torder, int stage, int64_t ntr
     // precedes every stage (the reference stops there); never index with them
     if (!(r > 0.0 && r < P.aspect && s > 0.0 && s < 1.0)) return;
     const TaylorPos tp = taylor_pos(P, r, s);
-    const double tr = taylor_eval(L, P, u, du, tp);
-    const double ts = taylor_eval(L, P, w, dw, tp);
+    double tr = taylor_eval(L, P, u, du, tp);
+    double ts = taylor_eval(L, P, w, dw, tp);
+    // stretched grids: the computational velocity, divided by the metric
+    // interpolated the same way (interpolate_xr / interpolate_zs,
+    // composition.f90:938-998; energy.f90:195-203)
+    if (P.M.gx) tr = tr / (mt(P.M.xr, tp.i) + mt(P.M.dxr, tp.i) * tp.a1);
+    if (P.M.gz)
+        ts = ts / (tp.slo ? mt(P.M.zs, tp.k) + mt(P.M.dzs, tp.k) * (tp.hs / 1.0)
+                          : mt(P.M.zs, tp.k + 1) + mt(P.M.dzs, tp.k + 1) * ((-tp.hs) / 1.0));
     if (tT.f) {
         // energy.f90:213-223, 292-310, 371-375, 437-440
         const double te = taylor_eval(L, P, tT.f, tT.der, tp);
@@ -369,6 +376,16 @@ __global__ void k_tracer_space(Lay L, Phys P, Range2 r, const double* __restrict
         for (int j = 0; j < P.ntype; j++) sC = sC + Cv.p[j][x];
         heat = P.H * (1.0 - sC);
         for (int j = 0; j < P.ntype; j++) heat = P.Htype[j] * Cv.p[j][x] + heat;
+    }
+    if (P.M.on) {
+        // tracer_space on a stretched grid (energy.f90:82-100)
+        const double x1 = mt(P.M.xr, i), z1 = mt(P.M.zs, k);
+        const double kx = cr[x] / x1, kz = cs[x] / z1;
+        const double Tx = Trd / x1, Tz = Tsd / z1;
+        const double Txx = (Trr - Tx * mt(P.M.xrr, i)) / (x1 * x1);
+        const double Tzz = (Tss - Tz * mt(P.M.zss, k)) / (z1 * z1);
+        out[x] = cd[x] * (Txx + Tzz) + (kx * Tx + kz * Tz) + heat;
+        return;
     }
     out[x] = cd[x] * (Trr + Tss) + (cr[x] * Trd + cs[x] * Tsd) + heat;
 }

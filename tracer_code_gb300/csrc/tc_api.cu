@@ -1776,10 +1776,6 @@ tc_status create(Handle* h, const tc_params* in) {
     tc_params& p = h->p;
     if (p.order != 2) { h->err = "the GPU path implements order=2"; return TC_ERR_UNSUPPORTED; }
     if (p.gridX < 0 || p.gridX > 2 || p.gridZ < 0 || p.gridZ > 2) { h->err = "gridX and gridZ must be 0..2"; return TC_ERR_ARG; }
-    if ((p.gridX != 0 || p.gridZ != 0) && (p.comp == 1 || p.tracer == 1)) {
-        h->err = "stretched grids are implemented for the field-temperature path (comp = 0, tracer = 0)";
-        return TC_ERR_UNSUPPORTED;
-    }
     if (p.gridZ == 2 && (p.nbound < 2 || p.nz - 2 * p.nbound + 2 <= 0)) {
         h->err = "gridZ = 2 needs 2 <= nbound and nz > 2 nbound - 2";
         return TC_ERR_ARG;
@@ -1876,6 +1872,8 @@ tc_status create(Handle* h, const tc_params* in) {
     P.Trr_max = -h->eb.Trr / s1.dr2; P.Tss_max = -h->eb.Trr / s1.ds2;
     P.M = Metric{};
     P.M.on = stretched ? 1 : 0;
+    P.M.gx = (p.gridX != 0) ? 1 : 0;
+    P.M.gz = (p.gridZ != 0) ? 1 : 0;
     // ---- stream ----
     cudaGetDevice(&h->device);
     cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
@@ -1979,11 +1977,11 @@ tc_status create(Handle* h, const tc_params* in) {
     std::memset(h->hs, 0, sizeof(DevScalars));
     if (stretched) {
         // the metric arrays, each over fine index -pad..n+pad
-        const std::vector<double>* xs[6] = {&gm.xr, &gm.xrr, &gm.xrrr, &gm.xrrrr, &gm.xr3, &gm.xr4};
-        const std::vector<double>* zs_[6] = {&gm.zs, &gm.zss, &gm.zsss, &gm.zssss, &gm.zs3, &gm.zs4};
-        const double** xd[6] = {&P.M.xr, &P.M.xrr, &P.M.xrrr, &P.M.xrrrr, &P.M.xr3, &P.M.xr4};
-        const double** zd[6] = {&P.M.zs, &P.M.zss, &P.M.zsss, &P.M.zssss, &P.M.zs3, &P.M.zs4};
-        for (int q = 0; q < 6; q++) {
+        const std::vector<double>* xs[7] = {&gm.xr, &gm.xrr, &gm.xrrr, &gm.xrrrr, &gm.xr3, &gm.xr4, &gm.dxr};
+        const std::vector<double>* zs_[7] = {&gm.zs, &gm.zss, &gm.zsss, &gm.zssss, &gm.zs3, &gm.zs4, &gm.dzs};
+        const double** xd[7] = {&P.M.xr, &P.M.xrr, &P.M.xrrr, &P.M.xrrrr, &P.M.xr3, &P.M.xr4, &P.M.dxr};
+        const double** zd[7] = {&P.M.zs, &P.M.zss, &P.M.zsss, &P.M.zssss, &P.M.zs3, &P.M.zs4, &P.M.dzs};
+        for (int q = 0; q < 7; q++) {
             double* dx = nullptr;
             double* dz = nullptr;
             TRY(dalloc_t(h, &dx, xs[q]->size()));

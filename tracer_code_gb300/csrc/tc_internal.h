@@ -49,7 +49,11 @@ size_t IX(const Lay& L, int i, int k) { return (size_t)(i + SP) + (size_t)(k + S
 struct Metric {
     const double *xr, *xrr, *xrrr, *xrrrr, *xr3, *xr4;
     const double *zs, *zss, *zsss, *zssss, *zs3, *zs4;
+    // d(xr)/dr and d(zs)/ds at the nodes (the tracer metric interpolation,
+    // composition.f90:921-936)
+    const double *dxr, *dzs;
     int on;
+    int gx, gz;  // gridX != 0, gridZ != 0: the tracer velocities are divided by the interpolated metric
 };
 
 // scaled eigenvalue bounds of one level (the reference's test_eigenvalues /

@@ -231,8 +231,8 @@ void grid_metrics(double aspect, int nx, int nz, int gridX, int gridZ, double sp
     const double Ax = std::pow(std::atan(spaceX * 0.5) - std::atan(spaceX * (-0.5)), -1.0);
     const double Az = std::pow(std::atan(spaceZ * 0.5) - std::atan(spaceZ * (-0.5)), -1.0);
     auto alloc = [&](std::vector<double>& v, int n) { v.assign((size_t)n + 1 + 2 * P, 0.0); };
-    for (auto* v : {&g.xg, &g.xr, &g.xrr, &g.xrrr, &g.xrrrr, &g.xr3, &g.xr4}) alloc(*v, nx);
-    for (auto* v : {&g.zg, &g.zs, &g.zss, &g.zsss, &g.zssss, &g.zs3, &g.zs4}) alloc(*v, nz);
+    for (auto* v : {&g.xg, &g.xr, &g.xrr, &g.xrrr, &g.xrrrr, &g.xr3, &g.xr4, &g.dxr}) alloc(*v, nx);
+    for (auto* v : {&g.zg, &g.zs, &g.zss, &g.zsss, &g.zssss, &g.zs3, &g.zs4, &g.dzs}) alloc(*v, nz);
     auto X = [&](std::vector<double>& v, int i) -> double& { return v[(size_t)(i + P)]; };
     for (int i = 0; i <= nx; i++) X(g.xg, i) = xgrid(dr * (double)i, aspect, gridX, spaceX, Ax);
     for (int k = 0; k <= nz; k++) X(g.zg, k) = zgrid(ds * (double)k, nz, ds, gridZ, spaceZ, thickness, nbound, Az);
@@ -271,6 +271,9 @@ void grid_metrics(double aspect, int nx, int nz, int gridX, int gridZ, double sp
         X(g.zs3, k) = std::pow(X(g.zs, k), 3.0);
         X(g.zs4, k) = std::pow(X(g.zs, k), 4.0);
     }
+    // compute_metric_interpolator_derivatives: D(1,-1:1) . xr(i-1:i+1) / dr**1
+    for (int i = 0; i <= nx; i++) X(g.dxr, i) = dot(fd.D1, si, g.xr, i) / std::pow(dr, 1.0);
+    for (int k = 0; k <= nz; k++) X(g.dzs, k) = dot(fd.D1, si, g.zs, k) / std::pow(ds, 1.0);
 }
 
 }  // namespace tcs

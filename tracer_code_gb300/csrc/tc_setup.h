@@ -32,6 +32,7 @@ void coarse_bandwidth(int nxc, int nzc, int span, int span1, int& kl, int& ku);
 struct GridMetrics {
     int pad = 3;
     std::vector<double> xg, zg, xr, xrr, xrrr, xrrrr, xr3, xr4, zs, zss, zsss, zssss, zs3, zs4;
+    std::vector<double> dxr, dzs;  // DERxr(1,i), DERzs(1,k) over 0..n (composition.f90:921-936)
 };
 void grid_metrics(double aspect, int nx, int nz, int gridX, int gridZ, double spaceX, double spaceZ,
                   double thickness, int nbound, const FD& fd, GridMetrics& g);

@@ -45,35 +45,43 @@ def sizes(p: Params, nx: int | None = None, nz: int | None = None):
     return nx, nz, span
 
 
-def grid_coordinates(p: Params, nx: int | None = None, nz: int | None = None):
-    """Node coordinates x(i) = xgrid(i dr), i = -span..nx+span, and z(k) =
-    zgrid(k ds) (grid.f90:1-35; Ax, Az as basics.f90:140-141): uniform for
-    gridX/gridZ = 0 (and gridX = 2), arctan stretching for 1, boundary layers
-    of nbound nodes and total thickness `thickness` for gridZ = 2."""
-    nx, nz, span = sizes(p, nx, nz)
-    dr = p.aspect / nx
-    ds = 1.0 / nz
-    r = np.arange(-span, nx + span + 1, dtype=np.float64) * dr
-    s = np.arange(-span, nz + span + 1, dtype=np.float64) * ds
+def xgrid(p: Params, r: np.ndarray) -> np.ndarray:
+    """x(r) of grid.f90:1-12: arctan stretching for gridX = 1 (Ax as
+    basics.f90:140), else x = r."""
+    r = np.asarray(r, dtype=np.float64)
     if p.gridX == 1:
         ax = 1.0 / (np.arctan(p.spaceX * 0.5) - np.arctan(p.spaceX * -0.5))
-        x = p.aspect * (ax * np.arctan(p.spaceX * (r / p.aspect - 0.5)) + 0.5)
-    else:
-        x = r
+        return p.aspect * (ax * np.arctan(p.spaceX * (r / p.aspect - 0.5)) + 0.5)
+    return r
+
+
+def zgrid(p: Params, s: np.ndarray, nz: int | None = None) -> np.ndarray:
+    """z(s) of grid.f90:14-35: arctan stretching for gridZ = 1, boundary layers
+    of nbound nodes and total thickness `thickness` for gridZ = 2, else z = s."""
+    s = np.asarray(s, dtype=np.float64)
+    nz = p.nz if nz is None else nz
+    ds = 1.0 / nz
     if p.gridZ == 1:
         az = 1.0 / (np.arctan(p.spaceZ * 0.5) - np.arctan(p.spaceZ * -0.5))
-        z = az * np.arctan(p.spaceZ * (s - 0.5)) + 0.5
-    elif p.gridZ == 2:
+        return az * np.arctan(p.spaceZ * (s - 0.5)) + 0.5
+    if p.gridZ == 2:
         dzin = (1.0 - 2.0 * p.thickness) / (nz - 2 * p.nbound + 2)
         s1 = (p.nbound - 1) * ds
         s2 = 1.0 - s1
         scale = p.thickness / (np.exp(p.spaceZ * s1) - 1.0)
-        z = np.where(s < s1, scale * (np.exp(p.spaceZ * s) - 1.0),
-                     np.where(s > s2, 1.0 - scale * (np.exp(-p.spaceZ * (s - 1.0)) - 1.0),
-                              p.thickness + (s - s1) * dzin / ds))
-    else:
-        z = s
-    return x, z
+        return np.where(s < s1, scale * (np.exp(p.spaceZ * s) - 1.0),
+                        np.where(s > s2, 1.0 - scale * (np.exp(-p.spaceZ * (s - 1.0)) - 1.0),
+                                 p.thickness + (s - s1) * dzin / ds))
+    return s
+
+
+def grid_coordinates(p: Params, nx: int | None = None, nz: int | None = None):
+    """Node coordinates x(i) = xgrid(i dr), i = -span..nx+span, and z(k) =
+    zgrid(k ds)."""
+    nx, nz, span = sizes(p, nx, nz)
+    r = np.arange(-span, nx + span + 1, dtype=np.float64) * (p.aspect / nx)
+    s = np.arange(-span, nz + span + 1, dtype=np.float64) * (1.0 / nz)
+    return xgrid(p, r), zgrid(p, s, nz)
 
 
 def initial_temperature(p: Params, nx: int | None = None, nz: int | None = None) -> np.ndarray:
@@ -112,7 +120,7 @@ def initial_tracers(p: Params, seed: int = 1, nx: int | None = None, nz: int | N
     r = np.where(r >= p.aspect, p.aspect - dist_r, r)
     s = np.where(s <= 0.0, dist_s, s)
     s = np.where(s >= 1.0, 1.0 - dist_s, s)
-    ttype = np.where(s > p.dlayer, 0, 1).astype(np.int32)
+    ttype = np.where(zgrid(p, s, nz) > p.dlayer, 0, 1).astype(np.int32)
     return np.ascontiguousarray(r), np.ascontiguousarray(s), np.ascontiguousarray(ttype)
 
 
@@ -120,8 +128,7 @@ def initial_composition(p: Params, nx: int | None = None, nz: int | None = None)
     """Cnew(1, i, k) = composition(xg(i), zg(k)) (as in add_tracers,
     composition.f90:654-664): 1 in the dense layer z <= dlayer."""
     nx, nz, span = sizes(p, nx, nz)
-    ds = 1.0 / nz
-    z = np.arange(-span, nz + span + 1, dtype=np.float64) * ds
+    _, z = grid_coordinates(p, nx, nz)
     Cn = np.zeros((nz + 1 + 2 * span, nx + 1 + 2 * span, p.ntype), dtype=np.float64)
     if p.ntype > 0:
         Cn[:, :, 0] = np.where(z <= p.dlayer, 1.0, 0.0)[:, None]
@@ -139,12 +146,12 @@ def initial_state(p: Params, seed: int = 1, nx: int | None = None, nz: int | Non
         if p.comp == 1:
             st["Ttype"] = t
         if p.tracer == 1:
-            st["Ttr"] = initial_tracer_temperature(r, s)
+            st["Ttr"] = initial_tracer_temperature(xgrid(p, r), zgrid(p, s, nz))
     return st
 
 
-def initial_tracer_temperature(r: np.ndarray, s: np.ndarray) -> np.ndarray:
-    """Ttr = temperature(x, z) at each tracer (initialize_tracers,
+def initial_tracer_temperature(x: np.ndarray, z: np.ndarray) -> np.ndarray:
+    """Ttr = temperature(x, z) at each tracer's coordinates (initialize_tracers,
     composition.f90:630-633), with the grid's initial profile
     (1 - z) + 0.01 cos(pi x) sin(pi z)."""
-    return np.ascontiguousarray((1.0 - s) + 0.01 * np.cos(np.pi * r) * np.sin(np.pi * s))
+    return np.ascontiguousarray((1.0 - z) + 0.01 * np.cos(np.pi * x) * np.sin(np.pi * z))
