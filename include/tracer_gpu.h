@@ -76,7 +76,7 @@ typedef struct tc_params {
     int32_t nx, nz;             /* cells; multigrid_setup may change them (optimize_grid) */
     double  aspect;
     int32_t order;              /* space order (even); the GPU path implements order=2   */
-    int32_t gridX, gridZ;       /* 0 = uniform (GPU path: uniform only)                  */
+    int32_t gridX, gridZ;       /* 0 uniform; gridX 1 arctan; gridZ 1 arctan, 2 layers  */
     double  spaceX, spaceZ, thickness;
     int32_t nbound;
     /* velocity solver options (main.f90:23-34) */
@@ -339,15 +339,21 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path);
  * nodes (grid.f90:46-54, 97-108): xg(-3:nx+3), zg(-3:nz+3). */
 void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg);
 
+/* build_grid's node coordinates of a handle (grid.f90:37-109, restart = 0:
+ * xgrid(i dr), zgrid(k ds) with the mirrored ghosts), xg[i + 3] for i =
+ * -3..nx+3 and zg[k + 3] for k = -3..nz+3; on a uniform grid they equal
+ * tc_restart_grid's. */
+tc_status tc_grid_coordinates(const tc_handle* h, double* xg, double* zg);
+
 /* print_restart for a handle: downloads the state and writes Trestart (and
  * restart_tracers when comp = 1 or tracer = 1 and `tracers` is not NULL),
- * the coordinates from tc_restart_grid. */
+ * the coordinates from tc_grid_coordinates. */
 tc_status tc_write_restart(tc_handle* h, const char* trestart, const char* tracers);
 
 /* build_grid's restart branch for a handle: reads Trestart (and
  * restart_tracers when comp = 1 or tracer = 1; then `tracers` must not be
  * NULL) and uploads them with tc_upload_state_ex.  The file's xg, zg are read and
- * dropped: the GPU path uses the uniform grid of the handle. */
+ * dropped: the handle keeps the grid its parameters build (tc_grid_coordinates). */
 tc_status tc_read_restart(tc_handle* h, const char* trestart, const char* tracers);
 
 /* Module clock: basics::tstep and basics::time, owned by the host loop. */

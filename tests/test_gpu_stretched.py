@@ -174,3 +174,23 @@ def test_stretched_dense_layer_stops_as_the_oracle_does(gpu_lib):
         except TracerError as e:
             stop[side] = (n, e.status)
     assert stop["oracle"] is not None and stop["gpu"] == stop["oracle"]
+
+
+def test_stretched_coordinates_in_the_handle_and_its_restart_file(gpu_lib, tmp_path):
+    """The handle's node coordinates are build_grid's xgrid / zgrid (within
+    the libm difference to numpy's), and tc_write_restart writes them."""
+    from tracer_code_gb300 import restart
+    p = stretched(1, 2)
+    g = Simulation(p)
+    g.upload(state.initial_state(p, seed=1))
+    xg, zg = g.grid_coordinates()
+    x, z = state.grid_coordinates(p)
+    # interior nodes (the handle's ghosts mirror about the walls)
+    assert np.allclose(xg[3:3 + p.nx + 1], x[2:2 + p.nx + 1], rtol=0, atol=1e-14)
+    assert np.allclose(zg[3:3 + p.nz + 1], z[2:2 + p.nz + 1], rtol=0, atol=1e-14)
+    assert xg[3] == 0.0 and xg[3 + p.nx] == p.aspect and zg[3] == 0.0 and zg[3 + p.nz] == 1.0
+    path = str(tmp_path / "Trestart")
+    g.write_restart(path)
+    d = restart.read_trestart(path, p.nx, p.nz, 0, True)
+    assert np.array_equal(d["xg"], xg) and np.array_equal(d["zg"], zg)
+    g.close()

@@ -37,7 +37,7 @@ EXPORTS = [
     "tc_restart_grid", "tc_write_restart", "tc_read_restart", "tc_format_g", "tc_format_stats_line",
     "tc_format_vis_line", "tc_write_snapshot", "tc_upload_state_ex", "tc_download_tracer_temperature",
     "tc_equalize_row", "tc_format_equalize_line", "tc_set_step_graph", "tc_step_graph_info",
-    "tc_ensemble_create", "tc_ensemble_run", "tc_ensemble_info", "tc_ensemble_destroy",
+    "tc_ensemble_create", "tc_ensemble_run", "tc_ensemble_info", "tc_ensemble_destroy", "tc_grid_coordinates",
 ]
 
 
@@ -118,6 +118,7 @@ def load_library(build_if_missing: bool = False):
         L.tc_ensemble_run.argtypes = [vp, C.POINTER(vp), C.c_int32, vp, vp, vp, vp]
         L.tc_ensemble_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.tc_ensemble_destroy.argtypes = [vp]
+        L.tc_grid_coordinates.argtypes = [vp, vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]
@@ -265,6 +266,12 @@ class Simulation:
         row = StatsRow(); q = C.c_int32(0); dt = C.c_double(0)
         self._chk(self.L.tc_step(self.h, C.byref(row), C.byref(q), C.byref(dt)), "step")
         return row.as_dict(), q.value, dt.value
+
+    def grid_coordinates(self):
+        """(xg, zg): the handle's node coordinates, index i + 3 for i = -3..n+3."""
+        xg = np.empty(self.nx + 7); zg = np.empty(self.nz + 7)
+        self._chk(self.L.tc_grid_coordinates(self.h, _ptr(xg), _ptr(zg)), "grid_coordinates")
+        return xg, zg
 
     def set_step_graph(self, on: bool = True) -> None:
         """From the next ready step on, each tc_step is one captured graph

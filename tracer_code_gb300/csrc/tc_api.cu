@@ -200,6 +200,7 @@ struct Handle {
     long long sub_tab_key = -1;                    // the sweep tables now in sub_tab
     long long graph_steps = 0;                     // steps run as one graph launch
     long long epoch = 0;  // bumped whenever a captured step would be stale (launch shapes, network, stream)
+    std::vector<double> xg_h, zg_h;  // node coordinates of build_grid, index i + 3 for i = -3..n+3
 };
 
 constexpr int kMaxSnap = 64;
@@ -1851,6 +1852,8 @@ tc_status create(Handle* h, const tc_params* in) {
     tcs::GridMetrics gm;
     tcs::grid_metrics(p.aspect, nx, nz, p.gridX, p.gridZ, p.spaceX, p.spaceZ, p.thickness, p.nbound, fd, gm);
     const bool stretched = (p.gridX != 0 || p.gridZ != 0);
+    h->xg_h = gm.xg;
+    h->zg_h = gm.zg;
     // entrainment_setup (composition.f90:582-591)
     h->kent = 0;
     for (int k = 0; k <= nz; k++)
@@ -2615,6 +2618,13 @@ tc_status tc_get_info(const tc_handle* H, tc_info* info) {
     info->ku = h->ku;
     for (int l = 1; l <= h->grids && l <= 8; l++) { info->nx_grid[l - 1] = h->lev[l].L.a; info->nz_grid[l - 1] = h->lev[l].L.b; }
     info->dr = h->grid_dr; info->ds = h->grid_ds;
+    return TC_OK;
+}
+
+tc_status tc_grid_coordinates(const tc_handle* H, double* xg, double* zg) {
+    if (!H || !xg || !zg) return TC_ERR_ARG;
+    std::copy(H->h.xg_h.begin(), H->h.xg_h.end(), xg);
+    std::copy(H->h.zg_h.begin(), H->h.zg_h.end(), zg);
     return TC_OK;
 }
 

@@ -182,7 +182,8 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path) {
     if (st == TC_OK && counted) st = tc_download_counts(h, cnt.data());
     if (st != TC_OK) return st;
     std::vector<double> xg(nx + 7), zg(nz + 7);
-    tc_restart_grid(nx, nz, p.aspect, xg.data(), zg.data());
+    st = tc_grid_coordinates(h, xg.data(), zg.data());
+    if (st != TC_OK) return st;
     FILE* f = std::fopen(path, "w");
     if (!f) return TC_ERR_ARG;
     std::string line;

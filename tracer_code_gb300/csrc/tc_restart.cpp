@@ -162,7 +162,8 @@ tc_status tc_write_restart(tc_handle* h, const char* trestart, const char* trace
                           trc ? st.data() : nullptr, tt.empty() ? nullptr : tt.data());
     if (s == TC_OK && !Tt.empty()) s = tc_download_tracer_temperature(h, Tt.data());
     if (s != TC_OK) return s;
-    tc_restart_grid(nx, nz, p.aspect, xg.data(), zg.data());
+    s = tc_grid_coordinates(h, xg.data(), zg.data());
+    if (s != TC_OK) return s;
     s = tc_restart_write(trestart, nx, nz, ntype, p.RaT != 0.0, xg.data(), zg.data(), T.data(), C.data(), SF.data());
     if (s != TC_OK || !trc || !tracers) return s;
     return tc_restart_tracers_write(tracers, info.ntr, r.data(), st.data(), tt.empty() ? nullptr : tt.data(),
