@@ -1,5 +1,6 @@
 """The 2048x512 configuration (Ra = 1e8, contrast 1e6 x 30, 6 levels) does
-not converge under the reference's multigrid, on the CPU oracle itself.
+not converge under the reference's multigrid, on the CPU oracle itself (the
+windowed correction makes it converge: tests/test_gpu_config3.py).
 
 tests/golden/make_config3_trace.py ran the oracle's first solve of the
 seeded state (capped W-cycles, both coarse-level starts) and committed the
