@@ -78,6 +78,28 @@ def test_graph_steps_equal_eager_steps(gpu_lib, prec, cc):
     assert graph[2] == (11, 1)  # every step after the first was one graph launch
 
 
+@pytest.mark.parametrize("gx,gz", [(0, 0), (1, 1)])
+def test_graph_steps_with_temperature_tracers(gpu_lib, gx, gz):
+    """Temperature tracers (tracer = 1, comp = 0): the stage's tracers_to_corners
+    and T filter inside the captured step; uniform and stretched grids."""
+    p = case(prec=0, cc=0, Ra=1e5, visT=100.0)
+    p.comp, p.tracer, p.RaC[0] = 0, 1, 0.0
+    p.gridX, p.gridZ, p.spaceX, p.spaceZ = gx, gz, 2.0, 1.0
+    eager = run(p, 5, 6, False)
+    graph = run(p, 5, 6, True)
+    assert_same_fields(eager, graph, ("T", "SF", "rtr", "str", "Ttr"))
+    assert graph[2] == (5, 1)
+
+
+def assert_same_fields(a, b, keys):
+    (ra, da, _), (rb, db, _) = a, b
+    for (row_a, qa, dta), (row_b, qb, dtb) in zip(ra, rb):
+        assert qa == qb and dta == dtb
+        assert row_a == row_b
+    for k in keys:
+        assert np.array_equal(da[k], db[k]), k
+
+
 def test_graph_steps_equal_eager_steps_at_512x128(gpu_lib):
     p = case(nx=512, nz=128, grids=5, prec=1, Ra=3e6, visT=3e3, tpc=6)
     assert_same(run(p, 5, 4, False), run(p, 5, 4, True))
