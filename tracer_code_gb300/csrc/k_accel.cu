@@ -263,7 +263,12 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
     pdl_entry();
     const int n = __ldcg(&ds->win_n), head = __ldcg(&ds->win_head);
     const int nold = min(n, TC_WIN - 1);
-    const int nd = 1 + nold + (use_dnn ? 1 : 0);
+    // the network's direction joins the corrections while the window of
+    // changes fills; once it holds TC_WIN changes their span has taken up
+    // what the direction adds, and the correction costs what it costs
+    // without the network
+    const int dnn_now = (use_dnn && n < TC_WIN) ? 1 : 0;
+    const int nd = 1 + nold + dnn_now;
     const int snew = (n == 0) ? 0 : (head + 1) % TC_WIN;
     double s[kWS];
 #pragma unroll
@@ -378,6 +383,7 @@ __global__ void __launch_bounds__(256) k_win_dots(Lay L, const double* __restric
         }
         for (int i = 0; i < kWD; i++) ds->win_beta[i] = beta[i];
         ds->win_nd = nd;
+        ds->win_dnn = dnn_now;
         ds->win_head = snew;
         ds->win_n = min(n + 1, TC_WIN);
         *rs.count = 0u;
@@ -401,7 +407,8 @@ __global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const d
     if (inr) {
     const size_t x = IX(L, i, k);
     const int nd = __ldcg(&ds->win_nd), head = __ldcg(&ds->win_head);
-    const int nold = nd - 1 - (use_dnn ? 1 : 0);
+    const int dnn_now = use_dnn ? __ldcg(&ds->win_dnn) : 0;
+    const int nold = nd - 1 - dnn_now;
     double beta[kWD], pv[kWD], av[kWD];
 #pragma unroll
     for (int j = 0; j < kWD; j++) beta[j] = __ldcg(&ds->win_beta[j]);
@@ -415,7 +422,7 @@ __global__ void k_win_update(Lay L, Range2 r, double* psi, double* prev, const d
             const size_t o = (size_t)win_slot(head, j) * L.plane + x;
             pv[j] = ld_state(P + o);
             av[j] = ld_state(AP + o);
-        } else if (use_dnn && j == nd - 1) {
+        } else if (dnn_now && j == nd - 1) {
             pv[j] = ld_state(dnn + x);
             av[j] = ld_state(adnn + x);
         }

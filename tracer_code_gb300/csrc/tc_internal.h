@@ -113,9 +113,10 @@ struct DevScalars {
     int    net_fail;         // the network's bounded-wait flag, copied after each forward pass
     // windowed correction (cycle_correction 3/4, k_accel.cu): coefficients of
     // the last correction (newest change first, the network's direction
-    // last), stored changes, slot of the newest, directions used
+    // last), stored changes, slot of the newest, directions used, and
+    // whether the network's direction was one of them
     double win_beta[TC_WIN + 1];
-    int    win_n, win_head, win_nd, win_pad;
+    int    win_n, win_head, win_nd, win_dnn;
     // filter loops on the device (k_loop.cu): the factor of the next
     // smoothing step, the loop counters, the counts and the fine-level
     // eigenvalue ratio they report, and TC_ERR_LOOP_CAP when a loop hit
