@@ -194,3 +194,37 @@ def test_stretched_coordinates_in_the_handle_and_its_restart_file(gpu_lib, tmp_p
     d = restart.read_trestart(path, p.nx, p.nz, 0, True)
     assert np.array_equal(d["xg"], xg) and np.array_equal(d["zg"], zg)
     g.close()
+
+
+@pytest.mark.parametrize("gx,gz", [(1, 0), (0, 1), (1, 2)])
+def test_stretched_time_step_tables_bitexact(gpu_lib, gx, gz):
+    """The smoothers' pseudo-time steps with the metrics (stability_RK4_smoother,
+    stability_vis_smoother) are host tables: bit for bit with the oracle."""
+    p = stretched(gx, gz)
+    g, o = pair(p)
+    assert np.array_equal(interior(g.get("dts_array"), p.nx, p.nz), interior(o.get("dts_array"), p.nx, p.nz))
+    for lev in range(1, g.info.grids + 1):
+        nxl, nzl = g.info.nx_grid[lev - 1], g.info.nz_grid[lev - 1]
+        a = g.get("dt_vis", lev)[SP + 1:SP + nzl, SP:SP + nxl + 1]
+        b = o.get("dt_vis", lev)[SP + 1:SP + nzl, SP:SP + nxl + 1]
+        assert np.array_equal(a, b), lev
+
+
+@pytest.mark.parametrize("gx,gz", [(1, 0), (1, 1)])
+def test_stretched_viscosity_derivatives_and_local_steps(gpu_lib, gx, gz):
+    """After a solve's level setup: the metric viscosity derivatives, the
+    eigenvalue ratio and the local time step of every level (eigR / eigI with
+    the chain rule) against the oracle's, within 1e-10 of each field's largest
+    value (the level viscosity agrees to 1e-12, its exp differing in the last
+    ulp at most, and differencing amplifies that)."""
+    p = stretched(gx, gz)
+    g, o = pair(p)
+    g.multigrid()
+    o.multigrid()
+    for lev in range(1, g.info.grids):
+        nxl, nzl = g.info.nx_grid[lev - 1], g.info.nz_grid[lev - 1]
+        for name in ("vis_x", "vis_z", "vis_xx", "vis_zz", "vis_xz", "dt_stream"):
+            a = g.get(name, lev)[SP + 1:SP + nzl, SP + 1:SP + nxl]
+            b = o.get(name, lev)[SP + 1:SP + nzl, SP + 1:SP + nxl]
+            scale = np.abs(b).max()
+            assert np.abs(a - b).max() <= 1e-10 * scale, (lev, name)
