@@ -183,8 +183,6 @@ struct Handle {
     double *win_p = nullptr, *win_ap = nullptr;  // windowed correction: TC_WIN changes and their images
     double *win_rn = nullptr, *win_rp = nullptr, *win_adnn = nullptr;  // r of psi, of prev; A dnn
     bool acc_dnn_on = false;  // the current solve has a network direction
-    cudaStream_t net_st = nullptr;  // the network's forward pass, beside the solve's setup
-    cudaEvent_t net_fork = nullptr, net_join = nullptr;
     // whole-step graphs (tc_set_step_graph, tc_ensemble_*): while a step is
     // captured, each point where the host would read the device scalars
     // instead records them into hsnap[k] (a copy node of the graph) and
@@ -1364,34 +1362,8 @@ tc_status multigrid(Handle* h) {
     // cycle_correction = 2 / 4: d spans the correction with the cycles' own)
     h->acc_dnn_on = h->net != nullptr && !nonN && h->acc_dnn != nullptr &&
                     (h->p.learned_guess == 3 || h->p.cycle_correction == 2 || h->p.cycle_correction == 4);
-    // with the fields the network reads in place (level 1's viscosity, the
-    // RHS, the start), its forward pass runs on a side stream while the
-    // coarse factors and the bottom-of-cycle matrices are built
-    bool dnn_forked = false;
-    auto fork_network = [&]() -> tc_status {
-        if (!h->acc_dnn_on) return TC_OK;
-        cudaStream_t ns = h->st;
-        if (h->net_st) {
-            CK(cudaEventRecord(h->net_fork, h->st));
-            CK(cudaStreamWaitEvent(h->net_st, h->net_fork, 0));
-            ns = h->net_st;
-        }
-        if (nn_guess(h->net, ns, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
-                     h->p.Vbc, h->p.learned_smooth) != 0) {
-            h->err = "learned guess: network forward failed";
-            return TC_ERR_CUDA;
-        }
-        CK(cudaMemcpyAsync(&h->ds->net_fail, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToDevice, ns));
-        launch_plane_diff(ns, h->acc_dnn, h->guess, cur_err(h, 1), h->L1.plane);
-        if (h->net_st) CK(cudaEventRecord(h->net_join, h->net_st));
-        dnn_forked = true;
-        return TC_OK;
-    };
-    // (a start the host chooses, learned_guess 1 or 2, runs the network first: no overlap)
-    const bool overlap_net = !(h->p.learned_guess == 1 || h->p.learned_guess == 2);
     if (!nonN) {
         TRY(level_setup());
-        if (overlap_net) TRY(fork_network());
         const bool rebuild = (h->time == 0.0 || h->p.ivis > 0 || !h->lu_valid);
         if (rebuild) coarse_setup();
         if (h->sub_on && (rebuild || !h->sub_valid)) TRY(subcycle_setup());
@@ -1421,12 +1393,13 @@ tc_status multigrid(Handle* h) {
         launch_residual(h->st, h->lev[1], h->guess, h->rs, &h->ds->res_mag[0]);
     }
     if (h->acc_dnn_on) {
-        if (dnn_forked) {
-            if (h->net_st) CK(cudaStreamWaitEvent(h->st, h->net_join, 0));
-        } else {
-            TRY(fork_network());
-            if (h->net_st) CK(cudaStreamWaitEvent(h->st, h->net_join, 0));
+        if (nn_guess(h->net, h->st, h->lev[1].L, cur_vis(h, 1), h->lev[1].rhs, cur_err(h, 1), h->nn_raw, h->guess,
+                     h->p.Vbc, h->p.learned_smooth) != 0) {
+            h->err = "learned guess: network forward failed";
+            return TC_ERR_CUDA;
         }
+        CK(cudaMemcpyAsync(&h->ds->net_fail, net_fail(h->net), sizeof(int), cudaMemcpyDeviceToDevice, h->st));
+        launch_plane_diff(h->st, h->acc_dnn, h->guess, cur_err(h, 1), h->L1.plane);
         if (h->p.learned_guess == 3)
             launch_accel(h->st, h->lev[1], cur_err(h, 1), nullptr, h->acc_dnn, TC_ACCEL_DNN, TC_ACCEL_NONE, 0, h->rs,
                          h->ds, h->p.Vbc);
@@ -2589,11 +2562,6 @@ tc_status tc_attach_net(tc_handle* H, tc_net* net) {
         if (!h->nn_raw) TRY(dalloc_t(h, &h->nn_raw, (size_t)3 * h->nx * h->nz));
     }
     h->net = n;
-    if (n && !h->net_st) {
-        CK(cudaStreamCreateWithFlags(&h->net_st, cudaStreamNonBlocking));
-        CK(cudaEventCreateWithFlags(&h->net_fork, cudaEventDisableTiming));
-        CK(cudaEventCreateWithFlags(&h->net_join, cudaEventDisableTiming));
-    }
     drop_step_graphs(h);
     return TC_OK;
 }
@@ -2636,10 +2604,6 @@ tc_status tc_destroy(tc_handle* H) {
     drop_step_graphs(h);
     if (h->hsnap) cudaFreeHost(h->hsnap);
     if (h->body_st) cudaStreamDestroy(h->body_st);
-    if (h->net_st) cudaStreamSynchronize(h->net_st);
-    if (h->net_fork) cudaEventDestroy(h->net_fork);
-    if (h->net_join) cudaEventDestroy(h->net_join);
-    if (h->net_st) cudaStreamDestroy(h->net_st);
     if (h->own_stream && h->st) cudaStreamDestroy(h->st);
     delete H;
     return TC_OK;
