@@ -2652,6 +2652,14 @@ int tco_scalars(void* h, double* out8) {
     out8[4] = o->delta_T; out8[5] = o->res_ref[1]; out8[6] = o->residual_mag[1]; out8[7] = o->last_cycles;
     return TC_OK;
 }
+// build_grid's node coordinates: xg(-3:nx+3), zg(-3:nz+3)
+int tco_coordinates(void* h, double* xg, double* zg) {
+    Oracle* o = (Oracle*)h;
+    for (int i = -3; i <= o->nx + 3; i++) xg[i + 3] = o->xg(i);
+    for (int k = -3; k <= o->nz + 3; k++) zg[k + 3] = o->zg(k);
+    return TC_OK;
+}
+
 int tco_eig_bases(void* h, double* out12) {
     Oracle* o = (Oracle*)h;
     double v[12] = {o->Tr_base, o->Trr_base, o->Trrr_base, o->Trrrr_base, o->Ts_base, o->Tss_base,

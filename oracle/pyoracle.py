@@ -73,6 +73,7 @@ def lib():
             L.tco_smoother_time_T.argtypes = [vp]
             L.tco_scalars.argtypes = [vp, dp]
             L.tco_eig_bases.argtypes = [vp, dp]
+            L.tco_coordinates.argtypes = [vp, dp, dp]
             L.tco_fd_coefficients.argtypes = [vp, dp]
             L.tco_coarse_matrix.argtypes = [vp, dp, dp]
             L.tco_set_threads.argtypes = [C.c_int]
@@ -273,6 +274,12 @@ class Oracle:
         self.L.tco_scalars(self.h, out)
         keys = ["eig_fine", "n_eta", "n_temp", "dt", "delta_T", "res_ref1", "residual_mag1", "cycles"]
         return dict(zip(keys, out.tolist()))
+
+    def coordinates(self):
+        """(xg, zg): build_grid's node coordinates, index i + 3 for i = -3..n+3."""
+        xg = np.empty(self.nx + 7); zg = np.empty(self.nz + 7)
+        self.L.tco_coordinates(self.h, xg, zg)
+        return xg, zg
 
     def eig_bases(self) -> dict:
         out = np.empty(12)

@@ -1,0 +1,31 @@
+"""The initial state's node coordinates (tracer_code_gb300.state.grid_coordinates,
+numpy) are build_grid's (grid.f90:1-109) as the oracle builds them, on the
+uniform, arctan and boundary-layer grids: equal on a uniform grid, within the
+libm difference (1e-14) on stretched ones."""
+import numpy as np
+import pytest
+
+from tracer_code_gb300 import state
+from tracer_code_gb300.abi import default_params
+
+
+@pytest.mark.parametrize("gx,gz", [(0, 0), (1, 0), (0, 1), (1, 2), (2, 2)])
+def test_initial_state_coordinates_are_build_grids(gx, gz):
+    from oracle.pyoracle import Oracle
+    p = default_params()
+    p.nx, p.nz, p.aspect, p.grids = 64, 32, 2.0, 3
+    p.comp, p.tracer = 0, 0
+    p.gridX, p.gridZ, p.spaceX, p.spaceZ, p.thickness, p.nbound = gx, gz, 2.0, 1.5, 0.1, 4
+    xg, zg = Oracle(p).coordinates()
+    x, z = state.grid_coordinates(p)
+    # interior nodes (build_grid mirrors its ghosts about the walls)
+    xi, zi = xg[3:3 + p.nx + 1], zg[3:3 + p.nz + 1]
+    assert np.allclose(x[2:2 + p.nx + 1], xi, rtol=0, atol=1e-14)
+    assert np.allclose(z[2:2 + p.nz + 1], zi, rtol=0, atol=1e-14)
+    if gx == 0:
+        assert np.array_equal(x[2:2 + p.nx], xi[:-1])
+    if gz == 0:
+        assert np.array_equal(z[2:2 + p.nz], zi[:-1])
+    # monotone nodes, ends on the walls
+    assert np.all(np.diff(xi) > 0) and np.all(np.diff(zi) > 0)
+    assert xi[0] == 0.0 and xi[-1] == p.aspect and zi[0] == 0.0 and zi[-1] == 1.0
