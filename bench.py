@@ -241,7 +241,10 @@ def run_reference(args, rank: int, world: int):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": len(times),
         "steps_requested": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(workload_desc(p, "plain"), mg_zero_coarse=p.mg_zero_coarse),
+        "config": dict(workload_desc(p, "plain"), mg_zero_coarse=p.mg_zero_coarse,
+                       solver="the reference's plain FP64 multigrid restated on the CPU (W-cycle, Chebyshev-"
+                              "Richardson smoother, banded LU coarse solve, every level visit and coarse solve "
+                              "carried out), coarse corrections restart from zero (mg_zero_coarse=1)"),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{len(times)} whole timesteps of the CPU restatement from the seeded initial "
                                    f"state (every solve to the 1e-8 test), wall clock; W-cycles per step {cycles}; "
