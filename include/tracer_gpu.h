@@ -436,7 +436,7 @@ tc_status tc_ensemble_step(tc_handle* const* hs, int32_t n, int32_t nthreads, tc
  * failing step may differ: a graph step runs to its end).  Steps that need a
  * host decision run eagerly: the first step, non_Newtonian = 1, equalize =
  * 1, learned_guess 1 or 2, a solve recorder, the host loops.  A capture the
- * driver refuses switches the handle back to eager steps (state 2).
+ * CUDA runtime refuses switches the handle back to eager steps (state 2).
  * tc_step_graph_info: steps run as one graph, state 0 off / 1 on / 2
  * refused. */
 tc_status tc_set_step_graph(tc_handle* h, int32_t on);

@@ -1,4 +1,4 @@
-// tc_api.cu -- the C ABI of include/tracer_gpu.h and the host-side drivers
+// tc_api.cu -- the C ABI of include/tracer_gpu.h and the host-side sequencing
 // that sequence the kernels exactly as the reference sequences its loops.
 //
 // Control flow replaces these reference subroutines (one C++ function each,
@@ -324,7 +324,7 @@ tc_status sync_point(Handle* h, std::function<tc_status()> post) {
 // Inside a step being captured on h->st: pre(cond), then a WHILE node on
 // cond whose body(cond) is captured on body_st into the node's body graph.
 // The body's kernels are taken out of the launch count (*n_body holds them).
-// False (with h->enq_err set) when the driver refuses.
+// False (with h->enq_err set) when the CUDA runtime refuses.
 bool emit_while(Handle* h, const std::function<void(cudaGraphConditionalHandle)>& pre,
                 const std::function<void(cudaGraphConditionalHandle)>& body, long long* n_body) {
     *n_body = 0;
@@ -370,7 +370,7 @@ bool emit_while(Handle* h, const std::function<void(cudaGraphConditionalHandle)>
 
 // A graph of pre(cond) followed by a WHILE node on cond whose body is
 // body(cond), captured from the handle's stream; the kernels of body are
-// counted by the check kernels, not here.  False when the driver refuses.
+// counted by the check kernels, not here.  False when the CUDA runtime refuses.
 bool build_while_graph(Handle* h, const std::function<void(cudaGraphConditionalHandle)>& pre,
                        const std::function<void(cudaGraphConditionalHandle)>& body, cudaGraphExec_t* out) {
     cudaGraph_t g = nullptr;
@@ -430,7 +430,7 @@ bool build_while_graph(Handle* h, const std::function<void(cudaGraphConditionalH
 }
 
 // The cached filter graph `key`, built by make() on first use; null when
-// graphs are off or the driver refused one (from then on the host loops
+// graphs are off or the CUDA runtime refused one (from then on the host loops
 // run, after the device's filter state was read back).
 cudaGraphExec_t filter_graph(Handle* h, int key, const std::function<bool(cudaGraphExec_t*)>& make) {
     if (h->flt_failed || h->no_graphs || h->no_device_loop) return nullptr;
@@ -1132,7 +1132,7 @@ struct CycleGraphs {
     // kernels before the WHILE node and in its body
     cudaGraphExec_t loop = nullptr;
     long long n_pre = 0, n_body = 0;
-    bool loop_failed = false;  // the driver refused the conditional node: host loop
+    bool loop_failed = false;  // the CUDA runtime refused the conditional node: host loop
     int ratio_level = -1, zero = -1, dir1 = -1, dnn = -1;
     cudaStream_t st = nullptr;
 };
@@ -1159,7 +1159,7 @@ tc_status capture(Handle* h, cudaGraphExec_t* out, void (*fn)(Handle*, int), int
 // whose body is [rest of the cycle, level-1 visit, check]; both parts are
 // filled by stream capture (cudaStreamBeginCaptureToGraph).  Returns false
 // (with the stream out of capture and no error left pending) when the
-// driver does not take the conditional node.
+// CUDA runtime does not take the conditional node.
 bool build_loop_graph(Handle* h, void (*f_l1)(Handle*, int), void (*f_rest)(Handle*, int), int dir1,
                       cudaGraphExec_t* out, long long* n_pre, long long* n_body) {
     cudaGraph_t g = nullptr;
@@ -2359,7 +2359,7 @@ tc_status finish_step(Handle* h, const StepGraph& sg, tc_stats_row* row, int32_t
 
 // tc_step as one graph launch: the step's graph for this sort flag (captured
 // on first use), one synchronisation, then the deferred host work.  False in
-// *ran when the step must run eagerly (a capture the driver refused).
+// *ran when the step must run eagerly (a capture the CUDA runtime refused).
 tc_status step_as_graph(Handle* h, tc_stats_row* row, int32_t* cycles, double* dt_out, bool* ran) {
     *ran = false;
     const int key = sorts_this_step(h) ? 1 : 0;
@@ -2973,7 +2973,7 @@ tc_status tc_ensemble_run(tc_ensemble* e, tc_handle* const* hs, int32_t n, tc_st
                     e->cache.erase(e->cache.begin());
                 }
             } else {
-                e->failed = true;  // the driver refused the capture: the thread pool from now on
+                e->failed = true;  // the CUDA runtime refused the capture: the thread pool from now on
             }
         }
     }
