@@ -339,6 +339,13 @@ tc_status tc_write_snapshot(tc_handle* h, const char* path);
  * nodes (grid.f90:46-54, 97-108): xg(-3:nx+3), zg(-3:nz+3). */
 void tc_restart_grid(int32_t nx, int32_t nz, double aspect, double* xg, double* zg);
 
+/* build_grid's metrics for the grid of `p` (p->nx, p->nz as given; host
+ * only, no device needed): x5 receives five arrays of nx+7 doubles, xr, xrr,
+ * xrrr, xrrrr and DERxr (composition.f90:921-936), each at [i + 3]; z5 the
+ * same five for z over nz+7.  Entries outside the reference's ranges (xr,
+ * xrr: -1..nx+1; the others 0..nx) are 0. */
+tc_status tc_grid_metrics(const tc_params* p, double* x5, double* z5);
+
 /* build_grid's node coordinates of a handle (grid.f90:37-109, restart = 0:
  * xgrid(i dr), zgrid(k ds) with the mirrored ghosts), xg[i + 3] for i =
  * -3..nx+3 and zg[k + 3] for k = -3..nz+3; on a uniform grid they equal

@@ -2652,6 +2652,25 @@ int tco_scalars(void* h, double* out8) {
     out8[4] = o->delta_T; out8[5] = o->res_ref[1]; out8[6] = o->residual_mag[1]; out8[7] = o->last_cycles;
     return TC_OK;
 }
+// build_grid's metrics, layout of tc_grid_metrics: xr, xrr, xrrr, xrrrr, DERxr
+// over -3..nx+3 (0 outside their ranges), the same for z
+int tco_metrics(void* h, double* x5, double* z5) {
+    Oracle* o = (Oracle*)h;
+    const int nx = o->nx, nz = o->nz, si = o->span_interp;
+    const size_t lx = (size_t)nx + 7, lz = (size_t)nz + 7;
+    std::fill(x5, x5 + 5 * lx, 0.0);
+    std::fill(z5, z5 + 5 * lz, 0.0);
+    for (int i = -si; i <= nx + si; i++) { x5[i + 3] = o->xr(i); x5[lx + i + 3] = o->xrr(i); }
+    for (int i = 0; i <= nx; i++) {
+        x5[2 * lx + i + 3] = o->xrrr(i); x5[3 * lx + i + 3] = o->xrrrr(i); x5[4 * lx + i + 3] = o->DERxr[1](i);
+    }
+    for (int k = -si; k <= nz + si; k++) { z5[k + 3] = o->zs(k); z5[lz + k + 3] = o->zss(k); }
+    for (int k = 0; k <= nz; k++) {
+        z5[2 * lz + k + 3] = o->zsss(k); z5[3 * lz + k + 3] = o->zssss(k); z5[4 * lz + k + 3] = o->DERzs[1](k);
+    }
+    return TC_OK;
+}
+
 // build_grid's node coordinates: xg(-3:nx+3), zg(-3:nz+3)
 int tco_coordinates(void* h, double* xg, double* zg) {
     Oracle* o = (Oracle*)h;

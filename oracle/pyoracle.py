@@ -74,6 +74,7 @@ def lib():
             L.tco_scalars.argtypes = [vp, dp]
             L.tco_eig_bases.argtypes = [vp, dp]
             L.tco_coordinates.argtypes = [vp, dp, dp]
+            L.tco_metrics.argtypes = [vp, dp, dp]
             L.tco_fd_coefficients.argtypes = [vp, dp]
             L.tco_coarse_matrix.argtypes = [vp, dp, dp]
             L.tco_set_threads.argtypes = [C.c_int]
@@ -280,6 +281,12 @@ class Oracle:
         xg = np.empty(self.nx + 7); zg = np.empty(self.nz + 7)
         self.L.tco_coordinates(self.h, xg, zg)
         return xg, zg
+
+    def metrics(self):
+        """(x5, z5): xr, xrr, xrrr, xrrrr, DERxr (and z) as rows over -3..n+3."""
+        x5 = np.empty(5 * (self.nx + 7)); z5 = np.empty(5 * (self.nz + 7))
+        self.L.tco_metrics(self.h, x5, z5)
+        return x5.reshape(5, -1), z5.reshape(5, -1)
 
     def eig_bases(self) -> dict:
         out = np.empty(12)

@@ -29,3 +29,30 @@ def test_initial_state_coordinates_are_build_grids(gx, gz):
     # monotone nodes, ends on the walls
     assert np.all(np.diff(xi) > 0) and np.all(np.diff(zi) > 0)
     assert xi[0] == 0.0 and xi[-1] == p.aspect and zi[0] == 0.0 and zi[-1] == 1.0
+
+
+@pytest.mark.parametrize("gx,gz", [(0, 0), (1, 0), (0, 1), (1, 2), (2, 1)])
+def test_library_metrics_equal_the_oracles(gx, gz):
+    """The library's host build of the metrics (tc_grid_metrics: xr, xrr,
+    xrrr, xrrrr and DERxr, the same in z) equals the oracle's build_grid bit
+    for bit; the kernels read these arrays."""
+    import ctypes as C
+    from oracle.pyoracle import Oracle
+    from tracer_code_gb300 import load_library
+    p = default_params()
+    p.nx, p.nz, p.aspect, p.grids = 64, 32, 2.0, 3
+    p.comp, p.tracer = 0, 0
+    p.gridX, p.gridZ, p.spaceX, p.spaceZ, p.thickness, p.nbound = gx, gz, 2.0, 1.5, 0.1, 4
+    o = Oracle(p)
+    assert (o.nx, o.nz) == (p.nx, p.nz)
+    ox, oz = o.metrics()
+    L = load_library()
+    x5 = np.empty(5 * (p.nx + 7))
+    z5 = np.empty(5 * (p.nz + 7))
+    assert L.tc_grid_metrics(C.byref(p), x5.ctypes.data_as(C.c_void_p), z5.ctypes.data_as(C.c_void_p)) == 0
+    x5, z5 = x5.reshape(5, -1), z5.reshape(5, -1)
+    # the reference's ranges: xr, xrr over -1..n+1, the others over 0..n
+    for q, lo in zip(range(5), (2, 2, 3, 3, 3)):
+        hi = -2 if q < 2 else -3
+        assert np.array_equal(x5[q, lo:hi], ox[q, lo:hi]), ("x", q)
+        assert np.array_equal(z5[q, lo:hi], oz[q, lo:hi]), ("z", q)

@@ -38,6 +38,7 @@ EXPORTS = [
     "tc_format_vis_line", "tc_write_snapshot", "tc_upload_state_ex", "tc_download_tracer_temperature",
     "tc_equalize_row", "tc_format_equalize_line", "tc_set_step_graph", "tc_step_graph_info",
     "tc_ensemble_create", "tc_ensemble_run", "tc_ensemble_info", "tc_ensemble_destroy", "tc_grid_coordinates",
+    "tc_grid_metrics",
 ]
 
 
@@ -119,6 +120,7 @@ def load_library(build_if_missing: bool = False):
         L.tc_ensemble_info.argtypes = [vp, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
         L.tc_ensemble_destroy.argtypes = [vp]
         L.tc_grid_coordinates.argtypes = [vp, vp, vp]
+        L.tc_grid_metrics.argtypes = [C.POINTER(Params), vp, vp]
         L.tc_kernel_launches.argtypes = []
         L.tc_kernel_launches.restype = C.c_int64
         L.tc_last_error.argtypes = [vp]

@@ -2621,6 +2621,22 @@ tc_status tc_get_info(const tc_handle* H, tc_info* info) {
     return TC_OK;
 }
 
+tc_status tc_grid_metrics(const tc_params* p, double* x5, double* z5) {
+    if (!p || !x5 || !z5 || p->nx < 4 || p->nz < 4) return TC_ERR_ARG;
+    tcs::FD fd;
+    tcs::fd_coefficients(2, fd);
+    tcs::GridMetrics g;
+    tcs::grid_metrics(p->aspect, p->nx, p->nz, p->gridX, p->gridZ, p->spaceX, p->spaceZ, p->thickness, p->nbound, fd,
+                      g);
+    const std::vector<double>* xs[5] = {&g.xr, &g.xrr, &g.xrrr, &g.xrrrr, &g.dxr};
+    const std::vector<double>* zs[5] = {&g.zs, &g.zss, &g.zsss, &g.zssss, &g.dzs};
+    for (int q = 0; q < 5; q++) {
+        std::copy(xs[q]->begin(), xs[q]->end(), x5 + (size_t)q * (p->nx + 7));
+        std::copy(zs[q]->begin(), zs[q]->end(), z5 + (size_t)q * (p->nz + 7));
+    }
+    return TC_OK;
+}
+
 tc_status tc_grid_coordinates(const tc_handle* H, double* xg, double* zg) {
     if (!H || !xg || !zg) return TC_ERR_ARG;
     std::copy(H->h.xg_h.begin(), H->h.xg_h.end(), xg);
