@@ -22,6 +22,12 @@ clock.  A whole CPU timestep takes about a minute, so the arm times as many
 of the K requested steps as fit REF_BUDGET_S (at least one) and reports the
 number it timed in "steps" (the request in "steps_requested"); its W warm-up
 steps are bounded (one W-cycle each on a separate copy of the state).
+
+Other modes, each printing its own JSON line: --ensemble N (N independent
+cases of three grid sizes stepped together, one CUDA graph launch per
+ensemble step), --config3 N (the 2048x512 case, mixed precision against
+FP64 over N steps), and the --profile-* cases that end by themselves under
+ncu.
 """
 from __future__ import annotations
 
