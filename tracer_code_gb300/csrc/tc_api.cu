@@ -27,6 +27,7 @@
 #include <thread>
 
 static std::atomic<long long> g_launches{0};
+static std::atomic<long long> g_handle_uid{0};
 // per host thread, so that graph capture counts only its own thread's
 // launches while other handles run on other threads (tc_ensemble_step)
 static thread_local long long t_launches = 0;
@@ -200,6 +201,7 @@ struct Handle {
     long long sub_tab_key = -1;                    // the sweep tables now in sub_tab
     long long graph_steps = 0;                     // steps run as one graph launch
     long long epoch = 0;  // bumped whenever a captured step would be stale (launch shapes, network, stream)
+    long long uid = 0;    // unique per handle in the process (an ensemble's graph cache key)
     std::vector<double> xg_h, zg_h;  // node coordinates of build_grid, index i + 3 for i = -3..n+3
 };
 
@@ -2431,12 +2433,12 @@ tc_status graph_time(Handle* h, F&& fn, double* ms_out) {
 
 // An ensemble whose timestep is one graph launch: the cases' captured steps
 // as independent branches of one graph (fork from a root stream onto every
-// case's stream, join back), cached by the case list, each case's
-// configuration epoch and sort flag.
+// case's stream, join back), cached by the case list (each handle's address
+// and process-unique id), each case's configuration epoch and sort flag.
 struct tc_ensemble {
     struct Entry {
         std::vector<tc_handle*> hs;
-        std::vector<long long> epochs;
+        std::vector<long long> uids, epochs;
         std::vector<int> sorts;
         cudaGraphExec_t ge = nullptr;
         std::vector<StepGraph> cases;
@@ -2469,6 +2471,7 @@ tc_ensemble::Entry* build_entry(tc_ensemble* e, tc_handle* const* hs, int n) {
             drop_entry(en);
             return nullptr;
         }
+        en->uids.push_back(h->uid);
         en->epochs.push_back(h->epoch);
         en->sorts.push_back(sorts_this_step(h) ? 1 : 0);
     }
@@ -2539,6 +2542,7 @@ tc_status tc_create(const tc_params* p, tc_handle** out) {
     *out = nullptr;
     tc_handle* H = new (std::nothrow) tc_handle();
     if (!H) return TC_ERR_ALLOC;
+    H->h.uid = ++g_handle_uid;
     tc_status s = create(&H->h, p);
     if (s != TC_OK) {
         static thread_local std::string last;
@@ -2975,7 +2979,7 @@ tc_status tc_ensemble_run(tc_ensemble* e, tc_handle* const* hs, int32_t n, tc_st
             if (c->hs != key) continue;
             bool same = true;
             for (int i = 0; i < n && same; i++)
-                same = c->epochs[(size_t)i] == hs[i]->h.epoch &&
+                same = c->uids[(size_t)i] == hs[i]->h.uid && c->epochs[(size_t)i] == hs[i]->h.epoch &&
                        c->sorts[(size_t)i] == (sorts_this_step(&hs[i]->h) ? 1 : 0);
             if (same) en = c;
         }
