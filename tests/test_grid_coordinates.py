@@ -56,3 +56,29 @@ def test_library_metrics_equal_the_oracles(gx, gz):
         hi = -2 if q < 2 else -3
         assert np.array_equal(x5[q, lo:hi], ox[q, lo:hi]), ("x", q)
         assert np.array_equal(z5[q, lo:hi], oz[q, lo:hi]), ("z", q)
+
+
+def test_stretched_initial_state_uses_the_physical_coordinates():
+    """initialize_tracers / add_tracers on a stretched grid: a tracer is
+    enriched where zgrid(s) <= dlayer, a node's C where zg(k) <= dlayer, and
+    the temperature profile is evaluated at (xgrid, zgrid) (composition.f90:
+    593-664, basics.f90:223-231); on the uniform grid nothing changes."""
+    p = default_params()
+    p.nx, p.nz, p.aspect, p.tpc, p.dlayer = 32, 16, 2.0, 3, 0.2
+    p.gridX, p.gridZ, p.spaceX, p.spaceZ = 1, 1, 2.0, 2.0
+    st = state.initial_state(p, seed=4)
+    z_tr = state.zgrid(p, st["str"])
+    assert np.array_equal(st["Ttype"], np.where(z_tr > p.dlayer, 0, 1))
+    x, z = state.grid_coordinates(p)
+    assert np.array_equal(st["Cnew"][:, :, 0], np.broadcast_to(np.where(z <= p.dlayer, 1.0, 0.0)[:, None],
+                                                                st["Cnew"].shape[:2]))
+    T = st["T"]
+    span = 2
+    k, i = 5, 7
+    assert T[span + k, span + i] == (1.0 - z[span + k]) + 0.01 * np.cos(np.pi * x[span + i]) * np.sin(np.pi * z[span + k])
+    # the stretching moves the dense layer's boundary off the uniform one
+    assert (z_tr <= p.dlayer).sum() != (st["str"] <= p.dlayer).sum()
+    u = default_params()
+    u.nx, u.nz, u.aspect, u.tpc, u.dlayer = 32, 16, 2.0, 3, 0.2
+    su = state.initial_state(u, seed=4)
+    assert np.array_equal(su["Ttype"], np.where(su["str"] > u.dlayer, 0, 1))
